@@ -1,0 +1,226 @@
+/*
+ * spike_gb300.h - C ABI of the GB300-native clock-driven spiking-network step.
+ *
+ * This is the drop-in boundary for Spike's CUDA backend hot path.  In the
+ * reference the path sits behind per-component backend plugins built by a
+ * string-keyed factory (Spike/Backend/Macros.hpp:33-70) with the contract
+ * prepare()/reset_state() (Spike/Backend/Backend.hpp:15-25) and one
+ * state_update() virtual per component.  Here one network handle owns all of
+ * the step's device state and the whole step (LIF update + threshold + spike
+ * compaction, Poisson input, weight-dependent STDP, delayed propagation) runs
+ * in one persistent sm_103a kernel per block of timesteps.
+ *
+ * Conventions
+ *  - every function returns an int status: 0 (SPK_OK) or a negative SPK_ERR_*;
+ *    nothing in the library exits the process (the reference calls exit(-1),
+ *    Spike/Helpers/TerminalHelpers.hpp:15-20);
+ *  - the caller owns every host buffer; descriptor arrays are copied at create;
+ *  - a handle owns its device memory and one non-default CUDA stream;
+ *  - a handle is single-threaded; distinct handles may be used from distinct
+ *    host threads;
+ *  - spk_last_error() returns a per-thread message for the last failure.
+ *
+ * Timestep grouping: the reference advances G = min delay steps per launch
+ * (Spike/Models/SpikingModel.cpp:98).  This library implements G = 1, which is
+ * the value for every network whose minimum delay is one step; networks whose
+ * minimum delay is larger are rejected with SPK_ERR_UNSUPPORTED.
+ */
+#ifndef SPIKE_GB300_H
+#define SPIKE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPK_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define SPK_OK 0
+#define SPK_ERR_INVALID (-1)     /* bad argument or descriptor              */
+#define SPK_ERR_CUDA (-2)        /* a CUDA runtime call failed              */
+#define SPK_ERR_OOM (-3)         /* device or host allocation failed        */
+#define SPK_ERR_UNSUPPORTED (-4) /* valid in the reference, not implemented */
+#define SPK_ERR_TIMEOUT (-5)     /* a bounded device wait gave up           */
+#define SPK_ERR_OVERFLOW (-6)    /* spike store full: spikes were dropped   */
+#define SPK_ERR_STATE (-7)       /* call not valid in the handle's state    */
+#define SPK_ERR_BUSY (-8)        /* resource temporarily unavailable        */
+
+/* ---- synapse kinds --------------------------------------------------------
+ * Same numbering as the reference's SYNAPSE_TYPE enum
+ * (Spike/Backend/CUDA/Synapses/SpikingSynapses.hpp:234-240).               */
+#define SPK_SYN_CONDUCTANCE 1 /* ConductanceSpikingSynapses */
+#define SPK_SYN_CURRENT 2     /* CurrentSpikingSynapses     */
+#define SPK_SYN_VOLTAGE 3     /* VoltageSpikingSynapses     */
+
+/* ---- spike populations and state fields -------------------------------- */
+#define SPK_POP_NEURONS 0 /* LIF neurons (SpikingModel::spiking_neurons)     */
+#define SPK_POP_INPUTS 1  /* Poisson inputs (SpikingModel::input_spiking_neurons) */
+
+#define SPK_FIELD_V 0          /* float[n_neurons] membrane potential            */
+#define SPK_FIELD_LAST_SPIKE 1 /* float[n_neurons] last spike time (s)           */
+#define SPK_FIELD_SYN_TRACE 2  /* float[n_neurons*n_labels] conductance/current  */
+#define SPK_FIELD_INPUT_NEXT 3 /* float[n_inputs] next Poisson spike time (s)    */
+#define SPK_FIELD_RING 4       /* float[B*n_neurons*n_labels], [slot][post*L+l]  */
+#define SPK_FIELD_PRE_TRACE 5  /* float[n_inputs+n_neurons] STDP pre trace, inputs first */
+#define SPK_FIELD_POST_TRACE 6 /* float[n_neurons] STDP post trace               */
+
+/* One LIF neuron group (lif_spiking_neuron_parameters_struct,
+ * Spike/Neurons/LIFSpikingNeurons.hpp:7-14).  tau_m and R are the front end's
+ * float values C_m/g_0 and 1/g_0 (Spike/Neurons/LIFSpikingNeurons.cpp:29-30);
+ * the library derives k = dt/tau_m and k*R as the reference backend does
+ * (Spike/Backend/CUDA/Neurons/LIFSpikingNeurons.cu:26-46). */
+typedef struct spk_neuron_group {
+  int32_t start; /* first neuron id of the group        */
+  int32_t count; /* neurons in the group                */
+  float tau_m;
+  float R;
+  float v0;     /* resting_potential_v0                */
+  float vreset; /* after_spike_reset_potential_vreset  */
+  float theta;  /* threshold_for_action_potential_spike */
+  /* Extension (not in the reference, which resets V to v0): when
+   * v_init_lo < v_init_hi, reset draws V ~ U[lo, hi) from Philox keyed by
+   * (seed, neuron, SPK_DOMAIN_VINIT). */
+  float v_init_lo;
+  float v_init_hi;
+} spk_neuron_group;
+
+/* weightdependent_stdp_plasticity_parameters_struct
+ * (Spike/Plasticity/WeightDependentSTDPPlasticity.hpp:28-40). */
+typedef struct spk_stdp_params {
+  float a_minus;
+  float a_plus;
+  float tau_minus;
+  float tau_plus;
+  float lambda;
+  float alpha;
+  float w_max;
+  int32_t clip_upper; /* extension: also clip weights at w_max (reference clips at 0 only) */
+} spk_stdp_params;
+
+/* Flat network descriptor.  Synapse arrays are in CREATION order, with the
+ * reference's presynaptic id convention: LIF neuron n -> n, input i -> -i-1
+ * (Spike/Neurons/Neurons.hpp:34-35).  The library sorts them by presynaptic
+ * key (inputs first in reverse order, then neurons) with a stable sort, exactly
+ * as Synapses::sort_synapses does (Spike/Synapses/Synapses.cpp:33-81), and
+ * keeps the reverse map for weight readback in creation order. */
+typedef struct spk_net_desc {
+  int32_t abi_version; /* must be SPK_ABI_VERSION */
+  float dt;            /* SpikingModel::timestep (s) */
+  int32_t synapse_kind;
+
+  int32_t n_neurons;
+  int32_t n_groups;
+  const spk_neuron_group* groups; /* contiguous, ascending, covering [0,n_neurons) */
+  float refractory_period;        /* global, from the last group added (reference quirk) */
+  float background_current;       /* global, from the last group added (reference quirk) */
+
+  int32_t n_inputs;           /* Poisson input neurons (0 allowed) */
+  int32_t n_stimuli;          /* rate vectors; >= 1 when n_inputs > 0 */
+  const float* input_rates;   /* [n_stimuli][n_inputs] Hz */
+  int32_t stimulus;           /* selected stimulus */
+
+  int32_t n_labels;           /* syn labels L (>= 1) */
+  const float* label_tau;     /* [L] tau_g (conductance) or tau (current); unused for voltage */
+  const float* label_vhat;    /* [L] reversal potentials (conductance only) */
+
+  int64_t n_synapses;
+  const int32_t* pre;
+  const int32_t* post;
+  const float* weight;        /* synaptic_efficacies_or_weights */
+  const float* scale;         /* weight_scaling_constants */
+  const int32_t* delay;       /* in timesteps, >= 1 */
+  const int32_t* label;       /* syn_labels, < L */
+  const uint8_t* plastic;     /* 1 = governed by the STDP rule; may be NULL */
+
+  int32_t has_stdp;
+  spk_stdp_params stdp;
+
+  uint64_t seed;              /* Philox key (Poisson draws, V init) */
+  int64_t spike_capacity;     /* device spike store entries; 0 = default */
+  int32_t record_inputs;      /* also record input spikes */
+  int32_t reserved;
+} spk_net_desc;
+
+/* Launch schedule.  Zero fields are chosen by the library (planner for a
+ * single network, autotuner for a batch). */
+typedef struct spk_schedule {
+  int32_t warps_per_cta;    /* warps in one CTA; each warp owns one post tile   */
+  int32_t tile_posts;       /* posts per tile, multiple of 32                   */
+  int32_t ctas;             /* CTAs per network (1 = CTA-per-network schedule)  */
+  int32_t steps_per_launch; /* timesteps advanced by one persistent launch      */
+} spk_schedule;
+
+typedef struct spk_net spk_net;
+typedef struct spk_batch spk_batch;
+
+/* ---- single network -----------------------------------------------------
+ * spk_net_create replaces SpikingModel::finalise_model -> init_backend ->
+ * every component's prepare() (Spike/Models/SpikingModel.cpp:82-162,
+ * Spike/Backend/Macros.hpp:21-39) and ends with reset_state(). */
+int spk_net_create(const spk_net_desc* desc, const spk_schedule* schedule, spk_net** out);
+/* Replaces the backend destructors' cudaFree calls. */
+int spk_net_destroy(spk_net* net);
+/* SpikingModel::reset_state (Spike/Models/SpikingModel.cpp:181-190). */
+int spk_net_reset_state(spk_net* net);
+/* SpikingModel::reset_time (Spike/Models/SpikingModel.cpp:192-194). */
+int spk_net_reset_time(spk_net* net);
+/* InputSpikingNeurons::select_stimulus + reset of the inputs
+ * (Spike/Neurons/PoissonInputSpikingNeurons.cpp:48-51). */
+int spk_net_select_stimulus(spk_net* net, int32_t stimulus);
+/* SpikingModel::run(seconds, plasticity_on) (Spike/Models/SpikingModel.cpp:214-236):
+ * ceilf(seconds/dt) steps, t_s = start + s*dt in float, then time = start + seconds.
+ * Asynchronous: returns after enqueueing; device errors surface at the next
+ * synchronizing call. */
+int spk_net_run(spk_net* net, float seconds, int32_t plasticity_on);
+/* As spk_net_run for an explicit step count (time advances by n_steps*dt). */
+int spk_net_run_steps(spk_net* net, int64_t n_steps, int32_t plasticity_on);
+/* Wait for the handle's stream; returns the device status word
+ * (SPK_ERR_TIMEOUT / SPK_ERR_OVERFLOW) or SPK_OK. */
+int spk_net_synchronize(spk_net* net);
+int spk_net_current_time(const spk_net* net, float* seconds);
+/* Spikes recorded since the last clear (SpikingActivityMonitor store,
+ * Spike/ActivityMonitor/SpikingActivityMonitor.cpp:79-120).  Ordered by
+ * step, then by presynaptic key (the canonical order).  times are the float
+ * step times t_s the reference stores. */
+int spk_net_spike_count(spk_net* net, int32_t population, int64_t* n);
+int spk_net_read_spikes(spk_net* net, int32_t population, int32_t* ids, float* times,
+                        int64_t capacity, int64_t* n_written);
+int spk_net_clear_spikes(spk_net* net);
+/* Read one state field (SPK_FIELD_*) into dst (count elements). */
+int spk_net_read_state(spk_net* net, int32_t field, void* dst, int64_t count);
+/* Backend::Synapses::copy_to_frontend / copy_to_backend
+ * (Spike/Synapses/Synapses.hpp:54-55): weights in creation order. */
+int spk_net_read_weights(spk_net* net, float* weights, int64_t n);
+int spk_net_write_weights(spk_net* net, const float* weights, int64_t n);
+/* Synaptic events delivered so far: sum over spikes of the spiking neuron's
+ * out-degree. */
+int spk_net_synaptic_events(spk_net* net, uint64_t* events);
+int spk_net_get_schedule(const spk_net* net, spk_schedule* out);
+int spk_net_device_bytes(const spk_net* net, int64_t* bytes);
+/* Kernel launches issued so far by this handle. */
+int spk_net_launch_count(const spk_net* net, int64_t* launches);
+
+/* ---- batch: many independent networks in one persistent launch ---------- */
+int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* schedule,
+                     spk_batch** out);
+int spk_batch_run_steps(spk_batch* batch, int64_t n_steps, int32_t plasticity_on);
+int spk_batch_synchronize(spk_batch* batch);
+int spk_batch_launch_count(const spk_batch* batch, int64_t* launches);
+int spk_batch_destroy(spk_batch* batch);
+
+/* ---- misc ---------------------------------------------------------------- */
+/* Backend::MemoryManager::{free_bytes,total_bytes}
+ * (Spike/Backend/CUDA/Helpers/Memory.cu:7-25), returning a status instead of
+ * exit(1). */
+int spk_memory_info(uint64_t* free_bytes, uint64_t* total_bytes);
+int spk_abi_version(void);
+const char* spk_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPIKE_GB300_H */

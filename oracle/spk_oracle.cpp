@@ -1,0 +1,822 @@
+// spk_oracle.cpp - CPU restatement of Spike's clock-driven simulation step.
+//
+// TEST INFRASTRUCTURE ONLY (see spk_oracle.h): the checker for the CUDA path,
+// never linked into the product library.
+//
+// Compiled with -ffp-contract=off so every float expression below rounds
+// after each operation, as the CUDA kernels do under -fmad=false.  The
+// reference is cited function by function; variable names follow the
+// reference where that helps the side-by-side reading.
+#include "spk_oracle.h"
+
+#include <barrier>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "../spike_gb300/csrc/spk_rng.h"
+
+namespace {
+
+// (int)roundf(x) as the reference's device code evaluates it: round half away
+// from zero, then a saturating float->int conversion in which NaN becomes 0
+// (PTX cvt.rzi.s32.f32 semantics), so the host agrees with the GPU on every
+// input, including the ones C leaves undefined.
+inline int round_to_int(float x) {
+  if (x != x) return 0;
+  float r = std::roundf(x);
+  if (r >= 2147483648.0f) return 2147483647;
+  if (r <= -2147483648.0f) return (-2147483647 - 1);
+  return (int)r;
+}
+inline int round_to_int(double x) {
+  if (x != x) return 0;
+  double r = std::round(x);
+  if (r >= 2147483648.0) return 2147483647;
+  if (r <= -2147483648.0) return (-2147483647 - 1);
+  return (int)r;
+}
+
+template <typename R>
+struct Net {
+  // ---- model constants ---------------------------------------------------
+  float dt_f = 0.f;
+  R dt = 0;
+  int kind = 0;
+  int N = 0, Nin = 0, L = 1, B = 0, Dmax = 0;
+  std::vector<R> k, kR, v0, vreset, theta;  // per neuron, as the reference backend
+  std::vector<float> vinit_lo, vinit_hi;    // per neuron (extension)
+  R t_ref = 0, i_bg = 0;
+  std::vector<float> rates;  // [n_stim][Nin]
+  int n_stim = 0, stim = 0;
+  std::vector<R> decay, vhat;  // per label
+  uint64_t seed = 0;
+  bool record_inputs = false;
+
+  // ---- synapses in reference sorted order (Synapses::sort_synapses) -------
+  int64_t S = 0;
+  std::vector<int32_t> spre, spost, sdelay, slabel;
+  std::vector<R> sw, sscale;
+  std::vector<int64_t> revsort;          // creation index -> sorted index
+  std::vector<int64_t> eff_start, eff_count;  // per key
+  std::vector<int64_t> plastic_idx;       // sorted indices under the STDP rule
+  bool has_stdp = false;
+  spk_stdp_params stdp{};
+  R E_minus = 0, E_plus = 0, inc_minus = 0, inc_plus = 0, invE_minus = 0, invE_plus = 0;
+
+  // ---- dynamic state --------------------------------------------------------
+  std::vector<R> V, last, gtr, ring;  // ring [B][N*L]
+  std::vector<R> in_next;              // input last_spike_time (= next spike time)
+  std::vector<uint8_t> in_active;
+  std::vector<R> stdp_pre, stdp_post;  // per plastic synapse (reference layout)
+  float current_time = 0.f;
+  uint64_t events = 0;
+  std::vector<int32_t> rec_ids[2];
+  std::vector<float> rec_times[2];
+
+  // ---- per-step scratch -----------------------------------------------------
+  std::vector<uint8_t> spiked;  // per key, this step
+  std::vector<int64_t> active;  // keys, ascending
+
+  // ---- threading: post-range ownership --------------------------------------
+  int threads = 1;
+  std::vector<int> n0, n1, i0, i1;           // owned neuron / input ranges
+  std::vector<int64_t> split;                // [key][threads+1] sub-row starts
+  std::vector<int64_t> p0, p1;               // plastic ranges
+
+  int key_of_input(int i) const { return Nin - 1 - i; }  // N_in + (-i-1)
+  int key_of_neuron(int n) const { return Nin + n; }
+  int nkeys() const { return Nin + N; }
+
+  int init(const spk_net_desc* d);
+  void reset_state();
+  void reset_inputs();
+  void set_threads(int t);
+  void run_steps(int64_t n_steps, float start, bool plastic);
+  void lif_range(int a, int b, R t, int T);
+  void poisson_range(int a, int b, R t, int T);
+  void stdp_range(int64_t a, int64_t b, R t);
+  void propagate_thread(int th, int T);
+};
+
+template <typename R>
+int Net<R>::init(const spk_net_desc* d) {
+  dt_f = d->dt;
+  dt = (R)d->dt;
+  kind = d->synapse_kind;
+  N = d->n_neurons;
+  Nin = d->n_inputs;
+  L = d->n_labels;
+  seed = d->seed;
+  record_inputs = d->record_inputs != 0;
+  if (N <= 0 || L <= 0 || Nin < 0 || !(d->dt > 0.f)) return SPK_ERR_INVALID;
+  if (kind != SPK_SYN_CONDUCTANCE && kind != SPK_SYN_CURRENT && kind != SPK_SYN_VOLTAGE)
+    return SPK_ERR_INVALID;
+
+  // LIF constants: k = timestep / tau_m and k*R, computed on the host in the
+  // reference (Spike/Backend/CUDA/Neurons/LIFSpikingNeurons.cu:31-44).
+  k.assign(N, 0);
+  kR.assign(N, 0);
+  v0.assign(N, 0);
+  vreset.assign(N, 0);
+  theta.assign(N, 0);
+  vinit_lo.assign(N, 0.f);
+  vinit_hi.assign(N, 0.f);
+  for (int g = 0; g < d->n_groups; ++g) {
+    const spk_neuron_group& G = d->groups[g];
+    for (int n = G.start; n < G.start + G.count; ++n) {
+      if (n < 0 || n >= N) return SPK_ERR_INVALID;
+      if (sizeof(R) == 4) {
+        float kk = d->dt / G.tau_m;
+        k[n] = (R)kk;
+        kR[n] = (R)(kk * G.R);
+      } else {
+        double kk = (double)d->dt / (double)G.tau_m;
+        k[n] = (R)kk;
+        kR[n] = (R)(kk * (double)G.R);
+      }
+      v0[n] = (R)G.v0;
+      vreset[n] = (R)G.vreset;
+      theta[n] = (R)G.theta;
+      vinit_lo[n] = G.v_init_lo;
+      vinit_hi[n] = G.v_init_hi;
+    }
+  }
+  t_ref = (R)d->refractory_period;
+  i_bg = (R)d->background_current;
+
+  // Conductance decay expf(-dt/tau_g) on the host
+  // (Spike/Backend/CUDA/Synapses/ConductanceSpikingSynapses.cu:76-78); the
+  // current-synapse decay uses the same formula (written from the equations:
+  // the reference's current kernel never runs, CurrentSpikingSynapses.cu:67-68).
+  decay.assign(L, 0);
+  vhat.assign(L, 0);
+  for (int l = 0; l < L; ++l) {
+    if (kind != SPK_SYN_VOLTAGE) {
+      if (!d->label_tau) return SPK_ERR_INVALID;
+      if (sizeof(R) == 4)
+        decay[l] = (R)expf(-d->dt / d->label_tau[l]);
+      else
+        decay[l] = (R)std::exp(-(double)d->dt / (double)d->label_tau[l]);
+    }
+    if (kind == SPK_SYN_CONDUCTANCE) {
+      if (!d->label_vhat) return SPK_ERR_INVALID;
+      vhat[l] = (R)d->label_vhat[l];
+    }
+  }
+
+  if (Nin > 0) {
+    n_stim = d->n_stimuli;
+    stim = d->stimulus;
+    if (n_stim <= 0 || !d->input_rates || stim < 0 || stim >= n_stim) return SPK_ERR_INVALID;
+    rates.assign(d->input_rates, d->input_rates + (size_t)n_stim * Nin);
+  }
+
+  // ---- sort synapses by key N_in + pre, stable (Synapses.cpp:33-81) -------
+  S = d->n_synapses;
+  if (S < 0) return SPK_ERR_INVALID;
+  const int K = nkeys();
+  std::vector<int64_t> cnt(K + 1, 0);
+  Dmax = 0;
+  int Dmin = 1 << 30;
+  for (int64_t s = 0; s < S; ++s) {
+    int p = d->pre[s], q = d->post[s], dl = d->delay[s], lb = d->label ? d->label[s] : 0;
+    int key = Nin + p;
+    if (key < 0 || key >= K || q < 0 || q >= N || dl < 1 || lb < 0 || lb >= L)
+      return SPK_ERR_INVALID;
+    cnt[key + 1]++;
+    if (dl > Dmax) Dmax = dl;
+    if (dl < Dmin) Dmin = dl;
+  }
+  if (S > 0 && Dmin != 1) return SPK_ERR_UNSUPPORTED;  // timestep grouping G = 1 only
+  for (int kk = 0; kk < K; ++kk) cnt[kk + 1] += cnt[kk];
+  eff_start.assign(cnt.begin(), cnt.end() - 1);
+  eff_count.assign(K, 0);
+  for (int kk = 0; kk < K; ++kk) eff_count[kk] = cnt[kk + 1] - cnt[kk];
+  spre.resize(S);
+  spost.resize(S);
+  sdelay.resize(S);
+  slabel.resize(S);
+  sw.resize(S);
+  sscale.resize(S);
+  revsort.resize(S);
+  std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+  std::vector<uint8_t> splastic(S, 0);
+  for (int64_t s = 0; s < S; ++s) {
+    int key = Nin + d->pre[s];
+    int64_t pos = fill[key]++;
+    spre[pos] = d->pre[s];
+    spost[pos] = d->post[s];
+    sdelay[pos] = d->delay[s];
+    slabel[pos] = d->label ? d->label[s] : 0;
+    sw[pos] = (R)d->weight[s];
+    sscale[pos] = (R)d->scale[s];
+    revsort[s] = pos;
+    if (d->plastic && d->plastic[s]) splastic[pos] = 1;
+  }
+  // Ring depth D_max + 2G + 1 (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:48).
+  B = Dmax + 2 * 1 + 1;
+
+  has_stdp = d->has_stdp != 0;
+  stdp = d->stdp;
+  plastic_idx.clear();
+  if (has_stdp)
+    for (int64_t s = 0; s < S; ++s)
+      if (splastic[s]) plastic_idx.push_back(s);
+  if (has_stdp) {
+    // Trace constants of WeightDependentSTDPPlasticity.cu:125-145 for G = 1,
+    // where the only spike sub-step is g = 0: expf(-(G*dt)/tau) for the decay,
+    // a*expf(-((G-0)*dt)/tau) for the increment, 1/expf(-(G-0)*dt/tau) for
+    // the on-pre / on-post rescaling.
+    if (sizeof(R) == 4) {
+      float em = expf(-(1.0f * d->dt) / stdp.tau_minus);
+      float ep = expf(-(1.0f * d->dt) / stdp.tau_plus);
+      E_minus = (R)em;
+      E_plus = (R)ep;
+      inc_minus = (R)(stdp.a_minus * em);
+      inc_plus = (R)(stdp.a_plus * ep);
+      invE_minus = (R)(1.0f / em);
+      invE_plus = (R)(1.0f / ep);
+    } else {
+      double em = std::exp(-(double)d->dt / (double)stdp.tau_minus);
+      double ep = std::exp(-(double)d->dt / (double)stdp.tau_plus);
+      E_minus = (R)em;
+      E_plus = (R)ep;
+      inc_minus = (R)((double)stdp.a_minus * em);
+      inc_plus = (R)((double)stdp.a_plus * ep);
+      invE_minus = (R)(1.0 / em);
+      invE_plus = (R)(1.0 / ep);
+    }
+  }
+
+  V.assign(N, 0);
+  last.assign(N, 0);
+  gtr.assign((size_t)N * L, 0);
+  ring.assign((size_t)B * N * L, 0);
+  in_next.assign(Nin, 0);
+  in_active.assign(Nin, 0);
+  stdp_pre.assign(plastic_idx.size(), 0);
+  stdp_post.assign(plastic_idx.size(), 0);
+  spiked.assign(K, 0);
+  set_threads(1);
+  reset_state();
+  return SPK_OK;
+}
+
+template <typename R>
+void Net<R>::reset_inputs() {
+  // SpikingNeurons::reset_state: last spike time -1000
+  // (Spike/Backend/CUDA/Neurons/SpikingNeurons.cu:68-94) and
+  // PoissonInputSpikingNeurons::reset_state: active = false
+  // (Spike/Backend/CUDA/Neurons/PoissonInputSpikingNeurons.cu:27-34).
+  for (int i = 0; i < Nin; ++i) {
+    in_next[i] = (R)-1000.0f;
+    in_active[i] = 0;
+  }
+}
+
+template <typename R>
+void Net<R>::reset_state() {
+  // SpikingModel::reset_state order: synapses (ring, conductance traces),
+  // neurons (V := V0, last := -1000), inputs, plasticity (traces := 0)
+  // (Spike/Models/SpikingModel.cpp:181-190).
+  std::fill(ring.begin(), ring.end(), (R)0);
+  std::fill(gtr.begin(), gtr.end(), (R)0);
+  for (int n = 0; n < N; ++n) {
+    if (vinit_lo[n] < vinit_hi[n]) {
+      float u = spk::draw_uniform(seed, (uint32_t)n, 0u, spk::DOMAIN_VINIT);
+      if (sizeof(R) == 4) {
+        float span = vinit_hi[n] - vinit_lo[n];
+        V[n] = (R)(vinit_lo[n] + span * u);
+      } else {
+        V[n] = (R)((double)vinit_lo[n] + ((double)vinit_hi[n] - (double)vinit_lo[n]) * (double)u);
+      }
+    } else {
+      V[n] = v0[n];
+    }
+    last[n] = (R)-1000.0f;
+  }
+  reset_inputs();
+  std::fill(stdp_pre.begin(), stdp_pre.end(), (R)0);
+  std::fill(stdp_post.begin(), stdp_post.end(), (R)0);
+}
+
+template <typename R>
+void Net<R>::set_threads(int t) {
+  if (t < 1) t = 1;
+  threads = t;
+  n0.assign(t, 0);
+  n1.assign(t, 0);
+  i0.assign(t, 0);
+  i1.assign(t, 0);
+  for (int th = 0; th < t; ++th) {
+    n0[th] = (int)((int64_t)N * th / t);
+    n1[th] = (int)((int64_t)N * (th + 1) / t);
+    i0[th] = (int)((int64_t)Nin * th / t);
+    i1[th] = (int)((int64_t)Nin * (th + 1) / t);
+  }
+  // Split every efferent row by owning thread (rows keep sorted order inside
+  // each part, so per-cell accumulation order is unchanged).
+  const int K = nkeys();
+  split.assign((size_t)K * (t + 1), 0);
+  std::vector<int> owner(N, 0);
+  for (int th = 0; th < t; ++th)
+    for (int n = n0[th]; n < n1[th]; ++n) owner[n] = th;
+  if (t > 1) {
+    // Permute each row so entries are grouped by owner, stable within owner.
+    std::vector<int32_t> tp(S), tq(S), td(S), tl(S);
+    std::vector<R> tw(S), ts(S);
+    std::vector<int64_t> perm(S);
+    for (int kk = 0; kk < K; ++kk) {
+      int64_t a = eff_start[kk], b = a + eff_count[kk];
+      std::vector<int64_t> c(t + 1, 0);
+      for (int64_t s = a; s < b; ++s) c[owner[spost[s]] + 1]++;
+      for (int th = 0; th < t; ++th) c[th + 1] += c[th];
+      for (int th = 0; th <= t; ++th) split[(size_t)kk * (t + 1) + th] = a + c[th];
+      std::vector<int64_t> f(c.begin(), c.end() - 1);
+      for (int64_t s = a; s < b; ++s) perm[s] = a + f[owner[spost[s]]]++;
+    }
+    for (int64_t s = 0; s < S; ++s) {
+      int64_t p = perm[s];
+      tp[p] = spre[s];
+      tq[p] = spost[s];
+      td[p] = sdelay[s];
+      tl[p] = slabel[s];
+      tw[p] = sw[s];
+      ts[p] = sscale[s];
+    }
+    spre.swap(tp);
+    spost.swap(tq);
+    sdelay.swap(td);
+    slabel.swap(tl);
+    sw.swap(tw);
+    sscale.swap(ts);
+    for (int64_t s = 0; s < S; ++s) revsort[s] = perm[revsort[s]];
+    for (auto& pi : plastic_idx) pi = perm[pi];
+    // plastic_idx order only matters for the per-synapse trace arrays, which
+    // were all reset together: keep them aligned.
+  } else {
+    for (int kk = 0; kk < K; ++kk) {
+      split[(size_t)kk * 2] = eff_start[kk];
+      split[(size_t)kk * 2 + 1] = eff_start[kk] + eff_count[kk];
+    }
+  }
+  int64_t P = (int64_t)plastic_idx.size();
+  p0.assign(t, 0);
+  p1.assign(t, 0);
+  for (int th = 0; th < t; ++th) {
+    p0[th] = P * th / t;
+    p1[th] = P * (th + 1) / t;
+  }
+}
+
+// lif_update_membrane_potentials with the injection kernels inlined
+// (Spike/Backend/CUDA/Neurons/LIFSpikingNeurons.cu:105-193,
+// Spike/Backend/CUDA/InlineDeviceFunctions.hpp:22-111), G = 1 so g = 0.
+template <typename R>
+void Net<R>::lif_range(int a, int b, R t, int T) {
+  const int g = 0;
+  const R tg = t + (R)g * dt;
+  const R half_dt = (R)0.5f * dt;
+  const size_t row = (size_t)N * L;
+  const size_t bufferloc = (size_t)((T + g) % B) * row;
+  for (int idx = a; idx < b; ++idx) {
+    R Vi = V[idx];
+    R input = 0;
+    if (kind == SPK_SYN_CONDUCTANCE) {
+      R total = 0;
+      for (int l = 0; l < L; ++l) {
+        R& gl = gtr[(size_t)idx * L + l];
+        R& cell = ring[bufferloc + (size_t)idx * L + l];
+        R gnew = decay[l] * gl + cell;
+        cell = 0;
+        total += gnew * (vhat[l] - Vi);
+        gl = gnew;
+      }
+      input = total * kR[idx];
+    } else if (kind == SPK_SYN_CURRENT) {
+      R total = 0;
+      for (int l = 0; l < L; ++l) {
+        R& il = gtr[(size_t)idx * L + l];
+        R& cell = ring[bufferloc + (size_t)idx * L + l];
+        R inew = il * decay[l];
+        inew += cell;
+        cell = 0;
+        total += inew;
+        il = inew;
+      }
+      input = total * kR[idx];
+    } else {
+      R total = 0;
+      for (int l = 0; l < L; ++l) {
+        R& cell = ring[bufferloc + (size_t)idx * L + l];
+        total += cell;
+        cell = 0;
+      }
+      input = total;
+    }
+    if (((tg - last[idx]) - t_ref) > half_dt) {
+      const R kc = k[idx];
+      Vi = kc * v0[idx] + ((R)1 - kc) * Vi + kc * i_bg + input;
+      if (Vi >= theta[idx]) {
+        spiked[key_of_neuron(idx)] = 1;
+        last[idx] = tg;
+        Vi = vreset[idx];
+      }
+    }
+    V[idx] = Vi;
+  }
+}
+
+// poisson_update_membrane_potentials_kernel
+// (Spike/Backend/CUDA/Neurons/PoissonInputSpikingNeurons.cu:96-129), G = 1,
+// with the uniform drawn from Philox(seed, input, step).
+template <typename R>
+void Net<R>::poisson_range(int a, int b, R t, int T) {
+  const int g = 0;
+  const R tg = t + (R)g * dt;
+  const float* rt = rates.data() + (size_t)Nin * stim;
+  for (int idx = a; idx < b; ++idx) {
+    if ((in_next[idx] <= tg) || !in_active[idx]) {
+      const R rate = (R)rt[idx];
+      const float u = spk::draw_uniform(seed, (uint32_t)idx, (uint32_t)T, spk::DOMAIN_POISSON);
+      R lg;
+      if (sizeof(R) == 4)
+        lg = (R)spk::logf_spk(u);
+      else
+        lg = (R)std::log((double)u);
+      in_next[idx] = tg - ((R)1 / rate) * lg;
+      if (in_active[idx])
+        spiked[key_of_input(idx)] = 1;
+      else
+        in_active[idx] = 1;
+    }
+  }
+}
+
+// ltp_and_ltd (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:85-161),
+// G = 1: pre_g, post_g are 0 for a spike at this step and negative otherwise,
+// so the (post_g > pre_g) / (pre_g > post_g) corrections never apply.
+template <typename R>
+void Net<R>::stdp_range(int64_t a, int64_t b, R t) {
+  const int G = 1;
+  for (int64_t indx = a; indx < b; ++indx) {
+    const int64_t idx = plastic_idx[indx];
+    R pre_tr = stdp_pre[indx];
+    R post_tr = stdp_post[indx];
+    const int postid = spost[idx];
+    const int preid = spre[idx];
+    const R old_w = sw[idx];
+    const bool is_input = preid < 0;
+    const int corr = is_input ? (-preid - 1) : preid;
+    const R pre_last = is_input ? in_next[corr] : last[corr];
+    int pre_g = round_to_int((pre_last - t) / dt);
+    int post_g = round_to_int((last[postid] - t) / dt);
+    if (pre_g >= G) pre_g *= -1;
+
+    post_tr *= E_minus;
+    pre_tr *= E_plus;
+    post_tr += (post_g >= 0) ? inc_minus : (R)0;
+    pre_tr += (pre_g >= 0) ? inc_plus : (R)0;
+
+    R syn_update = 0;
+    if (pre_g >= 0) {
+      R temp_post = post_tr;
+      temp_post *= invE_minus;
+      syn_update -= (R)stdp.lambda * (R)stdp.alpha * old_w * temp_post;
+    }
+    if (post_g >= 0) {
+      R temp_pre = pre_tr;
+      temp_pre *= invE_plus;
+      syn_update += (R)stdp.lambda * ((R)stdp.w_max - old_w) * temp_pre;
+    }
+    R new_w = old_w + syn_update;
+    if (new_w < (R)0) new_w = 0;
+    if (stdp.clip_upper && new_w > (R)stdp.w_max) new_w = (R)stdp.w_max;
+    sw[idx] = new_w;
+    stdp_pre[indx] = pre_tr;
+    stdp_post[indx] = post_tr;
+  }
+}
+
+// activate_synapses (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:168-202):
+// slot (bufferloc + delay + g) % B with bufferloc = round(t/dt) % B (:127),
+// contributions w*scale applied in ascending key order, then row order.
+template <typename R>
+void Net<R>::propagate_thread(int th, int T) {
+  const size_t row = (size_t)N * L;
+  const int bufferloc = T % B;
+  for (int64_t key : active) {
+    const int64_t a = split[(size_t)key * (threads + 1) + th];
+    const int64_t b = split[(size_t)key * (threads + 1) + th + 1];
+    for (int64_t s = a; s < b; ++s) {
+      const int targetloc = (bufferloc + sdelay[s] + 0) % B;
+      ring[(size_t)targetloc * row + (size_t)spost[s] * L + slabel[s]] += sw[s] * sscale[s];
+    }
+  }
+}
+
+template <typename R>
+void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
+  auto step_time = [&](int64_t s, R& t, int& T) {
+    // current_time_in_seconds = starttime + s*timestep_grouping*timestep
+    // (Spike/Models/SpikingModel.cpp:226) and timestep_index =
+    // (int)roundf(t/dt) (Spike/Backend/CUDA/Neurons/LIFSpikingNeurons.cu:84).
+    float tf = start + (float)(s * 1) * dt_f;
+    T = round_to_int(tf / dt_f);
+    t = (sizeof(R) == 4) ? (R)tf : (R)start + (R)(s * 1) * dt;
+  };
+  auto finish_step = [&](R t) {
+    active.clear();
+    const int K = nkeys();
+    for (int kk = 0; kk < K; ++kk)
+      if (spiked[kk]) active.push_back(kk);
+    for (int64_t kk : active) events += (uint64_t)eff_count[kk];
+    return t;
+  };
+  auto record = [&](R t) {
+    // SpikingActivityMonitor: (id, current_time + g*timestep), here in key order.
+    const float tf = (float)t;
+    for (int64_t kk : active) {
+      if (kk >= Nin) {
+        rec_ids[SPK_POP_NEURONS].push_back((int32_t)(kk - Nin));
+        rec_times[SPK_POP_NEURONS].push_back(tf);
+      } else if (record_inputs) {
+        rec_ids[SPK_POP_INPUTS].push_back((int32_t)(Nin - 1 - kk));
+        rec_times[SPK_POP_INPUTS].push_back(tf);
+      }
+    }
+  };
+  const bool do_stdp = plastic && has_stdp && !plastic_idx.empty();
+  if (threads <= 1) {
+    for (int64_t s = 0; s < n_steps; ++s) {
+      R t;
+      int T;
+      step_time(s, t, T);
+      std::fill(spiked.begin(), spiked.end(), 0);
+      lif_range(0, N, t, T);
+      poisson_range(0, Nin, t, T);
+      if (do_stdp) stdp_range(0, (int64_t)plastic_idx.size(), t);
+      finish_step(t);
+      propagate_thread(0, T);
+      record(t);
+    }
+    return;
+  }
+  std::barrier<> bar(threads);
+  R t_cur = 0;
+  int T_cur = 0;
+  auto worker = [&](int th) {
+    for (int64_t s = 0; s < n_steps; ++s) {
+      if (th == 0) {
+        step_time(s, t_cur, T_cur);
+        std::fill(spiked.begin(), spiked.end(), 0);
+      }
+      bar.arrive_and_wait();
+      lif_range(n0[th], n1[th], t_cur, T_cur);
+      poisson_range(i0[th], i1[th], t_cur, T_cur);
+      bar.arrive_and_wait();
+      if (do_stdp) stdp_range(p0[th], p1[th], t_cur);
+      if (th == 0) finish_step(t_cur);
+      bar.arrive_and_wait();
+      propagate_thread(th, T_cur);
+      if (th == 0) record(t_cur);
+      bar.arrive_and_wait();
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int th = 1; th < threads; ++th) pool.emplace_back(worker, th);
+  worker(0);
+  for (auto& x : pool) x.join();
+}
+
+struct Handle {
+  int precision = 32;
+  Net<float>* f = nullptr;
+  Net<double>* d = nullptr;
+};
+
+}  // namespace
+
+struct oracle_net {
+  Handle h;
+};
+
+template <typename F>
+static auto dispatch(const oracle_net* n, F&& fn) {
+  if (n->h.precision == 64) return fn(*n->h.d);
+  return fn(*n->h.f);
+}
+
+extern "C" {
+
+int oracle_create(const spk_net_desc* desc, int precision, oracle_net** out) {
+  if (!desc || !out || desc->abi_version != SPK_ABI_VERSION) return SPK_ERR_INVALID;
+  if (precision != 32 && precision != 64) return SPK_ERR_INVALID;
+  oracle_net* n = new (std::nothrow) oracle_net();
+  if (!n) return SPK_ERR_OOM;
+  n->h.precision = precision;
+  int rc;
+  if (precision == 64) {
+    n->h.d = new Net<double>();
+    rc = n->h.d->init(desc);
+  } else {
+    n->h.f = new Net<float>();
+    rc = n->h.f->init(desc);
+  }
+  if (rc != SPK_OK) {
+    delete n->h.f;
+    delete n->h.d;
+    delete n;
+    return rc;
+  }
+  *out = n;
+  return SPK_OK;
+}
+
+int oracle_destroy(oracle_net* n) {
+  if (!n) return SPK_ERR_INVALID;
+  delete n->h.f;
+  delete n->h.d;
+  delete n;
+  return SPK_OK;
+}
+
+int oracle_set_threads(oracle_net* n, int threads) {
+  if (!n || threads < 1) return SPK_ERR_INVALID;
+  dispatch(n, [&](auto& net) {
+    net.set_threads(threads);
+    return 0;
+  });
+  return SPK_OK;
+}
+
+int oracle_reset_state(oracle_net* n) {
+  if (!n) return SPK_ERR_INVALID;
+  dispatch(n, [](auto& net) {
+    net.reset_state();
+    return 0;
+  });
+  return SPK_OK;
+}
+
+int oracle_reset_time(oracle_net* n) {
+  if (!n) return SPK_ERR_INVALID;
+  dispatch(n, [](auto& net) {
+    net.current_time = 0.0f;
+    return 0;
+  });
+  return SPK_OK;
+}
+
+int oracle_select_stimulus(oracle_net* n, int stimulus) {
+  if (!n) return SPK_ERR_INVALID;
+  return dispatch(n, [&](auto& net) {
+    if (stimulus < 0 || stimulus >= net.n_stim) return SPK_ERR_INVALID;
+    net.stim = stimulus;
+    net.reset_inputs();
+    return SPK_OK;
+  });
+}
+
+int oracle_run(oracle_net* n, float seconds, int plasticity_on) {
+  if (!n || !(seconds >= 0.0f)) return SPK_ERR_INVALID;
+  return dispatch(n, [&](auto& net) {
+    // number_of_timesteps = ceil(seconds / timestep); G = 1
+    // (Spike/Models/SpikingModel.cpp:221-222).
+    const float q = seconds / net.dt_f;
+    const int64_t steps = (int64_t)std::ceil(q);
+    const float start = net.current_time;
+    net.run_steps(steps, start, plasticity_on != 0);
+    net.current_time = start + seconds;
+    return SPK_OK;
+  });
+}
+
+int oracle_run_steps(oracle_net* n, int64_t n_steps, int plasticity_on) {
+  if (!n || n_steps < 0) return SPK_ERR_INVALID;
+  return dispatch(n, [&](auto& net) {
+    const float start = net.current_time;
+    net.run_steps(n_steps, start, plasticity_on != 0);
+    net.current_time = start + (float)n_steps * net.dt_f;
+    return SPK_OK;
+  });
+}
+
+int oracle_current_time(const oracle_net* n, float* seconds) {
+  if (!n || !seconds) return SPK_ERR_INVALID;
+  *seconds = dispatch(n, [](auto& net) { return net.current_time; });
+  return SPK_OK;
+}
+
+int oracle_spike_count(const oracle_net* n, int population, int64_t* out) {
+  if (!n || !out || population < 0 || population > 1) return SPK_ERR_INVALID;
+  *out = dispatch(n, [&](auto& net) { return (int64_t)net.rec_ids[population].size(); });
+  return SPK_OK;
+}
+
+int oracle_read_spikes(const oracle_net* n, int population, int32_t* ids, float* times,
+                       int64_t capacity, int64_t* n_written) {
+  if (!n || population < 0 || population > 1 || capacity < 0) return SPK_ERR_INVALID;
+  return dispatch(n, [&](auto& net) {
+    int64_t m = (int64_t)net.rec_ids[population].size();
+    if (m > capacity) m = capacity;
+    if (ids) std::memcpy(ids, net.rec_ids[population].data(), sizeof(int32_t) * m);
+    if (times) std::memcpy(times, net.rec_times[population].data(), sizeof(float) * m);
+    if (n_written) *n_written = m;
+    return SPK_OK;
+  });
+}
+
+int oracle_clear_spikes(oracle_net* n) {
+  if (!n) return SPK_ERR_INVALID;
+  dispatch(n, [](auto& net) {
+    for (int p = 0; p < 2; ++p) {
+      net.rec_ids[p].clear();
+      net.rec_times[p].clear();
+    }
+    return 0;
+  });
+  return SPK_OK;
+}
+
+int oracle_read_state(const oracle_net* n, int field, float* dst, int64_t count) {
+  if (!n || !dst) return SPK_ERR_INVALID;
+  return dispatch(n, [&](auto& net) {
+    auto put = [&](auto const& v) {
+      if ((int64_t)v.size() != count) return SPK_ERR_INVALID;
+      for (int64_t i = 0; i < count; ++i) dst[i] = (float)v[i];
+      return SPK_OK;
+    };
+    switch (field) {
+      case SPK_FIELD_V:
+        return put(net.V);
+      case SPK_FIELD_LAST_SPIKE:
+        return put(net.last);
+      case SPK_FIELD_SYN_TRACE:
+        return put(net.gtr);
+      case SPK_FIELD_INPUT_NEXT:
+        return put(net.in_next);
+      case SPK_FIELD_RING:
+        return put(net.ring);
+      case SPK_FIELD_PRE_TRACE:
+      case SPK_FIELD_POST_TRACE: {
+        // Per-neuron view of the per-synapse traces: all plastic synapses of
+        // one presynaptic (postsynaptic) neuron carry the same pre (post)
+        // trace, so the value is read off any of them.  Neurons with no
+        // plastic synapse read 0.
+        const bool pre = field == SPK_FIELD_PRE_TRACE;
+        int64_t want = pre ? (int64_t)net.Nin + net.N : (int64_t)net.N;
+        if (count != want) return SPK_ERR_INVALID;
+        for (int64_t i = 0; i < count; ++i) dst[i] = 0.0f;
+        for (size_t j = 0; j < net.plastic_idx.size(); ++j) {
+          int64_t s = net.plastic_idx[j];
+          if (pre) {
+            int p = net.spre[s];
+            int64_t slot = p < 0 ? (int64_t)(-p - 1) : (int64_t)net.Nin + p;
+            dst[slot] = (float)net.stdp_pre[j];
+          } else {
+            dst[net.spost[s]] = (float)net.stdp_post[j];
+          }
+        }
+        return SPK_OK;
+      }
+      default:
+        return SPK_ERR_INVALID;
+    }
+  });
+}
+
+int oracle_read_weights(const oracle_net* n, float* w, int64_t count) {
+  if (!n || !w) return SPK_ERR_INVALID;
+  return dispatch(n, [&](auto& net) {
+    if (count != net.S) return SPK_ERR_INVALID;
+    for (int64_t i = 0; i < count; ++i) w[i] = (float)net.sw[net.revsort[i]];
+    return SPK_OK;
+  });
+}
+
+int oracle_synaptic_events(const oracle_net* n, uint64_t* events) {
+  if (!n || !events) return SPK_ERR_INVALID;
+  *events = dispatch(n, [](auto& net) { return net.events; });
+  return SPK_OK;
+}
+
+int oracle_sorted_synapses(const oracle_net* n, int32_t* pre, int32_t* post, int32_t* delay,
+                           int64_t count) {
+  if (!n) return SPK_ERR_INVALID;
+  return dispatch(n, [&](auto& net) {
+    if (count != net.S || net.threads != 1) return SPK_ERR_INVALID;
+    for (int64_t s = 0; s < count; ++s) {
+      if (pre) pre[s] = net.spre[s];
+      if (post) post[s] = net.spost[s];
+      if (delay) delay[s] = net.sdelay[s];
+    }
+    return SPK_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,113 @@
+// spk_internal.h - host/device shared definitions of the step engine.
+#pragma once
+
+#include <stdint.h>
+#include <vector_types.h>
+
+#include "spk_error.h"
+#include "spk_rng.h"
+
+namespace spk {
+
+constexpr int MAX_GROUPS = 16;  // LIF groups per network
+constexpr int MAX_LABELS = 15;  // syn labels (4-bit field)
+constexpr int MAX_CLASSES = 16; // scale classes: 0 = pre-multiplied, 1..15 plastic
+constexpr int MAX_DELAY = 255;  // 8-bit delay field
+constexpr int LIST_CAP = 2048;  // active presynaptic keys staged per round
+constexpr int WPT_MAX = 16;     // bitmap words held per thread while listing
+
+// Packed synapse entry: x = post_local[0:16) | delay[16:24) | label[24:28) |
+// class[28:32), y = float bits of the value (w*scale for class 0, w otherwise).
+SPK_HD uint32_t pack_entry(uint32_t post_local, uint32_t delay, uint32_t label, uint32_t cls) {
+  return post_local | (delay << 16) | (label << 24) | (cls << 28);
+}
+
+struct GroupConst {
+  int start, end;  // [start, end)
+  float k, kR, v0, vreset, theta;
+};
+
+// Device-resident run control of one network.
+struct RunCtl {
+  float start_time;     // SpikingModel::current_time at run() entry
+  int step;             // steps done in the current run
+  int steps_total;      // steps in the current run
+  int plastic;          // plasticity_on for this run (and the net has STDP)
+  int inputs_active;    // Poisson 'active' flags (all equal, see reset)
+  int record_inputs;
+  long long gstep;      // steps since creation (bitmap / trace parity)
+  unsigned long long spike_count;  // entries in the spike store
+  unsigned long long events;       // synaptic events delivered
+  int status;           // 0 or SPK_ERR_* raised on the device
+  int pad;
+};
+
+// Everything one CTA needs to run its share of one network.
+struct NetDev {
+  // sizes and schedule
+  int N, Nin, KL, n_keys, n_words, L, B, kind;
+  int n_tiles, TS, ITS, W, nctas, n_groups;
+  float dt, half_dt, t_ref, i_bg;
+  GroupConst groups[MAX_GROUPS];
+  float decay[MAX_LABELS + 1], vhat[MAX_LABELS + 1];
+  float scale_tab[MAX_CLASSES];
+  // STDP (G = 1 constants of WeightDependentSTDPPlasticity.cu:125-145)
+  int has_stdp, clip_upper;
+  float E_m, E_p, inc_m, inc_p, invE_m, invE_p, lam, lam_alpha, wmax;
+  uint64_t seed;
+  // connectivity
+  const int* rowptr;   // [n_keys * n_tiles + 1]
+  uint2* entries;      // [S]
+  const int* csc_ptr;  // [N + 1] plastic afferents of each post
+  const uint2* csc;    // (entry index, pre key)
+  // home copies of the state held in shared memory during a launch
+  float* V;
+  float* last;
+  float* gtr;          // [N*L]
+  float* ring;         // [n_tiles][B][TS*L]
+  float* in_next;      // [Nin]
+  const float* rates;  // [Nin] of the selected stimulus
+  float* post_trace;   // [N]
+  float* pre_trace;    // [n_keys] own copy (home)
+  float* pre_pub;      // [2][n_keys] published each step for other CTAs
+  uint32_t* bitsA;     // [2][n_words] spikes of the step
+  uint32_t* bitsP;     // [2][n_words] STDP pre events of the step
+  uint2* spikes;       // spike store (key, float time bits)
+  long long spike_cap;
+  RunCtl* ctl;
+  unsigned int* barrier;  // per-network arrival counter (zeroed per launch)
+  int* abort_flag;        // shared by a launch: set on timeout
+};
+
+struct CtaMap {
+  int net;   // index into the NetDev array
+  int rank;  // CTA rank within the network
+};
+
+// Per-warp shared-memory words for a schedule (4-byte words).
+struct WarpLayout {
+  int ring, V, last, gtr, post_tr, pre_tr, spkw, in_next, in_rate, in_pre, seg, total;
+};
+SPK_HD WarpLayout warp_layout(int B, int TS, int L, int ITS, int kind, int has_stdp) {
+  WarpLayout w;
+  int o = 0;
+  w.ring = o; o += B * TS * L;
+  w.V = o; o += TS;
+  w.last = o; o += TS;
+  w.gtr = o; o += (kind == 3) ? 0 : TS * L;
+  w.post_tr = o; o += has_stdp ? TS : 0;
+  w.pre_tr = o; o += has_stdp ? TS : 0;
+  w.spkw = o; o += TS / 32;
+  w.in_next = o; o += ITS;
+  w.in_rate = o; o += ITS;
+  w.in_pre = o; o += has_stdp ? ITS : 0;
+  w.seg = o; o += 128;  // per batch of 32 rows: offset, row start, flags, pre trace
+  o = (o + 3) & ~3;
+  w.total = o;
+  return w;
+}
+// CTA-shared words: active list, scan scratch, flags.
+constexpr int SHARED_WORDS = LIST_CAP + 64 + 8;
+SPK_HD int smem_bytes(int W, const WarpLayout& wl) { return 4 * (SHARED_WORDS + W * wl.total); }
+
+}  // namespace spk

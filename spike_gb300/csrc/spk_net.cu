@@ -1,0 +1,1120 @@
+// spk_net.cu - C ABI of the step engine (spike_gb300.h): network creation
+// (planner + row-partitioned CSR builder), state management, launches.
+//
+// Compiled with -fmad=false (device) and -Xcompiler -ffp-contract=off (host):
+// the few float constants derived here on the host (k = dt/tau_m, k*R, label
+// decays, STDP trace constants, initial V) must round exactly as the oracle's.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "../../include/spike_gb300.h"
+#include "spk_internal.h"
+#include "spk_kernel.cuh"
+
+namespace spk {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+#define SPK_CUDA(call)                                                              \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) {                                                        \
+      ::spk::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                       __LINE__);                                                   \
+      return SPK_ERR_CUDA;                                                          \
+    }                                                                               \
+  } while (0)
+
+constexpr int U_ENTRIES = 8;
+constexpr int DEFAULT_STEPS_PER_LAUNCH = 1000;
+constexpr int64_t DEFAULT_SPIKE_CAPACITY = 1 << 24;
+
+static __global__ void set_ctl_kernel(RunCtl* ctl, float start, int steps_total, int plastic,
+                                      int record_inputs) {
+  ctl->start_time = start;
+  ctl->step = 0;
+  ctl->steps_total = steps_total;
+  ctl->plastic = plastic;
+  ctl->record_inputs = record_inputs;
+}
+
+static __global__ void clear_store_kernel(RunCtl* ctl) {
+  ctl->spike_count = 0ull;
+  if (ctl->status == SPK_ERR_OVERFLOW) ctl->status = 0;
+}
+
+static __global__ void reset_inputs_kernel(NetDev* nd, const float* rates, int Nin) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    nd->rates = rates;
+    nd->ctl->inputs_active = 0;
+  }
+  if (i < Nin) nd->in_next[i] = -1000.0f;
+}
+
+struct DeviceInfo {
+  int sms = 0;
+  int max_smem = 0;
+};
+
+static int device_info(DeviceInfo* di) {
+  int dev = 0;
+  SPK_CUDA(cudaGetDevice(&dev));
+  SPK_CUDA(cudaDeviceGetAttribute(&di->sms, cudaDevAttrMultiProcessorCount, dev));
+  SPK_CUDA(cudaDeviceGetAttribute(&di->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  return SPK_OK;
+}
+
+struct Plan {
+  int W, TS, ITS, nctas, n_tiles, KL, n_keys, n_words, K, smem;
+};
+
+static int plan_bytes(int B, int TS, int L, int ITS, int kind, int stdp, int W) {
+  return smem_bytes(W, warp_layout(B, TS, L, ITS, kind, stdp));
+}
+
+// Choose warps per CTA, tile size and CTA count for one network.  Small
+// networks run on one CTA (no inter-CTA barrier); larger ones spread tiles of
+// 64-256 posts over up to one CTA per SM.  Explicit schedule fields override.
+static int make_plan(int N, int Nin, int B, int L, int kind, int stdp, const spk_schedule* s,
+                     const DeviceInfo& di, Plan* p) {
+  auto finish = [&](int W, int TS, int nctas) {
+    p->W = W;
+    p->TS = TS;
+    p->nctas = nctas;
+    p->n_tiles = W * nctas;
+    p->ITS = Nin > 0 ? ((Nin + p->n_tiles - 1) / p->n_tiles + 31) / 32 * 32 : 0;
+    p->KL = p->n_tiles * p->ITS;
+    p->n_keys = p->KL + p->n_tiles * TS;
+    p->n_words = p->n_keys / 32;
+    p->smem = plan_bytes(B, TS, L, p->ITS, kind, stdp, W);
+    return p->smem <= di.max_smem && (int64_t)p->n_tiles * TS >= N;
+  };
+  const int K = (s && s->steps_per_launch > 0) ? s->steps_per_launch : DEFAULT_STEPS_PER_LAUNCH;
+  p->K = K;
+  const int Wreq = (s && s->warps_per_cta > 0) ? s->warps_per_cta : 0;
+  const int TSreq = (s && s->tile_posts > 0) ? s->tile_posts : 0;
+  const int Creq = (s && s->ctas > 0) ? s->ctas : 0;
+  if (Wreq > 16 || (TSreq && (TSreq % 32 || TSreq > 65504))) {
+    set_error("schedule: warps_per_cta must be <= 16 and tile_posts a multiple of 32 below 65536");
+    return SPK_ERR_INVALID;
+  }
+  if (Wreq || TSreq || Creq) {
+    const int W = Wreq ? Wreq : 8;
+    int TS = TSreq, C = Creq;
+    if (!TS && C) TS = std::max(32, ((N + W * C - 1) / (W * C) + 31) / 32 * 32);
+    if (!TS) TS = 64;
+    if (!C) C = (N + W * TS - 1) / (W * TS);
+    if (!finish(W, TS, C)) {
+      set_error("schedule W=%d tile=%d ctas=%d does not cover %d neurons within %d B of shared memory (needs %d)",
+                W, TS, C, N, di.max_smem, p->smem);
+      return SPK_ERR_INVALID;
+    }
+    return SPK_OK;
+  }
+  // one CTA when the whole network fits
+  for (int W : {16, 8}) {
+    const int TS = std::max(32, ((N + W - 1) / W + 31) / 32 * 32);
+    if (TS <= 65504 && finish(W, TS, 1)) return SPK_OK;
+  }
+  const int W = 8;
+  for (int TS : {64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096}) {
+    int C = (N + W * TS - 1) / (W * TS);
+    if (C > di.sms) continue;
+    if (finish(W, TS, C)) return SPK_OK;
+  }
+  for (int Wt : {4, 2, 1})
+    for (int TS = 32; TS <= 65504; TS *= 2) {
+      int C = (N + Wt * TS - 1) / (Wt * TS);
+      if (C > di.sms) continue;
+      if (finish(Wt, TS, C)) return SPK_OK;
+    }
+  set_error("no schedule fits %d neurons with ring depth %d and %d labels", N, B, L);
+  return SPK_ERR_UNSUPPORTED;
+}
+
+}  // namespace spk
+
+using namespace spk;
+
+struct spk_net {
+  // model
+  int N = 0, Nin = 0, L = 1, B = 0, kind = 0, n_stim = 0, stim = 0;
+  int64_t S = 0;
+  float dt = 0.f;
+  bool has_stdp = false, record_inputs = false;
+  uint64_t seed = 0;
+  std::vector<spk_neuron_group> groups;
+  std::vector<float> weights;      // creation order (host mirror)
+  std::vector<float> scales;       // creation order
+  std::vector<int32_t> entry_of;   // creation index -> entry index
+  std::vector<uint8_t> cls_of;     // creation index -> scale class
+  std::vector<float> scale_tab;
+  Plan plan{};
+  // device
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  NetDev hd{};             // host copy of the device descriptor
+  NetDev* dd = nullptr;    // device descriptor
+  CtaMap* dmap = nullptr;
+  float* rates_dev = nullptr;
+  int* abort_dev = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  bool cooperative = false;
+  int64_t launches = 0;
+  float current_time = 0.0f;
+  int pending_status = SPK_OK;
+};
+
+struct spk_batch {
+  std::vector<spk_net*> nets;
+  NetDev* dd = nullptr;
+  CtaMap* dmap = nullptr;
+  int* abort_dev = nullptr;
+  unsigned* barrier_pool = nullptr;
+  std::vector<std::pair<int, int>> waves;  // CTA ranges per launch
+  int W = 0, smem = 0, K = 0, total_ctas = 0;
+  bool cooperative = false;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+};
+
+namespace spk {
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+static int upload_state_defaults(spk_net* n) {
+  // SpikingModel::reset_state: V := V0 (or the V-init extension), last := -1000
+  // (Spike/Backend/CUDA/Neurons/SpikingNeurons.cu:68-94), ring and traces := 0
+  // (SpikingSynapses.cu:28-35, ConductanceSpikingSynapses.cu:49-56),
+  // inputs inactive (PoissonInputSpikingNeurons.cu:27-34), STDP traces := 0.
+  const NetDev& h = n->hd;
+  std::vector<float> V(n->N), last(n->N, -1000.0f);
+  for (const auto& g : n->groups)
+    for (int i = g.start; i < g.start + g.count; ++i) {
+      if (g.v_init_lo < g.v_init_hi) {
+        const float u = draw_uniform(n->seed, (uint32_t)i, 0u, DOMAIN_VINIT);
+        const float span = g.v_init_hi - g.v_init_lo;
+        V[i] = g.v_init_lo + span * u;
+      } else {
+        V[i] = g.v0;
+      }
+    }
+  SPK_CUDA(cudaMemcpyAsync(h.V, V.data(), sizeof(float) * n->N, cudaMemcpyHostToDevice, n->stream));
+  SPK_CUDA(cudaMemcpyAsync(h.last, last.data(), sizeof(float) * n->N, cudaMemcpyHostToDevice, n->stream));
+  SPK_CUDA(cudaMemsetAsync(h.gtr, 0, sizeof(float) * (size_t)n->N * n->L, n->stream));
+  SPK_CUDA(cudaMemsetAsync(h.ring, 0, sizeof(float) * (size_t)h.n_tiles * h.B * h.TS * h.L, n->stream));
+  if (n->has_stdp) {
+    SPK_CUDA(cudaMemsetAsync(h.post_trace, 0, sizeof(float) * n->N, n->stream));
+    SPK_CUDA(cudaMemsetAsync(h.pre_trace, 0, sizeof(float) * h.n_keys, n->stream));
+    SPK_CUDA(cudaMemsetAsync(h.pre_pub, 0, sizeof(float) * 2 * (size_t)h.n_keys, n->stream));
+  }
+  if (n->Nin > 0) {
+    reset_inputs_kernel<<<(n->Nin + 255) / 256, 256, 0, n->stream>>>(n->dd, n->rates_dev + (size_t)n->stim * n->Nin, n->Nin);
+    SPK_CUDA(cudaGetLastError());
+  } else {
+    int zero = 0;
+    SPK_CUDA(cudaMemcpyAsync(&h.ctl->inputs_active, &zero, sizeof(int), cudaMemcpyHostToDevice, n->stream));
+    SPK_CUDA(cudaStreamSynchronize(n->stream));
+  }
+  return SPK_OK;
+}
+
+static int launch_block(spk_net* n) {
+  SPK_CUDA(cudaMemsetAsync(n->hd.barrier, 0, sizeof(unsigned), n->stream));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(n->plan.nctas);
+  cfg.blockDim = dim3(n->plan.W * 32);
+  cfg.dynamicSmemBytes = n->plan.smem;
+  cfg.stream = n->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = n->cooperative ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  SPK_CUDA(cudaLaunchKernelEx(&cfg, step_kernel<U_ENTRIES>, (const NetDev*)n->dd, (const CtaMap*)n->dmap,
+                              n->plan.K));
+  return SPK_OK;
+}
+
+static int build_graph(spk_net* n) {
+  cudaGraph_t g = nullptr;
+  SPK_CUDA(cudaStreamBeginCapture(n->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = launch_block(n);
+  cudaError_t e = cudaStreamEndCapture(n->stream, &g);
+  if (rc != SPK_OK || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    n->graph = nullptr;
+    return SPK_OK;  // launches go direct
+  }
+  e = cudaGraphInstantiate(&n->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    n->graph = nullptr;
+  }
+  return SPK_OK;
+}
+
+static int run_steps_impl(spk_net* n, int64_t steps, int plastic, float start) {
+  if (steps <= 0) return SPK_OK;
+  if (steps > 0x7fffffff) {
+    set_error("run of %lld steps exceeds the 2^31-1 step limit of one run", (long long)steps);
+    return SPK_ERR_INVALID;
+  }
+  set_ctl_kernel<<<1, 1, 0, n->stream>>>(n->hd.ctl, start, (int)steps,
+                                         (plastic && n->has_stdp) ? 1 : 0, n->record_inputs ? 1 : 0);
+  SPK_CUDA(cudaGetLastError());
+  const int64_t blocks = (steps + n->plan.K - 1) / n->plan.K;
+  for (int64_t b = 0; b < blocks; ++b) {
+    if (n->graph) {
+      SPK_CUDA(cudaGraphLaunch(n->graph, n->stream));
+    } else {
+      int rc = launch_block(n);
+      if (rc) return rc;
+    }
+    ++n->launches;
+  }
+  return SPK_OK;
+}
+
+static int read_status(spk_net* n, int* status) {
+  SPK_CUDA(cudaStreamSynchronize(n->stream));
+  int st = 0;
+  SPK_CUDA(cudaMemcpy(&st, &n->hd.ctl->status, sizeof(int), cudaMemcpyDeviceToHost));
+  *status = st;
+  return SPK_OK;
+}
+
+template <typename F>
+static int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const std::bad_alloc&) {
+    set_error("host allocation failed");
+    return SPK_ERR_OOM;
+  }
+}
+
+static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net** out) {
+  if (!d || !out) {
+    set_error("null argument");
+    return SPK_ERR_INVALID;
+  }
+  if (d->abi_version != SPK_ABI_VERSION) {
+    set_error("descriptor ABI version %d, library %d", d->abi_version, SPK_ABI_VERSION);
+    return SPK_ERR_INVALID;
+  }
+  const int N = d->n_neurons, Nin = d->n_inputs, L = d->n_labels;
+  if (N <= 0 || Nin < 0 || L < 1 || L > MAX_LABELS || !(d->dt > 0.0f) || d->n_synapses < 0 ||
+      d->n_synapses > 0x7fffffffLL) {
+    set_error("descriptor sizes out of range (neurons %d, inputs %d, labels %d, synapses %lld)", N, Nin, L,
+              (long long)d->n_synapses);
+    return SPK_ERR_INVALID;
+  }
+  if (d->synapse_kind != SPK_SYN_CONDUCTANCE && d->synapse_kind != SPK_SYN_CURRENT &&
+      d->synapse_kind != SPK_SYN_VOLTAGE) {
+    set_error("unknown synapse kind %d", d->synapse_kind);
+    return SPK_ERR_INVALID;
+  }
+  if (d->n_groups < 1 || d->n_groups > MAX_GROUPS || !d->groups) {
+    set_error("between 1 and %d neuron groups are supported (got %d)", MAX_GROUPS, d->n_groups);
+    return d->n_groups > MAX_GROUPS ? SPK_ERR_UNSUPPORTED : SPK_ERR_INVALID;
+  }
+  {
+    int expect = 0;
+    for (int g = 0; g < d->n_groups; ++g) {
+      if (d->groups[g].start != expect || d->groups[g].count <= 0) {
+        set_error("neuron groups must be contiguous, ascending and non-empty");
+        return SPK_ERR_INVALID;
+      }
+      expect += d->groups[g].count;
+    }
+    if (expect != N) {
+      set_error("neuron groups cover %d neurons, descriptor says %d", expect, N);
+      return SPK_ERR_INVALID;
+    }
+  }
+  if (Nin > 0 && (d->n_stimuli < 1 || !d->input_rates || d->stimulus < 0 || d->stimulus >= d->n_stimuli)) {
+    set_error("inputs need rates and a valid stimulus");
+    return SPK_ERR_INVALID;
+  }
+  if (d->synapse_kind != SPK_SYN_VOLTAGE && !d->label_tau) {
+    set_error("conductance/current synapses need label_tau");
+    return SPK_ERR_INVALID;
+  }
+  if (d->synapse_kind == SPK_SYN_CONDUCTANCE && !d->label_vhat) {
+    set_error("conductance synapses need label_vhat");
+    return SPK_ERR_INVALID;
+  }
+  const int64_t S = d->n_synapses;
+  if (S > 0 && (!d->pre || !d->post || !d->weight || !d->scale || !d->delay)) {
+    set_error("synapse arrays missing");
+    return SPK_ERR_INVALID;
+  }
+  int Dmax = 0, Dmin = 1 << 30;
+  for (int64_t s = 0; s < S; ++s) {
+    const int p = d->pre[s], q = d->post[s], dl = d->delay[s], lb = d->label ? d->label[s] : 0;
+    if (p < -Nin || p >= N || q < 0 || q >= N || dl < 1 || lb < 0 || lb >= L) {
+      set_error("synapse %lld out of range (pre %d post %d delay %d label %d)", (long long)s, p, q, dl, lb);
+      return SPK_ERR_INVALID;
+    }
+    Dmax = std::max(Dmax, dl);
+    Dmin = std::min(Dmin, dl);
+  }
+  if (S > 0 && Dmin != 1) {
+    set_error("minimum delay %d steps: timestep grouping > 1 is not supported", Dmin);
+    return SPK_ERR_UNSUPPORTED;
+  }
+  if (Dmax > MAX_DELAY) {
+    set_error("delay %d steps exceeds the supported maximum %d", Dmax, MAX_DELAY);
+    return SPK_ERR_UNSUPPORTED;
+  }
+  if (S == 0) Dmax = 1;
+  const int B = Dmax + 2 * 1 + 1;  // SpikingSynapses.cu:48 with G = 1
+  const int stdp = d->has_stdp ? 1 : 0;
+
+  DeviceInfo di;
+  int rc = device_info(&di);
+  if (rc) return rc;
+  Plan plan;
+  rc = make_plan(N, Nin, B, L, d->synapse_kind, stdp, sched, di, &plan);
+  if (rc) return rc;
+
+  spk_net* n = new spk_net();
+  n->N = N;
+  n->Nin = Nin;
+  n->L = L;
+  n->B = B;
+  n->kind = d->synapse_kind;
+  n->S = S;
+  n->dt = d->dt;
+  n->has_stdp = stdp != 0;
+  n->record_inputs = d->record_inputs != 0;
+  n->seed = d->seed;
+  n->n_stim = Nin > 0 ? d->n_stimuli : 0;
+  n->stim = Nin > 0 ? d->stimulus : 0;
+  n->groups.assign(d->groups, d->groups + d->n_groups);
+  n->plan = plan;
+  n->weights.assign(d->weight, d->weight + S);
+  n->scales.assign(d->scale, d->scale + S);
+
+  // ---- scale classes of plastic synapses ------------------------------------
+  n->scale_tab.assign(MAX_CLASSES, 0.0f);
+  n->cls_of.assign(S, 0);
+  {
+    std::map<uint32_t, int> cls;
+    for (int64_t s = 0; s < S; ++s) {
+      if (!(stdp && d->plastic && d->plastic[s])) continue;
+      const uint32_t bits = f2u(d->scale[s]);
+      auto it = cls.find(bits);
+      int c;
+      if (it == cls.end()) {
+        c = (int)cls.size() + 1;
+        if (c >= MAX_CLASSES) {
+          set_error("more than %d distinct weight scales among plastic synapses", MAX_CLASSES - 1);
+          delete n;
+          return SPK_ERR_UNSUPPORTED;
+        }
+        cls[bits] = c;
+        n->scale_tab[c] = d->scale[s];
+      } else {
+        c = it->second;
+      }
+      n->cls_of[s] = (uint8_t)c;
+    }
+  }
+
+  // ---- row-partitioned CSR: entries sorted by (key, tile), stable ------------
+  const int n_tiles = plan.n_tiles, TS = plan.TS, KL = plan.KL, n_keys = plan.n_keys;
+  const size_t n_cells = (size_t)n_keys * n_tiles;
+  std::vector<int32_t> rowptr(n_cells + 1, 0);
+  auto key_of = [&](int p) { return p < 0 ? Nin + p : KL + p; };
+  for (int64_t s = 0; s < S; ++s) {
+    const size_t c = (size_t)key_of(d->pre[s]) * n_tiles + d->post[s] / TS;
+    rowptr[c + 1]++;
+  }
+  for (size_t c = 0; c < n_cells; ++c) rowptr[c + 1] += rowptr[c];
+  std::vector<uint2> entries(S);
+  n->entry_of.resize(S);
+  {
+    std::vector<int32_t> fill(rowptr.begin(), rowptr.end() - 1);
+    for (int64_t s = 0; s < S; ++s) {
+      const int q = d->post[s];
+      const size_t c = (size_t)key_of(d->pre[s]) * n_tiles + q / TS;
+      const int32_t pos = fill[c]++;
+      const int cl = n->cls_of[s];
+      const float v = cl ? d->weight[s] : d->weight[s] * d->scale[s];
+      entries[pos] = make_uint2(pack_entry((uint32_t)(q % TS), (uint32_t)d->delay[s],
+                                           (uint32_t)(d->label ? d->label[s] : 0), (uint32_t)cl),
+                                f2u(v));
+      n->entry_of[s] = pos;
+    }
+  }
+  // ---- plastic afferents per post (for the post-spike pass) -------------------
+  std::vector<int32_t> csc_ptr;
+  std::vector<uint2> csc;
+  if (stdp) {
+    csc_ptr.assign((size_t)N + 1, 0);
+    for (int64_t s = 0; s < S; ++s)
+      if (n->cls_of[s]) csc_ptr[d->post[s] + 1]++;
+    for (int q = 0; q < N; ++q) csc_ptr[q + 1] += csc_ptr[q];
+    csc.resize(csc_ptr[N]);
+    std::vector<int32_t> fill(csc_ptr.begin(), csc_ptr.end() - 1);
+    for (int64_t s = 0; s < S; ++s)
+      if (n->cls_of[s]) csc[fill[d->post[s]]++] = make_uint2((uint32_t)n->entry_of[s], (uint32_t)key_of(d->pre[s]));
+  }
+
+  // ---- device arena --------------------------------------------------------------
+  const int n_words = plan.n_words;
+  int64_t spike_cap = d->spike_capacity == 0 ? DEFAULT_SPIKE_CAPACITY : std::max<int64_t>(0, d->spike_capacity);
+  struct Part {
+    void** dst;
+    size_t bytes;
+  };
+  NetDev& h = n->hd;
+  std::memset(&h, 0, sizeof(h));
+  void* p_rowptr = nullptr; void* p_entries = nullptr; void* p_cscptr = nullptr; void* p_csc = nullptr;
+  void* p_V = nullptr; void* p_last = nullptr; void* p_gtr = nullptr; void* p_ring = nullptr;
+  void* p_innext = nullptr; void* p_rates = nullptr; void* p_post = nullptr; void* p_pre = nullptr;
+  void* p_pub = nullptr; void* p_bA = nullptr; void* p_bP = nullptr; void* p_spk = nullptr;
+  void* p_ctl = nullptr; void* p_bar = nullptr; void* p_abort = nullptr; void* p_dd = nullptr; void* p_map = nullptr;
+  std::vector<Part> parts = {
+      {&p_rowptr, sizeof(int32_t) * rowptr.size()},
+      {&p_entries, sizeof(uint2) * (size_t)std::max<int64_t>(S, 1)},
+      {&p_cscptr, sizeof(int32_t) * csc_ptr.size()},
+      {&p_csc, sizeof(uint2) * csc.size()},
+      {&p_V, sizeof(float) * N},
+      {&p_last, sizeof(float) * N},
+      {&p_gtr, sizeof(float) * (size_t)N * L},
+      {&p_ring, sizeof(float) * (size_t)n_tiles * B * TS * L},
+      {&p_innext, sizeof(float) * std::max(Nin, 1)},
+      {&p_rates, sizeof(float) * std::max<size_t>((size_t)n->n_stim * Nin, 1)},
+      {&p_post, sizeof(float) * (stdp ? N : 0)},
+      {&p_pre, sizeof(float) * (stdp ? n_keys : 0)},
+      {&p_pub, sizeof(float) * (stdp ? 2 * (size_t)n_keys : 0)},
+      {&p_bA, sizeof(uint32_t) * 2 * (size_t)n_words},
+      {&p_bP, sizeof(uint32_t) * 2 * (size_t)n_words},
+      {&p_spk, sizeof(uint2) * (size_t)std::max<int64_t>(spike_cap, 1)},
+      {&p_ctl, sizeof(RunCtl)},
+      {&p_bar, sizeof(unsigned)},
+      {&p_abort, sizeof(int)},
+      {&p_dd, sizeof(NetDev)},
+      {&p_map, sizeof(CtaMap) * plan.nctas},
+  };
+  size_t total = 0;
+  for (auto& p : parts) total = align_up(total, 256) + align_up(std::max<size_t>(p.bytes, 4), 256);
+  cudaError_t e = cudaMalloc(&n->arena, total);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("device allocation of %zu bytes failed: %s", total, cudaGetErrorString(e));
+    delete n;
+    return SPK_ERR_OOM;
+  }
+  n->arena_bytes = total;
+  {
+    size_t off = 0;
+    for (auto& p : parts) {
+      off = align_up(off, 256);
+      *p.dst = (char*)n->arena + off;
+      off += align_up(std::max<size_t>(p.bytes, 4), 256);
+    }
+  }
+  auto fail_free = [&](int code) {
+    if (n->stream) cudaStreamDestroy(n->stream);
+    cudaFree(n->arena);
+    delete n;
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error("cudaStreamCreate failed");
+    return fail_free(SPK_ERR_CUDA);
+  }
+
+  // ---- device descriptor ---------------------------------------------------------
+  h.N = N;
+  h.Nin = Nin;
+  h.KL = KL;
+  h.n_keys = n_keys;
+  h.n_words = n_words;
+  h.L = L;
+  h.B = B;
+  h.kind = d->synapse_kind;
+  h.n_tiles = n_tiles;
+  h.TS = TS;
+  h.ITS = plan.ITS;
+  h.W = plan.W;
+  h.nctas = plan.nctas;
+  h.n_groups = d->n_groups;
+  h.dt = d->dt;
+  h.half_dt = 0.5f * d->dt;
+  h.t_ref = d->refractory_period;
+  h.i_bg = d->background_current;
+  for (int g = 0; g < d->n_groups; ++g) {
+    const spk_neuron_group& G = d->groups[g];
+    GroupConst& c = h.groups[g];
+    c.start = G.start;
+    c.end = G.start + G.count;
+    // LIFSpikingNeurons.cu:31-44: k = timestep / tau_m, kR = k * R (host float).
+    c.k = d->dt / G.tau_m;
+    c.kR = c.k * G.R;
+    c.v0 = G.v0;
+    c.vreset = G.vreset;
+    c.theta = G.theta;
+  }
+  for (int l = 0; l < L; ++l) {
+    // ConductanceSpikingSynapses.cu:76-78: expf(-timestep / tau_g) on the host.
+    h.decay[l] = d->synapse_kind == SPK_SYN_VOLTAGE ? 0.0f : expf(-d->dt / d->label_tau[l]);
+    h.vhat[l] = d->synapse_kind == SPK_SYN_CONDUCTANCE ? d->label_vhat[l] : 0.0f;
+  }
+  for (int c = 0; c < MAX_CLASSES; ++c) h.scale_tab[c] = n->scale_tab[c];
+  h.has_stdp = stdp;
+  if (stdp) {
+    const spk_stdp_params& sp = d->stdp;
+    // WeightDependentSTDPPlasticity.cu:125-145 for G = 1 (see stdp_update).
+    const float em = expf(-(1.0f * d->dt) / sp.tau_minus);
+    const float ep = expf(-(1.0f * d->dt) / sp.tau_plus);
+    h.E_m = em;
+    h.E_p = ep;
+    h.inc_m = sp.a_minus * em;
+    h.inc_p = sp.a_plus * ep;
+    h.invE_m = 1.0f / em;
+    h.invE_p = 1.0f / ep;
+    h.lam = sp.lambda;
+    h.lam_alpha = sp.lambda * sp.alpha;
+    h.wmax = sp.w_max;
+    h.clip_upper = sp.clip_upper ? 1 : 0;
+  }
+  h.seed = d->seed;
+  h.rowptr = (const int*)p_rowptr;
+  h.entries = (uint2*)p_entries;
+  h.csc_ptr = (const int*)p_cscptr;
+  h.csc = (const uint2*)p_csc;
+  h.V = (float*)p_V;
+  h.last = (float*)p_last;
+  h.gtr = (float*)p_gtr;
+  h.ring = (float*)p_ring;
+  h.in_next = (float*)p_innext;
+  n->rates_dev = (float*)p_rates;
+  h.rates = n->rates_dev + (size_t)n->stim * Nin;
+  h.post_trace = (float*)p_post;
+  h.pre_trace = (float*)p_pre;
+  h.pre_pub = (float*)p_pub;
+  h.bitsA = (uint32_t*)p_bA;
+  h.bitsP = (uint32_t*)p_bP;
+  h.spikes = (uint2*)p_spk;
+  h.spike_cap = spike_cap;
+  h.ctl = (RunCtl*)p_ctl;
+  h.barrier = (unsigned*)p_bar;
+  h.abort_flag = (int*)p_abort;
+  n->abort_dev = (int*)p_abort;
+  n->dd = (NetDev*)p_dd;
+  n->dmap = (CtaMap*)p_map;
+
+  // ---- uploads ---------------------------------------------------------------------
+  auto up = [&](void* dst, const void* src, size_t bytes) -> int {
+    if (bytes == 0) return SPK_OK;
+    SPK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, n->stream));
+    return SPK_OK;
+  };
+  std::vector<CtaMap> map(plan.nctas);
+  for (int r = 0; r < plan.nctas; ++r) map[r] = CtaMap{0, r};
+  RunCtl ctl{};
+  int urc = SPK_OK;
+  urc |= up(p_rowptr, rowptr.data(), sizeof(int32_t) * rowptr.size());
+  urc |= up(p_entries, entries.data(), sizeof(uint2) * S);
+  urc |= up(p_cscptr, csc_ptr.data(), sizeof(int32_t) * csc_ptr.size());
+  urc |= up(p_csc, csc.data(), sizeof(uint2) * csc.size());
+  if (Nin > 0) urc |= up(p_rates, d->input_rates, sizeof(float) * (size_t)n->n_stim * Nin);
+  urc |= up(p_ctl, &ctl, sizeof(ctl));
+  urc |= up(p_dd, &h, sizeof(h));
+  urc |= up(p_map, map.data(), sizeof(CtaMap) * map.size());
+  if (urc) return fail_free(SPK_ERR_CUDA);
+  if (cudaMemsetAsync(p_bA, 0, sizeof(uint32_t) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
+      cudaMemsetAsync(p_bP, 0, sizeof(uint32_t) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
+      cudaMemsetAsync(p_abort, 0, sizeof(int), n->stream) != cudaSuccess) {
+    set_error("cudaMemsetAsync failed");
+    return fail_free(SPK_ERR_CUDA);
+  }
+  if (cudaFuncSetAttribute(step_kernel<U_ENTRIES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           di.max_smem) != cudaSuccess) {
+    set_error("cudaFuncSetAttribute failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return fail_free(SPK_ERR_CUDA);
+  }
+  if (plan.nctas > 1) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_kernel<U_ENTRIES>, plan.W * 32, plan.smem) !=
+        cudaSuccess) {
+      set_error("occupancy query failed");
+      return fail_free(SPK_ERR_CUDA);
+    }
+    if ((int64_t)per_sm * di.sms < plan.nctas) {
+      set_error("schedule needs %d co-resident CTAs, device holds %d", plan.nctas, per_sm * di.sms);
+      return fail_free(SPK_ERR_UNSUPPORTED);
+    }
+    n->cooperative = true;
+  }
+  int rrc = upload_state_defaults(n);
+  if (rrc) return fail_free(rrc);
+  if (cudaStreamSynchronize(n->stream) != cudaSuccess) {
+    set_error("initial upload failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return fail_free(SPK_ERR_CUDA);
+  }
+  build_graph(n);
+  *out = n;
+  return SPK_OK;
+}
+
+}  // namespace spk
+
+// =====================================================================================
+extern "C" {
+
+const char* spk_last_error(void) { return spk::g_err; }
+int spk_abi_version(void) { return SPK_ABI_VERSION; }
+
+int spk_net_create(const spk_net_desc* desc, const spk_schedule* schedule, spk_net** out) {
+  return guarded([&] { return create_impl(desc, schedule, out); });
+}
+
+int spk_net_destroy(spk_net* n) {
+  if (!n) return SPK_ERR_INVALID;
+  if (n->stream) cudaStreamSynchronize(n->stream);
+  if (n->graph) cudaGraphExecDestroy(n->graph);
+  if (n->stream) cudaStreamDestroy(n->stream);
+  if (n->arena) cudaFree(n->arena);
+  delete n;
+  return SPK_OK;
+}
+
+int spk_net_reset_state(spk_net* n) {
+  if (!n) return SPK_ERR_INVALID;
+  int rc = upload_state_defaults(n);
+  if (rc) return rc;
+  SPK_CUDA(cudaStreamSynchronize(n->stream));
+  return SPK_OK;
+}
+
+int spk_net_reset_time(spk_net* n) {
+  if (!n) return SPK_ERR_INVALID;
+  n->current_time = 0.0f;
+  return SPK_OK;
+}
+
+int spk_net_select_stimulus(spk_net* n, int32_t stimulus) {
+  if (!n) return SPK_ERR_INVALID;
+  if (n->Nin == 0 || stimulus < 0 || stimulus >= n->n_stim) {
+    set_error("stimulus %d out of range (%d loaded)", stimulus, n->n_stim);
+    return SPK_ERR_INVALID;
+  }
+  n->stim = stimulus;
+  n->hd.rates = n->rates_dev + (size_t)stimulus * n->Nin;
+  reset_inputs_kernel<<<(n->Nin + 255) / 256, 256, 0, n->stream>>>(n->dd, n->hd.rates, n->Nin);
+  SPK_CUDA(cudaGetLastError());
+  return SPK_OK;
+}
+
+int spk_net_run(spk_net* n, float seconds, int32_t plasticity_on) {
+  if (!n || !(seconds >= 0.0f)) return SPK_ERR_INVALID;
+  // number_of_timesteps = ceil(seconds / timestep) in float
+  // (Spike/Models/SpikingModel.cpp:221-222), end time start + seconds (:235).
+  const float q = seconds / n->dt;
+  const int64_t steps = (int64_t)std::ceil(q);
+  const float start = n->current_time;
+  int rc = run_steps_impl(n, steps, plasticity_on, start);
+  if (rc) return rc;
+  n->current_time = start + seconds;
+  return SPK_OK;
+}
+
+int spk_net_run_steps(spk_net* n, int64_t n_steps, int32_t plasticity_on) {
+  if (!n || n_steps < 0) return SPK_ERR_INVALID;
+  const float start = n->current_time;
+  int rc = run_steps_impl(n, n_steps, plasticity_on, start);
+  if (rc) return rc;
+  n->current_time = start + (float)n_steps * n->dt;
+  return SPK_OK;
+}
+
+int spk_net_synchronize(spk_net* n) {
+  if (!n) return SPK_ERR_INVALID;
+  int st = 0;
+  int rc = read_status(n, &st);
+  if (rc) return rc;
+  if (st == SPK_ERR_TIMEOUT) set_error("a device barrier timed out");
+  if (st == SPK_ERR_OVERFLOW) set_error("the device spike store overflowed; spikes were dropped");
+  return st;
+}
+
+int spk_net_current_time(const spk_net* n, float* s) {
+  if (!n || !s) return SPK_ERR_INVALID;
+  *s = n->current_time;
+  return SPK_OK;
+}
+
+static int read_store(spk_net* n, std::vector<uint2>& out) {
+  SPK_CUDA(cudaStreamSynchronize(n->stream));
+  RunCtl c;
+  SPK_CUDA(cudaMemcpy(&c, n->hd.ctl, sizeof(c), cudaMemcpyDeviceToHost));
+  const uint64_t cnt = std::min<uint64_t>(c.spike_count, (uint64_t)n->hd.spike_cap);
+  out.resize(cnt);
+  if (cnt) SPK_CUDA(cudaMemcpy(out.data(), n->hd.spikes, sizeof(uint2) * cnt, cudaMemcpyDeviceToHost));
+  return SPK_OK;
+}
+
+int spk_net_spike_count(spk_net* n, int32_t population, int64_t* count) {
+  if (!n || !count || population < 0 || population > 1) return SPK_ERR_INVALID;
+  return guarded([&] {
+    std::vector<uint2> st;
+    int rc = read_store(n, st);
+    if (rc) return rc;
+    int64_t c = 0;
+    for (const auto& e : st) c += ((int)e.x >= n->hd.KL) == (population == SPK_POP_NEURONS);
+    *count = c;
+    return SPK_OK;
+  });
+}
+
+int spk_net_read_spikes(spk_net* n, int32_t population, int32_t* ids, float* times, int64_t capacity,
+                        int64_t* n_written) {
+  if (!n || population < 0 || population > 1 || capacity < 0) return SPK_ERR_INVALID;
+  return guarded([&] {
+    std::vector<uint2> st;
+    int rc = read_store(n, st);
+    if (rc) return rc;
+    int64_t m = 0;
+    for (const auto& e : st) {
+      const int key = (int)e.x;
+      const bool is_neuron = key >= n->hd.KL;
+      if (is_neuron != (population == SPK_POP_NEURONS)) continue;
+      if (m >= capacity) break;
+      if (ids) ids[m] = is_neuron ? key - n->hd.KL : n->Nin - 1 - key;
+      if (times) times[m] = u2f(e.y);
+      ++m;
+    }
+    if (n_written) *n_written = m;
+    return SPK_OK;
+  });
+}
+
+int spk_net_clear_spikes(spk_net* n) {
+  if (!n) return SPK_ERR_INVALID;
+  clear_store_kernel<<<1, 1, 0, n->stream>>>(n->hd.ctl);
+  SPK_CUDA(cudaGetLastError());
+  return SPK_OK;
+}
+
+int spk_net_read_state(spk_net* n, int32_t field, void* dst, int64_t count) {
+  if (!n || !dst) return SPK_ERR_INVALID;
+  return guarded([&]() -> int {
+    SPK_CUDA(cudaStreamSynchronize(n->stream));
+    const NetDev& h = n->hd;
+    float* out = (float*)dst;
+    auto need = [&](int64_t c) {
+      if (count != c) {
+        set_error("field %d holds %lld values, %lld requested", field, (long long)c, (long long)count);
+        return false;
+      }
+      return true;
+    };
+    switch (field) {
+      case SPK_FIELD_V:
+        if (!need(n->N)) return SPK_ERR_INVALID;
+        SPK_CUDA(cudaMemcpy(out, h.V, sizeof(float) * n->N, cudaMemcpyDeviceToHost));
+        return SPK_OK;
+      case SPK_FIELD_LAST_SPIKE:
+        if (!need(n->N)) return SPK_ERR_INVALID;
+        SPK_CUDA(cudaMemcpy(out, h.last, sizeof(float) * n->N, cudaMemcpyDeviceToHost));
+        return SPK_OK;
+      case SPK_FIELD_SYN_TRACE:
+        if (!need((int64_t)n->N * n->L)) return SPK_ERR_INVALID;
+        if (n->kind == SPK_SYN_VOLTAGE) {
+          std::fill(out, out + count, 0.0f);
+          return SPK_OK;
+        }
+        SPK_CUDA(cudaMemcpy(out, h.gtr, sizeof(float) * n->N * n->L, cudaMemcpyDeviceToHost));
+        return SPK_OK;
+      case SPK_FIELD_INPUT_NEXT:
+        if (!need(n->Nin)) return SPK_ERR_INVALID;
+        if (n->Nin) SPK_CUDA(cudaMemcpy(out, h.in_next, sizeof(float) * n->Nin, cudaMemcpyDeviceToHost));
+        return SPK_OK;
+      case SPK_FIELD_RING: {
+        if (!need((int64_t)n->B * n->N * n->L)) return SPK_ERR_INVALID;
+        std::vector<float> r((size_t)h.n_tiles * h.B * h.TS * h.L);
+        SPK_CUDA(cudaMemcpy(r.data(), h.ring, sizeof(float) * r.size(), cudaMemcpyDeviceToHost));
+        for (int slot = 0; slot < h.B; ++slot)
+          for (int q = 0; q < n->N; ++q)
+            for (int l = 0; l < h.L; ++l) {
+              const int t = q / h.TS, ql = q % h.TS;
+              out[((size_t)slot * n->N + q) * h.L + l] = r[(((size_t)t * h.B + slot) * h.TS + ql) * h.L + l];
+            }
+        return SPK_OK;
+      }
+      case SPK_FIELD_PRE_TRACE: {
+        if (!need((int64_t)n->Nin + n->N)) return SPK_ERR_INVALID;
+        if (!n->has_stdp) {
+          std::fill(out, out + count, 0.0f);
+          return SPK_OK;
+        }
+        std::vector<float> p(h.n_keys);
+        SPK_CUDA(cudaMemcpy(p.data(), h.pre_trace, sizeof(float) * p.size(), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < n->Nin; ++i) out[i] = p[n->Nin - 1 - i];
+        for (int q = 0; q < n->N; ++q) out[n->Nin + q] = p[h.KL + q];
+        return SPK_OK;
+      }
+      case SPK_FIELD_POST_TRACE:
+        if (!need(n->N)) return SPK_ERR_INVALID;
+        if (!n->has_stdp) {
+          std::fill(out, out + count, 0.0f);
+          return SPK_OK;
+        }
+        SPK_CUDA(cudaMemcpy(out, h.post_trace, sizeof(float) * n->N, cudaMemcpyDeviceToHost));
+        return SPK_OK;
+      default:
+        set_error("unknown state field %d", field);
+        return SPK_ERR_INVALID;
+    }
+  });
+}
+
+int spk_net_read_weights(spk_net* n, float* w, int64_t count) {
+  if (!n || (!w && count) || count != n->S) {
+    set_error("weights: %lld requested, network has %lld synapses", (long long)count, n ? (long long)n->S : 0LL);
+    return SPK_ERR_INVALID;
+  }
+  return guarded([&]() -> int {
+    if (n->has_stdp) {
+      SPK_CUDA(cudaStreamSynchronize(n->stream));
+      std::vector<uint2> e(n->S);
+      SPK_CUDA(cudaMemcpy(e.data(), n->hd.entries, sizeof(uint2) * n->S, cudaMemcpyDeviceToHost));
+      for (int64_t s = 0; s < n->S; ++s)
+        if (n->cls_of[s]) n->weights[s] = u2f(e[n->entry_of[s]].y);
+    }
+    std::memcpy(w, n->weights.data(), sizeof(float) * n->S);
+    return SPK_OK;
+  });
+}
+
+int spk_net_write_weights(spk_net* n, const float* w, int64_t count) {
+  if (!n || (!w && count) || count != n->S) return SPK_ERR_INVALID;
+  return guarded([&]() -> int {
+    SPK_CUDA(cudaStreamSynchronize(n->stream));
+    std::vector<uint2> e(n->S);
+    SPK_CUDA(cudaMemcpy(e.data(), n->hd.entries, sizeof(uint2) * n->S, cudaMemcpyDeviceToHost));
+    for (int64_t s = 0; s < n->S; ++s) {
+      n->weights[s] = w[s];
+      const float v = n->cls_of[s] ? w[s] : w[s] * n->scales[s];
+      e[n->entry_of[s]].y = f2u(v);
+    }
+    SPK_CUDA(cudaMemcpy(n->hd.entries, e.data(), sizeof(uint2) * n->S, cudaMemcpyHostToDevice));
+    return SPK_OK;
+  });
+}
+
+int spk_net_synaptic_events(spk_net* n, uint64_t* events) {
+  if (!n || !events) return SPK_ERR_INVALID;
+  SPK_CUDA(cudaStreamSynchronize(n->stream));
+  RunCtl c;
+  SPK_CUDA(cudaMemcpy(&c, n->hd.ctl, sizeof(c), cudaMemcpyDeviceToHost));
+  *events = c.events;
+  return SPK_OK;
+}
+
+int spk_net_get_schedule(const spk_net* n, spk_schedule* out) {
+  if (!n || !out) return SPK_ERR_INVALID;
+  out->warps_per_cta = n->plan.W;
+  out->tile_posts = n->plan.TS;
+  out->ctas = n->plan.nctas;
+  out->steps_per_launch = n->plan.K;
+  return SPK_OK;
+}
+
+int spk_net_device_bytes(const spk_net* n, int64_t* bytes) {
+  if (!n || !bytes) return SPK_ERR_INVALID;
+  *bytes = (int64_t)n->arena_bytes;
+  return SPK_OK;
+}
+
+int spk_net_launch_count(const spk_net* n, int64_t* launches) {
+  if (!n || !launches) return SPK_ERR_INVALID;
+  *launches = n->launches;
+  return SPK_OK;
+}
+
+int spk_memory_info(uint64_t* free_bytes, uint64_t* total_bytes) {
+  size_t f = 0, t = 0;
+  SPK_CUDA(cudaMemGetInfo(&f, &t));
+  if (free_bytes) *free_bytes = f;
+  if (total_bytes) *total_bytes = t;
+  return SPK_OK;
+}
+
+// ---- batch -------------------------------------------------------------------------
+int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* schedule, spk_batch** out) {
+  if (!nets || n_nets < 1 || !out) return SPK_ERR_INVALID;
+  return guarded([&]() -> int {
+    DeviceInfo di;
+    int rc = device_info(&di);
+    if (rc) return rc;
+    auto* b = new spk_batch();
+    b->W = nets[0]->plan.W;
+    b->K = (schedule && schedule->steps_per_launch > 0) ? schedule->steps_per_launch : nets[0]->plan.K;
+    for (int i = 0; i < n_nets; ++i) {
+      spk_net* n = nets[i];
+      if (!n || n->plan.W != b->W) {
+        set_error("all networks of a batch need the same warps_per_cta (net %d)", i);
+        delete b;
+        return SPK_ERR_INVALID;
+      }
+      b->nets.push_back(n);
+      b->smem = std::max(b->smem, n->plan.smem);
+      b->total_ctas += n->plan.nctas;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_kernel<U_ENTRIES>, b->W * 32, b->smem) !=
+            cudaSuccess ||
+        per_sm < 1) {
+      set_error("batch: no CTA of %d threads with %d B shared memory fits", b->W * 32, b->smem);
+      delete b;
+      return SPK_ERR_UNSUPPORTED;
+    }
+    const int capacity = per_sm * di.sms;
+    // waves: consecutive networks whose CTAs fit co-resident
+    std::vector<CtaMap> map;
+    std::vector<NetDev> hds;
+    int wave_start = 0, wave_ctas = 0;
+    bool any_multi = false;
+    for (int i = 0; i < n_nets; ++i) {
+      spk_net* n = nets[i];
+      if (n->plan.nctas > capacity) {
+        set_error("network %d needs %d co-resident CTAs, device holds %d", i, n->plan.nctas, capacity);
+        delete b;
+        return SPK_ERR_UNSUPPORTED;
+      }
+      if (wave_ctas + n->plan.nctas > capacity) {
+        b->waves.push_back({wave_start, wave_ctas});
+        wave_start += wave_ctas;
+        wave_ctas = 0;
+      }
+      NetDev h = n->hd;
+      hds.push_back(h);
+      for (int r = 0; r < n->plan.nctas; ++r) map.push_back(CtaMap{i, r});
+      wave_ctas += n->plan.nctas;
+      any_multi |= n->plan.nctas > 1;
+    }
+    b->waves.push_back({wave_start, wave_ctas});
+    b->cooperative = any_multi;
+    const size_t bytes = align_up(sizeof(NetDev) * n_nets, 256) + align_up(sizeof(CtaMap) * map.size(), 256) +
+                         align_up(sizeof(unsigned) * n_nets, 256) + 256;
+    void* mem = nullptr;
+    if (cudaMalloc(&mem, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("batch: device allocation failed");
+      delete b;
+      return SPK_ERR_OOM;
+    }
+    b->dd = (NetDev*)mem;
+    b->dmap = (CtaMap*)((char*)mem + align_up(sizeof(NetDev) * n_nets, 256));
+    b->barrier_pool = (unsigned*)((char*)b->dmap + align_up(sizeof(CtaMap) * map.size(), 256));
+    b->abort_dev = (int*)((char*)b->barrier_pool + align_up(sizeof(unsigned) * n_nets, 256));
+    for (int i = 0; i < n_nets; ++i) {
+      hds[i].barrier = b->barrier_pool + i;
+      hds[i].abort_flag = b->abort_dev;
+    }
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMemcpy(b->dd, hds.data(), sizeof(NetDev) * n_nets, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b->dmap, map.data(), sizeof(CtaMap) * map.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(b->abort_dev, 0, sizeof(int)) != cudaSuccess) {
+      set_error("batch: setup failed: %s", cudaGetErrorString(cudaGetLastError()));
+      if (b->stream) cudaStreamDestroy(b->stream);
+      cudaFree(mem);
+      delete b;
+      return SPK_ERR_CUDA;
+    }
+    *out = b;
+    return SPK_OK;
+  });
+}
+
+int spk_batch_run_steps(spk_batch* b, int64_t n_steps, int32_t plasticity_on) {
+  if (!b || n_steps < 0 || n_steps > 0x7fffffff) return SPK_ERR_INVALID;
+  if (n_steps == 0) return SPK_OK;
+  // order the batch stream after each network's pending work
+  for (spk_net* n : b->nets) {
+    SPK_CUDA(cudaStreamSynchronize(n->stream));
+    set_ctl_kernel<<<1, 1, 0, b->stream>>>(n->hd.ctl, n->current_time, (int)n_steps,
+                                           (plasticity_on && n->has_stdp) ? 1 : 0, n->record_inputs ? 1 : 0);
+    SPK_CUDA(cudaGetLastError());
+  }
+  const int64_t blocks = (n_steps + b->K - 1) / b->K;
+  for (int64_t blk = 0; blk < blocks; ++blk) {
+    SPK_CUDA(cudaMemsetAsync(b->barrier_pool, 0, sizeof(unsigned) * b->nets.size(), b->stream));
+    for (const auto& wv : b->waves) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(wv.second);
+      cfg.blockDim = dim3(b->W * 32);
+      cfg.dynamicSmemBytes = b->smem;
+      cfg.stream = b->stream;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeCooperative;
+      attr[0].val.cooperative = b->cooperative ? 1 : 0;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      SPK_CUDA(cudaLaunchKernelEx(&cfg, step_kernel<U_ENTRIES>, (const NetDev*)b->dd,
+                                  (const CtaMap*)(b->dmap + wv.first), b->K));
+      ++b->launches;
+    }
+  }
+  for (spk_net* n : b->nets) n->current_time = n->current_time + (float)n_steps * n->dt;
+  return SPK_OK;
+}
+
+int spk_batch_synchronize(spk_batch* b) {
+  if (!b) return SPK_ERR_INVALID;
+  SPK_CUDA(cudaStreamSynchronize(b->stream));
+  int worst = SPK_OK;
+  for (spk_net* n : b->nets) {
+    int st = 0;
+    SPK_CUDA(cudaMemcpy(&st, &n->hd.ctl->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st == SPK_ERR_TIMEOUT) worst = st;
+    else if (st && worst == SPK_OK) worst = st;
+  }
+  return worst;
+}
+
+int spk_batch_launch_count(const spk_batch* b, int64_t* launches) {
+  if (!b || !launches) return SPK_ERR_INVALID;
+  *launches = b->launches;
+  return SPK_OK;
+}
+
+int spk_batch_destroy(spk_batch* b) {
+  if (!b) return SPK_ERR_INVALID;
+  if (b->stream) {
+    cudaStreamSynchronize(b->stream);
+    cudaStreamDestroy(b->stream);
+  }
+  cudaFree(b->dd);
+  delete b;
+  return SPK_OK;
+}
+
+}  // extern "C"

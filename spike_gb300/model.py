@@ -1,0 +1,387 @@
+"""Python mirror of the reference's model-building API over the C front end.
+
+``Model`` follows ``SpikingModel`` (Spike/Models/SpikingModel.hpp:24-67): add
+neuron / input / synapse groups with the reference's parameter fields, add a
+weight-dependent STDP rule, ``finalise()``, ``run(seconds, plasticity_on)``,
+``reset_state()`` / ``reset_time()``.  Connectivity is built by the C++ front
+end with the reference's rand() sequence.  ``Net`` wraps a network created
+directly from a flat descriptor; ``Batch`` advances many networks in one
+persistent launch.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+from ._native import check, lib
+
+
+@dataclass
+class LIFParams:
+    """lif_spiking_neuron_parameters_struct (Spike/Neurons/LIFSpikingNeurons.hpp:7-14)."""
+    n: int
+    resting_potential_v0: float = -0.074
+    after_spike_reset_potential_vreset: float = -0.074
+    threshold_for_action_potential_spike: float = 0.03
+    absolute_refractory_period: float = 0.002
+    somatic_capacitance_Cm: float = 0.0
+    somatic_leakage_conductance_g0: float = 0.0
+    background_current: float = 0.0
+    v_init_lo: float = 0.0
+    v_init_hi: float = 0.0
+
+
+@dataclass
+class SynapseParams:
+    """synapse_parameters_struct and its spiking/conductance/current extensions."""
+    connectivity_type: int = N.SPK_CONN_ALL_TO_ALL
+    weight_range: tuple = (0.0, 0.0)
+    weight_scaling_constant: float = 1.0
+    random_connectivity_probability: float = 0.0
+    delay_range: tuple = (0.0, 0.0)
+    reversal_potential_Vhat: float = 0.0
+    decay_term_tau_g: float = 0.001
+    decay_term_tau: float = 0.001
+    max_number_of_connections_per_pair: int = 1
+    gaussian_synapses_per_postsynaptic_neuron: int = 10
+    gaussian_synapses_standard_deviation: float = 10.0
+    pairwise_pre: list | None = None
+    pairwise_post: list | None = None
+    pairwise_weight: list | None = None
+    pairwise_delay: list | None = None
+    plasticity_rule: int = -1
+    _keep: list = field(default_factory=list, repr=False)
+
+    def to_c(self) -> N.SynapseParams:
+        s = N.SynapseParams()
+        s.connectivity_type = self.connectivity_type
+        s.weight_range[0], s.weight_range[1] = self.weight_range
+        s.weight_scaling_constant = self.weight_scaling_constant
+        s.random_connectivity_probability = self.random_connectivity_probability
+        s.delay_range[0], s.delay_range[1] = self.delay_range
+        s.reversal_potential_Vhat = self.reversal_potential_Vhat
+        s.decay_term_tau_g = self.decay_term_tau_g
+        s.decay_term_tau = self.decay_term_tau
+        s.max_number_of_connections_per_pair = self.max_number_of_connections_per_pair
+        s.gaussian_synapses_per_postsynaptic_neuron = self.gaussian_synapses_per_postsynaptic_neuron
+        s.gaussian_synapses_standard_deviation = self.gaussian_synapses_standard_deviation
+        s.plasticity_rule = self.plasticity_rule
+        s.n_pairwise = 0
+        self._keep.clear()
+        if self.pairwise_pre is not None:
+            pre = np.ascontiguousarray(self.pairwise_pre, dtype=np.int32)
+            post = np.ascontiguousarray(self.pairwise_post, dtype=np.int32)
+            self._keep += [pre, post]
+            s.n_pairwise = len(pre)
+            s.pairwise_connect_presynaptic = pre.ctypes.data_as(C.POINTER(C.c_int32))
+            s.pairwise_connect_postsynaptic = post.ctypes.data_as(C.POINTER(C.c_int32))
+            if self.pairwise_weight is not None:
+                w = np.ascontiguousarray(self.pairwise_weight, dtype=np.float32)
+                self._keep.append(w)
+                s.pairwise_connect_weight = w.ctypes.data_as(C.POINTER(C.c_float))
+            if self.pairwise_delay is not None:
+                d = np.ascontiguousarray(self.pairwise_delay, dtype=np.float32)
+                self._keep.append(d)
+                s.pairwise_connect_delay = d.ctypes.data_as(C.POINTER(C.c_float))
+        return s
+
+
+@dataclass
+class STDPParams:
+    """weightdependent_stdp_plasticity_parameters_struct
+    (Spike/Plasticity/WeightDependentSTDPPlasticity.hpp:28-40)."""
+    a_minus: float = 1.0
+    a_plus: float = 1.0
+    tau_minus: float = 0.02
+    tau_plus: float = 0.02
+    lambda_: float = 1.0
+    alpha: float = 1.0
+    w_max: float = 1.0
+    clip_upper: bool = False
+
+    def to_c(self) -> N.StdpParams:
+        return N.StdpParams(self.a_minus, self.a_plus, self.tau_minus, self.tau_plus, self.lambda_,
+                            self.alpha, self.w_max, 1 if self.clip_upper else 0)
+
+
+def schedule(warps_per_cta=0, tile_posts=0, ctas=0, steps_per_launch=0) -> N.Schedule:
+    return N.Schedule(warps_per_cta, tile_posts, ctas, steps_per_launch)
+
+
+def _i32(x):
+    return C.c_int32(x)
+
+
+class Net:
+    """A network handle of the engine (spk_net_*).  ``owned=False`` borrows a
+    handle that belongs to a Model."""
+
+    def __init__(self, handle: C.c_void_p, owned: bool = True):
+        self.h = handle
+        self.owned = owned
+
+    @classmethod
+    def from_desc(cls, desc: N.NetDesc, sched: N.Schedule | None = None) -> "Net":
+        h = C.c_void_p()
+        check(lib().spk_net_create(C.byref(desc), C.byref(sched) if sched else None, C.byref(h)),
+              "spk_net_create")
+        return cls(h)
+
+    def close(self):
+        if self.h and self.owned:
+            lib().spk_net_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- run control
+    def run(self, seconds: float, plasticity_on: bool = True) -> None:
+        check(lib().spk_net_run(self.h, C.c_float(seconds), 1 if plasticity_on else 0), "spk_net_run")
+
+    def run_steps(self, steps: int, plasticity_on: bool = True) -> None:
+        check(lib().spk_net_run_steps(self.h, steps, 1 if plasticity_on else 0), "spk_net_run_steps")
+
+    def synchronize(self) -> int:
+        return lib().spk_net_synchronize(self.h)
+
+    def reset_state(self):
+        check(lib().spk_net_reset_state(self.h), "spk_net_reset_state")
+
+    def reset_time(self):
+        check(lib().spk_net_reset_time(self.h), "spk_net_reset_time")
+
+    def select_stimulus(self, s: int):
+        check(lib().spk_net_select_stimulus(self.h, s), "spk_net_select_stimulus")
+
+    def current_time(self) -> float:
+        t = C.c_float()
+        check(lib().spk_net_current_time(self.h, C.byref(t)), "spk_net_current_time")
+        return t.value
+
+    # ---- readback
+    def spikes(self, population: int = N.SPK_POP_NEURONS):
+        n = C.c_int64()
+        check(lib().spk_net_spike_count(self.h, population, C.byref(n)), "spk_net_spike_count")
+        ids = np.empty(n.value, dtype=np.int32)
+        times = np.empty(n.value, dtype=np.float32)
+        got = C.c_int64()
+        check(lib().spk_net_read_spikes(self.h, population, ids.ctypes.data_as(C.POINTER(C.c_int32)),
+                                        times.ctypes.data_as(C.POINTER(C.c_float)), n.value, C.byref(got)),
+              "spk_net_read_spikes")
+        return ids[:got.value], times[:got.value]
+
+    def clear_spikes(self):
+        check(lib().spk_net_clear_spikes(self.h), "spk_net_clear_spikes")
+
+    def state(self, field: int, count: int) -> np.ndarray:
+        out = np.empty(count, dtype=np.float32)
+        check(lib().spk_net_read_state(self.h, field, out.ctypes.data_as(C.c_void_p), count), "spk_net_read_state")
+        return out
+
+    def weights(self, n: int) -> np.ndarray:
+        out = np.empty(n, dtype=np.float32)
+        check(lib().spk_net_read_weights(self.h, out.ctypes.data_as(C.POINTER(C.c_float)), n),
+              "spk_net_read_weights")
+        return out
+
+    def write_weights(self, w: np.ndarray):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        check(lib().spk_net_write_weights(self.h, w.ctypes.data_as(C.POINTER(C.c_float)), len(w)),
+              "spk_net_write_weights")
+
+    def events(self) -> int:
+        e = C.c_uint64()
+        check(lib().spk_net_synaptic_events(self.h, C.byref(e)), "spk_net_synaptic_events")
+        return e.value
+
+    def schedule(self) -> dict:
+        s = N.Schedule()
+        check(lib().spk_net_get_schedule(self.h, C.byref(s)), "spk_net_get_schedule")
+        return dict(warps_per_cta=s.warps_per_cta, tile_posts=s.tile_posts, ctas=s.ctas,
+                    steps_per_launch=s.steps_per_launch)
+
+    def device_bytes(self) -> int:
+        b = C.c_int64()
+        check(lib().spk_net_device_bytes(self.h, C.byref(b)), "spk_net_device_bytes")
+        return b.value
+
+    def launches(self) -> int:
+        b = C.c_int64()
+        check(lib().spk_net_launch_count(self.h, C.byref(b)), "spk_net_launch_count")
+        return b.value
+
+
+class Batch:
+    """Many networks advanced together by one persistent launch per step block."""
+
+    def __init__(self, nets: list[Net], sched: N.Schedule | None = None):
+        arr = (C.c_void_p * len(nets))(*[n.h for n in nets])
+        self.nets = nets
+        self.h = C.c_void_p()
+        check(lib().spk_batch_create(arr, len(nets), C.byref(sched) if sched else None, C.byref(self.h)),
+              "spk_batch_create")
+
+    def run_steps(self, steps: int, plasticity_on: bool = True):
+        check(lib().spk_batch_run_steps(self.h, steps, 1 if plasticity_on else 0), "spk_batch_run_steps")
+
+    def synchronize(self) -> int:
+        return lib().spk_batch_synchronize(self.h)
+
+    def launches(self) -> int:
+        b = C.c_int64()
+        check(lib().spk_batch_launch_count(self.h, C.byref(b)), "spk_batch_launch_count")
+        return b.value
+
+    def close(self):
+        if self.h:
+            lib().spk_batch_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Model:
+    """SpikingModel over the C front end (spike_gb300_model.h)."""
+
+    def __init__(self, synapse_kind: int = N.SPK_SYN_CONDUCTANCE, input_kind: int = N.SPK_INPUT_NONE,
+                 synapse_seed: int = -1, timestep: float = 0.0001, philox_seed: int = 1):
+        self.h = C.c_void_p()
+        check(lib().spk_model_create(synapse_kind, input_kind, synapse_seed, C.byref(self.h)), "spk_model_create")
+        check(lib().spk_model_set_timestep(self.h, C.c_float(timestep)), "spk_model_set_timestep")
+        check(lib().spk_model_set_seed(self.h, philox_seed), "spk_model_set_seed")
+        self.synapse_kind = synapse_kind
+        self.timestep = timestep
+        self._net = None
+
+    def close(self):
+        if self.h:
+            lib().spk_model_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_neuron_group(self, p: LIFParams) -> int:
+        c = N.LifParams()
+        c.group_shape[0], c.group_shape[1] = 1, p.n
+        for f in ("resting_potential_v0", "after_spike_reset_potential_vreset",
+                  "threshold_for_action_potential_spike", "absolute_refractory_period",
+                  "somatic_capacitance_Cm", "somatic_leakage_conductance_g0", "background_current",
+                  "v_init_lo", "v_init_hi"):
+            setattr(c, f, getattr(p, f))
+        gid = C.c_int32()
+        check(lib().spk_model_add_neuron_group(self.h, C.byref(c), C.byref(gid)), "spk_model_add_neuron_group")
+        return gid.value
+
+    def add_input_group(self, n: int, rate: float, shape0: int = 1) -> int:
+        gid = C.c_int32()
+        check(lib().spk_model_add_input_group(self.h, shape0, n // shape0, C.c_float(rate), C.byref(gid)),
+              "spk_model_add_input_group")
+        return gid.value
+
+    def add_stimulus(self, rates) -> int:
+        r = np.ascontiguousarray(rates, dtype=np.float32)
+        sid = C.c_int32()
+        check(lib().spk_model_add_stimulus(self.h, r.ctypes.data_as(C.POINTER(C.c_float)), len(r), C.byref(sid)),
+              "spk_model_add_stimulus")
+        return sid.value
+
+    def add_stdp_rule(self, p: STDPParams) -> int:
+        c = p.to_c()
+        rid = C.c_int32()
+        check(lib().spk_model_add_stdp_rule(self.h, C.byref(c), C.byref(rid)), "spk_model_add_stdp_rule")
+        return rid.value
+
+    def add_synapse_group(self, pre: int, post: int, p: SynapseParams) -> int:
+        c = p.to_c()
+        gid = C.c_int32()
+        check(lib().spk_model_add_synapse_group(self.h, pre, post, C.byref(c), C.byref(gid)),
+              "spk_model_add_synapse_group")
+        return gid.value
+
+    def connect_with_sparsity(self, pre: int, post: int, sparseness: float, p: SynapseParams) -> int:
+        c = p.to_c()
+        gid = C.c_int32()
+        check(lib().spk_model_connect_with_sparsity(self.h, pre, post, C.c_float(sparseness), C.byref(c),
+                                                    C.byref(gid)), "spk_model_connect_with_sparsity")
+        return gid.value
+
+    def set_recording(self, record_inputs: bool = False, spike_capacity: int = 0):
+        check(lib().spk_model_set_recording(self.h, 1 if record_inputs else 0, spike_capacity),
+              "spk_model_set_recording")
+
+    def counts(self):
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int64()
+        check(lib().spk_model_counts(self.h, C.byref(a), C.byref(b), C.byref(c)), "spk_model_counts")
+        return a.value, b.value, c.value
+
+    def desc(self) -> N.NetDesc:
+        d = N.NetDesc()
+        check(lib().spk_model_desc(self.h, C.byref(d)), "spk_model_desc")
+        return d
+
+    def finalise(self, sched: N.Schedule | None = None) -> Net:
+        check(lib().spk_model_finalise(self.h, C.byref(sched) if sched else None), "spk_model_finalise")
+        h = C.c_void_p()
+        check(lib().spk_model_net(self.h, C.byref(h)), "spk_model_net")
+        self._net = Net(h, owned=False)
+        return self._net
+
+    @property
+    def net(self) -> Net:
+        if self._net is None:
+            self.finalise()
+        return self._net
+
+    def run(self, seconds: float, plasticity_on: bool = True) -> int:
+        return check(lib().spk_model_run(self.h, C.c_float(seconds), 1 if plasticity_on else 0), "spk_model_run")
+
+    def reset_state(self):
+        check(lib().spk_model_reset_state(self.h), "spk_model_reset_state")
+
+    def reset_time(self):
+        check(lib().spk_model_reset_time(self.h), "spk_model_reset_time")
+
+    def select_stimulus(self, s: int):
+        check(lib().spk_model_select_stimulus(self.h, s), "spk_model_select_stimulus")
+
+    def spikes(self, population: int = N.SPK_POP_NEURONS):
+        ids = C.POINTER(C.c_int32)()
+        times = C.POINTER(C.c_float)()
+        n = C.c_int64()
+        check(lib().spk_model_spikes(self.h, population, C.byref(ids), C.byref(times), C.byref(n)),
+              "spk_model_spikes")
+        if n.value == 0:
+            return np.zeros(0, np.int32), np.zeros(0, np.float32)
+        return (np.ctypeslib.as_array(ids, (n.value,)).copy(), np.ctypeslib.as_array(times, (n.value,)).copy())
+
+    def clear_spikes(self):
+        check(lib().spk_model_clear_spikes(self.h), "spk_model_clear_spikes")
+
+
+def desc_arrays(d: N.NetDesc) -> dict:
+    """Copy the synapse arrays of a descriptor into numpy (creation order)."""
+    S = d.n_synapses
+
+    def arr(ptr, dt):
+        if not ptr or S == 0:
+            return np.zeros(S, dt)
+        return np.ctypeslib.as_array(ptr, (S,)).astype(dt, copy=True)
+
+    return dict(pre=arr(d.pre, np.int32), post=arr(d.post, np.int32), weight=arr(d.weight, np.float32),
+                scale=arr(d.scale, np.float32), delay=arr(d.delay, np.int32), label=arr(d.label, np.int32),
+                plastic=arr(d.plastic, np.uint8))

@@ -1,0 +1,113 @@
+"""The benchmark networks, built through the model API exactly as the
+reference examples build them.
+
+* ``vogels_abbott`` - Examples/VogelsAbbottNet.cpp (conductance LIF, E/I 4:1,
+  random 2 % connectivity, delay 1 step), plus the initial-V extension.
+* ``brunel`` - Examples/Brunel10K.cpp structure (voltage-jump LIF, Poisson
+  drive, fixed in-degree via connect_with_sparsity, Examples/UtilityFunctions.hpp:51-82),
+  with integer delays U{1..d_max} steps and optional weight-dependent STDP on
+  E->E.
+* ``plastic_ff`` - a large feed-forward + recurrent plastic network: patterned
+  Poisson inputs with log-normal rates, fixed in-degree, weights U[0,1].
+
+All sizes are parameters so the same builders give the parity-test networks.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _native as N
+from .model import LIFParams, Model, STDPParams, SynapseParams
+
+DT = 0.0001
+
+
+def vogels_abbott(n_exc: int = 3200, n_inh: int = 800, p: float = 0.02, delay_steps: int = 1,
+                  v_init: bool = True, philox_seed: int = 42, synapse_seed: int = -1) -> Model:
+    m = Model(N.SPK_SYN_CONDUCTANCE, N.SPK_INPUT_NONE, synapse_seed=synapse_seed, timestep=DT,
+              philox_seed=philox_seed)
+    common = dict(somatic_capacitance_Cm=200.0e-12, somatic_leakage_conductance_g0=10.0e-9,
+                  resting_potential_v0=-60.0e-3, after_spike_reset_potential_vreset=-60.0e-3,
+                  absolute_refractory_period=5.0e-3, threshold_for_action_potential_spike=-50.0e-3,
+                  background_current=2.0e-2)
+    if v_init:
+        common.update(v_init_lo=-60.0e-3, v_init_hi=-50.0e-3)
+    e = m.add_neuron_group(LIFParams(n_exc, **common))
+    i = m.add_neuron_group(LIFParams(n_inh, **common))
+    exc = SynapseParams(connectivity_type=N.SPK_CONN_RANDOM, weight_range=(0.4, 0.4),
+                        weight_scaling_constant=10.0e-9, random_connectivity_probability=p,
+                        delay_range=(delay_steps * DT, delay_steps * DT), reversal_potential_Vhat=0.0,
+                        decay_term_tau_g=5.0e-3)
+    inh = SynapseParams(connectivity_type=N.SPK_CONN_RANDOM, weight_range=(5.1, 5.1),
+                        weight_scaling_constant=10.0e-9, random_connectivity_probability=p,
+                        delay_range=(delay_steps * DT, delay_steps * DT), reversal_potential_Vhat=-80.0e-3,
+                        decay_term_tau_g=10.0e-3)
+    m.add_synapse_group(e, e, exc)
+    m.add_synapse_group(e, i, exc)
+    m.add_synapse_group(i, e, inh)
+    m.add_synapse_group(i, i, inh)
+    return m
+
+
+def brunel(n_exc: int = 10000, n_inh: int = 2500, n_in: int = 10000, rate: float = 20.0,
+           sparseness: float = 0.1, g: float = 5.0, J: float = 0.1e-3, d_max: int = 20,
+           plastic: bool = False, stdp: STDPParams | None = None, philox_seed: int = 42,
+           synapse_seed: int = 42) -> Model:
+    m = Model(N.SPK_SYN_VOLTAGE, N.SPK_INPUT_POISSON, synapse_seed=synapse_seed, timestep=DT,
+              philox_seed=philox_seed)
+    rule = -1
+    if plastic:
+        rule = m.add_stdp_rule(stdp or STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02,
+                                                  tau_minus=0.02, lambda_=1.0, alpha=1.0, w_max=1.0))
+    common = dict(somatic_capacitance_Cm=200.0e-12, somatic_leakage_conductance_g0=10.0e-9,
+                  resting_potential_v0=0.0, after_spike_reset_potential_vreset=0.0,
+                  absolute_refractory_period=2.0e-3, threshold_for_action_potential_spike=20.0e-3,
+                  background_current=0.0)
+    inp = m.add_input_group(n_in, rate)
+    e = m.add_neuron_group(LIFParams(n_exc, **common))
+    i = m.add_neuron_group(LIFParams(n_inh, **common))
+    delays = (1 * DT, d_max * DT)
+    exc = SynapseParams(weight_range=(J, J), weight_scaling_constant=1.0, delay_range=delays)
+    inh = SynapseParams(weight_range=(-g * J, -g * J), weight_scaling_constant=1.0, delay_range=delays)
+    ext = SynapseParams(weight_range=(J, J), weight_scaling_constant=1.0, delay_range=delays)
+    m.connect_with_sparsity(inp, e, sparseness, ext)
+    m.connect_with_sparsity(inp, i, sparseness, ext)
+    m.connect_with_sparsity(e, i, sparseness, exc)
+    exc_plastic = SynapseParams(weight_range=(J, J), weight_scaling_constant=1.0, delay_range=delays,
+                                plasticity_rule=rule)
+    m.connect_with_sparsity(e, e, sparseness, exc_plastic)
+    m.connect_with_sparsity(i, e, sparseness, inh)
+    m.connect_with_sparsity(i, i, sparseness, inh)
+    return m
+
+
+def lognormal_rates(n: int, median: float = 5.0, sigma: float = 1.0, hi: float = 100.0,
+                    seed: int = 42) -> np.ndarray:
+    """Per-input rates exp(ln median + sigma z), clipped to [0, hi] Hz."""
+    rng = np.random.default_rng(seed)
+    z = rng.standard_normal(n)
+    return np.clip(np.exp(np.log(median) + sigma * z), 0.0, hi).astype(np.float32)
+
+
+def plastic_ff(n_in: int = 50000, n_neurons: int = 200000, ff: int = 900, rec: int = 100,
+               d_max: int = 10, w_scale: float = 2.0e-4, sigma: float = 1.0, plastic: bool = True,
+               philox_seed: int = 42, synapse_seed: int = 42) -> Model:
+    m = Model(N.SPK_SYN_VOLTAGE, N.SPK_INPUT_PATTERNED, synapse_seed=synapse_seed, timestep=DT,
+              philox_seed=philox_seed)
+    rule = -1
+    if plastic:
+        rule = m.add_stdp_rule(STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02,
+                                          lambda_=1.0, alpha=1.0, w_max=1.0, clip_upper=True))
+    inp = m.add_input_group(n_in, 0.0)
+    m.add_stimulus(lognormal_rates(n_in, sigma=sigma, seed=philox_seed))
+    common = dict(somatic_capacitance_Cm=200.0e-12, somatic_leakage_conductance_g0=10.0e-9,
+                  resting_potential_v0=0.0, after_spike_reset_potential_vreset=0.0,
+                  absolute_refractory_period=2.0e-3, threshold_for_action_potential_spike=20.0e-3)
+    pop = m.add_neuron_group(LIFParams(n_neurons, **common))
+    delays = (1 * DT, d_max * DT)
+    ffp = SynapseParams(weight_range=(0.0, 1.0), weight_scaling_constant=w_scale, delay_range=delays,
+                        plasticity_rule=rule)
+    recp = SynapseParams(weight_range=(-1.0, 0.0), weight_scaling_constant=w_scale, delay_range=delays)
+    m.connect_with_sparsity(inp, pop, ff / n_in, ffp)
+    m.connect_with_sparsity(pop, pop, rec / n_neurons, recp)
+    return m

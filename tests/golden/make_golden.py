@@ -1,0 +1,105 @@
+"""Generate the connectivity golden fixtures from the REFERENCE front end.
+
+Runs oracle/_ref/ref_dump (the reference's own Spike front end and Dummy
+backend compiled from the reference sources by oracle/build_ref.sh) on the
+cases defined in oracle/ref_dump.cpp and stores what it produced:
+
+* small cases (va_mix, brunel, shapes): every array, as .npz;
+* the full VogelsAbbottNet network (va, 320,261 synapses): counts and SHA-256
+  digests of every array, as .json.
+
+Usage (in a checkout where the reference sources are present):
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+
+def read_dump(path: str) -> dict:
+    out = {}
+    with open(path, "rb") as f:
+        data = f.read()
+    o = 0
+    while o < len(data):
+        (nl,) = struct.unpack_from("<i", data, o)
+        o += 4
+        name = data[o:o + nl].decode()
+        o += nl
+        typ = chr(data[o])
+        o += 1
+        (cnt,) = struct.unpack_from("<q", data, o)
+        o += 8
+        dt = np.int32 if typ == "i" else np.float32
+        arr = np.frombuffer(data, dtype=dt, count=cnt, offset=o).copy()
+        o += 4 * cnt
+        out[name] = arr
+    return out
+
+
+def creation_order(d: dict) -> dict:
+    """Arrays in creation order: sorted_x[reversesort[i]] (the reference's
+    readback mapping, Spike/Synapses/Synapses.cpp:525-584)."""
+    rs = d["reversesort"]
+    out = {}
+    for k in ("pre", "post", "weight", "scale", "delay", "label"):
+        out[k] = d["sorted_" + k][rs]
+    return out
+
+
+def digest(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def run_case(ref_dump: str, case: str) -> dict:
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, case + ".bin")
+        subprocess.run([ref_dump, case, out], check=True, capture_output=True)
+        return read_dump(out)
+
+
+def main() -> int:
+    sys.path.insert(0, ROOT)
+    from spike_gb300 import _build
+    ref_dump = _build.build_reference_frontend()
+    if not ref_dump:
+        print("reference sources not available; fixtures unchanged")
+        return 1
+    for case in ("va_mix", "brunel", "shapes"):
+        d = run_case(ref_dump, case)
+        c = creation_order(d)
+        arrays = {**{"sorted_" + k: d["sorted_" + k] for k in ("pre", "post", "weight", "scale", "delay", "label")},
+                  **{"created_" + k: v for k, v in c.items()},
+                  **{k: v for k, v in d.items() if not k.startswith("sorted_")}}
+        np.savez_compressed(os.path.join(HERE, f"ref_{case}.npz"), **arrays)
+        print(case, int(d["n_synapses"][0]), "synapses")
+    d = run_case(ref_dump, "va")
+    c = creation_order(d)
+    meta = {k: int(d[k][0]) for k in ("n_synapses", "n_neurons", "n_inputs", "min_delay", "max_delay",
+                                      "num_syn_labels", "timestep_grouping")}
+    meta["digests_created"] = {k: digest(v) for k, v in c.items()}
+    meta["digests_sorted"] = {k: digest(d["sorted_" + k]) for k in ("pre", "post", "weight", "delay", "label")}
+    meta["eff_count_digest"] = digest(d["eff_count"])
+    meta["tau_m"] = float(d["tau_m"][0])
+    meta["R"] = float(d["R"][0])
+    meta["vhat"] = [float(x) for x in d["vhat"]]
+    meta["tau_g"] = [float(x) for x in d["tau_g"]]
+    with open(os.path.join(HERE, "ref_va.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+    print("va", meta["n_synapses"], "synapses")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
