@@ -170,6 +170,12 @@ int spk_net_reset_time(spk_net* net);
 /* InputSpikingNeurons::select_stimulus + reset of the inputs
  * (Spike/Neurons/PoissonInputSpikingNeurons.cpp:48-51). */
 int spk_net_select_stimulus(spk_net* net, int32_t stimulus);
+/* PatternedPoissonInputSpikingNeurons::copy_rates_to_device
+ * (Spike/Backend/CUDA/Neurons/PatternedPoissonInputSpikingNeurons.cu:13-18):
+ * overwrite the rates of one stimulus (n_inputs floats, Hz) with an
+ * asynchronous host-to-device copy on the handle's stream (pinned host memory
+ * makes it truly asynchronous).  Input state is not reset. */
+int spk_net_write_rates(spk_net* net, int32_t stimulus, const float* rates, int64_t n);
 /* SpikingModel::run(seconds, plasticity_on) (Spike/Models/SpikingModel.cpp:214-236):
  * ceilf(seconds/dt) steps, t_s = start + s*dt in float, then time = start + seconds.
  * Asynchronous: returns after enqueueing; device errors surface at the next
@@ -202,6 +208,9 @@ int spk_net_get_schedule(const spk_net* net, spk_schedule* out);
 int spk_net_device_bytes(const spk_net* net, int64_t* bytes);
 /* Kernel launches issued so far by this handle. */
 int spk_net_launch_count(const spk_net* net, int64_t* launches);
+/* The handle's CUDA stream (a cudaStream_t), for callers that order their own
+ * work or timing events against the engine. */
+int spk_net_stream(const spk_net* net, void** stream);
 
 /* ---- batch: many independent networks in one persistent launch ---------- */
 int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* schedule,
@@ -209,6 +218,7 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
 int spk_batch_run_steps(spk_batch* batch, int64_t n_steps, int32_t plasticity_on);
 int spk_batch_synchronize(spk_batch* batch);
 int spk_batch_launch_count(const spk_batch* batch, int64_t* launches);
+int spk_batch_stream(const spk_batch* batch, void** stream);
 int spk_batch_destroy(spk_batch* batch);
 
 /* ---- misc ---------------------------------------------------------------- */

@@ -43,6 +43,12 @@ def oracle_lib() -> C.CDLL:
             fn = getattr(L, name)
             fn.restype = C.c_int
             fn.argtypes = args
+        L.oracle_philox4x32_10.restype = None
+        L.oracle_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.oracle_logf.restype = C.c_float
+        L.oracle_logf.argtypes = [C.c_float]
+        L.oracle_log_max_ulp.restype = C.c_double
+        L.oracle_log_max_ulp.argtypes = []
         _lib = L
     return _lib
 
@@ -137,3 +143,11 @@ class OracleNet:
                                                 delay.ctypes.data_as(C.POINTER(C.c_int32)), S),
             "oracle_sorted_synapses")
         return pre, post, delay
+
+
+def philox4x32_10(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    oracle_lib().oracle_philox4x32_10(c, k, o)
+    return list(o)

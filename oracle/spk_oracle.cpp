@@ -819,4 +819,28 @@ int oracle_sorted_synapses(const oracle_net* n, int32_t* pre, int32_t* post, int
   });
 }
 
+void oracle_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  spk::u32x4 c{ctr[0], ctr[1], ctr[2], ctr[3]};
+  spk::u32x4 r = spk::philox4x32_10(c, key[0], key[1]);
+  out[0] = r.x;
+  out[1] = r.y;
+  out[2] = r.z;
+  out[3] = r.w;
+}
+
+float oracle_logf(float x) { return spk::logf_spk(x); }
+
+double oracle_log_max_ulp(void) {
+  double worst = 0.0;
+  for (uint32_t k = 1; k < (1u << 24); ++k) {
+    const float u = spk::uniform_open0((k - 1u) << 8);
+    const double ex = std::log((double)u);
+    const double ulp = std::ldexp(1.0, std::ilogb((float)ex) - 23);
+    const double e = std::fabs((double)spk::logf_spk(u) - ex) / ulp;
+    if (e > worst) worst = e;
+  }
+  if (spk::logf_spk(1.0f) != 0.0f) worst = 1e30;
+  return worst;
+}
+
 }  // extern "C"

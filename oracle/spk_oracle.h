@@ -54,6 +54,13 @@ int oracle_synaptic_events(const oracle_net* net, uint64_t* events);
 int oracle_sorted_synapses(const oracle_net* net, int32_t* pre, int32_t* post, int32_t* delay,
                            int64_t n);
 
+/* The shared counter-based generator and logarithm, for known-answer tests. */
+void oracle_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+float oracle_logf(float x);
+/* Largest error of the shared logarithm, in units of the last place, over
+ * every uniform the Poisson draw can produce (k * 2^-24, k = 1..2^24). */
+double oracle_log_max_ulp(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -110,6 +110,7 @@ _SIGS = {
     "spk_net_reset_state": (i32, [_VP]),
     "spk_net_reset_time": (i32, [_VP]),
     "spk_net_select_stimulus": (i32, [_VP, i32]),
+    "spk_net_write_rates": (i32, [_VP, i32, _VP, i64]),
     "spk_net_run": (i32, [_VP, f32, i32]),
     "spk_net_run_steps": (i32, [_VP, i64, i32]),
     "spk_net_synchronize": (i32, [_VP]),
@@ -124,10 +125,12 @@ _SIGS = {
     "spk_net_get_schedule": (i32, [_VP, P(Schedule)]),
     "spk_net_device_bytes": (i32, [_VP, P(i64)]),
     "spk_net_launch_count": (i32, [_VP, P(i64)]),
+    "spk_net_stream": (i32, [_VP, P(_VP)]),
     "spk_batch_create": (i32, [P(_VP), i32, P(Schedule), P(_VP)]),
     "spk_batch_run_steps": (i32, [_VP, i64, i32]),
     "spk_batch_synchronize": (i32, [_VP]),
     "spk_batch_launch_count": (i32, [_VP, P(i64)]),
+    "spk_batch_stream": (i32, [_VP, P(_VP)]),
     "spk_batch_destroy": (i32, [_VP]),
     "spk_memory_info": (i32, [P(u64), P(u64)]),
     "spk_abi_version": (i32, []),

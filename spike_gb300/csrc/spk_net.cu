@@ -732,6 +732,17 @@ int spk_net_select_stimulus(spk_net* n, int32_t stimulus) {
   return SPK_OK;
 }
 
+int spk_net_write_rates(spk_net* n, int32_t stimulus, const float* rates, int64_t count) {
+  if (!n || !rates || stimulus < 0 || stimulus >= n->n_stim || count != n->Nin) {
+    set_error("write_rates: stimulus %d of %d, %lld rates for %d inputs", stimulus, n ? n->n_stim : 0,
+              (long long)count, n ? n->Nin : 0);
+    return SPK_ERR_INVALID;
+  }
+  SPK_CUDA(cudaMemcpyAsync(n->rates_dev + (size_t)stimulus * n->Nin, rates, sizeof(float) * n->Nin,
+                           cudaMemcpyHostToDevice, n->stream));
+  return SPK_OK;
+}
+
 int spk_net_run(spk_net* n, float seconds, int32_t plasticity_on) {
   if (!n || !(seconds >= 0.0f)) return SPK_ERR_INVALID;
   // number_of_timesteps = ceil(seconds / timestep) in float
@@ -959,6 +970,12 @@ int spk_net_launch_count(const spk_net* n, int64_t* launches) {
   return SPK_OK;
 }
 
+int spk_net_stream(const spk_net* n, void** stream) {
+  if (!n || !stream) return SPK_ERR_INVALID;
+  *stream = (void*)n->stream;
+  return SPK_OK;
+}
+
 int spk_memory_info(uint64_t* free_bytes, uint64_t* total_bytes) {
   size_t f = 0, t = 0;
   SPK_CUDA(cudaMemGetInfo(&f, &t));
@@ -1103,6 +1120,12 @@ int spk_batch_synchronize(spk_batch* b) {
 int spk_batch_launch_count(const spk_batch* b, int64_t* launches) {
   if (!b || !launches) return SPK_ERR_INVALID;
   *launches = b->launches;
+  return SPK_OK;
+}
+
+int spk_batch_stream(const spk_batch* b, void** stream) {
+  if (!b || !stream) return SPK_ERR_INVALID;
+  *stream = (void*)b->stream;
   return SPK_OK;
 }
 

@@ -160,6 +160,10 @@ class Net:
     def select_stimulus(self, s: int):
         check(lib().spk_net_select_stimulus(self.h, s), "spk_net_select_stimulus")
 
+    def write_rates(self, stimulus: int, rates_ptr: int, n: int):
+        """Asynchronous upload of one stimulus' rates from host address rates_ptr."""
+        check(lib().spk_net_write_rates(self.h, stimulus, C.c_void_p(rates_ptr), n), "spk_net_write_rates")
+
     def current_time(self) -> float:
         t = C.c_float()
         check(lib().spk_net_current_time(self.h, C.byref(t)), "spk_net_current_time")
@@ -217,6 +221,11 @@ class Net:
         check(lib().spk_net_launch_count(self.h, C.byref(b)), "spk_net_launch_count")
         return b.value
 
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(lib().spk_net_stream(self.h, C.byref(s)), "spk_net_stream")
+        return s.value or 0
+
 
 class Batch:
     """Many networks advanced together by one persistent launch per step block."""
@@ -238,6 +247,11 @@ class Batch:
         b = C.c_int64()
         check(lib().spk_batch_launch_count(self.h, C.byref(b)), "spk_batch_launch_count")
         return b.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(lib().spk_batch_stream(self.h, C.byref(s)), "spk_batch_stream")
+        return s.value or 0
 
     def close(self):
         if self.h:
