@@ -13,8 +13,10 @@ constexpr int MAX_GROUPS = 16;  // LIF groups per network
 constexpr int MAX_LABELS = 15;  // syn labels (4-bit field)
 constexpr int MAX_CLASSES = 16; // scale classes: 0 = pre-multiplied, 1..15 plastic
 constexpr int MAX_DELAY = 255;  // 8-bit delay field
-constexpr int LIST_CAP = 2048;  // active presynaptic keys staged per round
-constexpr int WPT_MAX = 16;     // bitmap words held per thread while listing
+constexpr int LIST_CAP = 1024;     // active presynaptic keys listed per round
+constexpr int WPT_MAX = 16;        // bitmap words held per thread while listing
+constexpr int STAGE_KEYS = 64;     // sub-rows staged per warp per round
+constexpr int STAGE_ENTRIES = 256; // synapse entries staged per warp per round
 
 // Packed synapse entry: x = post_local[0:16) | delay[16:24) | label[24:28) |
 // class[28:32), y = float bits of the value (w*scale for class 0, w otherwise).
@@ -70,13 +72,16 @@ struct NetDev {
   float* post_trace;   // [N]
   float* pre_trace;    // [n_keys] own copy (home)
   float* pre_pub;      // [2][n_keys] published each step for other CTAs
-  uint32_t* bitsA;     // [2][n_words] spikes of the step
-  uint32_t* bitsP;     // [2][n_words] STDP pre events of the step
-  uint2* spikes;       // spike store (key, float time bits)
+  // Spike bitmaps, double-buffered by step parity.  Each 64-bit word holds 32
+  // key bits in its low half and the step stamp (global step + 1) in its high
+  // half, written with one release store: a consumer that sees the stamp sees
+  // the bits, so polling the words is the step's only synchronization.
+  unsigned long long* bitsA;  // [2][n_words] spikes of the step
+  unsigned long long* bitsP;  // [2][n_words] STDP pre events of the step
+  uint2* spikes;              // spike store (key, float time bits)
   long long spike_cap;
   RunCtl* ctl;
-  unsigned int* barrier;  // per-network arrival counter (zeroed per launch)
-  int* abort_flag;        // shared by a launch: set on timeout
+  int* abort_flag;            // shared by a launch: set on timeout
 };
 
 struct CtaMap {
@@ -86,11 +91,18 @@ struct CtaMap {
 
 // Per-warp shared-memory words for a schedule (4-byte words).
 struct WarpLayout {
-  int ring, V, last, gtr, post_tr, pre_tr, spkw, in_next, in_rate, in_pre, seg, total;
+  int stage, sidx, kst, koff, kfl, kpre, ring, V, last, gtr, post_tr, pre_tr, spkw, in_next, in_rate,
+      in_pre, total;
 };
 SPK_HD WarpLayout warp_layout(int B, int TS, int L, int ITS, int kind, int has_stdp) {
   WarpLayout w;
   int o = 0;
+  w.stage = o; o += 2 * STAGE_ENTRIES;  // uint2 entries (8-byte aligned: o even)
+  w.sidx = o; o += STAGE_ENTRIES / 2;   // uint16 sub-row index per staged entry
+  w.kst = o; o += STAGE_KEYS;           // sub-row start (entry index)
+  w.koff = o; o += STAGE_KEYS + 4;      // exclusive prefix of sub-row lengths
+  w.kfl = o; o += STAGE_KEYS;           // list word (key | spike | pre-event flags)
+  w.kpre = o; o += STAGE_KEYS;          // presynaptic STDP trace of the step
   w.ring = o; o += B * TS * L;
   w.V = o; o += TS;
   w.last = o; o += TS;
@@ -101,12 +113,12 @@ SPK_HD WarpLayout warp_layout(int B, int TS, int L, int ITS, int kind, int has_s
   w.in_next = o; o += ITS;
   w.in_rate = o; o += ITS;
   w.in_pre = o; o += has_stdp ? ITS : 0;
-  w.seg = o; o += 128;  // per batch of 32 rows: offset, row start, flags, pre trace
   o = (o + 3) & ~3;
   w.total = o;
   return w;
 }
-// CTA-shared words: active list, scan scratch, flags.
+// CTA-shared words: active list, scan scratch, flags (multiple of 4 words so
+// every warp region starts 16-byte aligned).
 constexpr int SHARED_WORDS = LIST_CAP + 64 + 8;
 SPK_HD int smem_bytes(int W, const WarpLayout& wl) { return 4 * (SHARED_WORDS + W * wl.total); }
 

@@ -10,15 +10,15 @@
 //            Spike/Backend/CUDA/Neurons/LIFSpikingNeurons.cu:105-193 with
 //            Spike/Backend/CUDA/InlineDeviceFunctions.hpp:22-111) and inputs
 //            (Spike/Backend/CUDA/Neurons/PoissonInputSpikingNeurons.cu:96-129),
-//            advances the per-neuron STDP traces, and publishes one ballot word
-//            per 32 keys into the network's spike bitmap (replaces the atomic
-//            activation list of InlineDeviceFunctions.hpp:4-18);
-//   barrier  CTA barrier, or a bounded arrival counter when the network spans
-//            several CTAs;
-//   phase B  each CTA lists the step's active presynaptic keys in ascending
-//            order; each warp walks that list, reads the (key, tile) sub-row of
-//            the row-partitioned CSR (8 B per synapse) and adds w*scale into
-//            its own ring cells (reference activate_synapses,
+//            advances the per-neuron STDP traces, and publishes one stamped
+//            ballot word per 32 keys into the network's spike bitmap (replaces
+//            the atomic activation list of InlineDeviceFunctions.hpp:4-18);
+//   phase B  each CTA polls the bitmap words until they carry this step's
+//            stamp (the only inter-CTA synchronization, bounded by a timeout),
+//            lists the step's active presynaptic keys in ascending order, and
+//            each warp stages the (key, tile) sub-rows of the row-partitioned
+//            CSR (8 B per synapse) into shared memory with cp.async and adds
+//            w*scale into its own ring cells (reference activate_synapses,
 //            Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:168-202), after
 //            updating plastic weights of rows with a pre event
 //            (WeightDependentSTDPPlasticity.cu:85-161); then it updates the
@@ -28,7 +28,7 @@
 // Every ring cell has exactly one writer (the tile's warp) which applies the
 // contributions of a step in canonical order (ascending key, then synapse
 // order), so the result is deterministic and atomic-free.  Phase A of the next
-// step reads only the warp's own cells, so one barrier per step suffices.
+// step reads only the warp's own cells.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -39,53 +39,54 @@
 namespace spk {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr unsigned long long BARRIER_TIMEOUT_NS = 4000000000ull;  // 4 s
+constexpr unsigned long long POLL_TIMEOUT_NS = 4000000000ull;  // 4 s
 
 __device__ __forceinline__ unsigned long long globaltimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ int ld_volatile(const int* p) { return *(volatile const int*)p; }
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
   return m;
 }
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
 
-// Arrival barrier over the nctas CTAs of one network.  Every wait is bounded:
-// on timeout the launch's abort flag and the network status are set and all
-// CTAs leave their step loops.
-__device__ bool net_barrier(const NetDev& d, unsigned target, int* flag_smem) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    __threadfence();
-    atomicAdd(d.barrier, 1u);
-    const unsigned long long t0 = globaltimer();
-    while (ld_acquire(d.barrier) < target) {
-      if (ld_volatile(d.abort_flag)) {
-        ok = 0;
-        break;
-      }
-      if (globaltimer() - t0 > BARRIER_TIMEOUT_NS) {
-        atomicExch(d.abort_flag, 1);
-        atomicCAS(&d.ctl->status, 0, SPK_ERR_TIMEOUT);
-        ok = 0;
-        break;
-      }
-      __nanosleep(64);
+// Wait until a bitmap word carries the expected stamp; returns false on
+// timeout or abort (then the launch's abort flag and the status are set).
+__device__ __forceinline__ bool poll_word(const unsigned long long* p, unsigned stamp, const NetDev& d,
+                                          unsigned long long& v) {
+  v = ld_relaxed_u64(p);
+  if ((unsigned)(v >> 32) == stamp) return true;
+  const unsigned long long t0 = globaltimer();
+  while (true) {
+    __nanosleep(32);
+    v = ld_relaxed_u64(p);
+    if ((unsigned)(v >> 32) == stamp) return true;
+    if (ld_volatile(d.abort_flag)) return false;
+    if (globaltimer() - t0 > POLL_TIMEOUT_NS) {
+      atomicExch(d.abort_flag, 1);
+      atomicCAS(&d.ctl->status, 0, SPK_ERR_TIMEOUT);
+      return false;
     }
-    __threadfence();
-    *flag_smem = ok;
   }
-  __syncthreads();
-  return *flag_smem != 0;
 }
 
 // Exclusive block-wide scan of one int per thread; returns the prefix and the
@@ -138,7 +139,15 @@ __device__ __forceinline__ float stdp_update(const NetDev& d, float old_w, bool 
   return nw;
 }
 
-template <int U>
+// Largest j in [0, n) with koff[j] <= f (koff nondecreasing, koff[0] = 0).
+__device__ __forceinline__ int find_segment(const int* koff, int n, int f) {
+  int j = 0;
+#pragma unroll
+  for (int st = STAGE_KEYS / 2; st >= 1; st >>= 1)
+    if (j + st < n && koff[j + st] <= f) j += st;
+  return j;
+}
+
 __global__ void __launch_bounds__(512, 1)
     step_kernel(const NetDev* __restrict__ nets, const CtaMap* __restrict__ map, int K) {
   extern __shared__ __align__(16) uint32_t sm[];
@@ -152,9 +161,14 @@ __global__ void __launch_bounds__(512, 1)
 
   uint32_t* list = sm;
   int* scan = (int*)(sm + LIST_CAP);
-  int* misc = (int*)(sm + LIST_CAP + 64);
   const WarpLayout wl = warp_layout(B, TS, L, ITS, kind, d.has_stdp);
   uint32_t* wreg = sm + SHARED_WORDS + w * wl.total;
+  uint2* stage = (uint2*)(wreg + wl.stage);
+  unsigned short* sidx = (unsigned short*)(wreg + wl.sidx);
+  int* kst = (int*)(wreg + wl.kst);
+  int* koff = (int*)(wreg + wl.koff);
+  uint32_t* kfl = wreg + wl.kfl;
+  float* kpre = (float*)(wreg + wl.kpre);
   float* ring_s = (float*)(wreg + wl.ring);
   float* V_s = (float*)(wreg + wl.V);
   float* last_s = (float*)(wreg + wl.last);
@@ -165,17 +179,27 @@ __global__ void __launch_bounds__(512, 1)
   float* innext_s = (float*)(wreg + wl.in_next);
   float* inrate_s = (float*)(wreg + wl.in_rate);
   float* inpre_s = (float*)(wreg + wl.in_pre);
-  int* seg = (int*)(wreg + wl.seg);
 
   const RunCtl ctl0 = *d.ctl;
   const int steps_here = min(K, ctl0.steps_total - ctl0.step);
   if (steps_here <= 0) return;
   const bool stdp_run = d.has_stdp && ctl0.plastic;
-  const bool rank0 = cm.rank == 0;
+  const bool recorder = cm.rank == 0 && w == W - 1 && d.spike_cap > 0;
 
   const int t_idx = cm.rank * W + w;  // tile owned by this warp
   const int p0 = t_idx * TS;          // first post of the tile
   const int kin0 = t_idx * ITS;       // first input key of the tile
+
+  // Group constants: uniform over the tile unless the tile straddles groups.
+  int g_first = 0, g_last = 0;
+  {
+    const int n_hi = min(p0 + TS, N) - 1;
+    while (g_first + 1 < d.n_groups && p0 >= d.groups[g_first].end) ++g_first;
+    g_last = g_first;
+    while (g_last + 1 < d.n_groups && n_hi >= d.groups[g_last].end) ++g_last;
+  }
+  const GroupConst G0 = d.groups[g_first];
+  const float t_ref = d.t_ref, i_bg = d.i_bg;
 
   // ---- load the tile's state into shared memory -------------------------------
   {
@@ -210,17 +234,21 @@ __global__ void __launch_bounds__(512, 1)
   unsigned long long ev = 0;
   bool inputs_active = ctl0.inputs_active != 0;
   int steps_done = 0;
-  __syncthreads();
+  bool ok_run = true;
+  __syncwarp();
 
-  for (int s = 0; s < steps_here; ++s) {
+  for (int s = 0; s < steps_here && ok_run; ++s) {
     const int sr = ctl0.step + s;
     // current_time_in_seconds = starttime + s*timestep_grouping*timestep
     // (Spike/Models/SpikingModel.cpp:226), timestep_index = roundf(t/dt).
     const float t = ctl0.start_time + (float)(sr * 1) * dt;
     const int T = (int)roundf(t / dt);
-    const int par = (int)((ctl0.gstep + s) & 1);
-    uint32_t* bitsA = d.bitsA + (size_t)par * n_words;
-    uint32_t* bitsP = d.bitsP + (size_t)par * n_words;
+    const long long gs = ctl0.gstep + s;
+    const int par = (int)(gs & 1);
+    const unsigned stamp = (unsigned)(gs + 1);
+    const unsigned long long stamp_hi = (unsigned long long)stamp << 32;
+    unsigned long long* bitsA = d.bitsA + (size_t)par * n_words;
+    unsigned long long* bitsP = d.bitsP + (size_t)par * n_words;
     float* pub = d.pre_pub + (size_t)par * n_keys;
     const int slot = T % B;
     const float tg = t + 0.0f * dt;  // t + g*timestep with g = 0
@@ -234,9 +262,12 @@ __global__ void __launch_bounds__(512, 1)
         const int n = p0 + li;
         bool spk = false;
         if (n < N) {
-          int gi = 0;
-          while (gi + 1 < d.n_groups && n >= d.groups[gi].end) ++gi;
-          const GroupConst& G = d.groups[gi];
+          GroupConst G = G0;
+          if (g_last != g_first) {
+            int gi = g_first;
+            while (gi < g_last && n >= d.groups[gi].end) ++gi;
+            G = d.groups[gi];
+          }
           float Vi = V_s[li];
           float input;
           if (kind == SPK_SYN_CONDUCTANCE) {
@@ -268,8 +299,8 @@ __global__ void __launch_bounds__(512, 1)
             }
             input = total;
           }
-          if (((tg - last_s[li]) - d.t_ref) > half_dt) {
-            Vi = G.k * G.v0 + (1.0f - G.k) * Vi + G.k * d.i_bg + input;
+          if (((tg - last_s[li]) - t_ref) > half_dt) {
+            Vi = G.k * G.v0 + (1.0f - G.k) * Vi + G.k * i_bg + input;
             if (Vi >= G.theta) {
               spk = true;
               last_s[li] = tg;
@@ -288,11 +319,12 @@ __global__ void __launch_bounds__(512, 1)
           }
         }
         const unsigned word = __ballot_sync(FULL, spk);
+        __syncwarp();
         if (lane == 0) {
           const int wi = (KL + p0 + base) >> 5;
-          bitsA[wi] = word;
-          if (stdp_run) bitsP[wi] = word;
           spkw_s[base >> 5] = word;
+          if (stdp_run) st_release_u64(bitsP + wi, stamp_hi | word);
+          st_release_u64(bitsA + wi, stamp_hi | word);
         }
       }
     }
@@ -323,44 +355,49 @@ __global__ void __launch_bounds__(512, 1)
       }
       const unsigned wa = __ballot_sync(FULL, spk);
       const unsigned wp = __ballot_sync(FULL, pev);
+      __syncwarp();
       if (lane == 0) {
         const int wi = (kin0 + base) >> 5;
-        bitsA[wi] = wa;
-        if (stdp_run) bitsP[wi] = wp;
+        if (stdp_run) st_release_u64(bitsP + wi, stamp_hi | wp);
+        st_release_u64(bitsA + wi, stamp_hi | wa);
       }
     }
     inputs_active = true;
 
-    // ---- barrier: the step's bitmap is complete --------------------------------
-    if (d.nctas > 1) {
-      if (!net_barrier(d, (unsigned)(d.nctas * (s + 1)), misc)) break;
-    } else {
-      __syncthreads();
-    }
-
-    // ---- phase B: list active keys (ascending), propagate, STDP ---------------
+    // ---- phase B: poll the bitmap, list active keys (ascending) ---------------
     const int nthreads = blockDim.x;
-    for (int wbase = 0; wbase < n_words; wbase += nthreads * WPT_MAX) {
+    for (int wbase = 0; wbase < n_words && ok_run; wbase += nthreads * WPT_MAX) {
       const int wchunk = min(n_words - wbase, nthreads * WPT_MAX);
       const int wpt = (wchunk + nthreads - 1) / nthreads;
       const int my0 = wbase + threadIdx.x * wpt;
       uint32_t wA[WPT_MAX], wP[WPT_MAX];
       int cnt = 0;
+      bool ok = true;
 #pragma unroll
       for (int i = 0; i < WPT_MAX; ++i) {
         wA[i] = 0u;
         wP[i] = 0u;
-        if (i < wpt && my0 + i < wbase + wchunk) {
-          wA[i] = __ldcg(bitsA + my0 + i);
-          if (stdp_run) wP[i] = __ldcg(bitsP + my0 + i);
+        if (ok && i < wpt && my0 + i < wbase + wchunk) {
+          unsigned long long v;
+          ok = poll_word(bitsA + my0 + i, stamp, d, v);
+          wA[i] = (uint32_t)v;
+          if (ok && stdp_run) {
+            ok = poll_word(bitsP + my0 + i, stamp, d, v);
+            wP[i] = (uint32_t)v;
+          }
           cnt += __popc(wA[i] | wP[i]);
         }
+      }
+      if (stdp_run) fence_acq_rel_gpu();  // the pre traces published with the words
+      if (__syncthreads_or(!ok)) {
+        ok_run = false;
+        break;
       }
       int total;
       const int my_off = block_exclusive_scan(cnt, scan, &total);
       for (int rbase = 0; rbase < total; rbase += LIST_CAP) {
         const int n_round = min(LIST_CAP, total - rbase);
-        // write this thread's keys that fall in the round
+        if (rbase > 0) __syncthreads();  // previous round fully consumed
         int pos = my_off;
 #pragma unroll
         for (int i = 0; i < WPT_MAX; ++i) {
@@ -378,10 +415,10 @@ __global__ void __launch_bounds__(512, 1)
         }
         __syncthreads();
 
-        // spike store: recorded by rank 0 in list (canonical) order
-        if (rank0 && d.spike_cap > 0) {
-          for (int c0 = 0; c0 < n_round; c0 += nthreads) {
-            const int j = c0 + threadIdx.x;
+        // spike store: one warp of rank 0, in list (canonical) order
+        if (recorder) {
+          for (int c0 = 0; c0 < n_round; c0 += 32) {
+            const int j = c0 + lane;
             bool rec = false;
             uint32_t key = 0;
             if (j < n_round) {
@@ -389,88 +426,83 @@ __global__ void __launch_bounds__(512, 1)
               key = lv & 0x3fffffffu;
               rec = (lv >> 31) && ((int)key >= KL || ctl0.record_inputs);
             }
-            int tot;
-            const int off = block_exclusive_scan(rec ? 1 : 0, scan, &tot);
+            const unsigned m = __ballot_sync(FULL, rec);
             if (rec) {
-              const unsigned long long p = spike_count + (unsigned long long)off;
+              const unsigned long long p = spike_count + (unsigned long long)__popc(m & lanemask_lt());
               if (p < (unsigned long long)d.spike_cap)
                 d.spikes[p] = make_uint2(key, __float_as_uint(t));
               else
                 atomicCAS(&d.ctl->status, 0, SPK_ERR_OVERFLOW);
             }
-            spike_count += (unsigned long long)tot;
+            spike_count += (unsigned long long)__popc(m);
           }
           if (spike_count > (unsigned long long)d.spike_cap) spike_count = d.spike_cap;
         }
 
-        // each warp: its tile's sub-rows of the listed keys, in list order
-        for (int jb = 0; jb < n_round; jb += 32) {
-          const int j = jb + lane;
-          uint32_t lv = 0u;
-          int rp0 = 0, len = 0;
-          float prt = 0.0f;
-          if (j < n_round) {
-            lv = list[j];
+        // ---- each warp: stage its tile's sub-rows of the listed keys ----------
+        for (int kb = 0; kb < n_round; kb += STAGE_KEYS) {
+          const int nk = min(STAGE_KEYS, n_round - kb);
+          for (int i = lane; i < nk; i += 32) {
+            const uint32_t lv = list[kb + i];
             const int key = (int)(lv & 0x3fffffffu);
             const size_t ri = (size_t)key * n_tiles + t_idx;
-            rp0 = __ldg(d.rowptr + ri);
-            len = __ldg(d.rowptr + ri + 1) - rp0;
-            if (stdp_run) prt = __ldcg(pub + key);
+            const int rp0 = __ldg(d.rowptr + ri);
+            const int len = __ldg(d.rowptr + ri + 1) - rp0;
+            kst[i] = rp0;
+            koff[i] = len;
+            kfl[i] = lv;
+            if (stdp_run) kpre[i] = __ldcg(pub + key);
             if (lv >> 31) ev += (unsigned long long)len;
           }
-          int incl = len;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(FULL, incl, o);
-            if (lane >= o) incl += y;
-          }
-          const int tot = __shfl_sync(FULL, incl, 31);
-          seg[lane] = incl - len;
-          seg[32 + lane] = rp0;
-          seg[64 + lane] = (int)lv;
-          seg[96 + lane] = __float_as_int(prt);
           __syncwarp();
-          for (int f0 = 0; f0 < tot; f0 += 32 * U) {
-            uint2 ent[U];
-            int eid[U], jj[U];
+          // exclusive prefix of the sub-row lengths
+          int carry = 0;
+          for (int c0 = 0; c0 < nk; c0 += 32) {
+            const int i = c0 + lane;
+            const int len = i < nk ? koff[i] : 0;
+            int incl = len;
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-              const int f = f0 + u * 32 + lane;
-              jj[u] = -1;
-              eid[u] = 0;
-              ent[u] = make_uint2(0u, 0u);
-              if (f < tot) {
-                int sj = 0;
-#pragma unroll
-                for (int st = 16; st >= 1; st >>= 1)
-                  if (seg[sj + st] <= f) sj += st;
-                const int e = seg[32 + sj] + (f - seg[sj]);
-                jj[u] = sj;
-                eid[u] = e;
-                ent[u] = d.entries[e];
-              }
+            for (int o = 1; o < 32; o <<= 1) {
+              const int y = __shfl_up_sync(FULL, incl, o);
+              if (lane >= o) incl += y;
             }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
+            __syncwarp();
+            if (i < nk) koff[i] = carry + incl - len;
+            carry += __shfl_sync(FULL, incl, 31);
+          }
+          const int total_e = carry;
+          __syncwarp();
+          for (int f0 = 0; f0 < total_e; f0 += STAGE_ENTRIES) {
+            const int nf = min(STAGE_ENTRIES, total_e - f0);
+            for (int f = lane; f < nf; f += 32) {
+              const int j = find_segment(koff, nk, f0 + f);
+              sidx[f] = (unsigned short)j;
+              cp_async8(stage + f, d.entries + kst[j] + (f0 + f - koff[j]));
+            }
+            cp_async_wait_all();
+            __syncwarp();
+            for (int c0 = 0; c0 < nf; c0 += 32) {
+              const int f = c0 + lane;
               bool add = false;
               int cell = -1 - lane;
               float contrib = 0.0f;
-              if (jj[u] >= 0) {
-                const uint32_t flv = (uint32_t)seg[64 + jj[u]];
+              if (f < nf) {
+                const int j = sidx[f];
+                const uint32_t flv = kfl[j];
                 const bool A = (flv >> 31) != 0;
                 const bool P = ((flv >> 30) & 1u) != 0;
-                const uint32_t x = ent[u].x;
-                const int q = (int)(x & 0xffffu);
-                const int dl = (int)((x >> 16) & 0xffu);
-                const int lb = (int)((x >> 24) & 0xfu);
-                const int c = (int)(x >> 28);
-                float v = __uint_as_float(ent[u].y);
+                const uint2 en = stage[f];
+                const int q = (int)(en.x & 0xffffu);
+                const int dl = (int)((en.x >> 16) & 0xffu);
+                const int lb = (int)((en.x >> 24) & 0xfu);
+                const int c = (int)(en.x >> 28);
+                float v = __uint_as_float(en.y);
                 if (c != 0) {
                   if (stdp_run) {
                     const bool post_ev = ((spkw_s[q >> 5] >> (q & 31)) & 1u) != 0;
                     if (P || post_ev) {
-                      v = stdp_update(d, v, P, post_ev, post_s[q], __int_as_float(seg[96 + jj[u]]));
-                      d.entries[eid[u]].y = __float_as_uint(v);
+                      v = stdp_update(d, v, P, post_ev, post_s[q], kpre[j]);
+                      d.entries[kst[j] + (f0 + f - koff[j])].y = __float_as_uint(v);
                     }
                   }
                   contrib = v * d.scale_tab[c];
@@ -484,8 +516,8 @@ __global__ void __launch_bounds__(512, 1)
                   cell = (sl * TS + q) * L + lb;
                 }
               }
-              // apply in lane order within a chunk (match_any groups lanes that
-              // hit the same cell), chunks in program order
+              // apply in lane order within a chunk (match_any groups the lanes
+              // that hit one cell), chunks in program order
               const unsigned grp = __match_any_sync(FULL, cell);
               const int rank = __popc(grp & lanemask_lt());
               const int maxr = __reduce_max_sync(FULL, add ? rank : 0);
@@ -494,12 +526,12 @@ __global__ void __launch_bounds__(512, 1)
                 __syncwarp();
               }
             }
+            __syncwarp();
           }
-          __syncwarp();
         }
-        __syncthreads();
       }
     }
+    if (!ok_run) break;
 
     // ---- phase B: plastic afferents of the tile's spiking posts ---------------
     if (stdp_run) {
@@ -514,9 +546,9 @@ __global__ void __launch_bounds__(512, 1)
           for (int a = a0 + lane; a < a1; a += 32) {
             const uint2 cc = __ldg(d.csc + a);
             const int pk = (int)cc.y;
-            const uint32_t wa = __ldcg(bitsA + (pk >> 5));
-            const uint32_t wp = __ldcg(bitsP + (pk >> 5));
-            if (((wa | wp) >> (pk & 31)) & 1u) continue;  // row handled in the pre pass
+            const unsigned long long va = ld_relaxed_u64(bitsA + (pk >> 5));
+            const unsigned long long vp = ld_relaxed_u64(bitsP + (pk >> 5));
+            if ((((uint32_t)va | (uint32_t)vp) >> (pk & 31)) & 1u) continue;  // handled in the pre pass
             const float old = __uint_as_float(d.entries[cc.x].y);
             const float prt = __ldcg(pub + pk);
             const float nw = stdp_update(d, old, false, true, post_s[ql], prt);
@@ -565,11 +597,13 @@ __global__ void __launch_bounds__(512, 1)
     for (int o = 16; o >= 1; o >>= 1) e += __shfl_xor_sync(FULL, e, o);
     if (lane == 0 && e) atomicAdd(&d.ctl->events, e);
   }
-  if (rank0 && threadIdx.x == 0) {
-    d.ctl->step = ctl0.step + steps_done;
-    d.ctl->gstep = ctl0.gstep + steps_done;
-    if (steps_done > 0) d.ctl->inputs_active = 1;
-    d.ctl->spike_count = spike_count;
+  if (recorder || (cm.rank == 0 && w == W - 1)) {
+    if (lane == 0) {
+      d.ctl->step = ctl0.step + steps_done;
+      d.ctl->gstep = ctl0.gstep + steps_done;
+      if (steps_done > 0) d.ctl->inputs_active = 1;
+      if (recorder) d.ctl->spike_count = spike_count;
+    }
   }
 }
 

@@ -41,7 +41,7 @@ void set_error(const char* fmt, ...) {
     }                                                                               \
   } while (0)
 
-constexpr int U_ENTRIES = 8;
+
 constexpr int DEFAULT_STEPS_PER_LAUNCH = 1000;
 constexpr int64_t DEFAULT_SPIKE_CAPACITY = 1 << 24;
 
@@ -188,7 +188,6 @@ struct spk_batch {
   NetDev* dd = nullptr;
   CtaMap* dmap = nullptr;
   int* abort_dev = nullptr;
-  unsigned* barrier_pool = nullptr;
   std::vector<std::pair<int, int>> waves;  // CTA ranges per launch
   int W = 0, smem = 0, K = 0, total_ctas = 0;
   bool cooperative = false;
@@ -238,7 +237,6 @@ static int upload_state_defaults(spk_net* n) {
 }
 
 static int launch_block(spk_net* n) {
-  SPK_CUDA(cudaMemsetAsync(n->hd.barrier, 0, sizeof(unsigned), n->stream));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(n->plan.nctas);
   cfg.blockDim = dim3(n->plan.W * 32);
@@ -249,7 +247,7 @@ static int launch_block(spk_net* n) {
   attr[0].val.cooperative = n->cooperative ? 1 : 0;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  SPK_CUDA(cudaLaunchKernelEx(&cfg, step_kernel<U_ENTRIES>, (const NetDev*)n->dd, (const CtaMap*)n->dmap,
+  SPK_CUDA(cudaLaunchKernelEx(&cfg, step_kernel, (const NetDev*)n->dd, (const CtaMap*)n->dmap,
                               n->plan.K));
   return SPK_OK;
 }
@@ -496,7 +494,7 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
   void* p_V = nullptr; void* p_last = nullptr; void* p_gtr = nullptr; void* p_ring = nullptr;
   void* p_innext = nullptr; void* p_rates = nullptr; void* p_post = nullptr; void* p_pre = nullptr;
   void* p_pub = nullptr; void* p_bA = nullptr; void* p_bP = nullptr; void* p_spk = nullptr;
-  void* p_ctl = nullptr; void* p_bar = nullptr; void* p_abort = nullptr; void* p_dd = nullptr; void* p_map = nullptr;
+  void* p_ctl = nullptr; void* p_abort = nullptr; void* p_dd = nullptr; void* p_map = nullptr;
   std::vector<Part> parts = {
       {&p_rowptr, sizeof(int32_t) * rowptr.size()},
       {&p_entries, sizeof(uint2) * (size_t)std::max<int64_t>(S, 1)},
@@ -511,11 +509,10 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
       {&p_post, sizeof(float) * (stdp ? N : 0)},
       {&p_pre, sizeof(float) * (stdp ? n_keys : 0)},
       {&p_pub, sizeof(float) * (stdp ? 2 * (size_t)n_keys : 0)},
-      {&p_bA, sizeof(uint32_t) * 2 * (size_t)n_words},
-      {&p_bP, sizeof(uint32_t) * 2 * (size_t)n_words},
+      {&p_bA, sizeof(unsigned long long) * 2 * (size_t)n_words},
+      {&p_bP, sizeof(unsigned long long) * 2 * (size_t)n_words},
       {&p_spk, sizeof(uint2) * (size_t)std::max<int64_t>(spike_cap, 1)},
       {&p_ctl, sizeof(RunCtl)},
-      {&p_bar, sizeof(unsigned)},
       {&p_abort, sizeof(int)},
       {&p_dd, sizeof(NetDev)},
       {&p_map, sizeof(CtaMap) * plan.nctas},
@@ -618,12 +615,11 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
   h.post_trace = (float*)p_post;
   h.pre_trace = (float*)p_pre;
   h.pre_pub = (float*)p_pub;
-  h.bitsA = (uint32_t*)p_bA;
-  h.bitsP = (uint32_t*)p_bP;
+  h.bitsA = (unsigned long long*)p_bA;
+  h.bitsP = (unsigned long long*)p_bP;
   h.spikes = (uint2*)p_spk;
   h.spike_cap = spike_cap;
   h.ctl = (RunCtl*)p_ctl;
-  h.barrier = (unsigned*)p_bar;
   h.abort_flag = (int*)p_abort;
   n->abort_dev = (int*)p_abort;
   n->dd = (NetDev*)p_dd;
@@ -648,20 +644,20 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
   urc |= up(p_dd, &h, sizeof(h));
   urc |= up(p_map, map.data(), sizeof(CtaMap) * map.size());
   if (urc) return fail_free(SPK_ERR_CUDA);
-  if (cudaMemsetAsync(p_bA, 0, sizeof(uint32_t) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
-      cudaMemsetAsync(p_bP, 0, sizeof(uint32_t) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
+  if (cudaMemsetAsync(p_bA, 0, sizeof(unsigned long long) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
+      cudaMemsetAsync(p_bP, 0, sizeof(unsigned long long) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
       cudaMemsetAsync(p_abort, 0, sizeof(int), n->stream) != cudaSuccess) {
     set_error("cudaMemsetAsync failed");
     return fail_free(SPK_ERR_CUDA);
   }
-  if (cudaFuncSetAttribute(step_kernel<U_ENTRIES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (cudaFuncSetAttribute(step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            di.max_smem) != cudaSuccess) {
     set_error("cudaFuncSetAttribute failed: %s", cudaGetErrorString(cudaGetLastError()));
     return fail_free(SPK_ERR_CUDA);
   }
   if (plan.nctas > 1) {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_kernel<U_ENTRIES>, plan.W * 32, plan.smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_kernel, plan.W * 32, plan.smem) !=
         cudaSuccess) {
       set_error("occupancy query failed");
       return fail_free(SPK_ERR_CUDA);
@@ -770,7 +766,7 @@ int spk_net_synchronize(spk_net* n) {
   int st = 0;
   int rc = read_status(n, &st);
   if (rc) return rc;
-  if (st == SPK_ERR_TIMEOUT) set_error("a device barrier timed out");
+  if (st == SPK_ERR_TIMEOUT) set_error("a device wait on another CTA timed out");
   if (st == SPK_ERR_OVERFLOW) set_error("the device spike store overflowed; spikes were dropped");
   return st;
 }
@@ -1006,7 +1002,7 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
       b->total_ctas += n->plan.nctas;
     }
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_kernel<U_ENTRIES>, b->W * 32, b->smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_kernel, b->W * 32, b->smem) !=
             cudaSuccess ||
         per_sm < 1) {
       set_error("batch: no CTA of %d threads with %d B shared memory fits", b->W * 32, b->smem);
@@ -1039,8 +1035,7 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
     }
     b->waves.push_back({wave_start, wave_ctas});
     b->cooperative = any_multi;
-    const size_t bytes = align_up(sizeof(NetDev) * n_nets, 256) + align_up(sizeof(CtaMap) * map.size(), 256) +
-                         align_up(sizeof(unsigned) * n_nets, 256) + 256;
+    const size_t bytes = align_up(sizeof(NetDev) * n_nets, 256) + align_up(sizeof(CtaMap) * map.size(), 256) + 256;
     void* mem = nullptr;
     if (cudaMalloc(&mem, bytes) != cudaSuccess) {
       cudaGetLastError();
@@ -1050,12 +1045,8 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
     }
     b->dd = (NetDev*)mem;
     b->dmap = (CtaMap*)((char*)mem + align_up(sizeof(NetDev) * n_nets, 256));
-    b->barrier_pool = (unsigned*)((char*)b->dmap + align_up(sizeof(CtaMap) * map.size(), 256));
-    b->abort_dev = (int*)((char*)b->barrier_pool + align_up(sizeof(unsigned) * n_nets, 256));
-    for (int i = 0; i < n_nets; ++i) {
-      hds[i].barrier = b->barrier_pool + i;
-      hds[i].abort_flag = b->abort_dev;
-    }
+    b->abort_dev = (int*)((char*)b->dmap + align_up(sizeof(CtaMap) * map.size(), 256));
+    for (int i = 0; i < n_nets; ++i) hds[i].abort_flag = b->abort_dev;
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMemcpy(b->dd, hds.data(), sizeof(NetDev) * n_nets, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b->dmap, map.data(), sizeof(CtaMap) * map.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -1083,7 +1074,6 @@ int spk_batch_run_steps(spk_batch* b, int64_t n_steps, int32_t plasticity_on) {
   }
   const int64_t blocks = (n_steps + b->K - 1) / b->K;
   for (int64_t blk = 0; blk < blocks; ++blk) {
-    SPK_CUDA(cudaMemsetAsync(b->barrier_pool, 0, sizeof(unsigned) * b->nets.size(), b->stream));
     for (const auto& wv : b->waves) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(wv.second);
@@ -1095,7 +1085,7 @@ int spk_batch_run_steps(spk_batch* b, int64_t n_steps, int32_t plasticity_on) {
       attr[0].val.cooperative = b->cooperative ? 1 : 0;
       cfg.attrs = attr;
       cfg.numAttrs = 1;
-      SPK_CUDA(cudaLaunchKernelEx(&cfg, step_kernel<U_ENTRIES>, (const NetDev*)b->dd,
+      SPK_CUDA(cudaLaunchKernelEx(&cfg, step_kernel, (const NetDev*)b->dd,
                                   (const CtaMap*)(b->dmap + wv.first), b->K));
       ++b->launches;
     }

@@ -82,7 +82,7 @@ class Desc:
 
 
 def random_voltage_net(n=300, n_in=200, rate=40.0, p=0.08, d_max=12, seed=5, plastic=False, stdp=None,
-                       j=4.0e-4, g=4.0, record_inputs=True):
+                       j=8.0e-4, g=4.0, record_inputs=True):
     """A small random voltage-synapse network with inputs, E/I weights and
     delays 1..d_max (multapses included), for parity tests."""
     rng = np.random.default_rng(seed)
