@@ -91,8 +91,8 @@ struct CtaMap {
 
 // Per-warp shared-memory words for a schedule (4-byte words).
 struct WarpLayout {
-  int stage, sidx, kst, koff, kfl, kpre, ring, V, last, gtr, post_tr, pre_tr, spkw, in_next, in_rate,
-      in_pre, total;
+  int stage, sidx, kst, koff, kfl, kpre, ring, V, last, gtr, post_tr, pre_tr, spkw, inw, inwp, in_next,
+      in_rate, in_pre, total;
 };
 SPK_HD WarpLayout warp_layout(int B, int TS, int L, int ITS, int kind, int has_stdp) {
   WarpLayout w;
@@ -109,7 +109,9 @@ SPK_HD WarpLayout warp_layout(int B, int TS, int L, int ITS, int kind, int has_s
   w.gtr = o; o += (kind == 3) ? 0 : TS * L;
   w.post_tr = o; o += has_stdp ? TS : 0;
   w.pre_tr = o; o += has_stdp ? TS : 0;
-  w.spkw = o; o += TS / 32;
+  w.spkw = o; o += TS / 32;   // spike words of the tile's neurons (this step)
+  w.inw = o; o += ITS / 32;   // spike words of the tile's inputs
+  w.inwp = o; o += ITS / 32;  // STDP pre-event words of the tile's inputs
   w.in_next = o; o += ITS;
   w.in_rate = o; o += ITS;
   w.in_pre = o; o += has_stdp ? ITS : 0;

@@ -51,8 +51,8 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ int ld_volatile(const int* p) { return *(volatile const int*)p; }
@@ -151,9 +151,16 @@ __device__ __forceinline__ int find_segment(const int* koff, int n, int f) {
 __global__ void __launch_bounds__(512, 1)
     step_kernel(const NetDev* __restrict__ nets, const CtaMap* __restrict__ map, int K) {
   extern __shared__ __align__(16) uint32_t sm[];
+  __shared__ float s_decay[MAX_LABELS + 1], s_vhat[MAX_LABELS + 1], s_scale[MAX_CLASSES];
   const CtaMap cm = map[blockIdx.x];
   const NetDev& d = nets[cm.net];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x < MAX_LABELS + 1) {
+    s_decay[threadIdx.x] = d.decay[threadIdx.x];
+    s_vhat[threadIdx.x] = d.vhat[threadIdx.x];
+  }
+  if (threadIdx.x < MAX_CLASSES) s_scale[threadIdx.x] = d.scale_tab[threadIdx.x];
+  __syncthreads();
   const int W = d.W;
   const int N = d.N, Nin = d.Nin, KL = d.KL, L = d.L, B = d.B, kind = d.kind;
   const int TS = d.TS, ITS = d.ITS, n_tiles = d.n_tiles, n_keys = d.n_keys, n_words = d.n_words;
@@ -176,6 +183,8 @@ __global__ void __launch_bounds__(512, 1)
   float* post_s = (float*)(wreg + wl.post_tr);
   float* pre_s = (float*)(wreg + wl.pre_tr);
   uint32_t* spkw_s = wreg + wl.spkw;
+  uint32_t* inw_s = wreg + wl.inw;
+  uint32_t* inwp_s = wreg + wl.inwp;
   float* innext_s = (float*)(wreg + wl.in_next);
   float* inrate_s = (float*)(wreg + wl.in_rate);
   float* inpre_s = (float*)(wreg + wl.in_pre);
@@ -275,8 +284,8 @@ __global__ void __launch_bounds__(512, 1)
             for (int l = 0; l < L; ++l) {
               const float cell = ring_slot[li * L + l];
               ring_slot[li * L + l] = 0.0f;
-              const float gnew = d.decay[l] * gtr_s[li * L + l] + cell;
-              total = total + gnew * (d.vhat[l] - Vi);
+              const float gnew = s_decay[l] * gtr_s[li * L + l] + cell;
+              total = total + gnew * (s_vhat[l] - Vi);
               gtr_s[li * L + l] = gnew;
             }
             input = total * G.kR;
@@ -285,7 +294,7 @@ __global__ void __launch_bounds__(512, 1)
             for (int l = 0; l < L; ++l) {
               const float cell = ring_slot[li * L + l];
               ring_slot[li * L + l] = 0.0f;
-              float inew = gtr_s[li * L + l] * d.decay[l];
+              float inew = gtr_s[li * L + l] * s_decay[l];
               inew = inew + cell;
               total = total + inew;
               gtr_s[li * L + l] = inew;
@@ -319,13 +328,7 @@ __global__ void __launch_bounds__(512, 1)
           }
         }
         const unsigned word = __ballot_sync(FULL, spk);
-        __syncwarp();
-        if (lane == 0) {
-          const int wi = (KL + p0 + base) >> 5;
-          spkw_s[base >> 5] = word;
-          if (stdp_run) st_release_u64(bitsP + wi, stamp_hi | word);
-          st_release_u64(bitsA + wi, stamp_hi | word);
-        }
+        if (lane == 0) spkw_s[base >> 5] = word;
       }
     }
     // ---- phase A: Poisson inputs of the tile ----------------------------------
@@ -355,14 +358,36 @@ __global__ void __launch_bounds__(512, 1)
       }
       const unsigned wa = __ballot_sync(FULL, spk);
       const unsigned wp = __ballot_sync(FULL, pev);
-      __syncwarp();
       if (lane == 0) {
-        const int wi = (kin0 + base) >> 5;
-        if (stdp_run) st_release_u64(bitsP + wi, stamp_hi | wp);
-        st_release_u64(bitsA + wi, stamp_hi | wa);
+        inw_s[base >> 5] = wa;
+        inwp_s[base >> 5] = wp;
       }
     }
     inputs_active = true;
+
+    // ---- publish the tile's words: stamp and bits in one 64-bit store ---------
+    // Without plasticity the word is the only data another CTA reads, so a
+    // relaxed store suffices; with plasticity one fence per warp orders the
+    // published pre traces before the words (fence + strong store = release).
+    __syncwarp();
+    if (stdp_run) fence_acq_rel_gpu();
+    {
+      const int nl = TS >> 5, ni = ITS >> 5;
+      for (int i = lane; i < nl + ni; i += 32) {
+        uint32_t wa, wp;
+        int wi;
+        if (i < nl) {
+          wa = wp = spkw_s[i];
+          wi = ((KL + p0) >> 5) + i;
+        } else {
+          wa = inw_s[i - nl];
+          wp = inwp_s[i - nl];
+          wi = (kin0 >> 5) + (i - nl);
+        }
+        if (stdp_run) st_relaxed_u64(bitsP + wi, stamp_hi | wp);
+        st_relaxed_u64(bitsA + wi, stamp_hi | wa);
+      }
+    }
 
     // ---- phase B: poll the bitmap, list active keys (ascending) ---------------
     const int nthreads = blockDim.x;
@@ -505,7 +530,7 @@ __global__ void __launch_bounds__(512, 1)
                       d.entries[kst[j] + (f0 + f - koff[j])].y = __float_as_uint(v);
                     }
                   }
-                  contrib = v * d.scale_tab[c];
+                  contrib = v * s_scale[c];
                 } else {
                   contrib = v;
                 }
