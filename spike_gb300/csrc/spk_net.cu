@@ -78,6 +78,10 @@ static int device_info(DeviceInfo* di) {
   SPK_CUDA(cudaGetDevice(&dev));
   SPK_CUDA(cudaDeviceGetAttribute(&di->sms, cudaDevAttrMultiProcessorCount, dev));
   SPK_CUDA(cudaDeviceGetAttribute(&di->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  // the dynamic shared-memory limit excludes the kernel's static shared memory
+  cudaFuncAttributes fa;
+  SPK_CUDA(cudaFuncGetAttributes(&fa, step_kernel));
+  di->max_smem -= (int)fa.sharedSizeBytes;
   return SPK_OK;
 }
 
