@@ -139,15 +139,6 @@ __device__ __forceinline__ float stdp_update(const NetDev& d, float old_w, bool 
   return nw;
 }
 
-// Largest j in [0, n) with koff[j] <= f (koff nondecreasing, koff[0] = 0).
-__device__ __forceinline__ int find_segment(const int* koff, int n, int f) {
-  int j = 0;
-#pragma unroll
-  for (int st = STAGE_KEYS / 2; st >= 1; st >>= 1)
-    if (j + st < n && koff[j + st] <= f) j += st;
-  return j;
-}
-
 __global__ void __launch_bounds__(512, 1)
     step_kernel(const NetDev* __restrict__ nets, const CtaMap* __restrict__ map, int K) {
   extern __shared__ __align__(16) uint32_t sm[];
@@ -398,20 +389,24 @@ __global__ void __launch_bounds__(512, 1)
       uint32_t wA[WPT_MAX], wP[WPT_MAX];
       int cnt = 0;
       bool ok = true;
+      // first read every word with independent loads, then re-poll only the
+      // words whose producer has not published this step yet
+      unsigned long long va[WPT_MAX], vp[WPT_MAX];
 #pragma unroll
       for (int i = 0; i < WPT_MAX; ++i) {
-        wA[i] = 0u;
-        wP[i] = 0u;
-        if (ok && i < wpt && my0 + i < wbase + wchunk) {
-          unsigned long long v;
-          ok = poll_word(bitsA + my0 + i, stamp, d, v);
-          wA[i] = (uint32_t)v;
-          if (ok && stdp_run) {
-            ok = poll_word(bitsP + my0 + i, stamp, d, v);
-            wP[i] = (uint32_t)v;
-          }
-          cnt += __popc(wA[i] | wP[i]);
-        }
+        const bool mine = i < wpt && my0 + i < wbase + wchunk;
+        va[i] = mine ? ld_relaxed_u64(bitsA + my0 + i) : stamp_hi;
+        vp[i] = (mine && stdp_run) ? ld_relaxed_u64(bitsP + my0 + i) : stamp_hi;
+      }
+#pragma unroll
+      for (int i = 0; i < WPT_MAX; ++i) {
+        const bool mine = i < wpt && my0 + i < wbase + wchunk;
+        if (mine && ok && (unsigned)(va[i] >> 32) != stamp) ok = poll_word(bitsA + my0 + i, stamp, d, va[i]);
+        if (mine && ok && stdp_run && (unsigned)(vp[i] >> 32) != stamp)
+          ok = poll_word(bitsP + my0 + i, stamp, d, vp[i]);
+        wA[i] = mine ? (uint32_t)va[i] : 0u;
+        wP[i] = (mine && stdp_run) ? (uint32_t)vp[i] : 0u;
+        cnt += __popc(wA[i] | wP[i]);
       }
       if (stdp_run) fence_acq_rel_gpu();  // the pre traces published with the words
       if (__syncthreads_or(!ok)) {
@@ -467,17 +462,34 @@ __global__ void __launch_bounds__(512, 1)
         // ---- each warp: stage its tile's sub-rows of the listed keys ----------
         for (int kb = 0; kb < n_round; kb += STAGE_KEYS) {
           const int nk = min(STAGE_KEYS, n_round - kb);
-          for (int i = lane; i < nk; i += 32) {
-            const uint32_t lv = list[kb + i];
-            const int key = (int)(lv & 0x3fffffffu);
-            const size_t ri = (size_t)key * n_tiles + t_idx;
-            const int rp0 = __ldg(d.rowptr + ri);
-            const int len = __ldg(d.rowptr + ri + 1) - rp0;
-            kst[i] = rp0;
-            koff[i] = len;
-            kfl[i] = lv;
-            if (stdp_run) kpre[i] = __ldcg(pub + key);
-            if (lv >> 31) ev += (unsigned long long)len;
+          {
+            // all row-pointer loads of the round are independent: issue them together
+            constexpr int KPL = STAGE_KEYS / 32;
+            int rp0[KPL], rp1[KPL];
+            uint32_t lvs[KPL];
+            float prs[KPL];
+#pragma unroll
+            for (int u = 0; u < KPL; ++u) {
+              const int i = u * 32 + lane;
+              lvs[u] = i < nk ? list[kb + i] : 0u;
+              const int key = (int)(lvs[u] & 0x3fffffffu);
+              const size_t ri = (size_t)key * n_tiles + t_idx;
+              rp0[u] = i < nk ? __ldg(d.rowptr + ri) : 0;
+              rp1[u] = i < nk ? __ldg(d.rowptr + ri + 1) : 0;
+              prs[u] = (i < nk && stdp_run) ? __ldcg(pub + key) : 0.0f;
+            }
+#pragma unroll
+            for (int u = 0; u < KPL; ++u) {
+              const int i = u * 32 + lane;
+              if (i < nk) {
+                const int len = rp1[u] - rp0[u];
+                kst[i] = rp0[u];
+                koff[i] = len;
+                kfl[i] = lvs[u];
+                kpre[i] = prs[u];
+                if (lvs[u] >> 31) ev += (unsigned long long)len;
+              }
+            }
           }
           __syncwarp();
           // exclusive prefix of the sub-row lengths
@@ -499,10 +511,16 @@ __global__ void __launch_bounds__(512, 1)
           __syncwarp();
           for (int f0 = 0; f0 < total_e; f0 += STAGE_ENTRIES) {
             const int nf = min(STAGE_ENTRIES, total_e - f0);
-            for (int f = lane; f < nf; f += 32) {
-              const int j = find_segment(koff, nk, f0 + f);
-              sidx[f] = (unsigned short)j;
-              cp_async8(stage + f, d.entries + kst[j] + (f0 + f - koff[j]));
+            // each lane copies the part of its own sub-rows that falls in this
+            // round's window [f0, f0 + nf) (no search per entry)
+            for (int i = lane; i < nk; i += 32) {
+              const int o = koff[i];
+              const int e0 = max(o, f0), e1 = min(o + (i + 1 < nk ? koff[i + 1] - o : total_e - o), f0 + nf);
+              const int base = kst[i] - o;
+              for (int f = e0; f < e1; ++f) {
+                sidx[f - f0] = (unsigned short)i;
+                cp_async8(stage + (f - f0), d.entries + base + f);
+              }
             }
             cp_async_wait_all();
             __syncwarp();

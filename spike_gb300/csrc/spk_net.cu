@@ -132,13 +132,14 @@ static int make_plan(int N, int Nin, int B, int L, int kind, int stdp, const spk
     }
     return SPK_OK;
   }
-  // one CTA when the whole network fits
-  for (int W : {16, 8}) {
-    const int TS = std::max(32, ((N + W - 1) / W + 31) / 32 * 32);
-    if (TS <= 65504 && finish(W, TS, 1)) return SPK_OK;
+  // The step is latency-bound: the smallest tiles (most warps working in
+  // parallel) win while the CTAs fit one per SM.
+  if (N <= 16 * 32) {
+    const int W = (N + 31) / 32;
+    if (finish(W, 32, 1)) return SPK_OK;
   }
   const int W = 8;
-  for (int TS : {64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096}) {
+  for (int TS : {32, 64, 96, 128, 160, 192, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096}) {
     int C = (N + W * TS - 1) / (W * TS);
     if (C > di.sms) continue;
     if (finish(W, TS, C)) return SPK_OK;
