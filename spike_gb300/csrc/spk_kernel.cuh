@@ -65,6 +65,11 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
 }
+// Barrier 1 over the whole CTA: releases and retires list rounds between warp 0
+// (the list builder) and the other warps, which reach it from different code.
+__device__ __forceinline__ void round_barrier(int nthreads) {
+  asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
@@ -87,36 +92,6 @@ __device__ __forceinline__ bool poll_word(const unsigned long long* p, unsigned 
       return false;
     }
   }
-}
-
-// Exclusive block-wide scan of one int per thread; returns the prefix and the
-// total in *total.  scratch needs 33 ints.
-__device__ int block_exclusive_scan(int v, int* scratch, int* total) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  int x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(FULL, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) scratch[warp] = x;
-  __syncthreads();
-  if (warp == 0) {
-    int s = lane < nw ? scratch[lane] : 0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(FULL, s, o);
-      if (lane >= o) s += y;
-    }
-    if (lane < nw) scratch[lane] = s;  // inclusive warp totals
-    if (lane == nw - 1) scratch[32] = s;
-  }
-  __syncthreads();
-  const int before = warp > 0 ? scratch[warp - 1] : 0;
-  *total = scratch[32];
-  const int r = before + x - v;
-  __syncthreads();
-  return r;
 }
 
 // ltp_and_ltd update of one synapse for G = 1
@@ -143,6 +118,7 @@ __global__ void __launch_bounds__(512, 1)
     step_kernel(const NetDev* __restrict__ nets, const CtaMap* __restrict__ map, int K) {
   extern __shared__ __align__(16) uint32_t sm[];
   __shared__ float s_decay[MAX_LABELS + 1], s_vhat[MAX_LABELS + 1], s_scale[MAX_CLASSES];
+  __shared__ int s_round[4];  // keys in the round, last round, poll ok
   const CtaMap cm = map[blockIdx.x];
   const NetDev& d = nets[cm.net];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -158,7 +134,6 @@ __global__ void __launch_bounds__(512, 1)
   const float dt = d.dt;
 
   uint32_t* list = sm;
-  int* scan = (int*)(sm + LIST_CAP);
   const WarpLayout wl = warp_layout(B, TS, L, ITS, kind, d.has_stdp);
   uint32_t* wreg = sm + SHARED_WORDS + w * wl.total;
   uint2* stage = (uint2*)(wreg + wl.stage);
@@ -184,7 +159,7 @@ __global__ void __launch_bounds__(512, 1)
   const int steps_here = min(K, ctl0.steps_total - ctl0.step);
   if (steps_here <= 0) return;
   const bool stdp_run = d.has_stdp && ctl0.plastic;
-  const bool recorder = cm.rank == 0 && w == W - 1 && d.spike_cap > 0;
+  const bool recorder = cm.rank == 0 && w == 0 && d.spike_cap > 0;
 
   const int t_idx = cm.rank * W + w;  // tile owned by this warp
   const int p0 = t_idx * TS;          // first post of the tile
@@ -380,86 +355,14 @@ __global__ void __launch_bounds__(512, 1)
       }
     }
 
-    // ---- phase B: poll the bitmap, list active keys (ascending) ---------------
-    const int nthreads = blockDim.x;
-    for (int wbase = 0; wbase < n_words && ok_run; wbase += nthreads * WPT_MAX) {
-      const int wchunk = min(n_words - wbase, nthreads * WPT_MAX);
-      const int wpt = (wchunk + nthreads - 1) / nthreads;
-      const int my0 = wbase + threadIdx.x * wpt;
-      uint32_t wA[WPT_MAX], wP[WPT_MAX];
-      int cnt = 0;
-      bool ok = true;
-      // first read every word with independent loads, then re-poll only the
-      // words whose producer has not published this step yet
-      unsigned long long va[WPT_MAX], vp[WPT_MAX];
-#pragma unroll
-      for (int i = 0; i < WPT_MAX; ++i) {
-        const bool mine = i < wpt && my0 + i < wbase + wchunk;
-        va[i] = mine ? ld_relaxed_u64(bitsA + my0 + i) : stamp_hi;
-        vp[i] = (mine && stdp_run) ? ld_relaxed_u64(bitsP + my0 + i) : stamp_hi;
-      }
-#pragma unroll
-      for (int i = 0; i < WPT_MAX; ++i) {
-        const bool mine = i < wpt && my0 + i < wbase + wchunk;
-        if (mine && ok && (unsigned)(va[i] >> 32) != stamp) ok = poll_word(bitsA + my0 + i, stamp, d, va[i]);
-        if (mine && ok && stdp_run && (unsigned)(vp[i] >> 32) != stamp)
-          ok = poll_word(bitsP + my0 + i, stamp, d, vp[i]);
-        wA[i] = mine ? (uint32_t)va[i] : 0u;
-        wP[i] = (mine && stdp_run) ? (uint32_t)vp[i] : 0u;
-        cnt += __popc(wA[i] | wP[i]);
-      }
-      if (stdp_run) fence_acq_rel_gpu();  // the pre traces published with the words
-      if (__syncthreads_or(!ok)) {
-        ok_run = false;
-        break;
-      }
-      int total;
-      const int my_off = block_exclusive_scan(cnt, scan, &total);
-      for (int rbase = 0; rbase < total; rbase += LIST_CAP) {
-        const int n_round = min(LIST_CAP, total - rbase);
-        if (rbase > 0) __syncthreads();  // previous round fully consumed
-        int pos = my_off;
-#pragma unroll
-        for (int i = 0; i < WPT_MAX; ++i) {
-          uint32_t m = wA[i] | wP[i];
-          while (m) {
-            const int b = __ffs(m) - 1;
-            m &= m - 1;
-            if (pos >= rbase && pos < rbase + n_round) {
-              const uint32_t key = (uint32_t)((my0 + i) * 32 + b);
-              const uint32_t fl = (((wA[i] >> b) & 1u) << 31) | (((wP[i] >> b) & 1u) << 30);
-              list[pos - rbase] = key | fl;
-            }
-            ++pos;
-          }
-        }
-        __syncthreads();
-
-        // spike store: one warp of rank 0, in list (canonical) order
-        if (recorder) {
-          for (int c0 = 0; c0 < n_round; c0 += 32) {
-            const int j = c0 + lane;
-            bool rec = false;
-            uint32_t key = 0;
-            if (j < n_round) {
-              const uint32_t lv = list[j];
-              key = lv & 0x3fffffffu;
-              rec = (lv >> 31) && ((int)key >= KL || ctl0.record_inputs);
-            }
-            const unsigned m = __ballot_sync(FULL, rec);
-            if (rec) {
-              const unsigned long long p = spike_count + (unsigned long long)__popc(m & lanemask_lt());
-              if (p < (unsigned long long)d.spike_cap)
-                d.spikes[p] = make_uint2(key, __float_as_uint(t));
-              else
-                atomicCAS(&d.ctl->status, 0, SPK_ERR_OVERFLOW);
-            }
-            spike_count += (unsigned long long)__popc(m);
-          }
-          if (spike_count > (unsigned long long)d.spike_cap) spike_count = d.spike_cap;
-        }
-
-        // ---- each warp: stage its tile's sub-rows of the listed keys ----------
+    // ---- phase B: warp 0 polls the bitmap and lists the active keys ----------
+    // Warp 0 of each CTA reads the step's bitmap words (coalesced, eight words
+    // per lane in flight, re-polling only words not stamped yet), builds the
+    // list of active keys in ascending order in rounds of at most LIST_CAP
+    // keys, records spikes (rank 0), and releases each round to the CTA's
+    // other warps through a named barrier.  Every warp then stages and applies
+    // its tile's part of the round.
+    auto process_round = [&](const int n_round) {
         for (int kb = 0; kb < n_round; kb += STAGE_KEYS) {
           const int nk = min(STAGE_KEYS, n_round - kb);
           {
@@ -572,6 +475,114 @@ __global__ void __launch_bounds__(512, 1)
             __syncwarp();
           }
         }
+    };
+    const int nthreads = blockDim.x;
+    if (w == 0) {
+      int list_n = 0;
+      bool ok = true;
+      for (int cbase = 0; cbase < n_words && ok; cbase += 256) {
+        unsigned long long va[8], vp[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int wi = cbase + u * 32 + lane;
+          const bool mine = wi < n_words;
+          va[u] = mine ? ld_relaxed_u64(bitsA + wi) : stamp_hi;
+          vp[u] = (mine && stdp_run) ? ld_relaxed_u64(bitsP + wi) : stamp_hi;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int wi = cbase + u * 32 + lane;
+          if (wi < n_words && ok && (unsigned)(va[u] >> 32) != stamp) ok = poll_word(bitsA + wi, stamp, d, va[u]);
+          if (wi < n_words && ok && stdp_run && (unsigned)(vp[u] >> 32) != stamp)
+            ok = poll_word(bitsP + wi, stamp, d, vp[u]);
+        }
+        ok = __all_sync(FULL, ok);
+        if (!ok) break;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int wi = cbase + u * 32 + lane;
+          const uint32_t a = wi < n_words ? (uint32_t)va[u] : 0u;
+          const uint32_t p = (wi < n_words && stdp_run) ? (uint32_t)vp[u] : 0u;
+          uint32_t m = a | p;
+          const int c = __popc(m);
+          int incl = c;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const int tot = __shfl_sync(FULL, incl, 31);
+          if (tot == 0) continue;
+          if (list_n + tot > LIST_CAP) {
+            // the list is full: hand this round to the CTA, then go on
+            if (lane == 0) {
+              s_round[0] = list_n;
+              s_round[1] = 0;
+              s_round[2] = 1;
+            }
+            round_barrier(nthreads);
+            process_round(list_n);
+            round_barrier(nthreads);
+            list_n = 0;
+          }
+          int pos = list_n + incl - c;
+          const uint32_t wkey = (uint32_t)wi * 32u;
+          while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            list[pos++] = (wkey + b) | (((a >> b) & 1u) << 31) | (((p >> b) & 1u) << 30);
+          }
+          if (recorder) {
+            // spike store in canonical order: LIF keys, and inputs on request
+            const uint32_t r = ((int)wkey >= KL || ctl0.record_inputs) ? a : 0u;
+            const int rc = __popc(r);
+            int rincl = rc;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const int y = __shfl_up_sync(FULL, rincl, o);
+              if (lane >= o) rincl += y;
+            }
+            const int rtot = __shfl_sync(FULL, rincl, 31);
+            unsigned long long sp = spike_count + (unsigned long long)(rincl - rc);
+            uint32_t mm = r;
+            while (mm) {
+              const int b = __ffs(mm) - 1;
+              mm &= mm - 1;
+              if (sp < (unsigned long long)d.spike_cap)
+                d.spikes[sp] = make_uint2(wkey + b, __float_as_uint(t));
+              else
+                atomicCAS(&d.ctl->status, 0, SPK_ERR_OVERFLOW);
+              ++sp;
+            }
+            spike_count += (unsigned long long)rtot;
+          }
+          list_n += tot;
+        }
+      }
+      if (recorder && spike_count > (unsigned long long)d.spike_cap) spike_count = d.spike_cap;
+      if (stdp_run && ok) fence_acq_rel_gpu();  // the pre traces published with the words
+      if (lane == 0) {
+        s_round[0] = list_n;
+        s_round[1] = 1;
+        s_round[2] = ok ? 1 : 0;
+      }
+      round_barrier(nthreads);
+      if (ok)
+        process_round(list_n);
+      else
+        ok_run = false;
+    } else {
+      while (true) {
+        round_barrier(nthreads);
+        const int n = s_round[0];
+        const bool last = s_round[1] != 0;
+        if (s_round[2] == 0) {
+          ok_run = false;
+          break;
+        }
+        process_round(n);
+        if (last) break;
+        round_barrier(nthreads);
       }
     }
     if (!ok_run) break;
@@ -640,7 +651,7 @@ __global__ void __launch_bounds__(512, 1)
     for (int o = 16; o >= 1; o >>= 1) e += __shfl_xor_sync(FULL, e, o);
     if (lane == 0 && e) atomicAdd(&d.ctl->events, e);
   }
-  if (recorder || (cm.rank == 0 && w == W - 1)) {
+  if (cm.rank == 0 && w == 0) {
     if (lane == 0) {
       d.ctl->step = ctl0.step + steps_done;
       d.ctl->gstep = ctl0.gstep + steps_done;
