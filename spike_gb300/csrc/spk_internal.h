@@ -72,13 +72,20 @@ struct NetDev {
   float* post_trace;   // [N]
   float* pre_trace;    // [n_keys] own copy (home)
   float* pre_pub;      // [2][n_keys] published each step for other CTAs
-  // Spike bitmaps, double-buffered by step parity.  Each 64-bit word holds 32
-  // key bits in its low half and the step stamp (global step + 1) in its high
-  // half, written with one release store: a consumer that sees the stamp sees
-  // the bits, so polling the words is the step's only synchronization.
-  unsigned long long* bitsA;  // [2][n_words] spikes of the step
-  unsigned long long* bitsP;  // [2][n_words] STDP pre events of the step
-  uint2* spikes;              // spike store (key, float time bits)
+  // Per-step exchange between the CTAs of a network, double-buffered by step
+  // parity.  CTA r writes its active keys (key | spike << 31 | pre-event << 30),
+  // inputs first then neurons, each part ascending, into cta_keys[par][r][*],
+  // then one stamp word (step + 1) << 32 | inputs << 16 | neurons into
+  // cta_stamp[par][r] after a fence.  Consumers poll the stamps and gather the
+  // keys: the step's only inter-CTA synchronization.
+  uint32_t* cta_keys;               // [2][nctas][key_cap]
+  unsigned long long* cta_stamp;    // [2][nctas]
+  int key_cap;                      // W * (TS + ITS)
+  // Spike / pre-event bitmaps of the step (plastic runs only), for the
+  // post-spike STDP pass to look up arbitrary presynaptic keys.
+  uint32_t* bitsA;  // [2][n_words]
+  uint32_t* bitsP;  // [2][n_words]
+  uint2* spikes;    // spike store (key, float time bits)
   long long spike_cap;
   RunCtl* ctl;
   int* abort_flag;            // shared by a launch: set on timeout
@@ -119,9 +126,11 @@ SPK_HD WarpLayout warp_layout(int B, int TS, int L, int ITS, int kind, int has_s
   w.total = o;
   return w;
 }
-// CTA-shared words: active list, scan scratch, flags (multiple of 4 words so
-// every warp region starts 16-byte aligned).
-constexpr int SHARED_WORDS = LIST_CAP + 64 + 8;
+// CTA-shared words: active list, per-source-segment offsets of the key gather
+// (2 segments per CTA of the network), flags; a multiple of 4 words so every
+// warp region starts 16-byte aligned.
+constexpr int MAX_CTAS_PER_NET = 256;
+constexpr int SHARED_WORDS = LIST_CAP + 2 * MAX_CTAS_PER_NET + 8;
 SPK_HD int smem_bytes(int W, const WarpLayout& wl) { return 4 * (SHARED_WORDS + W * wl.total); }
 
 }  // namespace spk

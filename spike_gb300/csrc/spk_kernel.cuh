@@ -61,6 +61,10 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
   return m;
 }
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
@@ -72,26 +76,6 @@ __device__ __forceinline__ void round_barrier(int nthreads) {
 }
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
-}
-
-// Wait until a bitmap word carries the expected stamp; returns false on
-// timeout or abort (then the launch's abort flag and the status are set).
-__device__ __forceinline__ bool poll_word(const unsigned long long* p, unsigned stamp, const NetDev& d,
-                                          unsigned long long& v) {
-  v = ld_relaxed_u64(p);
-  if ((unsigned)(v >> 32) == stamp) return true;
-  const unsigned long long t0 = globaltimer();
-  while (true) {
-    __nanosleep(32);
-    v = ld_relaxed_u64(p);
-    if ((unsigned)(v >> 32) == stamp) return true;
-    if (ld_volatile(d.abort_flag)) return false;
-    if (globaltimer() - t0 > POLL_TIMEOUT_NS) {
-      atomicExch(d.abort_flag, 1);
-      atomicCAS(&d.ctl->status, 0, SPK_ERR_TIMEOUT);
-      return false;
-    }
-  }
 }
 
 // ltp_and_ltd update of one synapse for G = 1
@@ -134,6 +118,7 @@ __global__ void __launch_bounds__(512, 1)
   const float dt = d.dt;
 
   uint32_t* list = sm;
+  int* segoff = (int*)(sm + LIST_CAP);  // [2 * nctas + 1] offsets of the gather segments
   const WarpLayout wl = warp_layout(B, TS, L, ITS, kind, d.has_stdp);
   uint32_t* wreg = sm + SHARED_WORDS + w * wl.total;
   uint2* stage = (uint2*)(wreg + wl.stage);
@@ -222,8 +207,8 @@ __global__ void __launch_bounds__(512, 1)
     const int par = (int)(gs & 1);
     const unsigned stamp = (unsigned)(gs + 1);
     const unsigned long long stamp_hi = (unsigned long long)stamp << 32;
-    unsigned long long* bitsA = d.bitsA + (size_t)par * n_words;
-    unsigned long long* bitsP = d.bitsP + (size_t)par * n_words;
+    uint32_t* bitsA = d.bitsA + (size_t)par * n_words;
+    uint32_t* bitsP = d.bitsP + (size_t)par * n_words;
     float* pub = d.pre_pub + (size_t)par * n_keys;
     const int slot = T % B;
     const float tg = t + 0.0f * dt;  // t + g*timestep with g = 0
@@ -331,37 +316,79 @@ __global__ void __launch_bounds__(512, 1)
     }
     inputs_active = true;
 
-    // ---- publish the tile's words: stamp and bits in one 64-bit store ---------
-    // Without plasticity the word is the only data another CTA reads, so a
-    // relaxed store suffices; with plasticity one fence per warp orders the
-    // published pre traces before the words (fence + strong store = release).
+    // ---- publish: the CTA's active keys, then one stamp word per CTA ---------
     __syncwarp();
-    if (stdp_run) fence_acq_rel_gpu();
-    {
+    if (stdp_run) {
+      // bitmaps for the post-spike pass, which looks up arbitrary pre keys
       const int nl = TS >> 5, ni = ITS >> 5;
       for (int i = lane; i < nl + ni; i += 32) {
-        uint32_t wa, wp;
-        int wi;
         if (i < nl) {
-          wa = wp = spkw_s[i];
-          wi = ((KL + p0) >> 5) + i;
+          const int wi = ((KL + p0) >> 5) + i;
+          bitsA[wi] = spkw_s[i];
+          bitsP[wi] = spkw_s[i];
         } else {
-          wa = inw_s[i - nl];
-          wp = inwp_s[i - nl];
-          wi = (kin0 >> 5) + (i - nl);
+          const int wi = (kin0 >> 5) + (i - nl);
+          bitsA[wi] = inw_s[i - nl];
+          bitsP[wi] = inwp_s[i - nl];
         }
-        if (stdp_run) st_relaxed_u64(bitsP + wi, stamp_hi | wp);
-        st_relaxed_u64(bitsA + wi, stamp_hi | wa);
       }
     }
+    __syncthreads();  // every warp's words are in shared memory, its traces written
+    if (w == 0) {
+      const int ni = ITS >> 5, nl = TS >> 5;
+      const int nw_in = W * ni, nw_all = W * (ni + nl);
+      uint32_t* keys_out = d.cta_keys + ((size_t)par * d.nctas + cm.rank) * d.key_cap;
+      int pos = 0, n_in = 0;
+      for (int x0 = 0; x0 < nw_all; x0 += 32) {
+        const int x = x0 + lane;
+        uint32_t a = 0u, p = 0u, wkey = 0u;
+        if (x < nw_in) {
+          const int wx = x / ni, k = x - (x / ni) * ni;
+          const uint32_t* r = sm + SHARED_WORDS + wx * wl.total;
+          a = r[wl.inw + k];
+          p = stdp_run ? r[wl.inwp + k] : 0u;
+          wkey = (uint32_t)((cm.rank * W + wx) * ITS + k * 32);
+        } else if (x < nw_all) {
+          const int y = x - nw_in;
+          const int wx = y / nl, k = y - (y / nl) * nl;
+          const uint32_t* r = sm + SHARED_WORDS + wx * wl.total;
+          a = r[wl.spkw + k];
+          p = stdp_run ? a : 0u;
+          wkey = (uint32_t)(KL + (cm.rank * W + wx) * TS + k * 32);
+        }
+        uint32_t m = a | p;
+        const int c = __popc(m);
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(FULL, incl, o);
+          if (lane >= o) incl += y;
+        }
+        int o = pos + incl - c;
+        while (m) {
+          const int b = __ffs(m) - 1;
+          m &= m - 1;
+          keys_out[o++] = (wkey + b) | (((a >> b) & 1u) << 31) | (((p >> b) & 1u) << 30);
+        }
+        n_in += __reduce_add_sync(FULL, x < nw_in ? c : 0);
+        pos += __shfl_sync(FULL, incl, 31);
+      }
+      // each lane's key stores, and (through the CTA barrier) the other warps'
+      // traces and bitmap words, are ordered before the stamp
+      fence_acq_rel_gpu();
+      __syncwarp();
+      if (lane == 0)
+        st_relaxed_u64(d.cta_stamp + (size_t)par * d.nctas + cm.rank,
+                       stamp_hi | ((unsigned long long)n_in << 16) | (unsigned long long)(pos - n_in));
+    }
 
-    // ---- phase B: warp 0 polls the bitmap and lists the active keys ----------
-    // Warp 0 of each CTA reads the step's bitmap words (coalesced, eight words
-    // per lane in flight, re-polling only words not stamped yet), builds the
-    // list of active keys in ascending order in rounds of at most LIST_CAP
-    // keys, records spikes (rank 0), and releases each round to the CTA's
-    // other warps through a named barrier.  Every warp then stages and applies
-    // its tile's part of the round.
+    // ---- phase B: warp 0 gathers the step's active keys from every CTA ------
+    // It polls the stamps of all the network's CTAs (all pending loads in
+    // flight at once, bounded by a timeout), gathers their keys in ascending
+    // order (inputs of CTA 0..C-1, then neurons of CTA 0..C-1) into the list
+    // in rounds of at most LIST_CAP keys, records spikes (rank 0), and
+    // releases each round to the CTA's other warps through a named barrier.
+    // Every warp then stages and applies its tile's part of the round.
     auto process_round = [&](const int n_round) {
         for (int kb = 0; kb < n_round; kb += STAGE_KEYS) {
           const int nk = min(STAGE_KEYS, n_round - kb);
@@ -478,99 +505,124 @@ __global__ void __launch_bounds__(512, 1)
     };
     const int nthreads = blockDim.x;
     if (w == 0) {
-      int list_n = 0;
+      const int C = d.nctas;
+      const unsigned long long* stp = d.cta_stamp + (size_t)par * C;
+      constexpr int SPL = MAX_CTAS_PER_NET / 32;
+      unsigned long long sv[SPL];
       bool ok = true;
-      for (int cbase = 0; cbase < n_words && ok; cbase += 256) {
-        unsigned long long va[8], vp[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int wi = cbase + u * 32 + lane;
-          const bool mine = wi < n_words;
-          va[u] = mine ? ld_relaxed_u64(bitsA + wi) : stamp_hi;
-          vp[u] = (mine && stdp_run) ? ld_relaxed_u64(bitsP + wi) : stamp_hi;
+      for (int u = 0; u < SPL; ++u) {
+        const int r = u * 32 + lane;
+        sv[u] = r < C ? ld_relaxed_u64(stp + r) : stamp_hi;
+      }
+      unsigned long long t0 = 0ull;
+      while (true) {
+        bool pending = false;
+#pragma unroll
+        for (int u = 0; u < SPL; ++u) pending |= (unsigned)(sv[u] >> 32) != stamp;
+        if (!__any_sync(FULL, pending)) break;
+        const unsigned long long now = globaltimer();
+        if (t0 == 0ull) t0 = now;
+        if (now - t0 > POLL_TIMEOUT_NS || ld_volatile(d.abort_flag)) {
+          if (lane == 0 && now - t0 > POLL_TIMEOUT_NS) {
+            atomicExch(d.abort_flag, 1);
+            atomicCAS(&d.ctl->status, 0, SPK_ERR_TIMEOUT);
+          }
+          ok = false;
+          break;
         }
+        __nanosleep(32);
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int wi = cbase + u * 32 + lane;
-          if (wi < n_words && ok && (unsigned)(va[u] >> 32) != stamp) ok = poll_word(bitsA + wi, stamp, d, va[u]);
-          if (wi < n_words && ok && stdp_run && (unsigned)(vp[u] >> 32) != stamp)
-            ok = poll_word(bitsP + wi, stamp, d, vp[u]);
+        for (int u = 0; u < SPL; ++u) {
+          const int r = u * 32 + lane;
+          if (r < C && (unsigned)(sv[u] >> 32) != stamp) sv[u] = ld_relaxed_u64(stp + r);
         }
-        ok = __all_sync(FULL, ok);
-        if (!ok) break;
+      }
+      int total = 0;
+      if (ok) {
+        fence_acq_rel_gpu();  // keys, traces and bitmaps published before the stamps
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int wi = cbase + u * 32 + lane;
-          const uint32_t a = wi < n_words ? (uint32_t)va[u] : 0u;
-          const uint32_t p = (wi < n_words && stdp_run) ? (uint32_t)vp[u] : 0u;
-          uint32_t m = a | p;
-          const int c = __popc(m);
-          int incl = c;
+        for (int u = 0; u < SPL; ++u) {
+          const int r = u * 32 + lane;
+          if (r < C) {
+            segoff[r] = (int)((sv[u] >> 16) & 0xffffu);
+            segoff[C + r] = (int)(sv[u] & 0xffffu);
+          }
+        }
+        __syncwarp();
+        int carry = 0;
+        for (int i0 = 0; i0 < 2 * C; i0 += 32) {
+          const int i = i0 + lane;
+          const int cnt = i < 2 * C ? segoff[i] : 0;
+          int incl = cnt;
 #pragma unroll
           for (int o = 1; o < 32; o <<= 1) {
             const int y = __shfl_up_sync(FULL, incl, o);
             if (lane >= o) incl += y;
           }
-          const int tot = __shfl_sync(FULL, incl, 31);
-          if (tot == 0) continue;
-          if (list_n + tot > LIST_CAP) {
-            // the list is full: hand this round to the CTA, then go on
-            if (lane == 0) {
-              s_round[0] = list_n;
-              s_round[1] = 0;
-              s_round[2] = 1;
-            }
-            round_barrier(nthreads);
-            process_round(list_n);
-            round_barrier(nthreads);
-            list_n = 0;
-          }
-          int pos = list_n + incl - c;
-          const uint32_t wkey = (uint32_t)wi * 32u;
-          while (m) {
-            const int b = __ffs(m) - 1;
-            m &= m - 1;
-            list[pos++] = (wkey + b) | (((a >> b) & 1u) << 31) | (((p >> b) & 1u) << 30);
-          }
-          if (recorder) {
-            // spike store in canonical order: LIF keys, and inputs on request
-            const uint32_t r = ((int)wkey >= KL || ctl0.record_inputs) ? a : 0u;
-            const int rc = __popc(r);
-            int rincl = rc;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-              const int y = __shfl_up_sync(FULL, rincl, o);
-              if (lane >= o) rincl += y;
-            }
-            const int rtot = __shfl_sync(FULL, rincl, 31);
-            unsigned long long sp = spike_count + (unsigned long long)(rincl - rc);
-            uint32_t mm = r;
-            while (mm) {
-              const int b = __ffs(mm) - 1;
-              mm &= mm - 1;
-              if (sp < (unsigned long long)d.spike_cap)
-                d.spikes[sp] = make_uint2(wkey + b, __float_as_uint(t));
-              else
-                atomicCAS(&d.ctl->status, 0, SPK_ERR_OVERFLOW);
-              ++sp;
-            }
-            spike_count += (unsigned long long)rtot;
-          }
-          list_n += tot;
+          __syncwarp();
+          if (i < 2 * C) segoff[i] = carry + incl - cnt;
+          carry += __shfl_sync(FULL, incl, 31);
         }
+        if (lane == 0) segoff[2 * C] = carry;
+        total = carry;
+        __syncwarp();
       }
-      if (recorder && spike_count > (unsigned long long)d.spike_cap) spike_count = d.spike_cap;
-      if (stdp_run && ok) fence_acq_rel_gpu();  // the pre traces published with the words
-      if (lane == 0) {
-        s_round[0] = list_n;
-        s_round[1] = 1;
-        s_round[2] = ok ? 1 : 0;
+      for (int rbase = 0;; rbase += LIST_CAP) {
+        const int n_round = ok ? min(LIST_CAP, total - rbase) : 0;
+        if (ok) {
+          // gather the round's keys: each lane copies its segments' part
+          for (int i = lane; i < 2 * C; i += 32) {
+            const int o0 = segoff[i], o1 = segoff[i + 1];
+            const int a0 = max(o0, rbase), a1 = min(o1, rbase + n_round);
+            if (a0 < a1) {
+              const int r = i < C ? i : i - C;
+              const int skip = i < C ? 0 : segoff[r + 1] - segoff[r];  // neurons follow the CTA's inputs
+              const uint32_t* src = d.cta_keys + ((size_t)par * C + r) * d.key_cap + skip - o0;
+              for (int x = a0; x < a1; ++x) cp_async4(list + (x - rbase), src + x);
+            }
+          }
+          cp_async_wait_all();
+          __syncwarp();
+          if (recorder) {
+            // spike store in canonical order: neurons, and inputs on request
+            for (int c0 = 0; c0 < n_round; c0 += 32) {
+              const int j = c0 + lane;
+              bool rec = false;
+              uint32_t key = 0u;
+              if (j < n_round) {
+                const uint32_t lv = list[j];
+                key = lv & 0x3fffffffu;
+                rec = (lv >> 31) && ((int)key >= KL || ctl0.record_inputs);
+              }
+              const unsigned m = __ballot_sync(FULL, rec);
+              if (rec) {
+                const unsigned long long sp = spike_count + (unsigned long long)__popc(m & lanemask_lt());
+                if (sp < (unsigned long long)d.spike_cap)
+                  d.spikes[sp] = make_uint2(key, __float_as_uint(t));
+                else
+                  atomicCAS(&d.ctl->status, 0, SPK_ERR_OVERFLOW);
+              }
+              spike_count += (unsigned long long)__popc(m);
+            }
+            if (spike_count > (unsigned long long)d.spike_cap) spike_count = d.spike_cap;
+          }
+        }
+        const bool last = !ok || rbase + LIST_CAP >= total;
+        if (lane == 0) {
+          s_round[0] = n_round;
+          s_round[1] = last ? 1 : 0;
+          s_round[2] = ok ? 1 : 0;
+        }
+        round_barrier(nthreads);
+        if (!ok) {
+          ok_run = false;
+          break;
+        }
+        process_round(n_round);
+        if (last) break;
+        round_barrier(nthreads);
       }
-      round_barrier(nthreads);
-      if (ok)
-        process_round(list_n);
-      else
-        ok_run = false;
     } else {
       while (true) {
         round_barrier(nthreads);
@@ -600,9 +652,9 @@ __global__ void __launch_bounds__(512, 1)
           for (int a = a0 + lane; a < a1; a += 32) {
             const uint2 cc = __ldg(d.csc + a);
             const int pk = (int)cc.y;
-            const unsigned long long va = ld_relaxed_u64(bitsA + (pk >> 5));
-            const unsigned long long vp = ld_relaxed_u64(bitsP + (pk >> 5));
-            if ((((uint32_t)va | (uint32_t)vp) >> (pk & 31)) & 1u) continue;  // handled in the pre pass
+            const uint32_t va = __ldcg(bitsA + (pk >> 5));
+            const uint32_t vp = __ldcg(bitsP + (pk >> 5));
+            if (((va | vp) >> (pk & 31)) & 1u) continue;  // handled in the pre pass
             const float old = __uint_as_float(d.entries[cc.x].y);
             const float prt = __ldcg(pub + pk);
             const float nw = stdp_update(d, old, false, true, post_s[ql], prt);

@@ -108,7 +108,9 @@ static int make_plan(int N, int Nin, int B, int L, int kind, int stdp, const spk
     p->n_keys = p->KL + p->n_tiles * TS;
     p->n_words = p->n_keys / 32;
     p->smem = plan_bytes(B, TS, L, p->ITS, kind, stdp, W);
-    return p->smem <= di.max_smem && (int64_t)p->n_tiles * TS >= N;
+    // per-CTA key counts travel in 16-bit fields of the stamp word
+    return p->smem <= di.max_smem && (int64_t)p->n_tiles * TS >= N && nctas <= MAX_CTAS_PER_NET &&
+           W * TS <= 65535 && W * p->ITS <= 65535;
   };
   const int K = (s && s->steps_per_launch > 0) ? s->steps_per_launch : DEFAULT_STEPS_PER_LAUNCH;
   p->K = K;
@@ -499,6 +501,8 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
   void* p_V = nullptr; void* p_last = nullptr; void* p_gtr = nullptr; void* p_ring = nullptr;
   void* p_innext = nullptr; void* p_rates = nullptr; void* p_post = nullptr; void* p_pre = nullptr;
   void* p_pub = nullptr; void* p_bA = nullptr; void* p_bP = nullptr; void* p_spk = nullptr;
+  void* p_ckeys = nullptr; void* p_cstamp = nullptr;
+  const int key_cap = plan.W * (plan.TS + plan.ITS);
   void* p_ctl = nullptr; void* p_abort = nullptr; void* p_dd = nullptr; void* p_map = nullptr;
   std::vector<Part> parts = {
       {&p_rowptr, sizeof(int32_t) * rowptr.size()},
@@ -514,8 +518,10 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
       {&p_post, sizeof(float) * (stdp ? N : 0)},
       {&p_pre, sizeof(float) * (stdp ? n_keys : 0)},
       {&p_pub, sizeof(float) * (stdp ? 2 * (size_t)n_keys : 0)},
-      {&p_bA, sizeof(unsigned long long) * 2 * (size_t)n_words},
-      {&p_bP, sizeof(unsigned long long) * 2 * (size_t)n_words},
+      {&p_bA, sizeof(uint32_t) * 2 * (size_t)n_words},
+      {&p_bP, sizeof(uint32_t) * 2 * (size_t)n_words},
+      {&p_ckeys, sizeof(uint32_t) * 2 * (size_t)plan.nctas * key_cap},
+      {&p_cstamp, sizeof(unsigned long long) * 2 * (size_t)plan.nctas},
       {&p_spk, sizeof(uint2) * (size_t)std::max<int64_t>(spike_cap, 1)},
       {&p_ctl, sizeof(RunCtl)},
       {&p_abort, sizeof(int)},
@@ -620,8 +626,11 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
   h.post_trace = (float*)p_post;
   h.pre_trace = (float*)p_pre;
   h.pre_pub = (float*)p_pub;
-  h.bitsA = (unsigned long long*)p_bA;
-  h.bitsP = (unsigned long long*)p_bP;
+  h.bitsA = (uint32_t*)p_bA;
+  h.bitsP = (uint32_t*)p_bP;
+  h.cta_keys = (uint32_t*)p_ckeys;
+  h.cta_stamp = (unsigned long long*)p_cstamp;
+  h.key_cap = key_cap;
   h.spikes = (uint2*)p_spk;
   h.spike_cap = spike_cap;
   h.ctl = (RunCtl*)p_ctl;
@@ -649,8 +658,9 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
   urc |= up(p_dd, &h, sizeof(h));
   urc |= up(p_map, map.data(), sizeof(CtaMap) * map.size());
   if (urc) return fail_free(SPK_ERR_CUDA);
-  if (cudaMemsetAsync(p_bA, 0, sizeof(unsigned long long) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
-      cudaMemsetAsync(p_bP, 0, sizeof(unsigned long long) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
+  if (cudaMemsetAsync(p_bA, 0, sizeof(uint32_t) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
+      cudaMemsetAsync(p_bP, 0, sizeof(uint32_t) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
+      cudaMemsetAsync(p_cstamp, 0, sizeof(unsigned long long) * 2 * (size_t)plan.nctas, n->stream) != cudaSuccess ||
       cudaMemsetAsync(p_abort, 0, sizeof(int), n->stream) != cudaSuccess) {
     set_error("cudaMemsetAsync failed");
     return fail_free(SPK_ERR_CUDA);
