@@ -61,6 +61,16 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
   return m;
 }
+// Bulk prefetch of a byte range into L2 (the TMA engine's L2 prefetch); the
+// range is widened to 16-byte boundaries.
+__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes) {
+  const uintptr_t a = (uintptr_t)p & ~(uintptr_t)15;
+  const uintptr_t e = ((uintptr_t)p + bytes + 15) & ~(uintptr_t)15;
+  for (uintptr_t c = a; c < e; c += (1u << 20)) {
+    const unsigned n = (unsigned)min((uintptr_t)(1u << 20), e - c);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(c), "r"(n) : "memory");
+  }
+}
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
@@ -380,6 +390,17 @@ __global__ void __launch_bounds__(512, 1)
       if (lane == 0)
         st_relaxed_u64(d.cta_stamp + (size_t)par * d.nctas + cm.rank,
                        stamp_hi | ((unsigned long long)n_in << 16) | (unsigned long long)(pos - n_in));
+      // Every CTA of the network will read the row pointers and the synapse
+      // row of these keys this step: pull them into L2 now, while the stamps
+      // travel (one bulk prefetch per row).
+      for (int i = lane; i < pos; i += 32) {
+        const int key = (int)(keys_out[i] & 0x3fffffffu);
+        if (!((keys_out[i] >> 31) & 1u) && !stdp_run) continue;
+        const int* rp = d.rowptr + (size_t)key * n_tiles;
+        prefetch_l2(rp, sizeof(int) * (size_t)(n_tiles + 1));
+        const int e0 = __ldg(rp), e1 = __ldg(rp + n_tiles);
+        if (e1 > e0) prefetch_l2(d.entries + e0, sizeof(uint2) * (size_t)(e1 - e0));
+      }
     }
 
     // ---- phase B: warp 0 gathers the step's active keys from every CTA ------
