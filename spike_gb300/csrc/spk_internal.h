@@ -17,6 +17,7 @@ constexpr int LIST_CAP = 1024;     // active presynaptic keys listed per round
 constexpr int WPT_MAX = 16;        // bitmap words held per thread while listing
 constexpr int STAGE_KEYS = 64;     // sub-rows staged per warp per round
 constexpr int STAGE_ENTRIES = 256; // synapse entries staged per warp per round
+constexpr int APPLY_TAGS = 256;    // cell-hash slots of the ordered apply
 
 // Packed synapse entry: x = post_local[0:16) | delay[16:24) | label[24:28) |
 // class[28:32), y = float bits of the value (w*scale for class 0, w otherwise).
@@ -73,12 +74,13 @@ struct NetDev {
   float* pre_trace;    // [n_keys] own copy (home)
   float* pre_pub;      // [2][n_keys] published each step for other CTAs
   // Per-step exchange between the CTAs of a network, double-buffered by step
-  // parity.  CTA r writes its active keys (key | spike << 31 | pre-event << 30),
-  // inputs first then neurons, each part ascending, into cta_keys[par][r][*],
-  // then one stamp word (step + 1) << 32 | inputs << 16 | neurons into
-  // cta_stamp[par][r] after a fence.  Consumers poll the stamps and gather the
-  // keys: the step's only inter-CTA synchronization.
-  uint32_t* cta_keys;               // [2][nctas][key_cap]
+  // parity.  CTA r writes its active keys, inputs first then neurons, each part
+  // ascending, into cta_keys[par][r][*] as (step + 1) << 32 | key | spike << 31
+  // | pre-event << 30, and one stamp word (step + 1) << 32 | inputs << 16 |
+  // neurons into cta_stamp[par][r].  Every word carries its step, so a
+  // consumer that polls the stamps and then the keys needs no fence in
+  // between: the step's only inter-CTA synchronization.
+  unsigned long long* cta_keys;     // [2][nctas][key_cap]
   unsigned long long* cta_stamp;    // [2][nctas]
   int key_cap;                      // W * (TS + ITS)
   // Spike / pre-event bitmaps of the step (plastic runs only), for the
@@ -98,7 +100,7 @@ struct CtaMap {
 
 // Per-warp shared-memory words for a schedule (4-byte words).
 struct WarpLayout {
-  int stage, sidx, kst, koff, kfl, kpre, ring, V, last, gtr, post_tr, pre_tr, spkw, inw, inwp, in_next,
+  int stage, sidx, kst, koff, kfl, kpre, tag, ring, V, last, gtr, post_tr, pre_tr, spkw, inw, inwp, in_next,
       in_rate, in_pre, total;
 };
 SPK_HD WarpLayout warp_layout(int B, int TS, int L, int ITS, int kind, int has_stdp) {
@@ -110,6 +112,7 @@ SPK_HD WarpLayout warp_layout(int B, int TS, int L, int ITS, int kind, int has_s
   w.koff = o; o += STAGE_KEYS + 4;      // exclusive prefix of sub-row lengths
   w.kfl = o; o += STAGE_KEYS;           // list word (key | spike | pre-event flags)
   w.kpre = o; o += STAGE_KEYS;          // presynaptic STDP trace of the step
+  w.tag = o; o += APPLY_TAGS;           // lowest lane per cell hash (ordered apply)
   w.ring = o; o += B * TS * L;
   w.V = o; o += TS;
   w.last = o; o += TS;

@@ -88,6 +88,27 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
+// Re-read a stamped word until it carries `stamp`; bounded by the poll timeout
+// and the launch's abort flag (ok turns false, the status records a timeout).
+__device__ __forceinline__ unsigned long long repoll(const unsigned long long* p, unsigned long long v,
+                                                     unsigned stamp, const NetDev& d, bool& ok) {
+  unsigned long long t0 = 0ull;
+  while (ok && (unsigned)(v >> 32) != stamp) {
+    const unsigned long long now = globaltimer();
+    if (t0 == 0ull) t0 = now;
+    if (ld_volatile(d.abort_flag)) {
+      ok = false;
+    } else if (now - t0 > POLL_TIMEOUT_NS) {
+      atomicExch(d.abort_flag, 1);
+      atomicCAS(&d.ctl->status, 0, SPK_ERR_TIMEOUT);
+      ok = false;
+    } else {
+      v = ld_relaxed_u64(p);
+    }
+  }
+  return v;
+}
+
 // ltp_and_ltd update of one synapse for G = 1
 // (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:132-151):
 // pre_ev/post_ev are "spike sub-step >= 0", the traces are this step's values.
@@ -137,6 +158,7 @@ __global__ void __launch_bounds__(512, 1)
   int* koff = (int*)(wreg + wl.koff);
   uint32_t* kfl = wreg + wl.kfl;
   float* kpre = (float*)(wreg + wl.kpre);
+  int* tag_s = (int*)(wreg + wl.tag);
   float* ring_s = (float*)(wreg + wl.ring);
   float* V_s = (float*)(wreg + wl.V);
   float* last_s = (float*)(wreg + wl.last);
@@ -154,7 +176,7 @@ __global__ void __launch_bounds__(512, 1)
   const int steps_here = min(K, ctl0.steps_total - ctl0.step);
   if (steps_here <= 0) return;
   const bool stdp_run = d.has_stdp && ctl0.plastic;
-  const bool recorder = cm.rank == 0 && w == 0 && d.spike_cap > 0;
+  const bool recorder = cm.rank == 0 && w == W - 1 && d.spike_cap > 0;  // off warp 0's path
 
   const int t_idx = cm.rank * W + w;  // tile owned by this warp
   const int p0 = t_idx * TS;          // first post of the tile
@@ -200,6 +222,7 @@ __global__ void __launch_bounds__(512, 1)
       if (d.has_stdp) inpre_s[i] = ok ? d.pre_trace[k] : 0.0f;
     }
   }
+  for (int i = lane; i < APPLY_TAGS; i += 32) tag_s[i] = 32;
   unsigned long long spike_count = ctl0.spike_count;
   unsigned long long ev = 0;
   bool inputs_active = ctl0.inputs_active != 0;
@@ -347,7 +370,7 @@ __global__ void __launch_bounds__(512, 1)
     if (w == 0) {
       const int ni = ITS >> 5, nl = TS >> 5;
       const int nw_in = W * ni, nw_all = W * (ni + nl);
-      uint32_t* keys_out = d.cta_keys + ((size_t)par * d.nctas + cm.rank) * d.key_cap;
+      unsigned long long* keys_out = d.cta_keys + ((size_t)par * d.nctas + cm.rank) * d.key_cap;
       int pos = 0, n_in = 0;
       for (int x0 = 0; x0 < nw_all; x0 += 32) {
         const int x = x0 + lane;
@@ -378,25 +401,29 @@ __global__ void __launch_bounds__(512, 1)
         while (m) {
           const int b = __ffs(m) - 1;
           m &= m - 1;
-          keys_out[o++] = (wkey + b) | (((a >> b) & 1u) << 31) | (((p >> b) & 1u) << 30);
+          st_relaxed_u64(keys_out + o++, stamp_hi | (wkey + b) | (((a >> b) & 1u) << 31) | (((p >> b) & 1u) << 30));
         }
         n_in += __reduce_add_sync(FULL, x < nw_in ? c : 0);
         pos += __shfl_sync(FULL, incl, 31);
       }
-      // each lane's key stores, and (through the CTA barrier) the other warps'
-      // traces and bitmap words, are ordered before the stamp
-      fence_acq_rel_gpu();
+      // The key words carry their step, so without plasticity nothing else has
+      // to be ordered before the stamp.  With plasticity the other warps'
+      // traces and bitmap words (through the CTA barrier) must be: one fence.
+      if (stdp_run) fence_acq_rel_gpu();
       __syncwarp();
       if (lane == 0)
         st_relaxed_u64(d.cta_stamp + (size_t)par * d.nctas + cm.rank,
                        stamp_hi | ((unsigned long long)n_in << 16) | (unsigned long long)(pos - n_in));
-      // Every CTA of the network will read the row pointers and the synapse
-      // row of these keys this step: pull them into L2 now, while the stamps
-      // travel (one bulk prefetch per row).
-      for (int i = lane; i < pos; i += 32) {
-        const int key = (int)(keys_out[i] & 0x3fffffffu);
-        if (!((keys_out[i] >> 31) & 1u) && !stdp_run) continue;
-        const int* rp = d.rowptr + (size_t)key * n_tiles;
+    } else {
+      // Every CTA of the network reads the row pointers and the synapse row of
+      // this warp's spiking keys this step: pull them into L2 now, while the
+      // stamps travel (one bulk prefetch per row).
+      const int nl = TS >> 5, ni = ITS >> 5;
+      for (int i = 0; i < nl + ni; ++i) {
+        uint32_t m = i < nl ? spkw_s[i] : (inw_s[i - nl] | (stdp_run ? inwp_s[i - nl] : 0u));
+        const int wkey = i < nl ? KL + p0 + 32 * i : kin0 + 32 * (i - nl);
+        if (!((m >> lane) & 1u)) continue;
+        const int* rp = d.rowptr + (size_t)(wkey + lane) * n_tiles;
         prefetch_l2(rp, sizeof(int) * (size_t)(n_tiles + 1));
         const int e0 = __ldg(rp), e1 = __ldg(rp + n_tiles);
         if (e1 > e0) prefetch_l2(d.entries + e0, sizeof(uint2) * (size_t)(e1 - e0));
@@ -411,6 +438,29 @@ __global__ void __launch_bounds__(512, 1)
     // releases each round to the CTA's other warps through a named barrier.
     // Every warp then stages and applies its tile's part of the round.
     auto process_round = [&](const int n_round) {
+      if (recorder) {
+            // spike store in canonical order: neurons, and inputs on request
+            for (int c0 = 0; c0 < n_round; c0 += 32) {
+              const int j = c0 + lane;
+              bool rec = false;
+              uint32_t key = 0u;
+              if (j < n_round) {
+                const uint32_t lv = list[j];
+                key = lv & 0x3fffffffu;
+                rec = (lv >> 31) && ((int)key >= KL || ctl0.record_inputs);
+              }
+              const unsigned m = __ballot_sync(FULL, rec);
+              if (rec) {
+                const unsigned long long sp = spike_count + (unsigned long long)__popc(m & lanemask_lt());
+                if (sp < (unsigned long long)d.spike_cap)
+                  d.spikes[sp] = make_uint2(key, __float_as_uint(t));
+                else
+                  atomicCAS(&d.ctl->status, 0, SPK_ERR_OVERFLOW);
+              }
+              spike_count += (unsigned long long)__popc(m);
+            }
+            if (spike_count > (unsigned long long)d.spike_cap) spike_count = d.spike_cap;
+          }
         for (int kb = 0; kb < n_round; kb += STAGE_KEYS) {
           const int nk = min(STAGE_KEYS, n_round - kb);
           {
@@ -421,13 +471,15 @@ __global__ void __launch_bounds__(512, 1)
             float prs[KPL];
 #pragma unroll
             for (int u = 0; u < KPL; ++u) {
+              // out-of-range lanes read key 0's pointers (always valid) so all
+              // loads are issued unconditionally
               const int i = u * 32 + lane;
               lvs[u] = i < nk ? list[kb + i] : 0u;
               const int key = (int)(lvs[u] & 0x3fffffffu);
-              const size_t ri = (size_t)key * n_tiles + t_idx;
-              rp0[u] = i < nk ? __ldg(d.rowptr + ri) : 0;
-              rp1[u] = i < nk ? __ldg(d.rowptr + ri + 1) : 0;
-              prs[u] = (i < nk && stdp_run) ? __ldcg(pub + key) : 0.0f;
+              const int* rp = d.rowptr + (size_t)key * n_tiles + t_idx;
+              rp0[u] = __ldg(rp);
+              rp1[u] = __ldg(rp + 1);
+              prs[u] = stdp_run ? __ldcg(pub + key) : 0.0f;
             }
 #pragma unroll
             for (int u = 0; u < KPL; ++u) {
@@ -510,13 +562,23 @@ __global__ void __launch_bounds__(512, 1)
                   cell = (sl * TS + q) * L + lb;
                 }
               }
-              // apply in lane order within a chunk (match_any groups the lanes
-              // that hit one cell), chunks in program order
-              const unsigned grp = __match_any_sync(FULL, cell);
-              const int rank = __popc(grp & lanemask_lt());
-              const int maxr = __reduce_max_sync(FULL, add ? rank : 0);
-              for (int r = 0; r <= maxr; ++r) {
-                if (add && rank == r) ring_s[cell] = ring_s[cell] + contrib;
+              // Apply in lane order within a chunk, chunks in program order.
+              // Each pass, the lowest pending lane of every cell hash (an
+              // atomicMin on a shared tag) adds its contribution; lanes that
+              // share a hash are thereby serialized in lane order, which keeps
+              // same-cell additions in canonical order.
+              bool pending = add;
+              const int h = cell & (APPLY_TAGS - 1);
+              while (__any_sync(FULL, pending)) {
+                if (pending) atomicMin(tag_s + h, lane);
+                __syncwarp();
+                const bool win = pending && tag_s[h] == lane;
+                if (win) ring_s[cell] = ring_s[cell] + contrib;
+                __syncwarp();
+                if (win) {
+                  tag_s[h] = 32;
+                  pending = false;
+                }
                 __syncwarp();
               }
             }
@@ -592,42 +654,34 @@ __global__ void __launch_bounds__(512, 1)
       for (int rbase = 0;; rbase += LIST_CAP) {
         const int n_round = ok ? min(LIST_CAP, total - rbase) : 0;
         if (ok) {
-          // gather the round's keys: each lane copies its segments' part
+          // gather the round's keys: each lane reads its segments' part (the
+          // key words carry their step; a stale word is polled again)
           for (int i = lane; i < 2 * C; i += 32) {
             const int o0 = segoff[i], o1 = segoff[i + 1];
             const int a0 = max(o0, rbase), a1 = min(o1, rbase + n_round);
             if (a0 < a1) {
               const int r = i < C ? i : i - C;
               const int skip = i < C ? 0 : segoff[r + 1] - segoff[r];  // neurons follow the CTA's inputs
-              const uint32_t* src = d.cta_keys + ((size_t)par * C + r) * d.key_cap + skip - o0;
-              for (int x = a0; x < a1; ++x) cp_async4(list + (x - rbase), src + x);
+              const unsigned long long* src = d.cta_keys + ((size_t)par * C + r) * d.key_cap + skip - o0;
+              int x = a0;
+              for (; x + 4 <= a1; x += 4) {
+                unsigned long long v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = ld_relaxed_u64(src + x + u);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                  v[u] = repoll(src + x + u, v[u], stamp, d, ok);
+                  list[x + u - rbase] = (uint32_t)v[u];
+                }
+              }
+              for (; x < a1; ++x) {
+                const unsigned long long v = repoll(src + x, ld_relaxed_u64(src + x), stamp, d, ok);
+                list[x - rbase] = (uint32_t)v;
+              }
             }
           }
-          cp_async_wait_all();
+          ok = __all_sync(FULL, ok);
           __syncwarp();
-          if (recorder) {
-            // spike store in canonical order: neurons, and inputs on request
-            for (int c0 = 0; c0 < n_round; c0 += 32) {
-              const int j = c0 + lane;
-              bool rec = false;
-              uint32_t key = 0u;
-              if (j < n_round) {
-                const uint32_t lv = list[j];
-                key = lv & 0x3fffffffu;
-                rec = (lv >> 31) && ((int)key >= KL || ctl0.record_inputs);
-              }
-              const unsigned m = __ballot_sync(FULL, rec);
-              if (rec) {
-                const unsigned long long sp = spike_count + (unsigned long long)__popc(m & lanemask_lt());
-                if (sp < (unsigned long long)d.spike_cap)
-                  d.spikes[sp] = make_uint2(key, __float_as_uint(t));
-                else
-                  atomicCAS(&d.ctl->status, 0, SPK_ERR_OVERFLOW);
-              }
-              spike_count += (unsigned long long)__popc(m);
-            }
-            if (spike_count > (unsigned long long)d.spike_cap) spike_count = d.spike_cap;
-          }
         }
         const bool last = !ok || rbase + LIST_CAP >= total;
         if (lane == 0) {
@@ -724,7 +778,7 @@ __global__ void __launch_bounds__(512, 1)
     for (int o = 16; o >= 1; o >>= 1) e += __shfl_xor_sync(FULL, e, o);
     if (lane == 0 && e) atomicAdd(&d.ctl->events, e);
   }
-  if (cm.rank == 0 && w == 0) {
+  if (cm.rank == 0 && w == W - 1) {
     if (lane == 0) {
       d.ctl->step = ctl0.step + steps_done;
       d.ctl->gstep = ctl0.gstep + steps_done;

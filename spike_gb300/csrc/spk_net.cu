@@ -520,7 +520,7 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
       {&p_pub, sizeof(float) * (stdp ? 2 * (size_t)n_keys : 0)},
       {&p_bA, sizeof(uint32_t) * 2 * (size_t)n_words},
       {&p_bP, sizeof(uint32_t) * 2 * (size_t)n_words},
-      {&p_ckeys, sizeof(uint32_t) * 2 * (size_t)plan.nctas * key_cap},
+      {&p_ckeys, sizeof(unsigned long long) * 2 * (size_t)plan.nctas * key_cap},
       {&p_cstamp, sizeof(unsigned long long) * 2 * (size_t)plan.nctas},
       {&p_spk, sizeof(uint2) * (size_t)std::max<int64_t>(spike_cap, 1)},
       {&p_ctl, sizeof(RunCtl)},
@@ -628,7 +628,7 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
   h.pre_pub = (float*)p_pub;
   h.bitsA = (uint32_t*)p_bA;
   h.bitsP = (uint32_t*)p_bP;
-  h.cta_keys = (uint32_t*)p_ckeys;
+  h.cta_keys = (unsigned long long*)p_ckeys;
   h.cta_stamp = (unsigned long long*)p_cstamp;
   h.key_cap = key_cap;
   h.spikes = (uint2*)p_spk;
@@ -661,6 +661,7 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
   if (cudaMemsetAsync(p_bA, 0, sizeof(uint32_t) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
       cudaMemsetAsync(p_bP, 0, sizeof(uint32_t) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
       cudaMemsetAsync(p_cstamp, 0, sizeof(unsigned long long) * 2 * (size_t)plan.nctas, n->stream) != cudaSuccess ||
+      cudaMemsetAsync(p_ckeys, 0, sizeof(unsigned long long) * 2 * (size_t)plan.nctas * key_cap, n->stream) != cudaSuccess ||
       cudaMemsetAsync(p_abort, 0, sizeof(int), n->stream) != cudaSuccess) {
     set_error("cudaMemsetAsync failed");
     return fail_free(SPK_ERR_CUDA);
