@@ -100,7 +100,7 @@ struct CtaMap {
 
 // Per-warp shared-memory words for a schedule (4-byte words).
 struct WarpLayout {
-  int stage, sidx, kst, koff, kfl, kpre, tag, ring, V, last, gtr, post_tr, pre_tr, spkw, inw, inwp, in_next,
+  int stage, sidx, kst, koff, kfl, kpre, tag, rowb, rowe, ring, V, last, gtr, post_tr, pre_tr, spkw, inw, inwp, in_next,
       in_rate, in_pre, total;
 };
 SPK_HD WarpLayout warp_layout(int B, int TS, int L, int ITS, int kind, int has_stdp) {
@@ -113,6 +113,8 @@ SPK_HD WarpLayout warp_layout(int B, int TS, int L, int ITS, int kind, int has_s
   w.kfl = o; o += STAGE_KEYS;           // list word (key | spike | pre-event flags)
   w.kpre = o; o += STAGE_KEYS;          // presynaptic STDP trace of the step
   w.tag = o; o += APPLY_TAGS;           // lowest lane per cell hash (ordered apply)
+  w.rowb = o; o += TS + ITS;            // synapse-row bounds of the warp's own keys
+  w.rowe = o; o += TS + ITS;            //   (neurons, then inputs), for L2 prefetch
   w.ring = o; o += B * TS * L;
   w.V = o; o += TS;
   w.last = o; o += TS;

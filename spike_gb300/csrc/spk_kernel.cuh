@@ -159,6 +159,8 @@ __global__ void __launch_bounds__(512, 1)
   uint32_t* kfl = wreg + wl.kfl;
   float* kpre = (float*)(wreg + wl.kpre);
   int* tag_s = (int*)(wreg + wl.tag);
+  int* rowb_s = (int*)(wreg + wl.rowb);
+  int* rowe_s = (int*)(wreg + wl.rowe);
   float* ring_s = (float*)(wreg + wl.ring);
   float* V_s = (float*)(wreg + wl.V);
   float* last_s = (float*)(wreg + wl.last);
@@ -223,6 +225,11 @@ __global__ void __launch_bounds__(512, 1)
     }
   }
   for (int i = lane; i < APPLY_TAGS; i += 32) tag_s[i] = 32;
+  for (int i = lane; i < TS + ITS; i += 32) {
+    const int key = i < TS ? KL + p0 + i : kin0 + (i - TS);
+    rowb_s[i] = __ldg(d.rowptr + (size_t)key * n_tiles);
+    rowe_s[i] = __ldg(d.rowptr + (size_t)(key + 1) * n_tiles);
+  }
   unsigned long long spike_count = ctl0.spike_count;
   unsigned long long ev = 0;
   bool inputs_active = ctl0.inputs_active != 0;
@@ -349,6 +356,22 @@ __global__ void __launch_bounds__(512, 1)
     }
     inputs_active = true;
 
+    // ---- prefetch: every CTA of the network reads the row pointers and the
+    // synapse row of this warp's spiking keys this step; pull them into L2
+    // now, while the keys travel (bulk prefetches, no dependent loads)
+    {
+      const int nl = TS >> 5, ni = ITS >> 5;
+      for (int i = 0; i < nl + ni; ++i) {
+        const uint32_t m = i < nl ? spkw_s[i] : (inw_s[i - nl] | (stdp_run ? inwp_s[i - nl] : 0u));
+        if (!((m >> lane) & 1u)) continue;
+        const int li = i < nl ? 32 * i + lane : TS + 32 * (i - nl) + lane;
+        const int key = i < nl ? KL + p0 + li : kin0 + (li - TS);
+        prefetch_l2(d.rowptr + (size_t)key * n_tiles, sizeof(int) * (size_t)(n_tiles + 1));
+        if (rowe_s[li] > rowb_s[li])
+          prefetch_l2(d.entries + rowb_s[li], sizeof(uint2) * (size_t)(rowe_s[li] - rowb_s[li]));
+      }
+    }
+
     // ---- publish: the CTA's active keys, then one stamp word per CTA ---------
     __syncwarp();
     if (stdp_run) {
@@ -414,20 +437,6 @@ __global__ void __launch_bounds__(512, 1)
       if (lane == 0)
         st_relaxed_u64(d.cta_stamp + (size_t)par * d.nctas + cm.rank,
                        stamp_hi | ((unsigned long long)n_in << 16) | (unsigned long long)(pos - n_in));
-    } else {
-      // Every CTA of the network reads the row pointers and the synapse row of
-      // this warp's spiking keys this step: pull them into L2 now, while the
-      // stamps travel (one bulk prefetch per row).
-      const int nl = TS >> 5, ni = ITS >> 5;
-      for (int i = 0; i < nl + ni; ++i) {
-        uint32_t m = i < nl ? spkw_s[i] : (inw_s[i - nl] | (stdp_run ? inwp_s[i - nl] : 0u));
-        const int wkey = i < nl ? KL + p0 + 32 * i : kin0 + 32 * (i - nl);
-        if (!((m >> lane) & 1u)) continue;
-        const int* rp = d.rowptr + (size_t)(wkey + lane) * n_tiles;
-        prefetch_l2(rp, sizeof(int) * (size_t)(n_tiles + 1));
-        const int e0 = __ldg(rp), e1 = __ldg(rp + n_tiles);
-        if (e1 > e0) prefetch_l2(d.entries + e0, sizeof(uint2) * (size_t)(e1 - e0));
-      }
     }
 
     // ---- phase B: warp 0 gathers the step's active keys from every CTA ------
@@ -654,34 +663,42 @@ __global__ void __launch_bounds__(512, 1)
       for (int rbase = 0;; rbase += LIST_CAP) {
         const int n_round = ok ? min(LIST_CAP, total - rbase) : 0;
         if (ok) {
-          // gather the round's keys: each lane reads its segments' part (the
-          // key words carry their step; a stale word is polled again)
-          for (int i = lane; i < 2 * C; i += 32) {
-            const int o0 = segoff[i], o1 = segoff[i + 1];
-            const int a0 = max(o0, rbase), a1 = min(o1, rbase + n_round);
-            if (a0 < a1) {
-              const int r = i < C ? i : i - C;
-              const int skip = i < C ? 0 : segoff[r + 1] - segoff[r];  // neurons follow the CTA's inputs
-              const unsigned long long* src = d.cta_keys + ((size_t)par * C + r) * d.key_cap + skip - o0;
-              int x = a0;
-              for (; x + 4 <= a1; x += 4) {
-                unsigned long long v[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) v[u] = ld_relaxed_u64(src + x + u);
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                  v[u] = repoll(src + x + u, v[u], stamp, d, ok);
-                  list[x + u - rbase] = (uint32_t)v[u];
-                }
-              }
-              for (; x < a1; ++x) {
-                const unsigned long long v = repoll(src + x, ld_relaxed_u64(src + x), stamp, d, ok);
-                list[x - rbase] = (uint32_t)v;
+          // gather the round's keys in windows of STAGE_ENTRIES: every lane
+          // issues async copies of its segments' words into warp 0's staging
+          // buffer, then each word's step stamp is checked (a stale word is
+          // polled again) and the key written to the list
+          unsigned long long* kw = reinterpret_cast<unsigned long long*>(stage);
+          for (int p0w = 0; p0w < n_round; p0w += STAGE_ENTRIES) {
+            const int pw1 = min(n_round, p0w + STAGE_ENTRIES);
+            for (int i = lane; i < 2 * C; i += 32) {
+              const int o0 = segoff[i], o1 = segoff[i + 1];
+              const int a0 = max(o0, rbase + p0w), a1 = min(o1, rbase + pw1);
+              if (a0 < a1) {
+                const int r = i < C ? i : i - C;
+                const int skip = i < C ? 0 : segoff[r + 1] - segoff[r];  // neurons follow the CTA's inputs
+                const unsigned long long* src = d.cta_keys + ((size_t)par * C + r) * d.key_cap + skip - o0;
+                for (int x = a0; x < a1; ++x) cp_async8(kw + (x - rbase - p0w), src + x);
               }
             }
+            cp_async_wait_all();
+            __syncwarp();
+            for (int x = p0w + lane; x < pw1; x += 32) {
+              unsigned long long v = kw[x - p0w];
+              if ((unsigned)(v >> 32) != stamp) {
+                // locate the word's source to poll it again
+                int i = 0;
+                while (i + 1 < 2 * C && segoff[i + 1] <= rbase + x) ++i;
+                const int r = i < C ? i : i - C;
+                const int skip = i < C ? 0 : segoff[r + 1] - segoff[r];
+                const unsigned long long* src =
+                    d.cta_keys + ((size_t)par * C + r) * d.key_cap + skip + (rbase + x - segoff[i]);
+                v = repoll(src, ld_relaxed_u64(src), stamp, d, ok);
+              }
+              list[x] = (uint32_t)v;
+            }
+            __syncwarp();
           }
           ok = __all_sync(FULL, ok);
-          __syncwarp();
         }
         const bool last = !ok || rbase + LIST_CAP >= total;
         if (lane == 0) {
