@@ -390,28 +390,36 @@ __global__ void __launch_bounds__(512, 1)
       }
     }
     __syncthreads();  // every warp's words are in shared memory, its traces written
-    if (w == 0) {
+    // The CTA's ballot words in key order: inputs of warps 0..W-1, then neurons
+    // of warps 0..W-1 (x-th word: bits a = spikes, p = pre events, first key).
+    const int nw_in = W * (ITS >> 5), nw_all = W * ((ITS >> 5) + (TS >> 5));
+    auto cta_word = [&](const int x, uint32_t& a, uint32_t& p, uint32_t& wkey) {
       const int ni = ITS >> 5, nl = TS >> 5;
-      const int nw_in = W * ni, nw_all = W * (ni + nl);
+      a = 0u;
+      p = 0u;
+      wkey = 0u;
+      if (x < nw_in) {
+        const int wx = x / ni, k = x - (x / ni) * ni;
+        const uint32_t* r = sm + SHARED_WORDS + wx * wl.total;
+        a = r[wl.inw + k];
+        p = stdp_run ? r[wl.inwp + k] : 0u;
+        wkey = (uint32_t)((cm.rank * W + wx) * ITS + k * 32);
+      } else if (x < nw_all) {
+        const int y = x - nw_in;
+        const int wx = y / nl, k = y - (y / nl) * nl;
+        const uint32_t* r = sm + SHARED_WORDS + wx * wl.total;
+        a = r[wl.spkw + k];
+        p = stdp_run ? a : 0u;
+        wkey = (uint32_t)(KL + (cm.rank * W + wx) * TS + k * 32);
+      }
+    };
+    if (w == 0 && d.nctas > 1) {
       unsigned long long* keys_out = d.cta_keys + ((size_t)par * d.nctas + cm.rank) * d.key_cap;
       int pos = 0, n_in = 0;
       for (int x0 = 0; x0 < nw_all; x0 += 32) {
         const int x = x0 + lane;
-        uint32_t a = 0u, p = 0u, wkey = 0u;
-        if (x < nw_in) {
-          const int wx = x / ni, k = x - (x / ni) * ni;
-          const uint32_t* r = sm + SHARED_WORDS + wx * wl.total;
-          a = r[wl.inw + k];
-          p = stdp_run ? r[wl.inwp + k] : 0u;
-          wkey = (uint32_t)((cm.rank * W + wx) * ITS + k * 32);
-        } else if (x < nw_all) {
-          const int y = x - nw_in;
-          const int wx = y / nl, k = y - (y / nl) * nl;
-          const uint32_t* r = sm + SHARED_WORDS + wx * wl.total;
-          a = r[wl.spkw + k];
-          p = stdp_run ? a : 0u;
-          wkey = (uint32_t)(KL + (cm.rank * W + wx) * TS + k * 32);
-        }
+        uint32_t a, p, wkey;
+        cta_word(x, a, p, wkey);
         uint32_t m = a | p;
         const int c = __popc(m);
         int incl = c;
@@ -596,7 +604,50 @@ __global__ void __launch_bounds__(512, 1)
         }
     };
     const int nthreads = blockDim.x;
-    if (w == 0) {
+    if (w == 0 && d.nctas == 1) {
+      // One CTA holds the whole network: the list comes straight from the
+      // warps' ballot words in shared memory, with no global exchange.
+      int list_n = 0;
+      for (int x0 = 0; x0 < nw_all; x0 += 32) {
+        uint32_t a, p, wkey;
+        cta_word(x0 + lane, a, p, wkey);
+        uint32_t m = a | p;
+        const int c = __popc(m);
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(FULL, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const int tot = __shfl_sync(FULL, incl, 31);
+        if (tot == 0) continue;
+        if (list_n + tot > LIST_CAP) {
+          if (lane == 0) {
+            s_round[0] = list_n;
+            s_round[1] = 0;
+            s_round[2] = 1;
+          }
+          round_barrier(nthreads);
+          process_round(list_n);
+          round_barrier(nthreads);
+          list_n = 0;
+        }
+        int o = list_n + incl - c;
+        while (m) {
+          const int b = __ffs(m) - 1;
+          m &= m - 1;
+          list[o++] = (wkey + b) | (((a >> b) & 1u) << 31) | (((p >> b) & 1u) << 30);
+        }
+        list_n += tot;
+      }
+      if (lane == 0) {
+        s_round[0] = list_n;
+        s_round[1] = 1;
+        s_round[2] = 1;
+      }
+      round_barrier(nthreads);
+      process_round(list_n);
+    } else if (w == 0) {
       const int C = d.nctas;
       const unsigned long long* stp = d.cta_stamp + (size_t)par * C;
       constexpr int SPL = MAX_CTAS_PER_NET / 32;
