@@ -221,6 +221,91 @@ int spk_batch_launch_count(const spk_batch* batch, int64_t* launches);
 int spk_batch_stream(const spk_batch* batch, void** stream);
 int spk_batch_destroy(spk_batch* batch);
 
+/* ---- allocation-free stepping --------------------------------------------
+ * This entry point has no counterpart in the reference.  It is for callers
+ * that cannot call cudaMalloc at the point where they step a network: code
+ * that runs under another framework's memory allocator (which owns every
+ * device allocation of the process), real-time or embedded hosts where device
+ * allocation is forbidden after start-up, and plug-ins that only receive
+ * device buffers from their host application.  The caller owns every input and
+ * output buffer below; the only extra device memory the step needs, the
+ * per-step exchange between CTAs and the launch descriptors, is a fixed
+ * SPK_NOALLOC_SCRATCH_BYTES array inside the library that every GPU loading
+ * the library holds until the process exits.
+ *
+ * Buffer layout (the layout spk_net_create builds for the same schedule):
+ *  - keys: input i has key Nin-1-i, neuron n has key KL+n, with
+ *    T = warps_per_cta*ctas tiles, ITS = 32*ceil(ceil(Nin/T)/32), KL = T*ITS,
+ *    n_keys = KL + T*tile_posts; a synapse's tile is post / tile_posts;
+ *  - rowptr[n_keys*T + 1]: start of each (key, tile) sub-row, exclusive prefix;
+ *  - entries[S] (pairs of uint32): sub-rows in (key, tile) order, synapses of
+ *    one sub-row in creation order; x = post%tile_posts | delay<<16 |
+ *    label<<24 | class<<28, y = float bits of weight*scale (class 0) or of
+ *    the weight (plastic class c >= 1, scale = plastic_scales[c-1]);
+ *  - csc_ptr[N+1], csc[2*P]: plastic afferents of each post as (entry index,
+ *    key), needed only with plasticity;
+ *  - state: V, last_spike [N]; syn_trace [N*L] (conductance/current);
+ *    ring [T][max_delay+3][tile_posts*L]; input_next [Nin]; rates [Nin];
+ *    post_trace [N] and pre_trace [n_keys] with plasticity;
+ *  - spikes [2*spike_capacity] uint32 pairs (key, float time bits), in
+ *    step order; spike_capacity 0 records nothing;
+ *  - run_state: SPK_RUN_STATE_BYTES of device memory (8-byte aligned), zeroed
+ *    by the caller before the first call; it carries the step counter and
+ *    Poisson activity from call to call, and holds the spikes recorded so far
+ *    (uint64 at byte 32; zero it to clear the store), the synaptic events
+ *    delivered (uint64 at byte 40) and the device status (int32 at byte 48: 0,
+ *    SPK_ERR_TIMEOUT or SPK_ERR_OVERFLOW), valid once the stream has finished.
+ *
+ * The first call on a device resolves the scratch array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  Every call shares the one scratch array and
+ * clears the parts that must start at zero, so calls whose work overlaps on
+ * the GPU (different streams, or different host threads on one device) race
+ * and must be serialized by the caller.  Networks whose scratch exceeds
+ * SPK_NOALLOC_SCRATCH_BYTES are rejected with SPK_ERR_INVALID. */
+#define SPK_NOALLOC_SCRATCH_BYTES (4u << 20)
+#define SPK_RUN_STATE_BYTES 64
+
+typedef struct spk_device_net {
+  /* shape, schedule and constants (host values) */
+  int32_t n_neurons, n_inputs, n_labels, synapse_kind, max_delay;
+  int32_t warps_per_cta, tile_posts, ctas;
+  float dt, refractory_period, background_current;
+  int32_t n_groups;
+  const spk_neuron_group* groups; /* host array; v_init_* ignored (state is the caller's) */
+  const float* label_tau;         /* host [L] */
+  const float* label_vhat;        /* host [L] */
+  int32_t has_stdp;
+  spk_stdp_params stdp;
+  int32_t n_plastic_scales;       /* classes 1..n (<= 15) */
+  const float* plastic_scales;    /* host [n_plastic_scales] */
+  uint64_t seed;
+  int32_t record_inputs;
+  /* caller-owned device buffers */
+  const int32_t* rowptr;
+  uint32_t* entries;
+  const int32_t* csc_ptr;
+  const uint32_t* csc;
+  float* V;
+  float* last_spike;
+  float* syn_trace;
+  float* ring;
+  float* input_next;
+  const float* rates;
+  float* post_trace;
+  float* pre_trace;
+  uint32_t* spikes;
+  int64_t spike_capacity;
+  void* run_state;
+} spk_device_net;
+
+/* Advance the network n_steps timesteps from start_time (seconds) on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream), as spk_net_run_steps
+ * does for a network created by spk_net_create.  Asynchronous; allocates no
+ * device or host memory. */
+int spk_step_noalloc(const spk_device_net* net, int64_t n_steps, int32_t plasticity_on, float start_time,
+                     void* stream);
+
 /* ---- misc ---------------------------------------------------------------- */
 /* Backend::MemoryManager::{free_bytes,total_bytes}
  * (Spike/Backend/CUDA/Helpers/Memory.cu:7-25), returning a status instead of

@@ -102,6 +102,25 @@ class SynapseParams(C.Structure):
                 ("plasticity_rule", i32)]
 
 
+class DeviceNet(C.Structure):
+    """spk_device_net: a network over caller-owned device buffers."""
+    _fields_ = [
+        ("n_neurons", i32), ("n_inputs", i32), ("n_labels", i32), ("synapse_kind", i32), ("max_delay", i32),
+        ("warps_per_cta", i32), ("tile_posts", i32), ("ctas", i32),
+        ("dt", f32), ("refractory_period", f32), ("background_current", f32),
+        ("n_groups", i32), ("groups", P(NeuronGroup)), ("label_tau", P(f32)), ("label_vhat", P(f32)),
+        ("has_stdp", i32), ("stdp", StdpParams), ("n_plastic_scales", i32), ("plastic_scales", P(f32)),
+        ("seed", u64), ("record_inputs", i32),
+        ("rowptr", C.c_void_p), ("entries", C.c_void_p), ("csc_ptr", C.c_void_p), ("csc", C.c_void_p),
+        ("V", C.c_void_p), ("last_spike", C.c_void_p), ("syn_trace", C.c_void_p), ("ring", C.c_void_p),
+        ("input_next", C.c_void_p), ("rates", C.c_void_p), ("post_trace", C.c_void_p),
+        ("pre_trace", C.c_void_p), ("spikes", C.c_void_p), ("spike_capacity", i64), ("run_state", C.c_void_p),
+    ]
+
+
+SPK_NOALLOC_SCRATCH_BYTES = 4 << 20
+SPK_RUN_STATE_BYTES = 64
+
 _VP = C.c_void_p
 _SIGS = {
     # spike_gb300.h
@@ -132,6 +151,7 @@ _SIGS = {
     "spk_batch_launch_count": (i32, [_VP, P(i64)]),
     "spk_batch_stream": (i32, [_VP, P(_VP)]),
     "spk_batch_destroy": (i32, [_VP]),
+    "spk_step_noalloc": (i32, [P(DeviceNet), i64, i32, f32, _VP]),
     "spk_memory_info": (i32, [P(u64), P(u64)]),
     "spk_abi_version": (i32, []),
     "spk_last_error": (C.c_char_p, []),

@@ -1147,3 +1147,310 @@ int spk_batch_destroy(spk_batch* b) {
 }
 
 }  // extern "C"
+
+// =====================================================================================
+// Allocation-free stepping: the step kernel over caller-owned network buffers.
+// The only device memory the library supplies is the fixed scratch array below,
+// which holds what the step exchanges between CTAs plus the launch descriptors.
+namespace spk {
+
+// Scratch of spk_step_noalloc.  Every device that loads the library holds this
+// array until the process exits; every call on a device shares it.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[SPK_NOALLOC_SCRATCH_BYTES];
+
+static_assert(sizeof(RunCtl) <= SPK_RUN_STATE_BYTES, "RunCtl does not fit the caller's run state");
+static_assert(offsetof(RunCtl, spike_count) == 32 && offsetof(RunCtl, events) == 40 &&
+                  offsetof(RunCtl, status) == 48,
+              "run state offsets published in spike_gb300.h");
+
+struct NoallocDevice {
+  bool ready = false;
+  unsigned char* scratch = nullptr;  // device address of g_noalloc_scratch
+  DeviceInfo di;
+};
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static NoallocDevice g_noalloc_dev[NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mu;
+
+// Resolves the scratch address and the step kernel's shared-memory limit of the
+// current device, once per device (on the first call made with it current).
+static int noalloc_device(NoallocDevice** out) {
+  int dev = 0;
+  SPK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+    set_error("device %d is beyond the %d devices spk_step_noalloc tracks", dev, NOALLOC_MAX_DEVICES);
+    return SPK_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  NoallocDevice& nd = g_noalloc_dev[dev];
+  if (!nd.ready) {
+    unsigned char* ptr = nullptr;
+    SPK_CUDA(cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch));
+    DeviceInfo di;
+    const int rc = device_info(&di);
+    if (rc) return rc;
+    SPK_CUDA(cudaFuncSetAttribute(step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, di.max_smem));
+    nd.scratch = ptr;
+    nd.di = di;
+    nd.ready = true;
+  }
+  *out = &nd;
+  return SPK_OK;
+}
+
+// Writes the network descriptor and CTA map into the scratch, clears the
+// exchange stamps and keys and the abort flag, and starts the run in the
+// caller's run state.  The stamps and keys must start at zero: a word left by an
+// earlier call of another network (or of this one after its step counter was
+// reset) can carry a stamp this call also produces.
+static __global__ void noalloc_setup_kernel(NetDev nd, NetDev* nd_out, CtaMap* map, unsigned long long* xchg,
+                                            size_t xchg_words, float start, int steps_total, int plastic,
+                                            int record_inputs) {
+  const size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = i0; i < xchg_words; i += stride) xchg[i] = 0ull;
+  for (size_t r = i0; r < (size_t)nd.nctas; r += stride) map[r] = CtaMap{0, (int)r};
+  if (i0 == 0) {
+    *nd_out = nd;
+    *nd.abort_flag = 0;
+    RunCtl* c = nd.ctl;
+    c->start_time = start;
+    c->step = 0;
+    c->steps_total = steps_total;
+    c->plastic = plastic;
+    c->record_inputs = record_inputs;
+  }
+}
+
+static bool aligned(const void* p, uintptr_t a) { return ((uintptr_t)p & (a - 1)) == 0; }
+
+static int step_noalloc_impl(const spk_device_net* a, int64_t n_steps, int plasticity_on, float start,
+                             cudaStream_t stream) {
+  if (!a) {
+    set_error("null network");
+    return SPK_ERR_INVALID;
+  }
+  if (n_steps < 0 || n_steps > 0x7fffffff) {
+    set_error("step count %lld outside [0, 2^31-1]", (long long)n_steps);
+    return SPK_ERR_INVALID;
+  }
+  const int N = a->n_neurons, Nin = a->n_inputs, L = a->n_labels, kind = a->synapse_kind;
+  const int W = a->warps_per_cta, TS = a->tile_posts, C = a->ctas;
+  const int stdp = a->has_stdp ? 1 : 0;
+  if (N <= 0 || Nin < 0 || L < 1 || L > MAX_LABELS || !(a->dt > 0.0f) || a->max_delay < 1 ||
+      a->max_delay > MAX_DELAY) {
+    set_error("sizes out of range (neurons %d, inputs %d, labels %d, max delay %d)", N, Nin, L, a->max_delay);
+    return SPK_ERR_INVALID;
+  }
+  if (kind != SPK_SYN_CONDUCTANCE && kind != SPK_SYN_CURRENT && kind != SPK_SYN_VOLTAGE) {
+    set_error("unknown synapse kind %d", kind);
+    return SPK_ERR_INVALID;
+  }
+  if (W < 1 || W > 16 || TS < 32 || TS % 32 || TS > 65504 || C < 1 || C > MAX_CTAS_PER_NET) {
+    set_error("schedule W=%d tile=%d ctas=%d: need 1 <= W <= 16, tile a multiple of 32, 1 <= ctas <= %d", W, TS, C,
+              MAX_CTAS_PER_NET);
+    return SPK_ERR_INVALID;
+  }
+  if (a->n_groups < 1 || a->n_groups > MAX_GROUPS || !a->groups) {
+    set_error("between 1 and %d neuron groups are supported (got %d)", MAX_GROUPS, a->n_groups);
+    return SPK_ERR_INVALID;
+  }
+  {
+    int expect = 0;
+    for (int g = 0; g < a->n_groups; ++g) {
+      if (a->groups[g].start != expect || a->groups[g].count <= 0) {
+        set_error("neuron groups must be contiguous, ascending and non-empty");
+        return SPK_ERR_INVALID;
+      }
+      expect += a->groups[g].count;
+    }
+    if (expect != N) {
+      set_error("neuron groups cover %d neurons, the network has %d", expect, N);
+      return SPK_ERR_INVALID;
+    }
+  }
+  if ((kind != SPK_SYN_VOLTAGE && !a->label_tau) || (kind == SPK_SYN_CONDUCTANCE && !a->label_vhat)) {
+    set_error("conductance/current synapses need label_tau (and label_vhat for conductance)");
+    return SPK_ERR_INVALID;
+  }
+  if (stdp && (a->n_plastic_scales < 0 || a->n_plastic_scales >= MAX_CLASSES ||
+               (a->n_plastic_scales > 0 && !a->plastic_scales))) {
+    set_error("between 0 and %d plastic weight scales are supported", MAX_CLASSES - 1);
+    return SPK_ERR_INVALID;
+  }
+  if (!a->rowptr || !a->entries || !a->V || !a->last_spike || !a->ring || !a->run_state ||
+      (kind != SPK_SYN_VOLTAGE && !a->syn_trace) || (Nin > 0 && (!a->input_next || !a->rates)) ||
+      (stdp && (!a->csc_ptr || !a->csc || !a->post_trace || !a->pre_trace)) ||
+      (a->spike_capacity > 0 && !a->spikes) || a->spike_capacity < 0) {
+    set_error("a device buffer the network needs is missing");
+    return SPK_ERR_INVALID;
+  }
+  if (!aligned(a->entries, 8) || !aligned(a->csc, 8) || !aligned(a->spikes, 8) || !aligned(a->run_state, 8)) {
+    set_error("entries, csc, spikes and run_state must be 8-byte aligned");
+    return SPK_ERR_INVALID;
+  }
+  const int B = a->max_delay + 2 * 1 + 1;  // SpikingSynapses.cu:48 with G = 1
+  const int n_tiles = W * C;
+  if ((int64_t)n_tiles * TS < N) {
+    set_error("schedule W=%d tile=%d ctas=%d covers %lld of %d neurons", W, TS, C, (long long)n_tiles * TS, N);
+    return SPK_ERR_INVALID;
+  }
+  const int ITS = Nin > 0 ? ((Nin + n_tiles - 1) / n_tiles + 31) / 32 * 32 : 0;
+  if (W * TS > 65535 || W * ITS > 65535) {
+    set_error("more than 65535 neurons or inputs per CTA");
+    return SPK_ERR_INVALID;
+  }
+  const int KL = n_tiles * ITS, n_keys = KL + n_tiles * TS, n_words = n_keys / 32;
+  const int key_cap = W * (TS + ITS);
+
+  // scratch layout: descriptor, CTA map, abort flag, stamps + keys (one range to
+  // clear), spike / pre-event bitmaps, published pre traces
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = align_up(off, 256);
+    off = at + bytes;
+    return at;
+  };
+  const size_t o_nd = take(sizeof(NetDev));
+  const size_t o_map = take(sizeof(CtaMap) * (size_t)C);
+  const size_t o_abort = take(sizeof(int));
+  const size_t xchg_words = 2 * (size_t)C + 2 * (size_t)C * key_cap;
+  const size_t o_xchg = take(sizeof(unsigned long long) * xchg_words);
+  const size_t o_bA = take(sizeof(uint32_t) * 2 * (size_t)n_words);
+  const size_t o_bP = take(sizeof(uint32_t) * 2 * (size_t)n_words);
+  const size_t o_pub = take(stdp ? sizeof(float) * 2 * (size_t)n_keys : 0);
+  if (off > SPK_NOALLOC_SCRATCH_BYTES) {
+    set_error("network needs %zu bytes of step scratch; spk_step_noalloc holds %u", off,
+              (unsigned)SPK_NOALLOC_SCRATCH_BYTES);
+    return SPK_ERR_INVALID;
+  }
+
+  NoallocDevice* dev = nullptr;
+  int rc = noalloc_device(&dev);
+  if (rc) return rc;
+  const int smem = smem_bytes(W, warp_layout(B, TS, L, ITS, kind, stdp));
+  if (smem > dev->di.max_smem) {
+    set_error("schedule W=%d tile=%d needs %d B of shared memory, the device offers %d", W, TS, smem,
+              dev->di.max_smem);
+    return SPK_ERR_INVALID;
+  }
+  if (C > 1) {
+    int per_sm = 0;
+    SPK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_kernel, W * 32, smem));
+    if ((int64_t)per_sm * dev->di.sms < C) {
+      set_error("schedule needs %d co-resident CTAs, device holds %d", C, per_sm * dev->di.sms);
+      return SPK_ERR_UNSUPPORTED;
+    }
+  }
+  if (n_steps == 0) return SPK_OK;
+
+  unsigned char* s = dev->scratch;
+  NetDev h;
+  std::memset(&h, 0, sizeof(h));
+  h.N = N;
+  h.Nin = Nin;
+  h.KL = KL;
+  h.n_keys = n_keys;
+  h.n_words = n_words;
+  h.L = L;
+  h.B = B;
+  h.kind = kind;
+  h.n_tiles = n_tiles;
+  h.TS = TS;
+  h.ITS = ITS;
+  h.W = W;
+  h.nctas = C;
+  h.n_groups = a->n_groups;
+  h.dt = a->dt;
+  h.half_dt = 0.5f * a->dt;
+  h.t_ref = a->refractory_period;
+  h.i_bg = a->background_current;
+  for (int g = 0; g < a->n_groups; ++g) {
+    const spk_neuron_group& G = a->groups[g];
+    GroupConst& c = h.groups[g];
+    c.start = G.start;
+    c.end = G.start + G.count;
+    // LIFSpikingNeurons.cu:31-44: k = timestep / tau_m, kR = k * R (host float).
+    c.k = a->dt / G.tau_m;
+    c.kR = c.k * G.R;
+    c.v0 = G.v0;
+    c.vreset = G.vreset;
+    c.theta = G.theta;
+  }
+  for (int l = 0; l < L; ++l) {
+    // ConductanceSpikingSynapses.cu:76-78: expf(-timestep / tau_g) on the host.
+    h.decay[l] = kind == SPK_SYN_VOLTAGE ? 0.0f : expf(-a->dt / a->label_tau[l]);
+    h.vhat[l] = kind == SPK_SYN_CONDUCTANCE ? a->label_vhat[l] : 0.0f;
+  }
+  if (stdp)
+    for (int c = 0; c < a->n_plastic_scales; ++c) h.scale_tab[c + 1] = a->plastic_scales[c];
+  h.has_stdp = stdp;
+  if (stdp) {
+    const spk_stdp_params& sp = a->stdp;
+    // WeightDependentSTDPPlasticity.cu:125-145 for G = 1.
+    const float em = expf(-(1.0f * a->dt) / sp.tau_minus);
+    const float ep = expf(-(1.0f * a->dt) / sp.tau_plus);
+    h.E_m = em;
+    h.E_p = ep;
+    h.inc_m = sp.a_minus * em;
+    h.inc_p = sp.a_plus * ep;
+    h.invE_m = 1.0f / em;
+    h.invE_p = 1.0f / ep;
+    h.lam = sp.lambda;
+    h.lam_alpha = sp.lambda * sp.alpha;
+    h.wmax = sp.w_max;
+    h.clip_upper = sp.clip_upper ? 1 : 0;
+  }
+  h.seed = a->seed;
+  h.rowptr = a->rowptr;
+  h.entries = (uint2*)a->entries;
+  h.csc_ptr = a->csc_ptr;
+  h.csc = (const uint2*)a->csc;
+  h.V = a->V;
+  h.last = a->last_spike;
+  h.gtr = a->syn_trace;
+  h.ring = a->ring;
+  h.in_next = a->input_next;
+  h.rates = a->rates;
+  h.post_trace = a->post_trace;
+  h.pre_trace = a->pre_trace;
+  h.pre_pub = stdp ? (float*)(s + o_pub) : nullptr;
+  h.bitsA = (uint32_t*)(s + o_bA);
+  h.bitsP = (uint32_t*)(s + o_bP);
+  h.cta_stamp = (unsigned long long*)(s + o_xchg);
+  h.cta_keys = h.cta_stamp + 2 * (size_t)C;
+  h.key_cap = key_cap;
+  h.spikes = (uint2*)a->spikes;
+  h.spike_cap = a->spike_capacity;
+  h.ctl = (RunCtl*)a->run_state;
+  h.abort_flag = (int*)(s + o_abort);
+
+  const int grid = (int)std::min<size_t>((xchg_words + 255) / 256, (size_t)dev->di.sms * 4);
+  noalloc_setup_kernel<<<std::max(grid, 1), 256, 0, stream>>>(
+      h, (NetDev*)(s + o_nd), (CtaMap*)(s + o_map), h.cta_stamp, xchg_words, start, (int)n_steps,
+      (plasticity_on && stdp) ? 1 : 0, a->record_inputs ? 1 : 0);
+  SPK_CUDA(cudaGetLastError());
+  const int K = DEFAULT_STEPS_PER_LAUNCH;
+  const int64_t blocks = (n_steps + K - 1) / K;
+  for (int64_t b = 0; b < blocks; ++b) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(W * 32);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = C > 1 ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    SPK_CUDA(cudaLaunchKernelEx(&cfg, step_kernel, (const NetDev*)(s + o_nd), (const CtaMap*)(s + o_map), K));
+  }
+  return SPK_OK;
+}
+
+}  // namespace spk
+
+extern "C" int spk_step_noalloc(const spk_device_net* net, int64_t n_steps, int32_t plasticity_on,
+                                float start_time, void* stream) {
+  return spk::step_noalloc_impl(net, n_steps, plasticity_on, start_time, (cudaStream_t)stream);
+}

@@ -35,3 +35,27 @@ def test_abi_version_and_error_without_gpu_work():
     assert lib.spk_net_create(None, None, None) == _native.SPK_ERR_INVALID
     assert lib.spk_net_run(None, ctypes.c_float(1.0), 1) == _native.SPK_ERR_INVALID
     assert isinstance(lib.spk_last_error(), bytes)
+
+
+def test_noalloc_rejects_networks_beyond_its_scratch():
+    """spk_step_noalloc checks its fixed scratch limit before any device call
+    (zero steps: nothing would run even if the check let it through)."""
+    lib = _native.lib()
+    g = (_native.NeuronGroup * 1)()
+    g[0].start, g[0].count, g[0].tau_m, g[0].R, g[0].theta = 0, 250000, 0.02, 1e8, 0.02
+    dummy = ctypes.create_string_buffer(64)
+    addr = ctypes.addressof(dummy)
+    dn = _native.DeviceNet()
+    dn.n_neurons, dn.n_inputs, dn.n_labels, dn.synapse_kind, dn.max_delay = 250000, 0, 1, _native.SPK_SYN_VOLTAGE, 1
+    dn.warps_per_cta, dn.tile_posts, dn.ctas = 8, 256, 128  # 4.2 MB of exchange keys
+    dn.dt, dn.refractory_period = 1e-4, 2e-3
+    dn.n_groups, dn.groups = 1, g
+    for f in ("rowptr", "entries", "V", "last_spike", "ring", "spikes", "run_state"):
+        setattr(dn, f, addr)
+    dn.spike_capacity = 1
+    rc = lib.spk_step_noalloc(ctypes.byref(dn), 0, 0, ctypes.c_float(0.0), None)
+    assert rc == _native.SPK_ERR_INVALID
+    assert b"bytes of step scratch" in lib.spk_last_error()
+    dn.tile_posts = 48  # not a multiple of 32
+    assert lib.spk_step_noalloc(ctypes.byref(dn), 0, 0, ctypes.c_float(0.0), None) == _native.SPK_ERR_INVALID
+    assert lib.spk_step_noalloc(None, 1, 0, ctypes.c_float(0.0), None) == _native.SPK_ERR_INVALID
