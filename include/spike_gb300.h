@@ -212,6 +212,69 @@ int spk_net_launch_count(const spk_net* net, int64_t* launches);
  * work or timing events against the engine. */
 int spk_net_stream(const spk_net* net, void** stream);
 
+/* ---- networks generated on the device -------------------------------------
+ * Replaces the host connectivity builder for large networks: the reference
+ * draws every (pre, post) pair of a RANDOM synapse group with rand() on the
+ * host and grows its synapse arrays with one realloc per synapse
+ * (Spike/Synapses/Synapses.cpp:208-228, 391-421), which takes minutes at
+ * 1e8-1e9 synapses.  Here each projection connects every (pre, post) pair of
+ * its rectangle with probability p, draws weight ~ U(lo, hi] and an integer
+ * delay ~ U{lo..hi}, all from Philox keyed by (connectivity_seed, pre, post),
+ * and the GPU writes the engine's CSR directly.
+ *
+ * Projections may not overlap in (pre, post), so a pair has at most one
+ * synapse and its draws do not depend on how projections are listed.  The
+ * synapse (creation) order of a generated network is ascending presynaptic
+ * key, then post: inputs n_inputs-1 .. 0, then neurons 0 .. n_neurons-1.
+ * spk_net_read_weights returns, in that order, the value each synapse
+ * delivers: weight*scale for static synapses, the weight for plastic ones
+ * (whose scale is applied on delivery); spk_net_write_weights is not
+ * available for generated networks. */
+typedef struct spk_projection {
+  int32_t pre_population; /* SPK_POP_NEURONS or SPK_POP_INPUTS */
+  int32_t pre_start;      /* first presynaptic index within that population */
+  int32_t pre_count;
+  int32_t post_start;     /* first postsynaptic neuron */
+  int32_t post_count;
+  float probability;      /* per pair, in [0, 1] */
+  float weight_lo, weight_hi;
+  float scale;            /* weight_scaling_constant */
+  int32_t delay_lo, delay_hi; /* timesteps, 1 <= lo <= hi <= 255 */
+  int32_t label;
+  int32_t plastic;        /* governed by the STDP rule (needs has_stdp) */
+} spk_projection;
+
+typedef struct spk_gen_desc {
+  int32_t abi_version;
+  float dt;
+  int32_t synapse_kind;
+  int32_t n_neurons;
+  int32_t n_groups;
+  const spk_neuron_group* groups;
+  float refractory_period;
+  float background_current;
+  int32_t n_inputs;
+  int32_t n_stimuli;
+  const float* input_rates; /* [n_stimuli][n_inputs] Hz */
+  int32_t stimulus;
+  int32_t n_labels;
+  const float* label_tau;
+  const float* label_vhat;
+  int32_t n_projections;
+  const spk_projection* projections;
+  int32_t has_stdp;
+  spk_stdp_params stdp;
+  uint64_t seed;              /* Poisson draws and V init, as in spk_net_desc */
+  uint64_t connectivity_seed; /* connection, weight and delay draws */
+  int64_t spike_capacity;
+  int32_t record_inputs;
+  int32_t reserved;
+} spk_gen_desc;
+
+int spk_net_generate(const spk_gen_desc* desc, const spk_schedule* schedule, spk_net** out);
+/* Synapses of a network (created or generated). */
+int spk_net_synapse_count(const spk_net* net, int64_t* n);
+
 /* ---- batch: many independent networks in one persistent launch ---------- */
 int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* schedule,
                      spk_batch** out);

@@ -49,6 +49,8 @@ def oracle_lib() -> C.CDLL:
         L.oracle_logf.argtypes = [C.c_float]
         L.oracle_log_max_ulp.restype = C.c_double
         L.oracle_log_max_ulp.argtypes = []
+        L.oracle_generate.restype = C.c_int64
+        L.oracle_generate.argtypes = [vp] + [vp] * 7 + [C.c_int64]
         _lib = L
     return _lib
 
@@ -151,3 +153,19 @@ def philox4x32_10(ctr, key):
     o = (C.c_uint32 * 4)()
     oracle_lib().oracle_philox4x32_10(c, k, o)
     return list(o)
+
+
+def generate_synapses(gen) -> dict:
+    """Synapse arrays (creation order) of a generated network, from the
+    oracle's restatement of the device generator.  `gen` is a GenDesc."""
+    L = oracle_lib()
+    n = L.oracle_generate(C.byref(gen), None, None, None, None, None, None, None, 0)
+    if n < 0:
+        raise RuntimeError("oracle_generate rejected the descriptor")
+    out = dict(pre=np.empty(n, np.int32), post=np.empty(n, np.int32), weight=np.empty(n, np.float32),
+               scale=np.empty(n, np.float32), delay=np.empty(n, np.int32), label=np.empty(n, np.int32),
+               plastic=np.empty(n, np.uint8))
+    got = L.oracle_generate(C.byref(gen), *(out[k].ctypes.data for k in
+                                            ("pre", "post", "weight", "scale", "delay", "label", "plastic")), n)
+    assert got == n
+    return out

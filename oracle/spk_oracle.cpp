@@ -843,4 +843,60 @@ double oracle_log_max_ulp(void) {
   return worst;
 }
 
+/* Connectivity of a generated network (spk_net_generate), restated on the
+ * host: for each presynaptic key in order (inputs n_inputs-1 .. 0, then
+ * neurons), each projection holding it (by ascending first post) and each of
+ * its posts, the pair connects when the uniform of Philox(connectivity_seed,
+ * (post/4, pre code, 0, CONNECT)) word post%4 is <= p; weight lo + (hi-lo)*u1
+ * and delay lo + min(floor(u2*(hi-lo+1)), hi-lo) come from Philox(post, pre
+ * code, 0, SYNAPSE) words 0 and 1.  Writes up to `capacity` synapses in that
+ * (creation) order with the spk_net_desc id convention and returns how many
+ * there are. */
+int64_t oracle_generate(const spk_gen_desc* d, int32_t* pre, int32_t* post, float* weight, float* scale,
+                        int32_t* delay, int32_t* label, uint8_t* plastic, int64_t capacity) {
+  if (!d || d->n_projections < 0 || (d->n_projections > 0 && !d->projections)) return -1;
+  std::vector<int> order(d->n_projections);
+  for (int j = 0; j < d->n_projections; ++j) order[j] = j;
+  for (int a = 1; a < d->n_projections; ++a)  // stable insertion sort by first post
+    for (int b = a; b > 0 && d->projections[order[b]].post_start < d->projections[order[b - 1]].post_start; --b) {
+      const int t = order[b];
+      order[b] = order[b - 1];
+      order[b - 1] = t;
+    }
+  int64_t n = 0;
+  const int n_keys = d->n_inputs + d->n_neurons;
+  for (int k = 0; k < n_keys; ++k) {
+    const bool is_input = k < d->n_inputs;
+    const int idx = is_input ? d->n_inputs - 1 - k : k - d->n_inputs;
+    const int pop = is_input ? SPK_POP_INPUTS : SPK_POP_NEURONS;
+    const uint32_t code = is_input ? (0x80000000u | (uint32_t)idx) : (uint32_t)idx;
+    for (int j : order) {
+      const spk_projection& P = d->projections[j];
+      if (P.pre_population != pop || idx < P.pre_start || idx >= P.pre_start + P.pre_count) continue;
+      for (int q = P.post_start; q < P.post_start + P.post_count; ++q) {
+        const spk::u32x4 c = spk::draw4(d->connectivity_seed, (uint32_t)q >> 2, code, spk::DOMAIN_CONNECT);
+        const uint32_t words[4] = {c.x, c.y, c.z, c.w};
+        if (!(spk::uniform_open0(words[q & 3]) <= P.probability)) continue;
+        if (n < capacity) {
+          const spk::u32x4 r = spk::draw4(d->connectivity_seed, (uint32_t)q, code, spk::DOMAIN_SYNAPSE);
+          const float span = P.weight_hi - P.weight_lo;
+          const float w = P.weight_lo + span * spk::uniform_open0(r.x);
+          const int nd = P.delay_hi - P.delay_lo + 1;
+          int dd = (int)(spk::uniform_open0(r.y) * (float)nd);
+          if (dd > nd - 1) dd = nd - 1;
+          if (pre) pre[n] = is_input ? -idx - 1 : idx;
+          if (post) post[n] = q;
+          if (weight) weight[n] = w;
+          if (scale) scale[n] = P.scale;
+          if (delay) delay[n] = P.delay_lo + dd;
+          if (label) label[n] = P.label;
+          if (plastic) plastic[n] = P.plastic ? 1 : 0;
+        }
+        ++n;
+      }
+    }
+  }
+  return n;
+}
+
 }  // extern "C"

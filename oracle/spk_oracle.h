@@ -54,6 +54,11 @@ int oracle_synaptic_events(const oracle_net* net, uint64_t* events);
 int oracle_sorted_synapses(const oracle_net* net, int32_t* pre, int32_t* post, int32_t* delay,
                            int64_t n);
 
+/* Synapses of a generated network (spk_gen_desc) in creation order; arrays
+ * may be NULL to count.  Returns the synapse count, or -1. */
+int64_t oracle_generate(const spk_gen_desc* desc, int32_t* pre, int32_t* post, float* weight, float* scale,
+                        int32_t* delay, int32_t* label, uint8_t* plastic, int64_t capacity);
+
 /* The shared counter-based generator and logarithm, for known-answer tests. */
 void oracle_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 float oracle_logf(float x);

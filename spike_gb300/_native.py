@@ -78,6 +78,26 @@ class NetDesc(C.Structure):
     ]
 
 
+class Projection(C.Structure):
+    _fields_ = [("pre_population", i32), ("pre_start", i32), ("pre_count", i32), ("post_start", i32),
+                ("post_count", i32), ("probability", f32), ("weight_lo", f32), ("weight_hi", f32), ("scale", f32),
+                ("delay_lo", i32), ("delay_hi", i32), ("label", i32), ("plastic", i32)]
+
+
+class GenDesc(C.Structure):
+    _fields_ = [
+        ("abi_version", i32), ("dt", f32), ("synapse_kind", i32),
+        ("n_neurons", i32), ("n_groups", i32), ("groups", P(NeuronGroup)),
+        ("refractory_period", f32), ("background_current", f32),
+        ("n_inputs", i32), ("n_stimuli", i32), ("input_rates", P(f32)), ("stimulus", i32),
+        ("n_labels", i32), ("label_tau", P(f32)), ("label_vhat", P(f32)),
+        ("n_projections", i32), ("projections", P(Projection)),
+        ("has_stdp", i32), ("stdp", StdpParams),
+        ("seed", u64), ("connectivity_seed", u64), ("spike_capacity", i64), ("record_inputs", i32),
+        ("reserved", i32),
+    ]
+
+
 class Schedule(C.Structure):
     _fields_ = [("warps_per_cta", i32), ("tile_posts", i32), ("ctas", i32), ("steps_per_launch", i32)]
 
@@ -125,6 +145,8 @@ _VP = C.c_void_p
 _SIGS = {
     # spike_gb300.h
     "spk_net_create": (i32, [P(NetDesc), P(Schedule), P(_VP)]),
+    "spk_net_generate": (i32, [P(GenDesc), P(Schedule), P(_VP)]),
+    "spk_net_synapse_count": (i32, [_VP, P(i64)]),
     "spk_net_destroy": (i32, [_VP]),
     "spk_net_reset_state": (i32, [_VP]),
     "spk_net_reset_time": (i32, [_VP]),

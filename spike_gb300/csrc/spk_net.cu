@@ -6,6 +6,9 @@
 // decays, STDP trace constants, initial V) must round exactly as the oracle's.
 #include <cuda_runtime.h>
 
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -17,6 +20,7 @@
 #include <vector>
 
 #include "../../include/spike_gb300.h"
+#include "spk_gen.cuh"
 #include "spk_internal.h"
 #include "spk_kernel.cuh"
 
@@ -188,6 +192,7 @@ struct spk_net {
   int64_t launches = 0;
   float current_time = 0.0f;
   int pending_status = SPK_OK;
+  bool generated = false;  // connectivity drawn on the device (no host synapse arrays)
 };
 
 struct spk_batch {
@@ -319,6 +324,317 @@ static int guarded(F&& f) {
   }
 }
 
+// Model constants shared by networks built from synapse arrays and networks
+// generated on the device.
+struct ModelSpec {
+  float dt = 0.f;
+  int kind = 0, N = 0, Nin = 0, L = 1;
+  int n_groups = 0;
+  const spk_neuron_group* groups = nullptr;
+  float t_ref = 0.f, i_bg = 0.f;
+  int n_stim = 0, stim = 0;
+  const float* rates = nullptr;
+  const float* label_tau = nullptr;
+  const float* label_vhat = nullptr;
+  int has_stdp = 0;
+  spk_stdp_params stdp{};
+  uint64_t seed = 0;
+  int64_t spike_capacity = 0;
+  int record_inputs = 0;
+};
+
+static int validate_spec(const ModelSpec& m) {
+  if (m.N <= 0 || m.Nin < 0 || m.L < 1 || m.L > MAX_LABELS || !(m.dt > 0.0f)) {
+    set_error("sizes out of range (neurons %d, inputs %d, labels %d)", m.N, m.Nin, m.L);
+    return SPK_ERR_INVALID;
+  }
+  if (m.kind != SPK_SYN_CONDUCTANCE && m.kind != SPK_SYN_CURRENT && m.kind != SPK_SYN_VOLTAGE) {
+    set_error("unknown synapse kind %d", m.kind);
+    return SPK_ERR_INVALID;
+  }
+  if (m.n_groups < 1 || m.n_groups > MAX_GROUPS || !m.groups) {
+    set_error("between 1 and %d neuron groups are supported (got %d)", MAX_GROUPS, m.n_groups);
+    return m.n_groups > MAX_GROUPS ? SPK_ERR_UNSUPPORTED : SPK_ERR_INVALID;
+  }
+  int expect = 0;
+  for (int g = 0; g < m.n_groups; ++g) {
+    if (m.groups[g].start != expect || m.groups[g].count <= 0) {
+      set_error("neuron groups must be contiguous, ascending and non-empty");
+      return SPK_ERR_INVALID;
+    }
+    expect += m.groups[g].count;
+  }
+  if (expect != m.N) {
+    set_error("neuron groups cover %d neurons, descriptor says %d", expect, m.N);
+    return SPK_ERR_INVALID;
+  }
+  if (m.Nin > 0 && (m.n_stim < 1 || !m.rates || m.stim < 0 || m.stim >= m.n_stim)) {
+    set_error("inputs need rates and a valid stimulus");
+    return SPK_ERR_INVALID;
+  }
+  if (m.kind != SPK_SYN_VOLTAGE && !m.label_tau) {
+    set_error("conductance/current synapses need label_tau");
+    return SPK_ERR_INVALID;
+  }
+  if (m.kind == SPK_SYN_CONDUCTANCE && !m.label_vhat) {
+    set_error("conductance synapses need label_vhat");
+    return SPK_ERR_INVALID;
+  }
+  return SPK_OK;
+}
+
+// A new handle with the model fields of `m` and a plan for ring depth B.
+static int new_net(const ModelSpec& m, int B, int64_t S, const spk_schedule* sched, spk_net** out) {
+  DeviceInfo di;
+  int rc = device_info(&di);
+  if (rc) return rc;
+  Plan plan;
+  rc = make_plan(m.N, m.Nin, B, m.L, m.kind, m.has_stdp ? 1 : 0, sched, di, &plan);
+  if (rc) return rc;
+  spk_net* n = new spk_net();
+  n->N = m.N;
+  n->Nin = m.Nin;
+  n->L = m.L;
+  n->B = B;
+  n->kind = m.kind;
+  n->S = S;
+  n->dt = m.dt;
+  n->has_stdp = m.has_stdp != 0;
+  n->record_inputs = m.record_inputs != 0;
+  n->seed = m.seed;
+  n->n_stim = m.Nin > 0 ? m.n_stim : 0;
+  n->stim = m.Nin > 0 ? m.stim : 0;
+  n->groups.assign(m.groups, m.groups + m.n_groups);
+  n->plan = plan;
+  n->scale_tab.assign(MAX_CLASSES, 0.0f);
+  *out = n;
+  return SPK_OK;
+}
+
+// Allocates the device arena of `n` (CSR parts sized by S and n_csc), creates
+// its stream, fills and uploads the device descriptor, uploads whichever host
+// CSR arrays are given (generated networks pass none and fill them on the
+// device afterwards), clears the exchange, checks co-residency and resets the
+// state.  On failure `n` is destroyed.
+static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int32_t* rowptr_h,
+                        const uint2* entries_h, const int32_t* csc_ptr_h, const uint2* csc_h) {
+  DeviceInfo di;
+  int rc = device_info(&di);
+  if (rc) {
+    delete n;
+    return rc;
+  }
+  const Plan& plan = n->plan;
+  const int N = n->N, Nin = n->Nin, L = n->L, B = n->B;
+  const int stdp = n->has_stdp ? 1 : 0;
+  const int64_t S = n->S;
+  const int n_tiles = plan.n_tiles, TS = plan.TS, KL = plan.KL, n_keys = plan.n_keys;
+  const size_t n_cells = (size_t)n_keys * n_tiles;
+  const int n_words = plan.n_words;
+  const int64_t spike_cap = m.spike_capacity == 0 ? DEFAULT_SPIKE_CAPACITY : std::max<int64_t>(0, m.spike_capacity);
+  struct Part {
+    void** dst;
+    size_t bytes;
+  };
+  NetDev& h = n->hd;
+  std::memset(&h, 0, sizeof(h));
+  void* p_rowptr = nullptr; void* p_entries = nullptr; void* p_cscptr = nullptr; void* p_csc = nullptr;
+  void* p_V = nullptr; void* p_last = nullptr; void* p_gtr = nullptr; void* p_ring = nullptr;
+  void* p_innext = nullptr; void* p_rates = nullptr; void* p_post = nullptr; void* p_pre = nullptr;
+  void* p_pub = nullptr; void* p_bA = nullptr; void* p_bP = nullptr; void* p_spk = nullptr;
+  void* p_ckeys = nullptr; void* p_cstamp = nullptr;
+  const int key_cap = plan.W * (plan.TS + plan.ITS);
+  void* p_ctl = nullptr; void* p_abort = nullptr; void* p_dd = nullptr; void* p_map = nullptr;
+  std::vector<Part> parts = {
+      {&p_rowptr, sizeof(int32_t) * (n_cells + 1)},
+      {&p_entries, sizeof(uint2) * (size_t)std::max<int64_t>(S, 1)},
+      {&p_cscptr, sizeof(int32_t) * (stdp ? (size_t)N + 1 : 0)},
+      {&p_csc, sizeof(uint2) * (size_t)n_csc},
+      {&p_V, sizeof(float) * N},
+      {&p_last, sizeof(float) * N},
+      {&p_gtr, sizeof(float) * (size_t)N * L},
+      {&p_ring, sizeof(float) * (size_t)n_tiles * B * TS * L},
+      {&p_innext, sizeof(float) * std::max(Nin, 1)},
+      {&p_rates, sizeof(float) * std::max<size_t>((size_t)n->n_stim * Nin, 1)},
+      {&p_post, sizeof(float) * (stdp ? N : 0)},
+      {&p_pre, sizeof(float) * (stdp ? n_keys : 0)},
+      {&p_pub, sizeof(float) * (stdp ? 2 * (size_t)n_keys : 0)},
+      {&p_bA, sizeof(uint32_t) * 2 * (size_t)n_words},
+      {&p_bP, sizeof(uint32_t) * 2 * (size_t)n_words},
+      {&p_ckeys, sizeof(unsigned long long) * 2 * (size_t)plan.nctas * key_cap},
+      {&p_cstamp, sizeof(unsigned long long) * 2 * (size_t)plan.nctas},
+      {&p_spk, sizeof(uint2) * (size_t)std::max<int64_t>(spike_cap, 1)},
+      {&p_ctl, sizeof(RunCtl)},
+      {&p_abort, sizeof(int)},
+      {&p_dd, sizeof(NetDev)},
+      {&p_map, sizeof(CtaMap) * plan.nctas},
+  };
+  size_t total = 0;
+  for (auto& p : parts) total = align_up(total, 256) + align_up(std::max<size_t>(p.bytes, 4), 256);
+  cudaError_t e = cudaMalloc(&n->arena, total);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error("device allocation of %zu bytes failed: %s", total, cudaGetErrorString(e));
+    delete n;
+    return SPK_ERR_OOM;
+  }
+  n->arena_bytes = total;
+  {
+    size_t off = 0;
+    for (auto& p : parts) {
+      off = align_up(off, 256);
+      *p.dst = (char*)n->arena + off;
+      off += align_up(std::max<size_t>(p.bytes, 4), 256);
+    }
+  }
+  auto fail_free = [&](int code) {
+    if (n->stream) cudaStreamDestroy(n->stream);
+    cudaFree(n->arena);
+    delete n;
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error("cudaStreamCreate failed");
+    return fail_free(SPK_ERR_CUDA);
+  }
+
+  // ---- device descriptor ---------------------------------------------------------
+  h.N = N;
+  h.Nin = Nin;
+  h.KL = KL;
+  h.n_keys = n_keys;
+  h.n_words = n_words;
+  h.L = L;
+  h.B = B;
+  h.kind = m.kind;
+  h.n_tiles = n_tiles;
+  h.TS = TS;
+  h.ITS = plan.ITS;
+  h.W = plan.W;
+  h.nctas = plan.nctas;
+  h.n_groups = m.n_groups;
+  h.dt = m.dt;
+  h.half_dt = 0.5f * m.dt;
+  h.t_ref = m.t_ref;
+  h.i_bg = m.i_bg;
+  for (int g = 0; g < m.n_groups; ++g) {
+    const spk_neuron_group& G = m.groups[g];
+    GroupConst& c = h.groups[g];
+    c.start = G.start;
+    c.end = G.start + G.count;
+    // LIFSpikingNeurons.cu:31-44: k = timestep / tau_m, kR = k * R (host float).
+    c.k = m.dt / G.tau_m;
+    c.kR = c.k * G.R;
+    c.v0 = G.v0;
+    c.vreset = G.vreset;
+    c.theta = G.theta;
+  }
+  for (int l = 0; l < L; ++l) {
+    // ConductanceSpikingSynapses.cu:76-78: expf(-timestep / tau_g) on the host.
+    h.decay[l] = m.kind == SPK_SYN_VOLTAGE ? 0.0f : expf(-m.dt / m.label_tau[l]);
+    h.vhat[l] = m.kind == SPK_SYN_CONDUCTANCE ? m.label_vhat[l] : 0.0f;
+  }
+  for (int c = 0; c < MAX_CLASSES; ++c) h.scale_tab[c] = n->scale_tab[c];
+  h.has_stdp = stdp;
+  if (stdp) {
+    const spk_stdp_params& sp = m.stdp;
+    // WeightDependentSTDPPlasticity.cu:125-145 for G = 1 (see stdp_update).
+    const float em = expf(-(1.0f * m.dt) / sp.tau_minus);
+    const float ep = expf(-(1.0f * m.dt) / sp.tau_plus);
+    h.E_m = em;
+    h.E_p = ep;
+    h.inc_m = sp.a_minus * em;
+    h.inc_p = sp.a_plus * ep;
+    h.invE_m = 1.0f / em;
+    h.invE_p = 1.0f / ep;
+    h.lam = sp.lambda;
+    h.lam_alpha = sp.lambda * sp.alpha;
+    h.wmax = sp.w_max;
+    h.clip_upper = sp.clip_upper ? 1 : 0;
+  }
+  h.seed = m.seed;
+  h.rowptr = (const int*)p_rowptr;
+  h.entries = (uint2*)p_entries;
+  h.csc_ptr = (const int*)p_cscptr;
+  h.csc = (const uint2*)p_csc;
+  h.V = (float*)p_V;
+  h.last = (float*)p_last;
+  h.gtr = (float*)p_gtr;
+  h.ring = (float*)p_ring;
+  h.in_next = (float*)p_innext;
+  n->rates_dev = (float*)p_rates;
+  h.rates = n->rates_dev + (size_t)n->stim * Nin;
+  h.post_trace = (float*)p_post;
+  h.pre_trace = (float*)p_pre;
+  h.pre_pub = (float*)p_pub;
+  h.bitsA = (uint32_t*)p_bA;
+  h.bitsP = (uint32_t*)p_bP;
+  h.cta_keys = (unsigned long long*)p_ckeys;
+  h.cta_stamp = (unsigned long long*)p_cstamp;
+  h.key_cap = key_cap;
+  h.spikes = (uint2*)p_spk;
+  h.spike_cap = spike_cap;
+  h.ctl = (RunCtl*)p_ctl;
+  h.abort_flag = (int*)p_abort;
+  n->abort_dev = (int*)p_abort;
+  n->dd = (NetDev*)p_dd;
+  n->dmap = (CtaMap*)p_map;
+
+  // ---- uploads ---------------------------------------------------------------------
+  auto up = [&](void* dst, const void* src, size_t bytes) -> int {
+    if (bytes == 0 || !src) return SPK_OK;
+    SPK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, n->stream));
+    return SPK_OK;
+  };
+  std::vector<CtaMap> map(plan.nctas);
+  for (int r = 0; r < plan.nctas; ++r) map[r] = CtaMap{0, r};
+  RunCtl ctl{};
+  int urc = SPK_OK;
+  urc |= up(p_rowptr, rowptr_h, sizeof(int32_t) * (n_cells + 1));
+  urc |= up(p_entries, entries_h, sizeof(uint2) * S);
+  urc |= up(p_cscptr, csc_ptr_h, sizeof(int32_t) * (stdp ? (size_t)N + 1 : 0));
+  urc |= up(p_csc, csc_h, sizeof(uint2) * (size_t)n_csc);
+  if (Nin > 0) urc |= up(p_rates, m.rates, sizeof(float) * (size_t)n->n_stim * Nin);
+  urc |= up(p_ctl, &ctl, sizeof(ctl));
+  urc |= up(p_dd, &h, sizeof(h));
+  urc |= up(p_map, map.data(), sizeof(CtaMap) * map.size());
+  if (urc) return fail_free(SPK_ERR_CUDA);
+  if (cudaMemsetAsync(p_bA, 0, sizeof(uint32_t) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
+      cudaMemsetAsync(p_bP, 0, sizeof(uint32_t) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
+      cudaMemsetAsync(p_cstamp, 0, sizeof(unsigned long long) * 2 * (size_t)plan.nctas, n->stream) != cudaSuccess ||
+      cudaMemsetAsync(p_ckeys, 0, sizeof(unsigned long long) * 2 * (size_t)plan.nctas * key_cap, n->stream) != cudaSuccess ||
+      cudaMemsetAsync(p_abort, 0, sizeof(int), n->stream) != cudaSuccess) {
+    set_error("cudaMemsetAsync failed");
+    return fail_free(SPK_ERR_CUDA);
+  }
+  if (cudaFuncSetAttribute(step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           di.max_smem) != cudaSuccess) {
+    set_error("cudaFuncSetAttribute failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return fail_free(SPK_ERR_CUDA);
+  }
+  if (plan.nctas > 1) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_kernel, plan.W * 32, plan.smem) !=
+        cudaSuccess) {
+      set_error("occupancy query failed");
+      return fail_free(SPK_ERR_CUDA);
+    }
+    if ((int64_t)per_sm * di.sms < plan.nctas) {
+      set_error("schedule needs %d co-resident CTAs, device holds %d", plan.nctas, per_sm * di.sms);
+      return fail_free(SPK_ERR_UNSUPPORTED);
+    }
+    n->cooperative = true;
+  }
+  int rrc = upload_state_defaults(n);
+  if (rrc) return fail_free(rrc);
+  if (cudaStreamSynchronize(n->stream) != cudaSuccess) {
+    set_error("initial upload failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return fail_free(SPK_ERR_CUDA);
+  }
+  build_graph(n);
+  return SPK_OK;
+}
+
 static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net** out) {
   if (!d || !out) {
     set_error("null argument");
@@ -328,46 +644,31 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
     set_error("descriptor ABI version %d, library %d", d->abi_version, SPK_ABI_VERSION);
     return SPK_ERR_INVALID;
   }
-  const int N = d->n_neurons, Nin = d->n_inputs, L = d->n_labels;
-  if (N <= 0 || Nin < 0 || L < 1 || L > MAX_LABELS || !(d->dt > 0.0f) || d->n_synapses < 0 ||
-      d->n_synapses > 0x7fffffffLL) {
-    set_error("descriptor sizes out of range (neurons %d, inputs %d, labels %d, synapses %lld)", N, Nin, L,
-              (long long)d->n_synapses);
-    return SPK_ERR_INVALID;
-  }
-  if (d->synapse_kind != SPK_SYN_CONDUCTANCE && d->synapse_kind != SPK_SYN_CURRENT &&
-      d->synapse_kind != SPK_SYN_VOLTAGE) {
-    set_error("unknown synapse kind %d", d->synapse_kind);
-    return SPK_ERR_INVALID;
-  }
-  if (d->n_groups < 1 || d->n_groups > MAX_GROUPS || !d->groups) {
-    set_error("between 1 and %d neuron groups are supported (got %d)", MAX_GROUPS, d->n_groups);
-    return d->n_groups > MAX_GROUPS ? SPK_ERR_UNSUPPORTED : SPK_ERR_INVALID;
-  }
-  {
-    int expect = 0;
-    for (int g = 0; g < d->n_groups; ++g) {
-      if (d->groups[g].start != expect || d->groups[g].count <= 0) {
-        set_error("neuron groups must be contiguous, ascending and non-empty");
-        return SPK_ERR_INVALID;
-      }
-      expect += d->groups[g].count;
-    }
-    if (expect != N) {
-      set_error("neuron groups cover %d neurons, descriptor says %d", expect, N);
-      return SPK_ERR_INVALID;
-    }
-  }
-  if (Nin > 0 && (d->n_stimuli < 1 || !d->input_rates || d->stimulus < 0 || d->stimulus >= d->n_stimuli)) {
-    set_error("inputs need rates and a valid stimulus");
-    return SPK_ERR_INVALID;
-  }
-  if (d->synapse_kind != SPK_SYN_VOLTAGE && !d->label_tau) {
-    set_error("conductance/current synapses need label_tau");
-    return SPK_ERR_INVALID;
-  }
-  if (d->synapse_kind == SPK_SYN_CONDUCTANCE && !d->label_vhat) {
-    set_error("conductance synapses need label_vhat");
+  ModelSpec m;
+  m.dt = d->dt;
+  m.kind = d->synapse_kind;
+  m.N = d->n_neurons;
+  m.Nin = d->n_inputs;
+  m.L = d->n_labels;
+  m.n_groups = d->n_groups;
+  m.groups = d->groups;
+  m.t_ref = d->refractory_period;
+  m.i_bg = d->background_current;
+  m.n_stim = d->n_stimuli;
+  m.stim = d->stimulus;
+  m.rates = d->input_rates;
+  m.label_tau = d->label_tau;
+  m.label_vhat = d->label_vhat;
+  m.has_stdp = d->has_stdp ? 1 : 0;
+  m.stdp = d->stdp;
+  m.seed = d->seed;
+  m.spike_capacity = d->spike_capacity;
+  m.record_inputs = d->record_inputs;
+  int rc = validate_spec(m);
+  if (rc) return rc;
+  const int N = m.N, Nin = m.Nin, L = m.L;
+  if (d->n_synapses < 0 || d->n_synapses > 0x7fffffffLL) {
+    set_error("synapse count %lld out of range", (long long)d->n_synapses);
     return SPK_ERR_INVALID;
   }
   const int64_t S = d->n_synapses;
@@ -395,35 +696,16 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
   }
   if (S == 0) Dmax = 1;
   const int B = Dmax + 2 * 1 + 1;  // SpikingSynapses.cu:48 with G = 1
-  const int stdp = d->has_stdp ? 1 : 0;
+  const int stdp = m.has_stdp;
 
-  DeviceInfo di;
-  int rc = device_info(&di);
+  spk_net* n = nullptr;
+  rc = new_net(m, B, S, sched, &n);
   if (rc) return rc;
-  Plan plan;
-  rc = make_plan(N, Nin, B, L, d->synapse_kind, stdp, sched, di, &plan);
-  if (rc) return rc;
-
-  spk_net* n = new spk_net();
-  n->N = N;
-  n->Nin = Nin;
-  n->L = L;
-  n->B = B;
-  n->kind = d->synapse_kind;
-  n->S = S;
-  n->dt = d->dt;
-  n->has_stdp = stdp != 0;
-  n->record_inputs = d->record_inputs != 0;
-  n->seed = d->seed;
-  n->n_stim = Nin > 0 ? d->n_stimuli : 0;
-  n->stim = Nin > 0 ? d->stimulus : 0;
-  n->groups.assign(d->groups, d->groups + d->n_groups);
-  n->plan = plan;
+  const Plan& plan = n->plan;
   n->weights.assign(d->weight, d->weight + S);
   n->scales.assign(d->scale, d->scale + S);
 
   // ---- scale classes of plastic synapses ------------------------------------
-  n->scale_tab.assign(MAX_CLASSES, 0.0f);
   n->cls_of.assign(S, 0);
   {
     std::map<uint32_t, int> cls;
@@ -487,210 +769,321 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
     for (int64_t s = 0; s < S; ++s)
       if (n->cls_of[s]) csc[fill[d->post[s]]++] = make_uint2((uint32_t)n->entry_of[s], (uint32_t)key_of(d->pre[s]));
   }
+  rc = setup_device(n, m, (int64_t)csc.size(), rowptr.data(), entries.data(), stdp ? csc_ptr.data() : nullptr,
+                    csc.data());
+  if (rc) return rc;
+  *out = n;
+  return SPK_OK;
+}
 
-  // ---- device arena --------------------------------------------------------------
-  const int n_words = plan.n_words;
-  int64_t spike_cap = d->spike_capacity == 0 ? DEFAULT_SPIKE_CAPACITY : std::max<int64_t>(0, d->spike_capacity);
-  struct Part {
-    void** dst;
-    size_t bytes;
-  };
-  NetDev& h = n->hd;
-  std::memset(&h, 0, sizeof(h));
-  void* p_rowptr = nullptr; void* p_entries = nullptr; void* p_cscptr = nullptr; void* p_csc = nullptr;
-  void* p_V = nullptr; void* p_last = nullptr; void* p_gtr = nullptr; void* p_ring = nullptr;
-  void* p_innext = nullptr; void* p_rates = nullptr; void* p_post = nullptr; void* p_pre = nullptr;
-  void* p_pub = nullptr; void* p_bA = nullptr; void* p_bP = nullptr; void* p_spk = nullptr;
-  void* p_ckeys = nullptr; void* p_cstamp = nullptr;
-  const int key_cap = plan.W * (plan.TS + plan.ITS);
-  void* p_ctl = nullptr; void* p_abort = nullptr; void* p_dd = nullptr; void* p_map = nullptr;
-  std::vector<Part> parts = {
-      {&p_rowptr, sizeof(int32_t) * rowptr.size()},
-      {&p_entries, sizeof(uint2) * (size_t)std::max<int64_t>(S, 1)},
-      {&p_cscptr, sizeof(int32_t) * csc_ptr.size()},
-      {&p_csc, sizeof(uint2) * csc.size()},
-      {&p_V, sizeof(float) * N},
-      {&p_last, sizeof(float) * N},
-      {&p_gtr, sizeof(float) * (size_t)N * L},
-      {&p_ring, sizeof(float) * (size_t)n_tiles * B * TS * L},
-      {&p_innext, sizeof(float) * std::max(Nin, 1)},
-      {&p_rates, sizeof(float) * std::max<size_t>((size_t)n->n_stim * Nin, 1)},
-      {&p_post, sizeof(float) * (stdp ? N : 0)},
-      {&p_pre, sizeof(float) * (stdp ? n_keys : 0)},
-      {&p_pub, sizeof(float) * (stdp ? 2 * (size_t)n_keys : 0)},
-      {&p_bA, sizeof(uint32_t) * 2 * (size_t)n_words},
-      {&p_bP, sizeof(uint32_t) * 2 * (size_t)n_words},
-      {&p_ckeys, sizeof(unsigned long long) * 2 * (size_t)plan.nctas * key_cap},
-      {&p_cstamp, sizeof(unsigned long long) * 2 * (size_t)plan.nctas},
-      {&p_spk, sizeof(uint2) * (size_t)std::max<int64_t>(spike_cap, 1)},
-      {&p_ctl, sizeof(RunCtl)},
-      {&p_abort, sizeof(int)},
-      {&p_dd, sizeof(NetDev)},
-      {&p_map, sizeof(CtaMap) * plan.nctas},
-  };
-  size_t total = 0;
-  for (auto& p : parts) total = align_up(total, 256) + align_up(std::max<size_t>(p.bytes, 4), 256);
-  cudaError_t e = cudaMalloc(&n->arena, total);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    set_error("device allocation of %zu bytes failed: %s", total, cudaGetErrorString(e));
-    delete n;
-    return SPK_ERR_OOM;
+// Device memory released on scope exit (temporaries of network generation).
+struct DevTemp {
+  void* p = nullptr;
+  DevTemp() = default;
+  DevTemp(const DevTemp&) = delete;
+  DevTemp& operator=(const DevTemp&) = delete;
+  ~DevTemp() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
   }
-  n->arena_bytes = total;
-  {
-    size_t off = 0;
-    for (auto& p : parts) {
-      off = align_up(off, 256);
-      *p.dst = (char*)n->arena + off;
-      off += align_up(std::max<size_t>(p.bytes, 4), 256);
+  bool alloc(size_t bytes) {
+    reset();
+    if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      set_error("device allocation of %zu bytes for network generation failed", bytes);
+      return false;
     }
+    return true;
   }
-  auto fail_free = [&](int code) {
-    if (n->stream) cudaStreamDestroy(n->stream);
-    cudaFree(n->arena);
-    delete n;
-    return code;
-  };
-  if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  template <typename T>
+  T* as() const {
+    return (T*)p;
+  }
+};
+
+static int generate_impl(const spk_gen_desc* d, const spk_schedule* sched, spk_net** out) {
+  if (!d || !out) {
+    set_error("null argument");
+    return SPK_ERR_INVALID;
+  }
+  if (d->abi_version != SPK_ABI_VERSION) {
+    set_error("descriptor ABI version %d, library %d", d->abi_version, SPK_ABI_VERSION);
+    return SPK_ERR_INVALID;
+  }
+  ModelSpec m;
+  m.dt = d->dt;
+  m.kind = d->synapse_kind;
+  m.N = d->n_neurons;
+  m.Nin = d->n_inputs;
+  m.L = d->n_labels;
+  m.n_groups = d->n_groups;
+  m.groups = d->groups;
+  m.t_ref = d->refractory_period;
+  m.i_bg = d->background_current;
+  m.n_stim = d->n_stimuli;
+  m.stim = d->stimulus;
+  m.rates = d->input_rates;
+  m.label_tau = d->label_tau;
+  m.label_vhat = d->label_vhat;
+  m.has_stdp = d->has_stdp ? 1 : 0;
+  m.stdp = d->stdp;
+  m.seed = d->seed;
+  m.spike_capacity = d->spike_capacity;
+  m.record_inputs = d->record_inputs;
+  int rc = validate_spec(m);
+  if (rc) return rc;
+  const int N = m.N, Nin = m.Nin, L = m.L;
+  const int n_proj = d->n_projections;
+  if (n_proj < 0 || n_proj > MAX_PROJECTIONS || (n_proj > 0 && !d->projections)) {
+    set_error("between 0 and %d projections are supported (got %d)", MAX_PROJECTIONS, n_proj);
+    return SPK_ERR_INVALID;
+  }
+  // ---- projections: validate, assign plastic scale classes, sort by first post
+  std::vector<GenProj> proj;
+  std::map<uint32_t, int> cls;
+  std::vector<float> scale_tab(MAX_CLASSES, 0.0f);
+  int dlo_min = 1 << 30;
+  for (int j = 0; j < n_proj; ++j) {
+    const spk_projection& P = d->projections[j];
+    const int pop_size = P.pre_population == SPK_POP_INPUTS ? Nin : N;
+    if ((P.pre_population != SPK_POP_NEURONS && P.pre_population != SPK_POP_INPUTS) || P.pre_start < 0 ||
+        P.pre_count < 0 || (int64_t)P.pre_start + P.pre_count > pop_size || P.post_start < 0 || P.post_count < 0 ||
+        (int64_t)P.post_start + P.post_count > N || !(P.probability >= 0.0f && P.probability <= 1.0f) ||
+        P.delay_lo < 1 || P.delay_hi < P.delay_lo || P.delay_hi > MAX_DELAY || P.label < 0 || P.label >= L ||
+        (P.plastic && !m.has_stdp)) {
+      set_error("projection %d out of range (pre %d+%d of %d, post %d+%d, p %g, delays %d..%d, label %d, plastic %d)",
+                j, P.pre_start, P.pre_count, pop_size, P.post_start, P.post_count, (double)P.probability,
+                P.delay_lo, P.delay_hi, P.label, P.plastic);
+      return SPK_ERR_INVALID;
+    }
+    for (int k = 0; k < j; ++k) {
+      const spk_projection& Q = d->projections[k];
+      const bool pre_overlap = Q.pre_population == P.pre_population && P.pre_start < Q.pre_start + Q.pre_count &&
+                               Q.pre_start < P.pre_start + P.pre_count;
+      const bool post_overlap =
+          P.post_start < Q.post_start + Q.post_count && Q.post_start < P.post_start + P.post_count;
+      if (pre_overlap && post_overlap && P.pre_count && P.post_count && Q.pre_count && Q.post_count) {
+        set_error("projections %d and %d overlap in (pre, post)", k, j);
+        return SPK_ERR_INVALID;
+      }
+    }
+    GenProj g;
+    g.pop = P.pre_population;
+    g.pre_lo = P.pre_start;
+    g.pre_hi = P.pre_start + P.pre_count;
+    g.post_lo = P.post_start;
+    g.post_hi = P.post_start + P.post_count;
+    g.p = P.probability;
+    g.w_lo = P.weight_lo;
+    g.w_span = P.weight_hi - P.weight_lo;
+    g.scale = P.scale;
+    g.d_lo = P.delay_lo;
+    g.d_n = P.delay_hi - P.delay_lo + 1;
+    g.label = P.label;
+    g.cls = 0;
+    if (P.plastic) {
+      const uint32_t bits = f2u(P.scale);
+      auto it = cls.find(bits);
+      if (it == cls.end()) {
+        const int c = (int)cls.size() + 1;
+        if (c >= MAX_CLASSES) {
+          set_error("more than %d distinct weight scales among plastic projections", MAX_CLASSES - 1);
+          return SPK_ERR_UNSUPPORTED;
+        }
+        cls[bits] = c;
+        scale_tab[c] = P.scale;
+        g.cls = c;
+      } else {
+        g.cls = it->second;
+      }
+    }
+    if (P.probability > 0.0f && P.pre_count > 0 && P.post_count > 0) dlo_min = std::min(dlo_min, P.delay_lo);
+    proj.push_back(g);
+  }
+  std::stable_sort(proj.begin(), proj.end(), [](const GenProj& a, const GenProj& b) { return a.post_lo < b.post_lo; });
+  if (dlo_min != (1 << 30) && dlo_min != 1) {
+    set_error("minimum delay %d steps: timestep grouping > 1 is not supported", dlo_min);
+    return SPK_ERR_UNSUPPORTED;
+  }
+
+  DeviceInfo di;
+  rc = device_info(&di);
+  if (rc) return rc;
+  // The schedule does not change the connectivity, only the cells it is cut
+  // into; the ring depth needs the largest drawn delay, so plan with the
+  // largest possible one first and re-plan if fewer are drawn.
+  int dmax_bound = 1;
+  for (const auto& g : proj) dmax_bound = std::max(dmax_bound, g.d_lo + g.d_n - 1);
+  spk_net* probe = nullptr;
+  rc = new_net(m, dmax_bound + 3, 0, sched, &probe);
+  if (rc) return rc;
+  const Plan plan0 = probe->plan;
+  delete probe;
+
+  cudaStream_t st = nullptr;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
     set_error("cudaStreamCreate failed");
-    return fail_free(SPK_ERR_CUDA);
+    return SPK_ERR_CUDA;
   }
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+  } sg{st};
+  const int grid = std::max(1, di.sms * 8);
+  auto gen_shape = [&](const Plan& pl) {
+    GenShape g;
+    g.N = N;
+    g.Nin = Nin;
+    g.KL = pl.KL;
+    g.n_tiles = pl.n_tiles;
+    g.TS = pl.TS;
+    g.n_proj = (int)proj.size();
+    g.n_cells = (long long)pl.n_keys * pl.n_tiles;
+    g.seed = d->connectivity_seed;
+    return g;
+  };
+  DevTemp proj_dev, small;
+  if (!proj_dev.alloc(sizeof(GenProj) * proj.size()) || !small.alloc(64)) return SPK_ERR_OOM;
+  if (!proj.empty())
+    SPK_CUDA(cudaMemcpyAsync(proj_dev.p, proj.data(), sizeof(GenProj) * proj.size(), cudaMemcpyHostToDevice, st));
+  unsigned long long* totals = small.as<unsigned long long>();  // [0] all, [1] plastic
+  int* drange = (int*)(totals + 2);                             // [0] min, [1] max drawn delay
 
-  // ---- device descriptor ---------------------------------------------------------
-  h.N = N;
-  h.Nin = Nin;
-  h.KL = KL;
-  h.n_keys = n_keys;
-  h.n_words = n_words;
-  h.L = L;
-  h.B = B;
-  h.kind = d->synapse_kind;
-  h.n_tiles = n_tiles;
-  h.TS = TS;
-  h.ITS = plan.ITS;
-  h.W = plan.W;
-  h.nctas = plan.nctas;
-  h.n_groups = d->n_groups;
-  h.dt = d->dt;
-  h.half_dt = 0.5f * d->dt;
-  h.t_ref = d->refractory_period;
-  h.i_bg = d->background_current;
-  for (int g = 0; g < d->n_groups; ++g) {
-    const spk_neuron_group& G = d->groups[g];
-    GroupConst& c = h.groups[g];
-    c.start = G.start;
-    c.end = G.start + G.count;
-    // LIFSpikingNeurons.cu:31-44: k = timestep / tau_m, kR = k * R (host float).
-    c.k = d->dt / G.tau_m;
-    c.kR = c.k * G.R;
-    c.v0 = G.v0;
-    c.vreset = G.vreset;
-    c.theta = G.theta;
-  }
-  for (int l = 0; l < L; ++l) {
-    // ConductanceSpikingSynapses.cu:76-78: expf(-timestep / tau_g) on the host.
-    h.decay[l] = d->synapse_kind == SPK_SYN_VOLTAGE ? 0.0f : expf(-d->dt / d->label_tau[l]);
-    h.vhat[l] = d->synapse_kind == SPK_SYN_CONDUCTANCE ? d->label_vhat[l] : 0.0f;
-  }
-  for (int c = 0; c < MAX_CLASSES; ++c) h.scale_tab[c] = n->scale_tab[c];
-  h.has_stdp = stdp;
-  if (stdp) {
-    const spk_stdp_params& sp = d->stdp;
-    // WeightDependentSTDPPlasticity.cu:125-145 for G = 1 (see stdp_update).
-    const float em = expf(-(1.0f * d->dt) / sp.tau_minus);
-    const float ep = expf(-(1.0f * d->dt) / sp.tau_plus);
-    h.E_m = em;
-    h.E_p = ep;
-    h.inc_m = sp.a_minus * em;
-    h.inc_p = sp.a_plus * ep;
-    h.invE_m = 1.0f / em;
-    h.invE_p = 1.0f / ep;
-    h.lam = sp.lambda;
-    h.lam_alpha = sp.lambda * sp.alpha;
-    h.wmax = sp.w_max;
-    h.clip_upper = sp.clip_upper ? 1 : 0;
-  }
-  h.seed = d->seed;
-  h.rowptr = (const int*)p_rowptr;
-  h.entries = (uint2*)p_entries;
-  h.csc_ptr = (const int*)p_cscptr;
-  h.csc = (const uint2*)p_csc;
-  h.V = (float*)p_V;
-  h.last = (float*)p_last;
-  h.gtr = (float*)p_gtr;
-  h.ring = (float*)p_ring;
-  h.in_next = (float*)p_innext;
-  n->rates_dev = (float*)p_rates;
-  h.rates = n->rates_dev + (size_t)n->stim * Nin;
-  h.post_trace = (float*)p_post;
-  h.pre_trace = (float*)p_pre;
-  h.pre_pub = (float*)p_pub;
-  h.bitsA = (uint32_t*)p_bA;
-  h.bitsP = (uint32_t*)p_bP;
-  h.cta_keys = (unsigned long long*)p_ckeys;
-  h.cta_stamp = (unsigned long long*)p_cstamp;
-  h.key_cap = key_cap;
-  h.spikes = (uint2*)p_spk;
-  h.spike_cap = spike_cap;
-  h.ctl = (RunCtl*)p_ctl;
-  h.abort_flag = (int*)p_abort;
-  n->abort_dev = (int*)p_abort;
-  n->dd = (NetDev*)p_dd;
-  n->dmap = (CtaMap*)p_map;
-
-  // ---- uploads ---------------------------------------------------------------------
-  auto up = [&](void* dst, const void* src, size_t bytes) -> int {
-    if (bytes == 0) return SPK_OK;
-    SPK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, n->stream));
+  // ---- count pass (with the plan for the largest possible delay) -------------------
+  auto count_pass = [&](const Plan& pl, DevTemp& counts, unsigned long long host_tot[2], int host_dr[2]) -> int {
+    const GenShape g = gen_shape(pl);
+    if (!counts.alloc(sizeof(int) * (size_t)(g.n_cells + 1))) return SPK_ERR_OOM;
+    const unsigned long long zero2[2] = {0ull, 0ull};
+    const int dr0[2] = {1 << 30, 0};
+    SPK_CUDA(cudaMemcpyAsync(totals, zero2, sizeof(zero2), cudaMemcpyHostToDevice, st));
+    SPK_CUDA(cudaMemcpyAsync(drange, dr0, sizeof(dr0), cudaMemcpyHostToDevice, st));
+    SPK_CUDA(cudaMemsetAsync(counts.as<int>() + g.n_cells, 0, sizeof(int), st));
+    gen_cells_kernel<false><<<grid, 256, 0, st>>>(g, proj_dev.as<GenProj>(), counts.as<int>(), totals, nullptr,
+                                                  nullptr, nullptr, nullptr, nullptr, drange);
+    SPK_CUDA(cudaGetLastError());
+    SPK_CUDA(cudaMemcpyAsync(host_tot, totals, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    SPK_CUDA(cudaMemcpyAsync(host_dr, drange, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    SPK_CUDA(cudaStreamSynchronize(st));
     return SPK_OK;
   };
-  std::vector<CtaMap> map(plan.nctas);
-  for (int r = 0; r < plan.nctas; ++r) map[r] = CtaMap{0, r};
-  RunCtl ctl{};
-  int urc = SPK_OK;
-  urc |= up(p_rowptr, rowptr.data(), sizeof(int32_t) * rowptr.size());
-  urc |= up(p_entries, entries.data(), sizeof(uint2) * S);
-  urc |= up(p_cscptr, csc_ptr.data(), sizeof(int32_t) * csc_ptr.size());
-  urc |= up(p_csc, csc.data(), sizeof(uint2) * csc.size());
-  if (Nin > 0) urc |= up(p_rates, d->input_rates, sizeof(float) * (size_t)n->n_stim * Nin);
-  urc |= up(p_ctl, &ctl, sizeof(ctl));
-  urc |= up(p_dd, &h, sizeof(h));
-  urc |= up(p_map, map.data(), sizeof(CtaMap) * map.size());
-  if (urc) return fail_free(SPK_ERR_CUDA);
-  if (cudaMemsetAsync(p_bA, 0, sizeof(uint32_t) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
-      cudaMemsetAsync(p_bP, 0, sizeof(uint32_t) * 2 * (size_t)n_words, n->stream) != cudaSuccess ||
-      cudaMemsetAsync(p_cstamp, 0, sizeof(unsigned long long) * 2 * (size_t)plan.nctas, n->stream) != cudaSuccess ||
-      cudaMemsetAsync(p_ckeys, 0, sizeof(unsigned long long) * 2 * (size_t)plan.nctas * key_cap, n->stream) != cudaSuccess ||
-      cudaMemsetAsync(p_abort, 0, sizeof(int), n->stream) != cudaSuccess) {
-    set_error("cudaMemsetAsync failed");
-    return fail_free(SPK_ERR_CUDA);
+  DevTemp counts;
+  unsigned long long tot[2] = {0, 0};
+  int dr[2] = {0, 0};
+  rc = count_pass(plan0, counts, tot, dr);
+  if (rc) return rc;
+  if (tot[0] > 0x7fffffffull) {
+    set_error("generated network has %llu synapses; at most 2^31-1 per network are supported", tot[0]);
+    return SPK_ERR_UNSUPPORTED;
   }
-  if (cudaFuncSetAttribute(step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           di.max_smem) != cudaSuccess) {
-    set_error("cudaFuncSetAttribute failed: %s", cudaGetErrorString(cudaGetLastError()));
-    return fail_free(SPK_ERR_CUDA);
+  if (tot[0] > 0 && dr[0] != 1) {
+    set_error("minimum drawn delay %d steps: timestep grouping > 1 is not supported", dr[0]);
+    return SPK_ERR_UNSUPPORTED;
   }
-  if (plan.nctas > 1) {
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_kernel, plan.W * 32, plan.smem) !=
+  const int Dmax = tot[0] > 0 ? dr[1] : 1;
+  const int B = Dmax + 2 * 1 + 1;  // SpikingSynapses.cu:48 with G = 1
+  spk_net* n = nullptr;
+  rc = new_net(m, B, (int64_t)tot[0], sched, &n);
+  if (rc) return rc;
+  if (n->plan.TS != plan0.TS || n->plan.nctas != plan0.nctas || n->plan.W != plan0.W) {
+    // a shallower ring let the planner pick another cut: count again
+    unsigned long long tot2[2];
+    int dr2[2];
+    rc = count_pass(n->plan, counts, tot2, dr2);
+    if (rc == SPK_OK && (tot2[0] != tot[0] || tot2[1] != tot[1])) {
+      set_error("generated synapse count changed with the schedule (%llu vs %llu)", tot2[0], tot[0]);
+      rc = SPK_ERR_CUDA;
+    }
+    if (rc) {
+      delete n;
+      return rc;
+    }
+  }
+  const int64_t S = (int64_t)tot[0], P = (int64_t)tot[1];
+  for (int c = 0; c < MAX_CLASSES; ++c) n->scale_tab[c] = scale_tab[c];
+  n->generated = true;
+  rc = setup_device(n, m, m.has_stdp ? P : 0, nullptr, nullptr, nullptr, nullptr);
+  if (rc) return rc;  // n destroyed
+  auto fail = [&](int code) {
+    cudaStreamSynchronize(st);
+    spk_net_destroy(n);
+    return code;
+  };
+  const Plan& pl = n->plan;
+  const GenShape g = gen_shape(pl);
+  const long long n_cells = g.n_cells;
+  // ---- row pointers, entries, plastic afferents -------------------------------------
+  {
+    size_t tb = 0;
+    if (cub::DeviceScan::ExclusiveSum(nullptr, tb, counts.as<int>(), (int*)n->hd.rowptr, n_cells + 1, st) !=
+        cudaSuccess)
+      return fail(SPK_ERR_CUDA);
+    DevTemp tmp;
+    if (!tmp.alloc(tb)) return fail(SPK_ERR_OOM);
+    if (cub::DeviceScan::ExclusiveSum(tmp.p, tb, counts.as<int>(), (int*)n->hd.rowptr, n_cells + 1, st) !=
         cudaSuccess) {
-      set_error("occupancy query failed");
-      return fail_free(SPK_ERR_CUDA);
+      set_error("row pointer scan failed: %s", cudaGetErrorString(cudaGetLastError()));
+      return fail(SPK_ERR_CUDA);
     }
-    if ((int64_t)per_sm * di.sms < plan.nctas) {
-      set_error("schedule needs %d co-resident CTAs, device holds %d", plan.nctas, per_sm * di.sms);
-      return fail_free(SPK_ERR_UNSUPPORTED);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return fail(SPK_ERR_CUDA);
+  }
+  const bool csc = m.has_stdp && P > 0;
+  DevTemp sort_a, sort_b, val_a, val_b, ekey, pcnt;
+  if (m.has_stdp && !csc &&
+      cudaMemsetAsync((void*)n->hd.csc_ptr, 0, sizeof(int) * ((size_t)N + 1), st) != cudaSuccess)
+    return fail(SPK_ERR_CUDA);
+  if (csc) {
+    if (!sort_a.alloc(sizeof(uint32_t) * S) || !sort_b.alloc(sizeof(uint32_t) * S) ||
+        !val_a.alloc(sizeof(uint32_t) * S) || !val_b.alloc(sizeof(uint32_t) * S) ||
+        !ekey.alloc(sizeof(uint32_t) * S) || !pcnt.alloc(sizeof(int) * ((size_t)N + 1)))
+      return fail(SPK_ERR_OOM);
+    if (cudaMemsetAsync(pcnt.p, 0, sizeof(int) * ((size_t)N + 1), st) != cudaSuccess) return fail(SPK_ERR_CUDA);
+  }
+  gen_cells_kernel<true><<<grid, 256, 0, st>>>(g, proj_dev.as<GenProj>(), nullptr, nullptr, n->hd.rowptr,
+                                               n->hd.entries, csc ? sort_a.as<uint32_t>() : nullptr,
+                                               csc ? ekey.as<uint32_t>() : nullptr, csc ? pcnt.as<int>() : nullptr,
+                                               nullptr);
+  if (cudaGetLastError() != cudaSuccess) return fail(SPK_ERR_CUDA);
+  if (csc) {
+    size_t tb = 0;
+    if (cub::DeviceScan::ExclusiveSum(nullptr, tb, pcnt.as<int>(), (int*)n->hd.csc_ptr, (long long)N + 1, st) !=
+        cudaSuccess)
+      return fail(SPK_ERR_CUDA);
+    DevTemp tmp;
+    if (!tmp.alloc(tb)) return fail(SPK_ERR_OOM);
+    if (cub::DeviceScan::ExclusiveSum(tmp.p, tb, pcnt.as<int>(), (int*)n->hd.csc_ptr, (long long)N + 1, st) !=
+        cudaSuccess)
+      return fail(SPK_ERR_CUDA);
+    gen_iota_kernel<<<grid, 256, 0, st>>>(val_a.as<uint32_t>(), S);
+    if (cudaGetLastError() != cudaSuccess) return fail(SPK_ERR_CUDA);
+    int end_bit = 1;
+    while (end_bit < 32 && ((uint32_t)N >> end_bit) != 0u) ++end_bit;
+    cub::DoubleBuffer<uint32_t> keys(sort_a.as<uint32_t>(), sort_b.as<uint32_t>());
+    cub::DoubleBuffer<uint32_t> vals(val_a.as<uint32_t>(), val_b.as<uint32_t>());
+    size_t sb = 0;
+    if (cub::DeviceRadixSort::SortPairs(nullptr, sb, keys, vals, (long long)S, 0, end_bit, st) != cudaSuccess)
+      return fail(SPK_ERR_CUDA);
+    DevTemp stmp;
+    if (!stmp.alloc(sb)) return fail(SPK_ERR_OOM);
+    if (cub::DeviceRadixSort::SortPairs(stmp.p, sb, keys, vals, (long long)S, 0, end_bit, st) != cudaSuccess) {
+      set_error("plastic afferent sort failed: %s", cudaGetErrorString(cudaGetLastError()));
+      return fail(SPK_ERR_CUDA);
     }
-    n->cooperative = true;
+    gen_csc_kernel<<<grid, 256, 0, st>>>((uint2*)n->hd.csc, vals.Current(), ekey.as<uint32_t>(), (long long)P);
+    if (cudaGetLastError() != cudaSuccess) return fail(SPK_ERR_CUDA);
+    if (cudaStreamSynchronize(st) != cudaSuccess) {
+      set_error("network generation failed: %s", cudaGetErrorString(cudaGetLastError()));
+      return fail(SPK_ERR_CUDA);
+    }
   }
-  int rrc = upload_state_defaults(n);
-  if (rrc) return fail_free(rrc);
-  if (cudaStreamSynchronize(n->stream) != cudaSuccess) {
-    set_error("initial upload failed: %s", cudaGetErrorString(cudaGetLastError()));
-    return fail_free(SPK_ERR_CUDA);
+  if (cudaStreamSynchronize(st) != cudaSuccess) {
+    set_error("network generation failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return fail(SPK_ERR_CUDA);
   }
-  build_graph(n);
   *out = n;
   return SPK_OK;
 }
@@ -705,6 +1098,16 @@ int spk_abi_version(void) { return SPK_ABI_VERSION; }
 
 int spk_net_create(const spk_net_desc* desc, const spk_schedule* schedule, spk_net** out) {
   return guarded([&] { return create_impl(desc, schedule, out); });
+}
+
+int spk_net_generate(const spk_gen_desc* desc, const spk_schedule* schedule, spk_net** out) {
+  return guarded([&] { return generate_impl(desc, schedule, out); });
+}
+
+int spk_net_synapse_count(const spk_net* n, int64_t* count) {
+  if (!n || !count) return SPK_ERR_INVALID;
+  *count = n->S;
+  return SPK_OK;
 }
 
 int spk_net_destroy(spk_net* n) {
@@ -924,6 +1327,14 @@ int spk_net_read_weights(spk_net* n, float* w, int64_t count) {
     return SPK_ERR_INVALID;
   }
   return guarded([&]() -> int {
+    if (n->generated) {
+      // creation order = entry order; the value each synapse delivers
+      SPK_CUDA(cudaStreamSynchronize(n->stream));
+      std::vector<uint2> e(n->S);
+      if (n->S) SPK_CUDA(cudaMemcpy(e.data(), n->hd.entries, sizeof(uint2) * n->S, cudaMemcpyDeviceToHost));
+      for (int64_t s = 0; s < n->S; ++s) w[s] = u2f(e[s].y);
+      return SPK_OK;
+    }
     if (n->has_stdp) {
       SPK_CUDA(cudaStreamSynchronize(n->stream));
       std::vector<uint2> e(n->S);
@@ -938,6 +1349,10 @@ int spk_net_read_weights(spk_net* n, float* w, int64_t count) {
 
 int spk_net_write_weights(spk_net* n, const float* w, int64_t count) {
   if (!n || (!w && count) || count != n->S) return SPK_ERR_INVALID;
+  if (n->generated) {
+    set_error("weights of a generated network cannot be written");
+    return SPK_ERR_UNSUPPORTED;
+  }
   return guarded([&]() -> int {
     SPK_CUDA(cudaStreamSynchronize(n->stream));
     std::vector<uint2> e(n->S);

@@ -29,7 +29,8 @@ namespace spk {
 enum : uint32_t {
   DOMAIN_POISSON = 0x504f4953u,  // Poisson inter-spike intervals
   DOMAIN_VINIT = 0x56494e49u,    // initial membrane potentials
-  DOMAIN_BUILD = 0x42554c44u,    // device-side connectivity builder
+  DOMAIN_CONNECT = 0x434f4e4eu,  // generated networks: Bernoulli connection draws
+  DOMAIN_SYNAPSE = 0x53594e41u,  // generated networks: weight and delay draws
 };
 
 struct u32x4 {
@@ -81,6 +82,16 @@ SPK_HD uint32_t draw_u32(uint64_t seed, uint32_t neuron, uint32_t step, uint32_t
   c.z = 0u;
   c.w = domain;
   return philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32)).x;
+}
+
+// All four words of one Philox block keyed by seed with counter (a, b, 0, domain).
+SPK_HD u32x4 draw4(uint64_t seed, uint32_t a, uint32_t b, uint32_t domain) {
+  u32x4 c;
+  c.x = a;
+  c.y = b;
+  c.z = 0u;
+  c.w = domain;
+  return philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
 }
 
 SPK_HD float draw_uniform(uint64_t seed, uint32_t neuron, uint32_t step, uint32_t domain) {

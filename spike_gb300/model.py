@@ -130,6 +130,20 @@ class Net:
               "spk_net_create")
         return cls(h)
 
+    @classmethod
+    def generate(cls, gen: "GenNetwork | N.GenDesc", sched: N.Schedule | None = None) -> "Net":
+        """A network whose connectivity the GPU draws (spk_net_generate)."""
+        d = gen.desc if isinstance(gen, GenNetwork) else gen
+        h = C.c_void_p()
+        check(lib().spk_net_generate(C.byref(d), C.byref(sched) if sched else None, C.byref(h)),
+              "spk_net_generate")
+        return cls(h)
+
+    def synapse_count(self) -> int:
+        n = C.c_int64()
+        check(lib().spk_net_synapse_count(self.h, C.byref(n)), "spk_net_synapse_count")
+        return n.value
+
     def close(self):
         if self.h and self.owned:
             lib().spk_net_destroy(self.h)
@@ -225,6 +239,93 @@ class Net:
         s = C.c_void_p()
         check(lib().spk_net_stream(self.h, C.byref(s)), "spk_net_stream")
         return s.value or 0
+
+
+@dataclass
+class Projection:
+    """One spk_projection: Bernoulli(p) connectivity over a (pre, post)
+    rectangle, weights ~ U(lo, hi], integer delays ~ U{lo..hi} steps."""
+    pre_population: int
+    pre_start: int
+    pre_count: int
+    post_start: int
+    post_count: int
+    probability: float
+    weight: tuple = (1.0, 1.0)
+    scale: float = 1.0
+    delay: tuple = (1, 1)
+    label: int = 0
+    plastic: bool = False
+
+    def to_c(self) -> N.Projection:
+        return N.Projection(self.pre_population, self.pre_start, self.pre_count, self.post_start, self.post_count,
+                            self.probability, self.weight[0], self.weight[1], self.scale, int(self.delay[0]),
+                            int(self.delay[1]), self.label, 1 if self.plastic else 0)
+
+
+class GenNetwork:
+    """Descriptor of a network whose connectivity is drawn on the GPU
+    (spk_net_generate).  ``groups`` are dicts with count, tau_m, R, v0,
+    vreset, theta and optionally v_init_lo / v_init_hi."""
+
+    def __init__(self, *, groups, projections, kind=N.SPK_SYN_VOLTAGE, dt=0.0001, refractory=0.002, i_bg=0.0,
+                 rates=None, n_inputs=0, label_tau=None, label_vhat=None, n_labels=1, stdp=None, seed=1,
+                 connectivity_seed=1, spike_capacity=0, record_inputs=False):
+        self.keep = []
+        d = N.GenDesc()
+        d.abi_version = N.SPK_ABI_VERSION
+        d.dt = dt
+        d.synapse_kind = kind
+        gs = (N.NeuronGroup * len(groups))()
+        start = 0
+        for i, g in enumerate(groups):
+            gs[i].start = start
+            gs[i].count = g["count"]
+            gs[i].tau_m = g.get("tau_m", 0.02)
+            gs[i].R = g.get("R", 1.0e8)
+            gs[i].v0 = g.get("v0", 0.0)
+            gs[i].vreset = g.get("vreset", 0.0)
+            gs[i].theta = g.get("theta", 0.02)
+            gs[i].v_init_lo = g.get("v_init_lo", 0.0)
+            gs[i].v_init_hi = g.get("v_init_hi", 0.0)
+            start += g["count"]
+        self.keep.append(gs)
+        d.n_neurons = start
+        d.n_groups = len(groups)
+        d.groups = C.cast(gs, C.POINTER(N.NeuronGroup))
+        d.refractory_period = refractory
+        d.background_current = i_bg
+        d.n_inputs = n_inputs
+        if n_inputs:
+            r = np.ascontiguousarray(rates, dtype=np.float32).reshape(-1)
+            self.keep.append(r)
+            d.n_stimuli = len(r) // n_inputs
+            d.input_rates = r.ctypes.data_as(C.POINTER(C.c_float))
+            d.stimulus = 0
+        d.n_labels = n_labels
+        tau = np.ascontiguousarray(label_tau if label_tau is not None else [0.005] * n_labels, np.float32)
+        vh = np.ascontiguousarray(label_vhat if label_vhat is not None else [0.0] * n_labels, np.float32)
+        self.keep += [tau, vh]
+        d.label_tau = tau.ctypes.data_as(C.POINTER(C.c_float))
+        d.label_vhat = vh.ctypes.data_as(C.POINTER(C.c_float))
+        ps = (N.Projection * max(len(projections), 1))()
+        for i, pr in enumerate(projections):
+            ps[i] = pr.to_c()
+        self.keep.append(ps)
+        self.projections = list(projections)
+        d.n_projections = len(projections)
+        d.projections = C.cast(ps, C.POINTER(N.Projection))
+        if stdp is not None:
+            d.has_stdp = 1
+            d.stdp = stdp.to_c()
+        d.seed = seed
+        d.connectivity_seed = connectivity_seed
+        d.spike_capacity = spike_capacity
+        d.record_inputs = 1 if record_inputs else 0
+        self.desc = d
+
+    def expected_synapses(self) -> float:
+        return sum(p.pre_count * p.post_count * p.probability for p in self.projections)
 
 
 class Batch:

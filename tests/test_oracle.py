@@ -173,3 +173,44 @@ def test_weight_dependent_stdp_single_pair():
         # numpy's exp and the C library's expf may differ in the last place
         assert o.weights()[0] == pytest.approx(float(w), rel=1e-6)
     assert n_pairs >= 8
+
+
+def test_generator_restatement_order_draws_and_statistics():
+    """The oracle's restatement of the device generator: creation order is
+    ascending (presynaptic key, post); each pair connects exactly when its
+    Philox uniform is <= p; counts, delays and weights follow the projection."""
+    from oracle.binding import generate_synapses
+    from spike_gb300 import GenNetwork, Projection
+    n_in, n = 200, 500
+    projs = [Projection(N.SPK_POP_INPUTS, 0, n_in, 0, n, 0.1, weight=(0.0, 1.0), scale=2e-3, delay=(1, 4)),
+             Projection(N.SPK_POP_NEURONS, 0, 400, 400, 100, 0.05, weight=(0.5, 1.0), scale=1e-3, delay=(2, 9)),
+             Projection(N.SPK_POP_NEURONS, 0, 400, 0, 400, 0.2, weight=(0.5, 1.0), scale=1e-3, delay=(1, 9)),
+             Projection(N.SPK_POP_NEURONS, 400, 100, 0, n, 0.3, weight=(-1.0, -0.5), scale=1e-3, delay=(1, 1))]
+    gen = GenNetwork(groups=[dict(count=400), dict(count=100)], projections=projs, n_inputs=n_in,
+                     rates=np.full(n_in, 10.0, np.float32), connectivity_seed=0x1234567890)
+    a = generate_synapses(gen.desc)
+    b = generate_synapses(gen.desc)
+    for k in a:
+        np.testing.assert_array_equal(a[k], b[k])
+    pre, post = a["pre"].astype(np.int64), a["post"].astype(np.int64)
+    key = np.where(pre < 0, n_in - 1 - (-pre - 1), n_in + pre)
+    order = key * n + post
+    assert (np.diff(order) > 0).all()
+    mu = gen.expected_synapses()
+    assert abs(len(pre) - mu) < 6 * np.sqrt(mu)
+    seed = 0x1234567890
+    for s in range(0, len(pre), max(1, len(pre) // 50)):
+        code = (0x80000000 | (-pre[s] - 1)) if pre[s] < 0 else pre[s]
+        w = philox4x32_10([post[s] >> 2, code, 0, 0x434f4e4e], [seed & 0xffffffff, seed >> 32])
+        u = F(((w[post[s] & 3] >> 8) + 1) * 2.0 ** -24)
+        proj = projs[0] if pre[s] < 0 else projs[3] if pre[s] >= 400 else projs[1] if post[s] >= 400 else projs[2]
+        assert u <= F(proj.probability)
+        assert proj.delay[0] <= a["delay"][s] <= proj.delay[1]
+        assert proj.weight[0] <= a["weight"][s] <= proj.weight[1]
+    # a pair is in the list exactly when its draw succeeds
+    in_list = set(zip(pre[pre >= 400].tolist(), post[pre >= 400].tolist()))
+    for p in range(400, 410):
+        for q in range(0, 40):
+            w = philox4x32_10([q >> 2, p, 0, 0x434f4e4e], [seed & 0xffffffff, seed >> 32])
+            u = F(((w[q & 3] >> 8) + 1) * 2.0 ** -24)
+            assert (u <= F(0.3)) == ((p, q) in in_list)
