@@ -283,6 +283,15 @@ int spk_batch_synchronize(spk_batch* batch);
 int spk_batch_launch_count(const spk_batch* batch, int64_t* launches);
 int spk_batch_stream(const spk_batch* batch, void** stream);
 int spk_batch_destroy(spk_batch* batch);
+/* Measured schedule search for a batch of generated networks (batching has
+ * no counterpart in the reference).  Tries a fixed set of policies (warps per
+ * CTA, largest tile), builds and packs the networks under each, times
+ * trial_steps steps of the batch and writes the fastest policy's schedule of
+ * every network to schedules[n_nets] (and its trial time to best_ms, which
+ * may be NULL).  Results never depend on the schedule.  Destroy a batch before
+ * the networks it holds. */
+int spk_batch_autotune(const spk_gen_desc* descs, int32_t n_nets, int32_t trial_steps,
+                       spk_schedule* schedules, float* best_ms);
 
 /* ---- allocation-free stepping --------------------------------------------
  * This entry point has no counterpart in the reference.  It is for callers
@@ -303,10 +312,12 @@ int spk_batch_destroy(spk_batch* batch);
  *  - rowptr[n_keys*T + 1]: start of each (key, tile) sub-row, exclusive prefix;
  *  - entries[S] (pairs of uint32): sub-rows in (key, tile) order, synapses of
  *    one sub-row in creation order; x = post%tile_posts | delay<<16 |
- *    label<<24 | class<<28, y = float bits of weight*scale (class 0) or of
- *    the weight (plastic class c >= 1, scale = plastic_scales[c-1]);
- *  - csc_ptr[N+1], csc[2*P]: plastic afferents of each post as (entry index,
- *    key), needed only with plasticity;
+ *    label<<24 | class<<28, y = float bits of weight*scale (class 0) or, for
+ *    a plastic synapse (class c >= 1, scale = plastic_scales[c-1]), the index
+ *    of its afferent record in csc;
+ *  - csc_ptr[N+1], csc[2*P]: the plastic afferent records of each post in
+ *    creation order, as (presynaptic key, float bits of the weight), needed
+ *    only with plasticity;
  *  - state: V, last_spike [N]; syn_trace [N*L] (conductance/current);
  *    ring [T][max_delay+3][tile_posts*L]; input_next [Nin]; rates [Nin];
  *    post_trace [N] and pre_trace [n_keys] with plasticity;
@@ -348,7 +359,7 @@ typedef struct spk_device_net {
   const int32_t* rowptr;
   uint32_t* entries;
   const int32_t* csc_ptr;
-  const uint32_t* csc;
+  uint32_t* csc;
   float* V;
   float* last_spike;
   float* syn_trace;

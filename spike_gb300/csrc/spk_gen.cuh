@@ -151,13 +151,15 @@ __global__ void gen_iota_kernel(uint32_t* v, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) v[i] = (uint32_t)i;
 }
 
-// csc[i] = (entry index, presynaptic key) of the i-th plastic synapse in
-// (post, entry index) order.
-__global__ void gen_csc_kernel(uint2* csc, const uint32_t* sorted_entry, const uint32_t* entry_key, long long P) {
+// The i-th plastic synapse in (post, entry index) order gets afferent record
+// csc[i] = (presynaptic key, weight); its entry then points at the record.
+__global__ void gen_csc_kernel(uint2* csc, uint2* entries, const uint32_t* sorted_entry, const uint32_t* entry_key,
+                               long long P) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < P; i += stride) {
     const uint32_t e = sorted_entry[i];
-    csc[i] = make_uint2(e, entry_key[e]);
+    csc[i] = make_uint2(entry_key[e], entries[e].y);
+    entries[e].y = (uint32_t)i;
   }
 }
 

@@ -20,7 +20,9 @@ constexpr int STAGE_ENTRIES = 256; // synapse entries staged per warp per round
 constexpr int APPLY_TAGS = 256;    // cell-hash slots of the ordered apply
 
 // Packed synapse entry: x = post_local[0:16) | delay[16:24) | label[24:28) |
-// class[28:32), y = float bits of the value (w*scale for class 0, w otherwise).
+// class[28:32), y = float bits of w*scale for class 0; for a plastic class
+// (>= 1) y is the index of the synapse's afferent record in the CSC, which
+// holds its weight (post-major, so a spiking post's afferents are contiguous).
 SPK_HD uint32_t pack_entry(uint32_t post_local, uint32_t delay, uint32_t label, uint32_t cls) {
   return post_local | (delay << 16) | (label << 24) | (cls << 28);
 }
@@ -62,7 +64,7 @@ struct NetDev {
   const int* rowptr;   // [n_keys * n_tiles + 1]
   uint2* entries;      // [S]
   const int* csc_ptr;  // [N + 1] plastic afferents of each post
-  const uint2* csc;    // (entry index, pre key)
+  uint2* csc;          // (pre key, float bits of the weight), post-major
   // home copies of the state held in shared memory during a launch
   float* V;
   float* last;
@@ -100,13 +102,14 @@ struct CtaMap {
 
 // Per-warp shared-memory words for a schedule (4-byte words).
 struct WarpLayout {
-  int stage, sidx, kst, koff, kfl, kpre, tag, rowb, rowe, ring, V, last, gtr, post_tr, pre_tr, spkw, inw, inwp, in_next,
+  int stage, stw, sidx, kst, koff, kfl, kpre, tag, rowb, rowe, ring, V, last, gtr, post_tr, pre_tr, spkw, inw, inwp, in_next,
       in_rate, in_pre, total;
 };
 SPK_HD WarpLayout warp_layout(int B, int TS, int L, int ITS, int kind, int has_stdp) {
   WarpLayout w;
   int o = 0;
   w.stage = o; o += 2 * STAGE_ENTRIES;  // uint2 entries (8-byte aligned: o even)
+  w.stw = o; o += has_stdp ? STAGE_ENTRIES : 0;  // weights of staged plastic entries
   w.sidx = o; o += STAGE_ENTRIES / 2;   // uint16 sub-row index per staged entry
   w.kst = o; o += STAGE_KEYS;           // sub-row start (entry index)
   w.koff = o; o += STAGE_KEYS + 4;      // exclusive prefix of sub-row lengths

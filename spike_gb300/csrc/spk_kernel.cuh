@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(512, 1)
   extern __shared__ __align__(16) uint32_t sm[];
   __shared__ float s_decay[MAX_LABELS + 1], s_vhat[MAX_LABELS + 1], s_scale[MAX_CLASSES];
   __shared__ int s_round[4];  // keys in the round, last round, poll ok
+  __shared__ int s_nsp;       // spiking posts listed for the CTA's afferent pass
   const CtaMap cm = map[blockIdx.x];
   const NetDev& d = nets[cm.net];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -153,6 +154,7 @@ __global__ void __launch_bounds__(512, 1)
   const WarpLayout wl = warp_layout(B, TS, L, ITS, kind, d.has_stdp);
   uint32_t* wreg = sm + SHARED_WORDS + w * wl.total;
   uint2* stage = (uint2*)(wreg + wl.stage);
+  float* stage_w = (float*)(wreg + wl.stw);
   unsigned short* sidx = (unsigned short*)(wreg + wl.sidx);
   int* kst = (int*)(wreg + wl.kst);
   int* koff = (int*)(wreg + wl.koff);
@@ -390,6 +392,7 @@ __global__ void __launch_bounds__(512, 1)
       }
     }
     __syncthreads();  // every warp's words are in shared memory, its traces written
+    if (threadIdx.x == 0) s_nsp = 0;  // read by every thread in the previous step's afferent pass
     // The CTA's ballot words in key order: inputs of warps 0..W-1, then neurons
     // of warps 0..W-1 (x-th word: bits a = spikes, p = pre events, first key).
     const int nw_in = W * (ITS >> 5), nw_all = W * ((ITS >> 5) + (TS >> 5));
@@ -544,6 +547,19 @@ __global__ void __launch_bounds__(512, 1)
             }
             cp_async_wait_all();
             __syncwarp();
+            if (d.has_stdp) {
+              // weights of the window's plastic entries, from their CSC records
+              bool any = false;
+              for (int f = lane; f < nf; f += 32) {
+                const uint2 en = stage[f];
+                if ((en.x >> 28) != 0u) {
+                  cp_async4(stage_w + f, &d.csc[en.y].y);
+                  any = true;
+                }
+              }
+              if (__any_sync(FULL, any)) cp_async_wait_all();
+              __syncwarp();
+            }
             for (int c0 = 0; c0 < nf; c0 += 32) {
               const int f = c0 + lane;
               bool add = false;
@@ -559,18 +575,18 @@ __global__ void __launch_bounds__(512, 1)
                 const int dl = (int)((en.x >> 16) & 0xffu);
                 const int lb = (int)((en.x >> 24) & 0xfu);
                 const int c = (int)(en.x >> 28);
-                float v = __uint_as_float(en.y);
                 if (c != 0) {
+                  float v = stage_w[f];
                   if (stdp_run) {
                     const bool post_ev = ((spkw_s[q >> 5] >> (q & 31)) & 1u) != 0;
                     if (P || post_ev) {
                       v = stdp_update(d, v, P, post_ev, post_s[q], kpre[j]);
-                      d.entries[kst[j] + (f0 + f - koff[j])].y = __float_as_uint(v);
+                      d.csc[en.y].y = __float_as_uint(v);
                     }
                   }
                   contrib = v * s_scale[c];
                 } else {
-                  contrib = v;
+                  contrib = __uint_as_float(en.y);
                 }
                 if (A) {
                   add = true;
@@ -782,28 +798,82 @@ __global__ void __launch_bounds__(512, 1)
     }
     if (!ok_run) break;
 
-    // ---- phase B: plastic afferents of the tile's spiking posts ---------------
+    // ---- phase B: plastic afferents of the CTA's spiking posts -----------------
+    // Every afferent of a spiking post whose presynaptic key had no event this
+    // step gets its LTP update here (those with an event were updated in the
+    // pre pass).  Each weight is touched at most once, so the order is free and
+    // the work is spread over all warps of the CTA: after a CTA barrier (every
+    // warp has applied its rounds) the warps list their spiking posts in
+    // shared memory, and the posts' afferents are cut into chunks of 32 * AFF
+    // that the warps take in turn.  Posts beyond the list's capacity are done
+    // by their own warp.
     if (stdp_run) {
+      constexpr int AFF = 4;
+      constexpr int SP_CAP = LIST_CAP / 2;
+      // AFF afferents per lane: their CSC records (pre key, weight; contiguous
+      // per post), then all of their bitmap words and pre traces are loaded
+      // together (lanes past the end read afferent a, always valid, and skip).
+      auto afferents = [&](const float post_tr, const int a, const int a1) {
+        uint2 cc[AFF];
+#pragma unroll
+        for (int u = 0; u < AFF; ++u) {
+          const int ai = a + u * 32 + lane;
+          cc[u] = d.csc[ai < a1 ? ai : a];
+        }
+        uint32_t vm[AFF];
+        float prt[AFF];
+#pragma unroll
+        for (int u = 0; u < AFF; ++u) {
+          const int pk = (int)cc[u].x;
+          vm[u] = __ldcg(bitsA + (pk >> 5)) | __ldcg(bitsP + (pk >> 5));
+          prt[u] = __ldcg(pub + pk);
+        }
+#pragma unroll
+        for (int u = 0; u < AFF; ++u) {
+          const int ai = a + u * 32 + lane;
+          const int pk = (int)cc[u].x;
+          if (ai >= a1 || ((vm[u] >> (pk & 31)) & 1u)) continue;  // pre event: done in the pre pass
+          const float nw = stdp_update(d, __uint_as_float(cc[u].y), false, true, post_tr, prt[u]);
+          d.csc[ai].y = __float_as_uint(nw);
+        }
+      };
+      __syncthreads();
       for (int wi = 0; wi < TS / 32; ++wi) {
-        uint32_t word = spkw_s[wi];
-        while (word) {
-          const int b = __ffs(word) - 1;
-          word &= word - 1;
-          const int ql = wi * 32 + b;
-          const int q = p0 + ql;
-          const int a0 = __ldg(d.csc_ptr + q), a1 = __ldg(d.csc_ptr + q + 1);
-          for (int a = a0 + lane; a < a1; a += 32) {
-            const uint2 cc = __ldg(d.csc + a);
-            const int pk = (int)cc.y;
-            const uint32_t va = __ldcg(bitsA + (pk >> 5));
-            const uint32_t vp = __ldcg(bitsP + (pk >> 5));
-            if (((va | vp) >> (pk & 31)) & 1u) continue;  // handled in the pre pass
-            const float old = __uint_as_float(d.entries[cc.x].y);
-            const float prt = __ldcg(pub + pk);
-            const float nw = stdp_update(d, old, false, true, post_s[ql], prt);
-            d.entries[cc.x].y = __float_as_uint(nw);
+        const uint32_t word = spkw_s[wi];
+        if (!word) continue;
+        const int c = __popc(word);
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&s_nsp, c);
+        base = __shfl_sync(FULL, base, 0);
+        const int mine = base + __popc(word & lanemask_lt());
+        if (((word >> lane) & 1u) && mine < SP_CAP) {
+          const int ql = wi * 32 + lane;
+          list[mine] = (uint32_t)(p0 + ql);
+          list[SP_CAP + mine] = __float_as_uint(post_s[ql]);
+        }
+        if (base + c > SP_CAP) {
+          // overflow posts: this warp updates them itself
+          uint32_t over = __ballot_sync(FULL, ((word >> lane) & 1u) && mine >= SP_CAP);
+          while (over) {
+            const int bb = __ffs(over) - 1;
+            over &= over - 1;
+            const int ql = wi * 32 + bb;
+            const int q = p0 + ql;
+            const int a0 = __ldg(d.csc_ptr + q), a1 = __ldg(d.csc_ptr + q + 1);
+            for (int a = a0; a < a1; a += 32 * AFF) afferents(post_s[ql], a, a1);
           }
         }
+      }
+      __syncthreads();
+      const int nsp = min(s_nsp, SP_CAP);
+      int item0 = 0;
+      for (int j = 0; j < nsp; ++j) {
+        const int q = (int)list[j];
+        const float post_tr = __uint_as_float(list[SP_CAP + j]);
+        const int a0 = __ldg(d.csc_ptr + q), a1 = __ldg(d.csc_ptr + q + 1);
+        const int nchunk = (a1 - a0 + 32 * AFF - 1) / (32 * AFF);
+        for (int c = ((w - item0) % W + W) % W; c < nchunk; c += W) afferents(post_tr, a0 + c * 32 * AFF, a1);
+        item0 += nchunk;
       }
     }
     ++steps_done;

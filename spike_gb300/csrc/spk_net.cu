@@ -175,6 +175,7 @@ struct spk_net {
   std::vector<float> weights;      // creation order (host mirror)
   std::vector<float> scales;       // creation order
   std::vector<int32_t> entry_of;   // creation index -> entry index
+  std::vector<int32_t> csc_of;     // creation index -> afferent record (plastic synapses)
   std::vector<uint8_t> cls_of;     // creation index -> scale class
   std::vector<float> scale_tab;
   Plan plan{};
@@ -193,17 +194,24 @@ struct spk_net {
   float current_time = 0.0f;
   int pending_status = SPK_OK;
   bool generated = false;  // connectivity drawn on the device (no host synapse arrays)
+  int64_t n_csc = 0;       // plastic afferent records
 };
 
 struct spk_batch {
+  struct Wave {
+    int first;  // first CTA-map entry of the wave
+    int ctas;   // CTAs of the wave (all co-resident)
+    int smem;   // dynamic shared memory of the wave's launch
+    bool cooperative;
+  };
   std::vector<spk_net*> nets;
   NetDev* dd = nullptr;
   CtaMap* dmap = nullptr;
   int* abort_dev = nullptr;
-  std::vector<std::pair<int, int>> waves;  // CTA ranges per launch
-  int W = 0, smem = 0, K = 0, total_ctas = 0;
-  bool cooperative = false;
+  std::vector<Wave> waves;
+  int W = 0, K = 0, total_ctas = 0;
   cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;  // recorded after each run; the networks' streams wait on it
   int64_t launches = 0;
 };
 
@@ -428,6 +436,7 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   const int N = n->N, Nin = n->Nin, L = n->L, B = n->B;
   const int stdp = n->has_stdp ? 1 : 0;
   const int64_t S = n->S;
+  n->n_csc = n_csc;
   const int n_tiles = plan.n_tiles, TS = plan.TS, KL = plan.KL, n_keys = plan.n_keys;
   const size_t n_cells = (size_t)n_keys * n_tiles;
   const int n_words = plan.n_words;
@@ -556,7 +565,7 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   h.rowptr = (const int*)p_rowptr;
   h.entries = (uint2*)p_entries;
   h.csc_ptr = (const int*)p_cscptr;
-  h.csc = (const uint2*)p_csc;
+  h.csc = (uint2*)p_csc;
   h.V = (float*)p_V;
   h.last = (float*)p_last;
   h.gtr = (float*)p_gtr;
@@ -740,6 +749,25 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
     rowptr[c + 1]++;
   }
   for (size_t c = 0; c < n_cells; ++c) rowptr[c + 1] += rowptr[c];
+  // ---- plastic afferent records per post: (pre key, weight), creation order --
+  std::vector<int32_t> csc_ptr;
+  std::vector<uint2> csc;
+  n->csc_of.assign(stdp ? S : 0, -1);
+  if (stdp) {
+    csc_ptr.assign((size_t)N + 1, 0);
+    for (int64_t s = 0; s < S; ++s)
+      if (n->cls_of[s]) csc_ptr[d->post[s] + 1]++;
+    for (int q = 0; q < N; ++q) csc_ptr[q + 1] += csc_ptr[q];
+    csc.resize(csc_ptr[N]);
+    std::vector<int32_t> fill(csc_ptr.begin(), csc_ptr.end() - 1);
+    for (int64_t s = 0; s < S; ++s)
+      if (n->cls_of[s]) {
+        const int32_t pos = fill[d->post[s]]++;
+        csc[pos] = make_uint2((uint32_t)key_of(d->pre[s]), f2u(d->weight[s]));
+        n->csc_of[s] = pos;
+      }
+  }
+  // ---- entries: static synapses carry w*scale, plastic ones their record ----
   std::vector<uint2> entries(S);
   n->entry_of.resize(S);
   {
@@ -749,25 +777,12 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
       const size_t c = (size_t)key_of(d->pre[s]) * n_tiles + q / TS;
       const int32_t pos = fill[c]++;
       const int cl = n->cls_of[s];
-      const float v = cl ? d->weight[s] : d->weight[s] * d->scale[s];
+      const uint32_t y = cl ? (uint32_t)n->csc_of[s] : f2u(d->weight[s] * d->scale[s]);
       entries[pos] = make_uint2(pack_entry((uint32_t)(q % TS), (uint32_t)d->delay[s],
                                            (uint32_t)(d->label ? d->label[s] : 0), (uint32_t)cl),
-                                f2u(v));
+                                y);
       n->entry_of[s] = pos;
     }
-  }
-  // ---- plastic afferents per post (for the post-spike pass) -------------------
-  std::vector<int32_t> csc_ptr;
-  std::vector<uint2> csc;
-  if (stdp) {
-    csc_ptr.assign((size_t)N + 1, 0);
-    for (int64_t s = 0; s < S; ++s)
-      if (n->cls_of[s]) csc_ptr[d->post[s] + 1]++;
-    for (int q = 0; q < N; ++q) csc_ptr[q + 1] += csc_ptr[q];
-    csc.resize(csc_ptr[N]);
-    std::vector<int32_t> fill(csc_ptr.begin(), csc_ptr.end() - 1);
-    for (int64_t s = 0; s < S; ++s)
-      if (n->cls_of[s]) csc[fill[d->post[s]]++] = make_uint2((uint32_t)n->entry_of[s], (uint32_t)key_of(d->pre[s]));
   }
   rc = setup_device(n, m, (int64_t)csc.size(), rowptr.data(), entries.data(), stdp ? csc_ptr.data() : nullptr,
                     csc.data());
@@ -1073,7 +1088,8 @@ static int generate_impl(const spk_gen_desc* d, const spk_schedule* sched, spk_n
       set_error("plastic afferent sort failed: %s", cudaGetErrorString(cudaGetLastError()));
       return fail(SPK_ERR_CUDA);
     }
-    gen_csc_kernel<<<grid, 256, 0, st>>>((uint2*)n->hd.csc, vals.Current(), ekey.as<uint32_t>(), (long long)P);
+    gen_csc_kernel<<<grid, 256, 0, st>>>(n->hd.csc, n->hd.entries, vals.Current(), ekey.as<uint32_t>(),
+                                         (long long)P);
     if (cudaGetLastError() != cudaSuccess) return fail(SPK_ERR_CUDA);
     if (cudaStreamSynchronize(st) != cudaSuccess) {
       set_error("network generation failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -1327,21 +1343,23 @@ int spk_net_read_weights(spk_net* n, float* w, int64_t count) {
     return SPK_ERR_INVALID;
   }
   return guarded([&]() -> int {
+    std::vector<uint2> csc;
+    if (n->has_stdp) {
+      SPK_CUDA(cudaStreamSynchronize(n->stream));
+      csc.resize(n->n_csc);
+      if (n->n_csc) SPK_CUDA(cudaMemcpy(csc.data(), n->hd.csc, sizeof(uint2) * n->n_csc, cudaMemcpyDeviceToHost));
+    }
     if (n->generated) {
       // creation order = entry order; the value each synapse delivers
       SPK_CUDA(cudaStreamSynchronize(n->stream));
       std::vector<uint2> e(n->S);
       if (n->S) SPK_CUDA(cudaMemcpy(e.data(), n->hd.entries, sizeof(uint2) * n->S, cudaMemcpyDeviceToHost));
-      for (int64_t s = 0; s < n->S; ++s) w[s] = u2f(e[s].y);
+      for (int64_t s = 0; s < n->S; ++s) w[s] = (e[s].x >> 28) ? u2f(csc[e[s].y].y) : u2f(e[s].y);
       return SPK_OK;
     }
-    if (n->has_stdp) {
-      SPK_CUDA(cudaStreamSynchronize(n->stream));
-      std::vector<uint2> e(n->S);
-      SPK_CUDA(cudaMemcpy(e.data(), n->hd.entries, sizeof(uint2) * n->S, cudaMemcpyDeviceToHost));
+    if (n->has_stdp)
       for (int64_t s = 0; s < n->S; ++s)
-        if (n->cls_of[s]) n->weights[s] = u2f(e[n->entry_of[s]].y);
-    }
+        if (n->cls_of[s]) n->weights[s] = u2f(csc[n->csc_of[s]].y);
     std::memcpy(w, n->weights.data(), sizeof(float) * n->S);
     return SPK_OK;
   });
@@ -1355,14 +1373,18 @@ int spk_net_write_weights(spk_net* n, const float* w, int64_t count) {
   }
   return guarded([&]() -> int {
     SPK_CUDA(cudaStreamSynchronize(n->stream));
-    std::vector<uint2> e(n->S);
+    std::vector<uint2> e(n->S), csc(n->n_csc);
     SPK_CUDA(cudaMemcpy(e.data(), n->hd.entries, sizeof(uint2) * n->S, cudaMemcpyDeviceToHost));
+    if (n->n_csc) SPK_CUDA(cudaMemcpy(csc.data(), n->hd.csc, sizeof(uint2) * n->n_csc, cudaMemcpyDeviceToHost));
     for (int64_t s = 0; s < n->S; ++s) {
       n->weights[s] = w[s];
-      const float v = n->cls_of[s] ? w[s] : w[s] * n->scales[s];
-      e[n->entry_of[s]].y = f2u(v);
+      if (n->cls_of[s])
+        csc[n->csc_of[s]].y = f2u(w[s]);
+      else
+        e[n->entry_of[s]].y = f2u(w[s] * n->scales[s]);
     }
     SPK_CUDA(cudaMemcpy(n->hd.entries, e.data(), sizeof(uint2) * n->S, cudaMemcpyHostToDevice));
+    if (n->n_csc) SPK_CUDA(cudaMemcpy(n->hd.csc, csc.data(), sizeof(uint2) * n->n_csc, cudaMemcpyHostToDevice));
     return SPK_OK;
   });
 }
@@ -1419,8 +1441,9 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
     int rc = device_info(&di);
     if (rc) return rc;
     auto* b = new spk_batch();
-    b->W = nets[0]->plan.W;
-    b->K = (schedule && schedule->steps_per_launch > 0) ? schedule->steps_per_launch : nets[0]->plan.K;
+    b->W = nets[0] ? nets[0]->plan.W : 0;
+    b->K = (schedule && schedule->steps_per_launch > 0) ? schedule->steps_per_launch
+                                                        : (nets[0] ? nets[0]->plan.K : DEFAULT_STEPS_PER_LAUNCH);
     for (int i = 0; i < n_nets; ++i) {
       spk_net* n = nets[i];
       if (!n || n->plan.W != b->W) {
@@ -1428,44 +1451,70 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
         delete b;
         return SPK_ERR_INVALID;
       }
+      for (int j = 0; j < i; ++j)
+        if (nets[j] == n) {
+          set_error("network %d appears twice in the batch", i);
+          delete b;
+          return SPK_ERR_INVALID;
+        }
       b->nets.push_back(n);
-      b->smem = std::max(b->smem, n->plan.smem);
       b->total_ctas += n->plan.nctas;
     }
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_kernel, b->W * 32, b->smem) !=
-            cudaSuccess ||
-        per_sm < 1) {
-      set_error("batch: no CTA of %d threads with %d B shared memory fits", b->W * 32, b->smem);
-      delete b;
-      return SPK_ERR_UNSUPPORTED;
-    }
-    const int capacity = per_sm * di.sms;
-    // waves: consecutive networks whose CTAs fit co-resident
+    // Waves: co-resident sets of CTAs, one cooperative launch each.  Networks
+    // are taken in decreasing shared-memory order so that each wave's launch
+    // (which gives every CTA the wave's largest footprint) wastes little.
+    std::vector<int> order(n_nets);
+    for (int i = 0; i < n_nets; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+      if (nets[a]->plan.smem != nets[c]->plan.smem) return nets[a]->plan.smem > nets[c]->plan.smem;
+      return nets[a]->plan.nctas > nets[c]->plan.nctas;
+    });
+    std::map<int, int> per_sm_of;
+    auto capacity_at = [&](int smem, int* cap) -> int {
+      auto it = per_sm_of.find(smem);
+      int per_sm = 0;
+      if (it == per_sm_of.end()) {
+        SPK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_kernel, b->W * 32, smem));
+        per_sm_of[smem] = per_sm;
+      } else {
+        per_sm = it->second;
+      }
+      *cap = per_sm * di.sms;
+      return SPK_OK;
+    };
     std::vector<CtaMap> map;
-    std::vector<NetDev> hds;
-    int wave_start = 0, wave_ctas = 0;
-    bool any_multi = false;
-    for (int i = 0; i < n_nets; ++i) {
+    map.reserve(b->total_ctas);
+    spk_batch::Wave cur{0, 0, 0, false};
+    for (int i : order) {
       spk_net* n = nets[i];
-      if (n->plan.nctas > capacity) {
-        set_error("network %d needs %d co-resident CTAs, device holds %d", i, n->plan.nctas, capacity);
+      int cap = 0;
+      rc = capacity_at(std::max(cur.smem, n->plan.smem), &cap);
+      if (rc) {
+        delete b;
+        return rc;
+      }
+      if (cur.ctas > 0 && cur.ctas + n->plan.nctas > cap) {
+        b->waves.push_back(cur);
+        cur = spk_batch::Wave{(int)map.size(), 0, 0, false};
+        rc = capacity_at(n->plan.smem, &cap);
+        if (rc) {
+          delete b;
+          return rc;
+        }
+      }
+      if (n->plan.nctas > cap) {
+        set_error("network %d needs %d co-resident CTAs, device holds %d", i, n->plan.nctas, cap);
         delete b;
         return SPK_ERR_UNSUPPORTED;
       }
-      if (wave_ctas + n->plan.nctas > capacity) {
-        b->waves.push_back({wave_start, wave_ctas});
-        wave_start += wave_ctas;
-        wave_ctas = 0;
-      }
-      NetDev h = n->hd;
-      hds.push_back(h);
       for (int r = 0; r < n->plan.nctas; ++r) map.push_back(CtaMap{i, r});
-      wave_ctas += n->plan.nctas;
-      any_multi |= n->plan.nctas > 1;
+      cur.ctas += n->plan.nctas;
+      cur.smem = std::max(cur.smem, n->plan.smem);
+      cur.cooperative |= n->plan.nctas > 1;
     }
-    b->waves.push_back({wave_start, wave_ctas});
-    b->cooperative = any_multi;
+    b->waves.push_back(cur);
+    std::vector<NetDev> hds(n_nets);
+    for (int i = 0; i < n_nets; ++i) hds[i] = nets[i]->hd;
     const size_t bytes = align_up(sizeof(NetDev) * n_nets, 256) + align_up(sizeof(CtaMap) * map.size(), 256) + 256;
     void* mem = nullptr;
     if (cudaMalloc(&mem, bytes) != cudaSuccess) {
@@ -1479,11 +1528,13 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
     b->abort_dev = (int*)((char*)b->dmap + align_up(sizeof(CtaMap) * map.size(), 256));
     for (int i = 0; i < n_nets; ++i) hds[i].abort_flag = b->abort_dev;
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess ||
         cudaMemcpy(b->dd, hds.data(), sizeof(NetDev) * n_nets, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(b->dmap, map.data(), sizeof(CtaMap) * map.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(b->abort_dev, 0, sizeof(int)) != cudaSuccess) {
       set_error("batch: setup failed: %s", cudaGetErrorString(cudaGetLastError()));
       if (b->stream) cudaStreamDestroy(b->stream);
+      if (b->done) cudaEventDestroy(b->done);
       cudaFree(mem);
       delete b;
       return SPK_ERR_CUDA;
@@ -1507,13 +1558,13 @@ int spk_batch_run_steps(spk_batch* b, int64_t n_steps, int32_t plasticity_on) {
   for (int64_t blk = 0; blk < blocks; ++blk) {
     for (const auto& wv : b->waves) {
       cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(wv.second);
+      cfg.gridDim = dim3(wv.ctas);
       cfg.blockDim = dim3(b->W * 32);
-      cfg.dynamicSmemBytes = b->smem;
+      cfg.dynamicSmemBytes = wv.smem;
       cfg.stream = b->stream;
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeCooperative;
-      attr[0].val.cooperative = b->cooperative ? 1 : 0;
+      attr[0].val.cooperative = wv.cooperative ? 1 : 0;
       cfg.attrs = attr;
       cfg.numAttrs = 1;
       SPK_CUDA(cudaLaunchKernelEx(&cfg, step_kernel, (const NetDev*)b->dd,
@@ -1521,7 +1572,12 @@ int spk_batch_run_steps(spk_batch* b, int64_t n_steps, int32_t plasticity_on) {
       ++b->launches;
     }
   }
-  for (spk_net* n : b->nets) n->current_time = n->current_time + (float)n_steps * n->dt;
+  // each network's own stream (its readbacks and runs) waits for the batch
+  SPK_CUDA(cudaEventRecord(b->done, b->stream));
+  for (spk_net* n : b->nets) {
+    SPK_CUDA(cudaStreamWaitEvent(n->stream, b->done, 0));
+    n->current_time = n->current_time + (float)n_steps * n->dt;
+  }
   return SPK_OK;
 }
 
@@ -1556,6 +1612,7 @@ int spk_batch_destroy(spk_batch* b) {
     cudaStreamSynchronize(b->stream);
     cudaStreamDestroy(b->stream);
   }
+  if (b->done) cudaEventDestroy(b->done);
   cudaFree(b->dd);
   delete b;
   return SPK_OK;
@@ -1820,7 +1877,7 @@ static int step_noalloc_impl(const spk_device_net* a, int64_t n_steps, int plast
   h.rowptr = a->rowptr;
   h.entries = (uint2*)a->entries;
   h.csc_ptr = a->csc_ptr;
-  h.csc = (const uint2*)a->csc;
+  h.csc = (uint2*)a->csc;
   h.V = a->V;
   h.last = a->last_spike;
   h.gtr = a->syn_trace;
@@ -1868,4 +1925,111 @@ static int step_noalloc_impl(const spk_device_net* a, int64_t n_steps, int plast
 extern "C" int spk_step_noalloc(const spk_device_net* net, int64_t n_steps, int32_t plasticity_on,
                                 float start_time, void* stream) {
   return spk::step_noalloc_impl(net, n_steps, plasticity_on, start_time, (cudaStream_t)stream);
+}
+
+// =====================================================================================
+// Batch autotuner: a measured search over schedule policies for a set of
+// generated networks.  A policy fixes warps per CTA W and a largest tile TS*;
+// each network then gets the tile min(TS*, its neurons / W rounded up to 32)
+// and as many CTAs as cover it, so small networks run on one CTA and large
+// ones spread over CTAs of TS*-post tiles.  Every policy is built (the same
+// networks, drawn again under its tiles), packed into waves and timed over a
+// trial run; the fastest policy's schedules are returned.  Results do not
+// depend on the schedule, only the time does.
+namespace spk {
+
+struct TunePolicy {
+  int W, TS;
+};
+
+static int policy_schedules(const spk_gen_desc* descs, int n, const TunePolicy& pol, const DeviceInfo& di,
+                            std::vector<spk_schedule>& out) {
+  out.assign(n, spk_schedule{});
+  for (int i = 0; i < n; ++i) {
+    const spk_gen_desc& d = descs[i];
+    int dmax = 1;
+    for (int j = 0; j < d.n_projections; ++j) dmax = std::max(dmax, d.projections[j].delay_hi);
+    const int B = dmax + 3;
+    const int want = std::max(32, ((d.n_neurons + pol.W - 1) / pol.W + 31) / 32 * 32);
+    bool ok = false;
+    for (int TS = std::min(pol.TS, want); TS >= 32 && !ok; TS -= 32) {
+      spk_schedule s{pol.W, TS, 0, 0};
+      Plan p;
+      if (make_plan(d.n_neurons, d.n_inputs, B, std::max(1, d.n_labels), d.synapse_kind, d.has_stdp ? 1 : 0, &s,
+                    di, &p) == SPK_OK &&
+          p.nctas <= di.sms) {
+        out[i] = spk_schedule{p.W, p.TS, p.nctas, 0};
+        ok = true;
+      }
+    }
+    if (!ok) {
+      set_error("autotune: no schedule with %d warps per CTA fits network %d", pol.W, i);
+      return SPK_ERR_UNSUPPORTED;
+    }
+  }
+  return SPK_OK;
+}
+
+static int trial_policy(const spk_gen_desc* descs, int n, const std::vector<spk_schedule>& sch, int steps,
+                        float* ms) {
+  std::vector<spk_net*> nets(n, nullptr);
+  spk_batch* b = nullptr;
+  auto cleanup = [&]() {
+    if (b) spk_batch_destroy(b);
+    for (spk_net* x : nets)
+      if (x) spk_net_destroy(x);
+  };
+  int rc = SPK_OK;
+  for (int i = 0; i < n && rc == SPK_OK; ++i) rc = generate_impl(&descs[i], &sch[i], &nets[i]);
+  if (rc == SPK_OK) rc = spk_batch_create(nets.data(), n, nullptr, &b);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (rc == SPK_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) rc = SPK_ERR_CUDA;
+  if (rc == SPK_OK) rc = spk_batch_run_steps(b, std::max(1, steps / 2), 1);
+  if (rc == SPK_OK && cudaStreamSynchronize(b->stream) != cudaSuccess) rc = SPK_ERR_CUDA;
+  if (rc == SPK_OK) {
+    cudaEventRecord(e0, b->stream);
+    rc = spk_batch_run_steps(b, steps, 1);
+    cudaEventRecord(e1, b->stream);
+    if (rc == SPK_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = SPK_ERR_CUDA;
+    if (rc == SPK_OK) {
+      cudaEventElapsedTime(ms, e0, e1);
+      rc = spk_batch_synchronize(b);
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cleanup();
+  return rc;
+}
+
+}  // namespace spk
+
+extern "C" int spk_batch_autotune(const spk_gen_desc* descs, int32_t n_nets, int32_t trial_steps,
+                                  spk_schedule* schedules, float* best_ms) {
+  using namespace spk;
+  if (!descs || n_nets < 1 || !schedules || trial_steps < 1) return SPK_ERR_INVALID;
+  return guarded([&]() -> int {
+    DeviceInfo di;
+    int rc = device_info(&di);
+    if (rc) return rc;
+    static const TunePolicy policies[] = {{8, 32}, {8, 64}, {8, 128}, {8, 256}, {4, 128}};
+    float best = -1.0f;
+    std::vector<spk_schedule> sch, best_sch;
+    int last_rc = SPK_ERR_UNSUPPORTED;
+    for (const TunePolicy& pol : policies) {
+      if (policy_schedules(descs, n_nets, pol, di, sch) != SPK_OK) continue;
+      float ms = 0.0f;
+      last_rc = trial_policy(descs, n_nets, sch, trial_steps, &ms);
+      if (last_rc == SPK_ERR_TIMEOUT || last_rc == SPK_ERR_CUDA) return last_rc;
+      if (last_rc != SPK_OK) continue;
+      if (best < 0.0f || ms < best) {
+        best = ms;
+        best_sch = sch;
+      }
+    }
+    if (best < 0.0f) return last_rc;
+    std::copy(best_sch.begin(), best_sch.end(), schedules);
+    if (best_ms) *best_ms = best;
+    return SPK_OK;
+  });
 }

@@ -338,6 +338,16 @@ class Batch:
         check(lib().spk_batch_create(arr, len(nets), C.byref(sched) if sched else None, C.byref(self.h)),
               "spk_batch_create")
 
+    @staticmethod
+    def autotune(gens: list, trial_steps: int = 200):
+        """Measured schedule search (spk_batch_autotune) for generated
+        networks: returns (schedules, trial milliseconds of the best policy)."""
+        descs = (N.GenDesc * len(gens))(*[g.desc for g in gens])
+        out = (N.Schedule * len(gens))()
+        ms = C.c_float()
+        check(lib().spk_batch_autotune(descs, len(gens), trial_steps, out, C.byref(ms)), "spk_batch_autotune")
+        return [N.Schedule(o.warps_per_cta, o.tile_posts, o.ctas, o.steps_per_launch) for o in out], ms.value
+
     def run_steps(self, steps: int, plasticity_on: bool = True):
         check(lib().spk_batch_run_steps(self.h, steps, 1 if plasticity_on else 0), "spk_batch_run_steps")
 

@@ -17,7 +17,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _native as N
-from .model import LIFParams, Model, STDPParams, SynapseParams
+from .model import GenNetwork, LIFParams, Model, Projection, STDPParams, SynapseParams
 
 DT = 0.0001
 
@@ -111,3 +111,66 @@ def plastic_ff(n_in: int = 50000, n_neurons: int = 200000, ff: int = 900, rec: i
     m.connect_with_sparsity(inp, pop, ff / n_in, ffp)
     m.connect_with_sparsity(pop, pop, rec / n_neurons, recp)
     return m
+
+
+BRUNEL_LIF = dict(tau_m=0.02, R=1.0e8, v0=0.0, vreset=0.0, theta=0.02)  # C_m 200 pF, g_0 10 nS
+
+
+def plastic_ff_generated(n_in: int = 50000, n_neurons: int = 200000, ff: int = 900, rec: int = 100,
+                         d_max: int = 10, w_scale: float = 2.0e-4, sigma: float = 1.0, plastic: bool = True,
+                         seed: int = 42) -> GenNetwork:
+    """The large plastic feed-forward + recurrent network drawn on the GPU:
+    each (input, neuron) pair connects with p = ff / n_in and each (neuron,
+    neuron) pair with p = rec / n_neurons (binomial in-degree, mean ff + rec),
+    weights U(0, 1] (inputs, plastic) and U(-1, 0] (recurrent) times w_scale
+    volts, delays U{1..d_max}, log-normal input rates."""
+    stdp = STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02, lambda_=1.0, alpha=1.0,
+                      w_max=1.0, clip_upper=True) if plastic else None
+    projs = [Projection(N.SPK_POP_INPUTS, 0, n_in, 0, n_neurons, ff / n_in, weight=(0.0, 1.0), scale=w_scale,
+                        delay=(1, d_max), plastic=plastic),
+             Projection(N.SPK_POP_NEURONS, 0, n_neurons, 0, n_neurons, rec / n_neurons, weight=(-1.0, 0.0),
+                        scale=w_scale, delay=(1, d_max))]
+    return GenNetwork(groups=[dict(count=n_neurons, **BRUNEL_LIF)], projections=projs, refractory=2.0e-3,
+                      n_inputs=n_in, rates=lognormal_rates(n_in, sigma=sigma, seed=seed), stdp=stdp, seed=seed,
+                      connectivity_seed=seed + 1)
+
+
+def sweep_instance(n: int, p: float, g: float, plastic: bool, seed: int, d_max: int = 10,
+                   rate: float = 20.0) -> GenNetwork:
+    """One instance of the batched sweep: a Brunel-style voltage-jump LIF
+    network of n neurons (80 % excitatory), Bernoulli(p) recurrent
+    connectivity, J = 0.1 V / C_E with C_E = 0.8 n p (J C_E as in
+    Examples/Brunel10K.cpp), inhibitory weight -g J, delays U{1..d_max}, and
+    an external drive of n / 5 Poisson inputs at `rate` Hz connected with
+    probability 4p (C_E inputs per neuron, nu_ext = 2 nu_thr).  With
+    plasticity the input synapses are plastic, weights U(0, 1] at scale 2J."""
+    n_e = int(round(0.8 * n))
+    n_i = n - n_e
+    n_in = max(1, n // 5)
+    c_e = max(1.0, 0.8 * n * p)
+    J = 0.1 / c_e
+    p_in = min(1.0, 4.0 * p)
+    stdp = STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02, lambda_=1.0, alpha=1.0,
+                      w_max=1.0, clip_upper=True) if plastic else None
+    projs = [Projection(N.SPK_POP_INPUTS, 0, n_in, 0, n, p_in,
+                        weight=(0.0, 1.0) if plastic else (1.0, 1.0), scale=2.0 * J if plastic else J,
+                        delay=(1, d_max), plastic=plastic),
+             Projection(N.SPK_POP_NEURONS, 0, n_e, 0, n, p, weight=(1.0, 1.0), scale=J, delay=(1, d_max)),
+             Projection(N.SPK_POP_NEURONS, n_e, n_i, 0, n, p, weight=(-g, -g), scale=J, delay=(1, d_max))]
+    return GenNetwork(groups=[dict(count=n_e, **BRUNEL_LIF), dict(count=n_i, **BRUNEL_LIF)], projections=projs,
+                      refractory=2.0e-3, n_inputs=n_in, rates=np.full(n_in, rate, np.float32), stdp=stdp,
+                      seed=seed, connectivity_seed=seed ^ 0x5eed)
+
+
+def batched_sweep(n_instances: int = 256, n_lo: int = 1000, n_hi: int = 50000, seed: int = 42,
+                  plastic_fraction: float = 0.5) -> list:
+    """The batched sweep: n_instances independent instances with N
+    log-uniform in [n_lo, n_hi], p ~ U[0.01, 0.05], g ~ U[3, 7], delays
+    U{1..10}, distinct seeds, the first plastic_fraction of them with STDP."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(n_lo), np.log(n_hi), n_instances)).astype(int)
+    ps = rng.uniform(0.01, 0.05, n_instances)
+    gs = rng.uniform(3.0, 7.0, n_instances)
+    n_plastic = int(round(plastic_fraction * n_instances))
+    return [sweep_instance(int(sizes[k]), float(ps[k]), float(gs[k]), k < n_plastic, seed=1000 + 7 * k)
+            for k in range(n_instances)]

@@ -1,0 +1,69 @@
+"""Batched stepping of uneven generated networks (GPU): the autotuned batch
+gives every instance exactly the result it has alone (bit for bit)."""
+import numpy as np
+import pytest
+
+from engine_checks import bits
+from spike_gb300 import Batch, Net
+from spike_gb300 import _native as N
+from spike_gb300.networks import sweep_instance
+
+pytestmark = pytest.mark.gpu
+
+
+def small_sweep(k=12, seed=3):
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(300), np.log(6000), k)).astype(int)
+    return [sweep_instance(int(sizes[i]), float(rng.uniform(0.02, 0.08)), float(rng.uniform(3, 7)), i % 2 == 0,
+                           seed=100 + i, d_max=8) for i in range(k)]
+
+
+def snapshot(net: Net, n: int, n_in: int, S: int):
+    ids, t = net.spikes()
+    ii, it = net.spikes(N.SPK_POP_INPUTS)
+    return dict(ids=ids, t=bits(t), iids=ii, it=bits(it), V=bits(net.state(N.SPK_FIELD_V, n)),
+                last=bits(net.state(N.SPK_FIELD_LAST_SPIKE, n)), w=bits(net.weights(S)), ev=net.events())
+
+
+def test_autotuned_batch_equals_each_instance_alone():
+    gens = small_sweep()
+    scheds, ms = Batch.autotune(gens, trial_steps=60)
+    assert ms > 0 and len(scheds) == len(gens)
+    batched = [Net.generate(g, s) for g, s in zip(gens, scheds)]
+    alone = [Net.generate(g, s) for g, s in zip(gens, scheds)]
+    b = Batch(batched)
+    for plastic, steps in ((True, 700), (False, 300)):
+        b.run_steps(steps, plastic)
+        for n in alone:
+            n.run_steps(steps, plastic)
+    assert b.synchronize() == 0
+    total = 0
+    for g, x, y in zip(gens, batched, alone):
+        assert y.synchronize() == 0
+        n, n_in, S = g.desc.n_neurons, g.desc.n_inputs, x.synapse_count()
+        sx, sy = snapshot(x, n, n_in, S), snapshot(y, n, n_in, S)
+        for k in sx:
+            np.testing.assert_array_equal(sx[k], sy[k], err_msg=f"instance n={n} field {k}")
+        total += len(sx["ids"])
+        assert abs(x.current_time() - y.current_time()) == 0
+    assert total > 1000
+    b.close()
+
+
+def test_batch_waves_cover_more_ctas_than_one_launch_holds():
+    """Enough multi-CTA instances that the batch needs several waves."""
+    gens = [sweep_instance(6000, 0.05, 5.0, False, seed=500 + i, d_max=6) for i in range(40)]
+    sched = N.Schedule(8, 32, 0, 0)  # 24 CTAs each: 960 CTAs, more than one wave
+    batched = [Net.generate(g, sched) for g in gens]
+    b = Batch(batched)
+    b.run_steps(200, False)
+    assert b.synchronize() == 0
+    assert b.launches() >= 2
+    ref = Net.generate(gens[-1], sched)
+    ref.run_steps(200, False)
+    assert ref.synchronize() == 0
+    i0, t0 = ref.spikes()
+    i1, t1 = batched[-1].spikes()
+    np.testing.assert_array_equal(i0, i1)
+    np.testing.assert_array_equal(bits(t0), bits(t1))
+    b.close()

@@ -74,17 +74,24 @@ class CallerNet:
         entry_of[order] = np.arange(S)
         rowptr = np.zeros(n_keys * n_tiles + 1, np.int32)
         rowptr[1:] = np.cumsum(np.bincount(cell, minlength=n_keys * n_tiles))
-        val = np.where(cls == 0, (a["weight"] * a["scale"]).astype(np.float32), a["weight"]).astype(np.float32)
-        x = (post % TS).astype(np.uint32) | (a["delay"].astype(np.uint32) << 16) | \
-            (a["label"].astype(np.uint32) << 24) | (cls << 28)
-        entries = np.stack([x, val.view(np.uint32)], axis=1)[order]
-        self.entry_of = entry_of
-
+        # plastic afferent records per post, creation order: (pre key, weight)
         pl = np.nonzero(cls)[0]
         csc_ptr = np.zeros(Nn + 1, np.int32)
         csc_ptr[1:] = np.cumsum(np.bincount(post[pl], minlength=Nn))
         by_post = pl[np.argsort(post[pl], kind="stable")]
-        csc = np.stack([entry_of[by_post].astype(np.uint32), key[by_post].astype(np.uint32)], axis=1)
+        csc_of = np.full(S, -1, np.int64)
+        csc_of[by_post] = np.arange(len(by_post))
+        csc = np.stack([key[by_post].astype(np.uint32), a["weight"][by_post].astype(np.float32).view(np.uint32)],
+                       axis=1)
+        self.csc_of = csc_of
+        # entries: w*scale for static synapses, the afferent record for plastic ones
+        y = np.where(cls == 0, (a["weight"] * a["scale"]).astype(np.float32).view(np.uint32),
+                     csc_of.astype(np.uint32)).astype(np.uint32)
+        x = (post % TS).astype(np.uint32) | (a["delay"].astype(np.uint32) << 16) | \
+            (a["label"].astype(np.uint32) << 24) | (cls << 28)
+        entries = np.stack([x, y], axis=1)[order]
+        self.entry_of = entry_of
+        self.plastic = cls != 0
 
         def dbuf(arr, dtype=None):
             t = torch.from_numpy(np.ascontiguousarray(arr if dtype is None else arr.astype(dtype)))
@@ -159,9 +166,10 @@ class CallerNet:
         ring = ring.reshape(B, self.n_tiles * TS, L)[:, :Nn].reshape(-1)
         assert_close(ring, ref.state(N.SPK_FIELD_RING, B * Nn * L), f"{tag} ring")
         if self.dn.has_stdp:
-            ent = self.t["entries"].cpu().numpy().reshape(-1, 2)
-            w = ent[self.entry_of, 1].copy().view(np.float32)
-            assert_close(w, ref.weights(n_synapses), f"{tag} weights")
+            csc = self.t["csc"].cpu().numpy().reshape(-1, 2)
+            w = ref.weights(n_synapses)
+            mine = csc[self.csc_of[self.plastic], 1].copy().view(np.float32)
+            assert_close(mine, w[self.plastic], f"{tag} plastic weights")
             assert_close(self.t["post_tr"].cpu().numpy(), ref.state(N.SPK_FIELD_POST_TRACE, Nn), f"{tag} post")
             pre = self.t["pre_tr"].cpu().numpy()
             pre_c = np.concatenate([pre[self.Nin - 1 - np.arange(self.Nin)], pre[self.KL:self.KL + Nn]])
