@@ -1,27 +1,37 @@
 """Benchmark of the clock-driven step: synaptic events/s on one GB300.
 
-Workload (default): the Brunel network of Examples/Brunel10K.cpp at the sizes
-of the benchmark's second configuration - 10,000 excitatory + 2,500
-inhibitory voltage-synapse LIF neurons, 10,000 Poisson inputs at 20 Hz, fixed
-in-degree 0.1 (1,000 E + 250 I + 1,000 input afferents per neuron), J = 0.1 mV,
-g = 5, delays U{1..20} steps, dt = 0.1 ms; 28.1 M synapses (225 MB of synapse
-entries, larger than the 129 MB L2).  Data are synthetic (built by the
-reference's construction rules), weights fixed as in the model.
+Workload (default, --workload batched): the batched sweep - 256 independent
+Brunel-style LIF instances, N log-uniform in [1k, 50k] (80 % excitatory),
+Bernoulli recurrent connectivity p ~ U[0.01, 0.05], g ~ U[3, 7], delays
+U{1..10} steps, external drive of N/5 Poisson inputs at 20 Hz, distinct
+seeds, half of them with weight-dependent STDP on the input synapses; about
+4.2e9 synapses (34 GB of entries) drawn on the GPU.  The autotuner picks the
+schedules, the instances run in one batch (co-resident waves of the
+persistent step kernel), and the same instances run alone one after another
+give the plain form (`plain`, `batched_over_plain`).
+
+Other workloads: brunel (Examples/Brunel10K.cpp at 10,000 + 2,500 LIF with
+10,000 Poisson inputs, in-degree 0.1, delays U{1..20}, 28.1 M synapses),
+vogels_abbott (Examples/VogelsAbbottNet.cpp, 4,000 conductance LIF),
+plastic_ff (50,000 log-normal Poisson inputs onto 200,000 LIF, 1,000
+afferents each, STDP).  Data are synthetic, built by the reference's
+construction rules or drawn on the GPU.
 
 A bench "step" is one block of --block timesteps (default 1000 = 0.1 s of
-simulated time); the default 20 steps cover the configuration's 2 s.
+simulated time); the default step count covers the workload's simulated time
+(1 s batched, 2 s brunel, 1 s vogels_abbott, 5 s plastic_ff).
 
 Printed JSON (one line): value = synaptic events/s over the timed region
 (events = sum over spikes of the spiking neuron's out-degree), device-timed
 with CUDA events on the engine's stream; e2e = the same metric through the
-public run API with a host->device rate upload and a device->host spike
-readback every step; roofline for the step kernel; cpu_baseline = the CPU
-oracle (a single-thread C++ transcription of the reference step loop) on a
-bounded sample.
+public API with a host->device rate upload and a device->host spike readback
+every step; roofline for the step kernel; cpu_baseline = the CPU oracle (a
+single-thread C++ transcription of the reference step loop) on a bounded
+sample.
 
 --impl reference: the reference has no CPU implementation of the step (its
 only backend is CUDA; the Dummy backend computes nothing), so the reference
-arm times the oracle port of its step loop with all host threads.
+arm times the oracle port of its step loop with the host's threads.
 """
 from __future__ import annotations
 
@@ -43,10 +53,16 @@ DT = 0.0001
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=None,
+                   help="timed bench steps (default: the workload's simulated time, 1000 timesteps per step)")
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="brunel", choices=["brunel", "vogels_abbott", "plastic_ff"])
+    p.add_argument("--workload", default="batched",
+                   choices=["batched", "brunel", "vogels_abbott", "plastic_ff"])
+    p.add_argument("--instances", type=int, default=256, help="batched: network instances")
+    p.add_argument("--tune-steps", type=int, default=100, help="batched: autotuner trial timesteps")
+    p.add_argument("--plain-block", type=int, default=200,
+                   help="batched: timesteps each instance runs alone for the plain comparison")
     p.add_argument("--block", type=int, default=1000, help="timesteps per bench step")
     p.add_argument("--ctas", type=int, default=0)
     p.add_argument("--warps", type=int, default=0)
@@ -55,7 +71,11 @@ def parse():
     p.add_argument("--cpu-sample-steps", type=int, default=5000)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    return p.parse_args()
+    a = p.parse_args()
+    if a.steps is None:
+        sim_s = {"batched": 1.0, "brunel": 2.0, "vogels_abbott": 1.0, "plastic_ff": 5.0}[a.workload]
+        a.steps = max(1, int(round(sim_s / (a.block * DT))))
+    return a
 
 
 def build_model(workload: str):
@@ -205,7 +225,11 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
+        if args.workload == "batched":
+            return run_reference_batched(args, rank, world)
         return run_reference(args, rank, world)
+    if args.workload == "batched":
+        return run_batched(args, rank, world, local)
 
     import torch
     torch.cuda.set_device(local)
@@ -323,6 +347,273 @@ def main():
             "gpu_launches": launches + args.steps,
         }
         print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+# ---- batched sweep ------------------------------------------------------------------
+
+BATCH_CPU_INSTANCES = 8      # smallest instances of the sweep run by the CPU baselines
+BATCH_CPU_STEPS = 400
+
+
+def batched_config(gens, n_syn=None):
+    n = [g.desc.n_neurons for g in gens]
+    cfg = {"workload": f"batched_sweep_{len(gens)}_instances_N{min(n)}-{max(n)}",
+           "instances": len(gens), "neurons": int(sum(n)), "inputs": int(sum(g.desc.n_inputs for g in gens)),
+           "plastic_instances": int(sum(1 for g in gens if g.desc.has_stdp)),
+           "connectivity": "Bernoulli p~U[0.01,0.05], inputs n/5 at 20 Hz with p_in=4p, g~U[3,7], delays U{1..10}",
+           "dt_ms": 0.1, "sim_s_per_instance_config": 1.0}
+    if n_syn is not None:
+        cfg["synapses"] = int(n_syn)
+    return cfg
+
+
+BATCH_CPU_MAX_N = 8000       # instances up to this size are drawn on the host in about a second
+
+
+def cpu_sample_gens(gens):
+    """Instances of the sweep spread over its sizes up to BATCH_CPU_MAX_N
+    neurons (their synapse lists are cheap to draw on the host with the
+    oracle's restatement of the generator)."""
+    order = sorted(range(len(gens)), key=lambda k: gens[k].desc.n_neurons)
+    small = [k for k in order if gens[k].desc.n_neurons <= BATCH_CPU_MAX_N] or order[:1]
+    n = min(BATCH_CPU_INSTANCES, len(small))
+    pick = [small[(i * (len(small) - 1)) // max(n - 1, 1)] for i in range(n)]
+    return [gens[k] for k in pick]
+
+
+def oracle_instance(gen):
+    from oracle import OracleNet
+    from oracle.binding import generate_synapses
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import descs
+    a = generate_synapses(gen.desc)
+    d = gen.desc
+    groups = [dict(count=d.groups[i].count, tau_m=d.groups[i].tau_m, R=d.groups[i].R, v0=d.groups[i].v0,
+                   vreset=d.groups[i].vreset, theta=d.groups[i].theta) for i in range(d.n_groups)]
+    import numpy as np
+    rates = np.ctypeslib.as_array(d.input_rates, (d.n_inputs,)).copy()
+    dd = descs.Desc(kind=d.synapse_kind, groups=groups, refractory=d.refractory_period, n_inputs=d.n_inputs,
+                    rates=rates, pre=a["pre"], post=a["post"], weight=a["weight"], scale=a["scale"],
+                    delay=a["delay"], label=a["label"], plastic=a["plastic"] if d.has_stdp else None,
+                    stdp=None, seed=d.seed)
+    if d.has_stdp:
+        dd.desc.has_stdp = 1
+        dd.desc.stdp = d.stdp
+    return OracleNet(dd.desc, 32, threads=1), dd
+
+
+class CpuSample:
+    """The oracle on the CPU sample of the sweep, built once."""
+
+    def __init__(self, gens):
+        picked = cpu_sample_gens(gens)
+        self.nets = [oracle_instance(g)[0] for g in picked]
+        sizes = [g.desc.n_neurons for g in picked]
+        self.label = f"{len(self.nets)} instances of the sweep (N {min(sizes)}-{max(sizes)})"
+
+    def run(self, steps, parallel):
+        """Events/s of `steps` timesteps of every sample instance, one thread
+        per instance (parallel) or one after another."""
+        import threading
+        results = [0] * len(self.nets)
+
+        def work(i):
+            o = self.nets[i]
+            e0 = o.events()
+            o.run_steps(steps, True)
+            results[i] = o.events() - e0
+
+        t0 = time.perf_counter()
+        if parallel:
+            th = [threading.Thread(target=work, args=(i,)) for i in range(len(self.nets))]
+            for t in th:
+                t.start()
+            for t in th:
+                t.join()
+        else:
+            for i in range(len(self.nets)):
+                work(i)
+        el = time.perf_counter() - t0
+        return sum(results) / el, el
+
+
+def run_reference_batched(args, rank, world):
+    """CPU reference arm for the batched sweep: the oracle port, one instance
+    per host thread, on the smallest instances of the sweep."""
+    if rank != 0:
+        return
+    from spike_gb300 import networks
+    gens = networks.batched_sweep(args.instances)
+    threads = min(os.cpu_count() or 1, BATCH_CPU_INSTANCES)
+    cs = CpuSample(gens)
+    per_step = min(args.block, 100)
+    vals, els = [], []
+    for i in range(args.warmup + args.steps):
+        v, el = cs.run(per_step, parallel=True)
+        if i >= args.warmup:
+            vals.append(v)
+            els.append(el)
+    value = sum(vals) / len(vals)
+    sample = f"{cs.label}, {per_step} timesteps each per step, one host thread per instance"
+    line = {"metric": "synaptic_events_per_s", "value": value, "unit": "events/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(els) / len(els),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference", "config": batched_config(gens),
+            "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_batched(args, rank, world, local):
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__
+    __graft_entry__.build()
+    from spike_gb300 import Batch, Net, networks
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    gens = networks.batched_sweep(args.instances)
+    t0 = time.perf_counter()
+    scheds, tune_ms = Batch.autotune(gens, trial_steps=args.tune_steps)
+    tune_s = time.perf_counter() - t0
+    nets = [Net.generate(g, s) for g, s in zip(gens, scheds)]
+    n_syn = sum(n.synapse_count() for n in nets)
+    b = Batch(nets)
+    stream = torch.cuda.ExternalStream(b.stream())
+    n_neurons = sum(g.desc.n_neurons for g in gens)
+    n_inputs = sum(g.desc.n_inputs for g in gens)
+
+    for _ in range(args.warmup):
+        b.run_steps(args.block, True)
+    assert b.synchronize() == 0
+    for n in nets:
+        n.clear_spikes()
+    barrier()
+    e0 = sum(n.events() for n in nets)
+    l0 = b.launches()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        start.record(stream)
+        for _ in range(args.steps):
+            b.run_steps(args.block, True)
+        stop.record(stream)
+        stop.synchronize()
+        barrier()
+    status = b.synchronize()
+    ms = start.elapsed_time(stop)
+    events = sum(n.events() for n in nets) - e0
+    launches = b.launches() - l0
+    el = torch.tensor([ms / 1000.0], device="cuda")
+    ev = torch.tensor([float(events)], device="cuda", dtype=torch.float64)
+    if dist:
+        dist.all_reduce(el, op=dist.ReduceOp.MAX)
+        dist.all_reduce(ev, op=dist.ReduceOp.SUM)
+    elapsed = float(el.item())
+    value = float(ev.item()) / elapsed
+    sim_s = args.steps * args.block * DT
+
+    # roofline: algorithmic bytes of all instances over the step-kernel launches
+    timesteps = args.steps * args.block
+    alg = algorithmic_bytes(events, 0, n_neurons * timesteps, n_inputs * timesteps, 1)
+    per_launch_s = (ms / 1000.0) / max(launches, 1)
+    per_launch_bytes = alg / max(launches, 1)
+    peak, peak_kind = peaks()
+    achieved = per_launch_bytes / per_launch_s / 1e9
+    tr = traffic_per_launch("batched")
+    traffic = None
+    if tr and tr.get("dram_bytes_per_event"):
+        traffic = tr["dram_bytes_per_event"] * events / max(launches, 1)
+
+    # plain form: the same instances, each alone on its own stream, one after another
+    plain_ev, plain_ms = 0, 0.0
+    for n in nets:
+        s = torch.cuda.ExternalStream(n.stream())
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        pe0 = n.events()
+        a0.record(s)
+        n.run_steps(args.plain_block, True)
+        a1.record(s)
+        a1.synchronize()
+        plain_ms += a0.elapsed_time(a1)
+        plain_ev += n.events() - pe0
+    plain = {"value": plain_ev / (plain_ms / 1000.0), "unit": "events/s",
+             "sample": f"every instance alone for {args.plain_block} timesteps, one after another",
+             "sim_s_per_wall_s": len(nets) * args.plain_block * DT / (plain_ms / 1000.0)}
+
+    # end to end through the public API: rates up, batch step, spikes back
+    e2e = None
+    if not args.no_e2e:
+        import numpy as np
+        pinned = [torch.from_numpy(np.ctypeslib.as_array(g.desc.input_rates, (g.desc.n_inputs,)).copy()).pin_memory()
+                  for g in gens]
+        for n in nets:
+            n.clear_spikes()
+        barrier()
+        ee0 = sum(n.events() for n in nets)
+        h2d = 4 * n_inputs
+        d2h = 0
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for n, r in zip(nets, pinned):
+                n.write_rates(0, r.data_ptr(), r.numel())
+            b.run_steps(args.block, True)
+            for n in nets:
+                ids, times = n.spikes()
+                d2h += 8 * len(ids) + 16
+                n.clear_spikes()
+        barrier()
+        t_e2e = time.perf_counter() - t0
+        e2e_events = sum(n.events() for n in nets) - ee0
+        e2e = {"value": e2e_events / t_e2e, "unit": "events/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": int(d2h / args.steps),
+               "sim_s_per_wall_s": len(nets) * sim_s / t_e2e}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cs = CpuSample(gens)
+        cv, cel = cs.run(BATCH_CPU_STEPS, parallel=False)
+        cpu = {"value": cv, "unit": "events/s", "cores": 1, "kind": "port",
+               "sample": f"{cs.label}, {BATCH_CPU_STEPS} timesteps each from reset, {cel:.1f} s of CPU"}
+
+    if rank == 0:
+        sch = {}
+        for s in scheds:
+            k = f"{s.warps_per_cta}x{s.tile_posts}"
+            sch[k] = sch.get(k, 0) + 1
+        line = {
+            "metric": "synaptic_events_per_s", "value": value, "unit": "events/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "ours",
+            "config": {**batched_config(gens, n_syn), "block_timesteps": args.block,
+                       "schedules": sch, "autotune_s": round(tune_s, 2), "autotune_trial_ms": tune_ms,
+                       "waves_per_block": launches / max(1, args.steps * -(-args.block // 1000)),
+                       "l2": f"synapse entries {8 * n_syn / 1e9:.1f} GB > 129 MB L2 (no flush)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "sim_s_per_wall_s": len(nets) * sim_s / elapsed,
+            "plain": plain, "batched_over_plain": value / plain["value"],
+            "status": status,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "spk::step_kernel", "launches": launches,
+                         "alg_bytes_per_launch": per_launch_bytes, "ms_per_launch": 1000 * per_launch_s},
+            "e2e": e2e, "cpu_baseline": cpu, "clocks": clk.summary(),
+            "gpu_launches": launches + args.steps * len(nets),
+        }
+        print(json.dumps(line), flush=True)
+    b.close()
     if dist:
         dist.destroy_process_group()
 
