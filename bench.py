@@ -485,9 +485,11 @@ def run_batched(args, rank, world, local):
 
     gens = networks.batched_sweep(args.instances)
     t0 = time.perf_counter()
-    scheds, tune_ms = Batch.autotune(gens, trial_steps=args.tune_steps)
+    scheds, tune_ms, costs = Batch.autotune(gens, trial_steps=args.tune_steps, costs=True)
     tune_s = time.perf_counter() - t0
     nets = [Net.generate(g, s) for g, s in zip(gens, scheds)]
+    for n, c in zip(nets, costs):
+        n.set_step_cost(c)
     n_syn = sum(n.synapse_count() for n in nets)
     b = Batch(nets)
     stream = torch.cuda.ExternalStream(b.stream())
@@ -600,6 +602,7 @@ def run_batched(args, rank, world, local):
             "config": {**batched_config(gens, n_syn), "block_timesteps": args.block,
                        "schedules": sch, "autotune_s": round(tune_s, 2), "autotune_trial_ms": tune_ms,
                        "waves_per_block": launches / max(1, args.steps * -(-args.block // 1000)),
+                       "plain_step_us_alone_sum": round(sum(costs), 1),
                        "l2": f"synapse entries {8 * n_syn / 1e9:.1f} GB > 129 MB L2 (no flush)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "sim_s_per_wall_s": len(nets) * sim_s / elapsed,

@@ -288,10 +288,17 @@ int spk_batch_destroy(spk_batch* batch);
  * CTA, largest tile), builds and packs the networks under each, times
  * trial_steps steps of the batch and writes the fastest policy's schedule of
  * every network to schedules[n_nets] (and its trial time to best_ms, which
- * may be NULL).  Results never depend on the schedule.  Destroy a batch before
- * the networks it holds. */
+ * may be NULL).  With step_us (may be NULL) it also times each network alone
+ * under its schedule and writes microseconds per step, for
+ * spk_net_set_step_cost.  Results never depend on the schedule.  Destroy a
+ * batch before the networks it holds. */
 int spk_batch_autotune(const spk_gen_desc* descs, int32_t n_nets, int32_t trial_steps,
-                       spk_schedule* schedules, float* best_ms);
+                       spk_schedule* schedules, float* best_ms, float* step_us);
+/* Cost of one step of the network (any unit, e.g. the step_us above).  A
+ * batch orders its networks by decreasing cost into its co-resident waves, so
+ * that each wave - which lasts as long as its slowest member - holds networks
+ * of similar cost; without costs it orders by shared memory and CTA count. */
+int spk_net_set_step_cost(spk_net* net, float cost);
 
 /* ---- allocation-free stepping --------------------------------------------
  * This entry point has no counterpart in the reference.  It is for callers

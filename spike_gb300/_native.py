@@ -173,7 +173,8 @@ _SIGS = {
     "spk_batch_launch_count": (i32, [_VP, P(i64)]),
     "spk_batch_stream": (i32, [_VP, P(_VP)]),
     "spk_batch_destroy": (i32, [_VP]),
-    "spk_batch_autotune": (i32, [P(GenDesc), i32, i32, P(Schedule), P(f32)]),
+    "spk_batch_autotune": (i32, [P(GenDesc), i32, i32, P(Schedule), P(f32), P(f32)]),
+    "spk_net_set_step_cost": (i32, [_VP, f32]),
     "spk_step_noalloc": (i32, [P(DeviceNet), i64, i32, f32, _VP]),
     "spk_memory_info": (i32, [P(u64), P(u64)]),
     "spk_abi_version": (i32, []),

@@ -195,6 +195,7 @@ struct spk_net {
   int pending_status = SPK_OK;
   bool generated = false;  // connectivity drawn on the device (no host synapse arrays)
   int64_t n_csc = 0;       // plastic afferent records
+  float step_cost = 0.0f;  // measured or estimated time of one step alone (batch packing)
 };
 
 struct spk_batch {
@@ -1120,6 +1121,12 @@ int spk_net_generate(const spk_gen_desc* desc, const spk_schedule* schedule, spk
   return guarded([&] { return generate_impl(desc, schedule, out); });
 }
 
+int spk_net_set_step_cost(spk_net* n, float cost) {
+  if (!n || !(cost >= 0.0f)) return SPK_ERR_INVALID;
+  n->step_cost = cost;
+  return SPK_OK;
+}
+
 int spk_net_synapse_count(const spk_net* n, int64_t* count) {
   if (!n || !count) return SPK_ERR_INVALID;
   *count = n->S;
@@ -1465,7 +1472,13 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
     // (which gives every CTA the wave's largest footprint) wastes little.
     std::vector<int> order(n_nets);
     for (int i = 0; i < n_nets; ++i) order[i] = i;
+    // With step costs (spk_net_set_step_cost) the order is by decreasing
+    // cost instead, so that each wave - which lasts as long as its slowest
+    // network - holds networks of similar cost.
+    bool costed = false;
+    for (int i = 0; i < n_nets; ++i) costed |= nets[i]->step_cost > 0.0f;
     std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+      if (costed && nets[a]->step_cost != nets[c]->step_cost) return nets[a]->step_cost > nets[c]->step_cost;
       if (nets[a]->plan.smem != nets[c]->plan.smem) return nets[a]->plan.smem > nets[c]->plan.smem;
       return nets[a]->plan.nctas > nets[c]->plan.nctas;
     });
@@ -2004,8 +2017,42 @@ static int trial_policy(const spk_gen_desc* descs, int n, const std::vector<spk_
 
 }  // namespace spk
 
+// Time of one step of each network alone under its schedule (microseconds).
+static int measure_alone(const spk_gen_desc* descs, int n, const std::vector<spk_schedule>& sch, int steps,
+                         float* step_us) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    set_error("cudaEventCreate failed");
+    return SPK_ERR_CUDA;
+  }
+  int rc = SPK_OK;
+  for (int i = 0; i < n && rc == SPK_OK; ++i) {
+    spk_net* x = nullptr;
+    rc = generate_impl(&descs[i], &sch[i], &x);
+    if (rc) break;
+    rc = run_steps_impl(x, std::max(1, steps / 2), 1, x->current_time);
+    x->current_time += (float)std::max(1, steps / 2) * x->dt;
+    if (rc == SPK_OK) {
+      cudaEventRecord(e0, x->stream);
+      rc = run_steps_impl(x, steps, 1, x->current_time);
+      cudaEventRecord(e1, x->stream);
+    }
+    float ms = 0.0f;
+    if (rc == SPK_OK && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+      rc = SPK_ERR_CUDA;
+    int st = SPK_OK;
+    if (rc == SPK_OK && read_status(x, &st) == SPK_OK && st != SPK_OK) rc = st;
+    step_us[i] = 1000.0f * ms / (float)steps;
+    spk_net_destroy(x);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
 extern "C" int spk_batch_autotune(const spk_gen_desc* descs, int32_t n_nets, int32_t trial_steps,
-                                  spk_schedule* schedules, float* best_ms) {
+                                  spk_schedule* schedules, float* best_ms, float* step_us) {
   using namespace spk;
   if (!descs || n_nets < 1 || !schedules || trial_steps < 1) return SPK_ERR_INVALID;
   return guarded([&]() -> int {
@@ -2030,6 +2077,7 @@ extern "C" int spk_batch_autotune(const spk_gen_desc* descs, int32_t n_nets, int
     if (best < 0.0f) return last_rc;
     std::copy(best_sch.begin(), best_sch.end(), schedules);
     if (best_ms) *best_ms = best;
+    if (step_us) return measure_alone(descs, n_nets, best_sch, trial_steps, step_us);
     return SPK_OK;
   });
 }

@@ -139,6 +139,10 @@ class Net:
               "spk_net_generate")
         return cls(h)
 
+    def set_step_cost(self, cost: float):
+        """Cost of one step (e.g. microseconds alone) for batch wave packing."""
+        check(lib().spk_net_set_step_cost(self.h, C.c_float(cost)), "spk_net_set_step_cost")
+
     def synapse_count(self) -> int:
         n = C.c_int64()
         check(lib().spk_net_synapse_count(self.h, C.byref(n)), "spk_net_synapse_count")
@@ -339,14 +343,19 @@ class Batch:
               "spk_batch_create")
 
     @staticmethod
-    def autotune(gens: list, trial_steps: int = 200):
+    def autotune(gens: list, trial_steps: int = 200, costs: bool = False):
         """Measured schedule search (spk_batch_autotune) for generated
-        networks: returns (schedules, trial milliseconds of the best policy)."""
+        networks: returns (schedules, trial milliseconds of the best policy),
+        plus each network's microseconds per step alone when costs=True."""
         descs = (N.GenDesc * len(gens))(*[g.desc for g in gens])
         out = (N.Schedule * len(gens))()
         ms = C.c_float()
-        check(lib().spk_batch_autotune(descs, len(gens), trial_steps, out, C.byref(ms)), "spk_batch_autotune")
-        return [N.Schedule(o.warps_per_cta, o.tile_posts, o.ctas, o.steps_per_launch) for o in out], ms.value
+        us = (C.c_float * len(gens))() if costs else None
+        check(lib().spk_batch_autotune(descs, len(gens), trial_steps, out, C.byref(ms), us), "spk_batch_autotune")
+        scheds = [N.Schedule(o.warps_per_cta, o.tile_posts, o.ctas, o.steps_per_launch) for o in out]
+        if costs:
+            return scheds, ms.value, [float(x) for x in us]
+        return scheds, ms.value
 
     def run_steps(self, steps: int, plasticity_on: bool = True):
         check(lib().spk_batch_run_steps(self.h, steps, 1 if plasticity_on else 0), "spk_batch_run_steps")

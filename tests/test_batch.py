@@ -27,9 +27,11 @@ def snapshot(net: Net, n: int, n_in: int, S: int):
 
 def test_autotuned_batch_equals_each_instance_alone():
     gens = small_sweep()
-    scheds, ms = Batch.autotune(gens, trial_steps=60)
-    assert ms > 0 and len(scheds) == len(gens)
+    scheds, ms, costs = Batch.autotune(gens, trial_steps=60, costs=True)
+    assert ms > 0 and len(scheds) == len(gens) and all(c > 0 for c in costs)
     batched = [Net.generate(g, s) for g, s in zip(gens, scheds)]
+    for n, c in zip(batched, costs):
+        n.set_step_cost(c)
     alone = [Net.generate(g, s) for g, s in zip(gens, scheds)]
     b = Batch(batched)
     for plastic, steps in ((True, 700), (False, 300)):
