@@ -183,6 +183,10 @@ int spk_net_write_rates(spk_net* net, int32_t stimulus, const float* rates, int6
 int spk_net_run(spk_net* net, float seconds, int32_t plasticity_on);
 /* As spk_net_run for an explicit step count (time advances by n_steps*dt). */
 int spk_net_run_steps(spk_net* net, int64_t n_steps, int32_t plasticity_on);
+/* Start a run of n_steps steps (time advances by n_steps*dt, as in
+ * spk_net_run_steps) without launching it; spk_batch_step_block then advances
+ * it a block at a time (the server's continuous batching). */
+int spk_net_begin_run(spk_net* net, int64_t n_steps, int32_t plasticity_on);
 /* Wait for the handle's stream; returns the device status word
  * (SPK_ERR_TIMEOUT / SPK_ERR_OVERFLOW) or SPK_OK. */
 int spk_net_synchronize(spk_net* net);
@@ -279,6 +283,16 @@ int spk_net_synapse_count(const spk_net* net, int64_t* n);
 int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* schedule,
                      spk_batch** out);
 int spk_batch_run_steps(spk_batch* batch, int64_t n_steps, int32_t plasticity_on);
+/* One round of the batch's launches: every network advances up to
+ * steps_per_launch steps of the run it was given with spk_net_begin_run
+ * (networks whose run is complete do nothing).  A run split this way gives the
+ * same result as the same run made in one call. */
+int spk_batch_step_block(spk_batch* batch);
+/* As spk_batch_run_steps with a step count and a plasticity switch per
+ * network (index i = the i-th network given to spk_batch_create;
+ * plasticity_on may be NULL: on for all); each network's time advances by its
+ * own count. */
+int spk_batch_run_steps_each(spk_batch* batch, const int64_t* n_steps, const int32_t* plasticity_on);
 int spk_batch_synchronize(spk_batch* batch);
 int spk_batch_launch_count(const spk_batch* batch, int64_t* launches);
 int spk_batch_stream(const spk_batch* batch, void** stream);
@@ -299,6 +313,83 @@ int spk_batch_autotune(const spk_gen_desc* descs, int32_t n_nets, int32_t trial_
  * that each wave - which lasts as long as its slowest member - holds networks
  * of similar cost; without costs it orders by shared memory and CTA count. */
 int spk_net_set_step_cost(spk_net* net, float cost);
+
+/* ---- simulation server: continuous batching (no counterpart in the
+ * reference) ---------------------------------------------------------------
+ * A server owns one host thread that drives the GPU.  Submitted jobs (a
+ * generated network and a step count) wait in a FIFO queue until the free
+ * device memory, less a reserve, holds their estimated footprint; then their
+ * network is generated on the device and joins the running set.  The running
+ * set advances in step blocks through one batch (co-resident waves of the
+ * persistent step kernel), each job by min(its remaining steps, the block);
+ * jobs admitted while a block runs join at the next block, and a finished
+ * job's spikes and counters are copied to the host and its device memory is
+ * freed.  A job's result does not depend on what else runs with it. */
+typedef struct spk_server spk_server;
+
+typedef struct spk_server_opts {
+  int32_t warps_per_cta;   /* schedule policy of admitted jobs (0 = 8)            */
+  int32_t tile_posts;      /* largest tile (0 = 64)                                */
+  int32_t steps_per_block; /* timesteps per batch round (0 = 1000)                 */
+  int32_t max_running;     /* running jobs at most (0 = 512)                       */
+  uint64_t reserve_bytes;  /* device memory kept free (0 = 8 GiB)                  */
+  int32_t record_spikes;   /* keep each finished job's neuron spikes on the host   */
+  int32_t reserved;
+} spk_server_opts;
+
+#define SPK_JOB_QUEUED 0
+#define SPK_JOB_RUNNING 1
+#define SPK_JOB_DONE 2
+#define SPK_JOB_FAILED 3
+#define SPK_JOB_CANCELLED 4
+
+typedef struct spk_job_info {
+  int32_t state;        /* SPK_JOB_* */
+  int32_t error;        /* SPK_ERR_* of a failed job */
+  int64_t steps_done;
+  int64_t steps_total;
+  uint64_t events;      /* synaptic events delivered */
+  int64_t spikes;       /* neuron spikes */
+  int64_t synapses;
+  double submit_s;      /* seconds since the server started */
+  double start_s;       /* admitted (network generated) */
+  double finish_s;
+} spk_job_info;
+
+typedef struct spk_server_stats {
+  int64_t submitted, running, queued, done, failed;
+  uint64_t events;      /* all jobs, delivered so far */
+  int64_t blocks;       /* batch rounds run */
+  double busy_s;        /* wall time with at least one job running */
+  double uptime_s;
+} spk_server_stats;
+
+int spk_server_start(const spk_server_opts* opts, spk_server** out);
+/* Copies the descriptor (and every array it points to); returns the job id. */
+int spk_server_submit(spk_server* server, const spk_gen_desc* desc, int64_t n_steps, int32_t plasticity_on,
+                      int64_t* job);
+int spk_server_poll(spk_server* server, int64_t job, spk_job_info* info);
+/* Block until the job is done, failed or cancelled, or timeout_s passes
+ * (SPK_ERR_BUSY). */
+int spk_server_wait(spk_server* server, int64_t job, double timeout_s);
+/* Neuron spikes of a finished job (needs record_spikes), ordered by step then
+ * neuron. */
+int spk_server_read_spikes(spk_server* server, int64_t job, int32_t* ids, float* times, int64_t capacity,
+                           int64_t* n_written);
+/* A queued job is dropped; a running one is stopped at the end of its block. */
+int spk_server_cancel(spk_server* server, int64_t job);
+/* Forget a finished job's results. */
+int spk_server_release(spk_server* server, int64_t job);
+int spk_server_stats_get(spk_server* server, spk_server_stats* stats);
+/* Finishes nothing further: running and queued jobs are cancelled, the
+ * thread joins and every device allocation of the server is freed. */
+int spk_server_stop(spk_server* server);
+
+/* Device memory a generated network will hold under a schedule (NULL = the
+ * planner's), from its projections' expected synapse counts plus six
+ * standard deviations, and the peak while it is generated. */
+int spk_net_generate_estimate(const spk_gen_desc* desc, const spk_schedule* schedule, int64_t* device_bytes,
+                              int64_t* peak_bytes);
 
 /* ---- allocation-free stepping --------------------------------------------
  * This entry point has no counterpart in the reference.  It is for callers

@@ -11,8 +11,8 @@ from ._native import (SPK_CONN_ALL_TO_ALL, SPK_CONN_GAUSSIAN_SAMPLE, SPK_CONN_ON
                       SPK_FIELD_V, SPK_INPUT_NONE, SPK_INPUT_PATTERNED, SPK_INPUT_POISSON,
                       SPK_POP_INPUTS, SPK_POP_NEURONS, SPK_SYN_CONDUCTANCE, SPK_SYN_CURRENT,
                       SPK_SYN_VOLTAGE, SpikeError, lib)
-from .model import (Batch, GenNetwork, LIFParams, Model, Net, Projection, STDPParams, SynapseParams,  # noqa: F401
-                    desc_arrays, schedule)
+from .model import (Batch, GenNetwork, LIFParams, Model, Net, Projection, Server, STDPParams,  # noqa: F401
+                    SynapseParams, desc_arrays, schedule)
 
-__all__ = ["Model", "Net", "Batch", "GenNetwork", "Projection", "LIFParams", "SynapseParams", "STDPParams",
-           "schedule", "lib"]
+__all__ = ["Model", "Net", "Batch", "Server", "GenNetwork", "Projection", "LIFParams", "SynapseParams",
+           "STDPParams", "schedule", "lib"]

@@ -2,7 +2,8 @@
 
 ``build()`` compiles
   * ``spike_gb300/libspike_gb300.so``: the sm_103a step engine and its C ABI
-    (``csrc/spk_net.cu``) plus the model-building front end (``csrc/frontend.cpp``);
+    (``csrc/spk_net.cu``), the model-building front end (``csrc/frontend.cpp``)
+    and the simulation server (``csrc/spk_server.cpp``);
   * ``oracle/liboracle.so``: the CPU oracle used by the tests and the benchmark's
     CPU baseline (test infrastructure, never linked into the engine).
 
@@ -41,6 +42,10 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build spike_gb300")
 
 
+def _cuda_include() -> str:
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(_nvcc()))), "include")
+
+
 def _newer(target: str, deps: list[str]) -> bool:
     if not os.path.exists(target):
         return True
@@ -72,13 +77,15 @@ def build_engine(force: bool = False) -> str:
          [nvcc, *ARCH, *NVCC_FLAGS, "-c"]),
         (os.path.join(CSRC, "frontend.cpp"), os.path.join(BUILD_DIR, "frontend.o"),
          ["g++", *CXX_FLAGS, "-c"]),
+        (os.path.join(CSRC, "spk_server.cpp"), os.path.join(BUILD_DIR, "spk_server.o"),
+         ["g++", *CXX_FLAGS, "-pthread", "-I" + _cuda_include(), "-c"]),
     ]
     todo = [(s, o, c) for (s, o, c) in units if force or _newer(o, [s, *hdrs])]
     with ThreadPoolExecutor(max_workers=len(units)) as ex:
         list(ex.map(lambda u: _run([*u[2], u[0], "-o", u[1]]), todo))
     objs = [o for (_, o, _) in units]
     if force or todo or _newer(LIB, objs):
-        _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+        _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-Xlinker", "-lpthread"])
     return LIB
 
 

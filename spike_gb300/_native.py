@@ -98,6 +98,25 @@ class GenDesc(C.Structure):
     ]
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("warps_per_cta", i32), ("tile_posts", i32), ("steps_per_block", i32), ("max_running", i32),
+                ("reserve_bytes", u64), ("record_spikes", i32), ("reserved", i32)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("state", i32), ("error", i32), ("steps_done", i64), ("steps_total", i64), ("events", u64),
+                ("spikes", i64), ("synapses", i64), ("submit_s", C.c_double), ("start_s", C.c_double),
+                ("finish_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", i64), ("running", i64), ("queued", i64), ("done", i64), ("failed", i64),
+                ("events", u64), ("blocks", i64), ("busy_s", C.c_double), ("uptime_s", C.c_double)]
+
+
+SPK_JOB_QUEUED, SPK_JOB_RUNNING, SPK_JOB_DONE, SPK_JOB_FAILED, SPK_JOB_CANCELLED = 0, 1, 2, 3, 4
+
+
 class Schedule(C.Structure):
     _fields_ = [("warps_per_cta", i32), ("tile_posts", i32), ("ctas", i32), ("steps_per_launch", i32)]
 
@@ -169,6 +188,9 @@ _SIGS = {
     "spk_net_stream": (i32, [_VP, P(_VP)]),
     "spk_batch_create": (i32, [P(_VP), i32, P(Schedule), P(_VP)]),
     "spk_batch_run_steps": (i32, [_VP, i64, i32]),
+    "spk_batch_run_steps_each": (i32, [_VP, P(i64), P(i32)]),
+    "spk_batch_step_block": (i32, [_VP]),
+    "spk_net_begin_run": (i32, [_VP, i64, i32]),
     "spk_batch_synchronize": (i32, [_VP]),
     "spk_batch_launch_count": (i32, [_VP, P(i64)]),
     "spk_batch_stream": (i32, [_VP, P(_VP)]),
@@ -176,6 +198,16 @@ _SIGS = {
     "spk_batch_autotune": (i32, [P(GenDesc), i32, i32, P(Schedule), P(f32), P(f32)]),
     "spk_net_set_step_cost": (i32, [_VP, f32]),
     "spk_step_noalloc": (i32, [P(DeviceNet), i64, i32, f32, _VP]),
+    "spk_server_start": (i32, [P(ServerOpts), P(_VP)]),
+    "spk_server_submit": (i32, [_VP, P(GenDesc), i64, i32, P(i64)]),
+    "spk_server_poll": (i32, [_VP, i64, P(JobInfo)]),
+    "spk_server_wait": (i32, [_VP, i64, C.c_double]),
+    "spk_server_read_spikes": (i32, [_VP, i64, P(i32), P(f32), i64, P(i64)]),
+    "spk_server_cancel": (i32, [_VP, i64]),
+    "spk_server_release": (i32, [_VP, i64]),
+    "spk_server_stats_get": (i32, [_VP, P(ServerStats)]),
+    "spk_server_stop": (i32, [_VP]),
+    "spk_net_generate_estimate": (i32, [P(GenDesc), P(Schedule), P(i64), P(i64)]),
     "spk_memory_info": (i32, [P(u64), P(u64)]),
     "spk_abi_version": (i32, []),
     "spk_last_error": (C.c_char_p, []),

@@ -420,6 +420,44 @@ static int new_net(const ModelSpec& m, int B, int64_t S, const spk_schedule* sch
   return SPK_OK;
 }
 
+// Bytes of each part of a network's device arena, in arena order: rowptr,
+// entries, csc_ptr, csc, V, last, traces, ring, input next, rates, post
+// traces, pre traces, pre-trace mailbox, spike and pre-event bitmaps, CTA key
+// lists and stamps, spike store, run control, abort flag, descriptor, CTA map.
+static std::vector<size_t> arena_part_sizes(const Plan& plan, int N, int Nin, int L, int B, int stdp, int64_t S,
+                                            int64_t n_csc, int n_stim, int64_t spike_cap) {
+  const size_t n_cells = (size_t)plan.n_keys * plan.n_tiles;
+  const size_t key_cap = (size_t)plan.W * (plan.TS + plan.ITS);
+  return {sizeof(int32_t) * (n_cells + 1),
+          sizeof(uint2) * (size_t)std::max<int64_t>(S, 1),
+          sizeof(int32_t) * (stdp ? (size_t)N + 1 : 0),
+          sizeof(uint2) * (size_t)n_csc,
+          sizeof(float) * N,
+          sizeof(float) * N,
+          sizeof(float) * (size_t)N * L,
+          sizeof(float) * (size_t)plan.n_tiles * B * plan.TS * L,
+          sizeof(float) * std::max(Nin, 1),
+          sizeof(float) * std::max<size_t>((size_t)n_stim * Nin, 1),
+          sizeof(float) * (stdp ? N : 0),
+          sizeof(float) * (stdp ? plan.n_keys : 0),
+          sizeof(float) * (stdp ? 2 * (size_t)plan.n_keys : 0),
+          sizeof(uint32_t) * 2 * (size_t)plan.n_words,
+          sizeof(uint32_t) * 2 * (size_t)plan.n_words,
+          sizeof(unsigned long long) * 2 * (size_t)plan.nctas * key_cap,
+          sizeof(unsigned long long) * 2 * (size_t)plan.nctas,
+          sizeof(uint2) * (size_t)std::max<int64_t>(spike_cap, 1),
+          sizeof(RunCtl),
+          sizeof(int),
+          sizeof(NetDev),
+          sizeof(CtaMap) * plan.nctas};
+}
+
+static size_t arena_total(const std::vector<size_t>& sizes) {
+  size_t total = 0;
+  for (size_t b : sizes) total = align_up(total, 256) + align_up(std::max<size_t>(b, 4), 256);
+  return total;
+}
+
 // Allocates the device arena of `n` (CSR parts sized by S and n_csc), creates
 // its stream, fills and uploads the device descriptor, uploads whichever host
 // CSR arrays are given (generated networks pass none and fill them on the
@@ -455,32 +493,13 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   void* p_ckeys = nullptr; void* p_cstamp = nullptr;
   const int key_cap = plan.W * (plan.TS + plan.ITS);
   void* p_ctl = nullptr; void* p_abort = nullptr; void* p_dd = nullptr; void* p_map = nullptr;
-  std::vector<Part> parts = {
-      {&p_rowptr, sizeof(int32_t) * (n_cells + 1)},
-      {&p_entries, sizeof(uint2) * (size_t)std::max<int64_t>(S, 1)},
-      {&p_cscptr, sizeof(int32_t) * (stdp ? (size_t)N + 1 : 0)},
-      {&p_csc, sizeof(uint2) * (size_t)n_csc},
-      {&p_V, sizeof(float) * N},
-      {&p_last, sizeof(float) * N},
-      {&p_gtr, sizeof(float) * (size_t)N * L},
-      {&p_ring, sizeof(float) * (size_t)n_tiles * B * TS * L},
-      {&p_innext, sizeof(float) * std::max(Nin, 1)},
-      {&p_rates, sizeof(float) * std::max<size_t>((size_t)n->n_stim * Nin, 1)},
-      {&p_post, sizeof(float) * (stdp ? N : 0)},
-      {&p_pre, sizeof(float) * (stdp ? n_keys : 0)},
-      {&p_pub, sizeof(float) * (stdp ? 2 * (size_t)n_keys : 0)},
-      {&p_bA, sizeof(uint32_t) * 2 * (size_t)n_words},
-      {&p_bP, sizeof(uint32_t) * 2 * (size_t)n_words},
-      {&p_ckeys, sizeof(unsigned long long) * 2 * (size_t)plan.nctas * key_cap},
-      {&p_cstamp, sizeof(unsigned long long) * 2 * (size_t)plan.nctas},
-      {&p_spk, sizeof(uint2) * (size_t)std::max<int64_t>(spike_cap, 1)},
-      {&p_ctl, sizeof(RunCtl)},
-      {&p_abort, sizeof(int)},
-      {&p_dd, sizeof(NetDev)},
-      {&p_map, sizeof(CtaMap) * plan.nctas},
-  };
-  size_t total = 0;
-  for (auto& p : parts) total = align_up(total, 256) + align_up(std::max<size_t>(p.bytes, 4), 256);
+  const std::vector<size_t> sizes = arena_part_sizes(plan, N, Nin, L, B, stdp, S, n_csc, n->n_stim, spike_cap);
+  void** dsts[] = {&p_rowptr, &p_entries, &p_cscptr, &p_csc,   &p_V,     &p_last,   &p_gtr,  &p_ring,
+                   &p_innext, &p_rates,   &p_post,   &p_pre,   &p_pub,   &p_bA,     &p_bP,   &p_ckeys,
+                   &p_cstamp, &p_spk,     &p_ctl,    &p_abort, &p_dd,    &p_map};
+  std::vector<Part> parts;
+  for (size_t i = 0; i < sizes.size(); ++i) parts.push_back(Part{dsts[i], sizes[i]});
+  const size_t total = arena_total(sizes);
   cudaError_t e = cudaMalloc(&n->arena, total);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -792,20 +811,23 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
   return SPK_OK;
 }
 
-// Device memory released on scope exit (temporaries of network generation).
+// Stream-ordered device memory released on scope exit (temporaries of network
+// generation; stream-ordered so that generating a network never waits for
+// kernels running on other streams, such as a batch in flight).
 struct DevTemp {
   void* p = nullptr;
-  DevTemp() = default;
+  cudaStream_t s = nullptr;
+  explicit DevTemp(cudaStream_t stream) : s(stream) {}
   DevTemp(const DevTemp&) = delete;
   DevTemp& operator=(const DevTemp&) = delete;
   ~DevTemp() { reset(); }
   void reset() {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, s);
     p = nullptr;
   }
   bool alloc(size_t bytes) {
     reset();
-    if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+    if (cudaMallocAsync(&p, std::max<size_t>(bytes, 16), s) != cudaSuccess) {
       cudaGetLastError();
       p = nullptr;
       set_error("device allocation of %zu bytes for network generation failed", bytes);
@@ -963,7 +985,7 @@ static int generate_impl(const spk_gen_desc* d, const spk_schedule* sched, spk_n
     g.seed = d->connectivity_seed;
     return g;
   };
-  DevTemp proj_dev, small;
+  DevTemp proj_dev(st), small(st);
   if (!proj_dev.alloc(sizeof(GenProj) * proj.size()) || !small.alloc(64)) return SPK_ERR_OOM;
   if (!proj.empty())
     SPK_CUDA(cudaMemcpyAsync(proj_dev.p, proj.data(), sizeof(GenProj) * proj.size(), cudaMemcpyHostToDevice, st));
@@ -987,7 +1009,7 @@ static int generate_impl(const spk_gen_desc* d, const spk_schedule* sched, spk_n
     SPK_CUDA(cudaStreamSynchronize(st));
     return SPK_OK;
   };
-  DevTemp counts;
+  DevTemp counts(st);
   unsigned long long tot[2] = {0, 0};
   int dr[2] = {0, 0};
   rc = count_pass(plan0, counts, tot, dr);
@@ -1038,7 +1060,7 @@ static int generate_impl(const spk_gen_desc* d, const spk_schedule* sched, spk_n
     if (cub::DeviceScan::ExclusiveSum(nullptr, tb, counts.as<int>(), (int*)n->hd.rowptr, n_cells + 1, st) !=
         cudaSuccess)
       return fail(SPK_ERR_CUDA);
-    DevTemp tmp;
+    DevTemp tmp(st);
     if (!tmp.alloc(tb)) return fail(SPK_ERR_OOM);
     if (cub::DeviceScan::ExclusiveSum(tmp.p, tb, counts.as<int>(), (int*)n->hd.rowptr, n_cells + 1, st) !=
         cudaSuccess) {
@@ -1048,7 +1070,7 @@ static int generate_impl(const spk_gen_desc* d, const spk_schedule* sched, spk_n
     if (cudaStreamSynchronize(st) != cudaSuccess) return fail(SPK_ERR_CUDA);
   }
   const bool csc = m.has_stdp && P > 0;
-  DevTemp sort_a, sort_b, val_a, val_b, ekey, pcnt;
+  DevTemp sort_a(st), sort_b(st), val_a(st), val_b(st), ekey(st), pcnt(st);
   if (m.has_stdp && !csc &&
       cudaMemsetAsync((void*)n->hd.csc_ptr, 0, sizeof(int) * ((size_t)N + 1), st) != cudaSuccess)
     return fail(SPK_ERR_CUDA);
@@ -1069,7 +1091,7 @@ static int generate_impl(const spk_gen_desc* d, const spk_schedule* sched, spk_n
     if (cub::DeviceScan::ExclusiveSum(nullptr, tb, pcnt.as<int>(), (int*)n->hd.csc_ptr, (long long)N + 1, st) !=
         cudaSuccess)
       return fail(SPK_ERR_CUDA);
-    DevTemp tmp;
+    DevTemp tmp(st);
     if (!tmp.alloc(tb)) return fail(SPK_ERR_OOM);
     if (cub::DeviceScan::ExclusiveSum(tmp.p, tb, pcnt.as<int>(), (int*)n->hd.csc_ptr, (long long)N + 1, st) !=
         cudaSuccess)
@@ -1083,7 +1105,7 @@ static int generate_impl(const spk_gen_desc* d, const spk_schedule* sched, spk_n
     size_t sb = 0;
     if (cub::DeviceRadixSort::SortPairs(nullptr, sb, keys, vals, (long long)S, 0, end_bit, st) != cudaSuccess)
       return fail(SPK_ERR_CUDA);
-    DevTemp stmp;
+    DevTemp stmp(st);
     if (!stmp.alloc(sb)) return fail(SPK_ERR_OOM);
     if (cub::DeviceRadixSort::SortPairs(stmp.p, sb, keys, vals, (long long)S, 0, end_bit, st) != cudaSuccess) {
       set_error("plastic afferent sort failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -1125,6 +1147,49 @@ int spk_net_set_step_cost(spk_net* n, float cost) {
   if (!n || !(cost >= 0.0f)) return SPK_ERR_INVALID;
   n->step_cost = cost;
   return SPK_OK;
+}
+
+int spk_net_generate_estimate(const spk_gen_desc* d, const spk_schedule* sched, int64_t* device_bytes,
+                              int64_t* peak_bytes) {
+  if (!d || d->n_neurons <= 0 || d->n_inputs < 0 || d->n_projections < 0 ||
+      (d->n_projections > 0 && !d->projections))
+    return SPK_ERR_INVALID;
+  return guarded([&]() -> int {
+    double mu = 0.0, var = 0.0, mu_p = 0.0, var_p = 0.0;
+    int dmax = 1;
+    for (int j = 0; j < d->n_projections; ++j) {
+      const spk_projection& P = d->projections[j];
+      const double n = (double)P.pre_count * (double)P.post_count, p = P.probability;
+      mu += n * p;
+      var += n * p * (1.0 - p);
+      if (P.plastic && d->has_stdp) {
+        mu_p += n * p;
+        var_p += n * p * (1.0 - p);
+      }
+      dmax = std::max(dmax, P.delay_hi);
+    }
+    const int64_t S = (int64_t)(mu + 6.0 * std::sqrt(var) + 16.0);
+    const int64_t Pl = d->has_stdp ? (int64_t)(mu_p + 6.0 * std::sqrt(var_p) + 16.0) : 0;
+    DeviceInfo di;
+    int rc = device_info(&di);
+    if (rc) return rc;
+    Plan plan;
+    const int B = dmax + 3;
+    rc = make_plan(d->n_neurons, d->n_inputs, B, std::max(1, d->n_labels), d->synapse_kind, d->has_stdp ? 1 : 0,
+                   sched, di, &plan);
+    if (rc) return rc;
+    const int64_t cap = d->spike_capacity == 0 ? DEFAULT_SPIKE_CAPACITY : std::max<int64_t>(0, d->spike_capacity);
+    const size_t arena = arena_total(arena_part_sizes(plan, d->n_neurons, d->n_inputs, std::max(1, d->n_labels), B,
+                                                      d->has_stdp ? 1 : 0, S, Pl, d->n_inputs ? d->n_stimuli : 0,
+                                                      cap));
+    // generation temporaries: cell counts, and for plastic synapses the sort
+    // keys, values, entry keys (both buffers) and the sort's own storage
+    const size_t cells = (size_t)plan.n_keys * plan.n_tiles + 1;
+    const size_t temp = 4 * cells + (Pl > 0 ? (size_t)S * (5 * 4 + 8) + 4 * ((size_t)d->n_neurons + 1) : 0);
+    if (device_bytes) *device_bytes = (int64_t)arena;
+    if (peak_bytes) *peak_bytes = (int64_t)(arena + temp);
+    return SPK_OK;
+  });
 }
 
 int spk_net_synapse_count(const spk_net* n, int64_t* count) {
@@ -1191,6 +1256,16 @@ int spk_net_run(spk_net* n, float seconds, int32_t plasticity_on) {
   int rc = run_steps_impl(n, steps, plasticity_on, start);
   if (rc) return rc;
   n->current_time = start + seconds;
+  return SPK_OK;
+}
+
+int spk_net_begin_run(spk_net* n, int64_t n_steps, int32_t plasticity_on) {
+  if (!n || n_steps < 0 || n_steps > 0x7fffffff) return SPK_ERR_INVALID;
+  const float start = n->current_time;
+  set_ctl_kernel<<<1, 1, 0, n->stream>>>(n->hd.ctl, start, (int)n_steps, (plasticity_on && n->has_stdp) ? 1 : 0,
+                                         n->record_inputs ? 1 : 0);
+  SPK_CUDA(cudaGetLastError());
+  n->current_time = start + (float)n_steps * n->dt;
   return SPK_OK;
 }
 
@@ -1557,17 +1632,25 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
   });
 }
 
-int spk_batch_run_steps(spk_batch* b, int64_t n_steps, int32_t plasticity_on) {
-  if (!b || n_steps < 0 || n_steps > 0x7fffffff) return SPK_ERR_INVALID;
-  if (n_steps == 0) return SPK_OK;
+int spk_batch_run_steps_each(spk_batch* b, const int64_t* n_steps, const int32_t* plasticity_on) {
+  if (!b || !n_steps) return SPK_ERR_INVALID;
+  int64_t most = 0;
+  for (size_t i = 0; i < b->nets.size(); ++i) {
+    if (n_steps[i] < 0 || n_steps[i] > 0x7fffffff) return SPK_ERR_INVALID;
+    most = std::max(most, n_steps[i]);
+  }
+  if (most == 0) return SPK_OK;
   // order the batch stream after each network's pending work
-  for (spk_net* n : b->nets) {
+  for (size_t i = 0; i < b->nets.size(); ++i) {
+    spk_net* n = b->nets[i];
     SPK_CUDA(cudaStreamSynchronize(n->stream));
-    set_ctl_kernel<<<1, 1, 0, b->stream>>>(n->hd.ctl, n->current_time, (int)n_steps,
-                                           (plasticity_on && n->has_stdp) ? 1 : 0, n->record_inputs ? 1 : 0);
+    const int plastic = (!plasticity_on || plasticity_on[i]) && n->has_stdp;
+    set_ctl_kernel<<<1, 1, 0, b->stream>>>(n->hd.ctl, n->current_time, (int)n_steps[i], plastic ? 1 : 0,
+                                           n->record_inputs ? 1 : 0);
     SPK_CUDA(cudaGetLastError());
   }
-  const int64_t blocks = (n_steps + b->K - 1) / b->K;
+  // networks that finish early leave their launches at once (no steps left)
+  const int64_t blocks = (most + b->K - 1) / b->K;
   for (int64_t blk = 0; blk < blocks; ++blk) {
     for (const auto& wv : b->waves) {
       cudaLaunchConfig_t cfg = {};
@@ -1587,11 +1670,46 @@ int spk_batch_run_steps(spk_batch* b, int64_t n_steps, int32_t plasticity_on) {
   }
   // each network's own stream (its readbacks and runs) waits for the batch
   SPK_CUDA(cudaEventRecord(b->done, b->stream));
-  for (spk_net* n : b->nets) {
+  for (size_t i = 0; i < b->nets.size(); ++i) {
+    spk_net* n = b->nets[i];
     SPK_CUDA(cudaStreamWaitEvent(n->stream, b->done, 0));
-    n->current_time = n->current_time + (float)n_steps * n->dt;
+    n->current_time = n->current_time + (float)n_steps[i] * n->dt;
   }
   return SPK_OK;
+}
+
+int spk_batch_step_block(spk_batch* b) {
+  if (!b) return SPK_ERR_INVALID;
+  // order the batch stream after each network's pending work (its run set-up)
+  for (spk_net* n : b->nets) SPK_CUDA(cudaStreamSynchronize(n->stream));
+  for (const auto& wv : b->waves) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(wv.ctas);
+    cfg.blockDim = dim3(b->W * 32);
+    cfg.dynamicSmemBytes = wv.smem;
+    cfg.stream = b->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = wv.cooperative ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    SPK_CUDA(cudaLaunchKernelEx(&cfg, step_kernel, (const NetDev*)b->dd, (const CtaMap*)(b->dmap + wv.first),
+                                b->K));
+    ++b->launches;
+  }
+  SPK_CUDA(cudaEventRecord(b->done, b->stream));
+  for (spk_net* n : b->nets) SPK_CUDA(cudaStreamWaitEvent(n->stream, b->done, 0));
+  return SPK_OK;
+}
+
+int spk_batch_run_steps(spk_batch* b, int64_t n_steps, int32_t plasticity_on) {
+  if (!b || n_steps < 0 || n_steps > 0x7fffffff) return SPK_ERR_INVALID;
+  if (n_steps == 0) return SPK_OK;
+  return guarded([&]() -> int {
+    std::vector<int64_t> each(b->nets.size(), n_steps);
+    std::vector<int32_t> plastic(b->nets.size(), plasticity_on ? 1 : 0);
+    return spk_batch_run_steps_each(b, each.data(), plastic.data());
+  });
 }
 
 int spk_batch_synchronize(spk_batch* b) {

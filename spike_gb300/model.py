@@ -519,3 +519,67 @@ def desc_arrays(d: N.NetDesc) -> dict:
     return dict(pre=arr(d.pre, np.int32), post=arr(d.post, np.int32), weight=arr(d.weight, np.float32),
                 scale=arr(d.scale, np.float32), delay=arr(d.delay, np.int32), label=arr(d.label, np.int32),
                 plastic=arr(d.plastic, np.uint8))
+
+
+class Server:
+    """Continuous-batching simulation server (spk_server_*): submit generated
+    networks with a step count; the server admits them by free device memory,
+    runs them together in step blocks and keeps each job's results."""
+
+    def __init__(self, warps_per_cta=0, tile_posts=0, steps_per_block=0, max_running=0, reserve_bytes=0,
+                 record_spikes=True):
+        o = N.ServerOpts(warps_per_cta, tile_posts, steps_per_block, max_running, reserve_bytes,
+                         1 if record_spikes else 0, 0)
+        self.h = C.c_void_p()
+        check(lib().spk_server_start(C.byref(o), C.byref(self.h)), "spk_server_start")
+        self._keep = {}
+
+    def submit(self, gen: "GenNetwork", steps: int, plasticity_on: bool = True) -> int:
+        j = C.c_int64()
+        check(lib().spk_server_submit(self.h, C.byref(gen.desc), steps, 1 if plasticity_on else 0, C.byref(j)),
+              "spk_server_submit")
+        return j.value
+
+    def poll(self, job: int) -> N.JobInfo:
+        info = N.JobInfo()
+        check(lib().spk_server_poll(self.h, job, C.byref(info)), "spk_server_poll")
+        return info
+
+    def wait(self, job: int, timeout_s: float = 600.0) -> N.JobInfo:
+        rc = lib().spk_server_wait(self.h, job, C.c_double(timeout_s))
+        if rc != N.SPK_OK:
+            raise N.SpikeError(rc, "spk_server_wait", "job did not finish in time" if rc == N.SPK_ERR_BUSY else "")
+        return self.poll(job)
+
+    def spikes(self, job: int):
+        info = self.poll(job)
+        n = int(info.spikes)
+        ids = np.empty(n, np.int32)
+        times = np.empty(n, np.float32)
+        got = C.c_int64()
+        check(lib().spk_server_read_spikes(self.h, job, ids.ctypes.data_as(C.POINTER(C.c_int32)),
+                                           times.ctypes.data_as(C.POINTER(C.c_float)), n, C.byref(got)),
+              "spk_server_read_spikes")
+        return ids[:got.value], times[:got.value]
+
+    def cancel(self, job: int):
+        check(lib().spk_server_cancel(self.h, job), "spk_server_cancel")
+
+    def release(self, job: int):
+        check(lib().spk_server_release(self.h, job), "spk_server_release")
+
+    def stats(self) -> N.ServerStats:
+        st = N.ServerStats()
+        check(lib().spk_server_stats_get(self.h, C.byref(st)), "spk_server_stats_get")
+        return st
+
+    def stop(self):
+        if self.h:
+            lib().spk_server_stop(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass

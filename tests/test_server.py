@@ -1,0 +1,65 @@
+"""The continuous-batching server (GPU): jobs submitted while others run are
+admitted, overlap on the device, and each job's result is bit for bit the
+result of the same network run alone."""
+import time
+
+import numpy as np
+import pytest
+
+from engine_checks import bits
+from spike_gb300 import Net, Server
+from spike_gb300 import _native as N
+from spike_gb300.networks import sweep_instance
+
+pytestmark = pytest.mark.gpu
+
+
+def jobs(k=8, seed=9):
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(400), np.log(5000), k)).astype(int)
+    out = []
+    for i in range(k):
+        gen = sweep_instance(int(sizes[i]), float(rng.uniform(0.02, 0.06)), float(rng.uniform(3, 7)), i % 3 == 0,
+                             seed=700 + i, d_max=8)
+        out.append((gen, int(rng.integers(300, 1500)), bool(i % 2 == 0)))
+    return out
+
+
+def test_served_jobs_equal_each_job_alone_and_overlap():
+    work = jobs()
+    srv = Server(steps_per_block=250, reserve_bytes=1 << 30)
+    ids = []
+    for i, (gen, steps, plastic) in enumerate(work):
+        ids.append(srv.submit(gen, steps, plastic))
+        if i == 3:
+            time.sleep(0.05)  # later jobs arrive while the first ones run
+    infos = [srv.wait(j, 300.0) for j in ids]
+    assert all(inf.state == N.SPK_JOB_DONE for inf in infos), [inf.state for inf in infos]
+    # work of different jobs overlapped on the device
+    assert any(b.start_s < a.finish_s and b.start_s > a.start_s for a in infos for b in infos)
+    st = srv.stats()
+    assert st.done == len(work) and st.blocks > 1
+    for (gen, steps, plastic), j, inf in zip(work, ids, infos):
+        ref = Net.generate(gen)
+        ref.run_steps(steps, plastic)
+        assert ref.synchronize() == 0
+        ri, rt = ref.spikes()
+        si, stt = srv.spikes(j)
+        assert inf.steps_done == steps and inf.synapses == ref.synapse_count()
+        np.testing.assert_array_equal(si, ri)
+        np.testing.assert_array_equal(bits(stt), bits(rt))
+        assert inf.events == ref.events()
+        ref.close()
+    srv.stop()
+
+
+def test_cancel_and_stop_with_work_queued():
+    work = jobs(k=5, seed=4)
+    srv = Server(steps_per_block=200, reserve_bytes=1 << 30)
+    ids = [srv.submit(gen, 50000, plastic) for gen, _, plastic in work]
+    srv.cancel(ids[-1])
+    time.sleep(0.2)
+    srv.cancel(ids[0])
+    info0 = srv.wait(ids[0], 120.0)
+    assert info0.state == N.SPK_JOB_CANCELLED and info0.steps_done < 50000
+    srv.stop()  # cancels the rest and frees every network
