@@ -58,7 +58,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="batched",
-                   choices=["batched", "brunel", "vogels_abbott", "plastic_ff"])
+                   choices=["batched", "brunel", "vogels_abbott", "plastic_ff", "served"])
+    p.add_argument("--duration", type=float, default=60.0, help="served: seconds of request arrivals")
+    p.add_argument("--arrival-rate", type=float, default=20.0, help="served: mean requests per second")
     p.add_argument("--instances", type=int, default=256, help="batched: network instances")
     p.add_argument("--tune-steps", type=int, default=100, help="batched: autotuner trial timesteps")
     p.add_argument("--plain-block", type=int, default=200,
@@ -73,7 +75,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     a = p.parse_args()
     if a.steps is None:
-        sim_s = {"batched": 1.0, "brunel": 2.0, "vogels_abbott": 1.0, "plastic_ff": 5.0}[a.workload]
+        sim_s = {"batched": 1.0, "brunel": 2.0, "vogels_abbott": 1.0, "plastic_ff": 5.0, "served": 0.1}[a.workload]
         a.steps = max(1, int(round(sim_s / (a.block * DT))))
     return a
 
@@ -230,6 +232,8 @@ def main():
         return run_reference(args, rank, world)
     if args.workload == "batched":
         return run_batched(args, rank, world, local)
+    if args.workload == "served":
+        return run_served(args, rank, world, local)
 
     import torch
     torch.cuda.set_device(local)
@@ -619,6 +623,84 @@ def run_batched(args, rank, world, local):
     b.close()
     if dist:
         dist.destroy_process_group()
+
+
+# ---- served stream ------------------------------------------------------------------
+
+def served_requests(duration, rate, seed=2024):
+    """Poisson arrivals (mean `rate` per second) of jobs with N log-uniform in
+    [2k, 100k], simulated time U[0.5, 5] s, 30 % with STDP, other draws as in
+    the batched sweep; fixed arrival seed."""
+    import numpy as np
+    from spike_gb300.networks import sweep_instance
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            break
+        n = int(np.exp(rng.uniform(np.log(2000), np.log(100000))))
+        p, g = float(rng.uniform(0.01, 0.05)), float(rng.uniform(3.0, 7.0))
+        plastic = bool(rng.uniform() < 0.3)
+        sim = float(rng.uniform(0.5, 5.0))
+        out.append((t, sweep_instance(n, p, g, plastic, seed=int(rng.integers(1, 2**31))), int(round(sim / DT))))
+    return out
+
+
+def run_served(args, rank, world, local):
+    """Requests arrive by a Poisson process for --duration seconds and are
+    submitted to the continuous-batching server.  value = synaptic events the
+    server delivered during the arrival window (all jobs, finished or
+    running) / window; latency percentiles are over the jobs that finished
+    inside the window (submit to finish).  When the window closes the server
+    stops: jobs still queued or running are cancelled."""
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    import __graft_entry__
+    __graft_entry__.build()
+    from spike_gb300 import Server
+    from spike_gb300 import _native as N
+    if rank != 0:
+        return
+    reqs = served_requests(args.duration, args.arrival_rate)
+    srv = Server(steps_per_block=args.block, record_spikes=False)
+    ids = []
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for (t, gen, steps) in reqs:
+            wait = t - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            ids.append(srv.submit(gen, steps, True))
+        rest = args.duration - (time.perf_counter() - t0)
+        if rest > 0:
+            time.sleep(rest)
+        window = time.perf_counter() - t0
+        st = srv.stats()
+        infos = [srv.poll(j) for j in ids]
+    srv.stop()
+    lat = [i.finish_s - i.submit_s for i in infos if i.state == N.SPK_JOB_DONE]
+    wait_s = [i.start_s - i.submit_s for i in infos if i.state in (N.SPK_JOB_DONE, N.SPK_JOB_RUNNING)]
+    sim_done = sum(i.steps_done for i in infos) * DT
+    line = {"metric": "synaptic_events_per_s", "value": float(st.events) / window, "unit": "events/s",
+            "n_gpus": 1, "steps": len(ids), "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "ours",
+            "config": {"workload": f"served_stream_rate{args.arrival_rate:g}_N2k-100k_T0.5-5s_stdp30pct",
+                       "arrival_window_s": args.duration, "block_timesteps": args.block},
+            "sim_s_per_wall_s": sim_done / window,
+            "latency_s": {"p50": float(np.percentile(lat, 50)) if lat else None,
+                          "p99": float(np.percentile(lat, 99)) if lat else None, "n": len(lat)},
+            "admission_wait_s": {"p50": float(np.percentile(wait_s, 50)) if wait_s else None,
+                                 "p99": float(np.percentile(wait_s, 99)) if wait_s else None},
+            "jobs": {"submitted": len(ids),
+                     "done": int(sum(1 for i in infos if i.state == N.SPK_JOB_DONE)),
+                     "running_at_close": int(sum(1 for i in infos if i.state == N.SPK_JOB_RUNNING)),
+                     "queued_at_close": int(sum(1 for i in infos if i.state == N.SPK_JOB_QUEUED)),
+                     "failed": int(sum(1 for i in infos if i.state == N.SPK_JOB_FAILED)),
+                     "blocks": int(st.blocks), "gpu_busy_s": st.busy_s},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

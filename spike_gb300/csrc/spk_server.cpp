@@ -63,7 +63,8 @@ struct Job {
   double submit_s = 0, start_s = -1, finish_s = -1;
   int64_t bytes = 0, peak_bytes = 0;
   spk_net* net = nullptr;
-  uint64_t events = 0;
+  uint64_t events = 0;       // delivered so far (updated after every block)
+  uint64_t events_seen = 0;  // part of `events` already counted in the server's total
   int64_t spikes = 0, synapses = 0;
   std::vector<int32_t> ids;
   std::vector<float> times;
@@ -187,6 +188,7 @@ void finish(spk_server* S, Job* j, int status) {
   spk_net_destroy(j->net);
   std::lock_guard<std::mutex> lk(S->mu);
   j->net = nullptr;
+  j->events_seen = j->events;
   j->events = ev;
   j->spikes = n;
   j->ids.swap(ids);
@@ -200,7 +202,8 @@ void finish(spk_server* S, Job* j, int status) {
     if (j->state == SPK_JOB_DONE) S->st.done++;
   }
   j->finish_s = S->now();
-  S->st.events += ev;
+  S->st.events += ev - std::min(ev, j->events_seen);
+  j->events_seen = ev;
   S->cv.notify_all();
 }
 
@@ -246,6 +249,15 @@ void loop(spk_server* S) {
       S->st.blocks++;
       S->st.busy_s += S->now() - tb;
       for (size_t i = 0; i < run.size(); ++i) run[i]->steps_done += steps[i];
+    }
+    // delivered events of every running job so far
+    for (Job* j : run) {
+      uint64_t ev = 0;
+      if (spk_net_synaptic_events(j->net, &ev) == SPK_OK) {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->st.events += ev - j->events;
+        j->events = ev;
+      }
     }
     std::vector<Job*> keep;
     for (Job* j : run) {
