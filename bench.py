@@ -63,6 +63,8 @@ def parse():
     p.add_argument("--arrival-rate", type=float, default=20.0, help="served: mean requests per second")
     p.add_argument("--instances", type=int, default=256, help="batched: network instances")
     p.add_argument("--tune-steps", type=int, default=100, help="batched: autotuner trial timesteps")
+    p.add_argument("--no-tune", action="store_true",
+                   help="batched: skip the autotuner (8 warps, tiles of up to 64 posts, costs from synapse counts)")
     p.add_argument("--plain-block", type=int, default=200,
                    help="batched: timesteps each instance runs alone for the plain comparison")
     p.add_argument("--block", type=int, default=1000, help="timesteps per bench step")
@@ -94,18 +96,24 @@ def build_model(workload: str):
                "dt_ms": 0.1, "sim_s_per_config": 1.0, "plasticity": False}
         L = 2
     else:
-        m = networks.plastic_ff()
-        cfg = {"workload": "plastic_ff_200000_lif_50000_poisson_stdp", "neurons": 200000, "inputs": 50000,
-               "dt_ms": 0.1, "sim_s_per_config": 5.0, "plasticity": True}
+        m = networks.plastic_ff_generated()
+        cfg = {"workload": "plastic_ff_200000_lif_50000_lognormal_poisson_stdp", "neurons": 200000,
+               "inputs": 50000, "in_degree": "binomial, mean 900 input + 100 recurrent", "delays_steps": [1, 10],
+               "dt_ms": 0.1, "sim_s_per_config": 5.0, "plasticity": True, "connectivity": "drawn on the GPU"}
         L = 1
     return m, cfg, L
 
 
-def algorithmic_bytes(events: int, plastic_events: int, neuron_steps: int, input_steps: int, L: int) -> int:
+def algorithmic_bytes(events: int, pre_updates: int, post_updates: int, neuron_steps: int, input_steps: int,
+                      L: int, trace_steps: int = 0) -> int:
     """Per-unit algorithmic HBM bytes of the step: 8 B per synaptic event
-    (int32 post + fp32 weight), +4 B per plastic event (weight write-back),
-    12 + 16 L B per neuron-step, 8 B per input-step."""
-    return 8 * events + 4 * plastic_events + (12 + 16 * L) * neuron_steps + 8 * input_steps
+    (packed post/delay/label + fp32 weight), 8 B per plastic weight updated on
+    a presynaptic event (weight read and write-back), 16 B per plastic
+    afferent updated on a postsynaptic spike (afferent record + weight
+    write-back + presynaptic trace), 12 + 16 L B per neuron-step, 8 B per
+    input-step, 4 B per presynaptic trace published in a plastic run."""
+    return (8 * events + 8 * pre_updates + 16 * post_updates + (12 + 16 * L) * neuron_steps + 8 * input_steps
+            + 4 * trace_steps)
 
 
 class ClockSampler:
@@ -182,6 +190,11 @@ def traffic_per_launch(workload: str):
         return None
 
 
+def networks_small_plastic_ff():
+    from spike_gb300 import networks
+    return networks.plastic_ff_generated(n_in=2500, n_neurons=10000, ff=900, rec=100)
+
+
 def cpu_baseline(desc, steps: int, threads: int):
     from oracle import OracleNet
     o = OracleNet(desc, 32, threads=threads)
@@ -196,9 +209,16 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     m, cfg, L = build_model(args.workload)
-    desc = m.desc()
     threads = os.cpu_count() or 1
     from oracle import OracleNet
+    from spike_gb300 import GenNetwork
+    if isinstance(m, GenNetwork):
+        # too large to draw on the host: the same construction at 1/20 size
+        dd = oracle_instance(networks_small_plastic_ff())[1]
+        desc = dd.desc
+        cfg = {**cfg, "cpu_sample_network": "same construction at 1/20 size (2,500 inputs, 10,000 neurons)"}
+    else:
+        desc = m.desc()
     o = OracleNet(desc, 32, threads=threads)
     sample = max(1, min(args.block, 1000))
     for _ in range(args.warmup):
@@ -246,11 +266,18 @@ def main():
     __graft_entry__.build()
     from spike_gb300 import schedule
 
+    from spike_gb300 import GenNetwork, Net
     m, cfg, L = build_model(args.workload)
-    desc = m.desc()
     sched = schedule(args.warps, args.tile, args.ctas, args.launch_steps or args.block)
-    net = m.finalise(sched)
-    n_neurons, n_inputs, n_syn = m.counts()
+    if isinstance(m, GenNetwork):
+        net = Net.generate(m, sched)
+        n_neurons, n_inputs, n_syn = m.desc.n_neurons, m.desc.n_inputs, net.synapse_count()
+        desc = None
+    else:
+        desc = m.desc()
+        net = m.finalise(sched)
+        n_neurons, n_inputs, n_syn = m.counts()
+    plastic_run = args.workload == "plastic_ff"
     stream = torch.cuda.ExternalStream(net.stream())
 
     def barrier():
@@ -265,6 +292,7 @@ def main():
     net.clear_spikes()
     barrier()
     e0, l0 = net.events(), net.launches()
+    pre0, post0 = net.stdp_counts()
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         barrier()
@@ -278,6 +306,7 @@ def main():
     ms = start.elapsed_time(stop)
     events = net.events() - e0
     launches = net.launches() - l0
+    pre1, post1 = net.stdp_counts()
     el = torch.tensor([ms / 1000.0], device="cuda")
     ev = torch.tensor([float(events)], device="cuda", dtype=torch.float64)
     if dist:
@@ -290,7 +319,8 @@ def main():
 
     # ---- roofline of the step kernel ----------------------------------------------------
     timesteps = args.steps * args.block
-    alg = algorithmic_bytes(events, 0, n_neurons * timesteps, n_inputs * timesteps, L)
+    alg = algorithmic_bytes(events, pre1 - pre0, post1 - post0, n_neurons * timesteps, n_inputs * timesteps, L,
+                            (n_neurons + n_inputs) * timesteps if plastic_run else 0)
     per_launch_s = (ms / 1000.0) / max(launches, 1)
     per_launch_bytes = alg / max(launches, 1)
     peak, peak_kind = peaks()
@@ -305,8 +335,8 @@ def main():
     if not args.no_e2e:
         rates = torch.full((max(n_inputs, 1),), 20.0, dtype=torch.float32).pin_memory()
         if n_inputs and args.workload == "plastic_ff":
-            from spike_gb300 import networks
-            rates.copy_(torch.from_numpy(networks.lognormal_rates(n_inputs)))
+            import numpy as np
+            rates.copy_(torch.from_numpy(np.ctypeslib.as_array(m.desc.input_rates, (n_inputs,)).copy()))
         h2d = 4 * n_inputs
         d2h = 0
         net.clear_spikes()
@@ -327,10 +357,19 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cv, cel = cpu_baseline(desc, args.cpu_sample_steps, 1)
-        cpu = {"value": cv, "unit": "events/s", "cores": 1, "kind": "port",
-               "sample": f"{args.cpu_sample_steps} timesteps ({args.cpu_sample_steps * DT:.2f} s simulated) "
-                         f"from reset, {cel:.1f} s of CPU"}
+        if desc is None:
+            # the generated network is too large to draw on the host: a
+            # 1/20-size network of the same construction stands in
+            cs = CpuSample([networks_small_plastic_ff()])
+            cv, cel = cs.run(args.cpu_sample_steps // 10, parallel=False)
+            cpu = {"value": cv, "unit": "events/s", "cores": 1, "kind": "port",
+                   "sample": f"the same construction at 1/20 size (2,500 inputs, 10,000 neurons), "
+                             f"{args.cpu_sample_steps // 10} timesteps from reset, {cel:.1f} s of CPU"}
+        else:
+            cv, cel = cpu_baseline(desc, args.cpu_sample_steps, 1)
+            cpu = {"value": cv, "unit": "events/s", "cores": 1, "kind": "port",
+                   "sample": f"{args.cpu_sample_steps} timesteps ({args.cpu_sample_steps * DT:.2f} s simulated) "
+                             f"from reset, {cel:.1f} s of CPU"}
 
     if rank == 0:
         line = {
@@ -339,7 +378,8 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "ours",
             "config": {**cfg, "block_timesteps": args.block, "synapses": n_syn,
-                       "schedule": net.schedule(), "l2": "synapse entries 225 MB > 129 MB L2 (no flush)",
+                       "schedule": net.schedule(),
+                       "l2": f"synapse entries {8 * n_syn / 1e6:.0f} MB > 129 MB L2 (no flush)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "sim_s_per_wall_s": sim_s * world / (elapsed * world) if world else None,
             "status": status,
@@ -489,9 +529,16 @@ def run_batched(args, rank, world, local):
 
     gens = networks.batched_sweep(args.instances)
     t0 = time.perf_counter()
-    scheds, tune_ms, costs = Batch.autotune(gens, trial_steps=args.tune_steps, costs=True)
+    if args.no_tune:
+        from spike_gb300 import schedule
+        scheds = [schedule(8, min(64, max(32, -(-(-(-g.desc.n_neurons // 8)) // 32) * 32)), 0, 0) for g in gens]
+        tune_ms = None
+        nets = [Net.generate(g, s) for g, s in zip(gens, scheds)]
+        costs = [float(n.synapse_count()) * (2.0 if g.desc.has_stdp else 1.0) for n, g in zip(nets, gens)]
+    else:
+        scheds, tune_ms, costs = Batch.autotune(gens, trial_steps=args.tune_steps, costs=True)
+        nets = [Net.generate(g, s) for g, s in zip(gens, scheds)]
     tune_s = time.perf_counter() - t0
-    nets = [Net.generate(g, s) for g, s in zip(gens, scheds)]
     for n, c in zip(nets, costs):
         n.set_step_cost(c)
     n_syn = sum(n.synapse_count() for n in nets)
@@ -508,6 +555,7 @@ def run_batched(args, rank, world, local):
     barrier()
     e0 = sum(n.events() for n in nets)
     l0 = b.launches()
+    st0 = [n.stdp_counts() for n in nets]
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         barrier()
@@ -532,7 +580,12 @@ def run_batched(args, rank, world, local):
 
     # roofline: algorithmic bytes of all instances over the step-kernel launches
     timesteps = args.steps * args.block
-    alg = algorithmic_bytes(events, 0, n_neurons * timesteps, n_inputs * timesteps, 1)
+    st1 = [n.stdp_counts() for n in nets]
+    pre_u = sum(b1[0] - a1[0] for a1, b1 in zip(st0, st1))
+    post_u = sum(b1[1] - a1[1] for a1, b1 in zip(st0, st1))
+    trace_keys = sum(g.desc.n_neurons + g.desc.n_inputs for g in gens if g.desc.has_stdp)
+    alg = algorithmic_bytes(events, pre_u, post_u, n_neurons * timesteps, n_inputs * timesteps, 1,
+                            trace_keys * timesteps)
     per_launch_s = (ms / 1000.0) / max(launches, 1)
     per_launch_bytes = alg / max(launches, 1)
     peak, peak_kind = peaks()
@@ -606,10 +659,11 @@ def run_batched(args, rank, world, local):
             "config": {**batched_config(gens, n_syn), "block_timesteps": args.block,
                        "schedules": sch, "autotune_s": round(tune_s, 2), "autotune_trial_ms": tune_ms,
                        "waves_per_block": launches / max(1, args.steps * -(-args.block // 1000)),
-                       "plain_step_us_alone_sum": round(sum(costs), 1),
+                       "autotuned": not args.no_tune,
                        "l2": f"synapse entries {8 * n_syn / 1e9:.1f} GB > 129 MB L2 (no flush)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "sim_s_per_wall_s": len(nets) * sim_s / elapsed,
+            "stdp_updates": {"pre": pre_u, "post_afferents": post_u},
             "plain": plain, "batched_over_plain": value / plain["value"],
             "status": status,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -208,6 +208,10 @@ int spk_net_write_weights(spk_net* net, const float* weights, int64_t n);
 /* Synaptic events delivered so far: sum over spikes of the spiking neuron's
  * out-degree. */
 int spk_net_synaptic_events(spk_net* net, uint64_t* events);
+/* STDP work done so far: plastic weights updated on a presynaptic event
+ * (propagation pass) and plastic afferents updated on a postsynaptic spike
+ * (afferent pass); for byte accounting. */
+int spk_net_stdp_counts(spk_net* net, uint64_t* pre_updates, uint64_t* post_updates);
 int spk_net_get_schedule(const spk_net* net, spk_schedule* out);
 int spk_net_device_bytes(const spk_net* net, int64_t* bytes);
 /* Kernel launches issued so far by this handle. */
@@ -436,7 +440,7 @@ int spk_net_generate_estimate(const spk_gen_desc* desc, const spk_schedule* sche
  * and must be serialized by the caller.  Networks whose scratch exceeds
  * SPK_NOALLOC_SCRATCH_BYTES are rejected with SPK_ERR_INVALID. */
 #define SPK_NOALLOC_SCRATCH_BYTES (4u << 20)
-#define SPK_RUN_STATE_BYTES 64
+#define SPK_RUN_STATE_BYTES 128
 
 typedef struct spk_device_net {
   /* shape, schedule and constants (host values) */

@@ -158,7 +158,7 @@ class DeviceNet(C.Structure):
 
 
 SPK_NOALLOC_SCRATCH_BYTES = 4 << 20
-SPK_RUN_STATE_BYTES = 64
+SPK_RUN_STATE_BYTES = 128
 
 _VP = C.c_void_p
 _SIGS = {
@@ -182,6 +182,7 @@ _SIGS = {
     "spk_net_read_weights": (i32, [_VP, P(f32), i64]),
     "spk_net_write_weights": (i32, [_VP, P(f32), i64]),
     "spk_net_synaptic_events": (i32, [_VP, P(u64)]),
+    "spk_net_stdp_counts": (i32, [_VP, P(u64), P(u64)]),
     "spk_net_get_schedule": (i32, [_VP, P(Schedule)]),
     "spk_net_device_bytes": (i32, [_VP, P(i64)]),
     "spk_net_launch_count": (i32, [_VP, P(i64)]),

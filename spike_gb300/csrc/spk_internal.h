@@ -45,6 +45,8 @@ struct RunCtl {
   unsigned long long events;       // synaptic events delivered
   int status;           // 0 or SPK_ERR_* raised on the device
   int pad;
+  unsigned long long stdp_pre;     // plastic weights updated on a presynaptic event
+  unsigned long long stdp_post;    // plastic afferents updated on a postsynaptic spike
 };
 
 // Everything one CTA needs to run its share of one network.

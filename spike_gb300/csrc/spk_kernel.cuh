@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(512, 1)
     rowe_s[i] = __ldg(d.rowptr + (size_t)(key + 1) * n_tiles);
   }
   unsigned long long spike_count = ctl0.spike_count;
-  unsigned long long ev = 0;
+  unsigned long long ev = 0, n_pre = 0, n_post = 0;  // events, STDP pre updates, STDP post afferents
   bool inputs_active = ctl0.inputs_active != 0;
   int steps_done = 0;
   bool ok_run = true;
@@ -582,6 +582,7 @@ __global__ void __launch_bounds__(512, 1)
                     if (P || post_ev) {
                       v = stdp_update(d, v, P, post_ev, post_s[q], kpre[j]);
                       d.csc[en.y].y = __float_as_uint(v);
+                      ++n_pre;
                     }
                   }
                   contrib = v * s_scale[c];
@@ -835,6 +836,7 @@ __global__ void __launch_bounds__(512, 1)
           if (ai >= a1 || ((vm[u] >> (pk & 31)) & 1u)) continue;  // pre event: done in the pre pass
           const float nw = stdp_update(d, __uint_as_float(cc[u].y), false, true, post_tr, prt[u]);
           d.csc[ai].y = __float_as_uint(nw);
+          ++n_post;
         }
       };
       __syncthreads();
@@ -915,6 +917,16 @@ __global__ void __launch_bounds__(512, 1)
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) e += __shfl_xor_sync(FULL, e, o);
     if (lane == 0 && e) atomicAdd(&d.ctl->events, e);
+    if (d.has_stdp) {
+      unsigned long long a = n_pre, b = n_post;
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        a += __shfl_xor_sync(FULL, a, o);
+        b += __shfl_xor_sync(FULL, b, o);
+      }
+      if (lane == 0 && a) atomicAdd(&d.ctl->stdp_pre, a);
+      if (lane == 0 && b) atomicAdd(&d.ctl->stdp_post, b);
+    }
   }
   if (cm.rank == 0 && w == W - 1) {
     if (lane == 0) {

@@ -1480,6 +1480,16 @@ int spk_net_synaptic_events(spk_net* n, uint64_t* events) {
   return SPK_OK;
 }
 
+int spk_net_stdp_counts(spk_net* n, uint64_t* pre_updates, uint64_t* post_updates) {
+  if (!n) return SPK_ERR_INVALID;
+  SPK_CUDA(cudaStreamSynchronize(n->stream));
+  RunCtl c;
+  SPK_CUDA(cudaMemcpy(&c, n->hd.ctl, sizeof(c), cudaMemcpyDeviceToHost));
+  if (pre_updates) *pre_updates = c.stdp_pre;
+  if (post_updates) *post_updates = c.stdp_post;
+  return SPK_OK;
+}
+
 int spk_net_get_schedule(const spk_net* n, spk_schedule* out) {
   if (!n || !out) return SPK_ERR_INVALID;
   out->warps_per_cta = n->plan.W;

@@ -223,6 +223,13 @@ class Net:
         check(lib().spk_net_synaptic_events(self.h, C.byref(e)), "spk_net_synaptic_events")
         return e.value
 
+    def stdp_counts(self) -> tuple:
+        """(plastic weights updated on presynaptic events, plastic afferents
+        updated on postsynaptic spikes) so far."""
+        a, b = C.c_uint64(), C.c_uint64()
+        check(lib().spk_net_stdp_counts(self.h, C.byref(a), C.byref(b)), "spk_net_stdp_counts")
+        return a.value, b.value
+
     def schedule(self) -> dict:
         s = N.Schedule()
         check(lib().spk_net_get_schedule(self.h, C.byref(s)), "spk_net_get_schedule")
