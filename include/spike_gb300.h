@@ -213,6 +213,27 @@ int spk_net_synaptic_events(spk_net* net, uint64_t* events);
  * (afferent pass); for byte accounting. */
 int spk_net_stdp_counts(spk_net* net, uint64_t* pre_updates, uint64_t* post_updates);
 int spk_net_get_schedule(const spk_net* net, spk_schedule* out);
+/* Snapshot of a network's dynamic state (no counterpart in the reference,
+ * which saves weights and connectivity only): membrane potentials, last spike
+ * times, synaptic traces, the delay ring, Poisson next-spike times, STDP
+ * traces and plastic weights, the run counters and the current time.  It
+ * restores into a network created from the same descriptor with the same
+ * schedule (checked); the spike store is not saved (it restarts empty).  The
+ * state holds no random-generator state: draws are keyed by (seed, neuron,
+ * step). */
+int spk_net_snapshot_bytes(spk_net* net, int64_t* bytes);
+int spk_net_snapshot(spk_net* net, void* buffer, int64_t bytes);
+int spk_net_restore(spk_net* net, const void* buffer, int64_t bytes);
+/* Limit of every device-side wait of one CTA on another (default 4 s).  A
+ * wait that runs out ends the run with SPK_ERR_TIMEOUT, returned by
+ * spk_net_synchronize; the network is usable again after
+ * spk_net_reset_state, which clears the failure. */
+int spk_net_set_wait_limit(spk_net* net, double seconds);
+/* Failure injection for testing (no counterpart in the reference, which has
+ * no failure detection): the next launch of the network leaves out CTA
+ * `rank`, so the other CTAs' bounded waits on it run out.  The fault is made
+ * on the host (a CTA that never runs); nothing on the device faults. */
+int spk_net_inject_withheld_cta(spk_net* net, int32_t rank);
 int spk_net_device_bytes(const spk_net* net, int64_t* bytes);
 /* Kernel launches issued so far by this handle. */
 int spk_net_launch_count(const spk_net* net, int64_t* launches);

@@ -184,6 +184,11 @@ _SIGS = {
     "spk_net_synaptic_events": (i32, [_VP, P(u64)]),
     "spk_net_stdp_counts": (i32, [_VP, P(u64), P(u64)]),
     "spk_net_get_schedule": (i32, [_VP, P(Schedule)]),
+    "spk_net_set_wait_limit": (i32, [_VP, C.c_double]),
+    "spk_net_snapshot_bytes": (i32, [_VP, P(i64)]),
+    "spk_net_snapshot": (i32, [_VP, _VP, i64]),
+    "spk_net_restore": (i32, [_VP, _VP, i64]),
+    "spk_net_inject_withheld_cta": (i32, [_VP, i32]),
     "spk_net_device_bytes": (i32, [_VP, P(i64)]),
     "spk_net_launch_count": (i32, [_VP, P(i64)]),
     "spk_net_stream": (i32, [_VP, P(_VP)]),

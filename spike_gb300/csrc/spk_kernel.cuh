@@ -39,7 +39,6 @@
 namespace spk {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr unsigned long long POLL_TIMEOUT_NS = 4000000000ull;  // 4 s
 
 __device__ __forceinline__ unsigned long long globaltimer() {
   unsigned long long t;
@@ -98,7 +97,7 @@ __device__ __forceinline__ unsigned long long repoll(const unsigned long long* p
     if (t0 == 0ull) t0 = now;
     if (ld_volatile(d.abort_flag)) {
       ok = false;
-    } else if (now - t0 > POLL_TIMEOUT_NS) {
+    } else if (now - t0 > d.poll_ns) {
       atomicExch(d.abort_flag, 1);
       atomicCAS(&d.ctl->status, 0, SPK_ERR_TIMEOUT);
       ok = false;
@@ -483,36 +482,36 @@ __global__ void __launch_bounds__(512, 1)
           }
         for (int kb = 0; kb < n_round; kb += STAGE_KEYS) {
           const int nk = min(STAGE_KEYS, n_round - kb);
-          {
-            // all row-pointer loads of the round are independent: issue them together
+          // row pointers of the round's keys straight into shared memory
+          // (cp.async: every load of the round in flight at once)
+          for (int i = lane; i < nk; i += 32) {
+            const uint32_t lv = list[kb + i];
+            const int* rp = d.rowptr + (size_t)(lv & 0x3fffffffu) * n_tiles + t_idx;
+            cp_async4(kst + i, rp);
+            cp_async4(koff + i, rp + 1);
+            kfl[i] = lv;
+          }
+          if (stdp_run) {
+            // this step's presynaptic traces, written by other CTAs: L2 loads
             constexpr int KPL = STAGE_KEYS / 32;
-            int rp0[KPL], rp1[KPL];
-            uint32_t lvs[KPL];
             float prs[KPL];
 #pragma unroll
             for (int u = 0; u < KPL; ++u) {
-              // out-of-range lanes read key 0's pointers (always valid) so all
-              // loads are issued unconditionally
               const int i = u * 32 + lane;
-              lvs[u] = i < nk ? list[kb + i] : 0u;
-              const int key = (int)(lvs[u] & 0x3fffffffu);
-              const int* rp = d.rowptr + (size_t)key * n_tiles + t_idx;
-              rp0[u] = __ldg(rp);
-              rp1[u] = __ldg(rp + 1);
-              prs[u] = stdp_run ? __ldcg(pub + key) : 0.0f;
+              prs[u] = i < nk ? __ldcg(pub + (list[kb + i] & 0x3fffffffu)) : 0.0f;
             }
 #pragma unroll
             for (int u = 0; u < KPL; ++u) {
               const int i = u * 32 + lane;
-              if (i < nk) {
-                const int len = rp1[u] - rp0[u];
-                kst[i] = rp0[u];
-                koff[i] = len;
-                kfl[i] = lvs[u];
-                kpre[i] = prs[u];
-                if (lvs[u] >> 31) ev += (unsigned long long)len;
-              }
+              if (i < nk) kpre[i] = prs[u];
             }
+          }
+          cp_async_wait_all();
+          __syncwarp();
+          for (int i = lane; i < nk; i += 32) {
+            const int len = koff[i] - kst[i];
+            koff[i] = len;
+            if (kfl[i] >> 31) ev += (unsigned long long)len;
           }
           __syncwarp();
           // exclusive prefix of the sub-row lengths
@@ -683,8 +682,8 @@ __global__ void __launch_bounds__(512, 1)
         if (!__any_sync(FULL, pending)) break;
         const unsigned long long now = globaltimer();
         if (t0 == 0ull) t0 = now;
-        if (now - t0 > POLL_TIMEOUT_NS || ld_volatile(d.abort_flag)) {
-          if (lane == 0 && now - t0 > POLL_TIMEOUT_NS) {
+        if (now - t0 > d.poll_ns || ld_volatile(d.abort_flag)) {
+          if (lane == 0 && now - t0 > d.poll_ns) {
             atomicExch(d.abort_flag, 1);
             atomicCAS(&d.ctl->status, 0, SPK_ERR_TIMEOUT);
           }

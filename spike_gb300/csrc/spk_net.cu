@@ -47,6 +47,7 @@ void set_error(const char* fmt, ...) {
 
 
 constexpr int DEFAULT_STEPS_PER_LAUNCH = 1000;
+constexpr unsigned long long DEFAULT_WAIT_LIMIT_NS = 4000000000ull;  // 4 s
 constexpr int64_t DEFAULT_SPIKE_CAPACITY = 1 << 24;
 
 static __global__ void set_ctl_kernel(RunCtl* ctl, float start, int steps_total, int plastic,
@@ -194,6 +195,7 @@ struct spk_net {
   float current_time = 0.0f;
   int pending_status = SPK_OK;
   bool generated = false;  // connectivity drawn on the device (no host synapse arrays)
+  int withhold = -1;       // fault injection: CTA rank left out of the next launch
   int64_t n_csc = 0;       // plastic afferent records
   float step_cost = 0.0f;  // measured or estimated time of one step alone (batch packing)
 };
@@ -246,6 +248,12 @@ static int upload_state_defaults(spk_net* n) {
     SPK_CUDA(cudaMemsetAsync(h.pre_trace, 0, sizeof(float) * h.n_keys, n->stream));
     SPK_CUDA(cudaMemsetAsync(h.pre_pub, 0, sizeof(float) * 2 * (size_t)h.n_keys, n->stream));
   }
+  // a run that ended on a timeout leaves the abort flag, the status and the
+  // aborted step's exchange words behind: clear them
+  SPK_CUDA(cudaMemsetAsync(n->abort_dev, 0, sizeof(int), n->stream));
+  SPK_CUDA(cudaMemsetAsync(&h.ctl->status, 0, sizeof(int), n->stream));
+  SPK_CUDA(cudaMemsetAsync(h.cta_stamp, 0, sizeof(unsigned long long) * 2 * (size_t)h.nctas, n->stream));
+  SPK_CUDA(cudaMemsetAsync(h.cta_keys, 0, sizeof(unsigned long long) * 2 * (size_t)h.nctas * h.key_cap, n->stream));
   if (n->Nin > 0) {
     reset_inputs_kernel<<<(n->Nin + 255) / 256, 256, 0, n->stream>>>(n->dd, n->rates_dev + (size_t)n->stim * n->Nin, n->Nin);
     SPK_CUDA(cudaGetLastError());
@@ -304,6 +312,26 @@ static int run_steps_impl(spk_net* n, int64_t steps, int plastic, float start) {
   SPK_CUDA(cudaGetLastError());
   const int64_t blocks = (steps + n->plan.K - 1) / n->plan.K;
   for (int64_t b = 0; b < blocks; ++b) {
+    if (n->withhold >= 0) {
+      // the launch leaves one CTA out: the others' waits on it run out
+      std::vector<CtaMap> map;
+      for (int r = 0; r < n->plan.nctas; ++r)
+        if (r != n->withhold) map.push_back(CtaMap{0, r});
+      n->withhold = -1;
+      SPK_CUDA(cudaMemcpyAsync(n->dmap, map.data(), sizeof(CtaMap) * map.size(), cudaMemcpyHostToDevice, n->stream));
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)map.size());
+      cfg.blockDim = dim3(n->plan.W * 32);
+      cfg.dynamicSmemBytes = n->plan.smem;
+      cfg.stream = n->stream;
+      SPK_CUDA(cudaLaunchKernelEx(&cfg, step_kernel, (const NetDev*)n->dd, (const CtaMap*)n->dmap, n->plan.K));
+      SPK_CUDA(cudaStreamSynchronize(n->stream));
+      map.clear();
+      for (int r = 0; r < n->plan.nctas; ++r) map.push_back(CtaMap{0, r});
+      SPK_CUDA(cudaMemcpy(n->dmap, map.data(), sizeof(CtaMap) * map.size(), cudaMemcpyHostToDevice));
+      ++n->launches;
+      continue;
+    }
     if (n->graph) {
       SPK_CUDA(cudaGraphLaunch(n->graph, n->stream));
     } else {
@@ -605,6 +633,7 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   h.spike_cap = spike_cap;
   h.ctl = (RunCtl*)p_ctl;
   h.abort_flag = (int*)p_abort;
+  h.poll_ns = DEFAULT_WAIT_LIMIT_NS;
   n->abort_dev = (int*)p_abort;
   n->dd = (NetDev*)p_dd;
   n->dmap = (CtaMap*)p_map;
@@ -1190,6 +1219,154 @@ int spk_net_generate_estimate(const spk_gen_desc* d, const spk_schedule* sched, 
     if (peak_bytes) *peak_bytes = (int64_t)(arena + temp);
     return SPK_OK;
   });
+}
+
+// ---- snapshot / restore of the dynamic state ------------------------------------------
+namespace {
+struct SnapHeader {
+  uint32_t magic, version;
+  int32_t N, Nin, L, B, n_tiles, TS, ITS, KL, n_keys, nctas, has_stdp, stim;
+  int64_t S, n_csc;
+  float current_time;
+  int32_t pad;
+  RunCtl ctl;
+};
+constexpr uint32_t SNAP_MAGIC = 0x53504b53u;  // "SPKS"
+
+struct SnapPart {
+  void* dev;
+  size_t bytes;
+};
+
+std::vector<SnapPart> snap_parts(spk_net* n) {
+  const NetDev& h = n->hd;
+  std::vector<SnapPart> p = {
+      {h.V, sizeof(float) * n->N},
+      {h.last, sizeof(float) * n->N},
+      {h.gtr, sizeof(float) * (size_t)n->N * n->L},
+      {h.ring, sizeof(float) * (size_t)h.n_tiles * h.B * h.TS * h.L},
+      {h.in_next, sizeof(float) * (size_t)n->Nin},
+  };
+  if (n->has_stdp) {
+    p.push_back({h.post_trace, sizeof(float) * n->N});
+    p.push_back({h.pre_trace, sizeof(float) * (size_t)h.n_keys});
+    p.push_back({h.csc, sizeof(uint2) * (size_t)n->n_csc});
+  }
+  return p;
+}
+}  // namespace
+
+int spk_net_snapshot_bytes(spk_net* n, int64_t* bytes) {
+  if (!n || !bytes) return SPK_ERR_INVALID;
+  return guarded([&]() -> int {
+    size_t b = sizeof(SnapHeader);
+    for (const auto& p : snap_parts(n)) b += p.bytes;
+    *bytes = (int64_t)b;
+    return SPK_OK;
+  });
+}
+
+int spk_net_snapshot(spk_net* n, void* buf, int64_t bytes) {
+  int64_t need = 0;
+  int rc = spk_net_snapshot_bytes(n, &need);
+  if (rc) return rc;
+  if (!buf || bytes < need) {
+    set_error("snapshot needs %lld bytes", (long long)need);
+    return SPK_ERR_INVALID;
+  }
+  return guarded([&]() -> int {
+    SPK_CUDA(cudaStreamSynchronize(n->stream));
+    SnapHeader hd{};
+    hd.magic = SNAP_MAGIC;
+    hd.version = 1;
+    hd.N = n->N;
+    hd.Nin = n->Nin;
+    hd.L = n->L;
+    hd.B = n->B;
+    hd.n_tiles = n->hd.n_tiles;
+    hd.TS = n->hd.TS;
+    hd.ITS = n->hd.ITS;
+    hd.KL = n->hd.KL;
+    hd.n_keys = n->hd.n_keys;
+    hd.nctas = n->hd.nctas;
+    hd.has_stdp = n->has_stdp ? 1 : 0;
+    hd.stim = n->stim;
+    hd.S = n->S;
+    hd.n_csc = n->n_csc;
+    hd.current_time = n->current_time;
+    SPK_CUDA(cudaMemcpy(&hd.ctl, n->hd.ctl, sizeof(RunCtl), cudaMemcpyDeviceToHost));
+    char* out = (char*)buf;
+    std::memcpy(out, &hd, sizeof(hd));
+    out += sizeof(hd);
+    for (const auto& p : snap_parts(n)) {
+      if (p.bytes) SPK_CUDA(cudaMemcpy(out, p.dev, p.bytes, cudaMemcpyDeviceToHost));
+      out += p.bytes;
+    }
+    return SPK_OK;
+  });
+}
+
+int spk_net_restore(spk_net* n, const void* buf, int64_t bytes) {
+  int64_t need = 0;
+  int rc = spk_net_snapshot_bytes(n, &need);
+  if (rc) return rc;
+  if (!buf || bytes < need) {
+    set_error("snapshot of %lld bytes, the network's needs %lld", (long long)bytes, (long long)need);
+    return SPK_ERR_INVALID;
+  }
+  SnapHeader hd;
+  std::memcpy(&hd, buf, sizeof(hd));
+  if (hd.magic != SNAP_MAGIC || hd.version != 1 || hd.N != n->N || hd.Nin != n->Nin || hd.L != n->L ||
+      hd.B != n->B || hd.n_tiles != n->hd.n_tiles || hd.TS != n->hd.TS || hd.ITS != n->hd.ITS ||
+      hd.n_keys != n->hd.n_keys || hd.nctas != n->hd.nctas || hd.has_stdp != (n->has_stdp ? 1 : 0) ||
+      hd.S != n->S || hd.n_csc != n->n_csc) {
+    set_error("snapshot was taken from a network of another shape or schedule");
+    return SPK_ERR_INVALID;
+  }
+  return guarded([&]() -> int {
+    SPK_CUDA(cudaStreamSynchronize(n->stream));
+    const char* in = (const char*)buf + sizeof(hd);
+    for (const auto& p : snap_parts(n)) {
+      if (p.bytes) SPK_CUDA(cudaMemcpy(p.dev, in, p.bytes, cudaMemcpyHostToDevice));
+      in += p.bytes;
+    }
+    RunCtl c = hd.ctl;
+    c.step = 0;
+    c.steps_total = 0;
+    c.spike_count = 0;  // the spike store is not part of a snapshot
+    c.status = 0;
+    SPK_CUDA(cudaMemcpy(n->hd.ctl, &c, sizeof(c), cudaMemcpyHostToDevice));
+    SPK_CUDA(cudaMemset(n->abort_dev, 0, sizeof(int)));
+    SPK_CUDA(cudaMemset(n->hd.cta_stamp, 0, sizeof(unsigned long long) * 2 * (size_t)n->hd.nctas));
+    SPK_CUDA(cudaMemset(n->hd.cta_keys, 0, sizeof(unsigned long long) * 2 * (size_t)n->hd.nctas * n->hd.key_cap));
+    if (hd.stim != n->stim && n->Nin > 0 && hd.stim >= 0 && hd.stim < n->n_stim) {
+      n->stim = hd.stim;
+      n->hd.rates = n->rates_dev + (size_t)n->stim * n->Nin;
+      SPK_CUDA(cudaMemcpy(&n->dd->rates, &n->hd.rates, sizeof(float*), cudaMemcpyHostToDevice));
+    }
+    n->current_time = hd.current_time;
+    return SPK_OK;
+  });
+}
+
+int spk_net_set_wait_limit(spk_net* n, double seconds) {
+  if (!n || !(seconds >= 1e-4 && seconds <= 60.0)) {
+    set_error("wait limit must be between 1e-4 and 60 seconds");
+    return SPK_ERR_INVALID;
+  }
+  SPK_CUDA(cudaStreamSynchronize(n->stream));
+  n->hd.poll_ns = (unsigned long long)(seconds * 1e9);
+  SPK_CUDA(cudaMemcpy(&n->dd->poll_ns, &n->hd.poll_ns, sizeof(unsigned long long), cudaMemcpyHostToDevice));
+  return SPK_OK;
+}
+
+int spk_net_inject_withheld_cta(spk_net* n, int32_t rank) {
+  if (!n || n->plan.nctas < 2 || rank < 0 || rank >= n->plan.nctas) {
+    set_error("withholding a CTA needs a multi-CTA network and a rank below its CTA count");
+    return SPK_ERR_INVALID;
+  }
+  n->withhold = rank;
+  return SPK_OK;
 }
 
 int spk_net_synapse_count(const spk_net* n, int64_t* count) {
@@ -2037,6 +2214,7 @@ static int step_noalloc_impl(const spk_device_net* a, int64_t n_steps, int plast
   h.spike_cap = a->spike_capacity;
   h.ctl = (RunCtl*)a->run_state;
   h.abort_flag = (int*)(s + o_abort);
+  h.poll_ns = DEFAULT_WAIT_LIMIT_NS;
 
   const int grid = (int)std::min<size_t>((xchg_words + 255) / 256, (size_t)dev->di.sms * 4);
   noalloc_setup_kernel<<<std::max(grid, 1), 256, 0, stream>>>(

@@ -223,6 +223,24 @@ class Net:
         check(lib().spk_net_synaptic_events(self.h, C.byref(e)), "spk_net_synaptic_events")
         return e.value
 
+    def snapshot(self) -> bytes:
+        """The dynamic state (spk_net_snapshot) as bytes."""
+        n = C.c_int64()
+        check(lib().spk_net_snapshot_bytes(self.h, C.byref(n)), "spk_net_snapshot_bytes")
+        buf = C.create_string_buffer(n.value)
+        check(lib().spk_net_snapshot(self.h, buf, n.value), "spk_net_snapshot")
+        return buf.raw
+
+    def restore(self, snap: bytes):
+        buf = C.create_string_buffer(snap, len(snap))
+        check(lib().spk_net_restore(self.h, buf, len(snap)), "spk_net_restore")
+
+    def set_wait_limit(self, seconds: float):
+        check(lib().spk_net_set_wait_limit(self.h, C.c_double(seconds)), "spk_net_set_wait_limit")
+
+    def inject_withheld_cta(self, rank: int):
+        check(lib().spk_net_inject_withheld_cta(self.h, rank), "spk_net_inject_withheld_cta")
+
     def stdp_counts(self) -> tuple:
         """(plastic weights updated on presynaptic events, plastic afferents
         updated on postsynaptic spikes) so far."""

@@ -59,3 +59,23 @@ def test_noalloc_rejects_networks_beyond_its_scratch():
     dn.tile_posts = 48  # not a multiple of 32
     assert lib.spk_step_noalloc(ctypes.byref(dn), 0, 0, ctypes.c_float(0.0), None) == _native.SPK_ERR_INVALID
     assert lib.spk_step_noalloc(None, 1, 0, ctypes.c_float(0.0), None) == _native.SPK_ERR_INVALID
+
+
+def test_malformed_generated_networks_are_rejected_before_any_device_call():
+    from spike_gb300 import GenNetwork, Projection
+    lib = _native.lib()
+    bad = [
+        [Projection(_native.SPK_POP_NEURONS, 0, 10, 0, 2000, 0.1)],                 # post range past N
+        [Projection(_native.SPK_POP_INPUTS, 0, 10, 0, 100, 0.1)],                   # no inputs exist
+        [Projection(_native.SPK_POP_NEURONS, 0, 10, 0, 100, 1.5)],                  # probability > 1
+        [Projection(_native.SPK_POP_NEURONS, 0, 10, 0, 100, 0.1, delay=(0, 3))],    # delay 0
+        [Projection(_native.SPK_POP_NEURONS, 0, 10, 0, 100, 0.1, plastic=True)],    # plastic without a rule
+        [Projection(_native.SPK_POP_NEURONS, 0, 50, 0, 100, 0.1),
+         Projection(_native.SPK_POP_NEURONS, 40, 20, 50, 10, 0.1)],                 # overlapping pairs
+    ]
+    for projs in bad:
+        gen = GenNetwork(groups=[dict(count=100)], projections=projs)
+        h = ctypes.c_void_p()
+        assert lib.spk_net_generate(ctypes.byref(gen.desc), None, ctypes.byref(h)) == _native.SPK_ERR_INVALID
+        assert lib.spk_last_error()
+    assert lib.spk_net_generate(None, None, None) == _native.SPK_ERR_INVALID
