@@ -15,7 +15,7 @@ constexpr int MAX_CLASSES = 16; // scale classes: 0 = pre-multiplied, 1..15 plas
 constexpr int MAX_DELAY = 255;  // 8-bit delay field
 constexpr int LIST_CAP = 1024;     // active presynaptic keys listed per round
 constexpr int WPT_MAX = 16;        // bitmap words held per thread while listing
-constexpr int STAGE_KEYS = 128;    // sub-rows staged per warp per round
+constexpr int STAGE_KEYS = 64;     // sub-rows staged per warp per round
 constexpr int STAGE_ENTRIES = 256; // synapse entries staged per warp per round
 constexpr int APPLY_TAGS = 256;    // cell-hash slots of the ordered apply
 
