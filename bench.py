@@ -62,6 +62,7 @@ def parse():
     p.add_argument("--duration", type=float, default=60.0, help="served: seconds of request arrivals")
     p.add_argument("--arrival-rate", type=float, default=20.0, help="served: mean requests per second")
     p.add_argument("--instances", type=int, default=256, help="batched: network instances")
+    p.add_argument("--scale", type=float, default=1.0, help="plastic_ff: network size factor (profiling cases)")
     p.add_argument("--tune-steps", type=int, default=100, help="batched: autotuner trial timesteps")
     p.add_argument("--no-tune", action="store_true",
                    help="batched: skip the autotuner (8 warps, tiles of up to 64 posts, costs from synapse counts)")
@@ -82,7 +83,7 @@ def parse():
     return a
 
 
-def build_model(workload: str):
+def build_model(workload: str, scale: float = 1.0):
     from spike_gb300 import networks
     if workload == "brunel":
         m = networks.brunel()
@@ -96,9 +97,10 @@ def build_model(workload: str):
                "dt_ms": 0.1, "sim_s_per_config": 1.0, "plasticity": False}
         L = 2
     else:
-        m = networks.plastic_ff_generated()
-        cfg = {"workload": "plastic_ff_200000_lif_50000_lognormal_poisson_stdp", "neurons": 200000,
-               "inputs": 50000, "in_degree": "binomial, mean 900 input + 100 recurrent", "delays_steps": [1, 10],
+        n_in, n_neu = int(round(50000 * scale)), int(round(200000 * scale))
+        m = networks.plastic_ff_generated(n_in=n_in, n_neurons=n_neu)
+        cfg = {"workload": f"plastic_ff_{n_neu}_lif_{n_in}_lognormal_poisson_stdp", "neurons": n_neu,
+               "inputs": n_in, "in_degree": "binomial, mean 900 input + 100 recurrent", "delays_steps": [1, 10],
                "dt_ms": 0.1, "sim_s_per_config": 5.0, "plasticity": True, "connectivity": "drawn on the GPU"}
         L = 1
     return m, cfg, L
@@ -180,8 +182,9 @@ def peaks():
 
 
 def traffic_per_launch(workload: str):
-    """DRAM bytes per launch of the step kernel from the committed ncu summary
-    (profiles/step_kernel_<workload>.json), scaled to this launch length."""
+    """The committed ncu summary of the step kernel on this workload
+    (profiles/step_kernel_<workload>.json): DRAM bytes of a captured launch per
+    algorithmic byte of that launch, applied to this run's launches."""
     path = os.path.join(ROOT, "profiles", f"step_kernel_{workload}.json")
     try:
         with open(path) as f:
@@ -208,7 +211,7 @@ def run_reference(args, rank, world):
     """CPU reference arm: the oracle port with all host threads."""
     if rank != 0:
         return
-    m, cfg, L = build_model(args.workload)
+    m, cfg, L = build_model(args.workload, args.scale)
     threads = os.cpu_count() or 1
     from oracle import OracleNet
     from spike_gb300 import GenNetwork
@@ -267,7 +270,7 @@ def main():
     from spike_gb300 import schedule
 
     from spike_gb300 import GenNetwork, Net
-    m, cfg, L = build_model(args.workload)
+    m, cfg, L = build_model(args.workload, args.scale)
     sched = schedule(args.warps, args.tile, args.ctas, args.launch_steps or args.block)
     if isinstance(m, GenNetwork):
         net = Net.generate(m, sched)
@@ -327,8 +330,8 @@ def main():
     achieved = per_launch_bytes / per_launch_s / 1e9
     tr = traffic_per_launch(args.workload)
     traffic = None
-    if tr and tr.get("dram_bytes_per_timestep"):
-        traffic = tr["dram_bytes_per_timestep"] * (timesteps / max(launches, 1))
+    if tr and tr.get("traffic_per_alg_byte"):
+        traffic = tr["traffic_per_alg_byte"] * per_launch_bytes
 
     # ---- end to end through the public API --------------------------------------------
     e2e = None
@@ -592,8 +595,8 @@ def run_batched(args, rank, world, local):
     achieved = per_launch_bytes / per_launch_s / 1e9
     tr = traffic_per_launch("batched")
     traffic = None
-    if tr and tr.get("dram_bytes_per_event"):
-        traffic = tr["dram_bytes_per_event"] * events / max(launches, 1)
+    if tr and tr.get("traffic_per_alg_byte"):
+        traffic = tr["traffic_per_alg_byte"] * per_launch_bytes
 
     # plain form: the same instances, each alone on its own stream, one after another
     plain_ev, plain_ms = 0, 0.0
