@@ -308,6 +308,16 @@ int spk_net_synapse_count(const spk_net* net, int64_t* n);
 int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* schedule,
                      spk_batch** out);
 int spk_batch_run_steps(spk_batch* batch, int64_t n_steps, int32_t plasticity_on);
+/* Execution mode of a batch.  WAVES (default): the persistent step kernel,
+ * each network's state in shared memory for a whole launch, networks packed
+ * into co-resident waves.  BULK: every timestep is three kernels over all
+ * tiles of all networks (neurons, the step's key lists, propagation with
+ * STDP), state in HBM, kernel boundaries as the only synchronization,
+ * captured in a CUDA graph per block; it suits batches whose networks do not
+ * fit the GPU's shared memory at once.  Both modes give the same bits. */
+#define SPK_BATCH_WAVES 0
+#define SPK_BATCH_BULK 1
+int spk_batch_set_mode(spk_batch* batch, int32_t mode);
 /* One round of the batch's launches: every network advances up to
  * steps_per_launch steps of the run it was given with spk_net_begin_run
  * (networks whose run is complete do nothing).  A run split this way gives the

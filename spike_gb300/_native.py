@@ -114,6 +114,7 @@ class ServerStats(C.Structure):
                 ("events", u64), ("blocks", i64), ("busy_s", C.c_double), ("uptime_s", C.c_double)]
 
 
+SPK_BATCH_WAVES, SPK_BATCH_BULK = 0, 1
 SPK_JOB_QUEUED, SPK_JOB_RUNNING, SPK_JOB_DONE, SPK_JOB_FAILED, SPK_JOB_CANCELLED = 0, 1, 2, 3, 4
 
 
@@ -196,6 +197,7 @@ _SIGS = {
     "spk_batch_run_steps": (i32, [_VP, i64, i32]),
     "spk_batch_run_steps_each": (i32, [_VP, P(i64), P(i32)]),
     "spk_batch_step_block": (i32, [_VP]),
+    "spk_batch_set_mode": (i32, [_VP, i32]),
     "spk_net_begin_run": (i32, [_VP, i64, i32]),
     "spk_batch_synchronize": (i32, [_VP]),
     "spk_batch_launch_count": (i32, [_VP, P(i64)]),

@@ -1,0 +1,530 @@
+// spk_bulk.cuh - bulk-synchronous stepping of a batch of networks.
+//
+// The persistent step kernel keeps each network's state in shared memory and
+// synchronizes a network's CTAs every timestep through stamped words in
+// global memory; a batch then runs as co-resident waves, each as slow as its
+// slowest network.  In bulk mode every timestep is instead three kernels over
+// all tiles of all networks of the batch, with the state in HBM and kernel
+// boundaries as the only synchronization:
+//
+//   bulk_neurons_kernel  one warp per tile: LIF + injection and Poisson inputs
+//                        (the persistent kernel's phase A), STDP traces,
+//                        spike / pre-event words into the network's bitmaps,
+//                        L2 prefetch of the spiking keys' rows;
+//   bulk_list_kernel     one CTA per network: the step's active keys in
+//                        canonical (ascending key) order from the bitmaps, and
+//                        the spike store;
+//   bulk_prop_kernel     one warp per tile: the list's sub-rows of the tile
+//                        staged and applied in canonical order into the tile's
+//                        ring cells in HBM (the persistent kernel's rounds),
+//                        with the STDP pre pass, then the tile's post-spike
+//                        afferent pass.
+//
+// Each ring cell still has one writer applying contributions in canonical
+// order, and every float operation is the persistent kernel's, so a network
+// gives the same bits in both modes.  A block of K timesteps is 3K launches
+// plus one that advances the networks' run counters, captured in a CUDA graph.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "spk_internal.h"
+#include "spk_kernel.cuh"
+
+namespace spk {
+
+struct BulkTile {
+  int net;   // index into the batch's NetDev array
+  int tile;  // tile of that network
+};
+
+// Timestep s of the current block of a network's run.
+struct BulkStep {
+  float t, tg;
+  int T, slot;
+  bool live, stdp_run, inputs_active;
+};
+
+__device__ __forceinline__ BulkStep bulk_step(const NetDev& d, const RunCtl& c, int s) {
+  BulkStep b;
+  const int sr = c.step + s;
+  b.live = sr < c.steps_total;
+  const float dt = d.dt;
+  // current_time_in_seconds = starttime + s*timestep_grouping*timestep
+  // (Spike/Models/SpikingModel.cpp:226), timestep_index = roundf(t/dt).
+  b.t = c.start_time + (float)(sr * 1) * dt;
+  b.T = (int)roundf(b.t / dt);
+  b.slot = b.T % d.B;
+  b.tg = b.t + 0.0f * dt;
+  b.stdp_run = d.has_stdp && c.plastic;
+  b.inputs_active = c.inputs_active != 0 || s > 0;
+  return b;
+}
+
+__device__ __forceinline__ RunCtl load_ctl(const RunCtl* p) {
+  RunCtl c;
+  c.start_time = p->start_time;
+  c.step = p->step;
+  c.steps_total = p->steps_total;
+  c.plastic = p->plastic;
+  c.inputs_active = p->inputs_active;
+  c.record_inputs = p->record_inputs;
+  return c;
+}
+
+// ---- timestep part 1: neurons and inputs -------------------------------------------
+__global__ void __launch_bounds__(256) bulk_neurons_kernel(const NetDev* __restrict__ nets,
+                                                           const BulkTile* __restrict__ tiles, int n_tiles_total,
+                                                           int s) {
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (gw >= n_tiles_total) return;
+  const BulkTile bt = tiles[gw];
+  const NetDev& d = nets[bt.net];
+  const RunCtl c = load_ctl(d.ctl);
+  const BulkStep st = bulk_step(d, c, s);
+  if (!st.live) return;
+  const int N = d.N, Nin = d.Nin, KL = d.KL, L = d.L, B = d.B, kind = d.kind, TS = d.TS, ITS = d.ITS;
+  const int p0 = bt.tile * TS, kin0 = bt.tile * ITS;
+  const float half_dt = 0.5f * d.dt;
+  int g_first = 0, g_last = 0;
+  {
+    const int n_hi = min(p0 + TS, N) - 1;
+    while (g_first + 1 < d.n_groups && p0 >= d.groups[g_first].end) ++g_first;
+    g_last = g_first;
+    while (g_last + 1 < d.n_groups && n_hi >= d.groups[g_last].end) ++g_last;
+  }
+  const GroupConst G0 = d.groups[g_first];
+  float* ring_slot = d.ring + ((size_t)bt.tile * B + st.slot) * TS * L;
+  float* pub = d.pre_pub;
+  for (int base = 0; base < TS; base += 32) {
+    const int li = base + lane;
+    const int n = p0 + li;
+    bool spk = false;
+    if (n < N) {
+      GroupConst G = G0;
+      if (g_last != g_first) {
+        int gi = g_first;
+        while (gi < g_last && n >= d.groups[gi].end) ++gi;
+        G = d.groups[gi];
+      }
+      float Vi = d.V[n];
+      float lastn = d.last[n];
+      float input;
+      if (kind == SPK_SYN_CONDUCTANCE) {
+        float total = 0.0f;
+        for (int l = 0; l < L; ++l) {
+          const float cell = ring_slot[li * L + l];
+          ring_slot[li * L + l] = 0.0f;
+          const float gnew = d.decay[l] * d.gtr[(size_t)n * L + l] + cell;
+          total = total + gnew * (d.vhat[l] - Vi);
+          d.gtr[(size_t)n * L + l] = gnew;
+        }
+        input = total * G.kR;
+      } else if (kind == SPK_SYN_CURRENT) {
+        float total = 0.0f;
+        for (int l = 0; l < L; ++l) {
+          const float cell = ring_slot[li * L + l];
+          ring_slot[li * L + l] = 0.0f;
+          float inew = d.gtr[(size_t)n * L + l] * d.decay[l];
+          inew = inew + cell;
+          total = total + inew;
+          d.gtr[(size_t)n * L + l] = inew;
+        }
+        input = total * G.kR;
+      } else {
+        float total = 0.0f;
+        for (int l = 0; l < L; ++l) {
+          total = total + ring_slot[li * L + l];
+          ring_slot[li * L + l] = 0.0f;
+        }
+        input = total;
+      }
+      if (((st.tg - lastn) - d.t_ref) > half_dt) {
+        Vi = G.k * G.v0 + (1.0f - G.k) * Vi + G.k * d.i_bg + input;
+        if (Vi >= G.theta) {
+          spk = true;
+          d.last[n] = st.tg;
+          Vi = G.vreset;
+        }
+      }
+      d.V[n] = Vi;
+      if (st.stdp_run) {
+        float po = d.post_trace[n] * d.E_m;
+        po = po + (spk ? d.inc_m : 0.0f);
+        d.post_trace[n] = po;
+        float pr = d.pre_trace[KL + n] * d.E_p;
+        pr = pr + (spk ? d.inc_p : 0.0f);
+        d.pre_trace[KL + n] = pr;
+        pub[KL + n] = pr;
+      }
+    }
+    const unsigned word = __ballot_sync(FULL, spk);
+    if (lane == 0) {
+      const int wi = ((KL + p0) >> 5) + (base >> 5);
+      d.bitsA[wi] = word;
+      d.bitsP[wi] = st.stdp_run ? word : 0u;
+    }
+    if (spk) {
+      // the row pointers and synapse row of the spiking key, into L2 for the
+      // propagation kernel
+      const int key = KL + n;
+      const int r0 = __ldg(d.rowptr + (size_t)key * d.n_tiles), r1 = __ldg(d.rowptr + (size_t)(key + 1) * d.n_tiles);
+      prefetch_l2(d.rowptr + (size_t)key * d.n_tiles, sizeof(int) * (size_t)(d.n_tiles + 1));
+      if (r1 > r0) prefetch_l2(d.entries + r0, sizeof(uint2) * (size_t)(r1 - r0));
+    }
+  }
+  for (int base = 0; base < ITS; base += 32) {
+    const int li = base + lane;
+    const int k = kin0 + li;
+    bool spk = false, pev = false;
+    if (k < Nin) {
+      const int idx = Nin - 1 - k;
+      float nx = d.in_next[idx];
+      if ((nx <= st.tg) || !st.inputs_active) {
+        const float rate = d.rates[idx];
+        const float u = draw_uniform(d.seed, (uint32_t)idx, (uint32_t)st.T, DOMAIN_POISSON);
+        nx = st.tg - (1.0f / rate) * logf_spk(u);
+        if (st.inputs_active) spk = true;
+      }
+      d.in_next[idx] = nx;
+      if (st.stdp_run) {
+        int pg = (int)roundf((nx - st.t) / d.dt);
+        if (pg >= 1) pg *= -1;
+        pev = pg >= 0;
+        float pr = d.pre_trace[k] * d.E_p;
+        pr = pr + (pev ? d.inc_p : 0.0f);
+        d.pre_trace[k] = pr;
+        pub[k] = pr;
+      }
+    }
+    const unsigned wa = __ballot_sync(FULL, spk);
+    const unsigned wp = __ballot_sync(FULL, pev);
+    if (lane == 0) {
+      const int wi = (kin0 >> 5) + (base >> 5);
+      d.bitsA[wi] = wa;
+      d.bitsP[wi] = wp;
+    }
+    if (spk || pev) {
+      const int r0 = __ldg(d.rowptr + (size_t)k * d.n_tiles), r1 = __ldg(d.rowptr + (size_t)(k + 1) * d.n_tiles);
+      prefetch_l2(d.rowptr + (size_t)k * d.n_tiles, sizeof(int) * (size_t)(d.n_tiles + 1));
+      if (r1 > r0) prefetch_l2(d.entries + r0, sizeof(uint2) * (size_t)(r1 - r0));
+    }
+  }
+}
+
+// ---- timestep part 2: the step's active keys and the spike store ----------------------
+// One CTA of BULK_LIST_THREADS per network; each thread owns a contiguous run
+// of bitmap words, so a block-wide exclusive scan of the per-thread counts
+// gives every key its place in ascending key order.
+constexpr int BULK_LIST_THREADS = 512;
+
+__global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetDev* __restrict__ nets, int s) {
+  __shared__ unsigned long long warp_tot[BULK_LIST_THREADS / 32];
+  __shared__ unsigned long long s_base;
+  const NetDev& d = nets[blockIdx.x];
+  const RunCtl c = load_ctl(d.ctl);
+  const BulkStep st = bulk_step(d, c, s);
+  if (!st.live) {
+    if (threadIdx.x == 0) *d.step_count = 0;
+    return;
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int n_words = d.n_words, KL = d.KL;
+  const bool rec_inputs = c.record_inputs != 0;
+  const int per = (n_words + BULK_LIST_THREADS - 1) / BULK_LIST_THREADS;
+  const int w0 = min(n_words, threadIdx.x * per), w1 = min(n_words, w0 + per);
+  // counts: list keys (low 32 bits) and recorded spikes (high 32 bits)
+  unsigned long long cnt = 0;
+  for (int i = w0; i < w1; ++i) {
+    const uint32_t a = d.bitsA[i], p = d.bitsP[i];
+    const bool rec = (i << 5) >= KL || rec_inputs;
+    cnt += (unsigned long long)__popc(a | p) + (rec ? ((unsigned long long)__popc(a) << 32) : 0ull);
+  }
+  unsigned long long incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_tot[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    const unsigned long long v = lane < BULK_LIST_THREADS / 32 ? warp_tot[lane] : 0ull;
+    unsigned long long wi = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(FULL, wi, o);
+      if (lane >= o) wi += y;
+    }
+    if (lane < BULK_LIST_THREADS / 32) warp_tot[lane] = wi - v;  // exclusive per warp
+    if (lane == 31) s_base = wi;                                // block total
+  }
+  __syncthreads();
+  const unsigned long long excl = warp_tot[w] + incl - cnt;
+  int pos = (int)(excl & 0xffffffffull);
+  const unsigned long long sc0 = d.ctl->spike_count;
+  unsigned long long sp = sc0 + (excl >> 32);
+  for (int i = w0; i < w1; ++i) {
+    const uint32_t a = d.bitsA[i], p = d.bitsP[i];
+    const bool rec = (i << 5) >= KL || rec_inputs;
+    uint32_t m = a | p;
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      const uint32_t key = (uint32_t)(i << 5) + (uint32_t)b;
+      const uint32_t fa = (a >> b) & 1u, fp = (p >> b) & 1u;
+      d.step_list[pos++] = key | (fa << 31) | (fp << 30);
+      if (fa && rec) {
+        if (sp < (unsigned long long)d.spike_cap)
+          d.spikes[sp] = make_uint2(key, __float_as_uint(st.t));
+        else
+          atomicCAS(&d.ctl->status, 0, SPK_ERR_OVERFLOW);
+        ++sp;
+      }
+    }
+  }
+  __syncthreads();  // every thread has read spike_count
+  if (threadIdx.x == 0) {
+    *d.step_count = (int)(s_base & 0xffffffffull);
+    const unsigned long long sc = sc0 + (s_base >> 32);
+    d.ctl->spike_count = sc > (unsigned long long)d.spike_cap ? (unsigned long long)d.spike_cap : sc;
+  }
+}
+
+// ---- timestep part 3: propagation and STDP ----------------------------------------------
+// Shared memory per warp (4-byte words).
+struct BulkWarpLayout {
+  int stage, stw, sidx, kst, koff, kfl, kpre, tag, total;
+};
+__host__ __device__ inline BulkWarpLayout bulk_warp_layout() {
+  BulkWarpLayout l;
+  int o = 0;
+  l.stage = o; o += 2 * STAGE_ENTRIES;
+  l.stw = o; o += STAGE_ENTRIES;
+  l.sidx = o; o += STAGE_ENTRIES / 2;
+  l.kst = o; o += STAGE_KEYS;
+  l.koff = o; o += STAGE_KEYS + 4;
+  l.kfl = o; o += STAGE_KEYS;
+  l.kpre = o; o += STAGE_KEYS;
+  l.tag = o; o += APPLY_TAGS;
+  o = (o + 3) & ~3;
+  l.total = o;
+  return l;
+}
+constexpr int BULK_PROP_WARPS = 8;
+
+__global__ void __launch_bounds__(BULK_PROP_WARPS * 32, 2) bulk_prop_kernel(NetDev* __restrict__ nets,
+                                                                            const BulkTile* __restrict__ tiles,
+                                                                            int n_tiles_total, int s) {
+  extern __shared__ __align__(16) uint32_t bsm[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int gw = blockIdx.x * BULK_PROP_WARPS + w;
+  if (gw >= n_tiles_total) return;
+  const BulkWarpLayout wl = bulk_warp_layout();
+  uint32_t* wreg = bsm + w * wl.total;
+  uint2* stage = (uint2*)(wreg + wl.stage);
+  float* stage_w = (float*)(wreg + wl.stw);
+  unsigned short* sidx = (unsigned short*)(wreg + wl.sidx);
+  int* kst = (int*)(wreg + wl.kst);
+  int* koff = (int*)(wreg + wl.koff);
+  uint32_t* kfl = wreg + wl.kfl;
+  float* kpre = (float*)(wreg + wl.kpre);
+  int* tag_s = (int*)(wreg + wl.tag);
+  const BulkTile bt = tiles[gw];
+  NetDev& d = nets[bt.net];
+  const RunCtl c = load_ctl(d.ctl);
+  const BulkStep st = bulk_step(d, c, s);
+  if (!st.live) return;
+  const int TS = d.TS, L = d.L, B = d.B, KL = d.KL, n_tiles = d.n_tiles, t_idx = bt.tile;
+  const int p0 = t_idx * TS;
+  float* ring = d.ring + (size_t)t_idx * B * TS * L;
+  const float* pub = d.pre_pub;
+  const uint32_t* tile_spk = d.bitsA + ((KL + p0) >> 5);  // spike words of the tile's posts
+  for (int i = lane; i < APPLY_TAGS; i += 32) tag_s[i] = 32;
+  unsigned long long ev = 0, n_pre = 0, n_post = 0;
+  const int n_list = *d.step_count;
+  __syncwarp();
+  for (int kb = 0; kb < n_list; kb += STAGE_KEYS) {
+    const int nk = min(STAGE_KEYS, n_list - kb);
+    for (int i = lane; i < nk; i += 32) {
+      const uint32_t lv = d.step_list[kb + i];
+      const int* rp = d.rowptr + (size_t)(lv & 0x3fffffffu) * n_tiles + t_idx;
+      cp_async4(kst + i, rp);
+      cp_async4(koff + i, rp + 1);
+      kfl[i] = lv;
+      if (st.stdp_run) kpre[i] = __ldcg(pub + (lv & 0x3fffffffu));
+    }
+    cp_async_wait_all();
+    __syncwarp();
+    for (int i = lane; i < nk; i += 32) {
+      const int len = koff[i] - kst[i];
+      koff[i] = len;
+      if (kfl[i] >> 31) ev += (unsigned long long)len;
+    }
+    __syncwarp();
+    int carry = 0;
+    for (int c0 = 0; c0 < nk; c0 += 32) {
+      const int i = c0 + lane;
+      const int len = i < nk ? koff[i] : 0;
+      int incl = len;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+      }
+      __syncwarp();
+      if (i < nk) koff[i] = carry + incl - len;
+      carry += __shfl_sync(FULL, incl, 31);
+    }
+    const int total_e = carry;
+    __syncwarp();
+    for (int f0 = 0; f0 < total_e; f0 += STAGE_ENTRIES) {
+      const int nf = min(STAGE_ENTRIES, total_e - f0);
+      for (int i = lane; i < nk; i += 32) {
+        const int o = koff[i];
+        const int e0 = max(o, f0), e1 = min(o + (i + 1 < nk ? koff[i + 1] - o : total_e - o), f0 + nf);
+        const int base = kst[i] - o;
+        for (int f = e0; f < e1; ++f) {
+          sidx[f - f0] = (unsigned short)i;
+          cp_async8(stage + (f - f0), d.entries + base + f);
+        }
+      }
+      cp_async_wait_all();
+      __syncwarp();
+      if (d.has_stdp) {
+        bool any = false;
+        for (int f = lane; f < nf; f += 32) {
+          const uint2 en = stage[f];
+          if ((en.x >> 28) != 0u) {
+            cp_async4(stage_w + f, &d.csc[en.y].y);
+            any = true;
+          }
+        }
+        if (__any_sync(FULL, any)) cp_async_wait_all();
+        __syncwarp();
+      }
+      for (int c0 = 0; c0 < nf; c0 += 32) {
+        const int f = c0 + lane;
+        bool add = false;
+        size_t cell = 0;
+        int h = lane;  // distinct dummy tags for lanes without a contribution
+        float contrib = 0.0f;
+        if (f < nf) {
+          const int j = sidx[f];
+          const uint32_t flv = kfl[j];
+          const bool A = (flv >> 31) != 0;
+          const bool P = ((flv >> 30) & 1u) != 0;
+          const uint2 en = stage[f];
+          const int q = (int)(en.x & 0xffffu);
+          const int dl = (int)((en.x >> 16) & 0xffu);
+          const int lb = (int)((en.x >> 24) & 0xfu);
+          const int cl = (int)(en.x >> 28);
+          if (cl != 0) {
+            float v = stage_w[f];
+            if (st.stdp_run) {
+              const bool post_ev = ((tile_spk[q >> 5] >> (q & 31)) & 1u) != 0;
+              if (P || post_ev) {
+                v = stdp_update(d, v, P, post_ev, d.post_trace[p0 + q], kpre[j]);
+                d.csc[en.y].y = __float_as_uint(v);
+                ++n_pre;
+              }
+            }
+            contrib = v * d.scale_tab[cl];
+          } else {
+            contrib = __uint_as_float(en.y);
+          }
+          if (A) {
+            add = true;
+            int sl = st.slot + dl;
+            if (sl >= B) sl -= B;
+            const int ci = (sl * TS + q) * L + lb;
+            cell = (size_t)ci;
+            h = ci & (APPLY_TAGS - 1);
+          }
+        }
+        // same-cell contributions in lane order (see the persistent kernel)
+        bool pending = add;
+        while (__any_sync(FULL, pending)) {
+          if (pending) atomicMin(tag_s + h, lane);
+          __syncwarp();
+          const bool win = pending && tag_s[h] == lane;
+          if (win) ring[cell] = ring[cell] + contrib;
+          __syncwarp();
+          if (win) {
+            tag_s[h] = 32;
+            pending = false;
+          }
+          __syncwarp();
+        }
+      }
+      __syncwarp();
+    }
+  }
+  // post-spike afferent pass of the tile's spiking posts (weights updated on a
+  // presynaptic event this step are skipped: done above)
+  if (st.stdp_run) {
+    const uint32_t* bA = d.bitsA;
+    const uint32_t* bP = d.bitsP;
+    constexpr int AFF = 4;
+    for (int wi = 0; wi < TS / 32; ++wi) {
+      uint32_t word = tile_spk[wi];
+      while (word) {
+        const int b = __ffs(word) - 1;
+        word &= word - 1;
+        const int q = p0 + wi * 32 + b;
+        const int a0 = __ldg(d.csc_ptr + q), a1 = __ldg(d.csc_ptr + q + 1);
+        const float post_tr = d.post_trace[q];
+        for (int a = a0; a < a1; a += 32 * AFF) {
+          uint2 cc[AFF];
+#pragma unroll
+          for (int u = 0; u < AFF; ++u) {
+            const int ai = a + u * 32 + lane;
+            cc[u] = d.csc[ai < a1 ? ai : a];
+          }
+          uint32_t vm[AFF];
+          float prt[AFF];
+#pragma unroll
+          for (int u = 0; u < AFF; ++u) {
+            const int pk = (int)cc[u].x;
+            vm[u] = bA[pk >> 5] | bP[pk >> 5];
+            prt[u] = pub[pk];
+          }
+#pragma unroll
+          for (int u = 0; u < AFF; ++u) {
+            const int ai = a + u * 32 + lane;
+            const int pk = (int)cc[u].x;
+            if (ai >= a1 || ((vm[u] >> (pk & 31)) & 1u)) continue;
+            const float nw = stdp_update(d, __uint_as_float(cc[u].y), false, true, post_tr, prt[u]);
+            d.csc[ai].y = __float_as_uint(nw);
+            ++n_post;
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    ev += __shfl_xor_sync(FULL, ev, o);
+    n_pre += __shfl_xor_sync(FULL, n_pre, o);
+    n_post += __shfl_xor_sync(FULL, n_post, o);
+  }
+  if (lane == 0) {
+    if (ev) atomicAdd(&d.ctl->events, ev);
+    if (n_pre) atomicAdd(&d.ctl->stdp_pre, n_pre);
+    if (n_post) atomicAdd(&d.ctl->stdp_post, n_post);
+  }
+}
+
+// ---- after a block: the networks' run counters -------------------------------------------
+__global__ void bulk_finish_kernel(const NetDev* __restrict__ nets, int n_nets, int K) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_nets) return;
+  RunCtl* c = nets[i].ctl;
+  const int done = max(0, min(K, c->steps_total - c->step));
+  c->step += done;
+  c->gstep += done;
+  if (done > 0) c->inputs_active = 1;
+}
+
+}  // namespace spk

@@ -96,6 +96,9 @@ struct NetDev {
   RunCtl* ctl;
   int* abort_flag;            // shared by a launch: set on timeout
   unsigned long long poll_ns; // limit of every wait on another CTA (globaltimer ns)
+  // bulk-synchronous batches only: the step's active keys in canonical order
+  uint32_t* step_list;        // [n_keys] key | spike << 31 | pre-event << 30
+  int* step_count;            // keys in step_list
 };
 
 struct CtaMap {

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/spike_gb300.h"
+#include "spk_bulk.cuh"
 #include "spk_gen.cuh"
 #include "spk_internal.h"
 #include "spk_kernel.cuh"
@@ -216,6 +217,13 @@ struct spk_batch {
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;  // recorded after each run; the networks' streams wait on it
   int64_t launches = 0;
+  // bulk-synchronous mode (spk_bulk.cuh)
+  int mode = SPK_BATCH_WAVES;
+  std::vector<NetDev> hds;       // host copies of the batch's descriptors
+  BulkTile* dtiles = nullptr;    // [tiles_total]
+  int tiles_total = 0;
+  void* bulk_mem = nullptr;      // tiles, step lists and counts
+  cudaGraphExec_t bulk_graph = nullptr;  // one block of K timesteps
 };
 
 namespace spk {
@@ -1788,7 +1796,8 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
       cur.cooperative |= n->plan.nctas > 1;
     }
     b->waves.push_back(cur);
-    std::vector<NetDev> hds(n_nets);
+    std::vector<NetDev>& hds = b->hds;
+    hds.resize(n_nets);
     for (int i = 0; i < n_nets; ++i) hds[i] = nets[i]->hd;
     const size_t bytes = align_up(sizeof(NetDev) * n_nets, 256) + align_up(sizeof(CtaMap) * map.size(), 256) + 256;
     void* mem = nullptr;
@@ -1819,6 +1828,48 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
   });
 }
 
+namespace spk {
+
+// One block of K timesteps in bulk mode: 3K kernels and the run-counter update.
+static int bulk_launch_block(spk_batch* b) {
+  const int n = (int)b->nets.size();
+  const int T = b->tiles_total;
+  const int wpb = 256 / 32;
+  const int prop_smem = BULK_PROP_WARPS * bulk_warp_layout().total * 4;
+  for (int s = 0; s < b->K; ++s) {
+    bulk_neurons_kernel<<<(T + wpb - 1) / wpb, 256, 0, b->stream>>>(b->dd, b->dtiles, T, s);
+    bulk_list_kernel<<<n, BULK_LIST_THREADS, 0, b->stream>>>(b->dd, s);
+    bulk_prop_kernel<<<(T + BULK_PROP_WARPS - 1) / BULK_PROP_WARPS, BULK_PROP_WARPS * 32, prop_smem, b->stream>>>(
+        b->dd, b->dtiles, T, s);
+  }
+  bulk_finish_kernel<<<(n + 255) / 256, 256, 0, b->stream>>>(b->dd, n, b->K);
+  SPK_CUDA(cudaGetLastError());
+  return SPK_OK;
+}
+
+static int bulk_run_block(spk_batch* b) {
+  if (!b->bulk_graph) {
+    cudaGraph_t g = nullptr;
+    SPK_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = bulk_launch_block(b);
+    const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (rc != SPK_OK || e != cudaSuccess || cudaGraphInstantiate(&b->bulk_graph, g, 0) != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      b->bulk_graph = nullptr;
+      const int rc2 = bulk_launch_block(b);  // launches go direct
+      b->launches += 3 * (int64_t)b->K + 1;
+      return rc2;
+    }
+    cudaGraphDestroy(g);
+  }
+  SPK_CUDA(cudaGraphLaunch(b->bulk_graph, b->stream));
+  b->launches += 3 * (int64_t)b->K + 1;
+  return SPK_OK;
+}
+
+}  // namespace spk
+
 int spk_batch_run_steps_each(spk_batch* b, const int64_t* n_steps, const int32_t* plasticity_on) {
   if (!b || !n_steps) return SPK_ERR_INVALID;
   int64_t most = 0;
@@ -1839,6 +1890,11 @@ int spk_batch_run_steps_each(spk_batch* b, const int64_t* n_steps, const int32_t
   // networks that finish early leave their launches at once (no steps left)
   const int64_t blocks = (most + b->K - 1) / b->K;
   for (int64_t blk = 0; blk < blocks; ++blk) {
+    if (b->mode == SPK_BATCH_BULK) {
+      const int rc = bulk_run_block(b);
+      if (rc) return rc;
+      continue;
+    }
     for (const auto& wv : b->waves) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(wv.ctas);
@@ -1865,10 +1921,62 @@ int spk_batch_run_steps_each(spk_batch* b, const int64_t* n_steps, const int32_t
   return SPK_OK;
 }
 
+
+int spk_batch_set_mode(spk_batch* b, int32_t mode) {
+  if (!b || (mode != SPK_BATCH_WAVES && mode != SPK_BATCH_BULK)) return SPK_ERR_INVALID;
+  if (mode == b->mode) return SPK_OK;
+  if (mode == SPK_BATCH_WAVES) {
+    b->mode = mode;
+    return SPK_OK;
+  }
+  return guarded([&]() -> int {
+    if (!b->bulk_mem) {
+      std::vector<BulkTile> tiles;
+      size_t list_words = 0;
+      for (size_t i = 0; i < b->nets.size(); ++i) {
+        for (int t = 0; t < b->nets[i]->plan.n_tiles; ++t) tiles.push_back(BulkTile{(int)i, t});
+        list_words += (size_t)b->nets[i]->plan.n_keys;
+      }
+      const size_t t_bytes = align_up(sizeof(BulkTile) * tiles.size(), 256);
+      const size_t l_bytes = align_up(sizeof(uint32_t) * list_words, 256);
+      const size_t c_bytes = align_up(sizeof(int) * b->nets.size(), 256);
+      if (cudaMalloc(&b->bulk_mem, t_bytes + l_bytes + c_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        b->bulk_mem = nullptr;
+        set_error("bulk mode: device allocation failed");
+        return SPK_ERR_OOM;
+      }
+      b->dtiles = (BulkTile*)b->bulk_mem;
+      b->tiles_total = (int)tiles.size();
+      uint32_t* lists = (uint32_t*)((char*)b->bulk_mem + t_bytes);
+      int* counts = (int*)((char*)b->bulk_mem + t_bytes + l_bytes);
+      size_t off = 0;
+      for (size_t i = 0; i < b->nets.size(); ++i) {
+        b->hds[i].step_list = lists + off;
+        b->hds[i].step_count = counts + i;
+        off += (size_t)b->nets[i]->plan.n_keys;
+      }
+      SPK_CUDA(cudaMemcpy(b->dtiles, tiles.data(), sizeof(BulkTile) * tiles.size(), cudaMemcpyHostToDevice));
+      SPK_CUDA(cudaMemcpy(b->dd, b->hds.data(), sizeof(NetDev) * b->hds.size(), cudaMemcpyHostToDevice));
+      SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    BULK_PROP_WARPS * bulk_warp_layout().total * 4));
+    }
+    b->mode = mode;
+    return SPK_OK;
+  });
+}
+
 int spk_batch_step_block(spk_batch* b) {
   if (!b) return SPK_ERR_INVALID;
   // order the batch stream after each network's pending work (its run set-up)
   for (spk_net* n : b->nets) SPK_CUDA(cudaStreamSynchronize(n->stream));
+  if (b->mode == SPK_BATCH_BULK) {
+    const int rc = bulk_run_block(b);
+    if (rc) return rc;
+    SPK_CUDA(cudaEventRecord(b->done, b->stream));
+    for (spk_net* n : b->nets) SPK_CUDA(cudaStreamWaitEvent(n->stream, b->done, 0));
+    return SPK_OK;
+  }
   for (const auto& wv : b->waves) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(wv.ctas);
@@ -1931,6 +2039,8 @@ int spk_batch_destroy(spk_batch* b) {
     cudaStreamDestroy(b->stream);
   }
   if (b->done) cudaEventDestroy(b->done);
+  if (b->bulk_graph) cudaGraphExecDestroy(b->bulk_graph);
+  if (b->bulk_mem) cudaFree(b->bulk_mem);
   cudaFree(b->dd);
   delete b;
   return SPK_OK;

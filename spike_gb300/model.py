@@ -367,6 +367,11 @@ class Batch:
         check(lib().spk_batch_create(arr, len(nets), C.byref(sched) if sched else None, C.byref(self.h)),
               "spk_batch_create")
 
+    def set_mode(self, mode: int):
+        """SPK_BATCH_WAVES (persistent kernel) or SPK_BATCH_BULK (three
+        kernels per timestep over all networks)."""
+        check(lib().spk_batch_set_mode(self.h, mode), "spk_batch_set_mode")
+
     @staticmethod
     def autotune(gens: list, trial_steps: int = 200, costs: bool = False):
         """Measured schedule search (spk_batch_autotune) for generated

@@ -69,3 +69,40 @@ def test_batch_waves_cover_more_ctas_than_one_launch_holds():
     np.testing.assert_array_equal(i0, i1)
     np.testing.assert_array_equal(bits(t0), bits(t1))
     b.close()
+
+
+@pytest.mark.parametrize("plastic_first", [True, False])
+def test_bulk_mode_equals_each_instance_alone(plastic_first):
+    """Bulk-synchronous batches (three kernels per timestep over all
+    instances, state in HBM) give every instance its persistent-kernel result,
+    bit for bit, including STDP weights, over blocks that cut runs."""
+    gens = small_sweep(k=10, seed=21)
+    sched = N.Schedule(8, 64, 0, 150)  # blocks of 150 timesteps
+    batched = [Net.generate(g, sched) for g in gens]
+    alone = [Net.generate(g, sched) for g in gens]
+    b = Batch(batched, sched)
+    b.set_mode(N.SPK_BATCH_BULK)
+    for plastic, steps in ((plastic_first, 400), (not plastic_first, 230)):
+        b.run_steps(steps, plastic)
+        for n in alone:
+            n.run_steps(steps, plastic)
+    assert b.synchronize() == 0
+    for g, x, y in zip(gens, batched, alone):
+        assert y.synchronize() == 0
+        n, n_in, S = g.desc.n_neurons, g.desc.n_inputs, x.synapse_count()
+        sx, sy = snapshot(x, n, n_in, S), snapshot(y, n, n_in, S)
+        for k in sx:
+            np.testing.assert_array_equal(sx[k], sy[k], err_msg=f"instance n={n} field {k}")
+        assert x.stdp_counts() == y.stdp_counts()
+    # switching back to waves continues the same runs
+    b.set_mode(N.SPK_BATCH_WAVES)
+    b.run_steps(120, True)
+    for n in alone:
+        n.run_steps(120, True)
+    assert b.synchronize() == 0
+    for g, x, y in zip(gens, batched, alone):
+        sx, sy = snapshot(x, g.desc.n_neurons, g.desc.n_inputs, x.synapse_count()), \
+            snapshot(y, g.desc.n_neurons, g.desc.n_inputs, y.synapse_count())
+        for k in sx:
+            np.testing.assert_array_equal(sx[k], sy[k], err_msg=k)
+    b.close()
