@@ -7,10 +7,10 @@
 // all tiles of all networks of the batch, with the state in HBM and kernel
 // boundaries as the only synchronization:
 //
-//   bulk_neurons_kernel  one warp per tile: LIF + injection and Poisson inputs
-//                        (the persistent kernel's phase A), STDP traces,
-//                        spike / pre-event words into the network's bitmaps,
-//                        L2 prefetch of the spiking keys' rows;
+//   bulk_neurons_kernel  one warp per 32 keys: LIF + injection and Poisson
+//                        inputs (the persistent kernel's phase A), STDP
+//                        traces, spike / pre-event words into the network's
+//                        bitmaps;
 //   bulk_list_kernel     one CTA per network: the step's active keys in
 //                        canonical (ascending key) order from the bitmaps, and
 //                        the spike store;
@@ -73,142 +73,179 @@ __device__ __forceinline__ RunCtl load_ctl(const RunCtl* p) {
 }
 
 // ---- timestep part 1: neurons and inputs -------------------------------------------
+// One warp per run of up to BULK_WPW consecutive 32-key words of one network
+// (inputs: keys 0..n_inputs-1; neurons: keys KL..KL+N-1).  A warp issues the
+// state loads of all its words before any update, so the chain of dependent
+// loads (descriptor, run control, state) is paid once per run of words, not
+// once per word.  Words of padding keys are never written: they stay zero
+// from set-up.  No L2 prefetch of the spiking rows here: a batch's rows of one
+// step exceed the L2.
+constexpr int BULK_WPW = 8;
+
+struct BulkWord {
+  int net;    // index into the batch's NetDev array
+  int word;   // first word (key / 32)
+  int count;  // words in the run (<= BULK_WPW), all inputs or all neurons
+  int pad;
+};
+
+// LIF update of neuron n (the persistent kernel's phase A, same operations)
+// with its state already loaded; returns whether it spiked.
+__device__ __forceinline__ bool bulk_lif(const NetDev& d, const BulkStep& st, int n, int key, float Vi,
+                                         float lastn, float* ring_cell, float input_voltage) {
+  int gi = 0;
+  while (gi + 1 < d.n_groups && n >= d.groups[gi].end) ++gi;
+  const GroupConst G = d.groups[gi];
+  const int L = d.L, kind = d.kind;
+  float input;
+  if (kind == SPK_SYN_CONDUCTANCE) {
+    float total = 0.0f;
+    for (int l = 0; l < L; ++l) {
+      const float cell = ring_cell[l];
+      ring_cell[l] = 0.0f;
+      const float gnew = d.decay[l] * d.gtr[(size_t)n * L + l] + cell;
+      total = total + gnew * (d.vhat[l] - Vi);
+      d.gtr[(size_t)n * L + l] = gnew;
+    }
+    input = total * G.kR;
+  } else if (kind == SPK_SYN_CURRENT) {
+    float total = 0.0f;
+    for (int l = 0; l < L; ++l) {
+      const float cell = ring_cell[l];
+      ring_cell[l] = 0.0f;
+      float inew = d.gtr[(size_t)n * L + l] * d.decay[l];
+      inew = inew + cell;
+      total = total + inew;
+      d.gtr[(size_t)n * L + l] = inew;
+    }
+    input = total * G.kR;
+  } else {
+    // voltage synapses: the caller summed the labels' cells in label order
+    input = input_voltage;
+  }
+  bool spk = false;
+  if (((st.tg - lastn) - d.t_ref) > 0.5f * d.dt) {
+    Vi = G.k * G.v0 + (1.0f - G.k) * Vi + G.k * d.i_bg + input;
+    if (Vi >= G.theta) {
+      spk = true;
+      d.last[n] = st.tg;
+      Vi = G.vreset;
+    }
+  }
+  d.V[n] = Vi;
+  return spk;
+}
+
 __global__ void __launch_bounds__(256) bulk_neurons_kernel(const NetDev* __restrict__ nets,
-                                                           const BulkTile* __restrict__ tiles, int n_tiles_total,
+                                                           const BulkWord* __restrict__ words, int n_words_total,
                                                            int s) {
   const int lane = threadIdx.x & 31;
   const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (gw >= n_tiles_total) return;
-  const BulkTile bt = tiles[gw];
-  const NetDev& d = nets[bt.net];
+  if (gw >= n_words_total) return;
+  const BulkWord bw = words[gw];
+  const NetDev& d = nets[bw.net];
   const RunCtl c = load_ctl(d.ctl);
   const BulkStep st = bulk_step(d, c, s);
   if (!st.live) return;
-  const int N = d.N, Nin = d.Nin, KL = d.KL, L = d.L, B = d.B, kind = d.kind, TS = d.TS, ITS = d.ITS;
-  const int p0 = bt.tile * TS, kin0 = bt.tile * ITS;
-  const float half_dt = 0.5f * d.dt;
-  int g_first = 0, g_last = 0;
-  {
-    const int n_hi = min(p0 + TS, N) - 1;
-    while (g_first + 1 < d.n_groups && p0 >= d.groups[g_first].end) ++g_first;
-    g_last = g_first;
-    while (g_last + 1 < d.n_groups && n_hi >= d.groups[g_last].end) ++g_last;
-  }
-  const GroupConst G0 = d.groups[g_first];
-  float* ring_slot = d.ring + ((size_t)bt.tile * B + st.slot) * TS * L;
+  const int KL = d.KL;
   float* pub = d.pre_pub;
-  for (int base = 0; base < TS; base += 32) {
-    const int li = base + lane;
-    const int n = p0 + li;
-    bool spk = false;
-    if (n < N) {
-      GroupConst G = G0;
-      if (g_last != g_first) {
-        int gi = g_first;
-        while (gi < g_last && n >= d.groups[gi].end) ++gi;
-        G = d.groups[gi];
-      }
-      float Vi = d.V[n];
-      float lastn = d.last[n];
-      float input;
-      if (kind == SPK_SYN_CONDUCTANCE) {
-        float total = 0.0f;
-        for (int l = 0; l < L; ++l) {
-          const float cell = ring_slot[li * L + l];
-          ring_slot[li * L + l] = 0.0f;
-          const float gnew = d.decay[l] * d.gtr[(size_t)n * L + l] + cell;
-          total = total + gnew * (d.vhat[l] - Vi);
-          d.gtr[(size_t)n * L + l] = gnew;
+  if (bw.word * 32 >= KL) {
+    const int N = d.N, L = d.L, B = d.B, TS = d.TS, kind = d.kind;
+    float Vv[BULK_WPW], lv[BULK_WPW], inv[BULK_WPW], pov[BULK_WPW], prv[BULK_WPW];
+    // phase 1: every word's loads in flight at once
+#pragma unroll
+    for (int u = 0; u < BULK_WPW; ++u) {
+      Vv[u] = lv[u] = inv[u] = pov[u] = prv[u] = 0.0f;
+      const int n = (bw.word + u) * 32 + lane - KL;
+      if (u < bw.count && n < N) {
+        Vv[u] = d.V[n];
+        lv[u] = d.last[n];
+        if (kind == SPK_SYN_VOLTAGE) {
+          const int tile = n / TS, li = n - tile * TS;
+          const float* cell = d.ring + ((size_t)tile * B + st.slot) * TS * L + (size_t)li * L;
+          float total = 0.0f;
+          for (int l = 0; l < L; ++l) total = total + cell[l];
+          inv[u] = total;
         }
-        input = total * G.kR;
-      } else if (kind == SPK_SYN_CURRENT) {
-        float total = 0.0f;
-        for (int l = 0; l < L; ++l) {
-          const float cell = ring_slot[li * L + l];
-          ring_slot[li * L + l] = 0.0f;
-          float inew = d.gtr[(size_t)n * L + l] * d.decay[l];
-          inew = inew + cell;
-          total = total + inew;
-          d.gtr[(size_t)n * L + l] = inew;
-        }
-        input = total * G.kR;
-      } else {
-        float total = 0.0f;
-        for (int l = 0; l < L; ++l) {
-          total = total + ring_slot[li * L + l];
-          ring_slot[li * L + l] = 0.0f;
-        }
-        input = total;
-      }
-      if (((st.tg - lastn) - d.t_ref) > half_dt) {
-        Vi = G.k * G.v0 + (1.0f - G.k) * Vi + G.k * d.i_bg + input;
-        if (Vi >= G.theta) {
-          spk = true;
-          d.last[n] = st.tg;
-          Vi = G.vreset;
+        if (st.stdp_run) {
+          pov[u] = d.post_trace[n];
+          prv[u] = d.pre_trace[KL + n];
         }
       }
-      d.V[n] = Vi;
-      if (st.stdp_run) {
-        float po = d.post_trace[n] * d.E_m;
-        po = po + (spk ? d.inc_m : 0.0f);
-        d.post_trace[n] = po;
-        float pr = d.pre_trace[KL + n] * d.E_p;
-        pr = pr + (spk ? d.inc_p : 0.0f);
-        d.pre_trace[KL + n] = pr;
-        pub[KL + n] = pr;
+    }
+    // phase 2: updates, traces, spike words
+#pragma unroll
+    for (int u = 0; u < BULK_WPW; ++u) {
+      if (u >= bw.count) break;
+      const int key = (bw.word + u) * 32 + lane;
+      const int n = key - KL;
+      bool spk = false;
+      if (n < N) {
+        const int tile = n / TS, li = n - tile * TS;
+        float* cell = d.ring + ((size_t)tile * B + st.slot) * TS * L + (size_t)li * L;
+        spk = bulk_lif(d, st, n, key, Vv[u], lv[u], cell, inv[u]);
+        if (kind == SPK_SYN_VOLTAGE)
+          for (int l = 0; l < L; ++l) cell[l] = 0.0f;
+        if (st.stdp_run) {
+          float po = pov[u] * d.E_m;
+          po = po + (spk ? d.inc_m : 0.0f);
+          d.post_trace[n] = po;
+          float pr = prv[u] * d.E_p;
+          pr = pr + (spk ? d.inc_p : 0.0f);
+          d.pre_trace[key] = pr;
+          pub[key] = pr;
+        }
+      }
+      const unsigned word = __ballot_sync(FULL, spk);
+      if (lane == 0) {
+        d.bitsA[bw.word + u] = word;
+        d.bitsP[bw.word + u] = st.stdp_run ? word : 0u;
       }
     }
-    const unsigned word = __ballot_sync(FULL, spk);
-    if (lane == 0) {
-      const int wi = ((KL + p0) >> 5) + (base >> 5);
-      d.bitsA[wi] = word;
-      d.bitsP[wi] = st.stdp_run ? word : 0u;
-    }
-    if (spk) {
-      // the row pointers and synapse row of the spiking key, into L2 for the
-      // propagation kernel
-      const int key = KL + n;
-      const int r0 = __ldg(d.rowptr + (size_t)key * d.n_tiles), r1 = __ldg(d.rowptr + (size_t)(key + 1) * d.n_tiles);
-      prefetch_l2(d.rowptr + (size_t)key * d.n_tiles, sizeof(int) * (size_t)(d.n_tiles + 1));
-      if (r1 > r0) prefetch_l2(d.entries + r0, sizeof(uint2) * (size_t)(r1 - r0));
-    }
-  }
-  for (int base = 0; base < ITS; base += 32) {
-    const int li = base + lane;
-    const int k = kin0 + li;
-    bool spk = false, pev = false;
-    if (k < Nin) {
-      const int idx = Nin - 1 - k;
-      float nx = d.in_next[idx];
-      if ((nx <= st.tg) || !st.inputs_active) {
-        const float rate = d.rates[idx];
-        const float u = draw_uniform(d.seed, (uint32_t)idx, (uint32_t)st.T, DOMAIN_POISSON);
-        nx = st.tg - (1.0f / rate) * logf_spk(u);
-        if (st.inputs_active) spk = true;
-      }
-      d.in_next[idx] = nx;
-      if (st.stdp_run) {
-        int pg = (int)roundf((nx - st.t) / d.dt);
-        if (pg >= 1) pg *= -1;
-        pev = pg >= 0;
-        float pr = d.pre_trace[k] * d.E_p;
-        pr = pr + (pev ? d.inc_p : 0.0f);
-        d.pre_trace[k] = pr;
-        pub[k] = pr;
+  } else {
+    // Poisson inputs (same operations as the persistent kernel)
+    const int Nin = d.Nin;
+    float nxv[BULK_WPW], rtv[BULK_WPW], prv[BULK_WPW];
+#pragma unroll
+    for (int u = 0; u < BULK_WPW; ++u) {
+      nxv[u] = rtv[u] = prv[u] = 0.0f;
+      const int key = (bw.word + u) * 32 + lane;
+      if (u < bw.count && key < Nin) {
+        nxv[u] = d.in_next[Nin - 1 - key];
+        rtv[u] = d.rates[Nin - 1 - key];
+        if (st.stdp_run) prv[u] = d.pre_trace[key];
       }
     }
-    const unsigned wa = __ballot_sync(FULL, spk);
-    const unsigned wp = __ballot_sync(FULL, pev);
-    if (lane == 0) {
-      const int wi = (kin0 >> 5) + (base >> 5);
-      d.bitsA[wi] = wa;
-      d.bitsP[wi] = wp;
-    }
-    if (spk || pev) {
-      const int r0 = __ldg(d.rowptr + (size_t)k * d.n_tiles), r1 = __ldg(d.rowptr + (size_t)(k + 1) * d.n_tiles);
-      prefetch_l2(d.rowptr + (size_t)k * d.n_tiles, sizeof(int) * (size_t)(d.n_tiles + 1));
-      if (r1 > r0) prefetch_l2(d.entries + r0, sizeof(uint2) * (size_t)(r1 - r0));
+#pragma unroll
+    for (int u = 0; u < BULK_WPW; ++u) {
+      if (u >= bw.count) break;
+      const int key = (bw.word + u) * 32 + lane;
+      bool spk = false, pev = false;
+      if (key < Nin) {
+        const int idx = Nin - 1 - key;
+        float nx = nxv[u];
+        if ((nx <= st.tg) || !st.inputs_active) {
+          const float u01 = draw_uniform(d.seed, (uint32_t)idx, (uint32_t)st.T, DOMAIN_POISSON);
+          nx = st.tg - (1.0f / rtv[u]) * logf_spk(u01);
+          if (st.inputs_active) spk = true;
+        }
+        d.in_next[idx] = nx;
+        if (st.stdp_run) {
+          int pg = (int)roundf((nx - st.t) / d.dt);
+          if (pg >= 1) pg *= -1;
+          pev = pg >= 0;
+          float pr = prv[u] * d.E_p;
+          pr = pr + (pev ? d.inc_p : 0.0f);
+          d.pre_trace[key] = pr;
+          pub[key] = pr;
+        }
+      }
+      const unsigned wa = __ballot_sync(FULL, spk);
+      const unsigned wp = __ballot_sync(FULL, pev);
+      if (lane == 0) {
+        d.bitsA[bw.word + u] = wa;
+        d.bitsP[bw.word + u] = wp;
+      }
     }
   }
 }

@@ -222,6 +222,8 @@ struct spk_batch {
   std::vector<NetDev> hds;       // host copies of the batch's descriptors
   BulkTile* dtiles = nullptr;    // [tiles_total]
   int tiles_total = 0;
+  BulkWord* dwords = nullptr;    // [words_total] runs of 32-key words with real keys
+  int words_total = 0;
   void* bulk_mem = nullptr;      // tiles, step lists and counts
   cudaGraphExec_t bulk_graph = nullptr;  // one block of K timesteps
 };
@@ -1837,7 +1839,8 @@ static int bulk_launch_block(spk_batch* b) {
   const int wpb = 256 / 32;
   const int prop_smem = BULK_PROP_WARPS * bulk_warp_layout().total * 4;
   for (int s = 0; s < b->K; ++s) {
-    bulk_neurons_kernel<<<(T + wpb - 1) / wpb, 256, 0, b->stream>>>(b->dd, b->dtiles, T, s);
+    bulk_neurons_kernel<<<(b->words_total + wpb - 1) / wpb, 256, 0, b->stream>>>(b->dd, b->dwords,
+                                                                                  b->words_total, s);
     bulk_list_kernel<<<n, BULK_LIST_THREADS, 0, b->stream>>>(b->dd, s);
     bulk_prop_kernel<<<(T + BULK_PROP_WARPS - 1) / BULK_PROP_WARPS, BULK_PROP_WARPS * 32, prop_smem, b->stream>>>(
         b->dd, b->dtiles, T, s);
@@ -1932,15 +1935,23 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
   return guarded([&]() -> int {
     if (!b->bulk_mem) {
       std::vector<BulkTile> tiles;
+      std::vector<BulkWord> words;
       size_t list_words = 0;
       for (size_t i = 0; i < b->nets.size(); ++i) {
-        for (int t = 0; t < b->nets[i]->plan.n_tiles; ++t) tiles.push_back(BulkTile{(int)i, t});
-        list_words += (size_t)b->nets[i]->plan.n_keys;
+        const spk_net* n = b->nets[i];
+        for (int t = 0; t < n->plan.n_tiles; ++t) tiles.push_back(BulkTile{(int)i, t});
+        const int in_end = (n->Nin + 31) / 32, lif0 = n->plan.KL / 32, lif_end = (n->plan.KL + n->N + 31) / 32;
+        for (int w = 0; w < in_end; w += BULK_WPW)
+          words.push_back(BulkWord{(int)i, w, std::min(BULK_WPW, in_end - w), 0});
+        for (int w = lif0; w < lif_end; w += BULK_WPW)
+          words.push_back(BulkWord{(int)i, w, std::min(BULK_WPW, lif_end - w), 0});
+        list_words += (size_t)n->plan.n_keys;
       }
       const size_t t_bytes = align_up(sizeof(BulkTile) * tiles.size(), 256);
+      const size_t w_bytes = align_up(sizeof(BulkWord) * words.size(), 256);
       const size_t l_bytes = align_up(sizeof(uint32_t) * list_words, 256);
       const size_t c_bytes = align_up(sizeof(int) * b->nets.size(), 256);
-      if (cudaMalloc(&b->bulk_mem, t_bytes + l_bytes + c_bytes) != cudaSuccess) {
+      if (cudaMalloc(&b->bulk_mem, t_bytes + w_bytes + l_bytes + c_bytes) != cudaSuccess) {
         cudaGetLastError();
         b->bulk_mem = nullptr;
         set_error("bulk mode: device allocation failed");
@@ -1948,8 +1959,10 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       }
       b->dtiles = (BulkTile*)b->bulk_mem;
       b->tiles_total = (int)tiles.size();
-      uint32_t* lists = (uint32_t*)((char*)b->bulk_mem + t_bytes);
-      int* counts = (int*)((char*)b->bulk_mem + t_bytes + l_bytes);
+      b->dwords = (BulkWord*)((char*)b->bulk_mem + t_bytes);
+      b->words_total = (int)words.size();
+      uint32_t* lists = (uint32_t*)((char*)b->bulk_mem + t_bytes + w_bytes);
+      int* counts = (int*)((char*)b->bulk_mem + t_bytes + w_bytes + l_bytes);
       size_t off = 0;
       for (size_t i = 0; i < b->nets.size(); ++i) {
         b->hds[i].step_list = lists + off;
@@ -1957,6 +1970,14 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
         off += (size_t)b->nets[i]->plan.n_keys;
       }
       SPK_CUDA(cudaMemcpy(b->dtiles, tiles.data(), sizeof(BulkTile) * tiles.size(), cudaMemcpyHostToDevice));
+      SPK_CUDA(cudaMemcpy(b->dwords, words.data(), sizeof(BulkWord) * words.size(), cudaMemcpyHostToDevice));
+      // words of padding keys are never written in bulk mode: zero them once
+      SPK_CUDA(cudaStreamSynchronize(b->stream));
+      for (const spk_net* n : b->nets) {
+        SPK_CUDA(cudaStreamSynchronize(n->stream));
+        SPK_CUDA(cudaMemset(n->hd.bitsA, 0, sizeof(uint32_t) * 2 * (size_t)n->hd.n_words));
+        SPK_CUDA(cudaMemset(n->hd.bitsP, 0, sizeof(uint32_t) * 2 * (size_t)n->hd.n_words));
+      }
       SPK_CUDA(cudaMemcpy(b->dd, b->hds.data(), sizeof(NetDev) * b->hds.size(), cudaMemcpyHostToDevice));
       SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     BULK_PROP_WARPS * bulk_warp_layout().total * 4));
