@@ -64,6 +64,8 @@ def parse():
     p.add_argument("--instances", type=int, default=256, help="batched: network instances")
     p.add_argument("--scale", type=float, default=1.0, help="plastic_ff: network size factor (profiling cases)")
     p.add_argument("--tune-steps", type=int, default=100, help="batched: autotuner trial timesteps")
+    p.add_argument("--mode", default="auto", choices=["auto", "waves", "bulk"],
+                   help="batched: execution mode (auto: the autotuner's choice; waves without the autotuner)")
     p.add_argument("--no-tune", action="store_true",
                    help="batched: skip the autotuner (8 warps, tiles of up to 64 posts, costs from synapse counts)")
     p.add_argument("--plain-block", type=int, default=200,
@@ -523,7 +525,8 @@ def run_batched(args, rank, world, local):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import __graft_entry__
     __graft_entry__.build()
-    from spike_gb300 import Batch, Net, networks
+    from spike_gb300 import Batch, Net, networks, schedule
+    from spike_gb300 import _native as N
 
     def barrier():
         torch.cuda.synchronize()
@@ -532,20 +535,25 @@ def run_batched(args, rank, world, local):
 
     gens = networks.batched_sweep(args.instances)
     t0 = time.perf_counter()
+    mode = N.SPK_BATCH_WAVES
     if args.no_tune:
-        from spike_gb300 import schedule
         scheds = [schedule(8, min(64, max(32, -(-(-(-g.desc.n_neurons // 8)) // 32) * 32)), 0, 0) for g in gens]
         tune_ms = None
         nets = [Net.generate(g, s) for g, s in zip(gens, scheds)]
         costs = [float(n.synapse_count()) * (2.0 if g.desc.has_stdp else 1.0) for n, g in zip(nets, gens)]
     else:
-        scheds, tune_ms, costs = Batch.autotune(gens, trial_steps=args.tune_steps, costs=True)
+        scheds, tune_ms, costs, mode = Batch.autotune(gens, trial_steps=args.tune_steps, costs=True,
+                                                      with_mode=True)
         nets = [Net.generate(g, s) for g, s in zip(gens, scheds)]
     tune_s = time.perf_counter() - t0
     for n, c in zip(nets, costs):
-        n.set_step_cost(c)
+        if c > 0:
+            n.set_step_cost(c)
     n_syn = sum(n.synapse_count() for n in nets)
-    b = Batch(nets)
+    b = Batch(nets, schedule(0, 0, 0, args.block))
+    if args.mode != "auto":
+        mode = N.SPK_BATCH_BULK if args.mode == "bulk" else N.SPK_BATCH_WAVES
+    b.set_mode(mode)
     stream = torch.cuda.ExternalStream(b.stream())
     n_neurons = sum(g.desc.n_neurons for g in gens)
     n_inputs = sum(g.desc.n_inputs for g in gens)
@@ -661,8 +669,9 @@ def run_batched(args, rank, world, local):
             "data": "synthetic", "impl": "ours",
             "config": {**batched_config(gens, n_syn), "block_timesteps": args.block,
                        "schedules": sch, "autotune_s": round(tune_s, 2), "autotune_trial_ms": tune_ms,
-                       "waves_per_block": launches / max(1, args.steps * -(-args.block // 1000)),
+                       "launches_per_block": launches / max(1, args.steps),
                        "autotuned": not args.no_tune,
+                       "mode": "bulk" if mode == N.SPK_BATCH_BULK else "waves",
                        "l2": f"synapse entries {8 * n_syn / 1e9:.1f} GB > 129 MB L2 (no flush)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "sim_s_per_wall_s": len(nets) * sim_s / elapsed,

@@ -334,15 +334,17 @@ int spk_batch_stream(const spk_batch* batch, void** stream);
 int spk_batch_destroy(spk_batch* batch);
 /* Measured schedule search for a batch of generated networks (batching has
  * no counterpart in the reference).  Tries a fixed set of policies (warps per
- * CTA, largest tile), builds and packs the networks under each, times
- * trial_steps steps of the batch and writes the fastest policy's schedule of
- * every network to schedules[n_nets] (and its trial time to best_ms, which
- * may be NULL).  With step_us (may be NULL) it also times each network alone
+ * CTA, largest tile), builds the networks under each, times trial_steps steps
+ * of the batch in both execution modes (spk_batch_set_mode) and writes the
+ * fastest policy's schedule of every network to schedules[n_nets], its trial
+ * time to best_ms and its mode to best_mode (both may be NULL).  With step_us
+ * (may be NULL) and the waves mode chosen it also times each network alone
  * under its schedule and writes microseconds per step, for
- * spk_net_set_step_cost.  Results never depend on the schedule.  Destroy a
- * batch before the networks it holds. */
+ * spk_net_set_step_cost (zeros for the bulk mode, which packs no waves).
+ * Results never depend on the schedule or the mode.  Destroy a batch before
+ * the networks it holds. */
 int spk_batch_autotune(const spk_gen_desc* descs, int32_t n_nets, int32_t trial_steps,
-                       spk_schedule* schedules, float* best_ms, float* step_us);
+                       spk_schedule* schedules, float* best_ms, float* step_us, int32_t* best_mode);
 /* Cost of one step of the network (any unit, e.g. the step_us above).  A
  * batch orders its networks by decreasing cost into its co-resident waves, so
  * that each wave - which lasts as long as its slowest member - holds networks
@@ -369,7 +371,7 @@ typedef struct spk_server_opts {
   int32_t max_running;     /* running jobs at most (0 = 512)                       */
   uint64_t reserve_bytes;  /* device memory kept free (0 = 8 GiB)                  */
   int32_t record_spikes;   /* keep each finished job's neuron spikes on the host   */
-  int32_t reserved;
+  int32_t mode;            /* batch execution mode, SPK_BATCH_WAVES (0) or _BULK    */
 } spk_server_opts;
 
 #define SPK_JOB_QUEUED 0

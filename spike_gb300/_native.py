@@ -100,7 +100,7 @@ class GenDesc(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("warps_per_cta", i32), ("tile_posts", i32), ("steps_per_block", i32), ("max_running", i32),
-                ("reserve_bytes", u64), ("record_spikes", i32), ("reserved", i32)]
+                ("reserve_bytes", u64), ("record_spikes", i32), ("mode", i32)]
 
 
 class JobInfo(C.Structure):
@@ -203,7 +203,7 @@ _SIGS = {
     "spk_batch_launch_count": (i32, [_VP, P(i64)]),
     "spk_batch_stream": (i32, [_VP, P(_VP)]),
     "spk_batch_destroy": (i32, [_VP]),
-    "spk_batch_autotune": (i32, [P(GenDesc), i32, i32, P(Schedule), P(f32), P(f32)]),
+    "spk_batch_autotune": (i32, [P(GenDesc), i32, i32, P(Schedule), P(f32), P(f32), P(i32)]),
     "spk_net_set_step_cost": (i32, [_VP, f32]),
     "spk_step_noalloc": (i32, [P(DeviceNet), i64, i32, f32, _VP]),
     "spk_server_start": (i32, [P(ServerOpts), P(_VP)]),

@@ -2420,6 +2420,8 @@ static int policy_schedules(const spk_gen_desc* descs, int n, const TunePolicy& 
   return SPK_OK;
 }
 
+// Times `steps` timesteps of the networks under schedules `sch` as one batch,
+// in waves mode (ms[0]) and in bulk mode (ms[1]).
 static int trial_policy(const spk_gen_desc* descs, int n, const std::vector<spk_schedule>& sch, int steps,
                         float* ms) {
   std::vector<spk_net*> nets(n, nullptr);
@@ -2431,18 +2433,21 @@ static int trial_policy(const spk_gen_desc* descs, int n, const std::vector<spk_
   };
   int rc = SPK_OK;
   for (int i = 0; i < n && rc == SPK_OK; ++i) rc = generate_impl(&descs[i], &sch[i], &nets[i]);
-  if (rc == SPK_OK) rc = spk_batch_create(nets.data(), n, nullptr, &b);
+  const spk_schedule bs{0, 0, 0, steps};  // one launch block per trial
+  if (rc == SPK_OK) rc = spk_batch_create(nets.data(), n, &bs, &b);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (rc == SPK_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) rc = SPK_ERR_CUDA;
-  if (rc == SPK_OK) rc = spk_batch_run_steps(b, std::max(1, steps / 2), 1);
-  if (rc == SPK_OK && cudaStreamSynchronize(b->stream) != cudaSuccess) rc = SPK_ERR_CUDA;
-  if (rc == SPK_OK) {
+  for (int mode = SPK_BATCH_WAVES; mode <= SPK_BATCH_BULK && rc == SPK_OK; ++mode) {
+    rc = spk_batch_set_mode(b, mode);
+    if (rc == SPK_OK) rc = spk_batch_run_steps(b, steps, 1);  // warm-up (and graph capture)
+    if (rc == SPK_OK && cudaStreamSynchronize(b->stream) != cudaSuccess) rc = SPK_ERR_CUDA;
+    if (rc != SPK_OK) break;
     cudaEventRecord(e0, b->stream);
     rc = spk_batch_run_steps(b, steps, 1);
     cudaEventRecord(e1, b->stream);
     if (rc == SPK_OK && cudaEventSynchronize(e1) != cudaSuccess) rc = SPK_ERR_CUDA;
     if (rc == SPK_OK) {
-      cudaEventElapsedTime(ms, e0, e1);
+      cudaEventElapsedTime(&ms[mode], e0, e1);
       rc = spk_batch_synchronize(b);
     }
   }
@@ -2489,7 +2494,7 @@ static int measure_alone(const spk_gen_desc* descs, int n, const std::vector<spk
 }
 
 extern "C" int spk_batch_autotune(const spk_gen_desc* descs, int32_t n_nets, int32_t trial_steps,
-                                  spk_schedule* schedules, float* best_ms, float* step_us) {
+                                  spk_schedule* schedules, float* best_ms, float* step_us, int32_t* best_mode) {
   using namespace spk;
   if (!descs || n_nets < 1 || !schedules || trial_steps < 1) return SPK_ERR_INVALID;
   return guarded([&]() -> int {
@@ -2498,23 +2503,30 @@ extern "C" int spk_batch_autotune(const spk_gen_desc* descs, int32_t n_nets, int
     if (rc) return rc;
     static const TunePolicy policies[] = {{8, 32}, {8, 64}, {8, 128}, {8, 256}, {4, 128}};
     float best = -1.0f;
+    int mode = SPK_BATCH_WAVES;
     std::vector<spk_schedule> sch, best_sch;
     int last_rc = SPK_ERR_UNSUPPORTED;
     for (const TunePolicy& pol : policies) {
       if (policy_schedules(descs, n_nets, pol, di, sch) != SPK_OK) continue;
-      float ms = 0.0f;
-      last_rc = trial_policy(descs, n_nets, sch, trial_steps, &ms);
+      float ms[2] = {0.0f, 0.0f};
+      last_rc = trial_policy(descs, n_nets, sch, trial_steps, ms);
       if (last_rc == SPK_ERR_TIMEOUT || last_rc == SPK_ERR_CUDA) return last_rc;
       if (last_rc != SPK_OK) continue;
-      if (best < 0.0f || ms < best) {
-        best = ms;
-        best_sch = sch;
-      }
+      for (int m = SPK_BATCH_WAVES; m <= SPK_BATCH_BULK; ++m)
+        if (best < 0.0f || ms[m] < best) {
+          best = ms[m];
+          best_sch = sch;
+          mode = m;
+        }
     }
     if (best < 0.0f) return last_rc;
     std::copy(best_sch.begin(), best_sch.end(), schedules);
     if (best_ms) *best_ms = best;
-    if (step_us) return measure_alone(descs, n_nets, best_sch, trial_steps, step_us);
+    if (best_mode) *best_mode = mode;
+    if (step_us) {
+      if (mode == SPK_BATCH_WAVES) return measure_alone(descs, n_nets, best_sch, trial_steps, step_us);
+      std::fill(step_us, step_us + n_nets, 0.0f);  // bulk mode packs no waves
+    }
     return SPK_OK;
   });
 }

@@ -229,7 +229,8 @@ void loop(spk_server* S) {
       std::vector<spk_net*> nets;
       for (Job* j : run) nets.push_back(j->net);
       const spk_schedule bs{0, 0, 0, K};
-      const int rc = spk_batch_create(nets.data(), (int32_t)nets.size(), &bs, &batch);
+      int rc = spk_batch_create(nets.data(), (int32_t)nets.size(), &bs, &batch);
+      if (rc == SPK_OK && S->o.mode == SPK_BATCH_BULK) rc = spk_batch_set_mode(batch, SPK_BATCH_BULK);
       if (rc != SPK_OK) {
         for (Job* j : run) finish(S, j, rc);
         run.clear();
@@ -326,7 +327,8 @@ int spk_server_start(const spk_server_opts* opts, spk_server** out) {
     if (S->o.steps_per_block <= 0) S->o.steps_per_block = 1000;
     if (S->o.max_running <= 0) S->o.max_running = 512;
     if (S->o.reserve_bytes == 0) S->o.reserve_bytes = 8ull << 30;
-    if (S->o.tile_posts % 32 || S->o.warps_per_cta > 16) {
+    if (S->o.tile_posts % 32 || S->o.warps_per_cta > 16 ||
+        (S->o.mode != SPK_BATCH_WAVES && S->o.mode != SPK_BATCH_BULK)) {
       delete S;
       return SPK_ERR_INVALID;
     }

@@ -373,19 +373,24 @@ class Batch:
         check(lib().spk_batch_set_mode(self.h, mode), "spk_batch_set_mode")
 
     @staticmethod
-    def autotune(gens: list, trial_steps: int = 200, costs: bool = False):
+    def autotune(gens: list, trial_steps: int = 200, costs: bool = False, with_mode: bool = False):
         """Measured schedule search (spk_batch_autotune) for generated
         networks: returns (schedules, trial milliseconds of the best policy),
-        plus each network's microseconds per step alone when costs=True."""
+        plus each network's microseconds per step alone when costs=True, plus
+        the best execution mode when with_mode=True."""
         descs = (N.GenDesc * len(gens))(*[g.desc for g in gens])
         out = (N.Schedule * len(gens))()
         ms = C.c_float()
+        mode = C.c_int32()
         us = (C.c_float * len(gens))() if costs else None
-        check(lib().spk_batch_autotune(descs, len(gens), trial_steps, out, C.byref(ms), us), "spk_batch_autotune")
-        scheds = [N.Schedule(o.warps_per_cta, o.tile_posts, o.ctas, o.steps_per_launch) for o in out]
+        check(lib().spk_batch_autotune(descs, len(gens), trial_steps, out, C.byref(ms), us, C.byref(mode)),
+              "spk_batch_autotune")
+        res = [[N.Schedule(o.warps_per_cta, o.tile_posts, o.ctas, o.steps_per_launch) for o in out], ms.value]
         if costs:
-            return scheds, ms.value, [float(x) for x in us]
-        return scheds, ms.value
+            res.append([float(x) for x in us])
+        if with_mode:
+            res.append(mode.value)
+        return tuple(res)
 
     def run_steps(self, steps: int, plasticity_on: bool = True):
         check(lib().spk_batch_run_steps(self.h, steps, 1 if plasticity_on else 0), "spk_batch_run_steps")
@@ -557,9 +562,9 @@ class Server:
     runs them together in step blocks and keeps each job's results."""
 
     def __init__(self, warps_per_cta=0, tile_posts=0, steps_per_block=0, max_running=0, reserve_bytes=0,
-                 record_spikes=True):
+                 record_spikes=True, mode=N.SPK_BATCH_WAVES):
         o = N.ServerOpts(warps_per_cta, tile_posts, steps_per_block, max_running, reserve_bytes,
-                         1 if record_spikes else 0, 0)
+                         1 if record_spikes else 0, mode)
         self.h = C.c_void_p()
         check(lib().spk_server_start(C.byref(o), C.byref(self.h)), "spk_server_start")
         self._keep = {}

@@ -27,13 +27,16 @@ def snapshot(net: Net, n: int, n_in: int, S: int):
 
 def test_autotuned_batch_equals_each_instance_alone():
     gens = small_sweep()
-    scheds, ms, costs = Batch.autotune(gens, trial_steps=60, costs=True)
-    assert ms > 0 and len(scheds) == len(gens) and all(c > 0 for c in costs)
+    scheds, ms, costs, mode = Batch.autotune(gens, trial_steps=60, costs=True, with_mode=True)
+    assert ms > 0 and len(scheds) == len(gens) and mode in (N.SPK_BATCH_WAVES, N.SPK_BATCH_BULK)
+    assert all(c > 0 for c in costs) if mode == N.SPK_BATCH_WAVES else all(c == 0 for c in costs)
     batched = [Net.generate(g, s) for g, s in zip(gens, scheds)]
     for n, c in zip(batched, costs):
-        n.set_step_cost(c)
+        if c > 0:
+            n.set_step_cost(c)
     alone = [Net.generate(g, s) for g, s in zip(gens, scheds)]
     b = Batch(batched)
+    b.set_mode(mode)
     for plastic, steps in ((True, 700), (False, 300)):
         b.run_steps(steps, plastic)
         for n in alone:

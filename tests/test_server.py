@@ -25,9 +25,10 @@ def jobs(k=8, seed=9):
     return out
 
 
-def test_served_jobs_equal_each_job_alone_and_overlap():
+@pytest.mark.parametrize("mode", [N.SPK_BATCH_WAVES, N.SPK_BATCH_BULK])
+def test_served_jobs_equal_each_job_alone_and_overlap(mode):
     work = jobs()
-    srv = Server(steps_per_block=250, reserve_bytes=1 << 30)
+    srv = Server(steps_per_block=250, reserve_bytes=1 << 30, mode=mode)
     ids = []
     for i, (gen, steps, plastic) in enumerate(work):
         ids.append(srv.submit(gen, steps, plastic))
