@@ -597,14 +597,20 @@ def run_batched(args, rank, world, local):
     trace_keys = sum(g.desc.n_neurons + g.desc.n_inputs for g in gens if g.desc.has_stdp)
     alg = algorithmic_bytes(events, pre_u, post_u, n_neurons * timesteps, n_inputs * timesteps, 1,
                             trace_keys * timesteps)
-    per_launch_s = (ms / 1000.0) / max(launches, 1)
-    per_launch_bytes = alg / max(launches, 1)
+    bulk = mode == N.SPK_BATCH_BULK
+    # waves: one launch of the persistent kernel per wave and block; bulk: the
+    # unit is one timestep of all instances (three kernels)
+    units = timesteps if bulk else max(launches, 1)
+    per_launch_s = (ms / 1000.0) / units
+    per_launch_bytes = alg / units
     peak, peak_kind = peaks()
     achieved = per_launch_bytes / per_launch_s / 1e9
-    tr = traffic_per_launch("batched")
+    tr = traffic_per_launch("batched_bulk" if bulk else "batched")
     traffic = None
     if tr and tr.get("traffic_per_alg_byte"):
         traffic = tr["traffic_per_alg_byte"] * per_launch_bytes
+    roof_kernel = ("spk::bulk_neurons_kernel + bulk_list_kernel + bulk_prop_kernel (one timestep of all instances)"
+                   if bulk else "spk::step_kernel")
 
     # plain form: the same instances, each alone on its own stream, one after another
     plain_ev, plain_ms = 0, 0.0
@@ -680,7 +686,7 @@ def run_batched(args, rank, world, local):
             "status": status,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "spk::step_kernel", "launches": launches,
+                         "kernel": roof_kernel, "launches": launches, "unit_timed": "timestep" if bulk else "launch",
                          "alg_bytes_per_launch": per_launch_bytes, "ms_per_launch": 1000 * per_launch_s},
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clk.summary(),
             "gpu_launches": launches + args.steps * len(nets),
