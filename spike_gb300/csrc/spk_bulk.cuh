@@ -17,12 +17,14 @@
 //   bulk_prop_kernel     one warp per tile: the list's sub-rows of the tile
 //                        staged and applied in canonical order into the tile's
 //                        ring cells in HBM (the persistent kernel's rounds),
-//                        with the STDP pre pass, then the tile's post-spike
-//                        afferent pass.
+//                        with the STDP pre pass;
+//   bulk_post_kernel     the post-spike afferent pass of every spiking post of
+//                        every network, in chunks of 128 afferents spread over
+//                        all warps (the list kernel builds the items).
 //
 // Each ring cell still has one writer applying contributions in canonical
 // order, and every float operation is the persistent kernel's, so a network
-// gives the same bits in both modes.  A block of K timesteps is 3K launches
+// gives the same bits in both modes.  A block of K timesteps is 4K launches
 // plus one that advances the networks' run counters, captured in a CUDA graph.
 #pragma once
 
@@ -31,7 +33,18 @@
 #include "spk_internal.h"
 #include "spk_kernel.cuh"
 
+// Tuning constants (measured on the 256-instance sweep): keys per round of the
+// propagation kernel, words per warp of the neuron kernel.
+#ifndef SPK_BULK_STAGE_KEYS
+#define SPK_BULK_STAGE_KEYS 64
+#endif
+#ifndef SPK_BULK_WPW
+#define SPK_BULK_WPW 4
+#endif
+
 namespace spk {
+
+constexpr int BULK_STAGE_KEYS = SPK_BULK_STAGE_KEYS;
 
 struct BulkTile {
   int net;   // index into the batch's NetDev array
@@ -80,7 +93,7 @@ __device__ __forceinline__ RunCtl load_ctl(const RunCtl* p) {
 // once per word.  Words of padding keys are never written: they stay zero
 // from set-up.  No L2 prefetch of the spiking rows here: a batch's rows of one
 // step exceed the L2.
-constexpr int BULK_WPW = 8;
+constexpr int BULK_WPW = SPK_BULK_WPW;
 
 struct BulkWord {
   int net;    // index into the batch's NetDev array
@@ -138,7 +151,8 @@ __device__ __forceinline__ bool bulk_lif(const NetDev& d, const BulkStep& st, in
 
 __global__ void __launch_bounds__(256) bulk_neurons_kernel(const NetDev* __restrict__ nets,
                                                            const BulkWord* __restrict__ words, int n_words_total,
-                                                           int s) {
+                                                           int s, int* item_count) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *item_count = 0;  // the afferent-pass list of this step
   const int lane = threadIdx.x & 31;
   const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (gw >= n_words_total) return;
@@ -256,9 +270,18 @@ __global__ void __launch_bounds__(256) bulk_neurons_kernel(const NetDev* __restr
 // gives every key its place in ascending key order.
 constexpr int BULK_LIST_THREADS = 512;
 
-__global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetDev* __restrict__ nets, int s) {
+// Work item of the afferent pass: afferents [a0, a1) of spiking post `post`.
+struct BulkPostItem {
+  int net, post, a0, a1;
+};
+constexpr int BULK_POST_CHUNK = 128;  // afferents per item (32 lanes x 4)
+
+__global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetDev* __restrict__ nets, int s,
+                                                                      BulkPostItem* items, int* item_count,
+                                                                      int item_cap) {
   __shared__ unsigned long long warp_tot[BULK_LIST_THREADS / 32];
   __shared__ unsigned long long s_base;
+  __shared__ int s_item_base;
   const NetDev& d = nets[blockIdx.x];
   const RunCtl c = load_ctl(d.ctl);
   const BulkStep st = bulk_step(d, c, s);
@@ -327,6 +350,106 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
     const unsigned long long sc = sc0 + (s_base >> 32);
     d.ctl->spike_count = sc > (unsigned long long)d.spike_cap ? (unsigned long long)d.spike_cap : sc;
   }
+  if (!st.stdp_run) return;
+  // afferent-pass items of the spiking posts: chunks of BULK_POST_CHUNK
+  // plastic afferents, reserved in the shared item list with one atomic
+  const int wl0 = max(w0, KL >> 5);
+  unsigned long long nch = 0;
+  for (int i = wl0; i < w1; ++i) {
+    uint32_t a = d.bitsA[i];
+    while (a) {
+      const int b = __ffs(a) - 1;
+      a &= a - 1;
+      const int q = (i << 5) + b - KL;
+      const int deg = __ldg(d.csc_ptr + q + 1) - __ldg(d.csc_ptr + q);
+      nch += (unsigned long long)((deg + BULK_POST_CHUNK - 1) / BULK_POST_CHUNK);
+    }
+  }
+  unsigned long long ic = nch;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(FULL, ic, o);
+    if (lane >= o) ic += y;
+  }
+  __syncthreads();
+  if (lane == 31) warp_tot[w] = ic;
+  __syncthreads();
+  if (w == 0) {
+    const unsigned long long v = lane < BULK_LIST_THREADS / 32 ? warp_tot[lane] : 0ull;
+    unsigned long long wi = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(FULL, wi, o);
+      if (lane >= o) wi += y;
+    }
+    if (lane < BULK_LIST_THREADS / 32) warp_tot[lane] = wi - v;
+    if (lane == 31) s_item_base = wi > 0 ? atomicAdd(item_count, (int)wi) : 0;
+  }
+  __syncthreads();
+  int ipos = s_item_base + (int)(warp_tot[w] + ic - nch);
+  for (int i = wl0; i < w1; ++i) {
+    uint32_t a = d.bitsA[i];
+    while (a) {
+      const int b = __ffs(a) - 1;
+      a &= a - 1;
+      const int q = (i << 5) + b - KL;
+      const int a0 = __ldg(d.csc_ptr + q), a1 = __ldg(d.csc_ptr + q + 1);
+      for (int x = a0; x < a1; x += BULK_POST_CHUNK) {
+        if (ipos < item_cap)
+          items[ipos] = BulkPostItem{(int)blockIdx.x, q, x, min(a1, x + BULK_POST_CHUNK)};
+        else
+          atomicCAS(&d.ctl->status, 0, SPK_ERR_OVERFLOW);
+        ++ipos;
+      }
+    }
+  }
+}
+
+// ---- timestep part 4: the post-spike afferent pass of every spiking post -----------------
+// Each warp takes items of the shared list in turn: up to BULK_POST_CHUNK
+// plastic afferents of one spiking post whose presynaptic key had no event
+// this step (those with an event were updated in the propagation kernel) get
+// their LTP update.  Each weight is updated at most once per step, so the
+// order of the items does not matter.
+__global__ void __launch_bounds__(256) bulk_post_kernel(const NetDev* __restrict__ nets,
+                                                        const BulkPostItem* __restrict__ items,
+                                                        const int* __restrict__ item_count, int item_cap) {
+  const int lane = threadIdx.x & 31;
+  const int n_items = min(*item_count, item_cap);
+  const int n_warps = gridDim.x * (blockDim.x >> 5);
+  for (int it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < n_items; it += n_warps) {
+    const BulkPostItem item = items[it];
+    const NetDev& d = nets[item.net];
+    const float post_tr = d.post_trace[item.post];
+    constexpr int AFF = BULK_POST_CHUNK / 32;
+    uint2 cc[AFF];
+#pragma unroll
+    for (int u = 0; u < AFF; ++u) {
+      const int ai = item.a0 + u * 32 + lane;
+      cc[u] = d.csc[ai < item.a1 ? ai : item.a0];
+    }
+    uint32_t vm[AFF];
+    float prt[AFF];
+#pragma unroll
+    for (int u = 0; u < AFF; ++u) {
+      const int pk = (int)cc[u].x;
+      vm[u] = d.bitsA[pk >> 5] | d.bitsP[pk >> 5];
+      prt[u] = d.pre_pub[pk];
+    }
+    unsigned long long n_post = 0;
+#pragma unroll
+    for (int u = 0; u < AFF; ++u) {
+      const int ai = item.a0 + u * 32 + lane;
+      const int pk = (int)cc[u].x;
+      if (ai >= item.a1 || ((vm[u] >> (pk & 31)) & 1u)) continue;
+      const float nw = stdp_update(d, __uint_as_float(cc[u].y), false, true, post_tr, prt[u]);
+      d.csc[ai].y = __float_as_uint(nw);
+      ++n_post;
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) n_post += __shfl_xor_sync(FULL, n_post, o);
+    if (lane == 0 && n_post) atomicAdd(&d.ctl->stdp_post, n_post);
+  }
 }
 
 // ---- timestep part 3: propagation and STDP ----------------------------------------------
@@ -340,10 +463,10 @@ __host__ __device__ inline BulkWarpLayout bulk_warp_layout() {
   l.stage = o; o += 2 * STAGE_ENTRIES;
   l.stw = o; o += STAGE_ENTRIES;
   l.sidx = o; o += STAGE_ENTRIES / 2;
-  l.kst = o; o += STAGE_KEYS;
-  l.koff = o; o += STAGE_KEYS + 4;
-  l.kfl = o; o += STAGE_KEYS;
-  l.kpre = o; o += STAGE_KEYS;
+  l.kst = o; o += BULK_STAGE_KEYS;
+  l.koff = o; o += BULK_STAGE_KEYS + 4;
+  l.kfl = o; o += BULK_STAGE_KEYS;
+  l.kpre = o; o += BULK_STAGE_KEYS;
   l.tag = o; o += APPLY_TAGS;
   o = (o + 3) & ~3;
   l.total = o;
@@ -379,11 +502,11 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, 2) bulk_prop_kernel(NetD
   const float* pub = d.pre_pub;
   const uint32_t* tile_spk = d.bitsA + ((KL + p0) >> 5);  // spike words of the tile's posts
   for (int i = lane; i < APPLY_TAGS; i += 32) tag_s[i] = 32;
-  unsigned long long ev = 0, n_pre = 0, n_post = 0;
+  unsigned long long ev = 0, n_pre = 0;
   const int n_list = *d.step_count;
   __syncwarp();
-  for (int kb = 0; kb < n_list; kb += STAGE_KEYS) {
-    const int nk = min(STAGE_KEYS, n_list - kb);
+  for (int kb = 0; kb < n_list; kb += BULK_STAGE_KEYS) {
+    const int nk = min(BULK_STAGE_KEYS, n_list - kb);
     for (int i = lane; i < nk; i += 32) {
       const uint32_t lv = d.step_list[kb + i];
       const int* rp = d.rowptr + (size_t)(lv & 0x3fffffffu) * n_tiles + t_idx;
@@ -498,58 +621,16 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, 2) bulk_prop_kernel(NetD
       __syncwarp();
     }
   }
-  // post-spike afferent pass of the tile's spiking posts (weights updated on a
-  // presynaptic event this step are skipped: done above)
-  if (st.stdp_run) {
-    const uint32_t* bA = d.bitsA;
-    const uint32_t* bP = d.bitsP;
-    constexpr int AFF = 4;
-    for (int wi = 0; wi < TS / 32; ++wi) {
-      uint32_t word = tile_spk[wi];
-      while (word) {
-        const int b = __ffs(word) - 1;
-        word &= word - 1;
-        const int q = p0 + wi * 32 + b;
-        const int a0 = __ldg(d.csc_ptr + q), a1 = __ldg(d.csc_ptr + q + 1);
-        const float post_tr = d.post_trace[q];
-        for (int a = a0; a < a1; a += 32 * AFF) {
-          uint2 cc[AFF];
-#pragma unroll
-          for (int u = 0; u < AFF; ++u) {
-            const int ai = a + u * 32 + lane;
-            cc[u] = d.csc[ai < a1 ? ai : a];
-          }
-          uint32_t vm[AFF];
-          float prt[AFF];
-#pragma unroll
-          for (int u = 0; u < AFF; ++u) {
-            const int pk = (int)cc[u].x;
-            vm[u] = bA[pk >> 5] | bP[pk >> 5];
-            prt[u] = pub[pk];
-          }
-#pragma unroll
-          for (int u = 0; u < AFF; ++u) {
-            const int ai = a + u * 32 + lane;
-            const int pk = (int)cc[u].x;
-            if (ai >= a1 || ((vm[u] >> (pk & 31)) & 1u)) continue;
-            const float nw = stdp_update(d, __uint_as_float(cc[u].y), false, true, post_tr, prt[u]);
-            d.csc[ai].y = __float_as_uint(nw);
-            ++n_post;
-          }
-        }
-      }
-    }
-  }
+  // the post-spike afferent pass runs in bulk_post_kernel, over all networks'
+  // spiking posts at once
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) {
     ev += __shfl_xor_sync(FULL, ev, o);
     n_pre += __shfl_xor_sync(FULL, n_pre, o);
-    n_post += __shfl_xor_sync(FULL, n_post, o);
   }
   if (lane == 0) {
     if (ev) atomicAdd(&d.ctl->events, ev);
     if (n_pre) atomicAdd(&d.ctl->stdp_pre, n_pre);
-    if (n_post) atomicAdd(&d.ctl->stdp_post, n_post);
   }
 }
 

@@ -224,6 +224,10 @@ struct spk_batch {
   int tiles_total = 0;
   BulkWord* dwords = nullptr;    // [words_total] runs of 32-key words with real keys
   int words_total = 0;
+  BulkPostItem* items = nullptr; // afferent-pass work list of a timestep
+  int* item_count = nullptr;
+  int item_cap = 0;
+  bool any_plastic = false;
   void* bulk_mem = nullptr;      // tiles, step lists and counts
   cudaGraphExec_t bulk_graph = nullptr;  // one block of K timesteps
 };
@@ -1838,12 +1842,17 @@ static int bulk_launch_block(spk_batch* b) {
   const int T = b->tiles_total;
   const int wpb = 256 / 32;
   const int prop_smem = BULK_PROP_WARPS * bulk_warp_layout().total * 4;
+  DeviceInfo di;
+  const int rc0 = device_info(&di);
+  if (rc0) return rc0;
   for (int s = 0; s < b->K; ++s) {
     bulk_neurons_kernel<<<(b->words_total + wpb - 1) / wpb, 256, 0, b->stream>>>(b->dd, b->dwords,
-                                                                                  b->words_total, s);
-    bulk_list_kernel<<<n, BULK_LIST_THREADS, 0, b->stream>>>(b->dd, s);
+                                                                                  b->words_total, s, b->item_count);
+    bulk_list_kernel<<<n, BULK_LIST_THREADS, 0, b->stream>>>(b->dd, s, b->items, b->item_count, b->item_cap);
     bulk_prop_kernel<<<(T + BULK_PROP_WARPS - 1) / BULK_PROP_WARPS, BULK_PROP_WARPS * 32, prop_smem, b->stream>>>(
         b->dd, b->dtiles, T, s);
+    if (b->any_plastic)
+      bulk_post_kernel<<<di.sms * 8, 256, 0, b->stream>>>(b->dd, b->items, b->item_count, b->item_cap);
   }
   bulk_finish_kernel<<<(n + 255) / 256, 256, 0, b->stream>>>(b->dd, n, b->K);
   SPK_CUDA(cudaGetLastError());
@@ -1861,13 +1870,13 @@ static int bulk_run_block(spk_batch* b) {
       cudaGetLastError();
       b->bulk_graph = nullptr;
       const int rc2 = bulk_launch_block(b);  // launches go direct
-      b->launches += 3 * (int64_t)b->K + 1;
+      b->launches += (b->any_plastic ? 4 : 3) * (int64_t)b->K + 1;
       return rc2;
     }
     cudaGraphDestroy(g);
   }
   SPK_CUDA(cudaGraphLaunch(b->bulk_graph, b->stream));
-  b->launches += 3 * (int64_t)b->K + 1;
+  b->launches += (b->any_plastic ? 4 : 3) * (int64_t)b->K + 1;
   return SPK_OK;
 }
 
@@ -1947,11 +1956,25 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
           words.push_back(BulkWord{(int)i, w, std::min(BULK_WPW, lif_end - w), 0});
         list_words += (size_t)n->plan.n_keys;
       }
+      // afferent-pass items: at most one per started chunk of every spiking
+      // post's plastic afferents, i.e. n_csc / chunk + N per network
+      size_t cap = 0;
+      for (const spk_net* n : b->nets)
+        if (n->has_stdp) {
+          cap += (size_t)(n->n_csc / BULK_POST_CHUNK) + (size_t)n->N + 1;
+          b->any_plastic = true;
+        }
+      if (cap > 0x7fffffff) {
+        set_error("bulk mode: the batch's afferent-pass list would exceed 2^31 items");
+        return SPK_ERR_UNSUPPORTED;
+      }
+      b->item_cap = (int)cap;
       const size_t t_bytes = align_up(sizeof(BulkTile) * tiles.size(), 256);
       const size_t w_bytes = align_up(sizeof(BulkWord) * words.size(), 256);
       const size_t l_bytes = align_up(sizeof(uint32_t) * list_words, 256);
-      const size_t c_bytes = align_up(sizeof(int) * b->nets.size(), 256);
-      if (cudaMalloc(&b->bulk_mem, t_bytes + w_bytes + l_bytes + c_bytes) != cudaSuccess) {
+      const size_t c_bytes = align_up(sizeof(int) * (b->nets.size() + 1), 256);
+      const size_t i_bytes = align_up(sizeof(BulkPostItem) * std::max<size_t>(cap, 1), 256);
+      if (cudaMalloc(&b->bulk_mem, t_bytes + w_bytes + l_bytes + c_bytes + i_bytes) != cudaSuccess) {
         cudaGetLastError();
         b->bulk_mem = nullptr;
         set_error("bulk mode: device allocation failed");
@@ -1963,6 +1986,8 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       b->words_total = (int)words.size();
       uint32_t* lists = (uint32_t*)((char*)b->bulk_mem + t_bytes + w_bytes);
       int* counts = (int*)((char*)b->bulk_mem + t_bytes + w_bytes + l_bytes);
+      b->item_count = counts + b->nets.size();
+      b->items = (BulkPostItem*)((char*)b->bulk_mem + t_bytes + w_bytes + l_bytes + c_bytes);
       size_t off = 0;
       for (size_t i = 0; i < b->nets.size(); ++i) {
         b->hds[i].step_list = lists + off;
