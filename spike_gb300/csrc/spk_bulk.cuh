@@ -453,11 +453,15 @@ __global__ void __launch_bounds__(256) bulk_post_kernel(const NetDev* __restrict
 }
 
 // ---- timestep part 3: propagation and STDP ----------------------------------------------
-// Shared memory per warp (4-byte words).
+// Shared memory per warp (4-byte words).  `win` holds the tile's ring window:
+// the delay slots 1..ws after the current one (ws <= B - 3, the longest
+// delay), each TS * L words, read from HBM when the step has active keys and
+// written back once; contributions to cells outside the window (a window too
+// small for the network) go to HBM directly.
 struct BulkWarpLayout {
-  int stage, stw, sidx, kst, koff, kfl, kpre, tag, total;
+  int stage, stw, sidx, kst, koff, kfl, kpre, scl, ptr, spw, win, total;
 };
-__host__ __device__ inline BulkWarpLayout bulk_warp_layout() {
+__host__ __device__ inline BulkWarpLayout bulk_warp_layout(int win_words, int ts_max) {
   BulkWarpLayout l;
   int o = 0;
   l.stage = o; o += 2 * STAGE_ENTRIES;
@@ -467,21 +471,30 @@ __host__ __device__ inline BulkWarpLayout bulk_warp_layout() {
   l.koff = o; o += BULK_STAGE_KEYS + 4;
   l.kfl = o; o += BULK_STAGE_KEYS;
   l.kpre = o; o += BULK_STAGE_KEYS;
-  l.tag = o; o += APPLY_TAGS;
+  l.scl = o; o += MAX_CLASSES;  // weight scale of each class
+  l.ptr = o; o += ts_max;       // post traces of the tile (plastic runs)
+  l.spw = o; o += ts_max / 32;  // spike words of the tile's posts (plastic runs)
+  o = (o + 3) & ~3;
+  l.win = o; o += win_words;    // 16-byte aligned
   o = (o + 3) & ~3;
   l.total = o;
   return l;
 }
 constexpr int BULK_PROP_WARPS = 8;
+constexpr int BULK_WIN_CAP = 1024;  // ring-window words per warp at most
+#ifndef SPK_BULK_PROP_MINB
+#define SPK_BULK_PROP_MINB 3
+#endif
 
-__global__ void __launch_bounds__(BULK_PROP_WARPS * 32, 2) bulk_prop_kernel(NetDev* __restrict__ nets,
+__global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB) bulk_prop_kernel(NetDev* __restrict__ nets,
                                                                             const BulkTile* __restrict__ tiles,
-                                                                            int n_tiles_total, int s) {
+                                                                            int n_tiles_total, int s, int win_words,
+                                                                            int ts_max) {
   extern __shared__ __align__(16) uint32_t bsm[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int gw = blockIdx.x * BULK_PROP_WARPS + w;
   if (gw >= n_tiles_total) return;
-  const BulkWarpLayout wl = bulk_warp_layout();
+  const BulkWarpLayout wl = bulk_warp_layout(win_words, ts_max);
   uint32_t* wreg = bsm + w * wl.total;
   uint2* stage = (uint2*)(wreg + wl.stage);
   float* stage_w = (float*)(wreg + wl.stw);
@@ -490,26 +503,57 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, 2) bulk_prop_kernel(NetD
   int* koff = (int*)(wreg + wl.koff);
   uint32_t* kfl = wreg + wl.kfl;
   float* kpre = (float*)(wreg + wl.kpre);
-  int* tag_s = (int*)(wreg + wl.tag);
+  float* scl_s = (float*)(wreg + wl.scl);
+  float* ptr_s = (float*)(wreg + wl.ptr);
+  uint32_t* spw_s = wreg + wl.spw;
+  float* win_s = (float*)(wreg + wl.win);
   const BulkTile bt = tiles[gw];
   NetDev& d = nets[bt.net];
   const RunCtl c = load_ctl(d.ctl);
   const BulkStep st = bulk_step(d, c, s);
   if (!st.live) return;
+  const int n_list = *d.step_count;
+  if (n_list == 0) return;
   const int TS = d.TS, L = d.L, B = d.B, KL = d.KL, n_tiles = d.n_tiles, t_idx = bt.tile;
   const int p0 = t_idx * TS;
-  float* ring = d.ring + (size_t)t_idx * B * TS * L;
+  const int slot_words = TS * L;  // a multiple of 32
+  // the network's pointers and STDP constants in registers: the asm memory
+  // clobbers of the staging copies would otherwise reload them from the
+  // descriptor in every loop
+  float* ring = d.ring + (size_t)t_idx * B * slot_words;
   const float* pub = d.pre_pub;
-  const uint32_t* tile_spk = d.bitsA + ((KL + p0) >> 5);  // spike words of the tile's posts
-  for (int i = lane; i < APPLY_TAGS; i += 32) tag_s[i] = 32;
+  const uint32_t* step_list = d.step_list;
+  const int* rowptr = d.rowptr + t_idx;
+  const uint2* entries = d.entries;
+  uint2* csc = d.csc;
+  const bool has_stdp = d.has_stdp != 0;
+  const StdpConst sc = stdp_const(d);
+  if (lane < MAX_CLASSES) scl_s[lane] = d.scale_tab[lane];
+  // the ring window, in flight while the first round's keys are staged
+  const int ws = min(B - 3, win_words / slot_words);
+  for (int k = 0; k < ws; ++k) {
+    int sl = st.slot + 1 + k;
+    if (sl >= B) sl -= B;
+    const float* src = ring + (size_t)sl * slot_words;
+    float* dst = win_s + k * slot_words;
+    for (int i = lane * 4; i < slot_words; i += 128) cp_async16(dst + i, src + i);
+  }
+  if (st.stdp_run) {
+    for (int i = lane; i < TS; i += 32) {
+      if (p0 + i < d.N)
+        cp_async4(ptr_s + i, d.post_trace + p0 + i);
+      else
+        ptr_s[i] = 0.0f;
+    }
+    for (int i = lane; i < TS / 32; i += 32) spw_s[i] = d.bitsA[((KL + p0) >> 5) + i];
+  }
   unsigned long long ev = 0, n_pre = 0;
-  const int n_list = *d.step_count;
-  __syncwarp();
+  bool wtouched = false;
   for (int kb = 0; kb < n_list; kb += BULK_STAGE_KEYS) {
     const int nk = min(BULK_STAGE_KEYS, n_list - kb);
     for (int i = lane; i < nk; i += 32) {
-      const uint32_t lv = d.step_list[kb + i];
-      const int* rp = d.rowptr + (size_t)(lv & 0x3fffffffu) * n_tiles + t_idx;
+      const uint32_t lv = step_list[kb + i];
+      const int* rp = rowptr + (size_t)(lv & 0x3fffffffu) * n_tiles;
       cp_async4(kst + i, rp);
       cp_async4(koff + i, rp + 1);
       kfl[i] = lv;
@@ -547,17 +591,17 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, 2) bulk_prop_kernel(NetD
         const int base = kst[i] - o;
         for (int f = e0; f < e1; ++f) {
           sidx[f - f0] = (unsigned short)i;
-          cp_async8(stage + (f - f0), d.entries + base + f);
+          cp_async8(stage + (f - f0), entries + base + f);
         }
       }
       cp_async_wait_all();
       __syncwarp();
-      if (d.has_stdp) {
+      if (has_stdp) {
         bool any = false;
         for (int f = lane; f < nf; f += 32) {
           const uint2 en = stage[f];
           if ((en.x >> 28) != 0u) {
-            cp_async4(stage_w + f, &d.csc[en.y].y);
+            cp_async4(stage_w + f, &csc[en.y].y);
             any = true;
           }
         }
@@ -566,9 +610,8 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, 2) bulk_prop_kernel(NetD
       }
       for (int c0 = 0; c0 < nf; c0 += 32) {
         const int f = c0 + lane;
-        bool add = false;
-        size_t cell = 0;
-        int h = lane;  // distinct dummy tags for lanes without a contribution
+        bool add = false, inwin = false;
+        int cell = 0;
         float contrib = 0.0f;
         if (f < nf) {
           const int j = sidx[f];
@@ -583,42 +626,65 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, 2) bulk_prop_kernel(NetD
           if (cl != 0) {
             float v = stage_w[f];
             if (st.stdp_run) {
-              const bool post_ev = ((tile_spk[q >> 5] >> (q & 31)) & 1u) != 0;
+              const bool post_ev = ((spw_s[q >> 5] >> (q & 31)) & 1u) != 0;
               if (P || post_ev) {
-                v = stdp_update(d, v, P, post_ev, d.post_trace[p0 + q], kpre[j]);
-                d.csc[en.y].y = __float_as_uint(v);
+                v = stdp_update(sc, v, P, post_ev, ptr_s[q], kpre[j]);
+                csc[en.y].y = __float_as_uint(v);
                 ++n_pre;
               }
             }
-            contrib = v * d.scale_tab[cl];
+            contrib = v * scl_s[cl];
           } else {
             contrib = __uint_as_float(en.y);
           }
           if (A) {
             add = true;
-            int sl = st.slot + dl;
-            if (sl >= B) sl -= B;
-            const int ci = (sl * TS + q) * L + lb;
-            cell = (size_t)ci;
-            h = ci & (APPLY_TAGS - 1);
+            if (dl >= 1 && dl <= ws) {
+              inwin = true;
+              cell = ((dl - 1) * TS + q) * L + lb;
+            } else {
+              int sl = st.slot + dl;
+              if (sl >= B) sl -= B;
+              cell = (sl * TS + q) * L + lb;
+            }
           }
         }
-        // same-cell contributions in lane order (see the persistent kernel)
-        bool pending = add;
-        while (__any_sync(FULL, pending)) {
-          if (pending) atomicMin(tag_s + h, lane);
-          __syncwarp();
-          const bool win = pending && tag_s[h] == lane;
-          if (win) ring[cell] = ring[cell] + contrib;
-          __syncwarp();
-          if (win) {
-            tag_s[h] = 32;
-            pending = false;
+        // same-cell contributions of the chunk in lane order: the lowest lane
+        // of each group adds its peers' contributions one by one
+        const unsigned key = add ? (inwin ? (unsigned)cell : 0x40000000u | (unsigned)cell) : 0x80000000u | lane;
+        const unsigned peers = __match_any_sync(FULL, key);
+        const bool leader = add && (__ffs(peers) - 1) == lane;
+        float acc = 0.0f;
+        if (leader) acc = inwin ? win_s[cell] : ring[cell];
+        unsigned rest = leader ? peers : 0u;
+        while (__any_sync(FULL, rest != 0u)) {
+          const int src = rest ? __ffs(rest) - 1 : lane;
+          const float cv = __shfl_sync(FULL, contrib, src);
+          if (rest) {
+            acc = acc + cv;
+            rest &= rest - 1;
           }
-          __syncwarp();
         }
+        if (leader) {
+          if (inwin) {
+            win_s[cell] = acc;
+            wtouched = true;
+          } else {
+            ring[cell] = acc;
+          }
+        }
+        __syncwarp();
       }
       __syncwarp();
+    }
+  }
+  if (__any_sync(FULL, wtouched)) {
+    for (int k = 0; k < ws; ++k) {
+      int sl = st.slot + 1 + k;
+      if (sl >= B) sl -= B;
+      float4* dst = (float4*)(ring + (size_t)sl * slot_words);
+      const float4* src = (const float4*)(win_s + k * slot_words);
+      for (int i = lane; i < slot_words / 4; i += 32) dst[i] = src[i];
     }
   }
   // the post-spike afferent pass runs in bulk_post_kernel, over all networks'

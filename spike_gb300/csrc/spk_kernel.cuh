@@ -78,6 +78,10 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
 // Barrier 1 over the whole CTA: releases and retires list rounds between warp 0
 // (the list builder) and the other warps, which reach it from different code.
 __device__ __forceinline__ void round_barrier(int nthreads) {
@@ -111,7 +115,16 @@ __device__ __forceinline__ unsigned long long repoll(const unsigned long long* p
 // ltp_and_ltd update of one synapse for G = 1
 // (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:132-151):
 // pre_ev/post_ev are "spike sub-step >= 0", the traces are this step's values.
-__device__ __forceinline__ float stdp_update(const NetDev& d, float old_w, bool pre_ev, bool post_ev,
+// The STDP constants of a network, for loops that keep them in registers.
+struct StdpConst {
+  float invE_m, invE_p, lam, lam_alpha, wmax;
+  int clip_upper;
+};
+__device__ __forceinline__ StdpConst stdp_const(const NetDev& d) {
+  return StdpConst{d.invE_m, d.invE_p, d.lam, d.lam_alpha, d.wmax, d.clip_upper};
+}
+template <class C>
+__device__ __forceinline__ float stdp_update(const C& d, float old_w, bool pre_ev, bool post_ev,
                                              float post_tr, float pre_tr) {
   float syn = 0.0f;
   if (pre_ev) {

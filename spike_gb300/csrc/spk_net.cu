@@ -228,6 +228,8 @@ struct spk_batch {
   int* item_count = nullptr;
   int item_cap = 0;
   bool any_plastic = false;
+  int win_words = 0;            // ring-window words per propagation warp
+  int ts_max = 0;               // largest post tile of the batch
   void* bulk_mem = nullptr;      // tiles, step lists and counts
   cudaGraphExec_t bulk_graph = nullptr;  // one block of K timesteps
 };
@@ -1841,7 +1843,7 @@ static int bulk_launch_block(spk_batch* b) {
   const int n = (int)b->nets.size();
   const int T = b->tiles_total;
   const int wpb = 256 / 32;
-  const int prop_smem = BULK_PROP_WARPS * bulk_warp_layout().total * 4;
+  const int prop_smem = BULK_PROP_WARPS * bulk_warp_layout(b->win_words, b->ts_max).total * 4;
   DeviceInfo di;
   const int rc0 = device_info(&di);
   if (rc0) return rc0;
@@ -1850,7 +1852,7 @@ static int bulk_launch_block(spk_batch* b) {
                                                                                   b->words_total, s, b->item_count);
     bulk_list_kernel<<<n, BULK_LIST_THREADS, 0, b->stream>>>(b->dd, s, b->items, b->item_count, b->item_cap);
     bulk_prop_kernel<<<(T + BULK_PROP_WARPS - 1) / BULK_PROP_WARPS, BULK_PROP_WARPS * 32, prop_smem, b->stream>>>(
-        b->dd, b->dtiles, T, s);
+        b->dd, b->dtiles, T, s, b->win_words, b->ts_max);
     if (b->any_plastic)
       bulk_post_kernel<<<di.sms * 8, 256, 0, b->stream>>>(b->dd, b->items, b->item_count, b->item_cap);
   }
@@ -1946,9 +1948,16 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       std::vector<BulkTile> tiles;
       std::vector<BulkWord> words;
       size_t list_words = 0;
+      // propagation tiles of the networks with the most keys first: their
+      // warps walk the longest key lists, so they start before the short ones
+      std::vector<int> by_keys(b->nets.size());
+      for (size_t i = 0; i < by_keys.size(); ++i) by_keys[i] = (int)i;
+      std::stable_sort(by_keys.begin(), by_keys.end(),
+                       [&](int x, int y) { return b->nets[x]->plan.n_keys > b->nets[y]->plan.n_keys; });
+      for (const int i : by_keys)
+        for (int t = 0; t < b->nets[i]->plan.n_tiles; ++t) tiles.push_back(BulkTile{i, t});
       for (size_t i = 0; i < b->nets.size(); ++i) {
         const spk_net* n = b->nets[i];
-        for (int t = 0; t < n->plan.n_tiles; ++t) tiles.push_back(BulkTile{(int)i, t});
         const int in_end = (n->Nin + 31) / 32, lif0 = n->plan.KL / 32, lif_end = (n->plan.KL + n->N + 31) / 32;
         for (int w = 0; w < in_end; w += BULK_WPW)
           words.push_back(BulkWord{(int)i, w, std::min(BULK_WPW, in_end - w), 0});
@@ -1969,6 +1978,14 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
         return SPK_ERR_UNSUPPORTED;
       }
       b->item_cap = (int)cap;
+      // ring windows: the longest delay's slots of the largest tile, capped
+      b->win_words = 0;
+      b->ts_max = 0;
+      for (const spk_net* n : b->nets) {
+        b->ts_max = std::max(b->ts_max, n->hd.TS);
+        b->win_words = std::max(b->win_words, (n->hd.B - 3) * n->hd.TS * n->hd.L);
+      }
+      b->win_words = std::min(b->win_words, BULK_WIN_CAP);
       const size_t t_bytes = align_up(sizeof(BulkTile) * tiles.size(), 256);
       const size_t w_bytes = align_up(sizeof(BulkWord) * words.size(), 256);
       const size_t l_bytes = align_up(sizeof(uint32_t) * list_words, 256);
@@ -2005,7 +2022,7 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       }
       SPK_CUDA(cudaMemcpy(b->dd, b->hds.data(), sizeof(NetDev) * b->hds.size(), cudaMemcpyHostToDevice));
       SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    BULK_PROP_WARPS * bulk_warp_layout().total * 4));
+                                    BULK_PROP_WARPS * bulk_warp_layout(b->win_words, b->ts_max).total * 4));
     }
     b->mode = mode;
     return SPK_OK;
