@@ -39,7 +39,7 @@
 #define SPK_BULK_STAGE_KEYS 64
 #endif
 #ifndef SPK_BULK_WPW
-#define SPK_BULK_WPW 4
+#define SPK_BULK_WPW 2
 #endif
 
 namespace spk {
@@ -86,20 +86,26 @@ __device__ __forceinline__ RunCtl load_ctl(const RunCtl* p) {
 }
 
 // ---- timestep part 1: neurons and inputs -------------------------------------------
-// One warp per run of up to BULK_WPW consecutive 32-key words of one network
-// (inputs: keys 0..n_inputs-1; neurons: keys KL..KL+N-1).  A warp issues the
-// state loads of all its words before any update, so the chain of dependent
-// loads (descriptor, run control, state) is paid once per run of words, not
-// once per word.  Words of padding keys are never written: they stay zero
-// from set-up.  No L2 prefetch of the spiking rows here: a batch's rows of one
-// step exceed the L2.
+// One CTA per block of up to BULK_BLOCK_WORDS consecutive 32-key words of one
+// network (inputs: keys 0..n_inputs-1; neurons: keys KL..KL+N-1), each warp
+// BULK_WPW of them.  The CTA copies the network's descriptor and run control
+// into shared memory with one round of parallel loads, so each warp's only
+// dependent global loads are its state loads, all issued before any update.
+// Words of padding keys are never written: they stay zero from set-up.
+#ifndef SPK_BULK_NEUR_MINB
+#define SPK_BULK_NEUR_MINB 6
+#endif
 constexpr int BULK_WPW = SPK_BULK_WPW;
+constexpr int BULK_NEUR_WARPS = 8;
+constexpr int BULK_BLOCK_WORDS = BULK_NEUR_WARPS * BULK_WPW;
 
-struct BulkWord {
-  int net;    // index into the batch's NetDev array
-  int word;   // first word (key / 32)
-  int count;  // words in the run (<= BULK_WPW), all inputs or all neurons
+struct BulkBlock {
+  int net;            // index into the batch's NetDev array
+  int word;           // first word (key / 32)
+  int count;          // words in the block (<= BULK_BLOCK_WORDS), all inputs or all neurons
   int pad;
+  const RunCtl* ctl;  // the network's run control, loaded beside its descriptor
+  const void* pad2;
 };
 
 // LIF update of neuron n (the persistent kernel's phase A, same operations)
@@ -149,18 +155,30 @@ __device__ __forceinline__ bool bulk_lif(const NetDev& d, const BulkStep& st, in
   return spk;
 }
 
-__global__ void __launch_bounds__(256) bulk_neurons_kernel(const NetDev* __restrict__ nets,
-                                                           const BulkWord* __restrict__ words, int n_words_total,
-                                                           int s, int* item_count) {
+__global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk_neurons_kernel(const NetDev* __restrict__ nets,
+                                                                         const BulkBlock* __restrict__ blocks,
+                                                                         int s, int* item_count) {
+  __shared__ __align__(16) NetDev sd;
+  __shared__ RunCtl sctl;
+  static_assert(sizeof(NetDev) % 4 == 0, "descriptor copied as words");
   if (blockIdx.x == 0 && threadIdx.x == 0) *item_count = 0;  // the afferent-pass list of this step
-  const int lane = threadIdx.x & 31;
-  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (gw >= n_words_total) return;
-  const BulkWord bw = words[gw];
-  const NetDev& d = nets[bw.net];
-  const RunCtl c = load_ctl(d.ctl);
-  const BulkStep st = bulk_step(d, c, s);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const BulkBlock bb = blocks[blockIdx.x];
+  {
+    const uint32_t* src = (const uint32_t*)(nets + bb.net);
+    uint32_t* dst = (uint32_t*)&sd;
+    for (int i = threadIdx.x; i < (int)(sizeof(NetDev) / 4); i += blockDim.x) dst[i] = __ldg(src + i);
+    if (threadIdx.x == 0) sctl = load_ctl(bb.ctl);
+  }
+  __syncthreads();
+  const NetDev& d = sd;
+  const BulkStep st = bulk_step(d, sctl, s);
   if (!st.live) return;
+  const int w0 = w * BULK_WPW;
+  if (w0 >= bb.count) return;
+  struct {
+    int word, count;
+  } const bw = {bb.word + w0, min(BULK_WPW, bb.count - w0)};
   const int KL = d.KL;
   float* pub = d.pre_pub;
   if (bw.word * 32 >= KL) {
@@ -529,15 +547,8 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB) bulk
   const bool has_stdp = d.has_stdp != 0;
   const StdpConst sc = stdp_const(d);
   if (lane < MAX_CLASSES) scl_s[lane] = d.scale_tab[lane];
-  // the ring window, in flight while the first round's keys are staged
-  const int ws = min(B - 3, win_words / slot_words);
-  for (int k = 0; k < ws; ++k) {
-    int sl = st.slot + 1 + k;
-    if (sl >= B) sl -= B;
-    const float* src = ring + (size_t)sl * slot_words;
-    float* dst = win_s + k * slot_words;
-    for (int i = lane * 4; i < slot_words; i += 128) cp_async16(dst + i, src + i);
-  }
+  // the ring window's depth, chosen once the first round's entries are counted
+  int ws = 0;
   if (st.stdp_run) {
     for (int i = lane; i < TS; i += 32) {
       if (p0 + i < d.N)
@@ -548,7 +559,7 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB) bulk
     for (int i = lane; i < TS / 32; i += 32) spw_s[i] = d.bitsA[((KL + p0) >> 5) + i];
   }
   unsigned long long ev = 0, n_pre = 0;
-  bool wtouched = false;
+  unsigned dirty = 0u;  // window slots this lane wrote
   for (int kb = 0; kb < n_list; kb += BULK_STAGE_KEYS) {
     const int nk = min(BULK_STAGE_KEYS, n_list - kb);
     for (int i = lane; i < nk; i += 32) {
@@ -582,6 +593,21 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB) bulk
       carry += __shfl_sync(FULL, incl, 31);
     }
     const int total_e = carry;
+    if (kb == 0) {
+      // A window pays when the step's entries (estimated from the first
+      // round) would touch more sectors one by one than the window holds;
+      // its reads overlap the first round's entry staging.
+      const int ws_max = min(min(B - 3, 32), win_words / slot_words);
+      const long long est = (long long)total_e * ((n_list + BULK_STAGE_KEYS - 1) / BULK_STAGE_KEYS);
+      ws = (ws_max > 0 && est * 8 > (long long)ws_max * slot_words) ? ws_max : 0;
+      for (int k = 0; k < ws; ++k) {
+        int sl = st.slot + 1 + k;
+        if (sl >= B) sl -= B;
+        const float* src = ring + (size_t)sl * slot_words;
+        float* dst = win_s + k * slot_words;
+        for (int i = lane * 4; i < slot_words; i += 128) cp_async16(dst + i, src + i);
+      }
+    }
     __syncwarp();
     for (int f0 = 0; f0 < total_e; f0 += STAGE_ENTRIES) {
       const int nf = min(STAGE_ENTRIES, total_e - f0);
@@ -611,7 +637,7 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB) bulk
       for (int c0 = 0; c0 < nf; c0 += 32) {
         const int f = c0 + lane;
         bool add = false, inwin = false;
-        int cell = 0;
+        int cell = 0, wslot = 0;
         float contrib = 0.0f;
         if (f < nf) {
           const int j = sidx[f];
@@ -641,7 +667,8 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB) bulk
             add = true;
             if (dl >= 1 && dl <= ws) {
               inwin = true;
-              cell = ((dl - 1) * TS + q) * L + lb;
+              wslot = dl - 1;
+              cell = (wslot * TS + q) * L + lb;
             } else {
               int sl = st.slot + dl;
               if (sl >= B) sl -= B;
@@ -668,7 +695,7 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB) bulk
         if (leader) {
           if (inwin) {
             win_s[cell] = acc;
-            wtouched = true;
+            dirty |= 1u << wslot;
           } else {
             ring[cell] = acc;
           }
@@ -678,8 +705,10 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB) bulk
       __syncwarp();
     }
   }
-  if (__any_sync(FULL, wtouched)) {
+  dirty = __reduce_or_sync(FULL, dirty);
+  if (dirty) {
     for (int k = 0; k < ws; ++k) {
+      if (!((dirty >> k) & 1u)) continue;
       int sl = st.slot + 1 + k;
       if (sl >= B) sl -= B;
       float4* dst = (float4*)(ring + (size_t)sl * slot_words);

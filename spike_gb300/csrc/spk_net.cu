@@ -222,8 +222,8 @@ struct spk_batch {
   std::vector<NetDev> hds;       // host copies of the batch's descriptors
   BulkTile* dtiles = nullptr;    // [tiles_total]
   int tiles_total = 0;
-  BulkWord* dwords = nullptr;    // [words_total] runs of 32-key words with real keys
-  int words_total = 0;
+  BulkBlock* dblocks = nullptr;  // [blocks_total] blocks of 32-key words with real keys
+  int blocks_total = 0;
   BulkPostItem* items = nullptr; // afferent-pass work list of a timestep
   int* item_count = nullptr;
   int item_cap = 0;
@@ -1842,14 +1842,13 @@ namespace spk {
 static int bulk_launch_block(spk_batch* b) {
   const int n = (int)b->nets.size();
   const int T = b->tiles_total;
-  const int wpb = 256 / 32;
   const int prop_smem = BULK_PROP_WARPS * bulk_warp_layout(b->win_words, b->ts_max).total * 4;
   DeviceInfo di;
   const int rc0 = device_info(&di);
   if (rc0) return rc0;
   for (int s = 0; s < b->K; ++s) {
-    bulk_neurons_kernel<<<(b->words_total + wpb - 1) / wpb, 256, 0, b->stream>>>(b->dd, b->dwords,
-                                                                                  b->words_total, s, b->item_count);
+    bulk_neurons_kernel<<<b->blocks_total, BULK_NEUR_WARPS * 32, 0, b->stream>>>(b->dd, b->dblocks, s,
+                                                                                  b->item_count);
     bulk_list_kernel<<<n, BULK_LIST_THREADS, 0, b->stream>>>(b->dd, s, b->items, b->item_count, b->item_cap);
     bulk_prop_kernel<<<(T + BULK_PROP_WARPS - 1) / BULK_PROP_WARPS, BULK_PROP_WARPS * 32, prop_smem, b->stream>>>(
         b->dd, b->dtiles, T, s, b->win_words, b->ts_max);
@@ -1946,7 +1945,7 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
   return guarded([&]() -> int {
     if (!b->bulk_mem) {
       std::vector<BulkTile> tiles;
-      std::vector<BulkWord> words;
+      std::vector<BulkBlock> words;
       size_t list_words = 0;
       // propagation tiles of the networks with the most keys first: their
       // warps walk the longest key lists, so they start before the short ones
@@ -1959,10 +1958,10 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       for (size_t i = 0; i < b->nets.size(); ++i) {
         const spk_net* n = b->nets[i];
         const int in_end = (n->Nin + 31) / 32, lif0 = n->plan.KL / 32, lif_end = (n->plan.KL + n->N + 31) / 32;
-        for (int w = 0; w < in_end; w += BULK_WPW)
-          words.push_back(BulkWord{(int)i, w, std::min(BULK_WPW, in_end - w), 0});
-        for (int w = lif0; w < lif_end; w += BULK_WPW)
-          words.push_back(BulkWord{(int)i, w, std::min(BULK_WPW, lif_end - w), 0});
+        for (int w = 0; w < in_end; w += BULK_BLOCK_WORDS)
+          words.push_back(BulkBlock{(int)i, w, std::min(BULK_BLOCK_WORDS, in_end - w), 0, b->hds[i].ctl, nullptr});
+        for (int w = lif0; w < lif_end; w += BULK_BLOCK_WORDS)
+          words.push_back(BulkBlock{(int)i, w, std::min(BULK_BLOCK_WORDS, lif_end - w), 0, b->hds[i].ctl, nullptr});
         list_words += (size_t)n->plan.n_keys;
       }
       // afferent-pass items: at most one per started chunk of every spiking
@@ -1987,7 +1986,7 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       }
       b->win_words = std::min(b->win_words, BULK_WIN_CAP);
       const size_t t_bytes = align_up(sizeof(BulkTile) * tiles.size(), 256);
-      const size_t w_bytes = align_up(sizeof(BulkWord) * words.size(), 256);
+      const size_t w_bytes = align_up(sizeof(BulkBlock) * words.size(), 256);
       const size_t l_bytes = align_up(sizeof(uint32_t) * list_words, 256);
       const size_t c_bytes = align_up(sizeof(int) * (b->nets.size() + 1), 256);
       const size_t i_bytes = align_up(sizeof(BulkPostItem) * std::max<size_t>(cap, 1), 256);
@@ -1999,8 +1998,8 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       }
       b->dtiles = (BulkTile*)b->bulk_mem;
       b->tiles_total = (int)tiles.size();
-      b->dwords = (BulkWord*)((char*)b->bulk_mem + t_bytes);
-      b->words_total = (int)words.size();
+      b->dblocks = (BulkBlock*)((char*)b->bulk_mem + t_bytes);
+      b->blocks_total = (int)words.size();
       uint32_t* lists = (uint32_t*)((char*)b->bulk_mem + t_bytes + w_bytes);
       int* counts = (int*)((char*)b->bulk_mem + t_bytes + w_bytes + l_bytes);
       b->item_count = counts + b->nets.size();
@@ -2012,7 +2011,7 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
         off += (size_t)b->nets[i]->plan.n_keys;
       }
       SPK_CUDA(cudaMemcpy(b->dtiles, tiles.data(), sizeof(BulkTile) * tiles.size(), cudaMemcpyHostToDevice));
-      SPK_CUDA(cudaMemcpy(b->dwords, words.data(), sizeof(BulkWord) * words.size(), cudaMemcpyHostToDevice));
+      SPK_CUDA(cudaMemcpy(b->dblocks, words.data(), sizeof(BulkBlock) * words.size(), cudaMemcpyHostToDevice));
       // words of padding keys are never written in bulk mode: zero them once
       SPK_CUDA(cudaStreamSynchronize(b->stream));
       for (const spk_net* n : b->nets) {
