@@ -46,11 +46,6 @@ namespace spk {
 
 constexpr int BULK_STAGE_KEYS = SPK_BULK_STAGE_KEYS;
 
-struct BulkTile {
-  int net;   // index into the batch's NetDev array
-  int tile;  // tile of that network
-};
-
 // Timestep s of the current block of a network's run.
 struct BulkStep {
   float t, tg;
@@ -471,85 +466,146 @@ __global__ void __launch_bounds__(256) bulk_post_kernel(const NetDev* __restrict
 }
 
 // ---- timestep part 3: propagation and STDP ----------------------------------------------
-// Shared memory per warp (4-byte words).  `win` holds the tile's ring window:
-// the delay slots 1..ws after the current one (ws <= B - 3, the longest
-// delay), each TS * L words, read from HBM when the step has active keys and
-// written back once; contributions to cells outside the window (a window too
-// small for the network) go to HBM directly.
-struct BulkWarpLayout {
-  int stage, stw, sidx, kst, koff, kfl, kpre, scl, ptr, spw, win, total;
+// One CTA per group of up to BULK_PROP_WARPS consecutive tiles of one network,
+// one warp per tile.  The CTA shares what every tile of the network reads
+// alike: the descriptor and run control (copied once), the step's key list
+// (staged BULK_LIST_CHUNK keys at a time) and, per round of BULK_STAGE_KEYS
+// keys, the keys' rowptr words of the CTA's tiles (one sector per key) and
+// their presynaptic traces.  Round r + 1 is staged while the warps stage and
+// apply round r's entries, so a round costs a warp two dependent loads (its
+// entries, then the plastic weights they name) instead of four.
+//
+// Shared memory: the CTA part (list chunk, two rounds of rowptr words, key
+// flags and pre traces, class scales) and per warp (entry stage, offsets, the
+// tile's post traces and spike words, and `win`, the tile's ring window: the
+// delay slots 1..ws after the current one, each TS * L words, read from HBM
+// when the step's entries fill enough of it and written back once per dirty
+// slot; contributions outside the window go to HBM directly).
+constexpr int BULK_PROP_WARPS = 8;
+constexpr int BULK_RPW = BULK_PROP_WARPS + 1;  // rowptr words per key: the tiles' starts and the last end
+constexpr int BULK_LIST_CHUNK = 1024;          // list keys staged at a time (a multiple of BULK_STAGE_KEYS)
+constexpr int BULK_WIN_CAP = 1024;             // ring-window words per warp at most
+static_assert(BULK_LIST_CHUNK % BULK_STAGE_KEYS == 0, "rounds never straddle a list chunk");
+
+struct BulkPropBlock {
+  int net;    // index into the batch's NetDev array
+  int tile0;  // first tile
+  int n;      // tiles (<= BULK_PROP_WARPS)
+  int pad;
+  const RunCtl* ctl;     // the network's run control
+  const int* n_list;     // the network's step key count
 };
-__host__ __device__ inline BulkWarpLayout bulk_warp_layout(int win_words, int ts_max) {
-  BulkWarpLayout l;
+
+struct BulkPropLayout {
+  // CTA part
+  int list, rp, kfl, kpre, scl, cta;
+  // per warp
+  int stage, stw, sidx, koff, ptr, spw, win, warp;
+  int total;  // words
+};
+__host__ __device__ inline BulkPropLayout bulk_prop_layout(int win_words, int ts_max) {
+  BulkPropLayout l;
   int o = 0;
-  l.stage = o; o += 2 * STAGE_ENTRIES;
-  l.stw = o; o += STAGE_ENTRIES;
-  l.sidx = o; o += STAGE_ENTRIES / 2;
-  l.kst = o; o += BULK_STAGE_KEYS;
-  l.koff = o; o += BULK_STAGE_KEYS + 4;
-  l.kfl = o; o += BULK_STAGE_KEYS;
-  l.kpre = o; o += BULK_STAGE_KEYS;
-  l.scl = o; o += MAX_CLASSES;  // weight scale of each class
-  l.ptr = o; o += ts_max;       // post traces of the tile (plastic runs)
-  l.spw = o; o += ts_max / 32;  // spike words of the tile's posts (plastic runs)
+  l.list = o; o += BULK_LIST_CHUNK;
+  l.rp = o; o += 2 * BULK_STAGE_KEYS * BULK_RPW;
+  l.kfl = o; o += 2 * BULK_STAGE_KEYS;
+  l.kpre = o; o += 2 * BULK_STAGE_KEYS;
+  l.scl = o; o += MAX_CLASSES;
   o = (o + 3) & ~3;
-  l.win = o; o += win_words;    // 16-byte aligned
-  o = (o + 3) & ~3;
-  l.total = o;
+  l.cta = o;
+  int p = 0;
+  l.stage = p; p += 2 * STAGE_ENTRIES;
+  l.stw = p; p += STAGE_ENTRIES;
+  l.sidx = p; p += STAGE_ENTRIES / 2;
+  l.koff = p; p += BULK_STAGE_KEYS + 4;
+  l.ptr = p; p += ts_max;       // post traces of the tile (plastic runs)
+  l.spw = p; p += ts_max / 32;  // spike words of the tile's posts (plastic runs)
+  p = (p + 3) & ~3;
+  l.win = p; p += win_words;    // 16-byte aligned
+  p = (p + 3) & ~3;
+  l.warp = p;
+  l.total = l.cta + BULK_PROP_WARPS * l.warp;
   return l;
 }
-constexpr int BULK_PROP_WARPS = 8;
-constexpr int BULK_WIN_CAP = 1024;  // ring-window words per warp at most
 #ifndef SPK_BULK_PROP_MINB
 #define SPK_BULK_PROP_MINB 3
 #endif
 
-__global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB) bulk_prop_kernel(NetDev* __restrict__ nets,
-                                                                            const BulkTile* __restrict__ tiles,
-                                                                            int n_tiles_total, int s, int win_words,
-                                                                            int ts_max) {
+__global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
+    bulk_prop_kernel(const NetDev* __restrict__ nets, const BulkPropBlock* __restrict__ blocks, int s, int win_words,
+                     int ts_max) {
   extern __shared__ __align__(16) uint32_t bsm[];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int gw = blockIdx.x * BULK_PROP_WARPS + w;
-  if (gw >= n_tiles_total) return;
-  const BulkWarpLayout wl = bulk_warp_layout(win_words, ts_max);
-  uint32_t* wreg = bsm + w * wl.total;
+  __shared__ __align__(16) NetDev sd;
+  __shared__ RunCtl sctl;
+  __shared__ int s_nlist;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nthr = BULK_PROP_WARPS * 32;
+  const BulkPropBlock pb = blocks[blockIdx.x];
+  {
+    const uint32_t* src = (const uint32_t*)(nets + pb.net);
+    uint32_t* dst = (uint32_t*)&sd;
+    for (int i = threadIdx.x; i < (int)(sizeof(NetDev) / 4); i += nthr) dst[i] = __ldg(src + i);
+    if (threadIdx.x == 0) {
+      sctl = load_ctl(pb.ctl);
+      s_nlist = *pb.n_list;
+    }
+  }
+  __syncthreads();
+  const NetDev& d = sd;
+  const BulkStep st = bulk_step(d, sctl, s);
+  const int n_list = s_nlist;
+  if (!st.live || n_list == 0) return;  // the whole CTA
+  const BulkPropLayout wl = bulk_prop_layout(win_words, ts_max);
+  uint32_t* list_s = bsm + wl.list;
+  int* rp_s = (int*)(bsm + wl.rp);
+  uint32_t* kfl_s = bsm + wl.kfl;
+  float* kpre_s = (float*)(bsm + wl.kpre);
+  float* scl_s = (float*)(bsm + wl.scl);
+  uint32_t* wreg = bsm + wl.cta + w * wl.warp;
   uint2* stage = (uint2*)(wreg + wl.stage);
   float* stage_w = (float*)(wreg + wl.stw);
   unsigned short* sidx = (unsigned short*)(wreg + wl.sidx);
-  int* kst = (int*)(wreg + wl.kst);
   int* koff = (int*)(wreg + wl.koff);
-  uint32_t* kfl = wreg + wl.kfl;
-  float* kpre = (float*)(wreg + wl.kpre);
-  float* scl_s = (float*)(wreg + wl.scl);
   float* ptr_s = (float*)(wreg + wl.ptr);
   uint32_t* spw_s = wreg + wl.spw;
   float* win_s = (float*)(wreg + wl.win);
-  const BulkTile bt = tiles[gw];
-  NetDev& d = nets[bt.net];
-  const RunCtl c = load_ctl(d.ctl);
-  const BulkStep st = bulk_step(d, c, s);
-  if (!st.live) return;
-  const int n_list = *d.step_count;
-  if (n_list == 0) return;
-  const int TS = d.TS, L = d.L, B = d.B, KL = d.KL, n_tiles = d.n_tiles, t_idx = bt.tile;
+
+  const int TS = d.TS, L = d.L, B = d.B, KL = d.KL, n_tiles = d.n_tiles;
+  const bool active = w < pb.n;  // warps past the network's last tile only help to stage
+  const int t_idx = pb.tile0 + w, nrp = pb.n + 1;
   const int p0 = t_idx * TS;
   const int slot_words = TS * L;  // a multiple of 32
-  // the network's pointers and STDP constants in registers: the asm memory
-  // clobbers of the staging copies would otherwise reload them from the
-  // descriptor in every loop
   float* ring = d.ring + (size_t)t_idx * B * slot_words;
   const float* pub = d.pre_pub;
   const uint32_t* step_list = d.step_list;
-  const int* rowptr = d.rowptr + t_idx;
+  const int* rowptr = d.rowptr + pb.tile0;
   const uint2* entries = d.entries;
   uint2* csc = d.csc;
   const bool has_stdp = d.has_stdp != 0;
   const StdpConst sc = stdp_const(d);
-  if (lane < MAX_CLASSES) scl_s[lane] = d.scale_tab[lane];
-  // the ring window's depth, chosen once the first round's entries are counted
-  int ws = 0;
-  if (st.stdp_run) {
+  if (threadIdx.x < MAX_CLASSES) scl_s[threadIdx.x] = d.scale_tab[threadIdx.x];
+
+  // staging of one round's keys into buffer `buf` (all threads)
+  auto stage_round = [&](int kb, int buf) {
+    const int nk = min(BULK_STAGE_KEYS, n_list - kb);
+    const int lb = kb % BULK_LIST_CHUNK;
+    int* rp = rp_s + buf * BULK_STAGE_KEYS * BULK_RPW;
+    for (int i = threadIdx.x; i < nk * nrp; i += nthr) {
+      const int j = i / nrp, t = i - j * nrp;
+      const uint32_t key = list_s[lb + j] & 0x3fffffffu;
+      cp_async4(rp + j * BULK_RPW + t, rowptr + (size_t)key * n_tiles + t);
+    }
+    for (int j = threadIdx.x; j < nk; j += nthr) {
+      const uint32_t lv = list_s[lb + j];
+      kfl_s[buf * BULK_STAGE_KEYS + j] = lv;
+      if (st.stdp_run) cp_async4(kpre_s + buf * BULK_STAGE_KEYS + j, pub + (lv & 0x3fffffffu));
+    }
+  };
+  auto stage_list = [&](int kb) {
+    const int n = min(BULK_LIST_CHUNK, n_list - kb);
+    for (int i = threadIdx.x; i < n; i += nthr) cp_async4(list_s + i, step_list + kb + i);
+  };
+
+  if (active && st.stdp_run) {
     for (int i = lane; i < TS; i += 32) {
       if (p0 + i < d.N)
         cp_async4(ptr_s + i, d.post_trace + p0 + i);
@@ -558,22 +614,34 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB) bulk
     }
     for (int i = lane; i < TS / 32; i += 32) spw_s[i] = d.bitsA[((KL + p0) >> 5) + i];
   }
+  stage_list(0);
+  cp_async_wait_all();
+  __syncthreads();
+  stage_round(0, 0);
+
   unsigned long long ev = 0, n_pre = 0;
   unsigned dirty = 0u;  // window slots this lane wrote
-  for (int kb = 0; kb < n_list; kb += BULK_STAGE_KEYS) {
+  int ws = 0;           // the ring window's depth, chosen once the first round's entries are counted
+  for (int kb = 0, r = 0; kb < n_list; kb += BULK_STAGE_KEYS, ++r) {
+    const int buf = r & 1;
     const int nk = min(BULK_STAGE_KEYS, n_list - kb);
-    for (int i = lane; i < nk; i += 32) {
-      const uint32_t lv = step_list[kb + i];
-      const int* rp = rowptr + (size_t)(lv & 0x3fffffffu) * n_tiles;
-      cp_async4(kst + i, rp);
-      cp_async4(koff + i, rp + 1);
-      kfl[i] = lv;
-      if (st.stdp_run) kpre[i] = __ldcg(pub + (lv & 0x3fffffffu));
-    }
     cp_async_wait_all();
-    __syncwarp();
+    __syncthreads();  // round r staged; every warp is done with round r - 1's buffer
+    const int kn = kb + BULK_STAGE_KEYS;
+    if (kn < n_list) {
+      if (kn % BULK_LIST_CHUNK == 0) {
+        stage_list(kn);
+        cp_async_wait_all();
+        __syncthreads();
+      }
+      stage_round(kn, buf ^ 1);
+    }
+    if (!active) continue;
+    const int* rp = rp_s + buf * BULK_STAGE_KEYS * BULK_RPW;
+    const uint32_t* kfl = kfl_s + buf * BULK_STAGE_KEYS;
+    const float* kpre = kpre_s + buf * BULK_STAGE_KEYS;
     for (int i = lane; i < nk; i += 32) {
-      const int len = koff[i] - kst[i];
+      const int len = rp[i * BULK_RPW + w + 1] - rp[i * BULK_RPW + w];
       koff[i] = len;
       if (kfl[i] >> 31) ev += (unsigned long long)len;
     }
@@ -593,7 +661,8 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB) bulk
       carry += __shfl_sync(FULL, incl, 31);
     }
     const int total_e = carry;
-    if (kb == 0) {
+    if (lane == 0) koff[nk] = total_e;
+    if (r == 0) {
       // A window pays when the step's entries (estimated from the first
       // round) would touch more sectors one by one than the window holds;
       // its reads overlap the first round's entry staging.
@@ -613,8 +682,8 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB) bulk
       const int nf = min(STAGE_ENTRIES, total_e - f0);
       for (int i = lane; i < nk; i += 32) {
         const int o = koff[i];
-        const int e0 = max(o, f0), e1 = min(o + (i + 1 < nk ? koff[i + 1] - o : total_e - o), f0 + nf);
-        const int base = kst[i] - o;
+        const int e0 = max(o, f0), e1 = min(koff[i + 1], f0 + nf);
+        const int base = rp[i * BULK_RPW + w] - o;
         for (int f = e0; f < e1; ++f) {
           sidx[f - f0] = (unsigned short)i;
           cp_async8(stage + (f - f0), entries + base + f);
@@ -705,6 +774,7 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB) bulk
       __syncwarp();
     }
   }
+  if (!active) return;
   dirty = __reduce_or_sync(FULL, dirty);
   if (dirty) {
     for (int k = 0; k < ws; ++k) {

@@ -220,8 +220,8 @@ struct spk_batch {
   // bulk-synchronous mode (spk_bulk.cuh)
   int mode = SPK_BATCH_WAVES;
   std::vector<NetDev> hds;       // host copies of the batch's descriptors
-  BulkTile* dtiles = nullptr;    // [tiles_total]
-  int tiles_total = 0;
+  BulkPropBlock* dpblocks = nullptr;  // [pblocks_total] propagation tile groups
+  int pblocks_total = 0;
   BulkBlock* dblocks = nullptr;  // [blocks_total] blocks of 32-key words with real keys
   int blocks_total = 0;
   BulkPostItem* items = nullptr; // afferent-pass work list of a timestep
@@ -1838,11 +1838,11 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
 
 namespace spk {
 
-// One block of K timesteps in bulk mode: 3K kernels and the run-counter update.
+// One block of K timesteps in bulk mode: 3K or 4K kernels (4 with plastic
+// networks) and the run-counter update.
 static int bulk_launch_block(spk_batch* b) {
   const int n = (int)b->nets.size();
-  const int T = b->tiles_total;
-  const int prop_smem = BULK_PROP_WARPS * bulk_warp_layout(b->win_words, b->ts_max).total * 4;
+  const int prop_smem = bulk_prop_layout(b->win_words, b->ts_max).total * 4;
   DeviceInfo di;
   const int rc0 = device_info(&di);
   if (rc0) return rc0;
@@ -1850,8 +1850,8 @@ static int bulk_launch_block(spk_batch* b) {
     bulk_neurons_kernel<<<b->blocks_total, BULK_NEUR_WARPS * 32, 0, b->stream>>>(b->dd, b->dblocks, s,
                                                                                   b->item_count);
     bulk_list_kernel<<<n, BULK_LIST_THREADS, 0, b->stream>>>(b->dd, s, b->items, b->item_count, b->item_cap);
-    bulk_prop_kernel<<<(T + BULK_PROP_WARPS - 1) / BULK_PROP_WARPS, BULK_PROP_WARPS * 32, prop_smem, b->stream>>>(
-        b->dd, b->dtiles, T, s, b->win_words, b->ts_max);
+    bulk_prop_kernel<<<b->pblocks_total, BULK_PROP_WARPS * 32, prop_smem, b->stream>>>(b->dd, b->dpblocks, s,
+                                                                                       b->win_words, b->ts_max);
     if (b->any_plastic)
       bulk_post_kernel<<<di.sms * 8, 256, 0, b->stream>>>(b->dd, b->items, b->item_count, b->item_cap);
   }
@@ -1944,17 +1944,19 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
   }
   return guarded([&]() -> int {
     if (!b->bulk_mem) {
-      std::vector<BulkTile> tiles;
+      std::vector<BulkPropBlock> tiles;
       std::vector<BulkBlock> words;
       size_t list_words = 0;
-      // propagation tiles of the networks with the most keys first: their
+      // propagation tile groups of the networks with the most keys first: their
       // warps walk the longest key lists, so they start before the short ones
       std::vector<int> by_keys(b->nets.size());
       for (size_t i = 0; i < by_keys.size(); ++i) by_keys[i] = (int)i;
       std::stable_sort(by_keys.begin(), by_keys.end(),
                        [&](int x, int y) { return b->nets[x]->plan.n_keys > b->nets[y]->plan.n_keys; });
       for (const int i : by_keys)
-        for (int t = 0; t < b->nets[i]->plan.n_tiles; ++t) tiles.push_back(BulkTile{i, t});
+        for (int t = 0; t < b->nets[i]->plan.n_tiles; t += BULK_PROP_WARPS)
+          tiles.push_back(BulkPropBlock{i, t, std::min(BULK_PROP_WARPS, b->nets[i]->plan.n_tiles - t), 0,
+                                        b->hds[i].ctl, nullptr});
       for (size_t i = 0; i < b->nets.size(); ++i) {
         const spk_net* n = b->nets[i];
         const int in_end = (n->Nin + 31) / 32, lif0 = n->plan.KL / 32, lif_end = (n->plan.KL + n->N + 31) / 32;
@@ -1985,7 +1987,7 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
         b->win_words = std::max(b->win_words, (n->hd.B - 3) * n->hd.TS * n->hd.L);
       }
       b->win_words = std::min(b->win_words, BULK_WIN_CAP);
-      const size_t t_bytes = align_up(sizeof(BulkTile) * tiles.size(), 256);
+      const size_t t_bytes = align_up(sizeof(BulkPropBlock) * tiles.size(), 256);
       const size_t w_bytes = align_up(sizeof(BulkBlock) * words.size(), 256);
       const size_t l_bytes = align_up(sizeof(uint32_t) * list_words, 256);
       const size_t c_bytes = align_up(sizeof(int) * (b->nets.size() + 1), 256);
@@ -1996,8 +1998,8 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
         set_error("bulk mode: device allocation failed");
         return SPK_ERR_OOM;
       }
-      b->dtiles = (BulkTile*)b->bulk_mem;
-      b->tiles_total = (int)tiles.size();
+      b->dpblocks = (BulkPropBlock*)b->bulk_mem;
+      b->pblocks_total = (int)tiles.size();
       b->dblocks = (BulkBlock*)((char*)b->bulk_mem + t_bytes);
       b->blocks_total = (int)words.size();
       uint32_t* lists = (uint32_t*)((char*)b->bulk_mem + t_bytes + w_bytes);
@@ -2010,7 +2012,8 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
         b->hds[i].step_count = counts + i;
         off += (size_t)b->nets[i]->plan.n_keys;
       }
-      SPK_CUDA(cudaMemcpy(b->dtiles, tiles.data(), sizeof(BulkTile) * tiles.size(), cudaMemcpyHostToDevice));
+      for (BulkPropBlock& pb : tiles) pb.n_list = counts + pb.net;
+      SPK_CUDA(cudaMemcpy(b->dpblocks, tiles.data(), sizeof(BulkPropBlock) * tiles.size(), cudaMemcpyHostToDevice));
       SPK_CUDA(cudaMemcpy(b->dblocks, words.data(), sizeof(BulkBlock) * words.size(), cudaMemcpyHostToDevice));
       // words of padding keys are never written in bulk mode: zero them once
       SPK_CUDA(cudaStreamSynchronize(b->stream));
@@ -2021,7 +2024,7 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       }
       SPK_CUDA(cudaMemcpy(b->dd, b->hds.data(), sizeof(NetDev) * b->hds.size(), cudaMemcpyHostToDevice));
       SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    BULK_PROP_WARPS * bulk_warp_layout(b->win_words, b->ts_max).total * 4));
+                                    bulk_prop_layout(b->win_words, b->ts_max).total * 4));
     }
     b->mode = mode;
     return SPK_OK;
