@@ -19,8 +19,8 @@
 //                        ring cells in HBM (the persistent kernel's rounds),
 //                        with the STDP pre pass;
 //   bulk_post_kernel     the post-spike afferent pass of every spiking post of
-//                        every network, in chunks of 128 afferents spread over
-//                        all warps (the list kernel builds the items).
+//                        every network, a warp per spiking post taken from a
+//                        shared list (the list kernel builds the items).
 //
 // Each ring cell still has one writer applying contributions in canonical
 // order, and every float operation is the persistent kernel's, so a network
@@ -283,11 +283,11 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
 // gives every key its place in ascending key order.
 constexpr int BULK_LIST_THREADS = 512;
 
-// Work item of the afferent pass: afferents [a0, a1) of spiking post `post`.
+// Work item of the afferent pass: spiking post `post` of network `net`.
 struct BulkPostItem {
-  int net, post, a0, a1;
+  int net, post;
 };
-constexpr int BULK_POST_CHUNK = 128;  // afferents per item (32 lanes x 4)
+constexpr int BULK_POST_CHUNK = 128;  // afferents per warp iteration (32 lanes x 4)
 
 __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetDev* __restrict__ nets, int s,
                                                                       BulkPostItem* items, int* item_count,
@@ -364,66 +364,53 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
     d.ctl->spike_count = sc > (unsigned long long)d.spike_cap ? (unsigned long long)d.spike_cap : sc;
   }
   if (!st.stdp_run) return;
-  // afferent-pass items of the spiking posts: chunks of BULK_POST_CHUNK
-  // plastic afferents, reserved in the shared item list with one atomic
+  // afferent-pass items: one per spiking post, reserved in the shared item
+  // list with one atomic per network
   const int wl0 = max(w0, KL >> 5);
-  unsigned long long nch = 0;
-  for (int i = wl0; i < w1; ++i) {
-    uint32_t a = d.bitsA[i];
-    while (a) {
-      const int b = __ffs(a) - 1;
-      a &= a - 1;
-      const int q = (i << 5) + b - KL;
-      const int deg = __ldg(d.csc_ptr + q + 1) - __ldg(d.csc_ptr + q);
-      nch += (unsigned long long)((deg + BULK_POST_CHUNK - 1) / BULK_POST_CHUNK);
-    }
-  }
-  unsigned long long ic = nch;
+  int nsp = 0;
+  for (int i = wl0; i < w1; ++i) nsp += __popc(d.bitsA[i]);
+  int ic = nsp;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const unsigned long long y = __shfl_up_sync(FULL, ic, o);
+    const int y = __shfl_up_sync(FULL, ic, o);
     if (lane >= o) ic += y;
   }
   __syncthreads();
-  if (lane == 31) warp_tot[w] = ic;
+  if (lane == 31) warp_tot[w] = (unsigned long long)ic;
   __syncthreads();
   if (w == 0) {
-    const unsigned long long v = lane < BULK_LIST_THREADS / 32 ? warp_tot[lane] : 0ull;
-    unsigned long long wi = v;
+    const int v = lane < BULK_LIST_THREADS / 32 ? (int)warp_tot[lane] : 0;
+    int wi = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const unsigned long long y = __shfl_up_sync(FULL, wi, o);
+      const int y = __shfl_up_sync(FULL, wi, o);
       if (lane >= o) wi += y;
     }
-    if (lane < BULK_LIST_THREADS / 32) warp_tot[lane] = wi - v;
-    if (lane == 31) s_item_base = wi > 0 ? atomicAdd(item_count, (int)wi) : 0;
+    if (lane < BULK_LIST_THREADS / 32) warp_tot[lane] = (unsigned long long)(wi - v);
+    if (lane == 31) s_item_base = wi > 0 ? atomicAdd(item_count, wi) : 0;
   }
   __syncthreads();
-  int ipos = s_item_base + (int)(warp_tot[w] + ic - nch);
+  int ipos = s_item_base + (int)warp_tot[w] + ic - nsp;
   for (int i = wl0; i < w1; ++i) {
     uint32_t a = d.bitsA[i];
     while (a) {
       const int b = __ffs(a) - 1;
       a &= a - 1;
-      const int q = (i << 5) + b - KL;
-      const int a0 = __ldg(d.csc_ptr + q), a1 = __ldg(d.csc_ptr + q + 1);
-      for (int x = a0; x < a1; x += BULK_POST_CHUNK) {
-        if (ipos < item_cap)
-          items[ipos] = BulkPostItem{(int)blockIdx.x, q, x, min(a1, x + BULK_POST_CHUNK)};
-        else
-          atomicCAS(&d.ctl->status, 0, SPK_ERR_OVERFLOW);
-        ++ipos;
-      }
+      if (ipos < item_cap)
+        items[ipos] = BulkPostItem{(int)blockIdx.x, (i << 5) + b - KL};
+      else
+        atomicCAS(&d.ctl->status, 0, SPK_ERR_OVERFLOW);
+      ++ipos;
     }
   }
 }
 
 // ---- timestep part 4: the post-spike afferent pass of every spiking post -----------------
-// Each warp takes items of the shared list in turn: up to BULK_POST_CHUNK
-// plastic afferents of one spiking post whose presynaptic key had no event
-// this step (those with an event were updated in the propagation kernel) get
-// their LTP update.  Each weight is updated at most once per step, so the
-// order of the items does not matter.
+// Each warp takes spiking posts of the shared item list in turn and gives the
+// post's plastic afferents whose presynaptic key had no event this step (those
+// with an event were updated in the propagation kernel) their LTP update,
+// BULK_POST_CHUNK afferents per iteration.  Each weight is updated at most once
+// per step, so the order of the items does not matter.
 __global__ void __launch_bounds__(256) bulk_post_kernel(const NetDev* __restrict__ nets,
                                                         const BulkPostItem* __restrict__ items,
                                                         const int* __restrict__ item_count, int item_cap) {
@@ -433,31 +420,39 @@ __global__ void __launch_bounds__(256) bulk_post_kernel(const NetDev* __restrict
   for (int it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < n_items; it += n_warps) {
     const BulkPostItem item = items[it];
     const NetDev& d = nets[item.net];
+    const int a0 = __ldg(d.csc_ptr + item.post), a1 = __ldg(d.csc_ptr + item.post + 1);
     const float post_tr = d.post_trace[item.post];
-    constexpr int AFF = BULK_POST_CHUNK / 32;
-    uint2 cc[AFF];
-#pragma unroll
-    for (int u = 0; u < AFF; ++u) {
-      const int ai = item.a0 + u * 32 + lane;
-      cc[u] = d.csc[ai < item.a1 ? ai : item.a0];
-    }
-    uint32_t vm[AFF];
-    float prt[AFF];
-#pragma unroll
-    for (int u = 0; u < AFF; ++u) {
-      const int pk = (int)cc[u].x;
-      vm[u] = d.bitsA[pk >> 5] | d.bitsP[pk >> 5];
-      prt[u] = d.pre_pub[pk];
-    }
+    const uint32_t* bA = d.bitsA;
+    const uint32_t* bP = d.bitsP;
+    const float* pub = d.pre_pub;
+    uint2* csc = d.csc;
+    const StdpConst sc = stdp_const(d);
     unsigned long long n_post = 0;
+    for (int a = a0; a < a1; a += BULK_POST_CHUNK) {
+      constexpr int AFF = BULK_POST_CHUNK / 32;
+      uint2 cc[AFF];
 #pragma unroll
-    for (int u = 0; u < AFF; ++u) {
-      const int ai = item.a0 + u * 32 + lane;
-      const int pk = (int)cc[u].x;
-      if (ai >= item.a1 || ((vm[u] >> (pk & 31)) & 1u)) continue;
-      const float nw = stdp_update(d, __uint_as_float(cc[u].y), false, true, post_tr, prt[u]);
-      d.csc[ai].y = __float_as_uint(nw);
-      ++n_post;
+      for (int u = 0; u < AFF; ++u) {
+        const int ai = a + u * 32 + lane;
+        cc[u] = csc[ai < a1 ? ai : a];
+      }
+      uint32_t vm[AFF];
+      float prt[AFF];
+#pragma unroll
+      for (int u = 0; u < AFF; ++u) {
+        const int pk = (int)cc[u].x;
+        vm[u] = bA[pk >> 5] | bP[pk >> 5];
+        prt[u] = pub[pk];
+      }
+#pragma unroll
+      for (int u = 0; u < AFF; ++u) {
+        const int ai = a + u * 32 + lane;
+        const int pk = (int)cc[u].x;
+        if (ai >= a1 || ((vm[u] >> (pk & 31)) & 1u)) continue;
+        const float nw = stdp_update(sc, __uint_as_float(cc[u].y), false, true, post_tr, prt[u]);
+        csc[ai].y = __float_as_uint(nw);
+        ++n_post;
+      }
     }
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) n_post += __shfl_xor_sync(FULL, n_post, o);

@@ -1966,12 +1966,11 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
           words.push_back(BulkBlock{(int)i, w, std::min(BULK_BLOCK_WORDS, lif_end - w), 0, b->hds[i].ctl, nullptr});
         list_words += (size_t)n->plan.n_keys;
       }
-      // afferent-pass items: at most one per started chunk of every spiking
-      // post's plastic afferents, i.e. n_csc / chunk + N per network
+      // afferent-pass items: at most one per post of every plastic network
       size_t cap = 0;
       for (const spk_net* n : b->nets)
         if (n->has_stdp) {
-          cap += (size_t)(n->n_csc / BULK_POST_CHUNK) + (size_t)n->N + 1;
+          cap += (size_t)n->N;
           b->any_plastic = true;
         }
       if (cap > 0x7fffffff) {
