@@ -33,10 +33,14 @@
 #include "spk_internal.h"
 #include "spk_kernel.cuh"
 
-// Tuning constants (measured on the 256-instance sweep): keys per round of the
-// propagation kernel, words per warp of the neuron kernel.
+// Tuning constants (measured on the 256-instance sweep): keys per round and
+// entries per stage of the propagation kernel, words per warp of the neuron
+// kernel.
 #ifndef SPK_BULK_STAGE_KEYS
 #define SPK_BULK_STAGE_KEYS 64
+#endif
+#ifndef SPK_BULK_STAGE_ENTRIES
+#define SPK_BULK_STAGE_ENTRIES 256
 #endif
 #ifndef SPK_BULK_WPW
 #define SPK_BULK_WPW 2
@@ -45,6 +49,7 @@
 namespace spk {
 
 constexpr int BULK_STAGE_KEYS = SPK_BULK_STAGE_KEYS;
+constexpr int BULK_STAGE_ENTRIES = SPK_BULK_STAGE_ENTRIES;  // entries staged per warp at a time
 
 // Timestep s of the current block of a network's run.
 struct BulkStep {
@@ -509,9 +514,9 @@ __host__ __device__ inline BulkPropLayout bulk_prop_layout(int win_words, int ts
   o = (o + 3) & ~3;
   l.cta = o;
   int p = 0;
-  l.stage = p; p += 2 * STAGE_ENTRIES;
-  l.stw = p; p += STAGE_ENTRIES;
-  l.sidx = p; p += STAGE_ENTRIES / 2;
+  l.stage = p; p += 2 * BULK_STAGE_ENTRIES;
+  l.stw = p; p += BULK_STAGE_ENTRIES;
+  l.sidx = p; p += BULK_STAGE_ENTRIES / 2;
   l.koff = p; p += BULK_STAGE_KEYS + 4;
   l.ptr = p; p += ts_max;       // post traces of the tile (plastic runs)
   l.spw = p; p += ts_max / 32;  // spike words of the tile's posts (plastic runs)
@@ -673,8 +678,8 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
       }
     }
     __syncwarp();
-    for (int f0 = 0; f0 < total_e; f0 += STAGE_ENTRIES) {
-      const int nf = min(STAGE_ENTRIES, total_e - f0);
+    for (int f0 = 0; f0 < total_e; f0 += BULK_STAGE_ENTRIES) {
+      const int nf = min(BULK_STAGE_ENTRIES, total_e - f0);
       for (int i = lane; i < nk; i += 32) {
         const int o = koff[i];
         const int e0 = max(o, f0), e1 = min(koff[i + 1], f0 + nf);
