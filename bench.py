@@ -599,7 +599,8 @@ def run_batched(args, rank, world, local):
                             trace_keys * timesteps)
     bulk = mode == N.SPK_BATCH_BULK
     # waves: one launch of the persistent kernel per wave and block; bulk: the
-    # unit is one timestep of all instances (three kernels)
+    # unit is one timestep of all instances (neuron, list, propagation and,
+    # with plastic instances, afferent-pass kernels)
     units = timesteps if bulk else max(launches, 1)
     per_launch_s = (ms / 1000.0) / units
     per_launch_bytes = alg / units
@@ -609,8 +610,8 @@ def run_batched(args, rank, world, local):
     traffic = None
     if tr and tr.get("traffic_per_alg_byte"):
         traffic = tr["traffic_per_alg_byte"] * per_launch_bytes
-    roof_kernel = ("spk::bulk_neurons_kernel + bulk_list_kernel + bulk_prop_kernel (one timestep of all instances)"
-                   if bulk else "spk::step_kernel")
+    roof_kernel = ("spk::bulk_neurons_kernel + bulk_list_kernel + bulk_prop_kernel + bulk_post_kernel "
+                   "(one timestep of all instances)" if bulk else "spk::step_kernel")
 
     # plain form: the same instances, each alone on its own stream, one after another
     plain_ev, plain_ms = 0, 0.0
