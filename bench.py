@@ -65,7 +65,7 @@ def parse():
     p.add_argument("--scale", type=float, default=1.0, help="plastic_ff: network size factor (profiling cases)")
     p.add_argument("--tune-steps", type=int, default=100, help="batched: autotuner trial timesteps")
     p.add_argument("--mode", default="auto", choices=["auto", "waves", "bulk"],
-                   help="batched: execution mode (auto: the autotuner's choice; waves without the autotuner)")
+                   help="batched: execution mode (auto: the autotuner's choice; waves without the autotuner); served: waves, else bulk")
     p.add_argument("--no-tune", action="store_true",
                    help="batched: skip the autotuner (8 warps, tiles of up to 64 posts, costs from synapse counts)")
     p.add_argument("--plain-block", type=int, default=200,
@@ -737,7 +737,8 @@ def run_served(args, rank, world, local):
     if rank != 0:
         return
     reqs = served_requests(args.duration, args.arrival_rate)
-    srv = Server(steps_per_block=args.block, record_spikes=False)
+    mode = N.SPK_BATCH_WAVES if args.mode == "waves" else N.SPK_BATCH_BULK
+    srv = Server(steps_per_block=args.block, record_spikes=False, mode=mode)
     ids = []
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
@@ -760,7 +761,8 @@ def run_served(args, rank, world, local):
             "n_gpus": 1, "steps": len(ids), "warmup": 0, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "ours",
             "config": {"workload": f"served_stream_rate{args.arrival_rate:g}_N2k-100k_T0.5-5s_stdp30pct",
-                       "arrival_window_s": args.duration, "block_timesteps": args.block},
+                       "arrival_window_s": args.duration, "block_timesteps": args.block,
+                       "mode": "waves" if mode == N.SPK_BATCH_WAVES else "bulk"},
             "sim_s_per_wall_s": sim_done / window,
             "latency_s": {"p50": float(np.percentile(lat, 50)) if lat else None,
                           "p99": float(np.percentile(lat, 99)) if lat else None, "n": len(lat)},

@@ -310,13 +310,14 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int n_words = d.n_words, KL = d.KL;
   const bool rec_inputs = c.record_inputs != 0;
+  const bool recording = d.spike_cap > 0;  // a network created without a spike store records nothing
   const int per = (n_words + BULK_LIST_THREADS - 1) / BULK_LIST_THREADS;
   const int w0 = min(n_words, threadIdx.x * per), w1 = min(n_words, w0 + per);
   // counts: list keys (low 32 bits) and recorded spikes (high 32 bits)
   unsigned long long cnt = 0;
   for (int i = w0; i < w1; ++i) {
     const uint32_t a = d.bitsA[i], p = d.bitsP[i];
-    const bool rec = (i << 5) >= KL || rec_inputs;
+    const bool rec = recording && ((i << 5) >= KL || rec_inputs);
     cnt += (unsigned long long)__popc(a | p) + (rec ? ((unsigned long long)__popc(a) << 32) : 0ull);
   }
   unsigned long long incl = cnt;
@@ -345,7 +346,7 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
   unsigned long long sp = sc0 + (excl >> 32);
   for (int i = w0; i < w1; ++i) {
     const uint32_t a = d.bitsA[i], p = d.bitsP[i];
-    const bool rec = (i << 5) >= KL || rec_inputs;
+    const bool rec = recording && ((i << 5) >= KL || rec_inputs);
     uint32_t m = a | p;
     while (m) {
       const int b = __ffs(m) - 1;

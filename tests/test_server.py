@@ -54,6 +54,25 @@ def test_served_jobs_equal_each_job_alone_and_overlap(mode):
     srv.stop()
 
 
+@pytest.mark.parametrize("mode", [N.SPK_BATCH_WAVES, N.SPK_BATCH_BULK])
+def test_served_jobs_without_spike_recording(mode):
+    """A server that records no spikes creates its networks without a spike
+    store; the jobs still finish and deliver the events of the same job run
+    alone."""
+    work = jobs(k=4, seed=13)
+    srv = Server(steps_per_block=200, reserve_bytes=1 << 30, mode=mode, record_spikes=False)
+    ids = [srv.submit(gen, steps, plastic) for gen, steps, plastic in work]
+    infos = [srv.wait(j, 300.0) for j in ids]
+    assert all(inf.state == N.SPK_JOB_DONE for inf in infos), [inf.state for inf in infos]
+    for (gen, steps, plastic), inf in zip(work, infos):
+        ref = Net.generate(gen)
+        ref.run_steps(steps, plastic)
+        assert ref.synchronize() == 0
+        assert inf.steps_done == steps and inf.events == ref.events()
+        ref.close()
+    srv.stop()
+
+
 def test_cancel_and_stop_with_work_queued():
     work = jobs(k=5, seed=4)
     srv = Server(steps_per_block=200, reserve_bytes=1 << 30)
