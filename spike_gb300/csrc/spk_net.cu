@@ -232,6 +232,10 @@ struct spk_batch {
   int ts_max = 0;               // largest post tile of the batch
   void* bulk_mem = nullptr;      // tiles, step lists and counts
   cudaGraphExec_t bulk_graph = nullptr;  // one block of K timesteps
+  // The afferent pass runs beside the propagation kernel (they update
+  // disjoint weights: afferents with and without a presynaptic event).
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 namespace spk {
@@ -1850,10 +1854,15 @@ static int bulk_launch_block(spk_batch* b) {
     bulk_neurons_kernel<<<b->blocks_total, BULK_NEUR_WARPS * 32, 0, b->stream>>>(b->dd, b->dblocks, s,
                                                                                   b->item_count);
     bulk_list_kernel<<<n, BULK_LIST_THREADS, 0, b->stream>>>(b->dd, s, b->items, b->item_count, b->item_cap);
+    if (b->any_plastic) {
+      SPK_CUDA(cudaEventRecord(b->fork, b->stream));
+      SPK_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0));
+      bulk_post_kernel<<<di.sms * 8, 256, 0, b->side>>>(b->dd, b->items, b->item_count, b->item_cap);
+      SPK_CUDA(cudaEventRecord(b->join, b->side));
+    }
     bulk_prop_kernel<<<b->pblocks_total, BULK_PROP_WARPS * 32, prop_smem, b->stream>>>(b->dd, b->dpblocks, s,
                                                                                        b->win_words, b->ts_max);
-    if (b->any_plastic)
-      bulk_post_kernel<<<di.sms * 8, 256, 0, b->stream>>>(b->dd, b->items, b->item_count, b->item_cap);
+    if (b->any_plastic) SPK_CUDA(cudaStreamWaitEvent(b->stream, b->join, 0));
   }
   bulk_finish_kernel<<<(n + 255) / 256, 256, 0, b->stream>>>(b->dd, n, b->K);
   SPK_CUDA(cudaGetLastError());
@@ -1978,6 +1987,14 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
         return SPK_ERR_UNSUPPORTED;
       }
       b->item_cap = (int)cap;
+      if (b->any_plastic && !b->side &&
+          (cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+           cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+           cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess)) {
+        cudaGetLastError();
+        set_error("bulk mode: stream or event creation failed");
+        return SPK_ERR_CUDA;
+      }
       // ring windows: the longest delay's slots of the largest tile, capped
       b->win_words = 0;
       b->ts_max = 0;
@@ -2103,6 +2120,12 @@ int spk_batch_destroy(spk_batch* b) {
     cudaStreamDestroy(b->stream);
   }
   if (b->done) cudaEventDestroy(b->done);
+  if (b->side) {
+    cudaStreamSynchronize(b->side);
+    cudaStreamDestroy(b->side);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
   if (b->bulk_graph) cudaGraphExecDestroy(b->bulk_graph);
   if (b->bulk_mem) cudaFree(b->bulk_mem);
   cudaFree(b->dd);
