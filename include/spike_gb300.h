@@ -331,6 +331,19 @@ int spk_batch_run_steps_each(spk_batch* batch, const int64_t* n_steps, const int
 int spk_batch_synchronize(spk_batch* batch);
 int spk_batch_launch_count(const spk_batch* batch, int64_t* launches);
 int spk_batch_stream(const spk_batch* batch, void** stream);
+/* Spikes of every network of the batch in one call: network after network,
+ * each exactly as spk_net_read_spikes gives it (canonical order), gathered on
+ * the device and copied with one transfer for ids and one for times (page-
+ * locked ids/times buffers make it a direct DMA).  counts[n_nets] receives each
+ * network's number of spikes of `population`; ids/times hold their sum.  If
+ * the sum exceeds capacity nothing is copied and SPK_ERR_OVERFLOW is returned
+ * (counts are still set).  clear != 0 then empties every network's store, as
+ * spk_net_clear_spikes.  Replaces, for a batch, spk_net_spike_count +
+ * spk_net_read_spikes + spk_net_clear_spikes per network (the monitor readback
+ * of Spike/ActivityMonitor/SpikingActivityMonitor.cpp:79-153, done once for all
+ * networks). */
+int spk_batch_read_spikes(spk_batch* batch, int32_t population, int32_t* ids, float* times,
+                          int64_t capacity, int64_t* counts, int32_t clear);
 int spk_batch_destroy(spk_batch* batch);
 /* Measured schedule search for a batch of generated networks (batching has
  * no counterpart in the reference).  Tries a fixed set of policies (warps per

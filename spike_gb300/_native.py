@@ -202,6 +202,7 @@ _SIGS = {
     "spk_batch_synchronize": (i32, [_VP]),
     "spk_batch_launch_count": (i32, [_VP, P(i64)]),
     "spk_batch_stream": (i32, [_VP, P(_VP)]),
+    "spk_batch_read_spikes": (i32, [_VP, i32, P(i32), P(f32), i64, P(i64), i32]),
     "spk_batch_destroy": (i32, [_VP]),
     "spk_batch_autotune": (i32, [P(GenDesc), i32, i32, P(Schedule), P(f32), P(f32), P(i32)]),
     "spk_net_set_step_cost": (i32, [_VP, f32]),

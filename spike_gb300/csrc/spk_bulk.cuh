@@ -96,7 +96,10 @@ __device__ __forceinline__ RunCtl load_ctl(const RunCtl* p) {
 #define SPK_BULK_NEUR_MINB 6
 #endif
 constexpr int BULK_WPW = SPK_BULK_WPW;
-constexpr int BULK_NEUR_WARPS = 8;
+#ifndef SPK_BULK_NEUR_WARPS
+#define SPK_BULK_NEUR_WARPS 8
+#endif
+constexpr int BULK_NEUR_WARPS = SPK_BULK_NEUR_WARPS;
 constexpr int BULK_BLOCK_WORDS = BULK_NEUR_WARPS * BULK_WPW;
 
 struct BulkBlock {

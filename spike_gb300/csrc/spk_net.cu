@@ -236,6 +236,13 @@ struct spk_batch {
   // disjoint weights: afferents with and without a presynaptic event).
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+  // spike readback of the whole batch (spk_batch_read_spikes)
+  cudaEvent_t rd = nullptr;
+  void* rb_mem = nullptr;       // counts, chunk list, chunk matches
+  size_t rb_bytes = 0;
+  int32_t* rb_ids = nullptr;    // gathered spikes
+  float* rb_times = nullptr;
+  int64_t rb_cap = 0;
 };
 
 namespace spk {
@@ -2113,6 +2120,193 @@ int spk_batch_stream(const spk_batch* b, void** stream) {
   return SPK_OK;
 }
 
+// ---- spike readback of a whole batch ------------------------------------------------------
+namespace spk {
+constexpr int SPIKE_CHUNK = 4096;  // store entries per gather CTA
+struct SpikeChunk {
+  int net;
+  int n;             // entries in the chunk
+  long long start;   // first entry of the network's store
+  long long out;     // first output slot of its matching entries
+};
+
+__global__ void spike_counts_kernel(const NetDev* __restrict__ nets, int n_nets, unsigned long long* counts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_nets) return;
+  const unsigned long long c = nets[i].ctl->spike_count;
+  const unsigned long long cap = (unsigned long long)nets[i].spike_cap;
+  counts[i] = c < cap ? c : cap;
+}
+
+// Entries of `population` in each chunk (networks that record their inputs
+// mix both populations in one store).
+__global__ void spike_match_kernel(const NetDev* __restrict__ nets, const SpikeChunk* __restrict__ chunks,
+                                   int population, int* matches) {
+  __shared__ int s_tot;
+  const SpikeChunk ch = chunks[blockIdx.x];
+  const NetDev& d = nets[ch.net];
+  if (threadIdx.x == 0) s_tot = 0;
+  __syncthreads();
+  int m = 0;
+  for (int i = threadIdx.x; i < ch.n; i += blockDim.x) {
+    const bool is_neuron = (int)d.spikes[ch.start + i].x >= d.KL;
+    m += is_neuron == (population == SPK_POP_NEURONS);
+  }
+  atomicAdd(&s_tot, m);
+  __syncthreads();
+  if (threadIdx.x == 0) matches[blockIdx.x] = s_tot;
+}
+
+// Matching entries of each chunk, in store order, as (id, time) at the
+// chunk's output slot (ids as spk_net_read_spikes gives them).
+__global__ void __launch_bounds__(256) spike_gather_kernel(const NetDev* __restrict__ nets,
+                                                           const SpikeChunk* __restrict__ chunks, int population,
+                                                           int32_t* ids, float* times) {
+  __shared__ int warp_n[8];
+  const SpikeChunk ch = chunks[blockIdx.x];
+  const NetDev& d = nets[ch.net];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int KL = d.KL, Nin = d.Nin;
+  long long out = ch.out;
+  for (int base = 0; base < ch.n; base += 256) {
+    const int i = base + (int)threadIdx.x;
+    uint2 e = make_uint2(0u, 0u);
+    bool m = false;
+    if (i < ch.n) {
+      e = d.spikes[ch.start + i];
+      m = ((int)e.x >= KL) == (population == SPK_POP_NEURONS);
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, m);
+    if (lane == 0) warp_n[w] = __popc(bal);
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int k = 0; k < 8; ++k) {
+      before += k < w ? warp_n[k] : 0;
+      total += warp_n[k];
+    }
+    if (m) {
+      const long long o = out + before + __popc(bal & ((1u << lane) - 1u));
+      const int key = (int)e.x;
+      ids[o] = key >= KL ? key - KL : Nin - 1 - key;
+      times[o] = __uint_as_float(e.y);
+    }
+    out += total;
+    __syncthreads();
+  }
+}
+
+__global__ void clear_stores_kernel(const NetDev* __restrict__ nets, int n_nets) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_nets) return;
+  RunCtl* ctl = nets[i].ctl;
+  ctl->spike_count = 0ull;
+  if (ctl->status == SPK_ERR_OVERFLOW) ctl->status = 0;
+}
+}  // namespace spk
+
+int spk_batch_read_spikes(spk_batch* b, int32_t population, int32_t* ids, float* times, int64_t capacity,
+                          int64_t* counts, int32_t clear) {
+  if (!b || population < 0 || population > 1 || capacity < 0 || !counts) return SPK_ERR_INVALID;
+  return guarded([&]() -> int {
+    const int n = (int)b->nets.size();
+    // after each network's own stream (per-network calls, runs alone)
+    if (!b->rd) SPK_CUDA(cudaEventCreateWithFlags(&b->rd, cudaEventDisableTiming));
+    for (spk_net* nt : b->nets) {
+      SPK_CUDA(cudaEventRecord(b->rd, nt->stream));
+      SPK_CUDA(cudaStreamWaitEvent(b->stream, b->rd, 0));
+    }
+    const size_t c_bytes = align_up(sizeof(unsigned long long) * n, 256);
+    auto scratch = [&](size_t bytes) -> int {
+      if (bytes <= b->rb_bytes) return SPK_OK;
+      if (b->rb_mem) cudaFree(b->rb_mem);
+      b->rb_mem = nullptr;
+      b->rb_bytes = 0;
+      if (cudaMalloc(&b->rb_mem, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("spike readback: device allocation failed");
+        return SPK_ERR_OOM;
+      }
+      b->rb_bytes = bytes;
+      return SPK_OK;
+    };
+    int rc = scratch(c_bytes);
+    if (rc) return rc;
+    unsigned long long* dcounts = (unsigned long long*)b->rb_mem;
+    spike_counts_kernel<<<(n + 255) / 256, 256, 0, b->stream>>>(b->dd, n, dcounts);
+    std::vector<unsigned long long> stored(n);
+    SPK_CUDA(cudaMemcpyAsync(stored.data(), dcounts, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost,
+                             b->stream));
+    SPK_CUDA(cudaStreamSynchronize(b->stream));
+    std::vector<SpikeChunk> chunks;
+    bool mixed = false;
+    for (int i = 0; i < n; ++i) {
+      mixed = mixed || b->nets[i]->record_inputs;
+      for (unsigned long long st = 0; st < stored[i]; st += SPIKE_CHUNK)
+        chunks.push_back(SpikeChunk{i, (int)std::min<unsigned long long>(SPIKE_CHUNK, stored[i] - st),
+                                    (long long)st, 0});
+    }
+    const int nch = (int)chunks.size();
+    const size_t ch_bytes = align_up(sizeof(SpikeChunk) * std::max(nch, 1), 256);
+    const size_t m_bytes = align_up(sizeof(int) * std::max(nch, 1), 256);
+    rc = scratch(c_bytes + ch_bytes + m_bytes);
+    if (rc) return rc;
+    SpikeChunk* dchunks = (SpikeChunk*)((char*)b->rb_mem + c_bytes);
+    int* dmatch = (int*)((char*)b->rb_mem + c_bytes + ch_bytes);
+    std::vector<int> match(nch);
+    if (mixed && nch) {
+      SPK_CUDA(cudaMemcpyAsync(dchunks, chunks.data(), sizeof(SpikeChunk) * nch, cudaMemcpyHostToDevice, b->stream));
+      spike_match_kernel<<<nch, 256, 0, b->stream>>>(b->dd, dchunks, population, dmatch);
+      SPK_CUDA(cudaMemcpyAsync(match.data(), dmatch, sizeof(int) * nch, cudaMemcpyDeviceToHost, b->stream));
+      SPK_CUDA(cudaStreamSynchronize(b->stream));
+    } else {
+      // a store without inputs holds neuron spikes only
+      for (int c = 0; c < nch; ++c) match[c] = population == SPK_POP_NEURONS ? chunks[c].n : 0;
+    }
+    long long total = 0;
+    for (int i = 0; i < n; ++i) counts[i] = 0;
+    for (int c = 0; c < nch; ++c) {
+      chunks[c].out = total;
+      total += match[c];
+      counts[chunks[c].net] += match[c];
+    }
+    if (total > capacity) {
+      set_error("spike readback: %lld spikes exceed the capacity %lld", total, (long long)capacity);
+      return SPK_ERR_OVERFLOW;
+    }
+    if (total > 0) {
+      if (total > b->rb_cap) {
+        if (b->rb_ids) cudaFree(b->rb_ids);
+        if (b->rb_times) cudaFree(b->rb_times);
+        b->rb_ids = nullptr;
+        b->rb_times = nullptr;
+        b->rb_cap = 0;
+        const int64_t cap = total + total / 4;
+        if (cudaMalloc(&b->rb_ids, sizeof(int32_t) * cap) != cudaSuccess ||
+            cudaMalloc(&b->rb_times, sizeof(float) * cap) != cudaSuccess) {
+          cudaGetLastError();
+          set_error("spike readback: device allocation failed");
+          return SPK_ERR_OOM;
+        }
+        b->rb_cap = cap;
+      }
+      SPK_CUDA(cudaMemcpyAsync(dchunks, chunks.data(), sizeof(SpikeChunk) * nch, cudaMemcpyHostToDevice, b->stream));
+      spike_gather_kernel<<<nch, 256, 0, b->stream>>>(b->dd, dchunks, population, b->rb_ids, b->rb_times);
+      SPK_CUDA(cudaGetLastError());
+      if (ids)
+        SPK_CUDA(cudaMemcpyAsync(ids, b->rb_ids, sizeof(int32_t) * total, cudaMemcpyDeviceToHost, b->stream));
+      if (times)
+        SPK_CUDA(cudaMemcpyAsync(times, b->rb_times, sizeof(float) * total, cudaMemcpyDeviceToHost, b->stream));
+    }
+    if (clear) clear_stores_kernel<<<(n + 255) / 256, 256, 0, b->stream>>>(b->dd, n);
+    SPK_CUDA(cudaGetLastError());
+    // later calls on the networks' own streams see the cleared stores
+    SPK_CUDA(cudaEventRecord(b->rd, b->stream));
+    for (spk_net* nt : b->nets) SPK_CUDA(cudaStreamWaitEvent(nt->stream, b->rd, 0));
+    SPK_CUDA(cudaStreamSynchronize(b->stream));
+    return SPK_OK;
+  });
+}
+
 int spk_batch_destroy(spk_batch* b) {
   if (!b) return SPK_ERR_INVALID;
   if (b->stream) {
@@ -2126,6 +2320,10 @@ int spk_batch_destroy(spk_batch* b) {
   }
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->join) cudaEventDestroy(b->join);
+  if (b->rd) cudaEventDestroy(b->rd);
+  if (b->rb_mem) cudaFree(b->rb_mem);
+  if (b->rb_ids) cudaFree(b->rb_ids);
+  if (b->rb_times) cudaFree(b->rb_times);
   if (b->bulk_graph) cudaGraphExecDestroy(b->bulk_graph);
   if (b->bulk_mem) cudaFree(b->bulk_mem);
   cudaFree(b->dd);

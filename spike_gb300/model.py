@@ -368,7 +368,7 @@ class Batch:
               "spk_batch_create")
 
     def set_mode(self, mode: int):
-        """SPK_BATCH_WAVES (persistent kernel) or SPK_BATCH_BULK (three
+        """SPK_BATCH_WAVES (persistent kernel) or SPK_BATCH_BULK (four
         kernels per timestep over all networks)."""
         check(lib().spk_batch_set_mode(self.h, mode), "spk_batch_set_mode")
 
@@ -407,6 +407,35 @@ class Batch:
         s = C.c_void_p()
         check(lib().spk_batch_stream(self.h, C.byref(s)), "spk_batch_stream")
         return s.value or 0
+
+    def read_spikes_into(self, ids_ptr: int, times_ptr: int, capacity: int,
+                         population: int = N.SPK_POP_NEURONS, clear: bool = False):
+        """spk_batch_read_spikes into caller buffers (addresses of int32 ids and
+        float32 times, page-locked for a direct copy).  Returns each network's
+        count, or None when their sum exceeds capacity (nothing copied)."""
+        counts = np.zeros(len(self.nets), np.int64)
+        rc = lib().spk_batch_read_spikes(self.h, population, C.cast(C.c_void_p(ids_ptr), C.POINTER(C.c_int32)),
+                                         C.cast(C.c_void_p(times_ptr), C.POINTER(C.c_float)), capacity,
+                                         counts.ctypes.data_as(C.POINTER(C.c_int64)), 1 if clear else 0)
+        if rc == N.SPK_ERR_OVERFLOW:
+            return None
+        check(rc, "spk_batch_read_spikes")
+        return counts
+
+    def spikes(self, population: int = N.SPK_POP_NEURONS, clear: bool = False):
+        """Every network's spikes in one call: a list of (ids, times), one per
+        network, each as Net.spikes gives it."""
+        cap = 1 << 16
+        while True:
+            ids = np.empty(cap, np.int32)
+            times = np.empty(cap, np.float32)
+            counts = self.read_spikes_into(ids.ctypes.data, times.ctypes.data, cap, population, clear)
+            if counts is not None:
+                break
+            cap *= 4
+        ends = np.cumsum(counts)
+        starts = ends - counts
+        return [(ids[a:e], times[a:e]) for a, e in zip(starts, ends)]
 
     def close(self):
         if self.h:

@@ -109,3 +109,35 @@ def test_bulk_mode_equals_each_instance_alone(plastic_first):
         for k in sx:
             np.testing.assert_array_equal(sx[k], sy[k], err_msg=k)
     b.close()
+
+
+@pytest.mark.parametrize("mode", [N.SPK_BATCH_WAVES, N.SPK_BATCH_BULK])
+def test_batch_spike_readback_equals_per_network_reads(mode):
+    """spk_batch_read_spikes gives every network's spikes exactly as the
+    per-network read does, for both populations (one network records its
+    inputs, so its store mixes them), and clears every store."""
+    from test_generate import small_gen
+    gens = small_sweep(k=6, seed=8) + [small_gen(seed=21)]
+    nets = [Net.generate(g) for g in gens]
+    b = Batch(nets)
+    b.set_mode(mode)
+    b.run_steps(300, True)
+    assert b.synchronize() == 0
+
+    def same_as_alone(got, pop):
+        assert len(got) == len(nets)
+        for (gi, gt), n in zip(got, nets):
+            ri, rt = n.spikes(pop)
+            np.testing.assert_array_equal(gi, ri)
+            np.testing.assert_array_equal(bits(gt), bits(rt))
+        return sum(len(i) for i, _ in got)
+
+    assert same_as_alone(b.spikes(N.SPK_POP_NEURONS), N.SPK_POP_NEURONS) > 1000
+    assert same_as_alone(b.spikes(N.SPK_POP_INPUTS), N.SPK_POP_INPUTS) > 0
+    assert b.read_spikes_into(0, 0, 0) is None  # too small: nothing copied
+    b.spikes(clear=True)
+    assert all(len(n.spikes()[0]) == 0 and len(n.spikes(N.SPK_POP_INPUTS)[0]) == 0 for n in nets)
+    b.run_steps(100, True)
+    assert b.synchronize() == 0
+    assert same_as_alone(b.spikes(), N.SPK_POP_NEURONS) > 0
+    b.close()
