@@ -49,6 +49,17 @@
 namespace spk {
 
 constexpr int BULK_STAGE_KEYS = SPK_BULK_STAGE_KEYS;
+
+// Programmatic dependent launch: a timestep's kernels are launched so that the
+// next one's CTAs may start while this one drains.  Each kernel reads only
+// static data (block records, descriptors, run control) before pdl_wait(),
+// which returns once the previous kernel has completed and its writes are
+// visible, and lets its own dependents launch only after that, so every
+// earlier kernel of the stream has completed too.
+__device__ __forceinline__ void pdl_wait_then_release() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 constexpr int BULK_STAGE_ENTRIES = SPK_BULK_STAGE_ENTRIES;  // entries staged per warp at a time
 
 // Timestep s of the current block of a network's run.
@@ -164,7 +175,6 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
   __shared__ __align__(16) NetDev sd;
   __shared__ RunCtl sctl;
   static_assert(sizeof(NetDev) % 4 == 0, "descriptor copied as words");
-  if (blockIdx.x == 0 && threadIdx.x == 0) *item_count = 0;  // the afferent-pass list of this step
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const BulkBlock bb = blocks[blockIdx.x];
   {
@@ -173,6 +183,8 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
     for (int i = threadIdx.x; i < (int)(sizeof(NetDev) / 4); i += blockDim.x) dst[i] = __ldg(src + i);
     if (threadIdx.x == 0) sctl = load_ctl(bb.ctl);
   }
+  pdl_wait_then_release();
+  if (blockIdx.x == 0 && threadIdx.x == 0) *item_count = 0;  // the afferent-pass list of this step
   __syncthreads();
   const NetDev& d = sd;
   const BulkStep st = bulk_step(d, sctl, s);
@@ -306,6 +318,7 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
   const NetDev& d = nets[blockIdx.x];
   const RunCtl c = load_ctl(d.ctl);
   const BulkStep st = bulk_step(d, c, s);
+  pdl_wait_then_release();
   if (!st.live) {
     if (threadIdx.x == 0) *d.step_count = 0;
     return;
@@ -548,11 +561,10 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
     const uint32_t* src = (const uint32_t*)(nets + pb.net);
     uint32_t* dst = (uint32_t*)&sd;
     for (int i = threadIdx.x; i < (int)(sizeof(NetDev) / 4); i += nthr) dst[i] = __ldg(src + i);
-    if (threadIdx.x == 0) {
-      sctl = load_ctl(pb.ctl);
-      s_nlist = *pb.n_list;
-    }
+    if (threadIdx.x == 0) sctl = load_ctl(pb.ctl);
   }
+  pdl_wait_then_release();
+  if (threadIdx.x == 0) s_nlist = *pb.n_list;
   __syncthreads();
   const NetDev& d = sd;
   const BulkStep st = bulk_step(d, sctl, s);

@@ -91,6 +91,24 @@ static int device_info(DeviceInfo* di) {
   return SPK_OK;
 }
 
+// A launch that may begin while the stream's previous kernel drains (the
+// kernel waits for it with griddepcontrol.wait before touching its outputs).
+template <typename... P, typename... A>
+static cudaError_t launch_overlapped(void (*k)(P...), int grid, int block, size_t smem, cudaStream_t st,
+                                     A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 struct Plan {
   int W, TS, ITS, nctas, n_tiles, KL, n_keys, n_words, K, smem;
 };
@@ -1858,17 +1876,19 @@ static int bulk_launch_block(spk_batch* b) {
   const int rc0 = device_info(&di);
   if (rc0) return rc0;
   for (int s = 0; s < b->K; ++s) {
-    bulk_neurons_kernel<<<b->blocks_total, BULK_NEUR_WARPS * 32, 0, b->stream>>>(b->dd, b->dblocks, s,
-                                                                                  b->item_count);
-    bulk_list_kernel<<<n, BULK_LIST_THREADS, 0, b->stream>>>(b->dd, s, b->items, b->item_count, b->item_cap);
+    SPK_CUDA(launch_overlapped(bulk_neurons_kernel, b->blocks_total, BULK_NEUR_WARPS * 32, 0, b->stream,
+                               (const NetDev*)b->dd, (const BulkBlock*)b->dblocks, s, b->item_count));
+    SPK_CUDA(launch_overlapped(bulk_list_kernel, n, BULK_LIST_THREADS, 0, b->stream, (const NetDev*)b->dd, s,
+                               b->items, b->item_count, b->item_cap));
     if (b->any_plastic) {
       SPK_CUDA(cudaEventRecord(b->fork, b->stream));
       SPK_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0));
       bulk_post_kernel<<<di.sms * 8, 256, 0, b->side>>>(b->dd, b->items, b->item_count, b->item_cap);
       SPK_CUDA(cudaEventRecord(b->join, b->side));
     }
-    bulk_prop_kernel<<<b->pblocks_total, BULK_PROP_WARPS * 32, prop_smem, b->stream>>>(b->dd, b->dpblocks, s,
-                                                                                       b->win_words, b->ts_max);
+    SPK_CUDA(launch_overlapped(bulk_prop_kernel, b->pblocks_total, BULK_PROP_WARPS * 32, (size_t)prop_smem,
+                               b->stream, (const NetDev*)b->dd, (const BulkPropBlock*)b->dpblocks, s, b->win_words,
+                               b->ts_max));
     if (b->any_plastic) SPK_CUDA(cudaStreamWaitEvent(b->stream, b->join, 0));
   }
   bulk_finish_kernel<<<(n + 255) / 256, 256, 0, b->stream>>>(b->dd, n, b->K);
