@@ -421,13 +421,13 @@ def batched_config(gens, n_syn=None):
 BATCH_CPU_MAX_N = 8000       # instances up to this size are drawn on the host in about a second
 
 
-def cpu_sample_gens(gens):
-    """Instances of the sweep spread over its sizes up to BATCH_CPU_MAX_N
-    neurons (their synapse lists are cheap to draw on the host with the
-    oracle's restatement of the generator)."""
+def cpu_sample_gens(gens, count=BATCH_CPU_INSTANCES):
+    """`count` instances of the sweep spread over its sizes up to
+    BATCH_CPU_MAX_N neurons (their synapse lists are cheap to draw on the host
+    with the oracle's restatement of the generator)."""
     order = sorted(range(len(gens)), key=lambda k: gens[k].desc.n_neurons)
     small = [k for k in order if gens[k].desc.n_neurons <= BATCH_CPU_MAX_N] or order[:1]
-    n = min(BATCH_CPU_INSTANCES, len(small))
+    n = min(count, len(small))
     pick = [small[(i * (len(small) - 1)) // max(n - 1, 1)] for i in range(n)]
     return [gens[k] for k in pick]
 
@@ -456,8 +456,8 @@ def oracle_instance(gen):
 class CpuSample:
     """The oracle on the CPU sample of the sweep, built once."""
 
-    def __init__(self, gens):
-        picked = cpu_sample_gens(gens)
+    def __init__(self, gens, count=BATCH_CPU_INSTANCES):
+        picked = cpu_sample_gens(gens, count)
         self.nets = [oracle_instance(g)[0] for g in picked]
         sizes = [g.desc.n_neurons for g in picked]
         self.label = f"{len(self.nets)} instances of the sweep (N {min(sizes)}-{max(sizes)})"
@@ -495,8 +495,9 @@ def run_reference_batched(args, rank, world):
         return
     from spike_gb300 import networks
     gens = networks.batched_sweep(args.instances)
-    threads = min(os.cpu_count() or 1, BATCH_CPU_INSTANCES)
-    cs = CpuSample(gens)
+    threads = os.cpu_count() or 1  # one instance per host thread, every thread busy
+    cs = CpuSample(gens, threads)
+    threads = len(cs.nets)
     per_step = min(args.block, 100)
     vals, els = [], []
     for i in range(args.warmup + args.steps):
