@@ -762,8 +762,10 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
           }
         }
         // same-cell contributions of the chunk in lane order: the lowest lane
-        // of each group adds its peers' contributions one by one
-        const unsigned key = add ? (inwin ? (unsigned)cell : 0x40000000u | (unsigned)cell) : 0x80000000u | lane;
+        // of each group adds its peers' contributions one by one.  Lanes
+        // without a contribution share one key: the match instruction's cost
+        // grows with the number of distinct keys it sees.
+        const unsigned key = add ? (inwin ? (unsigned)cell : 0x40000000u | (unsigned)cell) : 0xffffffffu;
         const unsigned peers = __match_any_sync(FULL, key);
         const bool leader = add && (__ffs(peers) - 1) == lane;
         float acc = 0.0f;
