@@ -141,3 +141,31 @@ def test_batch_spike_readback_equals_per_network_reads(mode):
     assert b.synchronize() == 0
     assert same_as_alone(b.spikes(), N.SPK_POP_NEURONS) > 0
     b.close()
+
+
+def test_bulk_mode_key_lists_longer_than_one_staged_chunk():
+    """Instances whose timesteps have more active keys than the propagation
+    kernel stages at once (1,024): inputs at 2 kHz, so a fifth of the inputs
+    fire every timestep.  Bulk mode still gives each instance its result
+    alone, bit for bit."""
+    gens = [sweep_instance(n, 0.02, g, plastic, seed=900 + i, d_max=6, rate=2000.0)
+            for i, (n, g, plastic) in enumerate(((30000, 5.0, True), (26000, 6.0, False), (3000, 4.0, True)))]
+    sched = N.Schedule(8, 64, 0, 100)
+    batched = [Net.generate(g, sched) for g in gens]
+    alone = [Net.generate(g, sched) for g in gens]
+    b = Batch(batched, sched)
+    b.set_mode(N.SPK_BATCH_BULK)
+    b.run_steps(150, True)
+    for n in alone:
+        n.run_steps(150, True)
+    assert b.synchronize() == 0
+    for g, x, y in zip(gens, batched, alone):
+        assert y.synchronize() == 0
+        n, n_in, S = g.desc.n_neurons, g.desc.n_inputs, x.synapse_count()
+        sx, sy = snapshot(x, n, n_in, S), snapshot(y, n, n_in, S)
+        for k in sx:
+            np.testing.assert_array_equal(sx[k], sy[k], err_msg=f"instance n={n} field {k}")
+    # the big instances' inputs alone put about 1,200 keys on every timestep's list
+    assert gens[0].desc.n_inputs * 2000.0 * 1e-4 > 1024
+    assert sum(len(x.spikes()[0]) for x in batched) > 1000
+    b.close()
