@@ -427,61 +427,6 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
   }
 }
 
-// ---- timestep part 4: the post-spike afferent pass of every spiking post -----------------
-// Each warp takes spiking posts of the shared item list in turn and gives the
-// post's plastic afferents whose presynaptic key had no event this step (those
-// with an event were updated in the propagation kernel) their LTP update,
-// BULK_POST_CHUNK afferents per iteration.  Each weight is updated at most once
-// per step, so the order of the items does not matter.
-__global__ void __launch_bounds__(256) bulk_post_kernel(const NetDev* __restrict__ nets,
-                                                        const BulkPostItem* __restrict__ items,
-                                                        const int* __restrict__ item_count, int item_cap) {
-  const int lane = threadIdx.x & 31;
-  const int n_items = min(*item_count, item_cap);
-  const int n_warps = gridDim.x * (blockDim.x >> 5);
-  for (int it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < n_items; it += n_warps) {
-    const BulkPostItem item = items[it];
-    const NetDev& d = nets[item.net];
-    const int a0 = __ldg(d.csc_ptr + item.post), a1 = __ldg(d.csc_ptr + item.post + 1);
-    const float post_tr = d.post_trace[item.post];
-    const uint32_t* bA = d.bitsA;
-    const uint32_t* bP = d.bitsP;
-    const float* pub = d.pre_pub;
-    uint2* csc = d.csc;
-    const StdpConst sc = stdp_const(d);
-    unsigned long long n_post = 0;
-    for (int a = a0; a < a1; a += BULK_POST_CHUNK) {
-      constexpr int AFF = BULK_POST_CHUNK / 32;
-      uint2 cc[AFF];
-#pragma unroll
-      for (int u = 0; u < AFF; ++u) {
-        const int ai = a + u * 32 + lane;
-        cc[u] = csc[ai < a1 ? ai : a];
-      }
-      uint32_t vm[AFF];
-      float prt[AFF];
-#pragma unroll
-      for (int u = 0; u < AFF; ++u) {
-        const int pk = (int)cc[u].x;
-        vm[u] = bA[pk >> 5] | bP[pk >> 5];
-        prt[u] = pub[pk];
-      }
-#pragma unroll
-      for (int u = 0; u < AFF; ++u) {
-        const int ai = a + u * 32 + lane;
-        const int pk = (int)cc[u].x;
-        if (ai >= a1 || ((vm[u] >> (pk & 31)) & 1u)) continue;
-        const float nw = stdp_update(sc, __uint_as_float(cc[u].y), false, true, post_tr, prt[u]);
-        csc[ai].y = __float_as_uint(nw);
-        ++n_post;
-      }
-    }
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) n_post += __shfl_xor_sync(FULL, n_post, o);
-    if (lane == 0 && n_post) atomicAdd(&d.ctl->stdp_post, n_post);
-  }
-}
-
 // ---- timestep part 3: propagation and STDP ----------------------------------------------
 // One CTA per group of up to BULK_PROP_WARPS consecutive tiles of one network,
 // one warp per tile.  The CTA shares what every tile of the network reads
@@ -814,6 +759,61 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
   if (lane == 0) {
     if (ev) atomicAdd(&d.ctl->events, ev);
     if (n_pre) atomicAdd(&d.ctl->stdp_pre, n_pre);
+  }
+}
+
+// ---- timestep part 4: the post-spike afferent pass of every spiking post -----------------
+// Each warp takes spiking posts of the shared item list in turn and gives the
+// post's plastic afferents whose presynaptic key had no event this step (those
+// with an event were updated in the propagation kernel) their LTP update,
+// BULK_POST_CHUNK afferents per iteration.  Each weight is updated at most once
+// per step, so the order of the items does not matter.
+__global__ void __launch_bounds__(256) bulk_post_kernel(const NetDev* __restrict__ nets,
+                                                        const BulkPostItem* __restrict__ items,
+                                                        const int* __restrict__ item_count, int item_cap) {
+  const int lane = threadIdx.x & 31;
+  const int n_items = min(*item_count, item_cap);
+  const int n_warps = gridDim.x * (blockDim.x >> 5);
+  for (int it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < n_items; it += n_warps) {
+    const BulkPostItem item = items[it];
+    const NetDev& d = nets[item.net];
+    const int a0 = __ldg(d.csc_ptr + item.post), a1 = __ldg(d.csc_ptr + item.post + 1);
+    const float post_tr = d.post_trace[item.post];
+    const uint32_t* bA = d.bitsA;
+    const uint32_t* bP = d.bitsP;
+    const float* pub = d.pre_pub;
+    uint2* csc = d.csc;
+    const StdpConst sc = stdp_const(d);
+    unsigned long long n_post = 0;
+    for (int a = a0; a < a1; a += BULK_POST_CHUNK) {
+      constexpr int AFF = BULK_POST_CHUNK / 32;
+      uint2 cc[AFF];
+#pragma unroll
+      for (int u = 0; u < AFF; ++u) {
+        const int ai = a + u * 32 + lane;
+        cc[u] = csc[ai < a1 ? ai : a];
+      }
+      uint32_t vm[AFF];
+      float prt[AFF];
+#pragma unroll
+      for (int u = 0; u < AFF; ++u) {
+        const int pk = (int)cc[u].x;
+        vm[u] = bA[pk >> 5] | bP[pk >> 5];
+        prt[u] = pub[pk];
+      }
+#pragma unroll
+      for (int u = 0; u < AFF; ++u) {
+        const int ai = a + u * 32 + lane;
+        const int pk = (int)cc[u].x;
+        if (ai >= a1 || ((vm[u] >> (pk & 31)) & 1u)) continue;
+        const float nw = stdp_update(sc, __uint_as_float(cc[u].y), false, true, post_tr, prt[u]);
+        csc[ai].y = __float_as_uint(nw);
+        ++n_post;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) n_post += __shfl_xor_sync(FULL, n_post, o);
+    if (lane == 0 && n_post) atomicAdd(&d.ctl->stdp_post, n_post);
   }
 }
 

@@ -10,20 +10,22 @@
 //            Spike/Backend/CUDA/Neurons/LIFSpikingNeurons.cu:105-193 with
 //            Spike/Backend/CUDA/InlineDeviceFunctions.hpp:22-111) and inputs
 //            (Spike/Backend/CUDA/Neurons/PoissonInputSpikingNeurons.cu:96-129),
-//            advances the per-neuron STDP traces, and publishes one stamped
-//            ballot word per 32 keys into the network's spike bitmap (replaces
-//            the atomic activation list of InlineDeviceFunctions.hpp:4-18);
-//   phase B  each CTA polls the bitmap words until they carry this step's
-//            stamp (the only inter-CTA synchronization, bounded by a timeout),
-//            lists the step's active presynaptic keys in ascending order, and
-//            each warp stages the (key, tile) sub-rows of the row-partitioned
-//            CSR (8 B per synapse) into shared memory with cp.async and adds
-//            w*scale into its own ring cells (reference activate_synapses,
-//            Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:168-202), after
-//            updating plastic weights of rows with a pre event
-//            (WeightDependentSTDPPlasticity.cu:85-161); then it updates the
-//            plastic afferents of its own spiking posts whose presynaptic
-//            neuron had no event.
+//            advances the per-neuron STDP traces and ballots its spike words;
+//            warp 0 then publishes the CTA's active keys (inputs, then
+//            neurons, each ascending), every word stamped with its step, and
+//            one stamp word with their counts (replaces the atomic activation
+//            list of InlineDeviceFunctions.hpp:4-18);
+//   phase B  warp 0 polls the stamps of all the network's CTAs (the only
+//            inter-CTA synchronization, bounded by a wall-clock limit) and
+//            gathers the step's keys in ascending order into rounds of a
+//            shared list; each warp stages the round's (key, tile) sub-rows of
+//            the row-partitioned CSR (8 B per synapse) into shared memory with
+//            cp.async and adds w*scale into its own ring cells (reference
+//            activate_synapses, Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:
+//            168-202), after updating plastic weights of rows with a pre event
+//            (WeightDependentSTDPPlasticity.cu:85-161); last, the CTA's warps
+//            share the plastic afferents of its spiking posts whose
+//            presynaptic key had no event (the post-spike pass).
 //
 // Every ring cell has exactly one writer (the tile's warp) which applies the
 // contributions of a step in canonical order (ascending key, then synapse
