@@ -443,7 +443,10 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
 // delay slots 1..ws after the current one, each TS * L words, read from HBM
 // when the step's entries fill enough of it and written back once per dirty
 // slot; contributions outside the window go to HBM directly).
-constexpr int BULK_PROP_WARPS = 8;
+#ifndef SPK_BULK_PROP_WARPS
+#define SPK_BULK_PROP_WARPS 8
+#endif
+constexpr int BULK_PROP_WARPS = SPK_BULK_PROP_WARPS;
 constexpr int BULK_RPW = BULK_PROP_WARPS + 1;  // rowptr words per key: the tiles' starts and the last end
 constexpr int BULK_LIST_CHUNK = 1024;          // list keys staged at a time (a multiple of BULK_STAGE_KEYS)
 constexpr int BULK_WIN_CAP = 1024;             // ring-window words per warp at most
