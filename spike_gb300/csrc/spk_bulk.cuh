@@ -198,18 +198,24 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
   float* pub = d.pre_pub;
   if (bw.word * 32 >= KL) {
     const int N = d.N, L = d.L, B = d.B, TS = d.TS, kind = d.kind;
+    // a word lies in one tile (TS is a multiple of 32): its tile by a shift
+    // when TS is a power of two
+    const bool ts_pow2 = (TS & (TS - 1)) == 0;
+    const int ts_shift = __ffs(TS) - 1;
     float Vv[BULK_WPW], lv[BULK_WPW], inv[BULK_WPW], pov[BULK_WPW], prv[BULK_WPW];
+    float* cellp[BULK_WPW];
     // phase 1: every word's loads in flight at once
 #pragma unroll
     for (int u = 0; u < BULK_WPW; ++u) {
       Vv[u] = lv[u] = inv[u] = pov[u] = prv[u] = 0.0f;
       const int n = (bw.word + u) * 32 + lane - KL;
+      const int tile = ts_pow2 ? n >> ts_shift : n / TS, li = n - tile * TS;
+      cellp[u] = d.ring + ((size_t)tile * B + st.slot) * TS * L + (size_t)li * L;
       if (u < bw.count && n < N) {
         Vv[u] = d.V[n];
         lv[u] = d.last[n];
         if (kind == SPK_SYN_VOLTAGE) {
-          const int tile = n / TS, li = n - tile * TS;
-          const float* cell = d.ring + ((size_t)tile * B + st.slot) * TS * L + (size_t)li * L;
+          const float* cell = cellp[u];
           float total = 0.0f;
           for (int l = 0; l < L; ++l) total = total + cell[l];
           inv[u] = total;
@@ -228,8 +234,7 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
       const int n = key - KL;
       bool spk = false;
       if (n < N) {
-        const int tile = n / TS, li = n - tile * TS;
-        float* cell = d.ring + ((size_t)tile * B + st.slot) * TS * L + (size_t)li * L;
+        float* cell = cellp[u];
         spk = bulk_lif(d, st, n, key, Vv[u], lv[u], cell, inv[u]);
         if (kind == SPK_SYN_VOLTAGE)
           for (int l = 0; l < L; ++l) cell[l] = 0.0f;
