@@ -149,8 +149,18 @@ __global__ void __launch_bounds__(512, 1)
   __shared__ float s_decay[MAX_LABELS + 1], s_vhat[MAX_LABELS + 1], s_scale[MAX_CLASSES];
   __shared__ int s_round[4];  // keys in the round, last round, poll ok
   __shared__ int s_nsp;       // spiking posts listed for the CTA's afferent pass
+  __shared__ __align__(16) NetDev s_net;
   const CtaMap cm = map[blockIdx.x];
-  const NetDev& d = nets[cm.net];
+  // The network's descriptor in shared memory: the asm memory clobbers of the
+  // staging copies would otherwise reload its fields from global memory in
+  // every loop.
+  {
+    const uint32_t* src = (const uint32_t*)(nets + cm.net);
+    uint32_t* dst = (uint32_t*)&s_net;
+    for (int i = threadIdx.x; i < (int)(sizeof(NetDev) / 4); i += blockDim.x) dst[i] = __ldg(src + i);
+  }
+  __syncthreads();
+  const NetDev& d = s_net;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (threadIdx.x < MAX_LABELS + 1) {
     s_decay[threadIdx.x] = d.decay[threadIdx.x];
