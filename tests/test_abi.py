@@ -35,6 +35,13 @@ def test_abi_version_and_error_without_gpu_work():
     assert lib.spk_net_create(None, None, None) == _native.SPK_ERR_INVALID
     assert lib.spk_net_run(None, ctypes.c_float(1.0), 1) == _native.SPK_ERR_INVALID
     assert isinstance(lib.spk_last_error(), bytes)
+    # batch entry points: no handle, no counts, an unknown mode or population
+    counts = (ctypes.c_int64 * 4)()
+    assert lib.spk_batch_read_spikes(None, 0, None, None, 0, counts, 0) == _native.SPK_ERR_INVALID
+    assert lib.spk_batch_set_mode(None, _native.SPK_BATCH_BULK) == _native.SPK_ERR_INVALID
+    assert lib.spk_batch_run_steps_each(None, None, None) == _native.SPK_ERR_INVALID
+    assert lib.spk_batch_step_block(None) == _native.SPK_ERR_INVALID
+    assert lib.spk_batch_destroy(None) == _native.SPK_ERR_INVALID
 
 
 def test_noalloc_rejects_networks_beyond_its_scratch():
