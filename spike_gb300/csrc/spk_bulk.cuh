@@ -456,6 +456,7 @@ constexpr int BULK_RPW = BULK_PROP_WARPS + 1;  // rowptr words per key: the tile
 constexpr int BULK_LIST_CHUNK = 1024;          // list keys staged at a time (a multiple of BULK_STAGE_KEYS)
 constexpr int BULK_WIN_CAP = 1024;             // ring-window words per warp at most
 static_assert(BULK_LIST_CHUNK % BULK_STAGE_KEYS == 0, "rounds never straddle a list chunk");
+static_assert(BULK_STAGE_KEYS % 32 == 0, "a round is whole lanes' worth of keys");
 
 struct BulkPropBlock {
   int net;    // index into the batch's NetDev array
@@ -609,27 +610,36 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
     const int* rp = rp_s + buf * BULK_STAGE_KEYS * BULK_RPW;
     const uint32_t* kfl = kfl_s + buf * BULK_STAGE_KEYS;
     const float* kpre = kpre_s + buf * BULK_STAGE_KEYS;
-    for (int i = lane; i < nk; i += 32) {
-      const int len = rp[i * BULK_RPW + w + 1] - rp[i * BULK_RPW + w];
-      koff[i] = len;
-      if (kfl[i] >> 31) ev += (unsigned long long)len;
-    }
-    __syncwarp();
-    int carry = 0;
-    for (int c0 = 0; c0 < nk; c0 += 32) {
-      const int i = c0 + lane;
-      const int len = i < nk ? koff[i] : 0;
-      int incl = len;
+    // the tile's sub-row lengths and their exclusive prefix: each lane takes
+    // KPL consecutive keys, one warp scan for the round
+    constexpr int KPL = BULK_STAGE_KEYS / 32;
+    int lens[KPL];
+    int lsum = 0;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += y;
+    for (int u = 0; u < KPL; ++u) {
+      const int i = lane * KPL + u;
+      int len = 0;
+      if (i < nk) {
+        len = rp[i * BULK_RPW + w + 1] - rp[i * BULK_RPW + w];
+        if (kfl[i] >> 31) ev += (unsigned long long)len;
       }
-      __syncwarp();
-      if (i < nk) koff[i] = carry + incl - len;
-      carry += __shfl_sync(FULL, incl, 31);
+      lens[u] = len;
+      lsum += len;
     }
-    const int total_e = carry;
+    int incl = lsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += y;
+    }
+    int off = incl - lsum;
+#pragma unroll
+    for (int u = 0; u < KPL; ++u) {
+      const int i = lane * KPL + u;
+      if (i < nk) koff[i] = off;
+      off += lens[u];
+    }
+    const int total_e = __shfl_sync(FULL, incl, 31);
     if (lane == 0) koff[nk] = total_e;
     if (r == 0) {
       // A window pays when the step's entries (estimated from the first
