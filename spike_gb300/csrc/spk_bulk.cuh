@@ -443,7 +443,7 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
 // entries, then the plastic weights they name) instead of four.
 //
 // Shared memory: the CTA part (list chunk, two rounds of rowptr words, key
-// flags and pre traces, class scales) and per warp (entry stage, offsets, the
+// flags and pre traces, class scales) and per warp (entry stage, the
 // tile's post traces and spike words, and `win`, the tile's ring window: the
 // delay slots 1..ws after the current one, each TS * L words, read from HBM
 // when the step's entries fill enough of it and written back once per dirty
@@ -471,7 +471,7 @@ struct BulkPropLayout {
   // CTA part
   int list, rp, kfl, kpre, scl, cta;
   // per warp
-  int stage, stw, sidx, koff, ptr, spw, win, warp;
+  int stage, stw, sidx, ptr, spw, win, warp;
   int total;  // words
 };
 __host__ __device__ inline BulkPropLayout bulk_prop_layout(int win_words, int ts_max) {
@@ -488,7 +488,6 @@ __host__ __device__ inline BulkPropLayout bulk_prop_layout(int win_words, int ts
   l.stage = p; p += 2 * BULK_STAGE_ENTRIES;
   l.stw = p; p += BULK_STAGE_ENTRIES;
   l.sidx = p; p += BULK_STAGE_ENTRIES / 2;
-  l.koff = p; p += BULK_STAGE_KEYS + 4;
   l.ptr = p; p += ts_max;       // post traces of the tile (plastic runs)
   l.spw = p; p += ts_max / 32;  // spike words of the tile's posts (plastic runs)
   p = (p + 3) & ~3;
@@ -534,7 +533,6 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
   uint2* stage = (uint2*)(wreg + wl.stage);
   float* stage_w = (float*)(wreg + wl.stw);
   unsigned short* sidx = (unsigned short*)(wreg + wl.sidx);
-  int* koff = (int*)(wreg + wl.koff);
   float* ptr_s = (float*)(wreg + wl.ptr);
   uint32_t* spw_s = wreg + wl.spw;
   float* win_s = (float*)(wreg + wl.win);
@@ -613,14 +611,16 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
     // the tile's sub-row lengths and their exclusive prefix: each lane takes
     // KPL consecutive keys, one warp scan for the round
     constexpr int KPL = BULK_STAGE_KEYS / 32;
-    int lens[KPL];
+    int lens[KPL], kstart[KPL];  // the lane's keys: sub-row lengths and first entries
     int lsum = 0;
 #pragma unroll
     for (int u = 0; u < KPL; ++u) {
       const int i = lane * KPL + u;
       int len = 0;
+      kstart[u] = 0;
       if (i < nk) {
-        len = rp[i * BULK_RPW + w + 1] - rp[i * BULK_RPW + w];
+        kstart[u] = rp[i * BULK_RPW + w];
+        len = rp[i * BULK_RPW + w + 1] - kstart[u];
         if (kfl[i] >> 31) ev += (unsigned long long)len;
       }
       lens[u] = len;
@@ -632,15 +632,8 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
       const int y = __shfl_up_sync(FULL, incl, o);
       if (lane >= o) incl += y;
     }
-    int off = incl - lsum;
-#pragma unroll
-    for (int u = 0; u < KPL; ++u) {
-      const int i = lane * KPL + u;
-      if (i < nk) koff[i] = off;
-      off += lens[u];
-    }
+    const int lane_off = incl - lsum;  // first stage slot of the lane's keys
     const int total_e = __shfl_sync(FULL, incl, 31);
-    if (lane == 0) koff[nk] = total_e;
     if (r == 0) {
       // A window pays when the step's entries (estimated from the first
       // round) would touch more sectors one by one than the window holds;
@@ -659,13 +652,28 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
     __syncwarp();
     for (int f0 = 0; f0 < total_e; f0 += BULK_STAGE_ENTRIES) {
       const int nf = min(BULK_STAGE_ENTRIES, total_e - f0);
-      for (int i = lane; i < nk; i += 32) {
-        const int o = koff[i];
-        const int e0 = max(o, f0), e1 = min(koff[i + 1], f0 + nf);
-        const int base = rp[i * BULK_RPW + w] - o;
-        for (int f = e0; f < e1; ++f) {
-          sidx[f - f0] = (unsigned short)i;
-          cp_async8(stage + (f - f0), entries + base + f);
+      // each lane copies the part of its keys' sub-rows that falls in this
+      // stage [f0, f0 + nf), all from registers: one loop over the lane's
+      // consecutive slots, switching key at each sub-row end
+      if constexpr (KPL == 2) {
+        const int b1 = lane_off + lens[0];
+        const int e1 = min(lane_off + lsum, f0 + nf);
+        const int src0 = kstart[0] - lane_off, src1 = kstart[1] - b1;
+        for (int f = max(lane_off, f0); f < e1; ++f) {
+          const bool second = f >= b1;
+          sidx[f - f0] = (unsigned short)(lane * 2 + (second ? 1 : 0));
+          cp_async8(stage + (f - f0), entries + (second ? src1 : src0) + f);
+        }
+      } else {
+        int o = lane_off;
+#pragma unroll
+        for (int u = 0; u < KPL; ++u) {
+          const int e0 = max(o, f0), e1 = min(o + lens[u], f0 + nf);
+          for (int f = e0; f < e1; ++f) {
+            sidx[f - f0] = (unsigned short)(lane * KPL + u);
+            cp_async8(stage + (f - f0), entries + kstart[u] - o + f);
+          }
+          o += lens[u];
         }
       }
       cp_async_wait_all();
