@@ -533,41 +533,46 @@ __global__ void __launch_bounds__(512, 1)
           }
           cp_async_wait_all();
           __syncwarp();
-          for (int i = lane; i < nk; i += 32) {
-            const int len = koff[i] - kst[i];
-            koff[i] = len;
-            if (kfl[i] >> 31) ev += (unsigned long long)len;
-          }
-          __syncwarp();
-          // exclusive prefix of the sub-row lengths
-          int carry = 0;
-          for (int c0 = 0; c0 < nk; c0 += 32) {
-            const int i = c0 + lane;
-            const int len = i < nk ? koff[i] : 0;
-            int incl = len;
+          // the sub-row lengths and their exclusive prefix: each lane takes
+          // KPL consecutive keys, one warp scan for the round
+          constexpr int KPL = STAGE_KEYS / 32;
+          int lens[KPL], kstart[KPL];
+          int lsum = 0;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-              const int y = __shfl_up_sync(FULL, incl, o);
-              if (lane >= o) incl += y;
+          for (int u = 0; u < KPL; ++u) {
+            const int i = lane * KPL + u;
+            int len = 0;
+            kstart[u] = 0;
+            if (i < nk) {
+              kstart[u] = kst[i];
+              len = koff[i] - kstart[u];
+              if (kfl[i] >> 31) ev += (unsigned long long)len;
             }
-            __syncwarp();
-            if (i < nk) koff[i] = carry + incl - len;
-            carry += __shfl_sync(FULL, incl, 31);
+            lens[u] = len;
+            lsum += len;
           }
-          const int total_e = carry;
+          int incl = lsum;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const int lane_off = incl - lsum;  // first stage slot of the lane's keys
+          const int total_e = __shfl_sync(FULL, incl, 31);
           __syncwarp();
           for (int f0 = 0; f0 < total_e; f0 += STAGE_ENTRIES) {
             const int nf = min(STAGE_ENTRIES, total_e - f0);
-            // each lane copies the part of its own sub-rows that falls in this
-            // round's window [f0, f0 + nf) (no search per entry)
-            for (int i = lane; i < nk; i += 32) {
-              const int o = koff[i];
-              const int e0 = max(o, f0), e1 = min(o + (i + 1 < nk ? koff[i + 1] - o : total_e - o), f0 + nf);
-              const int base = kst[i] - o;
+            // each lane copies the part of its keys' sub-rows that falls in
+            // this stage [f0, f0 + nf), from registers (no search per entry)
+            int o = lane_off;
+#pragma unroll
+            for (int u = 0; u < KPL; ++u) {
+              const int e0 = max(o, f0), e1 = min(o + lens[u], f0 + nf);
               for (int f = e0; f < e1; ++f) {
-                sidx[f - f0] = (unsigned short)i;
-                cp_async8(stage + (f - f0), d.entries + base + f);
+                sidx[f - f0] = (unsigned short)(lane * KPL + u);
+                cp_async8(stage + (f - f0), d.entries + kstart[u] - o + f);
               }
+              o += lens[u];
             }
             cp_async_wait_all();
             __syncwarp();
