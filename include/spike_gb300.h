@@ -199,6 +199,13 @@ int spk_net_spike_count(spk_net* net, int32_t population, int64_t* n);
 int spk_net_read_spikes(spk_net* net, int32_t population, int32_t* ids, float* times,
                         int64_t capacity, int64_t* n_written);
 int spk_net_clear_spikes(spk_net* net);
+/* Rate monitor (RateActivityMonitor, Spike/ActivityMonitor/RateActivityMonitor.cpp
+ * and Spike/Backend/CUDA/ActivityMonitor/RateActivityMonitor.cu:50-71): the
+ * spikes of every neuron (or input) of `population` since the last clear or
+ * reset, counted on the device as the spikes are decided.  count must be the
+ * population's size; counts[i] is neuron (input) i's. */
+int spk_net_rate_counts(spk_net* net, int32_t population, int32_t* counts, int64_t count);
+int spk_net_clear_rate_counts(spk_net* net);
 /* Read one state field (SPK_FIELD_*) into dst (count elements). */
 int spk_net_read_state(spk_net* net, int32_t field, void* dst, int64_t count);
 /* Backend::Synapses::copy_to_frontend / copy_to_backend

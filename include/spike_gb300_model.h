@@ -107,6 +107,10 @@ int spk_model_counts(spk_model* m, int32_t* n_neurons, int32_t* n_inputs, int64_
 int spk_model_spikes(spk_model* m, int32_t population, const int32_t** ids, const float** times,
                      int64_t* n);
 int spk_model_clear_spikes(spk_model* m);
+/* A RateActivityMonitor on the model's neurons (population SPK_POP_NEURONS) or
+ * inputs; its counts after run(): borrowed, valid until the next run/reset. */
+int spk_model_add_rate_monitor(spk_model* m, int32_t population);
+int spk_model_rate_counts(spk_model* m, int32_t population, const int32_t** counts, int64_t* n);
 
 #ifdef __cplusplus
 }

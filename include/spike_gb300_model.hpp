@@ -267,6 +267,19 @@ class SpikingActivityMonitor {
   void save_spikes_as_binary(std::string path, std::string prefix = "");
 };
 
+// RateActivityMonitor (Spike/ActivityMonitor/RateActivityMonitor.hpp): spikes per
+// neuron of its population, counted on the device as the spikes are decided,
+// copied to per_neuron_spike_counts after run() (final_update) and zeroed by
+// reset_state (host and device).
+class RateActivityMonitor {
+ public:
+  explicit RateActivityMonitor(SpikingNeurons* neurons_parameter) : neurons(neurons_parameter) {}
+  SpikingNeurons* neurons;
+  SpikingModel* model = nullptr;
+  std::vector<int> per_neuron_spike_counts;
+  void reset_state();
+};
+
 // ---- model ---------------------------------------------------------------------
 class SpikingModel {
  public:
@@ -277,6 +290,7 @@ class SpikingModel {
   SpikingNeurons* input_spiking_neurons = nullptr;
   std::vector<Plasticity*> plasticity_rule_vec;
   std::vector<SpikingActivityMonitor*> monitors_vec;
+  std::vector<RateActivityMonitor*> rate_monitors_vec;
   bool model_complete = false;
   float timestep = 0.0001f;
   int timestep_grouping = 1;
@@ -293,6 +307,7 @@ class SpikingModel {
                                                        synapse_parameters_struct* synapse_params);
   void AddPlasticityRule(Plasticity* plasticity_rule);
   void AddActivityMonitor(SpikingActivityMonitor* activityMonitor);
+  void AddActivityMonitor(RateActivityMonitor* activityMonitor);
   void finalise_model();
   void reset_state();
   void reset_time();
@@ -303,6 +318,7 @@ class SpikingModel {
   spk_net* net() const { return net_; }
   int last_status() const { return status_; }
   void collect_spikes();
+  void collect_rates();
 
  private:
   spk_net* net_ = nullptr;

@@ -179,6 +179,8 @@ _SIGS = {
     "spk_net_spike_count": (i32, [_VP, i32, P(i64)]),
     "spk_net_read_spikes": (i32, [_VP, i32, P(i32), P(f32), i64, P(i64)]),
     "spk_net_clear_spikes": (i32, [_VP]),
+    "spk_net_rate_counts": (i32, [_VP, i32, P(i32), i64]),
+    "spk_net_clear_rate_counts": (i32, [_VP]),
     "spk_net_read_state": (i32, [_VP, i32, _VP, i64]),
     "spk_net_read_weights": (i32, [_VP, P(f32), i64]),
     "spk_net_write_weights": (i32, [_VP, P(f32), i64]),
@@ -242,6 +244,8 @@ _SIGS = {
     "spk_model_counts": (i32, [_VP, P(i32), P(i32), P(i64)]),
     "spk_model_spikes": (i32, [_VP, i32, P(P(i32)), P(P(f32)), P(i64)]),
     "spk_model_clear_spikes": (i32, [_VP]),
+    "spk_model_add_rate_monitor": (i32, [_VP, i32]),
+    "spk_model_rate_counts": (i32, [_VP, i32, P(P(i32)), P(i64)]),
 }
 
 _lib = None

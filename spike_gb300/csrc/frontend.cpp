@@ -4,6 +4,7 @@
 // Built with -ffp-contract=off: the weight and delay draws below are float
 // expressions of rand() and must round exactly as the reference's x86 build
 // does (Spike/Synapses/Synapses.cpp:323, Spike/Synapses/SpikingSynapses.cpp:104).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -506,6 +507,13 @@ void SpikingActivityMonitor::save_spikes_as_binary(std::string path, std::string
            sizeof(float) * total_number_of_spikes_stored_on_host);
 }
 
+// RateActivityMonitor::reset_state (Spike/ActivityMonitor/RateActivityMonitor.cpp:17-22
+// with Spike/Backend/CUDA/ActivityMonitor/RateActivityMonitor.cu:12-16).
+void RateActivityMonitor::reset_state() {
+  std::fill(per_neuron_spike_counts.begin(), per_neuron_spike_counts.end(), 0);
+  if (model && model->net()) spk_net_clear_rate_counts(model->net());
+}
+
 // ---- model --------------------------------------------------------------------------
 SpikingModel::SpikingModel() {}
 SpikingModel::~SpikingModel() {
@@ -537,6 +545,10 @@ void SpikingModel::AddPlasticityRule(Plasticity* r) { plasticity_rule_vec.push_b
 void SpikingModel::AddActivityMonitor(SpikingActivityMonitor* m) {
   m->model = this;
   monitors_vec.push_back(m);
+}
+void SpikingModel::AddActivityMonitor(RateActivityMonitor* m) {
+  m->model = this;
+  rate_monitors_vec.push_back(m);
 }
 
 int SpikingModel::build_desc(spk_net_desc* d) {
@@ -645,6 +657,7 @@ void SpikingModel::finalise_model() {
   if (spiking_neurons) spiking_neurons->model = this;
   if (input_spiking_neurons) input_spiking_neurons->model = this;
   for (auto* m : monitors_vec) m->model = this;
+  for (auto* m : rate_monitors_vec) m->model = this;
   spk_net_desc d;
   int rc = build_desc(&d);
   if (rc) fail(rc, "model cannot be flattened into a network descriptor");
@@ -660,8 +673,9 @@ void SpikingModel::finalise_model() {
 
 void SpikingModel::reset_state() {
   finalise_model();
-  int rc = spk_net_reset_state(net_);
+  int rc = spk_net_reset_state(net_);  // zeroes the device rate counts too
   if (rc) fail(rc, spk_last_error());
+  for (auto* m : rate_monitors_vec) std::fill(m->per_neuron_spike_counts.begin(), m->per_neuron_spike_counts.end(), 0);
 }
 void SpikingModel::reset_time() {
   if (net_) spk_net_reset_time(net_);
@@ -686,6 +700,18 @@ void SpikingModel::collect_spikes() {
   spk_net_clear_spikes(net_);
 }
 
+// RateActivityMonitor::final_update (Spike/ActivityMonitor/RateActivityMonitor.cpp:28-30):
+// the device counts since the last reset, copied to each rate monitor.
+void SpikingModel::collect_rates() {
+  for (auto* m : rate_monitors_vec) {
+    const bool inputs = m->neurons == input_spiking_neurons && input_spiking_neurons;
+    const int n = inputs ? input_spiking_neurons->total_number_of_neurons : spiking_neurons->total_number_of_neurons;
+    m->per_neuron_spike_counts.assign(n, 0);
+    int rc = spk_net_rate_counts(net_, inputs ? SPK_POP_INPUTS : SPK_POP_NEURONS, m->per_neuron_spike_counts.data(), n);
+    if (rc) fail(rc, spk_last_error());
+  }
+}
+
 // SpikingModel::run (Spike/Models/SpikingModel.cpp:214-236); the monitors'
 // device store is drained after the run (final_update).
 void SpikingModel::run(float seconds, bool plasticity_on) {
@@ -694,6 +720,7 @@ void SpikingModel::run(float seconds, bool plasticity_on) {
   if (status_ == SPK_OK) status_ = spk_net_synchronize(net_);
   if (status_ != SPK_OK && status_ != SPK_ERR_OVERFLOW) fail(status_, spk_last_error());
   collect_spikes();
+  collect_rates();
 }
 
 // ---- C surface -------------------------------------------------------------------------
@@ -706,11 +733,14 @@ struct spk_model {
   std::vector<weightdependent_stdp_plasticity_parameters_struct*> rule_params;
   SpikingActivityMonitor* neuron_monitor = nullptr;
   SpikingActivityMonitor* input_monitor = nullptr;
+  RateActivityMonitor* rate_monitor[2] = {nullptr, nullptr};  // neurons, inputs
   ~spk_model() {
     for (auto* r : rules) delete r;
     for (auto* p : rule_params) delete p;
     delete neuron_monitor;
     delete input_monitor;
+    delete rate_monitor[0];
+    delete rate_monitor[1];
     delete synapses;
     delete inputs;
   }
@@ -1050,6 +1080,26 @@ int spk_model_clear_spikes(spk_model* m) {
   if (!m) return SPK_ERR_INVALID;
   if (m->neuron_monitor) m->neuron_monitor->reset_state();
   if (m->input_monitor) m->input_monitor->reset_state();
+  return SPK_OK;
+}
+
+int spk_model_add_rate_monitor(spk_model* m, int32_t pop) {
+  if (!m || pop < 0 || pop > 1) return SPK_ERR_INVALID;
+  if (pop == SPK_POP_INPUTS && !m->inputs) return SPK_ERR_INVALID;
+  if (m->rate_monitor[pop]) return SPK_OK;
+  return guarded([&] {
+    m->rate_monitor[pop] =
+        new RateActivityMonitor(pop == SPK_POP_NEURONS ? (SpikingNeurons*)&m->neurons : (SpikingNeurons*)m->inputs);
+    m->model.AddActivityMonitor(m->rate_monitor[pop]);
+    return SPK_OK;
+  });
+}
+
+int spk_model_rate_counts(spk_model* m, int32_t pop, const int32_t** counts, int64_t* n) {
+  if (!m || pop < 0 || pop > 1) return SPK_ERR_INVALID;
+  RateActivityMonitor* mon = m->rate_monitor[pop];
+  if (counts) *counts = mon ? mon->per_neuron_spike_counts.data() : nullptr;
+  if (n) *n = mon ? (int64_t)mon->per_neuron_spike_counts.size() : 0;
   return SPK_OK;
 }
 

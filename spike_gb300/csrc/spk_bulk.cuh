@@ -163,6 +163,7 @@ __device__ __forceinline__ bool bulk_lif(const NetDev& d, const BulkStep& st, in
       spk = true;
       d.last[n] = st.tg;
       Vi = G.vreset;
+      if (d.rate_counts) d.rate_counts[key] += 1;
     }
   }
   d.V[n] = Vi;
@@ -279,7 +280,10 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
         if ((nx <= st.tg) || !st.inputs_active) {
           const float u01 = draw_uniform(d.seed, (uint32_t)idx, (uint32_t)st.T, DOMAIN_POISSON);
           nx = st.tg - (1.0f / rtv[u]) * logf_spk(u01);
-          if (st.inputs_active) spk = true;
+          if (st.inputs_active) {
+            spk = true;
+            if (d.rate_counts) d.rate_counts[key] += 1;
+          }
         }
         d.in_next[idx] = nx;
         if (st.stdp_run) {

@@ -99,6 +99,8 @@ struct NetDev {
   // bulk-synchronous batches only: the step's active keys in canonical order
   uint32_t* step_list;        // [n_keys] key | spike << 31 | pre-event << 30
   int* step_count;            // keys in step_list
+  // rate monitor: spikes of each key since the last clear, or null
+  int* rate_counts;           // [n_keys]
 };
 
 struct CtaMap {

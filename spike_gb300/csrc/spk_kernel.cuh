@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(512, 1)
   const int N = d.N, Nin = d.Nin, KL = d.KL, L = d.L, B = d.B, kind = d.kind;
   const int TS = d.TS, ITS = d.ITS, n_tiles = d.n_tiles, n_keys = d.n_keys, n_words = d.n_words;
   const float dt = d.dt;
+  int* const rate_counts = d.rate_counts;  // rate monitor (one owner per key and step)
 
   uint32_t* list = sm;
   int* segoff = (int*)(sm + LIST_CAP);  // [2 * nctas + 1] offsets of the gather segments
@@ -331,6 +332,7 @@ __global__ void __launch_bounds__(512, 1)
               spk = true;
               last_s[li] = tg;
               Vi = G.vreset;
+              if (rate_counts) rate_counts[KL + n] += 1;
             }
           }
           V_s[li] = Vi;
@@ -360,7 +362,10 @@ __global__ void __launch_bounds__(512, 1)
           const float rate = inrate_s[li];
           const float u = draw_uniform(d.seed, (uint32_t)idx, (uint32_t)T, DOMAIN_POISSON);
           nx = tg - (1.0f / rate) * logf_spk(u);
-          if (inputs_active) spk = true;
+          if (inputs_active) {
+            spk = true;
+            if (rate_counts) rate_counts[k] += 1;
+          }
         }
         innext_s[li] = nx;
         if (stdp_run) {

@@ -288,6 +288,8 @@ static int upload_state_defaults(spk_net* n) {
   SPK_CUDA(cudaMemcpyAsync(h.last, last.data(), sizeof(float) * n->N, cudaMemcpyHostToDevice, n->stream));
   SPK_CUDA(cudaMemsetAsync(h.gtr, 0, sizeof(float) * (size_t)n->N * n->L, n->stream));
   SPK_CUDA(cudaMemsetAsync(h.ring, 0, sizeof(float) * (size_t)h.n_tiles * h.B * h.TS * h.L, n->stream));
+  // RateActivityMonitor::reset_state (Spike/Backend/CUDA/ActivityMonitor/RateActivityMonitor.cu:12-16)
+  if (h.rate_counts) SPK_CUDA(cudaMemsetAsync(h.rate_counts, 0, sizeof(int) * (size_t)h.n_keys, n->stream));
   if (n->has_stdp) {
     SPK_CUDA(cudaMemsetAsync(h.post_trace, 0, sizeof(float) * n->N, n->stream));
     SPK_CUDA(cudaMemsetAsync(h.pre_trace, 0, sizeof(float) * h.n_keys, n->stream));
@@ -496,7 +498,8 @@ static int new_net(const ModelSpec& m, int B, int64_t S, const spk_schedule* sch
 // Bytes of each part of a network's device arena, in arena order: rowptr,
 // entries, csc_ptr, csc, V, last, traces, ring, input next, rates, post
 // traces, pre traces, pre-trace mailbox, spike and pre-event bitmaps, CTA key
-// lists and stamps, spike store, run control, abort flag, descriptor, CTA map.
+// lists and stamps, spike store, run control, abort flag, descriptor, CTA map,
+// rate-monitor counts.
 static std::vector<size_t> arena_part_sizes(const Plan& plan, int N, int Nin, int L, int B, int stdp, int64_t S,
                                             int64_t n_csc, int n_stim, int64_t spike_cap) {
   const size_t n_cells = (size_t)plan.n_keys * plan.n_tiles;
@@ -522,7 +525,8 @@ static std::vector<size_t> arena_part_sizes(const Plan& plan, int N, int Nin, in
           sizeof(RunCtl),
           sizeof(int),
           sizeof(NetDev),
-          sizeof(CtaMap) * plan.nctas};
+          sizeof(CtaMap) * plan.nctas,
+          sizeof(int) * (size_t)plan.n_keys};
 }
 
 static size_t arena_total(const std::vector<size_t>& sizes) {
@@ -566,10 +570,11 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   void* p_ckeys = nullptr; void* p_cstamp = nullptr;
   const int key_cap = plan.W * (plan.TS + plan.ITS);
   void* p_ctl = nullptr; void* p_abort = nullptr; void* p_dd = nullptr; void* p_map = nullptr;
+  void* p_rate = nullptr;
   const std::vector<size_t> sizes = arena_part_sizes(plan, N, Nin, L, B, stdp, S, n_csc, n->n_stim, spike_cap);
   void** dsts[] = {&p_rowptr, &p_entries, &p_cscptr, &p_csc,   &p_V,     &p_last,   &p_gtr,  &p_ring,
                    &p_innext, &p_rates,   &p_post,   &p_pre,   &p_pub,   &p_bA,     &p_bP,   &p_ckeys,
-                   &p_cstamp, &p_spk,     &p_ctl,    &p_abort, &p_dd,    &p_map};
+                   &p_cstamp, &p_spk,     &p_ctl,    &p_abort, &p_dd,    &p_map,  &p_rate};
   std::vector<Part> parts;
   for (size_t i = 0; i < sizes.size(); ++i) parts.push_back(Part{dsts[i], sizes[i]});
   const size_t total = arena_total(sizes);
@@ -655,6 +660,7 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
     h.clip_upper = sp.clip_upper ? 1 : 0;
   }
   h.seed = m.seed;
+  h.rate_counts = (int*)p_rate;
   h.rowptr = (const int*)p_rowptr;
   h.entries = (uint2*)p_entries;
   h.csc_ptr = (const int*)p_cscptr;
@@ -1565,6 +1571,34 @@ int spk_net_clear_spikes(spk_net* n) {
   if (!n) return SPK_ERR_INVALID;
   clear_store_kernel<<<1, 1, 0, n->stream>>>(n->hd.ctl);
   SPK_CUDA(cudaGetLastError());
+  return SPK_OK;
+}
+
+int spk_net_rate_counts(spk_net* n, int32_t population, int32_t* counts, int64_t count) {
+  if (!n || !counts || population < 0 || population > 1) return SPK_ERR_INVALID;
+  const int64_t want = population == SPK_POP_NEURONS ? n->N : n->Nin;
+  if (count != want) {
+    set_error("rate_counts: %lld counts asked, the population has %lld", (long long)count, (long long)want);
+    return SPK_ERR_INVALID;
+  }
+  return guarded([&] {
+    if (count == 0) return SPK_OK;
+    SPK_CUDA(cudaStreamSynchronize(n->stream));
+    if (population == SPK_POP_NEURONS) {
+      SPK_CUDA(cudaMemcpy(counts, n->hd.rate_counts + n->hd.KL, sizeof(int32_t) * count, cudaMemcpyDeviceToHost));
+    } else {
+      // input i has key Nin - 1 - i
+      std::vector<int32_t> by_key(count);
+      SPK_CUDA(cudaMemcpy(by_key.data(), n->hd.rate_counts, sizeof(int32_t) * count, cudaMemcpyDeviceToHost));
+      for (int64_t i = 0; i < count; ++i) counts[i] = by_key[count - 1 - i];
+    }
+    return SPK_OK;
+  });
+}
+
+int spk_net_clear_rate_counts(spk_net* n) {
+  if (!n) return SPK_ERR_INVALID;
+  SPK_CUDA(cudaMemsetAsync(n->hd.rate_counts, 0, sizeof(int) * (size_t)n->hd.n_keys, n->stream));
   return SPK_OK;
 }
 

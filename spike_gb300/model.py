@@ -202,6 +202,17 @@ class Net:
     def clear_spikes(self):
         check(lib().spk_net_clear_spikes(self.h), "spk_net_clear_spikes")
 
+    def rate_counts(self, n: int, population: int = N.SPK_POP_NEURONS) -> np.ndarray:
+        """Spikes per neuron (or input) since the last clear or reset (the
+        rate monitor); n is the population's size."""
+        out = np.zeros(n, np.int32)
+        check(lib().spk_net_rate_counts(self.h, population, out.ctypes.data_as(C.POINTER(C.c_int32)), n),
+              "spk_net_rate_counts")
+        return out
+
+    def clear_rate_counts(self):
+        check(lib().spk_net_clear_rate_counts(self.h), "spk_net_clear_rate_counts")
+
     def state(self, field: int, count: int) -> np.ndarray:
         out = np.empty(count, dtype=np.float32)
         check(lib().spk_net_read_state(self.h, field, out.ctypes.data_as(C.c_void_p), count), "spk_net_read_state")
@@ -569,6 +580,19 @@ class Model:
 
     def clear_spikes(self):
         check(lib().spk_model_clear_spikes(self.h), "spk_model_clear_spikes")
+
+    def add_rate_monitor(self, population: int = N.SPK_POP_NEURONS):
+        """A RateActivityMonitor on the neurons or the inputs (before run)."""
+        check(lib().spk_model_add_rate_monitor(self.h, population), "spk_model_add_rate_monitor")
+
+    def rate_counts(self, population: int = N.SPK_POP_NEURONS) -> np.ndarray:
+        """The rate monitor's spikes per neuron (input) after the last run."""
+        p = C.POINTER(C.c_int32)()
+        n = C.c_int64()
+        check(lib().spk_model_rate_counts(self.h, population, C.byref(p), C.byref(n)), "spk_model_rate_counts")
+        if n.value == 0:
+            return np.zeros(0, np.int32)
+        return np.ctypeslib.as_array(p, (n.value,)).copy()
 
 
 def desc_arrays(d: N.NetDesc) -> dict:
