@@ -87,8 +87,25 @@ typedef struct spk_neuron_group {
   float v_init_hi;
 } spk_neuron_group;
 
+/* STDP rules (spk_net_desc.stdp_rule).  The weight-dependent rule is
+ * event-driven; the Evans and inhibitory rules keep two traces per plastic
+ * synapse and update every plastic synapse every timestep, seeing a
+ * presynaptic spike when it arrives (its delay after it was fired), as the
+ * reference's bit-buffer kernels do.  They run in bulk mode only. */
+#define SPK_STDP_WEIGHT_DEPENDENT 0 /* WeightDependentSTDPPlasticity */
+#define SPK_STDP_EVANS 1            /* EvansSTDPPlasticity (Spike/Plasticity/EvansSTDPPlasticity.hpp) */
+#define SPK_STDP_INHIBITORY 2       /* InhibitorySTDPPlasticity (Vogels et al. 2011,
+                                       Spike/Plasticity/InhibitorySTDPPlasticity.hpp) */
+
 /* weightdependent_stdp_plasticity_parameters_struct
- * (Spike/Plasticity/WeightDependentSTDPPlasticity.hpp:28-40). */
+ * (Spike/Plasticity/WeightDependentSTDPPlasticity.hpp:28-40).  The other
+ * rules reuse the fields:
+ *   SPK_STDP_EVANS       tau_minus = decay_term_tau_D, tau_plus = decay_term_tau_C,
+ *                        a_minus = model_parameter_alpha_D,
+ *                        a_plus = synaptic_neurotransmitter_concentration_alpha_C
+ *                        (weights clipped to [0, 1]);
+ *   SPK_STDP_INHIBITORY  tau_plus = tau_istdp, lambda = learningrate,
+ *                        alpha = targetrate (weights clipped at 0). */
 typedef struct spk_stdp_params {
   float a_minus;
   float a_plus;
@@ -141,7 +158,7 @@ typedef struct spk_net_desc {
   uint64_t seed;              /* Philox key (Poisson draws, V init) */
   int64_t spike_capacity;     /* device spike store entries; 0 = default */
   int32_t record_inputs;      /* also record input spikes */
-  int32_t reserved;
+  int32_t stdp_rule;          /* SPK_STDP_*; 0 = weight-dependent */
 } spk_net_desc;
 
 /* Launch schedule.  Zero fields are chosen by the library (planner for a

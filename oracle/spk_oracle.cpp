@@ -64,8 +64,15 @@ struct Net {
   std::vector<int64_t> eff_start, eff_count;  // per key
   std::vector<int64_t> plastic_idx;       // sorted indices under the STDP rule
   bool has_stdp = false;
+  int stdp_rule = SPK_STDP_WEIGHT_DEPENDENT;
   spk_stdp_params stdp{};
   R E_minus = 0, E_plus = 0, inc_minus = 0, inc_plus = 0, invE_minus = 0, invE_plus = 0;
+  R vogels_decay = 0;  // expf(-timestep / tau_istdp), computed on the host
+  // Spike bits of the last H timesteps per key, for rules that see a
+  // presynaptic spike when it arrives (the reference's spike bit-buffers,
+  // Spike/Backend/CUDA/Neurons/SpikingNeurons.cu:33-35).
+  int H = 1;
+  std::vector<uint8_t> hist;  // [H][keys]
 
   // ---- dynamic state --------------------------------------------------------
   std::vector<R> V, last, gtr, ring;  // ring [B][N*L]
@@ -99,6 +106,7 @@ struct Net {
   void lif_range(int a, int b, R t, int T);
   void poisson_range(int a, int b, R t, int T);
   void stdp_range(int64_t a, int64_t b, R t);
+  void dense_stdp_range(int64_t a, int64_t b, int T);
   void propagate_thread(int th, int T);
 };
 
@@ -222,6 +230,16 @@ int Net<R>::init(const spk_net_desc* d) {
 
   has_stdp = d->has_stdp != 0;
   stdp = d->stdp;
+  stdp_rule = d->stdp_rule;
+  if (stdp_rule < SPK_STDP_WEIGHT_DEPENDENT || stdp_rule > SPK_STDP_INHIBITORY) return SPK_ERR_INVALID;
+  if (has_stdp && stdp_rule == SPK_STDP_INHIBITORY) {
+    // expf(- timestep / tau_istdp) (Spike/Backend/CUDA/Plasticity/InhibitorySTDPPlasticity.cu:61)
+    if (sizeof(R) == 4)
+      vogels_decay = (R)expf(-d->dt / stdp.tau_plus);
+    else
+      vogels_decay = (R)std::exp(-(double)d->dt / (double)stdp.tau_plus);
+  }
+  H = Dmax + 1;
   plastic_idx.clear();
   if (has_stdp)
     for (int64_t s = 0; s < S; ++s)
@@ -261,6 +279,7 @@ int Net<R>::init(const spk_net_desc* d) {
   stdp_pre.assign(plastic_idx.size(), 0);
   stdp_post.assign(plastic_idx.size(), 0);
   spiked.assign(K, 0);
+  hist.assign((size_t)H * K, 0);
   set_threads(1);
   reset_state();
   return SPK_OK;
@@ -302,6 +321,7 @@ void Net<R>::reset_state() {
   reset_inputs();
   std::fill(stdp_pre.begin(), stdp_pre.end(), (R)0);
   std::fill(stdp_post.begin(), stdp_post.end(), (R)0);
+  std::fill(hist.begin(), hist.end(), (uint8_t)0);
 }
 
 template <typename R>
@@ -502,6 +522,66 @@ void Net<R>::stdp_range(int64_t a, int64_t b, R t) {
   }
 }
 
+// Rules with two traces per plastic synapse, updated every timestep; a
+// presynaptic spike is seen when it arrives, delay steps after it was fired
+// (bit T - delay of the presynaptic bit-buffer), a postsynaptic one at T.
+//   Evans: ltp_and_ltd (Spike/Backend/CUDA/Plasticity/EvansSTDPPlasticity.cu:59-141),
+//     traces C (presynaptic activity) and D (postsynaptic), weights in [0, 1];
+//   inhibitory: vogels_apply_stdp_to_synapse_weights_kernel
+//     (Spike/Backend/CUDA/Plasticity/InhibitorySTDPPlasticity.cu:71-154),
+//     weights clipped at 0; its constant term is evaluated in double, as the
+//     reference's 2.0 literal makes it.
+template <typename R>
+void Net<R>::dense_stdp_range(int64_t a, int64_t b, int T) {
+  const int K = nkeys();
+  const R dtR = dt;
+  for (int64_t indx = a; indx < b; ++indx) {
+    const int64_t idx = plastic_idx[indx];
+    const int postid = spost[idx];
+    const int preid = spre[idx];
+    const int prekey = Nin + preid;  // input -i-1 -> key Nin-1-i, neuron n -> Nin+n
+    int slot = (T - sdelay[idx]) % H;
+    if (slot < 0) slot += H;
+    const bool pre_sp = hist[(size_t)slot * K + prekey] != 0;
+    const bool post_sp = spiked[Nin + postid] != 0;
+    R tr_pre = stdp_pre[indx];
+    R tr_post = stdp_post[indx];
+    R w = sw[idx];
+    if (stdp_rule == SPK_STDP_EVANS) {
+      const R tau_C = (R)stdp.tau_plus, tau_D = (R)stdp.tau_minus;
+      const R alpha_C = (R)stdp.a_plus, alpha_D = (R)stdp.a_minus;
+      tr_pre = ((R)1 - (dtR / tau_C)) * tr_pre;
+      tr_post = ((R)1 - (dtR / tau_D)) * tr_post;
+      if (pre_sp) tr_pre += dtR * alpha_C * ((R)1 - tr_pre);
+      if (post_sp) tr_post += dtR * alpha_D * ((R)1 - tr_post);
+      R syn = 0;
+      const R old_w = w;
+      if (pre_sp) syn -= (old_w * tr_post);
+      if (post_sp) syn += (((R)1 - old_w) * tr_pre);
+      w = old_w + syn;
+      if (w < (R)0) w = (R)0;
+      if (w > (R)1) w = (R)1;
+    } else {
+      const R lr = (R)stdp.lambda;
+      tr_pre *= vogels_decay;
+      tr_post *= vogels_decay;
+      if (pre_sp) tr_pre += (R)1;
+      if (post_sp) tr_post += (R)1;
+      R syn = 0;
+      if (pre_sp) {
+        syn += lr * (tr_post);
+        syn += -lr * (2.0 * (double)stdp.alpha * (double)stdp.tau_plus);
+      }
+      if (post_sp) syn += lr * (tr_pre);
+      w += syn;
+      if (w < (R)0) w = (R)0;
+    }
+    sw[idx] = w;
+    stdp_pre[indx] = tr_pre;
+    stdp_post[indx] = tr_post;
+  }
+}
+
 // activate_synapses (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:168-202):
 // slot (bufferloc + delay + g) % B with bufferloc = round(t/dt) % B (:127),
 // contributions w*scale applied in ascending key order, then row order.
@@ -529,11 +609,13 @@ void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
     T = round_to_int(tf / dt_f);
     t = (sizeof(R) == 4) ? (R)tf : (R)start + (R)(s * 1) * dt;
   };
-  auto finish_step = [&](R t) {
+  auto finish_step = [&](R t, int T) {
     active.clear();
     const int K = nkeys();
     for (int kk = 0; kk < K; ++kk)
       if (spiked[kk]) active.push_back(kk);
+    // this step's spike bits, for the rules that look delays back
+    std::copy(spiked.begin(), spiked.end(), hist.begin() + (size_t)(T % H) * K);
     for (int64_t kk : active) events += (uint64_t)eff_count[kk];
     return t;
   };
@@ -550,7 +632,8 @@ void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
       }
     }
   };
-  const bool do_stdp = plastic && has_stdp && !plastic_idx.empty();
+  const bool do_stdp = plastic && has_stdp && !plastic_idx.empty() && stdp_rule == SPK_STDP_WEIGHT_DEPENDENT;
+  const bool do_dense = plastic && has_stdp && !plastic_idx.empty() && stdp_rule != SPK_STDP_WEIGHT_DEPENDENT;
   if (threads <= 1) {
     for (int64_t s = 0; s < n_steps; ++s) {
       R t;
@@ -560,7 +643,8 @@ void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
       lif_range(0, N, t, T);
       poisson_range(0, Nin, t, T);
       if (do_stdp) stdp_range(0, (int64_t)plastic_idx.size(), t);
-      finish_step(t);
+      if (do_dense) dense_stdp_range(0, (int64_t)plastic_idx.size(), T);
+      finish_step(t, T);
       propagate_thread(0, T);
       record(t);
     }
@@ -580,7 +664,10 @@ void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
       poisson_range(i0[th], i1[th], t_cur, T_cur);
       bar.arrive_and_wait();
       if (do_stdp) stdp_range(p0[th], p1[th], t_cur);
-      if (th == 0) finish_step(t_cur);
+      if (do_dense) dense_stdp_range(p0[th], p1[th], T_cur);
+      // finish_step writes history slot T, which no range reads this step
+      // (delays are 1..H-1)
+      if (th == 0) finish_step(t_cur, T_cur);
       bar.arrive_and_wait();
       propagate_thread(th, T_cur);
       if (th == 0) record(t_cur);

@@ -20,6 +20,9 @@ SPK_ERR_OOM = -3
 SPK_ERR_UNSUPPORTED = -4
 SPK_ERR_TIMEOUT = -5
 SPK_ERR_OVERFLOW = -6
+SPK_STDP_WEIGHT_DEPENDENT = 0
+SPK_STDP_EVANS = 1
+SPK_STDP_INHIBITORY = 2
 SPK_ERR_STATE = -7
 SPK_ERR_BUSY = -8
 ERROR_NAMES = {
@@ -74,7 +77,7 @@ class NetDesc(C.Structure):
         ("n_synapses", i64), ("pre", P(i32)), ("post", P(i32)), ("weight", P(f32)),
         ("scale", P(f32)), ("delay", P(i32)), ("label", P(i32)), ("plastic", P(C.c_uint8)),
         ("has_stdp", i32), ("stdp", StdpParams),
-        ("seed", u64), ("spike_capacity", i64), ("record_inputs", i32), ("reserved", i32),
+        ("seed", u64), ("spike_capacity", i64), ("record_inputs", i32), ("stdp_rule", i32),
     ]
 
 

@@ -67,6 +67,7 @@ struct BulkStep {
   float t, tg;
   int T, slot;
   bool live, stdp_run, inputs_active;
+  bool dense_run;  // a per-synapse-trace rule updates this step
 };
 
 __device__ __forceinline__ BulkStep bulk_step(const NetDev& d, const RunCtl& c, int s) {
@@ -80,7 +81,9 @@ __device__ __forceinline__ BulkStep bulk_step(const NetDev& d, const RunCtl& c, 
   b.T = (int)roundf(b.t / dt);
   b.slot = b.T % d.B;
   b.tg = b.t + 0.0f * dt;
-  b.stdp_run = d.has_stdp && c.plastic;
+  // the event-driven (weight-dependent) rule's passes, or the per-synapse-trace rules' pass
+  b.stdp_run = d.has_stdp && c.plastic && d.stdp_rule == SPK_STDP_WEIGHT_DEPENDENT;
+  b.dense_run = d.has_stdp && c.plastic && d.stdp_rule != SPK_STDP_WEIGHT_DEPENDENT;
   b.inputs_active = c.inputs_active != 0 || s > 0;
   return b;
 }
@@ -253,6 +256,7 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
       if (lane == 0) {
         d.bitsA[bw.word + u] = word;
         d.bitsP[bw.word + u] = st.stdp_run ? word : 0u;
+        if (d.hist) d.hist[(size_t)(st.T % d.H) * d.n_words + bw.word + u] = word;
       }
     }
   } else {
@@ -301,6 +305,7 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
       if (lane == 0) {
         d.bitsA[bw.word + u] = wa;
         d.bitsP[bw.word + u] = wp;
+        if (d.hist) d.hist[(size_t)(st.T % d.H) * d.n_words + bw.word + u] = wa;
       }
     }
   }
@@ -844,6 +849,73 @@ __global__ void __launch_bounds__(256) bulk_post_kernel(const NetDev* __restrict
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) n_post += __shfl_xor_sync(FULL, n_post, o);
     if (lane == 0 && n_post) atomicAdd(&d.ctl->stdp_post, n_post);
+  }
+}
+
+// ---- timestep part 3b: per-synapse-trace STDP rules ---------------------------------------
+// Every plastic synapse of the networks whose rule keeps two traces per
+// synapse, every timestep, before this timestep's propagation: the traces
+// decay, a presynaptic spike is seen when it arrives (the key's spike word of
+// timestep T - delay in the history), a postsynaptic one at T, and the weight
+// moves.  A warp per post; the records are the post's plastic afferents.
+//   Evans (EvansSTDPPlasticity.cu:95-133): traces C, D; weights in [0, 1].
+//   Inhibitory (InhibitorySTDPPlasticity.cu:102-143): Vogels' memory traces;
+//   weights clipped at 0; its constant term in double, as the reference's
+//   2.0 literal evaluates it.
+__global__ void __launch_bounds__(256) bulk_dense_stdp_kernel(const NetDev* __restrict__ nets,
+                                                              const BulkPostItem* __restrict__ items, int n_items,
+                                                              int s) {
+  const int lane = threadIdx.x & 31;
+  const int n_warps = gridDim.x * (blockDim.x >> 5);
+  for (int it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < n_items; it += n_warps) {
+    const BulkPostItem item = items[it];
+    const NetDev& d = nets[item.net];
+    const RunCtl c = load_ctl(d.ctl);
+    const BulkStep st = bulk_step(d, c, s);
+    if (!st.live || !st.dense_run) continue;
+    const int key = d.KL + item.post;
+    const bool post_sp = ((d.bitsA[key >> 5] >> (key & 31)) & 1u) != 0;
+    const int a0 = __ldg(d.csc_ptr + item.post), a1 = __ldg(d.csc_ptr + item.post + 1);
+    const float dt = d.dt;
+    const float c0 = d.rule_c[0], c1 = d.rule_c[1], c2 = d.rule_c[2], c3 = d.rule_c[3];
+    for (int a = a0 + lane; a < a1; a += 32) {
+      const uint2 rec = d.csc[a];
+      const int dl = d.csc_delay[a];
+      float2 tr = d.dense_tr[a];
+      int slot = (st.T - dl) % d.H;
+      if (slot < 0) slot += d.H;
+      const uint32_t pk = rec.x;
+      const bool pre_sp = ((d.hist[(size_t)slot * d.n_words + (pk >> 5)] >> (pk & 31)) & 1u) != 0;
+      float w = __uint_as_float(rec.y);
+      if (d.stdp_rule == SPK_STDP_EVANS) {
+        tr.x = (1.0f - (dt / c0)) * tr.x;
+        tr.y = (1.0f - (dt / c1)) * tr.y;
+        if (pre_sp) tr.x += dt * c2 * (1.0f - tr.x);
+        if (post_sp) tr.y += dt * c3 * (1.0f - tr.y);
+        float syn = 0.0f;
+        const float old_w = w;
+        if (pre_sp) syn -= (old_w * tr.y);
+        if (post_sp) syn += ((1.0f - old_w) * tr.x);
+        w = old_w + syn;
+        if (w < 0.0f) w = 0.0f;
+        if (w > 1.0f) w = 1.0f;
+      } else {
+        tr.x *= c0;
+        tr.y *= c0;
+        if (pre_sp) tr.x += 1.0f;
+        if (post_sp) tr.y += 1.0f;
+        float syn = 0.0f;
+        if (pre_sp) {
+          syn += c1 * (tr.y);
+          syn = (float)((double)syn + (double)(-c1) * (2.0 * (double)c2 * (double)c3));
+        }
+        if (post_sp) syn += c1 * (tr.x);
+        w += syn;
+        if (w < 0.0f) w = 0.0f;
+      }
+      d.csc[a].y = __float_as_uint(w);
+      d.dense_tr[a] = tr;
+    }
   }
 }
 

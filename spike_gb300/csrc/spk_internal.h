@@ -101,6 +101,16 @@ struct NetDev {
   int* step_count;            // keys in step_list
   // rate monitor: spikes of each key since the last clear, or null
   int* rate_counts;           // [n_keys]
+  // Rules with two traces per plastic synapse (SPK_STDP_EVANS,
+  // SPK_STDP_INHIBITORY; bulk mode only): the records' delays, the traces,
+  // and the spike words of the last H timesteps (slot T % H), in which a
+  // presynaptic spike is looked up delay steps back.
+  int stdp_rule;              // SPK_STDP_*
+  int H;                      // D_max + 1
+  const int* csc_delay;       // [n_csc]
+  float2* dense_tr;           // [n_csc]: presynaptic, postsynaptic trace
+  uint32_t* hist;             // [H][n_words]
+  float rule_c[4];            // the rule's constants
 };
 
 struct CtaMap {

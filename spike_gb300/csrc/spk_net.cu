@@ -215,6 +215,9 @@ struct spk_net {
   int pending_status = SPK_OK;
   bool generated = false;  // connectivity drawn on the device (no host synapse arrays)
   int withhold = -1;       // fault injection: CTA rank left out of the next launch
+  int stdp_rule = SPK_STDP_WEIGHT_DEPENDENT;
+  spk_batch* self_batch = nullptr;  // runs of a network with a per-synapse-trace rule (bulk mode)
+  bool dense() const { return has_stdp && stdp_rule != SPK_STDP_WEIGHT_DEPENDENT; }
   int64_t n_csc = 0;       // plastic afferent records
   float step_cost = 0.0f;  // measured or estimated time of one step alone (batch packing)
 };
@@ -243,6 +246,8 @@ struct spk_batch {
   BulkBlock* dblocks = nullptr;  // [blocks_total] blocks of 32-key words with real keys
   int blocks_total = 0;
   BulkPostItem* items = nullptr; // afferent-pass work list of a timestep
+  BulkPostItem* dense_items = nullptr;  // posts of the per-synapse-trace-rule networks
+  int n_dense_items = 0;
   int* item_count = nullptr;
   int item_cap = 0;
   bool any_plastic = false;
@@ -290,6 +295,10 @@ static int upload_state_defaults(spk_net* n) {
   SPK_CUDA(cudaMemsetAsync(h.ring, 0, sizeof(float) * (size_t)h.n_tiles * h.B * h.TS * h.L, n->stream));
   // RateActivityMonitor::reset_state (Spike/Backend/CUDA/ActivityMonitor/RateActivityMonitor.cu:12-16)
   if (h.rate_counts) SPK_CUDA(cudaMemsetAsync(h.rate_counts, 0, sizeof(int) * (size_t)h.n_keys, n->stream));
+  // per-synapse traces := 0 (EvansSTDPPlasticity.cpp:21-26, InhibitorySTDPPlasticity.cu:13-28)
+  // and the spike-bit history cleared
+  if (h.dense_tr) SPK_CUDA(cudaMemsetAsync(h.dense_tr, 0, sizeof(float2) * (size_t)n->n_csc, n->stream));
+  if (h.hist) SPK_CUDA(cudaMemsetAsync(h.hist, 0, sizeof(uint32_t) * (size_t)h.H * h.n_words, n->stream));
   if (n->has_stdp) {
     SPK_CUDA(cudaMemsetAsync(h.post_trace, 0, sizeof(float) * n->N, n->stream));
     SPK_CUDA(cudaMemsetAsync(h.pre_trace, 0, sizeof(float) * h.n_keys, n->stream));
@@ -353,6 +362,19 @@ static int run_steps_impl(spk_net* n, int64_t steps, int plastic, float start) {
   if (steps > 0x7fffffff) {
     set_error("run of %lld steps exceeds the 2^31-1 step limit of one run", (long long)steps);
     return SPK_ERR_INVALID;
+  }
+  if (n->dense()) {
+    // Per-synapse-trace STDP runs in bulk mode: a batch of this one network
+    // (the caller sets the network's time afterwards, as for any run).
+    if (!n->self_batch) {
+      const spk_schedule bs{0, 0, 0, n->plan.K};
+      int rc = spk_batch_create(&n, 1, &bs, &n->self_batch);
+      if (rc) return rc;
+    }
+    n->current_time = start;
+    const int64_t each = steps;
+    const int32_t pl = plastic ? 1 : 0;
+    return spk_batch_run_steps_each(n->self_batch, &each, &pl);
   }
   set_ctl_kernel<<<1, 1, 0, n->stream>>>(n->hd.ctl, start, (int)steps,
                                          (plastic && n->has_stdp) ? 1 : 0, n->record_inputs ? 1 : 0);
@@ -422,12 +444,17 @@ struct ModelSpec {
   const float* label_vhat = nullptr;
   int has_stdp = 0;
   spk_stdp_params stdp{};
+  int stdp_rule = SPK_STDP_WEIGHT_DEPENDENT;
   uint64_t seed = 0;
   int64_t spike_capacity = 0;
   int record_inputs = 0;
 };
 
 static int validate_spec(const ModelSpec& m) {
+  if (m.stdp_rule < SPK_STDP_WEIGHT_DEPENDENT || m.stdp_rule > SPK_STDP_INHIBITORY) {
+    set_error("unknown STDP rule %d", m.stdp_rule);
+    return SPK_ERR_INVALID;
+  }
   if (m.N <= 0 || m.Nin < 0 || m.L < 1 || m.L > MAX_LABELS || !(m.dt > 0.0f)) {
     set_error("sizes out of range (neurons %d, inputs %d, labels %d)", m.N, m.Nin, m.L);
     return SPK_ERR_INVALID;
@@ -484,6 +511,7 @@ static int new_net(const ModelSpec& m, int B, int64_t S, const spk_schedule* sch
   n->S = S;
   n->dt = m.dt;
   n->has_stdp = m.has_stdp != 0;
+  n->stdp_rule = m.stdp_rule;
   n->record_inputs = m.record_inputs != 0;
   n->seed = m.seed;
   n->n_stim = m.Nin > 0 ? m.n_stim : 0;
@@ -499,9 +527,10 @@ static int new_net(const ModelSpec& m, int B, int64_t S, const spk_schedule* sch
 // entries, csc_ptr, csc, V, last, traces, ring, input next, rates, post
 // traces, pre traces, pre-trace mailbox, spike and pre-event bitmaps, CTA key
 // lists and stamps, spike store, run control, abort flag, descriptor, CTA map,
-// rate-monitor counts.
+// rate-monitor counts, and for per-synapse-trace STDP rules the afferent
+// records' delays, their traces and the spike-word history.
 static std::vector<size_t> arena_part_sizes(const Plan& plan, int N, int Nin, int L, int B, int stdp, int64_t S,
-                                            int64_t n_csc, int n_stim, int64_t spike_cap) {
+                                            int64_t n_csc, int n_stim, int64_t spike_cap, int dense = 0) {
   const size_t n_cells = (size_t)plan.n_keys * plan.n_tiles;
   const size_t key_cap = (size_t)plan.W * (plan.TS + plan.ITS);
   return {sizeof(int32_t) * (n_cells + 1),
@@ -526,7 +555,10 @@ static std::vector<size_t> arena_part_sizes(const Plan& plan, int N, int Nin, in
           sizeof(int),
           sizeof(NetDev),
           sizeof(CtaMap) * plan.nctas,
-          sizeof(int) * (size_t)plan.n_keys};
+          sizeof(int) * (size_t)plan.n_keys,
+          sizeof(int32_t) * (dense ? (size_t)n_csc : 0),
+          sizeof(float) * (dense ? 2 * (size_t)n_csc : 0),
+          sizeof(uint32_t) * (dense ? (size_t)(B - 2) * plan.n_words : 0)};
 }
 
 static size_t arena_total(const std::vector<size_t>& sizes) {
@@ -541,7 +573,8 @@ static size_t arena_total(const std::vector<size_t>& sizes) {
 // device afterwards), clears the exchange, checks co-residency and resets the
 // state.  On failure `n` is destroyed.
 static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int32_t* rowptr_h,
-                        const uint2* entries_h, const int32_t* csc_ptr_h, const uint2* csc_h) {
+                        const uint2* entries_h, const int32_t* csc_ptr_h, const uint2* csc_h,
+                        const int32_t* csc_delay_h = nullptr) {
   DeviceInfo di;
   int rc = device_info(&di);
   if (rc) {
@@ -570,11 +603,14 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   void* p_ckeys = nullptr; void* p_cstamp = nullptr;
   const int key_cap = plan.W * (plan.TS + plan.ITS);
   void* p_ctl = nullptr; void* p_abort = nullptr; void* p_dd = nullptr; void* p_map = nullptr;
-  void* p_rate = nullptr;
-  const std::vector<size_t> sizes = arena_part_sizes(plan, N, Nin, L, B, stdp, S, n_csc, n->n_stim, spike_cap);
+  void* p_rate = nullptr; void* p_cdelay = nullptr; void* p_dtr = nullptr; void* p_hist = nullptr;
+  const int dense = n->dense() ? 1 : 0;
+  const std::vector<size_t> sizes =
+      arena_part_sizes(plan, N, Nin, L, B, stdp, S, n_csc, n->n_stim, spike_cap, dense);
   void** dsts[] = {&p_rowptr, &p_entries, &p_cscptr, &p_csc,   &p_V,     &p_last,   &p_gtr,  &p_ring,
                    &p_innext, &p_rates,   &p_post,   &p_pre,   &p_pub,   &p_bA,     &p_bP,   &p_ckeys,
-                   &p_cstamp, &p_spk,     &p_ctl,    &p_abort, &p_dd,    &p_map,  &p_rate};
+                   &p_cstamp, &p_spk,     &p_ctl,    &p_abort, &p_dd,    &p_map,  &p_rate,
+                   &p_cdelay, &p_dtr,     &p_hist};
   std::vector<Part> parts;
   for (size_t i = 0; i < sizes.size(); ++i) parts.push_back(Part{dsts[i], sizes[i]});
   const size_t total = arena_total(sizes);
@@ -661,6 +697,30 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   }
   h.seed = m.seed;
   h.rate_counts = (int*)p_rate;
+  h.stdp_rule = n->stdp_rule;
+  if (dense) {
+    h.H = B - 2;  // D_max + 1
+    h.csc_delay = (const int*)p_cdelay;
+    h.dense_tr = (float2*)p_dtr;
+    h.hist = (uint32_t*)p_hist;
+    const spk_stdp_params& sp = m.stdp;
+    if (n->stdp_rule == SPK_STDP_EVANS) {
+      // decay_term_tau_C, decay_term_tau_D, synaptic_neurotransmitter_concentration_alpha_C,
+      // model_parameter_alpha_D (Spike/Plasticity/EvansSTDPPlasticity.hpp)
+      h.rule_c[0] = sp.tau_plus;
+      h.rule_c[1] = sp.tau_minus;
+      h.rule_c[2] = sp.a_plus;
+      h.rule_c[3] = sp.a_minus;
+    } else {
+      // trace decay expf(- timestep / tau_istdp), computed on the host as the
+      // reference does (InhibitorySTDPPlasticity.cu:61), learningrate,
+      // targetrate, tau_istdp
+      h.rule_c[0] = expf(-m.dt / sp.tau_plus);
+      h.rule_c[1] = sp.lambda;
+      h.rule_c[2] = sp.alpha;
+      h.rule_c[3] = sp.tau_plus;
+    }
+  }
   h.rowptr = (const int*)p_rowptr;
   h.entries = (uint2*)p_entries;
   h.csc_ptr = (const int*)p_cscptr;
@@ -703,6 +763,7 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   urc |= up(p_entries, entries_h, sizeof(uint2) * S);
   urc |= up(p_cscptr, csc_ptr_h, sizeof(int32_t) * (stdp ? (size_t)N + 1 : 0));
   urc |= up(p_csc, csc_h, sizeof(uint2) * (size_t)n_csc);
+  if (dense) urc |= up(p_cdelay, csc_delay_h, sizeof(int32_t) * (size_t)n_csc);
   if (Nin > 0) urc |= up(p_rates, m.rates, sizeof(float) * (size_t)n->n_stim * Nin);
   urc |= up(p_ctl, &ctl, sizeof(ctl));
   urc |= up(p_dd, &h, sizeof(h));
@@ -770,6 +831,7 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
   m.label_vhat = d->label_vhat;
   m.has_stdp = d->has_stdp ? 1 : 0;
   m.stdp = d->stdp;
+  m.stdp_rule = d->stdp_rule;
   m.seed = d->seed;
   m.spike_capacity = d->spike_capacity;
   m.record_inputs = d->record_inputs;
@@ -852,6 +914,7 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
   // ---- plastic afferent records per post: (pre key, weight), creation order --
   std::vector<int32_t> csc_ptr;
   std::vector<uint2> csc;
+  std::vector<int32_t> csc_delay;
   n->csc_of.assign(stdp ? S : 0, -1);
   if (stdp) {
     csc_ptr.assign((size_t)N + 1, 0);
@@ -859,11 +922,13 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
       if (n->cls_of[s]) csc_ptr[d->post[s] + 1]++;
     for (int q = 0; q < N; ++q) csc_ptr[q + 1] += csc_ptr[q];
     csc.resize(csc_ptr[N]);
+    if (n->dense()) csc_delay.resize(csc_ptr[N]);
     std::vector<int32_t> fill(csc_ptr.begin(), csc_ptr.end() - 1);
     for (int64_t s = 0; s < S; ++s)
       if (n->cls_of[s]) {
         const int32_t pos = fill[d->post[s]]++;
         csc[pos] = make_uint2((uint32_t)key_of(d->pre[s]), f2u(d->weight[s]));
+        if (n->dense()) csc_delay[pos] = d->delay[s];
         n->csc_of[s] = pos;
       }
   }
@@ -885,7 +950,7 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
     }
   }
   rc = setup_device(n, m, (int64_t)csc.size(), rowptr.data(), entries.data(), stdp ? csc_ptr.data() : nullptr,
-                    csc.data());
+                    csc.data(), n->dense() ? csc_delay.data() : nullptr);
   if (rc) return rc;
   *out = n;
   return SPK_OK;
@@ -1303,6 +1368,10 @@ std::vector<SnapPart> snap_parts(spk_net* n) {
     p.push_back({h.pre_trace, sizeof(float) * (size_t)h.n_keys});
     p.push_back({h.csc, sizeof(uint2) * (size_t)n->n_csc});
   }
+  if (n->dense()) {
+    p.push_back({h.dense_tr, sizeof(float2) * (size_t)n->n_csc});
+    p.push_back({h.hist, sizeof(uint32_t) * (size_t)h.H * h.n_words});
+  }
   return p;
 }
 }  // namespace
@@ -1428,6 +1497,7 @@ int spk_net_synapse_count(const spk_net* n, int64_t* count) {
 
 int spk_net_destroy(spk_net* n) {
   if (!n) return SPK_ERR_INVALID;
+  if (n->self_batch) spk_batch_destroy(n->self_batch);
   if (n->stream) cudaStreamSynchronize(n->stream);
   if (n->graph) cudaGraphExecDestroy(n->graph);
   if (n->stream) cudaStreamDestroy(n->stream);
@@ -1894,6 +1964,16 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
       delete b;
       return SPK_ERR_CUDA;
     }
+    // per-synapse-trace STDP rules run in bulk mode only
+    bool any_dense = false;
+    for (int i = 0; i < n_nets; ++i) any_dense = any_dense || nets[i]->dense();
+    if (any_dense) {
+      const int rc = spk_batch_set_mode(b, SPK_BATCH_BULK);
+      if (rc) {
+        spk_batch_destroy(b);
+        return rc;
+      }
+    }
     *out = b;
     return SPK_OK;
   });
@@ -1914,6 +1994,9 @@ static int bulk_launch_block(spk_batch* b) {
                                (const NetDev*)b->dd, (const BulkBlock*)b->dblocks, s, b->item_count));
     SPK_CUDA(launch_overlapped(bulk_list_kernel, n, BULK_LIST_THREADS, 0, b->stream, (const NetDev*)b->dd, s,
                                b->items, b->item_count, b->item_cap));
+    if (b->n_dense_items)
+      bulk_dense_stdp_kernel<<<std::min((b->n_dense_items + 7) / 8, di.sms * 8), 256, 0, b->stream>>>(
+          b->dd, b->dense_items, b->n_dense_items, s);
     if (b->any_plastic) {
       SPK_CUDA(cudaEventRecord(b->fork, b->stream));
       SPK_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0));
@@ -2009,6 +2092,11 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
   if (!b || (mode != SPK_BATCH_WAVES && mode != SPK_BATCH_BULK)) return SPK_ERR_INVALID;
   if (mode == b->mode) return SPK_OK;
   if (mode == SPK_BATCH_WAVES) {
+    for (const spk_net* n : b->nets)
+      if (n->dense()) {
+        set_error("waves mode: a network with a per-synapse-trace STDP rule runs in bulk mode only");
+        return SPK_ERR_UNSUPPORTED;
+      }
     b->mode = mode;
     return SPK_OK;
   }
@@ -2048,6 +2136,24 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
         return SPK_ERR_UNSUPPORTED;
       }
       b->item_cap = (int)cap;
+      // posts of the networks with a per-synapse-trace rule: the dense STDP pass
+      {
+        std::vector<BulkPostItem> dense;
+        for (size_t i = 0; i < b->nets.size(); ++i)
+          if (b->nets[i]->dense())
+            for (int q = 0; q < b->nets[i]->N; ++q) dense.push_back(BulkPostItem{(int)i, q});
+        if (!dense.empty()) {
+          if (cudaMalloc(&b->dense_items, sizeof(BulkPostItem) * dense.size()) != cudaSuccess) {
+            cudaGetLastError();
+            b->dense_items = nullptr;
+            set_error("bulk mode: device allocation failed");
+            return SPK_ERR_OOM;
+          }
+          SPK_CUDA(cudaMemcpy(b->dense_items, dense.data(), sizeof(BulkPostItem) * dense.size(),
+                              cudaMemcpyHostToDevice));
+          b->n_dense_items = (int)dense.size();
+        }
+      }
       if (b->any_plastic && !b->side &&
           (cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
            cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
@@ -2375,6 +2481,7 @@ int spk_batch_destroy(spk_batch* b) {
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->join) cudaEventDestroy(b->join);
   if (b->rd) cudaEventDestroy(b->rd);
+  if (b->dense_items) cudaFree(b->dense_items);
   if (b->rb_mem) cudaFree(b->rb_mem);
   if (b->rb_ids) cudaFree(b->rb_ids);
   if (b->rb_times) cudaFree(b->rb_times);

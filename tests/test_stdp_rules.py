@@ -1,0 +1,79 @@
+"""STDP rules with two traces per plastic synapse (GPU): the Evans rule
+(Spike/Backend/CUDA/Plasticity/EvansSTDPPlasticity.cu) and the inhibitory
+rule of Vogels et al. 2011 (Spike/Backend/CUDA/Plasticity/
+InhibitorySTDPPlasticity.cu).  Both update every plastic synapse every
+timestep and see a presynaptic spike when it arrives; the engine runs them in
+bulk mode.  Checked against the oracle bit for bit (spikes, state, ring,
+weights), across runs with plasticity off, in a batch beside a network with the
+event-driven rule, and through a snapshot."""
+import numpy as np
+import pytest
+
+import descs
+from engine_checks import assert_same, bits
+from oracle import OracleNet
+from spike_gb300 import Batch, Net, schedule
+from spike_gb300 import _native as N
+from spike_gb300.model import STDPParams
+
+pytestmark = pytest.mark.gpu
+
+# Evans: a_plus = alpha_C, a_minus = alpha_D, tau_plus = tau_C, tau_minus = tau_D
+EVANS = STDPParams(a_plus=0.5, a_minus=0.5, tau_plus=0.004, tau_minus=0.005, lambda_=0.0, alpha=0.0, w_max=1.0)
+# inhibitory: tau_plus = tau_istdp, lambda = learningrate, alpha = targetrate
+VOGELS = STDPParams(a_plus=0.0, a_minus=0.0, tau_plus=0.02, tau_minus=0.02, lambda_=0.0004, alpha=10.0, w_max=1.0)
+RULES = [(N.SPK_STDP_EVANS, EVANS), (N.SPK_STDP_INHIBITORY, VOGELS)]
+
+
+def net_desc(rule, sp, seed=5):
+    return descs.random_voltage_net(n=300, n_in=200, plastic=True, stdp=sp, stdp_rule=rule, seed=seed)
+
+
+@pytest.mark.parametrize("rule,sp", RULES)
+def test_rule_matches_oracle(rule, sp):
+    d = net_desc(rule, sp)
+    net = Net.from_desc(d.desc)
+    o = OracleNet(d.desc)
+    for plastic, t in ((True, 0.03), (False, 0.01), (True, 0.03)):
+        net.run(t, plastic)
+        o.run(t, plastic)
+    assert net.synchronize() == 0
+    assert_same(net, o, 300, 200, 1, weights=True, tag=f"rule {rule}")
+    w = net.weights(o.n_synapses)
+    assert (w != d.arrays["weight"]).sum() > 100  # the rule moved weights
+    assert len(o.spikes()[0]) > 50
+
+
+@pytest.mark.parametrize("rule,sp", RULES)
+def test_rule_in_a_batch_beside_the_event_driven_rule(rule, sp):
+    wd = STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02, lambda_=1.0, alpha=1.0, w_max=1.0)
+    da = net_desc(rule, sp, seed=9)
+    db = descs.random_voltage_net(n=250, n_in=150, plastic=True, stdp=wd, seed=10)
+    sched = schedule(8, 32, 0, 0)  # a batch's networks share warps per CTA
+    batched = [Net.from_desc(da.desc, sched), Net.from_desc(db.desc, sched)]
+    b = Batch(batched)  # a network with a per-synapse-trace rule puts the batch in bulk mode
+    with pytest.raises(N.SpikeError):
+        b.set_mode(N.SPK_BATCH_WAVES)
+    b.run_steps(500, True)
+    assert b.synchronize() == 0
+    for x, d, n, n_in in ((batched[0], da, 300, 200), (batched[1], db, 250, 150)):
+        o = OracleNet(d.desc)
+        o.run_steps(500, True)
+        assert_same(x, o, n, n_in, 1, weights=True, tag="batched")
+    b.close()
+
+
+def test_snapshot_carries_the_rule_state():
+    d = net_desc(N.SPK_STDP_INHIBITORY, VOGELS)
+    a = Net.from_desc(d.desc)
+    a.run(0.02)
+    snap = a.snapshot()
+    a.run(0.02)
+    assert a.synchronize() == 0
+    b = Net.from_desc(d.desc)
+    b.restore(snap)
+    b.run(0.02)
+    assert b.synchronize() == 0
+    S = len(d.arrays["weight"])
+    np.testing.assert_array_equal(bits(a.weights(S)), bits(b.weights(S)))
+    np.testing.assert_array_equal(bits(a.state(N.SPK_FIELD_V, 300)), bits(b.state(N.SPK_FIELD_V, 300)))
