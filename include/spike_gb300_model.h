@@ -83,6 +83,9 @@ int spk_model_add_input_group(spk_model* m, int32_t shape0, int32_t shape1, floa
                               int32_t* group_id);
 int spk_model_add_stimulus(spk_model* m, const float* rates, int32_t n, int32_t* stimulus_id);
 int spk_model_add_stdp_rule(spk_model* m, const spk_stdp_params* p, int32_t* rule_id);
+/* Any of the SPK_STDP_* rules, its parameters in the descriptor's field
+ * mapping (spike_gb300.h); one rule per model. */
+int spk_model_add_plasticity_rule(spk_model* m, int32_t rule, const spk_stdp_params* p, int32_t* rule_id);
 int spk_model_add_synapse_group(spk_model* m, int32_t pre_group, int32_t post_group,
                                 const spk_synapse_params* p, int32_t* group_id);
 /* Examples/UtilityFunctions.hpp:51-82 connect_with_sparsity: fixed in-degree

@@ -109,6 +109,24 @@ struct weightdependent_stdp_plasticity_parameters_struct : stdp_plasticity_param
   bool clip_upper = false;  // extension: clip at w_max as well as at 0
 };
 
+// evans_stdp_plasticity_parameters_struct (Spike/Plasticity/EvansSTDPPlasticity.hpp);
+// learning_rate_rho is carried but, as in the reference's kernel, unused.
+struct evans_stdp_plasticity_parameters_struct : stdp_plasticity_parameters_struct {
+  float decay_term_tau_D = 0.005f;
+  float model_parameter_alpha_D = 0.5f;
+  float synaptic_neurotransmitter_concentration_alpha_C = 0.5f;
+  float decay_term_tau_C = 0.004f;
+  float learning_rate_rho = 0.1f;
+};
+// inhibitory_stdp_plasticity_parameters_struct
+// (Spike/Plasticity/InhibitorySTDPPlasticity.hpp); momentumrate is unused there too.
+struct inhibitory_stdp_plasticity_parameters_struct : stdp_plasticity_parameters_struct {
+  float tau_istdp = 0.02f;
+  float learningrate = 0.0004f;
+  float targetrate = 10.0f;
+  float momentumrate = 0.0f;
+};
+
 // ---- neurons -------------------------------------------------------------------
 class SpikingNeurons {
  public:
@@ -251,6 +269,22 @@ class WeightDependentSTDPPlasticity : public STDPPlasticity {
                                 SpikingNeurons* input_neurons,
                                 stdp_plasticity_parameters_struct* stdp_parameters);
   weightdependent_stdp_plasticity_parameters_struct* stdp_params;
+};
+
+// Rules with two traces per plastic synapse, updated every timestep (the
+// engine runs them in bulk mode).
+class EvansSTDPPlasticity : public STDPPlasticity {
+ public:
+  EvansSTDPPlasticity(SpikingSynapses* synapses, SpikingNeurons* neurons, SpikingNeurons* input_neurons,
+                      stdp_plasticity_parameters_struct* stdp_parameters);
+  evans_stdp_plasticity_parameters_struct* stdp_params;
+};
+
+class InhibitorySTDPPlasticity : public STDPPlasticity {
+ public:
+  InhibitorySTDPPlasticity(SpikingSynapses* synapses, SpikingNeurons* neurons, SpikingNeurons* input_neurons,
+                           stdp_plasticity_parameters_struct* stdp_parameters);
+  inhibitory_stdp_plasticity_parameters_struct* stdp_params;
 };
 
 // ---- monitors ------------------------------------------------------------------

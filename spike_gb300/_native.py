@@ -234,6 +234,7 @@ _SIGS = {
     "spk_model_add_input_group": (i32, [_VP, i32, i32, f32, P(i32)]),
     "spk_model_add_stimulus": (i32, [_VP, P(f32), i32, P(i32)]),
     "spk_model_add_stdp_rule": (i32, [_VP, P(StdpParams), P(i32)]),
+    "spk_model_add_plasticity_rule": (i32, [_VP, i32, P(StdpParams), P(i32)]),
     "spk_model_add_synapse_group": (i32, [_VP, i32, i32, P(SynapseParams), P(i32)]),
     "spk_model_connect_with_sparsity": (i32, [_VP, i32, i32, f32, P(SynapseParams), P(i32)]),
     "spk_model_set_recording": (i32, [_VP, i32, i64]),

@@ -483,6 +483,18 @@ WeightDependentSTDPPlasticity::WeightDependentSTDPPlasticity(SpikingSynapses*, S
   if (!stdp_params) fail(SPK_ERR_INVALID, "weight-dependent STDP needs its parameter struct");
 }
 
+EvansSTDPPlasticity::EvansSTDPPlasticity(SpikingSynapses*, SpikingNeurons*, SpikingNeurons*,
+                                         stdp_plasticity_parameters_struct* p) {
+  stdp_params = dynamic_cast<evans_stdp_plasticity_parameters_struct*>(p);
+  if (!stdp_params) fail(SPK_ERR_INVALID, "Evans STDP needs its parameter struct");
+}
+
+InhibitorySTDPPlasticity::InhibitorySTDPPlasticity(SpikingSynapses*, SpikingNeurons*, SpikingNeurons*,
+                                                   stdp_plasticity_parameters_struct* p) {
+  stdp_params = dynamic_cast<inhibitory_stdp_plasticity_parameters_struct*>(p);
+  if (!stdp_params) fail(SPK_ERR_INVALID, "inhibitory STDP needs its parameter struct");
+}
+
 // ---- monitor ------------------------------------------------------------------------
 void SpikingActivityMonitor::reset_state() {
   neuron_ids_of_stored_spikes_on_host.clear();
@@ -623,12 +635,31 @@ int SpikingModel::build_desc(spk_net_desc* d) {
   std::fill(s->plastic.begin(), s->plastic.end(), 0);
   int n_rules = 0;
   const weightdependent_stdp_plasticity_parameters_struct* wp = nullptr;
+  d->stdp_rule = SPK_STDP_WEIGHT_DEPENDENT;
+  std::memset(&d->stdp, 0, sizeof(d->stdp));
   for (Plasticity* r : plasticity_rule_vec) {
-    auto* wd = dynamic_cast<WeightDependentSTDPPlasticity*>(r);
-    if (!wd) return SPK_ERR_UNSUPPORTED;
     ++n_rules;
-    wp = wd->stdp_params;
-    for (int idx : wd->plastic_synapses) s->plastic[idx] = 1;
+    if (auto* wd = dynamic_cast<WeightDependentSTDPPlasticity*>(r)) {
+      wp = wd->stdp_params;
+    } else if (auto* ev = dynamic_cast<EvansSTDPPlasticity*>(r)) {
+      // the descriptor's field mapping for SPK_STDP_EVANS
+      d->stdp_rule = SPK_STDP_EVANS;
+      d->stdp.tau_minus = ev->stdp_params->decay_term_tau_D;
+      d->stdp.tau_plus = ev->stdp_params->decay_term_tau_C;
+      d->stdp.a_minus = ev->stdp_params->model_parameter_alpha_D;
+      d->stdp.a_plus = ev->stdp_params->synaptic_neurotransmitter_concentration_alpha_C;
+      d->stdp.w_max = 1.0f;
+    } else if (auto* ih = dynamic_cast<InhibitorySTDPPlasticity*>(r)) {
+      d->stdp_rule = SPK_STDP_INHIBITORY;
+      d->stdp.tau_plus = ih->stdp_params->tau_istdp;
+      d->stdp.tau_minus = ih->stdp_params->tau_istdp;
+      d->stdp.lambda = ih->stdp_params->learningrate;
+      d->stdp.alpha = ih->stdp_params->targetrate;
+      d->stdp.w_max = 1.0f;
+    } else {
+      return SPK_ERR_UNSUPPORTED;
+    }
+    for (int idx : r->plastic_synapses) s->plastic[idx] = 1;
   }
   if (n_rules > 1) return SPK_ERR_UNSUPPORTED;
   d->plastic = s->plastic.data();
@@ -729,8 +760,8 @@ struct spk_model {
   LIFSpikingNeurons neurons;
   PoissonInputSpikingNeurons* inputs = nullptr;
   SpikingSynapses* synapses = nullptr;
-  std::vector<WeightDependentSTDPPlasticity*> rules;
-  std::vector<weightdependent_stdp_plasticity_parameters_struct*> rule_params;
+  std::vector<Plasticity*> rules;
+  std::vector<stdp_plasticity_parameters_struct*> rule_params;
   SpikingActivityMonitor* neuron_monitor = nullptr;
   SpikingActivityMonitor* input_monitor = nullptr;
   RateActivityMonitor* rate_monitor[2] = {nullptr, nullptr};  // neurons, inputs
@@ -927,6 +958,36 @@ int spk_model_add_stimulus(spk_model* m, const float* rates, int32_t n, int32_t*
   return guarded([&] {
     int id = pp->add_stimulus(rates, n);
     if (sid) *sid = id;
+    return SPK_OK;
+  });
+}
+
+int spk_model_add_plasticity_rule(spk_model* m, int32_t rule, const spk_stdp_params* p, int32_t* rid) {
+  if (!m || !p) return SPK_ERR_INVALID;
+  if (rule == SPK_STDP_WEIGHT_DEPENDENT) return spk_model_add_stdp_rule(m, p, rid);
+  if (rule != SPK_STDP_EVANS && rule != SPK_STDP_INHIBITORY) return SPK_ERR_INVALID;
+  return guarded([&] {
+    Plasticity* r = nullptr;
+    if (rule == SPK_STDP_EVANS) {
+      // the descriptor's field mapping of SPK_STDP_EVANS, back into the rule's struct
+      auto* ep = new evans_stdp_plasticity_parameters_struct();
+      ep->decay_term_tau_D = p->tau_minus;
+      ep->decay_term_tau_C = p->tau_plus;
+      ep->model_parameter_alpha_D = p->a_minus;
+      ep->synaptic_neurotransmitter_concentration_alpha_C = p->a_plus;
+      m->rule_params.push_back(ep);
+      r = new EvansSTDPPlasticity(m->synapses, &m->neurons, m->inputs, ep);
+    } else {
+      auto* ip = new inhibitory_stdp_plasticity_parameters_struct();
+      ip->tau_istdp = p->tau_plus;
+      ip->learningrate = p->lambda;
+      ip->targetrate = p->alpha;
+      m->rule_params.push_back(ip);
+      r = new InhibitorySTDPPlasticity(m->synapses, &m->neurons, m->inputs, ip);
+    }
+    m->rules.push_back(r);
+    m->model.AddPlasticityRule(r);
+    if (rid) *rid = (int32_t)m->rules.size() - 1;
     return SPK_OK;
   });
 }

@@ -509,10 +509,13 @@ class Model:
               "spk_model_add_stimulus")
         return sid.value
 
-    def add_stdp_rule(self, p: STDPParams) -> int:
+    def add_stdp_rule(self, p: STDPParams, rule: int = N.SPK_STDP_WEIGHT_DEPENDENT) -> int:
+        """A plasticity rule (SPK_STDP_*; parameters in the descriptor's field
+        mapping for the Evans and inhibitory rules)."""
         c = p.to_c()
         rid = C.c_int32()
-        check(lib().spk_model_add_stdp_rule(self.h, C.byref(c), C.byref(rid)), "spk_model_add_stdp_rule")
+        check(lib().spk_model_add_plasticity_rule(self.h, rule, C.byref(c), C.byref(rid)),
+              "spk_model_add_plasticity_rule")
         return rid.value
 
     def add_synapse_group(self, pre: int, post: int, p: SynapseParams) -> int:

@@ -77,3 +77,34 @@ def test_snapshot_carries_the_rule_state():
     S = len(d.arrays["weight"])
     np.testing.assert_array_equal(bits(a.weights(S)), bits(b.weights(S)))
     np.testing.assert_array_equal(bits(a.state(N.SPK_FIELD_V, 300)), bits(b.state(N.SPK_FIELD_V, 300)))
+
+
+@pytest.mark.parametrize("rule,sp", RULES)
+def test_rule_through_the_model_api(rule, sp):
+    """The C++ front end's EvansSTDPPlasticity / InhibitorySTDPPlasticity
+    flatten into the descriptor's rule and field mapping: the reference-built
+    Brunel case with the rule on its excitatory recurrent synapses."""
+    import cases
+    from spike_gb300 import Model
+    from spike_gb300.model import SynapseParams
+    m = Model(N.SPK_SYN_VOLTAGE, N.SPK_INPUT_POISSON, synapse_seed=42, timestep=float(cases.DT))
+    rid = m.add_stdp_rule(sp, rule)
+    args = (0.0, 0.0, 20.0e-3, 2.0e-3, 0.0)
+    gin = m.add_input_group(150, 20.0)
+    ge = m.add_neuron_group(cases._lif(160, *args))
+    gi = m.add_neuron_group(cases._lif(40, *args))
+    J = float(cases.F(0.1) * cases.F(10.0 ** -3))
+    dl = (cases.steps(1), cases.steps(20))
+    m.connect_with_sparsity(gin, ge, 0.1, SynapseParams(weight_range=(0.0, float(cases.F(2.0) * cases.F(J))),
+                                                         delay_range=dl))
+    m.connect_with_sparsity(ge, ge, 0.1, SynapseParams(weight_range=(J, J), delay_range=dl, plasticity_rule=rid))
+    m.connect_with_sparsity(gi, ge, 0.1, SynapseParams(weight_range=(-5 * J, -5 * J), delay_range=dl))
+    m.connect_with_sparsity(ge, gi, 0.1, SynapseParams(weight_range=(J, J), delay_range=dl))
+    d = m.desc()
+    assert d.stdp_rule == rule and d.has_stdp == 1
+    o = OracleNet(d)
+    net = Net.from_desc(d)
+    net.run(0.1)
+    o.run(0.1)
+    assert net.synchronize() == 0
+    assert_same(net, o, 200, 150, 1, weights=True, tag=f"model rule {rule}")
