@@ -96,6 +96,7 @@ typedef struct spk_neuron_group {
 #define SPK_STDP_EVANS 1            /* EvansSTDPPlasticity (Spike/Plasticity/EvansSTDPPlasticity.hpp) */
 #define SPK_STDP_INHIBITORY 2       /* InhibitorySTDPPlasticity (Vogels et al. 2011,
                                        Spike/Plasticity/InhibitorySTDPPlasticity.hpp) */
+#define SPK_STDP_CUSTOM 3           /* CustomSTDPPlasticity (Spike/Plasticity/CustomSTDPPlasticity.hpp) */
 
 /* weightdependent_stdp_plasticity_parameters_struct
  * (Spike/Plasticity/WeightDependentSTDPPlasticity.hpp:28-40).  The other
@@ -105,7 +106,10 @@ typedef struct spk_neuron_group {
  *                        a_plus = synaptic_neurotransmitter_concentration_alpha_C
  *                        (weights clipped to [0, 1]);
  *   SPK_STDP_INHIBITORY  tau_plus = tau_istdp, lambda = learningrate,
- *                        alpha = targetrate (weights clipped at 0). */
+ *                        alpha = targetrate (weights clipped at 0);
+ *   SPK_STDP_CUSTOM      a_minus, a_plus, tau_minus, tau_plus, w_max as named,
+ *                        lambda = learning_rate, alpha = a_star,
+ *                        clip_upper = nearest_spike_only (weights clipped at 0). */
 typedef struct spk_stdp_params {
   float a_minus;
   float a_plus;

@@ -126,6 +126,18 @@ struct inhibitory_stdp_plasticity_parameters_struct : stdp_plasticity_parameters
   float targetrate = 10.0f;
   float momentumrate = 0.0f;
 };
+// custom_stdp_plasticity_parameters_struct (Spike/Plasticity/CustomSTDPPlasticity.hpp);
+// a_star and learning_rate start at 0 here (the reference leaves them unset).
+struct custom_stdp_plasticity_parameters_struct : stdp_plasticity_parameters_struct {
+  float a_minus = 1.0f;
+  float a_plus = 1.0f;
+  float a_star = 0.0f;
+  float tau_minus = 0.02f;
+  float tau_plus = 0.02f;
+  float w_max = 1.0f;
+  float learning_rate = 0.0f;
+  bool nearest_spike_only = false;
+};
 
 // ---- neurons -------------------------------------------------------------------
 class SpikingNeurons {
@@ -285,6 +297,13 @@ class InhibitorySTDPPlasticity : public STDPPlasticity {
   InhibitorySTDPPlasticity(SpikingSynapses* synapses, SpikingNeurons* neurons, SpikingNeurons* input_neurons,
                            stdp_plasticity_parameters_struct* stdp_parameters);
   inhibitory_stdp_plasticity_parameters_struct* stdp_params;
+};
+
+class CustomSTDPPlasticity : public STDPPlasticity {
+ public:
+  CustomSTDPPlasticity(SpikingSynapses* synapses, SpikingNeurons* neurons, SpikingNeurons* input_neurons,
+                       stdp_plasticity_parameters_struct* stdp_parameters);
+  custom_stdp_plasticity_parameters_struct* stdp_params;
 };
 
 // ---- monitors ------------------------------------------------------------------

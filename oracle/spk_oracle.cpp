@@ -68,6 +68,7 @@ struct Net {
   spk_stdp_params stdp{};
   R E_minus = 0, E_plus = 0, inc_minus = 0, inc_plus = 0, invE_minus = 0, invE_plus = 0;
   R vogels_decay = 0;  // expf(-timestep / tau_istdp), computed on the host
+  R custom_post_decay = 0, custom_pre_decay = 0;
   // Spike bits of the last H timesteps per key, for rules that see a
   // presynaptic spike when it arrives (the reference's spike bit-buffers,
   // Spike/Backend/CUDA/Neurons/SpikingNeurons.cu:33-35).
@@ -231,7 +232,17 @@ int Net<R>::init(const spk_net_desc* d) {
   has_stdp = d->has_stdp != 0;
   stdp = d->stdp;
   stdp_rule = d->stdp_rule;
-  if (stdp_rule < SPK_STDP_WEIGHT_DEPENDENT || stdp_rule > SPK_STDP_INHIBITORY) return SPK_ERR_INVALID;
+  if (stdp_rule < SPK_STDP_WEIGHT_DEPENDENT || stdp_rule > SPK_STDP_CUSTOM) return SPK_ERR_INVALID;
+  if (has_stdp && stdp_rule == SPK_STDP_CUSTOM) {
+    // expf(- timestep / tau_minus), expf(- timestep / tau_plus) (CustomSTDPPlasticity.cu:55-56)
+    if (sizeof(R) == 4) {
+      custom_post_decay = (R)expf(-d->dt / stdp.tau_minus);
+      custom_pre_decay = (R)expf(-d->dt / stdp.tau_plus);
+    } else {
+      custom_post_decay = (R)std::exp(-(double)d->dt / (double)stdp.tau_minus);
+      custom_pre_decay = (R)std::exp(-(double)d->dt / (double)stdp.tau_plus);
+    }
+  }
   if (has_stdp && stdp_rule == SPK_STDP_INHIBITORY) {
     // expf(- timestep / tau_istdp) (Spike/Backend/CUDA/Plasticity/InhibitorySTDPPlasticity.cu:61)
     if (sizeof(R) == 4)
@@ -530,7 +541,8 @@ void Net<R>::stdp_range(int64_t a, int64_t b, R t) {
 //   inhibitory: vogels_apply_stdp_to_synapse_weights_kernel
 //     (Spike/Backend/CUDA/Plasticity/InhibitorySTDPPlasticity.cu:71-154),
 //     weights clipped at 0; its constant term is evaluated in double, as the
-//     reference's 2.0 literal makes it.
+//     reference's 2.0 literal makes it;
+//   custom: pre and post memory traces, optionally nearest-spike, weights clipped at 0.
 template <typename R>
 void Net<R>::dense_stdp_range(int64_t a, int64_t b, int T) {
   const int K = nkeys();
@@ -561,6 +573,28 @@ void Net<R>::dense_stdp_range(int64_t a, int64_t b, int T) {
       w = old_w + syn;
       if (w < (R)0) w = (R)0;
       if (w > (R)1) w = (R)1;
+    } else if (stdp_rule == SPK_STDP_CUSTOM) {
+      // ltp_and_ltd (Spike/Backend/CUDA/Plasticity/CustomSTDPPlasticity.cu:67-156):
+      // lambda = learning_rate, alpha = a_star, clip_upper = nearest_spike_only
+      const R a_plus = (R)stdp.a_plus, a_minus = (R)stdp.a_minus, lr = (R)stdp.lambda;
+      const R a_star = (R)stdp.alpha, w_max = (R)stdp.w_max;
+      const bool nearest = stdp.clip_upper != 0;
+      tr_post *= custom_post_decay;
+      tr_pre *= custom_pre_decay;
+      if (pre_sp) {
+        tr_pre += a_plus;
+        if (nearest) tr_pre = a_plus;
+      }
+      if (post_sp) {
+        tr_post += a_minus;
+        if (nearest) tr_post = a_minus;
+      }
+      R syn = 0;
+      const R old_w = w;
+      if (pre_sp) syn -= lr * (old_w / w_max) * tr_post + lr * a_star;
+      if (post_sp) syn += lr * tr_pre;
+      w = old_w + syn;
+      if (w < (R)0) w = (R)0;
     } else {
       const R lr = (R)stdp.lambda;
       tr_pre *= vogels_decay;

@@ -23,6 +23,7 @@ SPK_ERR_OVERFLOW = -6
 SPK_STDP_WEIGHT_DEPENDENT = 0
 SPK_STDP_EVANS = 1
 SPK_STDP_INHIBITORY = 2
+SPK_STDP_CUSTOM = 3
 SPK_ERR_STATE = -7
 SPK_ERR_BUSY = -8
 ERROR_NAMES = {

@@ -495,6 +495,12 @@ InhibitorySTDPPlasticity::InhibitorySTDPPlasticity(SpikingSynapses*, SpikingNeur
   if (!stdp_params) fail(SPK_ERR_INVALID, "inhibitory STDP needs its parameter struct");
 }
 
+CustomSTDPPlasticity::CustomSTDPPlasticity(SpikingSynapses*, SpikingNeurons*, SpikingNeurons*,
+                                           stdp_plasticity_parameters_struct* p) {
+  stdp_params = dynamic_cast<custom_stdp_plasticity_parameters_struct*>(p);
+  if (!stdp_params) fail(SPK_ERR_INVALID, "custom STDP needs its parameter struct");
+}
+
 // ---- monitor ------------------------------------------------------------------------
 void SpikingActivityMonitor::reset_state() {
   neuron_ids_of_stored_spikes_on_host.clear();
@@ -656,6 +662,16 @@ int SpikingModel::build_desc(spk_net_desc* d) {
       d->stdp.lambda = ih->stdp_params->learningrate;
       d->stdp.alpha = ih->stdp_params->targetrate;
       d->stdp.w_max = 1.0f;
+    } else if (auto* cu = dynamic_cast<CustomSTDPPlasticity*>(r)) {
+      d->stdp_rule = SPK_STDP_CUSTOM;
+      d->stdp.a_minus = cu->stdp_params->a_minus;
+      d->stdp.a_plus = cu->stdp_params->a_plus;
+      d->stdp.tau_minus = cu->stdp_params->tau_minus;
+      d->stdp.tau_plus = cu->stdp_params->tau_plus;
+      d->stdp.w_max = cu->stdp_params->w_max;
+      d->stdp.lambda = cu->stdp_params->learning_rate;
+      d->stdp.alpha = cu->stdp_params->a_star;
+      d->stdp.clip_upper = cu->stdp_params->nearest_spike_only ? 1 : 0;
     } else {
       return SPK_ERR_UNSUPPORTED;
     }
@@ -965,7 +981,7 @@ int spk_model_add_stimulus(spk_model* m, const float* rates, int32_t n, int32_t*
 int spk_model_add_plasticity_rule(spk_model* m, int32_t rule, const spk_stdp_params* p, int32_t* rid) {
   if (!m || !p) return SPK_ERR_INVALID;
   if (rule == SPK_STDP_WEIGHT_DEPENDENT) return spk_model_add_stdp_rule(m, p, rid);
-  if (rule != SPK_STDP_EVANS && rule != SPK_STDP_INHIBITORY) return SPK_ERR_INVALID;
+  if (rule != SPK_STDP_EVANS && rule != SPK_STDP_INHIBITORY && rule != SPK_STDP_CUSTOM) return SPK_ERR_INVALID;
   return guarded([&] {
     Plasticity* r = nullptr;
     if (rule == SPK_STDP_EVANS) {
@@ -977,6 +993,18 @@ int spk_model_add_plasticity_rule(spk_model* m, int32_t rule, const spk_stdp_par
       ep->synaptic_neurotransmitter_concentration_alpha_C = p->a_plus;
       m->rule_params.push_back(ep);
       r = new EvansSTDPPlasticity(m->synapses, &m->neurons, m->inputs, ep);
+    } else if (rule == SPK_STDP_CUSTOM) {
+      auto* cp = new custom_stdp_plasticity_parameters_struct();
+      cp->a_minus = p->a_minus;
+      cp->a_plus = p->a_plus;
+      cp->tau_minus = p->tau_minus;
+      cp->tau_plus = p->tau_plus;
+      cp->w_max = p->w_max;
+      cp->learning_rate = p->lambda;
+      cp->a_star = p->alpha;
+      cp->nearest_spike_only = p->clip_upper != 0;
+      m->rule_params.push_back(cp);
+      r = new CustomSTDPPlasticity(m->synapses, &m->neurons, m->inputs, cp);
     } else {
       auto* ip = new inhibitory_stdp_plasticity_parameters_struct();
       ip->tau_istdp = p->tau_plus;

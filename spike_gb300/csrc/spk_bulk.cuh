@@ -862,6 +862,8 @@ __global__ void __launch_bounds__(256) bulk_post_kernel(const NetDev* __restrict
 //   Inhibitory (InhibitorySTDPPlasticity.cu:102-143): Vogels' memory traces;
 //   weights clipped at 0; its constant term in double, as the reference's
 //   2.0 literal evaluates it.
+//   Custom (CustomSTDPPlasticity.cu:100-142): pre and post memory traces,
+//   optionally nearest-spike, weight-scaled depression; weights clipped at 0.
 __global__ void __launch_bounds__(256) bulk_dense_stdp_kernel(const NetDev* __restrict__ nets,
                                                               const BulkPostItem* __restrict__ items, int n_items,
                                                               int s) {
@@ -899,7 +901,7 @@ __global__ void __launch_bounds__(256) bulk_dense_stdp_kernel(const NetDev* __re
         w = old_w + syn;
         if (w < 0.0f) w = 0.0f;
         if (w > 1.0f) w = 1.0f;
-      } else {
+      } else if (d.stdp_rule == SPK_STDP_INHIBITORY) {
         tr.x *= c0;
         tr.y *= c0;
         if (pre_sp) tr.x += 1.0f;
@@ -911,6 +913,25 @@ __global__ void __launch_bounds__(256) bulk_dense_stdp_kernel(const NetDev* __re
         }
         if (post_sp) syn += c1 * (tr.x);
         w += syn;
+        if (w < 0.0f) w = 0.0f;
+      } else {
+        const float a_plus = c2, a_minus = c3, lr = d.rule_c[4], a_star = d.rule_c[5], w_max = d.rule_c[6];
+        const bool nearest = d.rule_c[7] != 0.0f;
+        tr.y *= c0;
+        tr.x *= c1;
+        if (pre_sp) {
+          tr.x += a_plus;
+          if (nearest) tr.x = a_plus;
+        }
+        if (post_sp) {
+          tr.y += a_minus;
+          if (nearest) tr.y = a_minus;
+        }
+        float syn = 0.0f;
+        const float old_w = w;
+        if (pre_sp) syn -= lr * (old_w / w_max) * tr.y + lr * a_star;
+        if (post_sp) syn += lr * tr.x;
+        w = old_w + syn;
         if (w < 0.0f) w = 0.0f;
       }
       d.csc[a].y = __float_as_uint(w);

@@ -110,7 +110,7 @@ struct NetDev {
   const int* csc_delay;       // [n_csc]
   float2* dense_tr;           // [n_csc]: presynaptic, postsynaptic trace
   uint32_t* hist;             // [H][n_words]
-  float rule_c[4];            // the rule's constants
+  float rule_c[8];            // the rule's constants
 };
 
 struct CtaMap {

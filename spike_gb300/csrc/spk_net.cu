@@ -451,7 +451,7 @@ struct ModelSpec {
 };
 
 static int validate_spec(const ModelSpec& m) {
-  if (m.stdp_rule < SPK_STDP_WEIGHT_DEPENDENT || m.stdp_rule > SPK_STDP_INHIBITORY) {
+  if (m.stdp_rule < SPK_STDP_WEIGHT_DEPENDENT || m.stdp_rule > SPK_STDP_CUSTOM) {
     set_error("unknown STDP rule %d", m.stdp_rule);
     return SPK_ERR_INVALID;
   }
@@ -711,7 +711,7 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
       h.rule_c[1] = sp.tau_minus;
       h.rule_c[2] = sp.a_plus;
       h.rule_c[3] = sp.a_minus;
-    } else {
+    } else if (n->stdp_rule == SPK_STDP_INHIBITORY) {
       // trace decay expf(- timestep / tau_istdp), computed on the host as the
       // reference does (InhibitorySTDPPlasticity.cu:61), learningrate,
       // targetrate, tau_istdp
@@ -719,6 +719,18 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
       h.rule_c[1] = sp.lambda;
       h.rule_c[2] = sp.alpha;
       h.rule_c[3] = sp.tau_plus;
+    } else {
+      // post and pre trace decays expf(- timestep / tau_minus / tau_plus),
+      // computed on the host (CustomSTDPPlasticity.cu:55-56), a_plus, a_minus,
+      // learning_rate, a_star, w_max, nearest_spike_only
+      h.rule_c[0] = expf(-m.dt / sp.tau_minus);
+      h.rule_c[1] = expf(-m.dt / sp.tau_plus);
+      h.rule_c[2] = sp.a_plus;
+      h.rule_c[3] = sp.a_minus;
+      h.rule_c[4] = sp.lambda;
+      h.rule_c[5] = sp.alpha;
+      h.rule_c[6] = sp.w_max;
+      h.rule_c[7] = sp.clip_upper ? 1.0f : 0.0f;
     }
   }
   h.rowptr = (const int*)p_rowptr;

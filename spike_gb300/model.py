@@ -511,7 +511,7 @@ class Model:
 
     def add_stdp_rule(self, p: STDPParams, rule: int = N.SPK_STDP_WEIGHT_DEPENDENT) -> int:
         """A plasticity rule (SPK_STDP_*; parameters in the descriptor's field
-        mapping for the Evans and inhibitory rules)."""
+        mapping for the Evans, inhibitory and custom rules)."""
         c = p.to_c()
         rid = C.c_int32()
         check(lib().spk_model_add_plasticity_rule(self.h, rule, C.byref(c), C.byref(rid)),

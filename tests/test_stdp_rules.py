@@ -1,11 +1,13 @@
 """STDP rules with two traces per plastic synapse (GPU): the Evans rule
-(Spike/Backend/CUDA/Plasticity/EvansSTDPPlasticity.cu) and the inhibitory
+(Spike/Backend/CUDA/Plasticity/EvansSTDPPlasticity.cu), the inhibitory
 rule of Vogels et al. 2011 (Spike/Backend/CUDA/Plasticity/
-InhibitorySTDPPlasticity.cu).  Both update every plastic synapse every
-timestep and see a presynaptic spike when it arrives; the engine runs them in
-bulk mode.  Checked against the oracle bit for bit (spikes, state, ring,
-weights), across runs with plasticity off, in a batch beside a network with the
-event-driven rule, and through a snapshot."""
+InhibitorySTDPPlasticity.cu) and the custom rule (Spike/Backend/CUDA/
+Plasticity/CustomSTDPPlasticity.cu), with accumulating and nearest-spike
+traces.  All update every plastic synapse every timestep and see a presynaptic
+spike when it arrives; the engine runs them in bulk mode.  Checked against the
+oracle bit for bit (spikes, state, ring, weights), across runs with plasticity
+off, in a batch beside a network with the event-driven rule, and through a
+snapshot; the front end's descriptor mapping is checked on the CPU."""
 import numpy as np
 import pytest
 
@@ -16,19 +18,121 @@ from spike_gb300 import Batch, Net, schedule
 from spike_gb300 import _native as N
 from spike_gb300.model import STDPParams
 
-pytestmark = pytest.mark.gpu
 
 # Evans: a_plus = alpha_C, a_minus = alpha_D, tau_plus = tau_C, tau_minus = tau_D
 EVANS = STDPParams(a_plus=0.5, a_minus=0.5, tau_plus=0.004, tau_minus=0.005, lambda_=0.0, alpha=0.0, w_max=1.0)
 # inhibitory: tau_plus = tau_istdp, lambda = learningrate, alpha = targetrate
 VOGELS = STDPParams(a_plus=0.0, a_minus=0.0, tau_plus=0.02, tau_minus=0.02, lambda_=0.0004, alpha=10.0, w_max=1.0)
-RULES = [(N.SPK_STDP_EVANS, EVANS), (N.SPK_STDP_INHIBITORY, VOGELS)]
+# custom: lambda = learning_rate, alpha = a_star, clip_upper = nearest_spike_only
+CUSTOM = STDPParams(a_plus=1.0, a_minus=0.8, tau_plus=0.02, tau_minus=0.03, lambda_=1.0e-5, alpha=0.1, w_max=2.0e-3)
+CUSTOM_NEAREST = STDPParams(a_plus=1.0, a_minus=0.8, tau_plus=0.02, tau_minus=0.03, lambda_=2.0e-5, alpha=0.1,
+                            w_max=2.0e-3, clip_upper=True)
+RULES = [(N.SPK_STDP_EVANS, EVANS), (N.SPK_STDP_INHIBITORY, VOGELS), (N.SPK_STDP_CUSTOM, CUSTOM),
+         (N.SPK_STDP_CUSTOM, CUSTOM_NEAREST)]
+gpu = pytest.mark.gpu
+
+
+def host_expf(x):
+    """The C library's expf, with which the reference computes the decays on
+    the host."""
+    import ctypes
+    import ctypes.util
+    libm = ctypes.CDLL(ctypes.util.find_library("m"))
+    libm.expf.restype = ctypes.c_float
+    libm.expf.argtypes = [ctypes.c_float]
+    return np.float32(libm.expf(float(x)))
+
+
+def restated_rule(rule, sp, d, pre_spk, post_spk, steps, n_exc):
+    """The three kernels' per-synapse updates restated over whole arrays of
+    plastic synapses (float32 as the kernels compute, no contraction), driven
+    by the recorded rasters: at timestep T the postsynaptic bit is T and the
+    presynaptic bit is T - delay (EvansSTDPPlasticity.cu:96-131,
+    InhibitorySTDPPlasticity.cu:108-143, CustomSTDPPlasticity.cu:99-142)."""
+    f32, f64 = np.float32, np.float64
+    pre_a, post_a = d.arrays["pre"], d.arrays["post"]
+    plastic = pre_a < n_exc  # inputs and excitatory neurons
+    pre_key = np.where(pre_a >= 0, pre_a, 0)
+    pre_is_input = pre_a < 0
+    in_key = np.where(pre_is_input, -pre_a - 1, 0)
+    delay = d.arrays["delay"]
+    w = d.arrays["weight"].copy()
+    idx = np.nonzero(plastic)[0]
+    wp = w[idx].astype(f32)
+    tp = np.zeros(len(idx), f32)  # presynaptic trace
+    tq = np.zeros(len(idx), f32)  # postsynaptic trace
+    dt = f32(d.desc.dt)
+    one = f32(1)
+    for T in range(steps):
+        pT = T - delay[idx]
+        ok = pT >= 0
+        pTc = np.where(ok, pT, 0)
+        pre = ok & np.where(pre_is_input[idx], pre_spk[1][pTc, in_key[idx]], pre_spk[0][pTc, pre_key[idx]])
+        post = post_spk[T, post_a[idx]]
+        if rule == N.SPK_STDP_EVANS:
+            tp = (one - (dt / f32(sp.tau_plus))) * tp
+            tq = (one - (dt / f32(sp.tau_minus))) * tq
+            tp = np.where(pre, tp + dt * f32(sp.a_plus) * (one - tp), tp)
+            tq = np.where(post, tq + dt * f32(sp.a_minus) * (one - tq), tq)
+            syn = np.zeros_like(wp)
+            syn = np.where(pre, syn - (wp * tq), syn)
+            syn = np.where(post, syn + ((one - wp) * tp), syn)
+            wp = np.clip(wp + syn, f32(0), f32(1))
+        elif rule == N.SPK_STDP_INHIBITORY:
+            decay = host_expf(-dt / f32(sp.tau_plus))
+            tp = tp * decay
+            tq = tq * decay
+            tp = np.where(pre, tp + one, tp)
+            tq = np.where(post, tq + one, tq)
+            lr = f32(sp.lambda_)
+            syn = np.zeros_like(wp)
+            syn = np.where(pre, syn + lr * tq, syn)
+            const = f64(-lr) * (2.0 * f64(f32(sp.alpha)) * f64(f32(sp.tau_plus)))
+            syn = np.where(pre, (syn.astype(f64) + const).astype(f32), syn)
+            syn = np.where(post, syn + lr * tp, syn)
+            wp = np.maximum(wp + syn, f32(0))
+        else:
+            tq = tq * host_expf(-dt / f32(sp.tau_minus))
+            tp = tp * host_expf(-dt / f32(sp.tau_plus))
+            a_plus, a_minus = f32(sp.a_plus), f32(sp.a_minus)
+            tp = np.where(pre, a_plus if sp.clip_upper else tp + a_plus, tp)
+            tq = np.where(post, a_minus if sp.clip_upper else tq + a_minus, tq)
+            lr, a_star, w_max = f32(sp.lambda_), f32(sp.alpha), f32(sp.w_max)
+            syn = np.zeros_like(wp)
+            syn = np.where(pre, syn - (lr * (wp / w_max) * tq + lr * a_star), syn)
+            syn = np.where(post, syn + lr * tp, syn)
+            wp = np.maximum(wp + syn, f32(0))
+    w[idx] = wp
+    return w
+
+
+@pytest.mark.parametrize("rule,sp", RULES)
+def test_oracle_rules_follow_the_reference_kernels(rule, sp):
+    """The oracle's rule restatement against a second one written from the
+    reference's kernels, driven by the oracle's own rasters (CPU)."""
+    n, n_in, steps = 300, 200, 700
+    d = descs.random_voltage_net(n=n, n_in=n_in, plastic=True, stdp=sp, stdp_rule=rule, seed=21)
+    o = OracleNet(d.desc)
+    o.run_steps(steps, True)
+    dt = np.float32(d.desc.dt)
+    rasters = []
+    for pop, count in ((N.SPK_POP_NEURONS, n), (N.SPK_POP_INPUTS, n_in)):
+        ids, times = o.spikes(pop)
+        r = np.zeros((steps, count), bool)
+        r[np.rint(times / dt).astype(np.int64), ids] = True
+        rasters.append(r)
+    assert rasters[0].sum() > 20 and rasters[1].sum() > 100
+    want = restated_rule(rule, sp, d, rasters, rasters[0], steps, int(0.8 * n))
+    got = o.weights()
+    assert (want != d.arrays["weight"]).sum() > 50  # the rule moved weights
+    np.testing.assert_array_equal(bits(got), bits(want))
 
 
 def net_desc(rule, sp, seed=5):
     return descs.random_voltage_net(n=300, n_in=200, plastic=True, stdp=sp, stdp_rule=rule, seed=seed)
 
 
+@gpu
 @pytest.mark.parametrize("rule,sp", RULES)
 def test_rule_matches_oracle(rule, sp):
     d = net_desc(rule, sp)
@@ -44,6 +148,7 @@ def test_rule_matches_oracle(rule, sp):
     assert len(o.spikes()[0]) > 50
 
 
+@gpu
 @pytest.mark.parametrize("rule,sp", RULES)
 def test_rule_in_a_batch_beside_the_event_driven_rule(rule, sp):
     wd = STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02, lambda_=1.0, alpha=1.0, w_max=1.0)
@@ -63,6 +168,7 @@ def test_rule_in_a_batch_beside_the_event_driven_rule(rule, sp):
     b.close()
 
 
+@gpu
 def test_snapshot_carries_the_rule_state():
     d = net_desc(N.SPK_STDP_INHIBITORY, VOGELS)
     a = Net.from_desc(d.desc)
@@ -79,11 +185,9 @@ def test_snapshot_carries_the_rule_state():
     np.testing.assert_array_equal(bits(a.state(N.SPK_FIELD_V, 300)), bits(b.state(N.SPK_FIELD_V, 300)))
 
 
-@pytest.mark.parametrize("rule,sp", RULES)
-def test_rule_through_the_model_api(rule, sp):
-    """The C++ front end's EvansSTDPPlasticity / InhibitorySTDPPlasticity
-    flatten into the descriptor's rule and field mapping: the reference-built
-    Brunel case with the rule on its excitatory recurrent synapses."""
+def brunel_with_rule(rule, sp):
+    """The reference-built Brunel case with the rule on its excitatory
+    recurrent synapses, through the C++ front end."""
     import cases
     from spike_gb300 import Model
     from spike_gb300.model import SynapseParams
@@ -100,8 +204,36 @@ def test_rule_through_the_model_api(rule, sp):
     m.connect_with_sparsity(ge, ge, 0.1, SynapseParams(weight_range=(J, J), delay_range=dl, plasticity_rule=rid))
     m.connect_with_sparsity(gi, ge, 0.1, SynapseParams(weight_range=(-5 * J, -5 * J), delay_range=dl))
     m.connect_with_sparsity(ge, gi, 0.1, SynapseParams(weight_range=(J, J), delay_range=dl))
-    d = m.desc()
+    return m
+
+
+@pytest.mark.parametrize("rule,sp", RULES)
+def test_front_end_maps_the_rule_into_the_descriptor(rule, sp):
+    """EvansSTDPPlasticity / InhibitorySTDPPlasticity / CustomSTDPPlasticity
+    flatten into the descriptor's rule and field mapping and back (CPU)."""
+    m = brunel_with_rule(rule, sp)
+    d = m.desc()  # points into the model's arrays: keep m alive
     assert d.stdp_rule == rule and d.has_stdp == 1
+    st = d.stdp
+    if rule == N.SPK_STDP_EVANS:
+        got = (st.tau_minus, st.tau_plus, st.a_minus, st.a_plus, st.w_max)
+        want = (sp.tau_minus, sp.tau_plus, sp.a_minus, sp.a_plus, 1.0)
+    elif rule == N.SPK_STDP_INHIBITORY:
+        got = (st.tau_plus, st.tau_minus, st.lambda_, st.alpha, st.w_max)
+        want = (sp.tau_plus, sp.tau_plus, sp.lambda_, sp.alpha, 1.0)
+    else:
+        got = (st.a_minus, st.a_plus, st.tau_minus, st.tau_plus, st.w_max, st.lambda_, st.alpha, st.clip_upper)
+        want = (sp.a_minus, sp.a_plus, sp.tau_minus, sp.tau_plus, sp.w_max, sp.lambda_, sp.alpha, int(sp.clip_upper))
+    np.testing.assert_array_equal(np.float32(got), np.float32(want))
+
+
+@gpu
+@pytest.mark.parametrize("rule,sp", RULES)
+def test_rule_through_the_model_api(rule, sp):
+    """The reference-built Brunel case with the rule on its excitatory
+    recurrent synapses: the front end's network matches the oracle."""
+    m = brunel_with_rule(rule, sp)
+    d = m.desc()  # points into the model's arrays: keep m alive
     o = OracleNet(d)
     net = Net.from_desc(d)
     net.run(0.1)
