@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define SPK_ABI_VERSION 1
+#define SPK_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------ */
 #define SPK_OK 0
@@ -97,6 +97,13 @@ typedef struct spk_neuron_group {
 #define SPK_STDP_INHIBITORY 2       /* InhibitorySTDPPlasticity (Vogels et al. 2011,
                                        Spike/Plasticity/InhibitorySTDPPlasticity.hpp) */
 #define SPK_STDP_CUSTOM 3           /* CustomSTDPPlasticity (Spike/Plasticity/CustomSTDPPlasticity.hpp) */
+
+/* Position of the weight normalisation among the model's plasticity rules
+ * (SpikingModel::perform_per_step_model_instructions runs them in the order
+ * added, Spike/Models/SpikingModel.cpp:202-205). */
+#define SPK_NORM_OFF 0
+#define SPK_NORM_AFTER_RULE 1       /* added after the STDP rule (normalises this step's updates) */
+#define SPK_NORM_BEFORE_RULE 2      /* added before it */
 
 /* weightdependent_stdp_plasticity_parameters_struct
  * (Spike/Plasticity/WeightDependentSTDPPlasticity.hpp:28-40).  The other
@@ -163,6 +170,14 @@ typedef struct spk_net_desc {
   int64_t spike_capacity;     /* device spike store entries; 0 = default */
   int32_t record_inputs;      /* also record input spikes */
   int32_t stdp_rule;          /* SPK_STDP_*; 0 = weight-dependent */
+  /* Weight normalisation over the plastic synapses (WeightNormSTDPPlasticity,
+   * Spike/Plasticity/WeightNormSTDPPlasticity.cpp): SPK_NORM_*.  Needs an
+   * STDP rule on the same synapses; runs when plasticity is on. */
+  int32_t weight_norm;
+  const float* norm_initial;  /* per synapse, creation order: the rule's initial_weights
+                                 (NULL: the weights) */
+  const float* norm_sum;      /* per neuron: sum_squared_afferent_values (NULL: the sum of
+                                 powf(w, 2) over its plastic afferents in creation order) */
 } spk_net_desc;
 
 /* Launch schedule.  Zero fields are chosen by the library (planner for a

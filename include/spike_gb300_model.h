@@ -68,6 +68,8 @@ typedef struct spk_synapse_params {
   const float* pairwise_connect_weight; /* n_pairwise values or NULL */
   const float* pairwise_connect_delay;  /* n_pairwise values (s) or NULL */
   int32_t plasticity_rule;              /* rule id from spk_model_add_stdp_rule, or -1 */
+  int32_t plasticity_rule_2;            /* a second rule on the same synapses (the weight
+                                           normalisation), or -1 */
 } spk_synapse_params;
 
 typedef struct spk_model spk_model;
@@ -86,6 +88,11 @@ int spk_model_add_stdp_rule(spk_model* m, const spk_stdp_params* p, int32_t* rul
 /* Any of the SPK_STDP_* rules, its parameters in the descriptor's field
  * mapping (spike_gb300.h); one rule per model. */
 int spk_model_add_plasticity_rule(spk_model* m, int32_t rule, const spk_stdp_params* p, int32_t* rule_id);
+/* WeightNormSTDPPlasticity (Spike/Plasticity/WeightNormSTDPPlasticity.hpp):
+ * weightnorm_stdp_plasticity_parameters_struct's settarget and target.  Its
+ * synapses must be the STDP rule's; its position among the rules is the
+ * order the rules were added in. */
+int spk_model_add_weight_norm_rule(spk_model* m, int32_t settarget, float target, int32_t* rule_id);
 int spk_model_add_synapse_group(spk_model* m, int32_t pre_group, int32_t post_group,
                                 const spk_synapse_params* p, int32_t* group_id);
 /* Examples/UtilityFunctions.hpp:51-82 connect_with_sparsity: fixed in-degree

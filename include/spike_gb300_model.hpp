@@ -126,6 +126,12 @@ struct inhibitory_stdp_plasticity_parameters_struct : stdp_plasticity_parameters
   float targetrate = 10.0f;
   float momentumrate = 0.0f;
 };
+// weightnorm_stdp_plasticity_parameters_struct
+// (Spike/Plasticity/WeightNormSTDPPlasticity.hpp:41-46).
+struct weightnorm_stdp_plasticity_parameters_struct : stdp_plasticity_parameters_struct {
+  bool settarget = false;
+  float target = 0.0f;
+};
 // custom_stdp_plasticity_parameters_struct (Spike/Plasticity/CustomSTDPPlasticity.hpp);
 // a_star and learning_rate start at 0 here (the reference leaves them unset).
 struct custom_stdp_plasticity_parameters_struct : stdp_plasticity_parameters_struct {
@@ -306,6 +312,17 @@ class CustomSTDPPlasticity : public STDPPlasticity {
   custom_stdp_plasticity_parameters_struct* stdp_params;
 };
 
+// Per-post L2 normalisation of the plastic weights every timestep
+// (Spike/Plasticity/WeightNormSTDPPlasticity.hpp).  Supported on the synapses
+// of the model's STDP rule; it runs before or after that rule in the order
+// the two were added.
+class WeightNormSTDPPlasticity : public STDPPlasticity {
+ public:
+  WeightNormSTDPPlasticity(SpikingSynapses* synapses, SpikingNeurons* neurons, SpikingNeurons* input_neurons,
+                           stdp_plasticity_parameters_struct* parameters);
+  weightnorm_stdp_plasticity_parameters_struct* plasticity_parameters;
+};
+
 // ---- monitors ------------------------------------------------------------------
 class SpikingActivityMonitor {
  public:
@@ -379,4 +396,5 @@ class SpikingModel {
   std::vector<spk_neuron_group> groups_;
   std::vector<float> label_tau_, label_vhat_, rates_;
   std::vector<float> empty_f_;
+  std::vector<float> norm_initial_, norm_sum_;  // the weight normalisation's host arrays
 };

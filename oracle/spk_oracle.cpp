@@ -69,6 +69,12 @@ struct Net {
   R E_minus = 0, E_plus = 0, inc_minus = 0, inc_plus = 0, invE_minus = 0, invE_plus = 0;
   R vogels_decay = 0;  // expf(-timestep / tau_istdp), computed on the host
   R custom_post_decay = 0, custom_pre_decay = 0;
+  // Weight normalisation (WeightNormSTDPPlasticity): per post, its plastic
+  // afferents in creation order (sorted positions), their initial weights and
+  // the post's sum of squares.
+  int weight_norm = SPK_NORM_OFF;
+  std::vector<int64_t> norm_ptr, norm_pos;
+  std::vector<R> norm_w0, norm_S;
   // Spike bits of the last H timesteps per key, for rules that see a
   // presynaptic spike when it arrives (the reference's spike bit-buffers,
   // Spike/Backend/CUDA/Neurons/SpikingNeurons.cu:33-35).
@@ -108,6 +114,7 @@ struct Net {
   void poisson_range(int a, int b, R t, int T);
   void stdp_range(int64_t a, int64_t b, R t);
   void dense_stdp_range(int64_t a, int64_t b, int T);
+  void normalise_weights();
   void propagate_thread(int th, int T);
 };
 
@@ -251,6 +258,42 @@ int Net<R>::init(const spk_net_desc* d) {
       vogels_decay = (R)std::exp(-(double)d->dt / (double)stdp.tau_plus);
   }
   H = Dmax + 1;
+  weight_norm = d->weight_norm;
+  if (weight_norm < SPK_NORM_OFF || weight_norm > SPK_NORM_BEFORE_RULE) return SPK_ERR_INVALID;
+  if (weight_norm != SPK_NORM_OFF && !has_stdp) return SPK_ERR_INVALID;
+  norm_ptr.clear();
+  norm_pos.clear();
+  norm_w0.clear();
+  norm_S.clear();
+  if (weight_norm != SPK_NORM_OFF) {
+    // WeightNormSTDPPlasticity::prepare_backend_early
+    // (Spike/Plasticity/WeightNormSTDPPlasticity.cpp:31-70): the sum of
+    // pow(w, 2.0f) over each post's plastic afferents in the rule's order,
+    // and the initial weights.
+    norm_ptr.assign((size_t)N + 1, 0);
+    for (int64_t s = 0; s < S; ++s)
+      if (d->plastic && d->plastic[s]) norm_ptr[(size_t)d->post[s] + 1]++;
+    for (int q = 0; q < N; ++q) norm_ptr[q + 1] += norm_ptr[q];
+    norm_pos.resize(norm_ptr[N]);
+    norm_w0.resize(norm_ptr[N]);
+    norm_S.assign(N, (R)0);
+    std::vector<int64_t> fill(norm_ptr.begin(), norm_ptr.end() - 1);
+    for (int64_t s = 0; s < S; ++s) {
+      if (!(d->plastic && d->plastic[s])) continue;
+      const int q = d->post[s];
+      const int64_t j = fill[q]++;
+      norm_pos[j] = revsort[s];
+      norm_w0[j] = (R)(d->norm_initial ? d->norm_initial[s] : d->weight[s]);
+      if (!d->norm_sum) {
+        if (sizeof(R) == 4)
+          norm_S[q] = (R)((float)norm_S[q] + powf(d->weight[s], 2.0f));
+        else
+          norm_S[q] += (R)((double)d->weight[s] * (double)d->weight[s]);
+      }
+    }
+    if (d->norm_sum)
+      for (int q = 0; q < N; ++q) norm_S[q] = (R)d->norm_sum[q];
+  }
   plastic_idx.clear();
   if (has_stdp)
     for (int64_t s = 0; s < S; ++s)
@@ -387,6 +430,7 @@ void Net<R>::set_threads(int t) {
     sscale.swap(ts);
     for (int64_t s = 0; s < S; ++s) revsort[s] = perm[revsort[s]];
     for (auto& pi : plastic_idx) pi = perm[pi];
+    for (auto& pi : norm_pos) pi = perm[pi];
     // plastic_idx order only matters for the per-synapse trace arrays, which
     // were all reset together: keep them aligned.
   } else {
@@ -543,6 +587,29 @@ void Net<R>::stdp_range(int64_t a, int64_t b, R t) {
 //     weights clipped at 0; its constant term is evaluated in double, as the
 //     reference's 2.0 literal makes it;
 //   custom: pre and post memory traces, optionally nearest-spike, weights clipped at 0.
+// WeightNormSTDPPlasticity::weight_normalization
+// (Spike/Backend/CUDA/Plasticity/WeightNormSTDPPlasticity.cu:74-176): per post,
+// the change of its afferents' sum of squares against their initial weights,
+// (w - w0)^2 + 2 w0 (w - w0) over the afferents whose weight moved, summed in
+// creation order (the reference adds them with atomicAdd, in no fixed order);
+// divisor sqrt(S + change) / sqrt(S); the weights divided when it is not 1.
+template <typename R>
+void Net<R>::normalise_weights() {
+  for (int q = 0; q < N; ++q) {
+    const int64_t a0 = norm_ptr[q], a1 = norm_ptr[q + 1];
+    if (a0 == a1) continue;  // not in the rule's set
+    R upd = 0;
+    for (int64_t j = a0; j < a1; ++j) {
+      const R w0 = norm_w0[j];
+      const R dw = sw[norm_pos[j]] - w0;
+      if (dw != (R)0) upd += dw * dw + (R)2 * w0 * dw;
+    }
+    const R div = std::sqrt(norm_S[q] + upd) / std::sqrt(norm_S[q]);
+    if (div != (R)1)
+      for (int64_t j = a0; j < a1; ++j) sw[norm_pos[j]] = sw[norm_pos[j]] / div;
+  }
+}
+
 template <typename R>
 void Net<R>::dense_stdp_range(int64_t a, int64_t b, int T) {
   const int K = nkeys();
@@ -668,6 +735,9 @@ void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
   };
   const bool do_stdp = plastic && has_stdp && !plastic_idx.empty() && stdp_rule == SPK_STDP_WEIGHT_DEPENDENT;
   const bool do_dense = plastic && has_stdp && !plastic_idx.empty() && stdp_rule != SPK_STDP_WEIGHT_DEPENDENT;
+  // the rules in the order added (Spike/Models/SpikingModel.cpp:202-205)
+  const bool norm_before = plastic && weight_norm == SPK_NORM_BEFORE_RULE;
+  const bool norm_after = plastic && weight_norm == SPK_NORM_AFTER_RULE;
   if (threads <= 1) {
     for (int64_t s = 0; s < n_steps; ++s) {
       R t;
@@ -676,8 +746,10 @@ void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
       std::fill(spiked.begin(), spiked.end(), 0);
       lif_range(0, N, t, T);
       poisson_range(0, Nin, t, T);
+      if (norm_before) normalise_weights();
       if (do_stdp) stdp_range(0, (int64_t)plastic_idx.size(), t);
       if (do_dense) dense_stdp_range(0, (int64_t)plastic_idx.size(), T);
+      if (norm_after) normalise_weights();
       finish_step(t, T);
       propagate_thread(0, T);
       record(t);
@@ -697,8 +769,16 @@ void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
       lif_range(n0[th], n1[th], t_cur, T_cur);
       poisson_range(i0[th], i1[th], t_cur, T_cur);
       bar.arrive_and_wait();
+      if (norm_before) {
+        if (th == 0) normalise_weights();
+        bar.arrive_and_wait();
+      }
       if (do_stdp) stdp_range(p0[th], p1[th], t_cur);
       if (do_dense) dense_stdp_range(p0[th], p1[th], T_cur);
+      if (norm_after) {
+        bar.arrive_and_wait();
+        if (th == 0) normalise_weights();
+      }
       // finish_step writes history slot T, which no range reads this step
       // (delays are 1..H-1)
       if (th == 0) finish_step(t_cur, T_cur);

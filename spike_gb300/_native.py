@@ -12,7 +12,7 @@ import os
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libspike_gb300.so")
 
-SPK_ABI_VERSION = 1
+SPK_ABI_VERSION = 2
 SPK_OK = 0
 SPK_ERR_INVALID = -1
 SPK_ERR_CUDA = -2
@@ -24,6 +24,9 @@ SPK_STDP_WEIGHT_DEPENDENT = 0
 SPK_STDP_EVANS = 1
 SPK_STDP_INHIBITORY = 2
 SPK_STDP_CUSTOM = 3
+SPK_NORM_OFF = 0
+SPK_NORM_AFTER_RULE = 1
+SPK_NORM_BEFORE_RULE = 2
 SPK_ERR_STATE = -7
 SPK_ERR_BUSY = -8
 ERROR_NAMES = {
@@ -79,6 +82,7 @@ class NetDesc(C.Structure):
         ("scale", P(f32)), ("delay", P(i32)), ("label", P(i32)), ("plastic", P(C.c_uint8)),
         ("has_stdp", i32), ("stdp", StdpParams),
         ("seed", u64), ("spike_capacity", i64), ("record_inputs", i32), ("stdp_rule", i32),
+        ("weight_norm", i32), ("norm_initial", P(f32)), ("norm_sum", P(f32)),
     ]
 
 
@@ -143,7 +147,7 @@ class SynapseParams(C.Structure):
                 ("gaussian_synapses_standard_deviation", f32), ("n_pairwise", i32),
                 ("pairwise_connect_presynaptic", P(i32)), ("pairwise_connect_postsynaptic", P(i32)),
                 ("pairwise_connect_weight", P(f32)), ("pairwise_connect_delay", P(f32)),
-                ("plasticity_rule", i32)]
+                ("plasticity_rule", i32), ("plasticity_rule_2", i32)]
 
 
 class DeviceNet(C.Structure):
@@ -236,6 +240,7 @@ _SIGS = {
     "spk_model_add_stimulus": (i32, [_VP, P(f32), i32, P(i32)]),
     "spk_model_add_stdp_rule": (i32, [_VP, P(StdpParams), P(i32)]),
     "spk_model_add_plasticity_rule": (i32, [_VP, i32, P(StdpParams), P(i32)]),
+    "spk_model_add_weight_norm_rule": (i32, [_VP, i32, f32, P(i32)]),
     "spk_model_add_synapse_group": (i32, [_VP, i32, i32, P(SynapseParams), P(i32)]),
     "spk_model_connect_with_sparsity": (i32, [_VP, i32, i32, f32, P(SynapseParams), P(i32)]),
     "spk_model_set_recording": (i32, [_VP, i32, i64]),

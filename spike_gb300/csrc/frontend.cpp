@@ -495,6 +495,12 @@ InhibitorySTDPPlasticity::InhibitorySTDPPlasticity(SpikingSynapses*, SpikingNeur
   if (!stdp_params) fail(SPK_ERR_INVALID, "inhibitory STDP needs its parameter struct");
 }
 
+WeightNormSTDPPlasticity::WeightNormSTDPPlasticity(SpikingSynapses*, SpikingNeurons*, SpikingNeurons*,
+                                                   stdp_plasticity_parameters_struct* p) {
+  plasticity_parameters = dynamic_cast<weightnorm_stdp_plasticity_parameters_struct*>(p);
+  if (!plasticity_parameters) fail(SPK_ERR_INVALID, "weight normalisation needs its parameter struct");
+}
+
 CustomSTDPPlasticity::CustomSTDPPlasticity(SpikingSynapses*, SpikingNeurons*, SpikingNeurons*,
                                            stdp_plasticity_parameters_struct* p) {
   stdp_params = dynamic_cast<custom_stdp_plasticity_parameters_struct*>(p);
@@ -641,9 +647,17 @@ int SpikingModel::build_desc(spk_net_desc* d) {
   std::fill(s->plastic.begin(), s->plastic.end(), 0);
   int n_rules = 0;
   const weightdependent_stdp_plasticity_parameters_struct* wp = nullptr;
+  const WeightNormSTDPPlasticity* norm = nullptr;
+  bool norm_first = false;
   d->stdp_rule = SPK_STDP_WEIGHT_DEPENDENT;
   std::memset(&d->stdp, 0, sizeof(d->stdp));
   for (Plasticity* r : plasticity_rule_vec) {
+    if (auto* wn = dynamic_cast<WeightNormSTDPPlasticity*>(r)) {
+      if (norm) return SPK_ERR_UNSUPPORTED;  // one normalisation per model
+      norm = wn;
+      norm_first = n_rules == 0;
+      continue;
+    }
     ++n_rules;
     if (auto* wd = dynamic_cast<WeightDependentSTDPPlasticity*>(r)) {
       wp = wd->stdp_params;
@@ -689,6 +703,42 @@ int SpikingModel::build_desc(spk_net_desc* d) {
     d->stdp.alpha = wp->alpha;
     d->stdp.w_max = wp->w_max;
     d->stdp.clip_upper = wp->clip_upper ? 1 : 0;
+  }
+  d->weight_norm = SPK_NORM_OFF;
+  d->norm_initial = nullptr;
+  d->norm_sum = nullptr;
+  if (norm) {
+    // Supported on the STDP rule's own synapses.
+    if (n_rules != 1) return SPK_ERR_UNSUPPORTED;
+    std::vector<uint8_t> in_norm(s->plastic.size(), 0);
+    for (int idx : norm->plastic_synapses) in_norm[idx] = 1;
+    if (in_norm != s->plastic) return SPK_ERR_UNSUPPORTED;
+    d->weight_norm = norm_first ? SPK_NORM_BEFORE_RULE : SPK_NORM_AFTER_RULE;
+    const weightnorm_stdp_plasticity_parameters_struct* np = norm->plasticity_parameters;
+    if (np->settarget) {
+      // WeightNormSTDPPlasticity::prepare_backend_early
+      // (Spike/Plasticity/WeightNormSTDPPlasticity.cpp:31-70) with a target:
+      // the host weights are rescaled to w / sqrt(S) * target and S := target,
+      // after the synapses' backend has copied the unscaled weights to the
+      // device (SpikingModel::init_backend prepares the synapses first,
+      // Spike/Models/SpikingModel.cpp:148-153); reset_state then takes the
+      // rescaled host weights as the initial weights
+      // (Spike/Plasticity/WeightNormSTDPPlasticity.cpp:23-29).  So the run
+      // starts from the unscaled weights, measured against the rescaled ones.
+      const int N = d->n_neurons;
+      std::vector<float> sum(N, 0.0f);
+      for (int idx : norm->plastic_synapses) sum[s->postsynaptic_neuron_indices[idx]] += powf(s->synaptic_efficacies_or_weights[idx], 2.0f);
+      norm_initial_ = s->synaptic_efficacies_or_weights;
+      for (int idx : norm->plastic_synapses) {
+        float w = s->synaptic_efficacies_or_weights[idx];
+        w /= sqrtf(sum[s->postsynaptic_neuron_indices[idx]]);
+        w *= np->target;
+        norm_initial_[idx] = w;
+      }
+      norm_sum_.assign(N, np->target);
+      d->norm_initial = norm_initial_.data();
+      d->norm_sum = norm_sum_.data();
+    }
   }
   d->seed = philox_seed;
   d->spike_capacity = spike_capacity;
@@ -834,9 +884,10 @@ void fill_synapse_params(const spk_synapse_params* p, spiking_synapse_parameters
       s->pairwise_connect_delay.assign(p->pairwise_connect_delay,
                                        p->pairwise_connect_delay + p->n_pairwise);
   }
-  if (p->plasticity_rule >= 0) {
-    if (p->plasticity_rule >= (int)m->rules.size()) fail(SPK_ERR_INVALID, "unknown plasticity rule");
-    s->plasticity_vec.push_back(m->rules[p->plasticity_rule]);
+  for (int rid : {p->plasticity_rule, p->plasticity_rule_2}) {
+    if (rid < 0) continue;
+    if (rid >= (int)m->rules.size()) fail(SPK_ERR_INVALID, "unknown plasticity rule");
+    s->plasticity_vec.push_back(m->rules[rid]);
   }
 }
 
@@ -1013,6 +1064,21 @@ int spk_model_add_plasticity_rule(spk_model* m, int32_t rule, const spk_stdp_par
       m->rule_params.push_back(ip);
       r = new InhibitorySTDPPlasticity(m->synapses, &m->neurons, m->inputs, ip);
     }
+    m->rules.push_back(r);
+    m->model.AddPlasticityRule(r);
+    if (rid) *rid = (int32_t)m->rules.size() - 1;
+    return SPK_OK;
+  });
+}
+
+int spk_model_add_weight_norm_rule(spk_model* m, int32_t settarget, float target, int32_t* rid) {
+  if (!m) return SPK_ERR_INVALID;
+  return guarded([&] {
+    auto* np = new weightnorm_stdp_plasticity_parameters_struct();
+    np->settarget = settarget != 0;
+    np->target = target;
+    m->rule_params.push_back(np);
+    Plasticity* r = new WeightNormSTDPPlasticity(m->synapses, &m->neurons, m->inputs, np);
     m->rules.push_back(r);
     m->model.AddPlasticityRule(r);
     if (rid) *rid = (int32_t)m->rules.size() - 1;

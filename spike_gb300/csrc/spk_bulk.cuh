@@ -20,12 +20,17 @@
 //                        with the STDP pre pass;
 //   bulk_post_kernel     the post-spike afferent pass of every spiking post of
 //                        every network, a warp per spiking post taken from a
-//                        shared list (the list kernel builds the items).
+//                        shared list (the list kernel builds the items);
+//   bulk_dense_stdp_kernel, bulk_norm_kernel
+//                        a warp per post of the networks with a
+//                        per-synapse-trace STDP rule or the weight
+//                        normalisation (these run in bulk mode only).
 //
 // Each ring cell still has one writer applying contributions in canonical
 // order, and every float operation is the persistent kernel's, so a network
-// gives the same bits in both modes.  A block of K timesteps is 4K launches
-// plus one that advances the networks' run counters, captured in a CUDA graph.
+// gives the same bits in both modes.  A block of K timesteps is 3 to 8
+// launches per timestep plus one that advances the networks' run counters,
+// captured in a CUDA graph.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -512,7 +517,7 @@ __host__ __device__ inline BulkPropLayout bulk_prop_layout(int win_words, int ts
 
 __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
     bulk_prop_kernel(const NetDev* __restrict__ nets, const BulkPropBlock* __restrict__ blocks, int s, int win_words,
-                     int ts_max) {
+                     int ts_max, int pass) {
   extern __shared__ __align__(16) uint32_t bsm[];
   __shared__ __align__(16) NetDev sd;
   __shared__ RunCtl sctl;
@@ -529,9 +534,24 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
   if (threadIdx.x == 0) s_nlist = *pb.n_list;
   __syncthreads();
   const NetDev& d = sd;
-  const BulkStep st = bulk_step(d, sctl, s);
+  BulkStep st = bulk_step(d, sctl, s);
   const int n_list = s_nlist;
   if (!st.live || n_list == 0) return;  // the whole CTA
+  // A network that normalises its weights after the event-driven rule's
+  // updates takes two passes: the first (pass 1) only updates weights, the
+  // second (pass 2, after the normalisation) only delivers.  Pass 0 does both;
+  // pass 2 skips the other networks.
+  uint32_t kmask = 0xffffffffu;
+  if (pass != 0 && d.weight_norm == SPK_NORM_AFTER_RULE && d.has_stdp && d.stdp_rule == SPK_STDP_WEIGHT_DEPENDENT) {
+    if (pass == 1) {
+      kmask = ~(1u << 31);
+    } else {
+      kmask = ~(1u << 30);
+      st.stdp_run = false;
+    }
+  } else if (pass == 2) {
+    return;
+  }
   const BulkPropLayout wl = bulk_prop_layout(win_words, ts_max);
   uint32_t* list_s = bsm + wl.list;
   int* rp_s = (int*)(bsm + wl.rp);
@@ -573,7 +593,7 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
     }
     for (int j = threadIdx.x; j < nk; j += nthr) {
       const uint32_t lv = list_s[lb + j];
-      kfl_s[buf * BULK_STAGE_KEYS + j] = lv;
+      kfl_s[buf * BULK_STAGE_KEYS + j] = lv & kmask;
       if (st.stdp_run) cp_async4(kpre_s + buf * BULK_STAGE_KEYS + j, pub + (lv & 0x3fffffffu));
     }
   };
@@ -937,6 +957,63 @@ __global__ void __launch_bounds__(256) bulk_dense_stdp_kernel(const NetDev* __re
       d.csc[a].y = __float_as_uint(w);
       d.dense_tr[a] = tr;
     }
+  }
+}
+
+// ---- timestep part 3c: weight normalisation -----------------------------------------------
+// WeightNormSTDPPlasticity::weight_normalization (WeightNormSTDPPlasticity.cu:
+// 74-176), in one warp per post: the change of the post's sum of squared
+// plastic weights against their initial weights, (w - w0)^2 + 2 w0 (w - w0)
+// over the afferents whose weight moved, added in record (creation) order
+// (the reference's atomicAdd gives no fixed order), the divisor
+// sqrtf(S + change) / sqrtf(S), and the weights divided when it is not 1.
+// `slot` picks the networks whose normalisation runs at this point of the
+// timestep (0 before the rule, 1 after the per-synapse-trace pass, 2 after the
+// event-driven rule's weight-update pass).
+__device__ __forceinline__ int norm_slot_of(const NetDev& d) {
+  if (d.weight_norm == SPK_NORM_BEFORE_RULE) return 0;
+  return d.stdp_rule == SPK_STDP_WEIGHT_DEPENDENT ? 2 : 1;
+}
+
+__global__ void __launch_bounds__(256) bulk_norm_kernel(const NetDev* __restrict__ nets,
+                                                        const BulkPostItem* __restrict__ items, int n_items, int s,
+                                                        int slot) {
+  const int lane = threadIdx.x & 31;
+  const int n_warps = gridDim.x * (blockDim.x >> 5);
+  for (int it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < n_items; it += n_warps) {
+    const BulkPostItem item = items[it];
+    const NetDev& d = nets[item.net];
+    if (d.weight_norm == SPK_NORM_OFF || !d.has_stdp || norm_slot_of(d) != slot) continue;
+    const RunCtl c = load_ctl(d.ctl);
+    const BulkStep st = bulk_step(d, c, s);
+    if (!st.live || !c.plastic) continue;
+    const int a0 = __ldg(d.csc_ptr + item.post), a1 = __ldg(d.csc_ptr + item.post + 1);
+    if (a0 == a1) continue;  // not in the rule's set
+    float upd = 0.0f;
+    for (int a = a0; a < a1; a += 32) {
+      const int ai = a + lane;
+      float term = 0.0f;
+      bool moved = false;
+      if (ai < a1) {
+        const float w0 = d.norm_w0[ai];
+        const float dw = __uint_as_float(d.csc[ai].y) - w0;
+        if (dw != 0.0f) {
+          term = dw * dw + 2.0f * w0 * dw;
+          moved = true;
+        }
+      }
+      // every lane adds the terms in lane order, so all hold the same sum
+      unsigned m = __ballot_sync(FULL, moved);
+      while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        upd += __shfl_sync(FULL, term, src);
+      }
+    }
+    const float sum = d.norm_sum[item.post];
+    const float div = sqrtf(sum + upd) / sqrtf(sum);
+    if (div != 1.0f)
+      for (int a = a0 + lane; a < a1; a += 32) d.csc[a].y = __float_as_uint(__uint_as_float(d.csc[a].y) / div);
   }
 }
 

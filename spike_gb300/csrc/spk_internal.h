@@ -102,7 +102,7 @@ struct NetDev {
   // rate monitor: spikes of each key since the last clear, or null
   int* rate_counts;           // [n_keys]
   // Rules with two traces per plastic synapse (SPK_STDP_EVANS,
-  // SPK_STDP_INHIBITORY; bulk mode only): the records' delays, the traces,
+  // SPK_STDP_INHIBITORY, SPK_STDP_CUSTOM; bulk mode only): the records' delays, the traces,
   // and the spike words of the last H timesteps (slot T % H), in which a
   // presynaptic spike is looked up delay steps back.
   int stdp_rule;              // SPK_STDP_*
@@ -111,6 +111,11 @@ struct NetDev {
   float2* dense_tr;           // [n_csc]: presynaptic, postsynaptic trace
   uint32_t* hist;             // [H][n_words]
   float rule_c[8];            // the rule's constants
+  // Weight normalisation of the plastic afferents (SPK_NORM_*; bulk mode
+  // only): each record's initial weight and each post's sum of squares.
+  int weight_norm;
+  const float* norm_w0;       // [n_csc]
+  const float* norm_sum;      // [N]
 };
 
 struct CtaMap {

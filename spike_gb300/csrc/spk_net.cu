@@ -218,6 +218,18 @@ struct spk_net {
   int stdp_rule = SPK_STDP_WEIGHT_DEPENDENT;
   spk_batch* self_batch = nullptr;  // runs of a network with a per-synapse-trace rule (bulk mode)
   bool dense() const { return has_stdp && stdp_rule != SPK_STDP_WEIGHT_DEPENDENT; }
+  int weight_norm = SPK_NORM_OFF;   // SPK_NORM_* (with an STDP rule only)
+  std::vector<float> norm_w0_h;     // per plastic record: initial weight
+  std::vector<float> norm_sum_h;    // per post: sum of squares
+  // Runs in bulk mode only: a per-synapse-trace rule or the weight normalisation.
+  bool bulk_only() const { return dense() || weight_norm != SPK_NORM_OFF; }
+  // The normalisation's place in a bulk timestep: 0 before the rule, 1 after
+  // the per-synapse-trace pass, 2 after the event-driven rule's updates (a
+  // first propagation pass that only updates weights, and the afferent pass).
+  int norm_slot() const {
+    if (weight_norm == SPK_NORM_BEFORE_RULE) return 0;
+    return dense() ? 1 : 2;
+  }
   int64_t n_csc = 0;       // plastic afferent records
   float step_cost = 0.0f;  // measured or estimated time of one step alone (batch packing)
 };
@@ -246,8 +258,11 @@ struct spk_batch {
   BulkBlock* dblocks = nullptr;  // [blocks_total] blocks of 32-key words with real keys
   int blocks_total = 0;
   BulkPostItem* items = nullptr; // afferent-pass work list of a timestep
-  BulkPostItem* dense_items = nullptr;  // posts of the per-synapse-trace-rule networks
+  BulkPostItem* dense_items = nullptr;  // posts of the per-synapse-trace-rule and normalised networks
   int n_dense_items = 0;
+  bool any_dense = false;       // a network with a per-synapse-trace rule
+  int norm_slots = 0;           // bit k: a network normalises its weights in slot k (spk_net::norm_slot)
+  int step_launches = 0;        // kernels of one bulk timestep
   int* item_count = nullptr;
   int item_cap = 0;
   bool any_plastic = false;
@@ -363,8 +378,8 @@ static int run_steps_impl(spk_net* n, int64_t steps, int plastic, float start) {
     set_error("run of %lld steps exceeds the 2^31-1 step limit of one run", (long long)steps);
     return SPK_ERR_INVALID;
   }
-  if (n->dense()) {
-    // Per-synapse-trace STDP runs in bulk mode: a batch of this one network
+  if (n->bulk_only()) {
+    // Per-synapse-trace STDP and the weight normalisation run in bulk mode: a batch of this one network
     // (the caller sets the network's time afterwards, as for any run).
     if (!n->self_batch) {
       const spk_schedule bs{0, 0, 0, n->plan.K};
@@ -445,6 +460,9 @@ struct ModelSpec {
   int has_stdp = 0;
   spk_stdp_params stdp{};
   int stdp_rule = SPK_STDP_WEIGHT_DEPENDENT;
+  int weight_norm = SPK_NORM_OFF;
+  const float* norm_initial = nullptr;
+  const float* norm_sum = nullptr;
   uint64_t seed = 0;
   int64_t spike_capacity = 0;
   int record_inputs = 0;
@@ -453,6 +471,14 @@ struct ModelSpec {
 static int validate_spec(const ModelSpec& m) {
   if (m.stdp_rule < SPK_STDP_WEIGHT_DEPENDENT || m.stdp_rule > SPK_STDP_CUSTOM) {
     set_error("unknown STDP rule %d", m.stdp_rule);
+    return SPK_ERR_INVALID;
+  }
+  if (m.weight_norm < SPK_NORM_OFF || m.weight_norm > SPK_NORM_BEFORE_RULE) {
+    set_error("unknown weight normalisation mode %d", m.weight_norm);
+    return SPK_ERR_INVALID;
+  }
+  if (m.weight_norm != SPK_NORM_OFF && !m.has_stdp) {
+    set_error("the weight normalisation acts on the plastic synapses of an STDP rule");
     return SPK_ERR_INVALID;
   }
   if (m.N <= 0 || m.Nin < 0 || m.L < 1 || m.L > MAX_LABELS || !(m.dt > 0.0f)) {
@@ -512,6 +538,7 @@ static int new_net(const ModelSpec& m, int B, int64_t S, const spk_schedule* sch
   n->dt = m.dt;
   n->has_stdp = m.has_stdp != 0;
   n->stdp_rule = m.stdp_rule;
+  n->weight_norm = m.has_stdp ? m.weight_norm : SPK_NORM_OFF;
   n->record_inputs = m.record_inputs != 0;
   n->seed = m.seed;
   n->n_stim = m.Nin > 0 ? m.n_stim : 0;
@@ -530,7 +557,8 @@ static int new_net(const ModelSpec& m, int B, int64_t S, const spk_schedule* sch
 // rate-monitor counts, and for per-synapse-trace STDP rules the afferent
 // records' delays, their traces and the spike-word history.
 static std::vector<size_t> arena_part_sizes(const Plan& plan, int N, int Nin, int L, int B, int stdp, int64_t S,
-                                            int64_t n_csc, int n_stim, int64_t spike_cap, int dense = 0) {
+                                            int64_t n_csc, int n_stim, int64_t spike_cap, int dense = 0,
+                                            int norm = 0) {
   const size_t n_cells = (size_t)plan.n_keys * plan.n_tiles;
   const size_t key_cap = (size_t)plan.W * (plan.TS + plan.ITS);
   return {sizeof(int32_t) * (n_cells + 1),
@@ -558,7 +586,9 @@ static std::vector<size_t> arena_part_sizes(const Plan& plan, int N, int Nin, in
           sizeof(int) * (size_t)plan.n_keys,
           sizeof(int32_t) * (dense ? (size_t)n_csc : 0),
           sizeof(float) * (dense ? 2 * (size_t)n_csc : 0),
-          sizeof(uint32_t) * (dense ? (size_t)(B - 2) * plan.n_words : 0)};
+          sizeof(uint32_t) * (dense ? (size_t)(B - 2) * plan.n_words : 0),
+          sizeof(float) * (norm ? (size_t)n_csc : 0),
+          sizeof(float) * (norm ? (size_t)N : 0)};
 }
 
 static size_t arena_total(const std::vector<size_t>& sizes) {
@@ -604,13 +634,15 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   const int key_cap = plan.W * (plan.TS + plan.ITS);
   void* p_ctl = nullptr; void* p_abort = nullptr; void* p_dd = nullptr; void* p_map = nullptr;
   void* p_rate = nullptr; void* p_cdelay = nullptr; void* p_dtr = nullptr; void* p_hist = nullptr;
+  void* p_nw0 = nullptr; void* p_nsum = nullptr;
   const int dense = n->dense() ? 1 : 0;
+  const int norm = n->weight_norm != SPK_NORM_OFF ? 1 : 0;
   const std::vector<size_t> sizes =
-      arena_part_sizes(plan, N, Nin, L, B, stdp, S, n_csc, n->n_stim, spike_cap, dense);
+      arena_part_sizes(plan, N, Nin, L, B, stdp, S, n_csc, n->n_stim, spike_cap, dense, norm);
   void** dsts[] = {&p_rowptr, &p_entries, &p_cscptr, &p_csc,   &p_V,     &p_last,   &p_gtr,  &p_ring,
                    &p_innext, &p_rates,   &p_post,   &p_pre,   &p_pub,   &p_bA,     &p_bP,   &p_ckeys,
                    &p_cstamp, &p_spk,     &p_ctl,    &p_abort, &p_dd,    &p_map,  &p_rate,
-                   &p_cdelay, &p_dtr,     &p_hist};
+                   &p_cdelay, &p_dtr,     &p_hist,   &p_nw0,   &p_nsum};
   std::vector<Part> parts;
   for (size_t i = 0; i < sizes.size(); ++i) parts.push_back(Part{dsts[i], sizes[i]});
   const size_t total = arena_total(sizes);
@@ -733,6 +765,11 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
       h.rule_c[7] = sp.clip_upper ? 1.0f : 0.0f;
     }
   }
+  h.weight_norm = n->weight_norm;
+  if (norm) {
+    h.norm_w0 = (const float*)p_nw0;
+    h.norm_sum = (const float*)p_nsum;
+  }
   h.rowptr = (const int*)p_rowptr;
   h.entries = (uint2*)p_entries;
   h.csc_ptr = (const int*)p_cscptr;
@@ -776,6 +813,10 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   urc |= up(p_cscptr, csc_ptr_h, sizeof(int32_t) * (stdp ? (size_t)N + 1 : 0));
   urc |= up(p_csc, csc_h, sizeof(uint2) * (size_t)n_csc);
   if (dense) urc |= up(p_cdelay, csc_delay_h, sizeof(int32_t) * (size_t)n_csc);
+  if (norm) {
+    urc |= up(p_nw0, n->norm_w0_h.data(), sizeof(float) * n->norm_w0_h.size());
+    urc |= up(p_nsum, n->norm_sum_h.data(), sizeof(float) * n->norm_sum_h.size());
+  }
   if (Nin > 0) urc |= up(p_rates, m.rates, sizeof(float) * (size_t)n->n_stim * Nin);
   urc |= up(p_ctl, &ctl, sizeof(ctl));
   urc |= up(p_dd, &h, sizeof(h));
@@ -844,6 +885,9 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
   m.has_stdp = d->has_stdp ? 1 : 0;
   m.stdp = d->stdp;
   m.stdp_rule = d->stdp_rule;
+  m.weight_norm = d->weight_norm;
+  m.norm_initial = d->norm_initial;
+  m.norm_sum = d->norm_sum;
   m.seed = d->seed;
   m.spike_capacity = d->spike_capacity;
   m.record_inputs = d->record_inputs;
@@ -943,6 +987,21 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
         if (n->dense()) csc_delay[pos] = d->delay[s];
         n->csc_of[s] = pos;
       }
+    if (n->weight_norm != SPK_NORM_OFF) {
+      // WeightNormSTDPPlasticity::prepare_backend_early
+      // (Spike/Plasticity/WeightNormSTDPPlasticity.cpp:31-70): initial weights,
+      // and per post the sum of pow(w, 2.0f) over its plastic afferents in
+      // the rule's (creation) order, on the host
+      n->norm_w0_h.assign(csc.size(), 0.0f);
+      n->norm_sum_h.assign((size_t)N, 0.0f);
+      for (int64_t s = 0; s < S; ++s) {
+        const int32_t pos = n->csc_of[s];
+        if (pos < 0) continue;
+        n->norm_w0_h[pos] = m.norm_initial ? m.norm_initial[s] : d->weight[s];
+        if (!m.norm_sum) n->norm_sum_h[d->post[s]] += powf(d->weight[s], 2.0f);
+      }
+      if (m.norm_sum) n->norm_sum_h.assign(m.norm_sum, m.norm_sum + N);
+    }
   }
   // ---- entries: static synapses carry w*scale, plastic ones their record ----
   std::vector<uint2> entries(S);
@@ -1976,10 +2035,10 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
       delete b;
       return SPK_ERR_CUDA;
     }
-    // per-synapse-trace STDP rules run in bulk mode only
-    bool any_dense = false;
-    for (int i = 0; i < n_nets; ++i) any_dense = any_dense || nets[i]->dense();
-    if (any_dense) {
+    // per-synapse-trace STDP rules and the weight normalisation run in bulk mode only
+    bool any_bulk_only = false;
+    for (int i = 0; i < n_nets; ++i) any_bulk_only = any_bulk_only || nets[i]->bulk_only();
+    if (any_bulk_only) {
       const int rc = spk_batch_set_mode(b, SPK_BATCH_BULK);
       if (rc) {
         spk_batch_destroy(b);
@@ -1993,35 +2052,62 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
 
 namespace spk {
 
-// One block of K timesteps in bulk mode: 3K or 4K kernels (4 with plastic
-// networks) and the run-counter update.
+// One block of K timesteps in bulk mode and the run-counter update.  A
+// timestep: neurons, list, [normalisation before the rule], [per-synapse-trace
+// rules], [normalisation after them], the afferent pass beside propagation,
+// and where a network normalises after the event-driven rule, that
+// normalisation and a second propagation pass that delivers.
 static int bulk_launch_block(spk_batch* b) {
   const int n = (int)b->nets.size();
   const int prop_smem = bulk_prop_layout(b->win_words, b->ts_max).total * 4;
   DeviceInfo di;
   const int rc0 = device_info(&di);
   if (rc0) return rc0;
+  const bool split = (b->norm_slots & 4) != 0;
+  const int item_grid = std::min((b->n_dense_items + 7) / 8, di.sms * 8);
+  int per_step = 0;
   for (int s = 0; s < b->K; ++s) {
+    per_step = 0;
     SPK_CUDA(launch_overlapped(bulk_neurons_kernel, b->blocks_total, BULK_NEUR_WARPS * 32, 0, b->stream,
                                (const NetDev*)b->dd, (const BulkBlock*)b->dblocks, s, b->item_count));
     SPK_CUDA(launch_overlapped(bulk_list_kernel, n, BULK_LIST_THREADS, 0, b->stream, (const NetDev*)b->dd, s,
                                b->items, b->item_count, b->item_cap));
-    if (b->n_dense_items)
-      bulk_dense_stdp_kernel<<<std::min((b->n_dense_items + 7) / 8, di.sms * 8), 256, 0, b->stream>>>(
-          b->dd, b->dense_items, b->n_dense_items, s);
+    per_step += 2;
+    if (b->norm_slots & 1) {
+      bulk_norm_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s, 0);
+      ++per_step;
+    }
+    if (b->any_dense) {
+      bulk_dense_stdp_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s);
+      ++per_step;
+    }
+    if (b->norm_slots & 2) {
+      bulk_norm_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s, 1);
+      ++per_step;
+    }
     if (b->any_plastic) {
       SPK_CUDA(cudaEventRecord(b->fork, b->stream));
       SPK_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0));
       bulk_post_kernel<<<di.sms * 8, 256, 0, b->side>>>(b->dd, b->items, b->item_count, b->item_cap);
       SPK_CUDA(cudaEventRecord(b->join, b->side));
+      ++per_step;
     }
     SPK_CUDA(launch_overlapped(bulk_prop_kernel, b->pblocks_total, BULK_PROP_WARPS * 32, (size_t)prop_smem,
                                b->stream, (const NetDev*)b->dd, (const BulkPropBlock*)b->dpblocks, s, b->win_words,
-                               b->ts_max));
+                               b->ts_max, split ? 1 : 0));
+    ++per_step;
     if (b->any_plastic) SPK_CUDA(cudaStreamWaitEvent(b->stream, b->join, 0));
+    if (split) {
+      bulk_norm_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s, 2);
+      SPK_CUDA(launch_overlapped(bulk_prop_kernel, b->pblocks_total, BULK_PROP_WARPS * 32, (size_t)prop_smem,
+                                 b->stream, (const NetDev*)b->dd, (const BulkPropBlock*)b->dpblocks, s,
+                                 b->win_words, b->ts_max, 2));
+      per_step += 2;
+    }
   }
   bulk_finish_kernel<<<(n + 255) / 256, 256, 0, b->stream>>>(b->dd, n, b->K);
   SPK_CUDA(cudaGetLastError());
+  b->step_launches = per_step;
   return SPK_OK;
 }
 
@@ -2036,13 +2122,13 @@ static int bulk_run_block(spk_batch* b) {
       cudaGetLastError();
       b->bulk_graph = nullptr;
       const int rc2 = bulk_launch_block(b);  // launches go direct
-      b->launches += (b->any_plastic ? 4 : 3) * (int64_t)b->K + 1;
+      b->launches += (int64_t)b->step_launches * b->K + 1;
       return rc2;
     }
     cudaGraphDestroy(g);
   }
   SPK_CUDA(cudaGraphLaunch(b->bulk_graph, b->stream));
-  b->launches += (b->any_plastic ? 4 : 3) * (int64_t)b->K + 1;
+  b->launches += (int64_t)b->step_launches * b->K + 1;
   return SPK_OK;
 }
 
@@ -2105,8 +2191,9 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
   if (mode == b->mode) return SPK_OK;
   if (mode == SPK_BATCH_WAVES) {
     for (const spk_net* n : b->nets)
-      if (n->dense()) {
-        set_error("waves mode: a network with a per-synapse-trace STDP rule runs in bulk mode only");
+      if (n->bulk_only()) {
+        set_error("waves mode: a network with a per-synapse-trace STDP rule or the weight normalisation "
+                  "runs in bulk mode only");
         return SPK_ERR_UNSUPPORTED;
       }
     b->mode = mode;
@@ -2148,12 +2235,19 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
         return SPK_ERR_UNSUPPORTED;
       }
       b->item_cap = (int)cap;
-      // posts of the networks with a per-synapse-trace rule: the dense STDP pass
+      // posts of the networks with a per-synapse-trace rule or the weight
+      // normalisation: the per-post passes
       {
         std::vector<BulkPostItem> dense;
-        for (size_t i = 0; i < b->nets.size(); ++i)
-          if (b->nets[i]->dense())
-            for (int q = 0; q < b->nets[i]->N; ++q) dense.push_back(BulkPostItem{(int)i, q});
+        b->any_dense = false;
+        b->norm_slots = 0;
+        for (size_t i = 0; i < b->nets.size(); ++i) {
+          const spk_net* x = b->nets[i];
+          if (!x->bulk_only()) continue;
+          b->any_dense = b->any_dense || x->dense();
+          if (x->weight_norm != SPK_NORM_OFF) b->norm_slots |= 1 << x->norm_slot();
+          for (int q = 0; q < x->N; ++q) dense.push_back(BulkPostItem{(int)i, q});
+        }
         if (!dense.empty()) {
           if (cudaMalloc(&b->dense_items, sizeof(BulkPostItem) * dense.size()) != cudaSuccess) {
             cudaGetLastError();

@@ -53,6 +53,7 @@ class SynapseParams:
     pairwise_weight: list | None = None
     pairwise_delay: list | None = None
     plasticity_rule: int = -1
+    plasticity_rule_2: int = -1  # a second rule on the same synapses (the weight normalisation)
     _keep: list = field(default_factory=list, repr=False)
 
     def to_c(self) -> N.SynapseParams:
@@ -69,6 +70,7 @@ class SynapseParams:
         s.gaussian_synapses_per_postsynaptic_neuron = self.gaussian_synapses_per_postsynaptic_neuron
         s.gaussian_synapses_standard_deviation = self.gaussian_synapses_standard_deviation
         s.plasticity_rule = self.plasticity_rule
+        s.plasticity_rule_2 = self.plasticity_rule_2
         s.n_pairwise = 0
         self._keep.clear()
         if self.pairwise_pre is not None:
@@ -516,6 +518,15 @@ class Model:
         rid = C.c_int32()
         check(lib().spk_model_add_plasticity_rule(self.h, rule, C.byref(c), C.byref(rid)),
               "spk_model_add_plasticity_rule")
+        return rid.value
+
+    def add_weight_norm_rule(self, settarget: bool = False, target: float = 0.0) -> int:
+        """WeightNormSTDPPlasticity: per-post L2 normalisation of the STDP
+        rule's synapses (attach it to the same synapse groups as a second
+        rule)."""
+        rid = C.c_int32()
+        check(lib().spk_model_add_weight_norm_rule(self.h, 1 if settarget else 0, C.c_float(target), C.byref(rid)),
+              "spk_model_add_weight_norm_rule")
         return rid.value
 
     def add_synapse_group(self, pre: int, post: int, p: SynapseParams) -> int:

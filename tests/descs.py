@@ -15,7 +15,8 @@ class Desc:
     def __init__(self, *, kind=N.SPK_SYN_VOLTAGE, groups, dt=0.0001, refractory=0.002, i_bg=0.0,
                  n_inputs=0, rates=None, label_tau=None, label_vhat=None, n_labels=1,
                  pre=(), post=(), weight=(), scale=None, delay=(), label=None, plastic=None,
-                 stdp=None, seed=1, spike_capacity=0, record_inputs=False, stdp_rule=0):
+                 stdp=None, seed=1, spike_capacity=0, record_inputs=False, stdp_rule=0, weight_norm=0,
+                 norm_initial=None, norm_sum=None):
         self.keep = []
         d = N.NetDesc()
         d.abi_version = N.SPK_ABI_VERSION
@@ -79,11 +80,18 @@ class Desc:
         d.spike_capacity = spike_capacity
         d.record_inputs = 1 if record_inputs else 0
         d.stdp_rule = stdp_rule
+        d.weight_norm = weight_norm
+        for name, arr in (("norm_initial", norm_initial), ("norm_sum", norm_sum)):
+            if arr is not None:
+                a = np.ascontiguousarray(arr, np.float32)
+                self.keep.append(a)
+                setattr(d, name, a.ctypes.data_as(C.POINTER(C.c_float)))
         self.desc = d
 
 
 def random_voltage_net(n=300, n_in=200, rate=40.0, p=0.08, d_max=12, seed=5, plastic=False, stdp=None,
-                       j=8.0e-4, g=4.0, record_inputs=True, stdp_rule=0):
+                       j=8.0e-4, g=4.0, record_inputs=True, stdp_rule=0, weight_norm=0, norm_initial=None,
+                       norm_sum=None):
     """A small random voltage-synapse network with inputs, E/I weights and
     delays 1..d_max (multapses included), for parity tests."""
     rng = np.random.default_rng(seed)
@@ -115,4 +123,5 @@ def random_voltage_net(n=300, n_in=200, rate=40.0, p=0.08, d_max=12, seed=5, pla
                         dict(count=n - n_exc, tau_m=0.01, R=1e8, v0=0.0, vreset=0.002, theta=0.018)],
                 refractory=0.002, n_inputs=n_in, rates=rng.uniform(0.5 * rate, 1.5 * rate, n_in).astype(np.float32),
                 pre=pre, post=post, weight=w, delay=dl, plastic=plastic_mask, stdp=stdp, seed=seed + 100,
-                record_inputs=record_inputs, stdp_rule=stdp_rule)
+                record_inputs=record_inputs, stdp_rule=stdp_rule, weight_norm=weight_norm,
+                norm_initial=norm_initial, norm_sum=norm_sum)

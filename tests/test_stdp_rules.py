@@ -14,6 +14,7 @@ import pytest
 import descs
 from engine_checks import assert_same, bits
 from oracle import OracleNet
+from restated_rules import rasters_of, restated_rule
 from spike_gb300 import Batch, Net, schedule
 from spike_gb300 import _native as N
 from spike_gb300.model import STDPParams
@@ -32,80 +33,6 @@ RULES = [(N.SPK_STDP_EVANS, EVANS), (N.SPK_STDP_INHIBITORY, VOGELS), (N.SPK_STDP
 gpu = pytest.mark.gpu
 
 
-def host_expf(x):
-    """The C library's expf, with which the reference computes the decays on
-    the host."""
-    import ctypes
-    import ctypes.util
-    libm = ctypes.CDLL(ctypes.util.find_library("m"))
-    libm.expf.restype = ctypes.c_float
-    libm.expf.argtypes = [ctypes.c_float]
-    return np.float32(libm.expf(float(x)))
-
-
-def restated_rule(rule, sp, d, pre_spk, post_spk, steps, n_exc):
-    """The three kernels' per-synapse updates restated over whole arrays of
-    plastic synapses (float32 as the kernels compute, no contraction), driven
-    by the recorded rasters: at timestep T the postsynaptic bit is T and the
-    presynaptic bit is T - delay (EvansSTDPPlasticity.cu:96-131,
-    InhibitorySTDPPlasticity.cu:108-143, CustomSTDPPlasticity.cu:99-142)."""
-    f32, f64 = np.float32, np.float64
-    pre_a, post_a = d.arrays["pre"], d.arrays["post"]
-    plastic = pre_a < n_exc  # inputs and excitatory neurons
-    pre_key = np.where(pre_a >= 0, pre_a, 0)
-    pre_is_input = pre_a < 0
-    in_key = np.where(pre_is_input, -pre_a - 1, 0)
-    delay = d.arrays["delay"]
-    w = d.arrays["weight"].copy()
-    idx = np.nonzero(plastic)[0]
-    wp = w[idx].astype(f32)
-    tp = np.zeros(len(idx), f32)  # presynaptic trace
-    tq = np.zeros(len(idx), f32)  # postsynaptic trace
-    dt = f32(d.desc.dt)
-    one = f32(1)
-    for T in range(steps):
-        pT = T - delay[idx]
-        ok = pT >= 0
-        pTc = np.where(ok, pT, 0)
-        pre = ok & np.where(pre_is_input[idx], pre_spk[1][pTc, in_key[idx]], pre_spk[0][pTc, pre_key[idx]])
-        post = post_spk[T, post_a[idx]]
-        if rule == N.SPK_STDP_EVANS:
-            tp = (one - (dt / f32(sp.tau_plus))) * tp
-            tq = (one - (dt / f32(sp.tau_minus))) * tq
-            tp = np.where(pre, tp + dt * f32(sp.a_plus) * (one - tp), tp)
-            tq = np.where(post, tq + dt * f32(sp.a_minus) * (one - tq), tq)
-            syn = np.zeros_like(wp)
-            syn = np.where(pre, syn - (wp * tq), syn)
-            syn = np.where(post, syn + ((one - wp) * tp), syn)
-            wp = np.clip(wp + syn, f32(0), f32(1))
-        elif rule == N.SPK_STDP_INHIBITORY:
-            decay = host_expf(-dt / f32(sp.tau_plus))
-            tp = tp * decay
-            tq = tq * decay
-            tp = np.where(pre, tp + one, tp)
-            tq = np.where(post, tq + one, tq)
-            lr = f32(sp.lambda_)
-            syn = np.zeros_like(wp)
-            syn = np.where(pre, syn + lr * tq, syn)
-            const = f64(-lr) * (2.0 * f64(f32(sp.alpha)) * f64(f32(sp.tau_plus)))
-            syn = np.where(pre, (syn.astype(f64) + const).astype(f32), syn)
-            syn = np.where(post, syn + lr * tp, syn)
-            wp = np.maximum(wp + syn, f32(0))
-        else:
-            tq = tq * host_expf(-dt / f32(sp.tau_minus))
-            tp = tp * host_expf(-dt / f32(sp.tau_plus))
-            a_plus, a_minus = f32(sp.a_plus), f32(sp.a_minus)
-            tp = np.where(pre, a_plus if sp.clip_upper else tp + a_plus, tp)
-            tq = np.where(post, a_minus if sp.clip_upper else tq + a_minus, tq)
-            lr, a_star, w_max = f32(sp.lambda_), f32(sp.alpha), f32(sp.w_max)
-            syn = np.zeros_like(wp)
-            syn = np.where(pre, syn - (lr * (wp / w_max) * tq + lr * a_star), syn)
-            syn = np.where(post, syn + lr * tp, syn)
-            wp = np.maximum(wp + syn, f32(0))
-    w[idx] = wp
-    return w
-
-
 @pytest.mark.parametrize("rule,sp", RULES)
 def test_oracle_rules_follow_the_reference_kernels(rule, sp):
     """The oracle's rule restatement against a second one written from the
@@ -114,13 +41,7 @@ def test_oracle_rules_follow_the_reference_kernels(rule, sp):
     d = descs.random_voltage_net(n=n, n_in=n_in, plastic=True, stdp=sp, stdp_rule=rule, seed=21)
     o = OracleNet(d.desc)
     o.run_steps(steps, True)
-    dt = np.float32(d.desc.dt)
-    rasters = []
-    for pop, count in ((N.SPK_POP_NEURONS, n), (N.SPK_POP_INPUTS, n_in)):
-        ids, times = o.spikes(pop)
-        r = np.zeros((steps, count), bool)
-        r[np.rint(times / dt).astype(np.int64), ids] = True
-        rasters.append(r)
+    rasters = rasters_of(o, d, steps, n, n_in)
     assert rasters[0].sum() > 20 and rasters[1].sum() > 100
     want = restated_rule(rule, sp, d, rasters, rasters[0], steps, int(0.8 * n))
     got = o.weights()
