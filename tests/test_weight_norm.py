@@ -179,7 +179,8 @@ def test_normalisation_matches_oracle(rule, sp, norm):
     assert net.synchronize() == 0
     assert_same(net, o, 300, 200, 1, weights=True, tag=f"rule {rule} norm {norm}")
     # the normalisation acted: the same network without it ends elsewhere
-    plain = OracleNet(net_desc(rule, sp, N.SPK_NORM_OFF).desc)
+    dp = net_desc(rule, sp, N.SPK_NORM_OFF)  # keep the arrays alive while the oracle uses them
+    plain = OracleNet(dp.desc)
     for plastic, t in ((True, 0.03), (False, 0.01), (True, 0.03)):
         plain.run(t, plastic)
     S = len(d.arrays["weight"])
