@@ -63,6 +63,8 @@ def parse():
     p.add_argument("--arrival-rate", type=float, default=20.0, help="served: mean requests per second")
     p.add_argument("--instances", type=int, default=256, help="batched: network instances")
     p.add_argument("--scale", type=float, default=1.0, help="plastic_ff: network size factor (profiling cases)")
+    p.add_argument("--rule", default="weight_dependent", choices=["weight_dependent", "evans"],
+                   help="plastic_ff: STDP rule of the input synapses")
     p.add_argument("--tune-steps", type=int, default=100, help="batched: autotuner trial timesteps")
     p.add_argument("--mode", default="auto", choices=["auto", "waves", "bulk"],
                    help="batched: execution mode (auto: the autotuner's choice; waves without the autotuner); served: waves, else bulk")
@@ -85,7 +87,10 @@ def parse():
     return a
 
 
-def build_model(workload: str, scale: float = 1.0):
+RULES = {"weight_dependent": 0, "evans": 1}
+
+
+def build_model(workload: str, scale: float = 1.0, rule: str = "weight_dependent"):
     from spike_gb300 import networks
     if workload == "brunel":
         m = networks.brunel()
@@ -100,10 +105,12 @@ def build_model(workload: str, scale: float = 1.0):
         L = 2
     else:
         n_in, n_neu = int(round(50000 * scale)), int(round(200000 * scale))
-        m = networks.plastic_ff_generated(n_in=n_in, n_neurons=n_neu)
-        cfg = {"workload": f"plastic_ff_{n_neu}_lif_{n_in}_lognormal_poisson_stdp", "neurons": n_neu,
+        m = networks.plastic_ff_generated(n_in=n_in, n_neurons=n_neu, rule=RULES[rule])
+        tag = "stdp" if rule == "weight_dependent" else f"{rule}_stdp"
+        cfg = {"workload": f"plastic_ff_{n_neu}_lif_{n_in}_lognormal_poisson_{tag}", "neurons": n_neu,
                "inputs": n_in, "in_degree": "binomial, mean 900 input + 100 recurrent", "delays_steps": [1, 10],
-               "dt_ms": 0.1, "sim_s_per_config": 5.0, "plasticity": True, "connectivity": "drawn on the GPU"}
+               "dt_ms": 0.1, "sim_s_per_config": 5.0, "plasticity": True, "stdp_rule": rule,
+               "connectivity": "drawn on the GPU"}
         L = 1
     return m, cfg, L
 
@@ -195,9 +202,15 @@ def traffic_per_launch(workload: str):
         return None
 
 
-def networks_small_plastic_ff():
+def networks_small_plastic_ff(rule: str = "weight_dependent"):
     from spike_gb300 import networks
-    return networks.plastic_ff_generated(n_in=2500, n_neurons=10000, ff=900, rec=100)
+    return networks.plastic_ff_generated(n_in=2500, n_neurons=10000, ff=900, rec=100, rule=RULES[rule])
+
+
+# Per plastic synapse and timestep, a per-synapse-trace rule's pass reads the
+# afferent record (8 B), its delay (4 B) and its two traces (8 B) and writes
+# the weight (4 B) and the traces (8 B).
+TRACE_RULE_BYTES = 32
 
 
 def cpu_baseline(desc, steps: int, threads: int):
@@ -213,13 +226,13 @@ def run_reference(args, rank, world):
     """CPU reference arm: the oracle port with all host threads."""
     if rank != 0:
         return
-    m, cfg, L = build_model(args.workload, args.scale)
+    m, cfg, L = build_model(args.workload, args.scale, args.rule)
     threads = os.cpu_count() or 1
     from oracle import OracleNet
     from spike_gb300 import GenNetwork
     if isinstance(m, GenNetwork):
         # too large to draw on the host: the same construction at 1/20 size
-        dd = oracle_instance(networks_small_plastic_ff())[1]
+        dd = oracle_instance(networks_small_plastic_ff(args.rule))[1]
         desc = dd.desc
         cfg = {**cfg, "cpu_sample_network": "same construction at 1/20 size (2,500 inputs, 10,000 neurons)"}
     else:
@@ -272,7 +285,7 @@ def main():
     from spike_gb300 import schedule
 
     from spike_gb300 import GenNetwork, Net
-    m, cfg, L = build_model(args.workload, args.scale)
+    m, cfg, L = build_model(args.workload, args.scale, args.rule)
     sched = schedule(args.warps, args.tile, args.ctas, args.launch_steps or args.block)
     if isinstance(m, GenNetwork):
         net = Net.generate(m, sched)
@@ -282,7 +295,9 @@ def main():
         desc = m.desc()
         net = m.finalise(sched)
         n_neurons, n_inputs, n_syn = m.counts()
-    plastic_run = args.workload == "plastic_ff"
+    trace_rule = args.workload == "plastic_ff" and args.rule != "weight_dependent"
+    plastic_run = args.workload == "plastic_ff" and not trace_rule  # the event-driven rule's traces
+    n_plastic = net.plastic_synapse_count()
     stream = torch.cuda.ExternalStream(net.stream())
 
     def barrier():
@@ -326,11 +341,13 @@ def main():
     timesteps = args.steps * args.block
     alg = algorithmic_bytes(events, pre1 - pre0, post1 - post0, n_neurons * timesteps, n_inputs * timesteps, L,
                             (n_neurons + n_inputs) * timesteps if plastic_run else 0)
+    if trace_rule:
+        alg += TRACE_RULE_BYTES * n_plastic * timesteps
     per_launch_s = (ms / 1000.0) / max(launches, 1)
     per_launch_bytes = alg / max(launches, 1)
     peak, peak_kind = peaks()
     achieved = per_launch_bytes / per_launch_s / 1e9
-    tr = traffic_per_launch(args.workload)
+    tr = traffic_per_launch(args.workload if not trace_rule else f"{args.workload}_{args.rule}")
     traffic = None
     if tr and tr.get("traffic_per_alg_byte"):
         traffic = tr["traffic_per_alg_byte"] * per_launch_bytes
@@ -365,7 +382,7 @@ def main():
         if desc is None:
             # the generated network is too large to draw on the host: a
             # 1/20-size network of the same construction stands in
-            cs = CpuSample([networks_small_plastic_ff()])
+            cs = CpuSample([networks_small_plastic_ff(args.rule)])
             cv, cel = cs.run(args.cpu_sample_steps // 10, parallel=False)
             cpu = {"value": cv, "unit": "events/s", "cores": 1, "kind": "port",
                    "sample": f"the same construction at 1/20 size (2,500 inputs, 10,000 neurons), "
@@ -382,7 +399,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "ours",
-            "config": {**cfg, "block_timesteps": args.block, "synapses": n_syn,
+            "config": {**cfg, "block_timesteps": args.block, "synapses": n_syn, "plastic_synapses": n_plastic,
                        "schedule": net.schedule(),
                        "l2": f"synapse entries {8 * n_syn / 1e6:.0f} MB > 129 MB L2 (no flush)",
                        "parallelism": "replicas" if world > 1 else "single"},
@@ -390,7 +407,9 @@ def main():
             "status": status,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "spk::step_kernel", "launches": launches,
+                         "kernel": ("bulk kernels of one timestep (neurons, list, per-synapse-trace rule, "
+                                    "propagation)" if trace_rule else "spk::step_kernel"),
+                         "launches": launches,
                          "alg_bytes_per_launch": per_launch_bytes, "ms_per_launch": 1000 * per_launch_s},
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clk.summary(),
             "gpu_launches": launches + args.steps,
@@ -450,6 +469,7 @@ def oracle_instance(gen):
     if d.has_stdp:
         dd.desc.has_stdp = 1
         dd.desc.stdp = d.stdp
+        dd.desc.stdp_rule = d.stdp_rule
     return OracleNet(dd.desc, 32, threads=1), dd
 
 

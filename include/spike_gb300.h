@@ -340,12 +340,15 @@ typedef struct spk_gen_desc {
   uint64_t connectivity_seed; /* connection, weight and delay draws */
   int64_t spike_capacity;
   int32_t record_inputs;
-  int32_t reserved;
+  int32_t stdp_rule;          /* SPK_STDP_* of the plastic projections (the weight
+                                 normalisation needs a host-built network) */
 } spk_gen_desc;
 
 int spk_net_generate(const spk_gen_desc* desc, const spk_schedule* schedule, spk_net** out);
 /* Synapses of a network (created or generated). */
 int spk_net_synapse_count(const spk_net* net, int64_t* n);
+/* Synapses under the STDP rule (STDPPlasticity::total_number_of_plastic_synapses). */
+int spk_net_plastic_synapse_count(const spk_net* net, int64_t* n);
 
 /* ---- batch: many independent networks in one persistent launch ---------- */
 int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* schedule,

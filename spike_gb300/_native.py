@@ -102,7 +102,7 @@ class GenDesc(C.Structure):
         ("n_projections", i32), ("projections", P(Projection)),
         ("has_stdp", i32), ("stdp", StdpParams),
         ("seed", u64), ("connectivity_seed", u64), ("spike_capacity", i64), ("record_inputs", i32),
-        ("reserved", i32),
+        ("stdp_rule", i32),
     ]
 
 
@@ -175,6 +175,7 @@ _SIGS = {
     "spk_net_create": (i32, [P(NetDesc), P(Schedule), P(_VP)]),
     "spk_net_generate": (i32, [P(GenDesc), P(Schedule), P(_VP)]),
     "spk_net_synapse_count": (i32, [_VP, P(i64)]),
+    "spk_net_plastic_synapse_count": (i32, [_VP, P(i64)]),
     "spk_net_destroy": (i32, [_VP]),
     "spk_net_reset_state": (i32, [_VP]),
     "spk_net_reset_time": (i32, [_VP]),

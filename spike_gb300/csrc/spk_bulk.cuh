@@ -884,6 +884,62 @@ __global__ void __launch_bounds__(256) bulk_post_kernel(const NetDev* __restrict
 //   2.0 literal evaluates it.
 //   Custom (CustomSTDPPlasticity.cu:100-142): pre and post memory traces,
 //   optionally nearest-spike, weight-scaled depression; weights clipped at 0.
+// One record's update under the network's rule, in the reference's order of
+// float operations.
+__device__ __forceinline__ void dense_rule_update(const NetDev& d, float dt, bool pre_sp, bool post_sp, float& w,
+                                                  float2& tr) {
+  const float c0 = d.rule_c[0], c1 = d.rule_c[1], c2 = d.rule_c[2], c3 = d.rule_c[3];
+  if (d.stdp_rule == SPK_STDP_EVANS) {
+    tr.x = (1.0f - (dt / c0)) * tr.x;
+    tr.y = (1.0f - (dt / c1)) * tr.y;
+    if (pre_sp) tr.x += dt * c2 * (1.0f - tr.x);
+    if (post_sp) tr.y += dt * c3 * (1.0f - tr.y);
+    float syn = 0.0f;
+    const float old_w = w;
+    if (pre_sp) syn -= (old_w * tr.y);
+    if (post_sp) syn += ((1.0f - old_w) * tr.x);
+    w = old_w + syn;
+    if (w < 0.0f) w = 0.0f;
+    if (w > 1.0f) w = 1.0f;
+  } else if (d.stdp_rule == SPK_STDP_INHIBITORY) {
+    tr.x *= c0;
+    tr.y *= c0;
+    if (pre_sp) tr.x += 1.0f;
+    if (post_sp) tr.y += 1.0f;
+    float syn = 0.0f;
+    if (pre_sp) {
+      syn += c1 * (tr.y);
+      syn = (float)((double)syn + (double)(-c1) * (2.0 * (double)c2 * (double)c3));
+    }
+    if (post_sp) syn += c1 * (tr.x);
+    w += syn;
+    if (w < 0.0f) w = 0.0f;
+  } else {
+    const float a_plus = c2, a_minus = c3, lr = d.rule_c[4], a_star = d.rule_c[5], w_max = d.rule_c[6];
+    const bool nearest = d.rule_c[7] != 0.0f;
+    tr.y *= c0;
+    tr.x *= c1;
+    if (pre_sp) {
+      tr.x += a_plus;
+      if (nearest) tr.x = a_plus;
+    }
+    if (post_sp) {
+      tr.y += a_minus;
+      if (nearest) tr.y = a_minus;
+    }
+    float syn = 0.0f;
+    const float old_w = w;
+    if (pre_sp) syn -= lr * (old_w / w_max) * tr.y + lr * a_star;
+    if (post_sp) syn += lr * tr.x;
+    w = old_w + syn;
+    if (w < 0.0f) w = 0.0f;
+  }
+}
+
+// Records per lane in flight: the pass is bound by HBM latency as much as
+// by bandwidth (a record's history word depends on its key and delay).
+constexpr int DENSE_RECS = 4;
+
 __global__ void __launch_bounds__(256) bulk_dense_stdp_kernel(const NetDev* __restrict__ nets,
                                                               const BulkPostItem* __restrict__ items, int n_items,
                                                               int s) {
@@ -899,63 +955,48 @@ __global__ void __launch_bounds__(256) bulk_dense_stdp_kernel(const NetDev* __re
     const bool post_sp = ((d.bitsA[key >> 5] >> (key & 31)) & 1u) != 0;
     const int a0 = __ldg(d.csc_ptr + item.post), a1 = __ldg(d.csc_ptr + item.post + 1);
     const float dt = d.dt;
-    const float c0 = d.rule_c[0], c1 = d.rule_c[1], c2 = d.rule_c[2], c3 = d.rule_c[3];
-    for (int a = a0 + lane; a < a1; a += 32) {
-      const uint2 rec = d.csc[a];
-      const int dl = d.csc_delay[a];
-      float2 tr = d.dense_tr[a];
-      int slot = (st.T - dl) % d.H;
-      if (slot < 0) slot += d.H;
-      const uint32_t pk = rec.x;
-      const bool pre_sp = ((d.hist[(size_t)slot * d.n_words + (pk >> 5)] >> (pk & 31)) & 1u) != 0;
-      float w = __uint_as_float(rec.y);
-      if (d.stdp_rule == SPK_STDP_EVANS) {
-        tr.x = (1.0f - (dt / c0)) * tr.x;
-        tr.y = (1.0f - (dt / c1)) * tr.y;
-        if (pre_sp) tr.x += dt * c2 * (1.0f - tr.x);
-        if (post_sp) tr.y += dt * c3 * (1.0f - tr.y);
-        float syn = 0.0f;
-        const float old_w = w;
-        if (pre_sp) syn -= (old_w * tr.y);
-        if (post_sp) syn += ((1.0f - old_w) * tr.x);
-        w = old_w + syn;
-        if (w < 0.0f) w = 0.0f;
-        if (w > 1.0f) w = 1.0f;
-      } else if (d.stdp_rule == SPK_STDP_INHIBITORY) {
-        tr.x *= c0;
-        tr.y *= c0;
-        if (pre_sp) tr.x += 1.0f;
-        if (post_sp) tr.y += 1.0f;
-        float syn = 0.0f;
-        if (pre_sp) {
-          syn += c1 * (tr.y);
-          syn = (float)((double)syn + (double)(-c1) * (2.0 * (double)c2 * (double)c3));
+    const int H = d.H, n_words = d.n_words;
+    // (T - delay) mod H from T mod H: delays are 1..H-1, so one wrap at most
+    const int t_mod = st.T % H;
+    uint2* const csc = d.csc;
+    const int* const cdl = d.csc_delay;
+    float2* const dtr = d.dense_tr;
+    const uint32_t* const hist = d.hist;
+    for (int a = a0 + lane; a < a1; a += 32 * DENSE_RECS) {
+      uint2 rec[DENSE_RECS];
+      int dl[DENSE_RECS];
+      float2 tr[DENSE_RECS];
+#pragma unroll
+      for (int u = 0; u < DENSE_RECS; ++u) {
+        const int ai = a + 32 * u;
+        if (ai < a1) {
+          rec[u] = csc[ai];
+          dl[u] = cdl[ai];
+          tr[u] = dtr[ai];
         }
-        if (post_sp) syn += c1 * (tr.x);
-        w += syn;
-        if (w < 0.0f) w = 0.0f;
-      } else {
-        const float a_plus = c2, a_minus = c3, lr = d.rule_c[4], a_star = d.rule_c[5], w_max = d.rule_c[6];
-        const bool nearest = d.rule_c[7] != 0.0f;
-        tr.y *= c0;
-        tr.x *= c1;
-        if (pre_sp) {
-          tr.x += a_plus;
-          if (nearest) tr.x = a_plus;
-        }
-        if (post_sp) {
-          tr.y += a_minus;
-          if (nearest) tr.y = a_minus;
-        }
-        float syn = 0.0f;
-        const float old_w = w;
-        if (pre_sp) syn -= lr * (old_w / w_max) * tr.y + lr * a_star;
-        if (post_sp) syn += lr * tr.x;
-        w = old_w + syn;
-        if (w < 0.0f) w = 0.0f;
       }
-      d.csc[a].y = __float_as_uint(w);
-      d.dense_tr[a] = tr;
+      uint32_t hw[DENSE_RECS];
+#pragma unroll
+      for (int u = 0; u < DENSE_RECS; ++u) {
+        const int ai = a + 32 * u;
+        hw[u] = 0u;
+        if (ai < a1) {
+          int slot = t_mod - dl[u];
+          if (slot < 0) slot += H;
+          hw[u] = hist[(size_t)slot * n_words + (rec[u].x >> 5)];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < DENSE_RECS; ++u) {
+        const int ai = a + 32 * u;
+        if (ai < a1) {
+          const bool pre_sp = ((hw[u] >> (rec[u].x & 31)) & 1u) != 0;
+          float w = __uint_as_float(rec[u].y);
+          dense_rule_update(d, dt, pre_sp, post_sp, w, tr[u]);
+          csc[ai].y = __float_as_uint(w);
+          dtr[ai] = tr[u];
+        }
+      }
     }
   }
 }

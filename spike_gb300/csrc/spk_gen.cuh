@@ -152,13 +152,16 @@ __global__ void gen_iota_kernel(uint32_t* v, long long n) {
 }
 
 // The i-th plastic synapse in (post, entry index) order gets afferent record
-// csc[i] = (presynaptic key, weight); its entry then points at the record.
+// csc[i] = (presynaptic key, weight), and for the per-synapse-trace rules its
+// delay; its entry then points at the record.
 __global__ void gen_csc_kernel(uint2* csc, uint2* entries, const uint32_t* sorted_entry, const uint32_t* entry_key,
-                               long long P) {
+                               long long P, int* csc_delay) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < P; i += stride) {
     const uint32_t e = sorted_entry[i];
-    csc[i] = make_uint2(entry_key[e], entries[e].y);
+    const uint2 en = entries[e];
+    csc[i] = make_uint2(entry_key[e], en.y);
+    if (csc_delay) csc_delay[i] = (int)((en.x >> 16) & 0xffu);
     entries[e].y = (uint32_t)i;
   }
 }

@@ -1083,6 +1083,7 @@ static int generate_impl(const spk_gen_desc* d, const spk_schedule* sched, spk_n
   m.label_vhat = d->label_vhat;
   m.has_stdp = d->has_stdp ? 1 : 0;
   m.stdp = d->stdp;
+  m.stdp_rule = d->stdp_rule;
   m.seed = d->seed;
   m.spike_capacity = d->spike_capacity;
   m.record_inputs = d->record_inputs;
@@ -1328,7 +1329,7 @@ static int generate_impl(const spk_gen_desc* d, const spk_schedule* sched, spk_n
       return fail(SPK_ERR_CUDA);
     }
     gen_csc_kernel<<<grid, 256, 0, st>>>(n->hd.csc, n->hd.entries, vals.Current(), ekey.as<uint32_t>(),
-                                         (long long)P);
+                                         (long long)P, const_cast<int*>(n->hd.csc_delay));
     if (cudaGetLastError() != cudaSuccess) return fail(SPK_ERR_CUDA);
     if (cudaStreamSynchronize(st) != cudaSuccess) {
       set_error("network generation failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -1563,6 +1564,12 @@ int spk_net_inject_withheld_cta(spk_net* n, int32_t rank) {
 int spk_net_synapse_count(const spk_net* n, int64_t* count) {
   if (!n || !count) return SPK_ERR_INVALID;
   *count = n->S;
+  return SPK_OK;
+}
+
+int spk_net_plastic_synapse_count(const spk_net* n, int64_t* count) {
+  if (!n || !count) return SPK_ERR_INVALID;
+  *count = n->has_stdp ? n->n_csc : 0;
   return SPK_OK;
 }
 
@@ -1904,7 +1911,8 @@ int spk_net_device_bytes(const spk_net* n, int64_t* bytes) {
 
 int spk_net_launch_count(const spk_net* n, int64_t* launches) {
   if (!n || !launches) return SPK_ERR_INVALID;
-  *launches = n->launches;
+  // runs of a network that takes bulk mode go through its own batch
+  *launches = n->launches + (n->self_batch ? n->self_batch->launches : 0);
   return SPK_OK;
 }
 

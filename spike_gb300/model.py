@@ -150,6 +150,11 @@ class Net:
         check(lib().spk_net_synapse_count(self.h, C.byref(n)), "spk_net_synapse_count")
         return n.value
 
+    def plastic_synapse_count(self) -> int:
+        n = C.c_int64()
+        check(lib().spk_net_plastic_synapse_count(self.h, C.byref(n)), "spk_net_plastic_synapse_count")
+        return n.value
+
     def close(self):
         if self.h and self.owned:
             lib().spk_net_destroy(self.h)
@@ -312,9 +317,10 @@ class GenNetwork:
 
     def __init__(self, *, groups, projections, kind=N.SPK_SYN_VOLTAGE, dt=0.0001, refractory=0.002, i_bg=0.0,
                  rates=None, n_inputs=0, label_tau=None, label_vhat=None, n_labels=1, stdp=None, seed=1,
-                 connectivity_seed=1, spike_capacity=0, record_inputs=False):
+                 connectivity_seed=1, spike_capacity=0, record_inputs=False, stdp_rule=N.SPK_STDP_WEIGHT_DEPENDENT):
         self.keep = []
         d = N.GenDesc()
+        d.stdp_rule = stdp_rule
         d.abi_version = N.SPK_ABI_VERSION
         d.dt = dt
         d.synapse_kind = kind

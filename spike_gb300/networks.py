@@ -116,23 +116,35 @@ def plastic_ff(n_in: int = 50000, n_neurons: int = 200000, ff: int = 900, rec: i
 BRUNEL_LIF = dict(tau_m=0.02, R=1.0e8, v0=0.0, vreset=0.0, theta=0.02)  # C_m 200 pF, g_0 10 nS
 
 
+# Evans rule constants for the plastic workloads: alpha_C = a_plus, alpha_D =
+# a_minus, tau_C = tau_plus, tau_D = tau_minus (EvansSTDPPlasticity.hpp defaults)
+EVANS_STDP = STDPParams(a_plus=0.5, a_minus=0.5, tau_plus=0.004, tau_minus=0.005, lambda_=0.0, alpha=0.0, w_max=1.0)
+
+
 def plastic_ff_generated(n_in: int = 50000, n_neurons: int = 200000, ff: int = 900, rec: int = 100,
                          d_max: int = 10, w_scale: float = 2.0e-4, sigma: float = 1.0, plastic: bool = True,
-                         seed: int = 42) -> GenNetwork:
+                         seed: int = 42, rule: int = N.SPK_STDP_WEIGHT_DEPENDENT) -> GenNetwork:
     """The large plastic feed-forward + recurrent network drawn on the GPU:
     each (input, neuron) pair connects with p = ff / n_in and each (neuron,
     neuron) pair with p = rec / n_neurons (binomial in-degree, mean ff + rec),
     weights U(0, 1] (inputs, plastic) and U(-1, 0] (recurrent) times w_scale
-    volts, delays U{1..d_max}, log-normal input rates."""
-    stdp = STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02, lambda_=1.0, alpha=1.0,
-                      w_max=1.0, clip_upper=True) if plastic else None
+    volts, delays U{1..d_max}, log-normal input rates.  `rule` is the STDP rule
+    of the input synapses: weight-dependent (a+ 0.005, a- 0.00525, tau 20 ms,
+    weights clipped to [0, 1]) or Evans (EVANS_STDP)."""
+    if rule == N.SPK_STDP_EVANS:
+        stdp = EVANS_STDP if plastic else None
+    elif rule == N.SPK_STDP_WEIGHT_DEPENDENT:
+        stdp = STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02, lambda_=1.0, alpha=1.0,
+                          w_max=1.0, clip_upper=True) if plastic else None
+    else:
+        raise ValueError(f"plastic_ff_generated: rule {rule} has no parameter set here")
     projs = [Projection(N.SPK_POP_INPUTS, 0, n_in, 0, n_neurons, ff / n_in, weight=(0.0, 1.0), scale=w_scale,
                         delay=(1, d_max), plastic=plastic),
              Projection(N.SPK_POP_NEURONS, 0, n_neurons, 0, n_neurons, rec / n_neurons, weight=(-1.0, 0.0),
                         scale=w_scale, delay=(1, d_max))]
     return GenNetwork(groups=[dict(count=n_neurons, **BRUNEL_LIF)], projections=projs, refractory=2.0e-3,
                       n_inputs=n_in, rates=lognormal_rates(n_in, sigma=sigma, seed=seed), stdp=stdp, seed=seed,
-                      connectivity_seed=seed + 1)
+                      connectivity_seed=seed + 1, stdp_rule=rule)
 
 
 def sweep_instance(n: int, p: float, g: float, plastic: bool, seed: int, d_max: int = 10,

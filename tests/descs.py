@@ -75,7 +75,7 @@ class Desc:
             d.plastic = p.ctypes.data_as(C.POINTER(C.c_uint8))
         if stdp is not None:
             d.has_stdp = 1
-            d.stdp = stdp.to_c()
+            d.stdp = stdp.to_c() if hasattr(stdp, "to_c") else stdp
         d.seed = seed
         d.spike_capacity = spike_capacity
         d.record_inputs = 1 if record_inputs else 0

@@ -27,7 +27,7 @@ GROUPS = [dict(count=480, tau_m=0.02, R=1e8, v0=0.0, vreset=0.0, theta=0.02, v_i
 N_IN, RATE = 300, 30.0
 
 
-def small_gen(stdp=True, seed=11):
+def small_gen(stdp=True, seed=11, rule=N.SPK_STDP_WEIGHT_DEPENDENT, stdp_params=STDP):
     rates = np.random.default_rng(seed).uniform(0.5 * RATE, 1.5 * RATE, N_IN).astype(np.float32)
     projs = [
         Projection(N.SPK_POP_INPUTS, 0, N_IN, 0, 600, 0.05, weight=(0.0, 1.0), scale=5e-3, delay=(1, 3),
@@ -36,8 +36,9 @@ def small_gen(stdp=True, seed=11):
         Projection(N.SPK_POP_NEURONS, 0, 480, 0, 480, 0.06, weight=(0.5, 1.0), scale=1e-3, delay=(1, 8)),
         Projection(N.SPK_POP_NEURONS, 480, 120, 0, 600, 0.05, weight=(-1.0, -0.5), scale=4e-3, delay=(1, 5)),
     ]
-    return GenNetwork(groups=GROUPS, projections=projs, n_inputs=N_IN, rates=rates, stdp=STDP if stdp else None,
-                      seed=seed + 1, connectivity_seed=seed + 2, record_inputs=True)
+    return GenNetwork(groups=GROUPS, projections=projs, n_inputs=N_IN, rates=rates,
+                      stdp=stdp_params if stdp else None, seed=seed + 1, connectivity_seed=seed + 2,
+                      record_inputs=True, stdp_rule=rule)
 
 
 def desc_from_oracle(gen: GenNetwork, arrays: dict) -> descs.Desc:
@@ -47,7 +48,7 @@ def desc_from_oracle(gen: GenNetwork, arrays: dict) -> descs.Desc:
                       pre=arrays["pre"], post=arrays["post"], weight=arrays["weight"], scale=arrays["scale"],
                       delay=arrays["delay"], label=arrays["label"],
                       plastic=arrays["plastic"] if d.has_stdp else None,
-                      stdp=STDP if d.has_stdp else None, seed=d.seed, record_inputs=True)
+                      stdp=d.stdp if d.has_stdp else None, seed=d.seed, record_inputs=True, stdp_rule=d.stdp_rule)
 
 
 def delivered(arrays: dict, stdp: bool) -> np.ndarray:
@@ -81,6 +82,29 @@ def test_generated_network_matches_oracle_synapses_and_run(sched):
     plastic = arrays["plastic"].astype(bool)
     np.testing.assert_array_equal(w_gen[plastic].view(np.uint32), w_ref[plastic].view(np.uint32))
     assert len(o.spikes()[0]) > 300
+
+
+def test_generated_network_with_a_trace_rule_matches_oracle():
+    """A generated network whose plastic synapses follow the Evans rule: the
+    afferent records get their delays on the device, and the run matches
+    the oracle on the same synapses."""
+    from spike_gb300.networks import EVANS_STDP
+    gen = small_gen(rule=N.SPK_STDP_EVANS, stdp_params=EVANS_STDP, seed=13)
+    arrays = generate_synapses(gen.desc)
+    S = len(arrays["pre"])
+    g = Net.generate(gen)
+    ref_desc = desc_from_oracle(gen, arrays)
+    o = OracleNet(ref_desc.desc)
+    for plastic, steps in ((True, 400), (False, 100), (True, 300)):
+        g.run_steps(steps, plastic)
+        o.run_steps(steps, plastic)
+    assert g.synchronize() == 0
+    assert_same(g, o, 600, N_IN, 1, tag="generated evans")
+    plastic = arrays["plastic"].astype(bool)
+    w = g.weights(S)
+    np.testing.assert_array_equal(w[plastic].view(np.uint32), o.weights()[plastic].view(np.uint32))
+    assert (w[plastic] != arrays["weight"][plastic]).sum() > 100
+    assert g.plastic_synapse_count() == int(plastic.sum())
 
 
 def test_generated_network_is_schedule_independent():
