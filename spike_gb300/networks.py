@@ -148,14 +148,15 @@ def plastic_ff_generated(n_in: int = 50000, n_neurons: int = 200000, ff: int = 9
 
 
 def sweep_instance(n: int, p: float, g: float, plastic: bool, seed: int, d_max: int = 10,
-                   rate: float = 20.0) -> GenNetwork:
+                   rate: float = 20.0, rule: int = N.SPK_STDP_WEIGHT_DEPENDENT) -> GenNetwork:
     """One instance of the batched sweep: a Brunel-style voltage-jump LIF
     network of n neurons (80 % excitatory), Bernoulli(p) recurrent
     connectivity, J = 0.1 V / C_E with C_E = 0.8 n p (J C_E as in
     Examples/Brunel10K.cpp), inhibitory weight -g J, delays U{1..d_max}, and
     an external drive of n / 5 Poisson inputs at `rate` Hz connected with
     probability 4p (C_E inputs per neuron, nu_ext = 2 nu_thr).  With
-    plasticity the input synapses are plastic, weights U(0, 1] at scale 2J."""
+    plasticity the input synapses are plastic, weights U(0, 1] at scale 2J,
+    under the weight-dependent rule or (`rule`) the Evans rule."""
     n_e = int(round(0.8 * n))
     n_i = n - n_e
     n_in = max(1, n // 5)
@@ -164,6 +165,8 @@ def sweep_instance(n: int, p: float, g: float, plastic: bool, seed: int, d_max: 
     p_in = min(1.0, 4.0 * p)
     stdp = STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02, lambda_=1.0, alpha=1.0,
                       w_max=1.0, clip_upper=True) if plastic else None
+    if plastic and rule == N.SPK_STDP_EVANS:
+        stdp = EVANS_STDP
     projs = [Projection(N.SPK_POP_INPUTS, 0, n_in, 0, n, p_in,
                         weight=(0.0, 1.0) if plastic else (1.0, 1.0), scale=2.0 * J if plastic else J,
                         delay=(1, d_max), plastic=plastic),
@@ -171,7 +174,8 @@ def sweep_instance(n: int, p: float, g: float, plastic: bool, seed: int, d_max: 
              Projection(N.SPK_POP_NEURONS, n_e, n_i, 0, n, p, weight=(-g, -g), scale=J, delay=(1, d_max))]
     return GenNetwork(groups=[dict(count=n_e, **BRUNEL_LIF), dict(count=n_i, **BRUNEL_LIF)], projections=projs,
                       refractory=2.0e-3, n_inputs=n_in, rates=np.full(n_in, rate, np.float32), stdp=stdp,
-                      seed=seed, connectivity_seed=seed ^ 0x5eed)
+                      seed=seed, connectivity_seed=seed ^ 0x5eed,
+                      stdp_rule=rule if plastic else N.SPK_STDP_WEIGHT_DEPENDENT)
 
 
 def batched_sweep(n_instances: int = 256, n_lo: int = 1000, n_hi: int = 50000, seed: int = 42,

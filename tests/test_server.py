@@ -73,6 +73,35 @@ def test_served_jobs_without_spike_recording(mode):
     srv.stop()
 
 
+def test_served_jobs_with_the_trace_rules_and_the_event_driven_rule():
+    """Jobs with the Evans rule (bulk mode only) served beside jobs with the
+    event-driven rule and static jobs by a waves-mode server: a block that
+    holds a trace-rule job runs in bulk mode, and every job equals the same
+    network run alone."""
+    rng = np.random.default_rng(21)
+    work = []
+    for i in range(6):
+        n = int(np.exp(rng.uniform(np.log(500), np.log(3000))))
+        rule = N.SPK_STDP_EVANS if i % 3 == 0 else N.SPK_STDP_WEIGHT_DEPENDENT
+        gen = sweep_instance(n, float(rng.uniform(0.02, 0.05)), 5.0, i % 3 != 2, seed=900 + i, d_max=6, rule=rule)
+        work.append((gen, int(rng.integers(300, 900)), True))
+    srv = Server(steps_per_block=200, reserve_bytes=1 << 30, mode=N.SPK_BATCH_WAVES)
+    ids = [srv.submit(gen, steps, plastic) for gen, steps, plastic in work]
+    infos = [srv.wait(j, 300.0) for j in ids]
+    assert all(inf.state == N.SPK_JOB_DONE for inf in infos), [inf.state for inf in infos]
+    for (gen, steps, plastic), j, inf in zip(work, ids, infos):
+        ref = Net.generate(gen)
+        ref.run_steps(steps, plastic)
+        assert ref.synchronize() == 0
+        ri, rt = ref.spikes()
+        si, stt = srv.spikes(j)
+        np.testing.assert_array_equal(si, ri)
+        np.testing.assert_array_equal(bits(stt), bits(rt))
+        assert inf.events == ref.events()
+        ref.close()
+    srv.stop()
+
+
 def test_cancel_and_stop_with_work_queued():
     work = jobs(k=5, seed=4)
     srv = Server(steps_per_block=200, reserve_bytes=1 << 30)
