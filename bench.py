@@ -65,6 +65,9 @@ def parse():
     p.add_argument("--scale", type=float, default=1.0, help="plastic_ff: network size factor (profiling cases)")
     p.add_argument("--rule", default="weight_dependent", choices=["weight_dependent", "evans"],
                    help="plastic_ff: STDP rule of the input synapses")
+    p.add_argument("--norm", default="off", choices=["off", "after", "before"],
+                   help="brunel: weight-dependent STDP on the E->E synapses with the weight normalisation "
+                        "added after or before it")
     p.add_argument("--tune-steps", type=int, default=100, help="batched: autotuner trial timesteps")
     p.add_argument("--mode", default="auto", choices=["auto", "waves", "bulk"],
                    help="batched: execution mode (auto: the autotuner's choice; waves without the autotuner); served: waves, else bulk")
@@ -90,13 +93,17 @@ def parse():
 RULES = {"weight_dependent": 0, "evans": 1}
 
 
-def build_model(workload: str, scale: float = 1.0, rule: str = "weight_dependent"):
+NORMS = {"off": 0, "after": 1, "before": 2}
+
+
+def build_model(workload: str, scale: float = 1.0, rule: str = "weight_dependent", norm: str = "off"):
     from spike_gb300 import networks
     if workload == "brunel":
-        m = networks.brunel()
-        cfg = {"workload": "brunel_12500_lif_10000_poisson_delays1-20", "neurons": 12500, "inputs": 10000,
+        m = networks.brunel(norm=NORMS[norm])
+        tag = "" if norm == "off" else f"_ee_stdp_weight_norm_{norm}"
+        cfg = {"workload": f"brunel_12500_lif_10000_poisson_delays1-20{tag}", "neurons": 12500, "inputs": 10000,
                "in_degree": 2250, "delays_steps": [1, 20], "dt_ms": 0.1, "sim_s_per_config": 2.0,
-               "plasticity": False}
+               "plasticity": norm != "off"}
         L = 1
     elif workload == "vogels_abbott":
         m = networks.vogels_abbott()
@@ -207,6 +214,10 @@ def networks_small_plastic_ff(rule: str = "weight_dependent"):
     return networks.plastic_ff_generated(n_in=2500, n_neurons=10000, ff=900, rec=100, rule=RULES[rule])
 
 
+# Per plastic synapse and timestep, the weight normalisation reads the record
+# (8 B) and the initial weight (4 B) and writes the weight back (8 B record).
+NORM_BYTES = 20
+
 # Per plastic synapse and timestep, a per-synapse-trace rule's pass reads the
 # afferent record (8 B), its delay (4 B) and its two traces (8 B) and writes
 # the weight (4 B) and the traces (8 B).
@@ -226,7 +237,7 @@ def run_reference(args, rank, world):
     """CPU reference arm: the oracle port with all host threads."""
     if rank != 0:
         return
-    m, cfg, L = build_model(args.workload, args.scale, args.rule)
+    m, cfg, L = build_model(args.workload, args.scale, args.rule, args.norm)
     threads = os.cpu_count() or 1
     from oracle import OracleNet
     from spike_gb300 import GenNetwork
@@ -285,7 +296,7 @@ def main():
     from spike_gb300 import schedule
 
     from spike_gb300 import GenNetwork, Net
-    m, cfg, L = build_model(args.workload, args.scale, args.rule)
+    m, cfg, L = build_model(args.workload, args.scale, args.rule, args.norm)
     sched = schedule(args.warps, args.tile, args.ctas, args.launch_steps or args.block)
     if isinstance(m, GenNetwork):
         net = Net.generate(m, sched)
@@ -296,7 +307,9 @@ def main():
         net = m.finalise(sched)
         n_neurons, n_inputs, n_syn = m.counts()
     trace_rule = args.workload == "plastic_ff" and args.rule != "weight_dependent"
-    plastic_run = args.workload == "plastic_ff" and not trace_rule  # the event-driven rule's traces
+    normalised = args.workload == "brunel" and args.norm != "off"
+    # the event-driven rule's traces
+    plastic_run = (args.workload == "plastic_ff" and not trace_rule) or normalised
     n_plastic = net.plastic_synapse_count()
     stream = torch.cuda.ExternalStream(net.stream())
 
@@ -343,11 +356,14 @@ def main():
                             (n_neurons + n_inputs) * timesteps if plastic_run else 0)
     if trace_rule:
         alg += TRACE_RULE_BYTES * n_plastic * timesteps
+    if normalised:
+        alg += NORM_BYTES * n_plastic * timesteps
     per_launch_s = (ms / 1000.0) / max(launches, 1)
     per_launch_bytes = alg / max(launches, 1)
     peak, peak_kind = peaks()
     achieved = per_launch_bytes / per_launch_s / 1e9
-    tr = traffic_per_launch(args.workload if not trace_rule else f"{args.workload}_{args.rule}")
+    tr = traffic_per_launch(f"{args.workload}_{args.rule}" if trace_rule else
+                            f"{args.workload}_norm_{args.norm}" if normalised else args.workload)
     traffic = None
     if tr and tr.get("traffic_per_alg_byte"):
         traffic = tr["traffic_per_alg_byte"] * per_launch_bytes
@@ -408,7 +424,9 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": ("bulk kernels of one timestep (neurons, list, per-synapse-trace rule, "
-                                    "propagation)" if trace_rule else "spk::step_kernel"),
+                                    "propagation)" if trace_rule else
+                                    "bulk kernels of one timestep (neurons, list, propagation passes, afferent "
+                                    "pass, weight normalisation)" if normalised else "spk::step_kernel"),
                          "launches": launches,
                          "alg_bytes_per_launch": per_launch_bytes, "ms_per_launch": 1000 * per_launch_s},
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clk.summary(),

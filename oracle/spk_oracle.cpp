@@ -590,20 +590,26 @@ void Net<R>::stdp_range(int64_t a, int64_t b, R t) {
 // WeightNormSTDPPlasticity::weight_normalization
 // (Spike/Backend/CUDA/Plasticity/WeightNormSTDPPlasticity.cu:74-176): per post,
 // the change of its afferents' sum of squares against their initial weights,
-// (w - w0)^2 + 2 w0 (w - w0) over the afferents whose weight moved, summed in
-// creation order (the reference adds them with atomicAdd, in no fixed order);
-// divisor sqrt(S + change) / sqrt(S); the weights divided when it is not 1.
+// (w - w0)^2 + 2 w0 (w - w0) over the afferents whose weight moved; divisor
+// sqrt(S + change) / sqrt(S); the weights divided when it is not 1.  The
+// reference adds the terms with atomicAdd, in no fixed order; the fixed order
+// here: partial sum j takes the terms of afferents j, j + 32, j + 64, ... (in
+// creation order) in turn, then the 32 partials meet in a pairwise tree
+// (j with j + 16, then + 8, + 4, + 2, + 1).
 template <typename R>
 void Net<R>::normalise_weights() {
   for (int q = 0; q < N; ++q) {
     const int64_t a0 = norm_ptr[q], a1 = norm_ptr[q + 1];
     if (a0 == a1) continue;  // not in the rule's set
-    R upd = 0;
+    R part[32] = {};
     for (int64_t j = a0; j < a1; ++j) {
       const R w0 = norm_w0[j];
       const R dw = sw[norm_pos[j]] - w0;
-      if (dw != (R)0) upd += dw * dw + (R)2 * w0 * dw;
+      if (dw != (R)0) part[(j - a0) % 32] += dw * dw + (R)2 * w0 * dw;
     }
+    for (int o = 16; o >= 1; o >>= 1)
+      for (int i = 0; i < o; ++i) part[i] = part[i] + part[i + o];
+    const R upd = part[0];
     const R div = std::sqrt(norm_S[q] + upd) / std::sqrt(norm_S[q]);
     if (div != (R)1)
       for (int64_t j = a0; j < a1; ++j) sw[norm_pos[j]] = sw[norm_pos[j]] / div;

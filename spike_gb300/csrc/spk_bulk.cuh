@@ -1005,9 +1005,12 @@ __global__ void __launch_bounds__(256) bulk_dense_stdp_kernel(const NetDev* __re
 // WeightNormSTDPPlasticity::weight_normalization (WeightNormSTDPPlasticity.cu:
 // 74-176), in one warp per post: the change of the post's sum of squared
 // plastic weights against their initial weights, (w - w0)^2 + 2 w0 (w - w0)
-// over the afferents whose weight moved, added in record (creation) order
-// (the reference's atomicAdd gives no fixed order), the divisor
-// sqrtf(S + change) / sqrtf(S), and the weights divided when it is not 1.
+// over the afferents whose weight moved, the divisor sqrtf(S + change) /
+// sqrtf(S), and the weights divided when it is not 1.  The reference adds the
+// terms with atomicAdd, in no fixed order; here the order is fixed: lane j
+// adds the terms of records j, j + 32, j + 64, ... (record = creation order)
+// in turn, then the 32 partial sums meet in a pairwise tree (lane i with lane
+// i + 16, then + 8, + 4, + 2, + 1), which every lane evaluates alike.
 // `slot` picks the networks whose normalisation runs at this point of the
 // timestep (0 before the rule, 1 after the per-synapse-trace pass, 2 after the
 // event-driven rule's weight-update pass).
@@ -1030,27 +1033,19 @@ __global__ void __launch_bounds__(256) bulk_norm_kernel(const NetDev* __restrict
     if (!st.live || !c.plastic) continue;
     const int a0 = __ldg(d.csc_ptr + item.post), a1 = __ldg(d.csc_ptr + item.post + 1);
     if (a0 == a1) continue;  // not in the rule's set
+    const float* const w0s = d.norm_w0;
+    const uint2* const csc = d.csc;
     float upd = 0.0f;
-    for (int a = a0; a < a1; a += 32) {
-      const int ai = a + lane;
-      float term = 0.0f;
-      bool moved = false;
-      if (ai < a1) {
-        const float w0 = d.norm_w0[ai];
-        const float dw = __uint_as_float(d.csc[ai].y) - w0;
-        if (dw != 0.0f) {
-          term = dw * dw + 2.0f * w0 * dw;
-          moved = true;
-        }
-      }
-      // every lane adds the terms in lane order, so all hold the same sum
-      unsigned m = __ballot_sync(FULL, moved);
-      while (m) {
-        const int src = __ffs(m) - 1;
-        m &= m - 1;
-        upd += __shfl_sync(FULL, term, src);
-      }
+#pragma unroll 4
+    for (int a = a0 + lane; a < a1; a += 32) {
+      const float w0 = w0s[a];
+      const float dw = __uint_as_float(csc[a].y) - w0;
+      if (dw != 0.0f) upd += dw * dw + 2.0f * w0 * dw;
     }
+    // lane i + o's partial joins lane i's (and, addition being commutative,
+    // lane i's joins lane i + o's): all lanes end with the tree's sum
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) upd += __shfl_xor_sync(FULL, upd, o);
     const float sum = d.norm_sum[item.post];
     const float div = sqrtf(sum + upd) / sqrtf(sum);
     if (div != 1.0f)

@@ -52,13 +52,21 @@ def vogels_abbott(n_exc: int = 3200, n_inh: int = 800, p: float = 0.02, delay_st
 def brunel(n_exc: int = 10000, n_inh: int = 2500, n_in: int = 10000, rate: float = 20.0,
            sparseness: float = 0.1, g: float = 5.0, J: float = 0.1e-3, d_max: int = 20,
            plastic: bool = False, stdp: STDPParams | None = None, philox_seed: int = 42,
-           synapse_seed: int = 42) -> Model:
+           synapse_seed: int = 42, norm: int = N.SPK_NORM_OFF) -> Model:
+    """Examples/Brunel10K.cpp through the model API; with `plastic` the E->E
+    synapses follow the weight-dependent rule, and with `norm` also the
+    weight normalisation, added after (SPK_NORM_AFTER_RULE) or before it."""
     m = Model(N.SPK_SYN_VOLTAGE, N.SPK_INPUT_POISSON, synapse_seed=synapse_seed, timestep=DT,
               philox_seed=philox_seed)
-    rule = -1
+    rule = nrule = -1
+    plastic = plastic or norm != N.SPK_NORM_OFF
+    if norm == N.SPK_NORM_BEFORE_RULE:
+        nrule = m.add_weight_norm_rule()
     if plastic:
         rule = m.add_stdp_rule(stdp or STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02,
                                                   tau_minus=0.02, lambda_=1.0, alpha=1.0, w_max=1.0))
+    if norm == N.SPK_NORM_AFTER_RULE:
+        nrule = m.add_weight_norm_rule()
     common = dict(somatic_capacitance_Cm=200.0e-12, somatic_leakage_conductance_g0=10.0e-9,
                   resting_potential_v0=0.0, after_spike_reset_potential_vreset=0.0,
                   absolute_refractory_period=2.0e-3, threshold_for_action_potential_spike=20.0e-3,
@@ -74,7 +82,7 @@ def brunel(n_exc: int = 10000, n_inh: int = 2500, n_in: int = 10000, rate: float
     m.connect_with_sparsity(inp, i, sparseness, ext)
     m.connect_with_sparsity(e, i, sparseness, exc)
     exc_plastic = SynapseParams(weight_range=(J, J), weight_scaling_constant=1.0, delay_range=delays,
-                                plasticity_rule=rule)
+                                plasticity_rule=rule, plasticity_rule_2=nrule)
     m.connect_with_sparsity(e, e, sparseness, exc_plastic)
     m.connect_with_sparsity(i, e, sparseness, inh)
     m.connect_with_sparsity(i, i, sparseness, inh)

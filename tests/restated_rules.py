@@ -46,9 +46,11 @@ class Normaliser:
     order): S per post is the sum of powf(w, 2) over its plastic afferents in
     that order (WeightNormSTDPPlasticity.cpp:52-58); each step the change
     (w - w0)^2 + 2 w0 (w - w0) of the afferents whose weight moved is summed
-    per post in creation order (the order the engine fixes for the
-    reference's atomicAdd), the divisor is sqrt(S + change) / sqrt(S), and the
-    weights are divided when it is not 1 (WeightNormSTDPPlasticity.cu:101-176)."""
+    per post in the order the engine fixes for the reference's atomicAdd
+    (partial sum j over afferents j, j + 32, ... in creation order, then a
+    pairwise tree over the 32 partials: j + 16, + 8, + 4, + 2, + 1), the
+    divisor is sqrt(S + change) / sqrt(S), and the weights are divided when it
+    is not 1 (WeightNormSTDPPlasticity.cu:101-176)."""
 
     def __init__(self, post_of_plastic, w0, n_posts, sums=None):
         f32 = np.float32
@@ -57,7 +59,7 @@ class Normaliser:
         order = np.argsort(posts, kind="stable")  # creation order within each post
         counts = np.bincount(posts, minlength=n_posts)
         self.posts = np.nonzero(counts)[0]
-        width = counts.max()
+        width = -(-counts.max() // 32) * 32  # whole rows of 32 partial sums
         self.slot = np.full((len(self.posts), width), -1, np.int64)
         row = np.searchsorted(self.posts, posts[order])
         start = np.concatenate(([0], np.cumsum(counts[self.posts])[:-1]))
@@ -75,10 +77,15 @@ class Normaliser:
         w0 = self.w0 if w0 is None else w0
         dw = wp - w0
         term = np.where(dw != 0, dw * dw + f32(2) * w0 * dw, f32(0)).astype(f32)
-        upd = np.zeros(len(self.posts), f32)
-        for k in range(self.slot.shape[1]):
-            col = self.slot[:, k]
-            upd = upd + np.where(col >= 0, term[np.maximum(col, 0)], f32(0))
+        part = np.zeros((len(self.posts), 32), f32)
+        for k in range(self.slot.shape[1] // 32):
+            cols = self.slot[:, 32 * k:32 * (k + 1)]
+            part = part + np.where(cols >= 0, term[np.maximum(cols, 0)], f32(0))
+        o = 16
+        while o >= 1:
+            part = part[:, :o] + part[:, o:2 * o]
+            o //= 2
+        upd = part[:, 0]
         div = np.sqrt(self.S + upd) / np.sqrt(self.S)
         dv = div[self.row_of]
         return np.where(dv != f32(1), wp / dv, wp).astype(f32)
