@@ -2960,7 +2960,8 @@ static int policy_schedules(const spk_gen_desc* descs, int n, const TunePolicy& 
 }
 
 // Times `steps` timesteps of the networks under schedules `sch` as one batch,
-// in waves mode (ms[0]) and in bulk mode (ms[1]).
+// in waves mode (ms[0]) and in bulk mode (ms[1]); ms[0] stays negative when a
+// network runs in bulk mode only (a per-synapse-trace rule).
 static int trial_policy(const spk_gen_desc* descs, int n, const std::vector<spk_schedule>& sch, int steps,
                         float* ms) {
   std::vector<spk_net*> nets(n, nullptr);
@@ -2976,7 +2977,13 @@ static int trial_policy(const spk_gen_desc* descs, int n, const std::vector<spk_
   if (rc == SPK_OK) rc = spk_batch_create(nets.data(), n, &bs, &b);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (rc == SPK_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) rc = SPK_ERR_CUDA;
+  bool bulk_only = false;
+  for (int i = 0; i < n && rc == SPK_OK; ++i) bulk_only = bulk_only || nets[i]->bulk_only();
   for (int mode = SPK_BATCH_WAVES; mode <= SPK_BATCH_BULK && rc == SPK_OK; ++mode) {
+    if (mode == SPK_BATCH_WAVES && bulk_only) {
+      ms[mode] = -1.0f;
+      continue;
+    }
     rc = spk_batch_set_mode(b, mode);
     if (rc == SPK_OK) rc = spk_batch_run_steps(b, steps, 1);  // warm-up (and graph capture)
     if (rc == SPK_OK && cudaStreamSynchronize(b->stream) != cudaSuccess) rc = SPK_ERR_CUDA;
@@ -3047,12 +3054,12 @@ extern "C" int spk_batch_autotune(const spk_gen_desc* descs, int32_t n_nets, int
     int last_rc = SPK_ERR_UNSUPPORTED;
     for (const TunePolicy& pol : policies) {
       if (policy_schedules(descs, n_nets, pol, di, sch) != SPK_OK) continue;
-      float ms[2] = {0.0f, 0.0f};
+      float ms[2] = {-1.0f, -1.0f};
       last_rc = trial_policy(descs, n_nets, sch, trial_steps, ms);
       if (last_rc == SPK_ERR_TIMEOUT || last_rc == SPK_ERR_CUDA) return last_rc;
       if (last_rc != SPK_OK) continue;
       for (int m = SPK_BATCH_WAVES; m <= SPK_BATCH_BULK; ++m)
-        if (best < 0.0f || ms[m] < best) {
+        if (ms[m] >= 0.0f && (best < 0.0f || ms[m] < best)) {
           best = ms[m];
           best_sch = sch;
           mode = m;

@@ -25,6 +25,27 @@ def snapshot(net: Net, n: int, n_in: int, S: int):
                 last=bits(net.state(N.SPK_FIELD_LAST_SPIKE, n)), w=bits(net.weights(S)), ev=net.events())
 
 
+def test_autotune_with_a_trace_rule_instance_picks_bulk_mode():
+    """A sweep holding an Evans-rule instance (bulk mode only) is tuned over
+    bulk-mode trials alone, and the tuned batch equals each instance alone."""
+    gens = [sweep_instance(n, 0.04, 5.0, plastic, seed=80 + i, d_max=6, rule=rule)
+            for i, (n, plastic, rule) in enumerate(((900, True, N.SPK_STDP_EVANS), (2000, True, 0), (600, False, 0)))]
+    scheds, ms, mode = Batch.autotune(gens, trial_steps=40, with_mode=True)
+    assert mode == N.SPK_BATCH_BULK and ms > 0
+    nets = [Net.generate(g, s) for g, s in zip(gens, scheds)]
+    b = Batch(nets)
+    b.run_steps(300, True)
+    assert b.synchronize() == 0
+    for g, net in zip(gens, nets):
+        ref = Net.generate(g)
+        ref.run_steps(300, True)
+        assert ref.synchronize() == 0
+        np.testing.assert_array_equal(net.spikes()[0], ref.spikes()[0])
+        assert net.events() == ref.events()
+        ref.close()
+    b.close()
+
+
 def test_autotuned_batch_equals_each_instance_alone():
     gens = small_sweep()
     scheds, ms, costs, mode = Batch.autotune(gens, trial_steps=60, costs=True, with_mode=True)
