@@ -515,9 +515,12 @@ __host__ __device__ inline BulkPropLayout bulk_prop_layout(int win_words, int ts
 #define SPK_BULK_PROP_MINB 3
 #endif
 
+// kPass: 0 the single fused pass; 1 and 2 the two passes of a batch in which
+// a network normalises its weights after the event-driven rule (see below).
+template <int kPass>
 __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
     bulk_prop_kernel(const NetDev* __restrict__ nets, const BulkPropBlock* __restrict__ blocks, int s, int win_words,
-                     int ts_max, int pass) {
+                     int ts_max) {
   extern __shared__ __align__(16) uint32_t bsm[];
   __shared__ __align__(16) NetDev sd;
   __shared__ RunCtl sctl;
@@ -539,18 +542,20 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
   if (!st.live || n_list == 0) return;  // the whole CTA
   // A network that normalises its weights after the event-driven rule's
   // updates takes two passes: the first (pass 1) only updates weights, the
-  // second (pass 2, after the normalisation) only delivers.  Pass 0 does both;
-  // pass 2 skips the other networks.
+  // second (pass 2, after the normalisation) only delivers.  Pass 1 does both
+  // for the other networks of the batch; pass 2 skips them.
   uint32_t kmask = 0xffffffffu;
-  if (pass != 0 && d.weight_norm == SPK_NORM_AFTER_RULE && d.has_stdp && d.stdp_rule == SPK_STDP_WEIGHT_DEPENDENT) {
-    if (pass == 1) {
+  if constexpr (kPass != 0) {
+    const bool split =
+        d.weight_norm == SPK_NORM_AFTER_RULE && d.has_stdp && d.stdp_rule == SPK_STDP_WEIGHT_DEPENDENT;
+    if (!split) {
+      if (kPass == 2) return;
+    } else if (kPass == 1) {
       kmask = ~(1u << 31);
     } else {
       kmask = ~(1u << 30);
       st.stdp_run = false;
     }
-  } else if (pass == 2) {
-    return;
   }
   const BulkPropLayout wl = bulk_prop_layout(win_words, ts_max);
   uint32_t* list_s = bsm + wl.list;

@@ -2100,16 +2100,16 @@ static int bulk_launch_block(spk_batch* b) {
       SPK_CUDA(cudaEventRecord(b->join, b->side));
       ++per_step;
     }
-    SPK_CUDA(launch_overlapped(bulk_prop_kernel, b->pblocks_total, BULK_PROP_WARPS * 32, (size_t)prop_smem,
-                               b->stream, (const NetDev*)b->dd, (const BulkPropBlock*)b->dpblocks, s, b->win_words,
-                               b->ts_max, split ? 1 : 0));
+    SPK_CUDA(launch_overlapped(split ? bulk_prop_kernel<1> : bulk_prop_kernel<0>, b->pblocks_total,
+                               BULK_PROP_WARPS * 32, (size_t)prop_smem, b->stream, (const NetDev*)b->dd,
+                               (const BulkPropBlock*)b->dpblocks, s, b->win_words, b->ts_max));
     ++per_step;
     if (b->any_plastic) SPK_CUDA(cudaStreamWaitEvent(b->stream, b->join, 0));
     if (split) {
       bulk_norm_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s, 2);
-      SPK_CUDA(launch_overlapped(bulk_prop_kernel, b->pblocks_total, BULK_PROP_WARPS * 32, (size_t)prop_smem,
+      SPK_CUDA(launch_overlapped(bulk_prop_kernel<2>, b->pblocks_total, BULK_PROP_WARPS * 32, (size_t)prop_smem,
                                  b->stream, (const NetDev*)b->dd, (const BulkPropBlock*)b->dpblocks, s,
-                                 b->win_words, b->ts_max, 2));
+                                 b->win_words, b->ts_max));
       per_step += 2;
     }
   }
@@ -2320,8 +2320,10 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
         SPK_CUDA(cudaMemset(n->hd.bitsP, 0, sizeof(uint32_t) * 2 * (size_t)n->hd.n_words));
       }
       SPK_CUDA(cudaMemcpy(b->dd, b->hds.data(), sizeof(NetDev) * b->hds.size(), cudaMemcpyHostToDevice));
-      SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    bulk_prop_layout(b->win_words, b->ts_max).total * 4));
+      const int prop_smem = bulk_prop_layout(b->win_words, b->ts_max).total * 4;
+      SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, prop_smem));
+      SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, prop_smem));
+      SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, prop_smem));
     }
     b->mode = mode;
     return SPK_OK;
