@@ -356,11 +356,14 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
 int spk_batch_run_steps(spk_batch* batch, int64_t n_steps, int32_t plasticity_on);
 /* Execution mode of a batch.  WAVES (default): the persistent step kernel,
  * each network's state in shared memory for a whole launch, networks packed
- * into co-resident waves.  BULK: every timestep is three kernels over all
+ * into co-resident waves.  BULK: every timestep is a few kernels over all
  * tiles of all networks (neurons, the step's key lists, propagation with
- * STDP), state in HBM, kernel boundaries as the only synchronization,
- * captured in a CUDA graph per block; it suits batches whose networks do not
- * fit the GPU's shared memory at once.  Both modes give the same bits. */
+ * STDP, the afferent pass, and the per-synapse-trace rules' and weight
+ * normalisation's passes where a network has them), state in HBM, kernel
+ * boundaries as the only synchronization, captured in a CUDA graph per block;
+ * it suits batches whose networks do not fit the GPU's shared memory at once,
+ * and networks with a per-synapse-trace rule or the weight normalisation run
+ * in it only.  Both modes give the same bits. */
 #define SPK_BATCH_WAVES 0
 #define SPK_BATCH_BULK 1
 int spk_batch_set_mode(spk_batch* batch, int32_t mode);
