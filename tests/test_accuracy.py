@@ -111,14 +111,22 @@ def test_conductance_network_against_fp64():
     assert abs(cv_g - cv_o) <= CV_TOL
 
 
-def test_plastic_network_against_fp64():
+@pytest.mark.parametrize("rule", ["weight_dependent", "evans", "weight_dependent_normalised"])
+def test_plastic_network_against_fp64(rule):
     """600 voltage-synapse neurons (480 E, 120 I) with 300 Poisson inputs whose
-    synapses are plastic (weights U(0, 1) at scale 5 mV, weight-dependent
-    STDP), for 0.5 s."""
+    synapses are plastic (weights U(0, 1) at scale 5 mV), for 0.5 s, under
+    weight-dependent STDP, the Evans rule, or weight-dependent STDP with the
+    weight normalisation after it."""
     from test_generate import STDP, desc_from_oracle, small_gen
-    gen = small_gen()
+    from spike_gb300.networks import EVANS_STDP
+    if rule == "evans":
+        gen = small_gen(rule=N.SPK_STDP_EVANS, stdp_params=EVANS_STDP)
+    else:
+        gen = small_gen()
     arrays = generate_synapses(gen.desc)
     d = desc_from_oracle(gen, arrays)
+    if rule == "weight_dependent_normalised":
+        d.desc.weight_norm = N.SPK_NORM_AFTER_RULE
     n = 600
     net = Net.from_desc(d.desc)
     o = OracleNet(d.desc, 64)
@@ -141,7 +149,7 @@ def test_plastic_network_against_fp64():
     hg, _ = np.histogram(wg[plastic], bins=20, range=(0.0, STDP.w_max))
     ho, _ = np.histogram(wo[plastic], bins=20, range=(0.0, STDP.w_max))
     l1 = float(np.abs(hg / hg.sum() - ho / ho.sum()).sum())
-    print(json.dumps({"case": "plastic_voltage_600_0.5s", "rasters_agree_steps": h, "errors_at_horizon": err,
+    print(json.dumps({"case": f"plastic_voltage_600_0.5s_{rule}", "rasters_agree_steps": h, "errors_at_horizon": err,
                       "rate_hz": [rate_g, rate_o], "isi_cv": [cv_g, cv_o], "weight_hist_l1": l1,
                       "mean_weight": [float(wg[plastic].mean()), float(wo[plastic].mean())]}))
     assert abs(rate_g - rate_o) <= RATE_TOL * rate_o
