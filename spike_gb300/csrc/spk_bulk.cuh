@@ -326,6 +326,12 @@ constexpr int BULK_LIST_THREADS = 512;
 struct BulkPostItem {
   int net, post;
 };
+// Work item of the per-synapse-trace rules' and the normalisation's passes: a
+// post with plastic afferents and the range [a0, a1) of its records, fixed
+// when the batch is set up.
+struct BulkRuleItem {
+  int net, post, a0, a1;
+};
 constexpr int BULK_POST_CHUNK = 128;  // afferents per warp iteration (32 lanes x 4)
 
 __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetDev* __restrict__ nets, int s,
@@ -946,19 +952,23 @@ __device__ __forceinline__ void dense_rule_update(const NetDev& d, float dt, boo
 constexpr int DENSE_RECS = 4;
 
 __global__ void __launch_bounds__(256) bulk_dense_stdp_kernel(const NetDev* __restrict__ nets,
-                                                              const BulkPostItem* __restrict__ items, int n_items,
+                                                              const BulkRuleItem* __restrict__ items, int n_items,
                                                               int s) {
   const int lane = threadIdx.x & 31;
   const int n_warps = gridDim.x * (blockDim.x >> 5);
+  int cached = -1;  // the network whose step the warp holds (items come network by network)
+  BulkStep st{};
   for (int it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < n_items; it += n_warps) {
-    const BulkPostItem item = items[it];
+    const BulkRuleItem item = items[it];
     const NetDev& d = nets[item.net];
-    const RunCtl c = load_ctl(d.ctl);
-    const BulkStep st = bulk_step(d, c, s);
+    if (item.net != cached) {
+      st = bulk_step(d, load_ctl(d.ctl), s);
+      cached = item.net;
+    }
     if (!st.live || !st.dense_run) continue;
     const int key = d.KL + item.post;
     const bool post_sp = ((d.bitsA[key >> 5] >> (key & 31)) & 1u) != 0;
-    const int a0 = __ldg(d.csc_ptr + item.post), a1 = __ldg(d.csc_ptr + item.post + 1);
+    const int a0 = item.a0, a1 = item.a1;
     const float dt = d.dt;
     const int H = d.H, n_words = d.n_words;
     // (T - delay) mod H from T mod H: delays are 1..H-1, so one wrap at most
@@ -1025,19 +1035,25 @@ __device__ __forceinline__ int norm_slot_of(const NetDev& d) {
 }
 
 __global__ void __launch_bounds__(256) bulk_norm_kernel(const NetDev* __restrict__ nets,
-                                                        const BulkPostItem* __restrict__ items, int n_items, int s,
+                                                        const BulkRuleItem* __restrict__ items, int n_items, int s,
                                                         int slot) {
   const int lane = threadIdx.x & 31;
   const int n_warps = gridDim.x * (blockDim.x >> 5);
+  int cached = -1;  // the network whose step the warp holds (items come network by network)
+  bool run = false;
   for (int it = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); it < n_items; it += n_warps) {
-    const BulkPostItem item = items[it];
+    const BulkRuleItem item = items[it];
     const NetDev& d = nets[item.net];
-    if (d.weight_norm == SPK_NORM_OFF || !d.has_stdp || norm_slot_of(d) != slot) continue;
-    const RunCtl c = load_ctl(d.ctl);
-    const BulkStep st = bulk_step(d, c, s);
-    if (!st.live || !c.plastic) continue;
-    const int a0 = __ldg(d.csc_ptr + item.post), a1 = __ldg(d.csc_ptr + item.post + 1);
-    if (a0 == a1) continue;  // not in the rule's set
+    if (item.net != cached) {
+      run = false;
+      if (d.weight_norm != SPK_NORM_OFF && d.has_stdp && norm_slot_of(d) == slot) {
+        const RunCtl c = load_ctl(d.ctl);
+        run = bulk_step(d, c, s).live && c.plastic;
+      }
+      cached = item.net;
+    }
+    if (!run) continue;
+    const int a0 = item.a0, a1 = item.a1;
     const float* const w0s = d.norm_w0;
     const uint2* const csc = d.csc;
     float upd = 0.0f;

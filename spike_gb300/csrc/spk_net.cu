@@ -258,7 +258,8 @@ struct spk_batch {
   BulkBlock* dblocks = nullptr;  // [blocks_total] blocks of 32-key words with real keys
   int blocks_total = 0;
   BulkPostItem* items = nullptr; // afferent-pass work list of a timestep
-  BulkPostItem* dense_items = nullptr;  // posts of the per-synapse-trace-rule and normalised networks
+  BulkRuleItem* dense_items = nullptr;  // posts with plastic afferents of the per-synapse-trace-rule
+                                        // and normalised networks
   int n_dense_items = 0;
   bool any_dense = false;       // a network with a per-synapse-trace rule
   int norm_slots = 0;           // bit k: a network normalises its weights in slot k (spk_net::norm_slot)
@@ -2081,15 +2082,15 @@ static int bulk_launch_block(spk_batch* b) {
     SPK_CUDA(launch_overlapped(bulk_list_kernel, n, BULK_LIST_THREADS, 0, b->stream, (const NetDev*)b->dd, s,
                                b->items, b->item_count, b->item_cap));
     per_step += 2;
-    if (b->norm_slots & 1) {
+    if ((b->norm_slots & 1) && b->n_dense_items) {
       bulk_norm_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s, 0);
       ++per_step;
     }
-    if (b->any_dense) {
+    if (b->any_dense && b->n_dense_items) {
       bulk_dense_stdp_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s);
       ++per_step;
     }
-    if (b->norm_slots & 2) {
+    if ((b->norm_slots & 2) && b->n_dense_items) {
       bulk_norm_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s, 1);
       ++per_step;
     }
@@ -2106,11 +2107,14 @@ static int bulk_launch_block(spk_batch* b) {
     ++per_step;
     if (b->any_plastic) SPK_CUDA(cudaStreamWaitEvent(b->stream, b->join, 0));
     if (split) {
-      bulk_norm_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s, 2);
+      if (b->n_dense_items) {
+        bulk_norm_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s, 2);
+        ++per_step;
+      }
       SPK_CUDA(launch_overlapped(bulk_prop_kernel<2>, b->pblocks_total, BULK_PROP_WARPS * 32, (size_t)prop_smem,
                                  b->stream, (const NetDev*)b->dd, (const BulkPropBlock*)b->dpblocks, s,
                                  b->win_words, b->ts_max));
-      per_step += 2;
+      ++per_step;
     }
   }
   bulk_finish_kernel<<<(n + 255) / 256, 256, 0, b->stream>>>(b->dd, n, b->K);
@@ -2246,7 +2250,7 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       // posts of the networks with a per-synapse-trace rule or the weight
       // normalisation: the per-post passes
       {
-        std::vector<BulkPostItem> dense;
+        std::vector<BulkRuleItem> dense;
         b->any_dense = false;
         b->norm_slots = 0;
         for (size_t i = 0; i < b->nets.size(); ++i) {
@@ -2254,16 +2258,21 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
           if (!x->bulk_only()) continue;
           b->any_dense = b->any_dense || x->dense();
           if (x->weight_norm != SPK_NORM_OFF) b->norm_slots |= 1 << x->norm_slot();
-          for (int q = 0; q < x->N; ++q) dense.push_back(BulkPostItem{(int)i, q});
+          // the record ranges (uploaded or generated on the network's stream)
+          std::vector<int32_t> cp((size_t)x->N + 1);
+          SPK_CUDA(cudaStreamSynchronize(x->stream));
+          SPK_CUDA(cudaMemcpy(cp.data(), x->hd.csc_ptr, sizeof(int32_t) * cp.size(), cudaMemcpyDeviceToHost));
+          for (int q = 0; q < x->N; ++q)
+            if (cp[q + 1] > cp[q]) dense.push_back(BulkRuleItem{(int)i, q, cp[q], cp[q + 1]});
         }
         if (!dense.empty()) {
-          if (cudaMalloc(&b->dense_items, sizeof(BulkPostItem) * dense.size()) != cudaSuccess) {
+          if (cudaMalloc(&b->dense_items, sizeof(BulkRuleItem) * dense.size()) != cudaSuccess) {
             cudaGetLastError();
             b->dense_items = nullptr;
             set_error("bulk mode: device allocation failed");
             return SPK_ERR_OOM;
           }
-          SPK_CUDA(cudaMemcpy(b->dense_items, dense.data(), sizeof(BulkPostItem) * dense.size(),
+          SPK_CUDA(cudaMemcpy(b->dense_items, dense.data(), sizeof(BulkRuleItem) * dense.size(),
                               cudaMemcpyHostToDevice));
           b->n_dense_items = (int)dense.size();
         }
