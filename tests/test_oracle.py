@@ -111,9 +111,20 @@ def test_poisson_first_draw_emits_no_spike_and_rate():
     assert abs(rate - 50.0) < 2.0
 
 
-def test_threaded_oracle_is_bit_identical():
-    d = descs.random_voltage_net(n=240, n_in=160, plastic=True,
-                                 stdp=STDPParams(a_plus=0.005, a_minus=0.00525, lambda_=1.0, alpha=1.0, w_max=1.0))
+WD_PARAMS = STDPParams(a_plus=0.005, a_minus=0.00525, lambda_=1.0, alpha=1.0, w_max=1.0)
+EVANS_PARAMS = STDPParams(a_plus=0.5, a_minus=0.5, tau_plus=0.004, tau_minus=0.005, lambda_=0.0, alpha=0.0, w_max=1.0)
+
+
+@pytest.mark.parametrize("rule,sp,norm", [
+    (N.SPK_STDP_WEIGHT_DEPENDENT, WD_PARAMS, N.SPK_NORM_OFF),
+    (N.SPK_STDP_WEIGHT_DEPENDENT, WD_PARAMS, N.SPK_NORM_AFTER_RULE),
+    (N.SPK_STDP_EVANS, EVANS_PARAMS, N.SPK_NORM_BEFORE_RULE),
+])
+def test_threaded_oracle_is_bit_identical(rule, sp, norm):
+    """Post-range threads (with the barriers around the normalisation) give
+    the single thread's bits, for the event-driven rule, the normalisation
+    after it, and a trace rule with the normalisation before it."""
+    d = descs.random_voltage_net(n=240, n_in=160, plastic=True, stdp=sp, stdp_rule=rule, weight_norm=norm)
     a = OracleNet(d.desc)
     b = OracleNet(d.desc, threads=4)
     a.run(0.05)
