@@ -74,7 +74,7 @@ Built build(bool evans) {
   ext.delay_range[1] = 0.002f;
   ext.weight_range[0] = evans ? 0.0f : J;
   ext.weight_range[1] = evans ? 1.0f : J;
-  ext.weight_scaling_constant = evans ? J : 1.0f;
+  ext.weight_scaling_constant = evans ? 2.5f * J : 1.0f;
   if (evans) ext.plasticity_vec.push_back(stdp);
   model->AddSynapseGroup(gin, ge, &ext);
   model->AddSynapseGroup(gin, gi, &ext);
