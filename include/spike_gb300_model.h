@@ -86,7 +86,8 @@ int spk_model_add_input_group(spk_model* m, int32_t shape0, int32_t shape1, floa
 int spk_model_add_stimulus(spk_model* m, const float* rates, int32_t n, int32_t* stimulus_id);
 int spk_model_add_stdp_rule(spk_model* m, const spk_stdp_params* p, int32_t* rule_id);
 /* Any of the SPK_STDP_* rules, its parameters in the descriptor's field
- * mapping (spike_gb300.h); one rule per model. */
+ * mapping (spike_gb300.h); one STDP rule per model (the weight normalisation,
+ * spk_model_add_weight_norm_rule, may go beside it). */
 int spk_model_add_plasticity_rule(spk_model* m, int32_t rule, const spk_stdp_params* p, int32_t* rule_id);
 /* WeightNormSTDPPlasticity (Spike/Plasticity/WeightNormSTDPPlasticity.hpp):
  * weightnorm_stdp_plasticity_parameters_struct's settarget and target.  Its
