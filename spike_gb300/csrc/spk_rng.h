@@ -59,7 +59,9 @@ SPK_HD u32x4 philox_round(u32x4 c, uint32_t k0, uint32_t k1) {
 // rounds.
 SPK_HD u32x4 philox4x32_10(u32x4 ctr, uint32_t k0, uint32_t k1) {
   const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#ifdef __CUDACC__
 #pragma unroll
+#endif
   for (int r = 0; r < 10; ++r) {
     ctr = philox_round(ctr, k0, k1);
     k0 += W0;
