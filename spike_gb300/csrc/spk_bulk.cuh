@@ -948,10 +948,12 @@ __device__ __forceinline__ void dense_rule_update(const NetDev& d, float dt, boo
 }
 
 // Records per lane in flight: the pass is bound by HBM latency as much as
-// by bandwidth (a record's history word depends on its key and delay).
+// by bandwidth (a record's history word depends on its key and delay).  With
+// four blocks of 256 threads per SM (64 registers) the kernel keeps 32 warps
+// per SM; at 70 registers it had 24.
 constexpr int DENSE_RECS = 4;
 
-__global__ void __launch_bounds__(256) bulk_dense_stdp_kernel(const NetDev* __restrict__ nets,
+__global__ void __launch_bounds__(256, 4) bulk_dense_stdp_kernel(const NetDev* __restrict__ nets,
                                                               const BulkRuleItem* __restrict__ items, int n_items,
                                                               int s) {
   const int lane = threadIdx.x & 31;
