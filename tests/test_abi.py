@@ -86,3 +86,22 @@ def test_malformed_generated_networks_are_rejected_before_any_device_call():
         assert lib.spk_net_generate(ctypes.byref(gen.desc), None, ctypes.byref(h)) == _native.SPK_ERR_INVALID
         assert lib.spk_last_error()
     assert lib.spk_net_generate(None, None, None) == _native.SPK_ERR_INVALID
+
+
+def test_rule_fields_are_validated_before_any_device_call():
+    """An unknown STDP rule or normalisation mode, or a normalisation without
+    an STDP rule, is refused by spk_net_create before it touches a device."""
+    import descs
+    from spike_gb300.model import STDPParams
+    lib = _native.lib()
+    sp = STDPParams()
+    cases = [dict(plastic=True, stdp=sp, stdp_rule=9), dict(plastic=True, stdp=sp, weight_norm=7),
+             dict(plastic=True, stdp=sp, stdp_rule=-1), dict(weight_norm=_native.SPK_NORM_BEFORE_RULE)]
+    for kw in cases:
+        d = descs.random_voltage_net(n=40, n_in=10, **kw)
+        h = ctypes.c_void_p()
+        assert lib.spk_net_create(ctypes.byref(d.desc), None, ctypes.byref(h)) == _native.SPK_ERR_INVALID, kw
+        assert lib.spk_last_error()
+    # the weight-norm entry point of the model API needs a model
+    assert lib.spk_model_add_weight_norm_rule(None, 0, ctypes.c_float(0.0), None) == _native.SPK_ERR_INVALID
+    assert lib.spk_net_plastic_synapse_count(None, None) == _native.SPK_ERR_INVALID
