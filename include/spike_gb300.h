@@ -533,7 +533,10 @@ int spk_net_generate_estimate(const spk_gen_desc* desc, const spk_schedule* sche
  * clears the parts that must start at zero, so calls whose work overlaps on
  * the GPU (different streams, or different host threads on one device) race
  * and must be serialized by the caller.  Networks whose scratch exceeds
- * SPK_NOALLOC_SCRATCH_BYTES are rejected with SPK_ERR_INVALID. */
+ * SPK_NOALLOC_SCRATCH_BYTES are rejected with SPK_ERR_INVALID.  Plasticity
+ * here is the weight-dependent rule (the persistent kernel's); the
+ * per-synapse-trace rules and the weight normalisation need a network from
+ * spk_net_create. */
 #define SPK_NOALLOC_SCRATCH_BYTES (4u << 20)
 #define SPK_RUN_STATE_BYTES 128
 
