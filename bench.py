@@ -188,6 +188,19 @@ class ClockSampler:
         return out
 
 
+def aggregate_over_ranks(elapsed_s: float, events: int, dist, device: str):
+    """Whole-job timing of replicas: the slowest rank's time and the events
+    of all ranks (each rank simulates its own networks; no data-path
+    exchange).  `dist` is torch.distributed or None for one process."""
+    import torch
+    el = torch.tensor([float(elapsed_s)], device=device, dtype=torch.float64)
+    ev = torch.tensor([float(events)], device=device, dtype=torch.float64)
+    if dist:
+        dist.all_reduce(el, op=dist.ReduceOp.MAX)
+        dist.all_reduce(ev, op=dist.ReduceOp.SUM)
+    return float(el.item()), float(ev.item())
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -340,13 +353,7 @@ def main():
     events = net.events() - e0
     launches = net.launches() - l0
     pre1, post1 = net.stdp_counts()
-    el = torch.tensor([ms / 1000.0], device="cuda")
-    ev = torch.tensor([float(events)], device="cuda", dtype=torch.float64)
-    if dist:
-        dist.all_reduce(el, op=dist.ReduceOp.MAX)
-        dist.all_reduce(ev, op=dist.ReduceOp.SUM)
-    elapsed = float(el.item())
-    total_events = float(ev.item())
+    elapsed, total_events = aggregate_over_ranks(ms / 1000.0, events, dist, "cuda")
     value = total_events / elapsed
     sim_s = args.steps * args.block * DT
 
@@ -619,13 +626,8 @@ def run_batched(args, rank, world, local):
     ms = start.elapsed_time(stop)
     events = sum(n.events() for n in nets) - e0
     launches = b.launches() - l0
-    el = torch.tensor([ms / 1000.0], device="cuda")
-    ev = torch.tensor([float(events)], device="cuda", dtype=torch.float64)
-    if dist:
-        dist.all_reduce(el, op=dist.ReduceOp.MAX)
-        dist.all_reduce(ev, op=dist.ReduceOp.SUM)
-    elapsed = float(el.item())
-    value = float(ev.item()) / elapsed
+    elapsed, total_events = aggregate_over_ranks(ms / 1000.0, events, dist, "cuda")
+    value = total_events / elapsed
     sim_s = args.steps * args.block * DT
 
     # roofline: algorithmic bytes of all instances over the step-kernel launches
