@@ -45,7 +45,16 @@ def net_desc(rule, sp, norm, seed=5, n=300, n_in=200, **kw):
                                     seed=seed, **kw)
 
 
-@pytest.mark.parametrize("rule,sp,norm", [c for c in CASES if c[0] != N.SPK_STDP_WEIGHT_DEPENDENT])
+CUSTOM_NEAREST = STDPParams(a_plus=1.0, a_minus=0.8, tau_plus=0.02, tau_minus=0.03, lambda_=2.0e-5, alpha=0.1,
+                            w_max=2.0e-3, clip_upper=True)
+ORACLE_CASES = [c for c in CASES if c[0] != N.SPK_STDP_WEIGHT_DEPENDENT] + [
+    (N.SPK_STDP_INHIBITORY, VOGELS, BEFORE),
+    (N.SPK_STDP_CUSTOM, CUSTOM_NEAREST, AFTER),
+    (N.SPK_STDP_EVANS, EVANS, BEFORE),
+]
+
+
+@pytest.mark.parametrize("rule,sp,norm", ORACLE_CASES)
 def test_oracle_normalisation_follows_the_reference_kernels(rule, sp, norm):
     """The oracle's trace rule with the normalisation before or after it,
     against the restatement driven by the oracle's rasters (CPU)."""
