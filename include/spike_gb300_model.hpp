@@ -237,6 +237,8 @@ class SpikingSynapses {
   void save_weights_as_binary(std::string path, std::string prefix = "", int synapsegroupid = -1);
   void save_weights_as_txt(std::string path, std::string prefix = "", int synapsegroupid = -1);
   void load_weights(std::vector<float> weights, int synapsegroupid = -1);
+  void load_weights_from_txt(std::string filepath, int synapsegroupid = -1);
+  void load_weights_from_binary(std::string filepath, int synapsegroupid = -1);
   void save_connectivity_as_binary(std::string path, std::string prefix = "",
                                    int synapsegroupid = -1);
   void save_connectivity_as_txt(std::string path, std::string prefix = "",

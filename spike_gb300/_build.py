@@ -100,17 +100,16 @@ def build_oracle(force: bool = False) -> str:
 
 
 def build_reference_frontend() -> str | None:
-    """Compile the reference front end into oracle/_ref when its sources exist
-    here (test fixtures only; absent on machines without the reference)."""
+    """Compile the reference front end into oracle/_ref with the recipe
+    oracle/build_ref.sh (test fixtures only).  The recipe locates the
+    reference sources and builds nothing where they are absent."""
     script = os.path.join(ORACLE, "build_ref.sh")
-    ref = os.environ.get("SPIKE_REFERENCE_ROOT", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "Spike")):
-        return None
     target = os.path.join(ORACLE, "_ref", "ref_dump")
-    if os.path.exists(target) and not _newer(target, [os.path.join(ORACLE, "ref_dump.cpp"), script]):
+    deps = [os.path.join(ORACLE, "ref_dump.cpp"), os.path.join(ORACLE, "ref_cases.inc"), script]
+    if os.path.exists(target) and not _newer(target, deps):
         return target
-    _run(["bash", script, ref])
-    return target
+    _run(["bash", script])
+    return target if os.path.exists(target) else None
 
 
 def build(force: bool = False) -> None:

@@ -418,6 +418,23 @@ void SpikingSynapses::load_weights(std::vector<float> weights, int gid) {
     if (rc) fail(rc, spk_last_error());
   }
 }
+// load_weights_from_txt / _binary (Spike/Synapses/Synapses.cpp:586-614): every
+// value the stream yields (text: operator>> on float; binary: native 4-byte
+// floats) in file order, then load_weights.
+void SpikingSynapses::load_weights_from_txt(std::string filepath, int gid) {
+  std::ifstream f(filepath, std::ios::in | std::ios::binary);
+  std::vector<float> w;
+  float v = 0.0f;
+  while (f >> v) w.push_back(v);
+  load_weights(w, gid);
+}
+void SpikingSynapses::load_weights_from_binary(std::string filepath, int gid) {
+  std::ifstream f(filepath, std::ios::in | std::ios::binary);
+  std::vector<float> w;
+  float v = 0.0f;
+  while (f.read(reinterpret_cast<char*>(&v), sizeof(float))) w.push_back(v);
+  load_weights(w, gid);
+}
 // save_connectivity_as_* (Spike/Synapses/Synapses.cpp:423-519,
 // Spike/Synapses/SpikingSynapses.cpp:136-189).
 void SpikingSynapses::save_connectivity_as_binary(std::string path, std::string prefix, int gid) {

@@ -6,7 +6,11 @@ cases defined in oracle/ref_dump.cpp and stores what it produced:
 
 * small cases (va_mix, brunel, shapes): every array, as .npz;
 * the full VogelsAbbottNet network (va, 320,261 synapses): counts and SHA-256
-  digests of every array, as .json.
+  digests of every array, as .json;
+* the weight and connectivity files the reference's save functions write for
+  each case (Spike/Synapses/Synapses.cpp:423-614, SpikingSynapses.cpp:136-189;
+  ref_dump's save mode), and the weights read back from the text file and
+  written again: size and SHA-256 of every file, as ref_checkpoint.json.
 
 Usage (in a checkout where the reference sources are present):
     python tests/golden/make_golden.py
@@ -69,6 +73,17 @@ def run_case(ref_dump: str, case: str) -> dict:
         return read_dump(out)
 
 
+def checkpoint_digests(ref_dump: str, case: str) -> dict:
+    with tempfile.TemporaryDirectory() as td:
+        subprocess.run([ref_dump, "save", case, td], check=True, capture_output=True)
+        out = {}
+        for name in sorted(os.listdir(td)):
+            with open(os.path.join(td, name), "rb") as f:
+                data = f.read()
+            out[name] = {"bytes": len(data), "sha256": hashlib.sha256(data).hexdigest()}
+        return out
+
+
 def main() -> int:
     sys.path.insert(0, ROOT)
     from spike_gb300 import _build
@@ -98,6 +113,10 @@ def main() -> int:
     with open(os.path.join(HERE, "ref_va.json"), "w") as f:
         json.dump(meta, f, indent=1, sort_keys=True)
     print("va", meta["n_synapses"], "synapses")
+    ck = {case: checkpoint_digests(ref_dump, case) for case in ("va", "va_mix", "brunel", "shapes")}
+    with open(os.path.join(HERE, "ref_checkpoint.json"), "w") as f:
+        json.dump(ck, f, indent=1, sort_keys=True)
+    print("checkpoint files", {k: len(v) for k, v in ck.items()})
     return 0
 
 
