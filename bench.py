@@ -73,6 +73,8 @@ def parse():
                    help="batched: execution mode (auto: the autotuner's choice; waves without the autotuner); served: waves, else bulk")
     p.add_argument("--no-tune", action="store_true",
                    help="batched: skip the autotuner (8 warps, tiles of up to 64 posts, costs from synapse counts)")
+    p.add_argument("--range", type=int, default=0,
+                   help="batched: skip the autotuner and propagate over post ranges of this many posts (bulk mode)")
     p.add_argument("--plain-block", type=int, default=200,
                    help="batched: timesteps each instance runs alone for the plain comparison")
     p.add_argument("--block", type=int, default=1000, help="timesteps per bench step")
@@ -582,7 +584,13 @@ def run_batched(args, rank, world, local):
     gens = networks.batched_sweep(args.instances)
     t0 = time.perf_counter()
     mode = N.SPK_BATCH_WAVES
-    if args.no_tune:
+    if args.range:
+        scheds = [schedule(1, min(args.range, -(-g.desc.n_neurons // 32) * 32), 0, 0) for g in gens]
+        tune_ms = None
+        nets = [Net.generate(g, s) for g, s in zip(gens, scheds)]
+        costs = [0.0 for _ in gens]
+        mode = N.SPK_BATCH_BULK
+    elif args.no_tune:
         scheds = [schedule(8, min(64, max(32, -(-(-(-g.desc.n_neurons // 8)) // 32) * 32)), 0, 0) for g in gens]
         tune_ms = None
         nets = [Net.generate(g, s) for g, s in zip(gens, scheds)]
@@ -726,7 +734,7 @@ def run_batched(args, rank, world, local):
             "config": {**batched_config(gens, n_syn), "block_timesteps": args.block,
                        "schedules": sch, "autotune_s": round(tune_s, 2), "autotune_trial_ms": tune_ms,
                        "launches_per_block": launches / max(1, args.steps),
-                       "autotuned": not args.no_tune,
+                       "autotuned": not (args.no_tune or args.range),
                        "mode": "bulk" if mode == N.SPK_BATCH_BULK else "waves",
                        "l2": f"synapse entries {8 * n_syn / 1e9:.1f} GB > 129 MB L2 (no flush)",
                        "parallelism": "replicas" if world > 1 else "single"},

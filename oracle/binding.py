@@ -36,6 +36,7 @@ def oracle_lib() -> C.CDLL:
             "oracle_read_state": [vp, C.c_int, C.POINTER(C.c_float), C.c_int64],
             "oracle_read_weights": [vp, C.POINTER(C.c_float), C.c_int64],
             "oracle_synaptic_events": [vp, C.POINTER(C.c_uint64)],
+            "oracle_ring_depth": [vp, C.POINTER(C.c_int32)],
             "oracle_sorted_synapses": [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                        C.c_int64],
         }
@@ -134,6 +135,11 @@ class OracleNet:
         e = C.c_uint64()
         _ok(oracle_lib().oracle_synaptic_events(self.h, C.byref(e)), "oracle_synaptic_events")
         return e.value
+
+    def ring_depth(self) -> int:
+        b = C.c_int32()
+        _ok(oracle_lib().oracle_ring_depth(self.h, C.byref(b)), "oracle_ring_depth")
+        return b.value
 
     def sorted_synapses(self):
         S = self.n_synapses

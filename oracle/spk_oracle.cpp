@@ -9,6 +9,8 @@
 // reference where that helps the side-by-side reading.
 #include "spk_oracle.h"
 
+#include <algorithm>
+#include <atomic>
 #include <barrier>
 #include <cmath>
 #include <cstdint>
@@ -233,7 +235,9 @@ int Net<R>::init(const spk_net_desc* d) {
     revsort[s] = pos;
     if (d->plastic && d->plastic[s]) splastic[pos] = 1;
   }
-  // Ring depth D_max + 2G + 1 (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:48).
+  // Ring depth D_max + 2G + 1 (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:48);
+  // a network without synapses keeps a ring of delay-1 depth.
+  if (S == 0) Dmax = 1;
   B = Dmax + 2 * 1 + 1;
 
   has_stdp = d->has_stdp != 0;
@@ -1012,6 +1016,14 @@ int oracle_synaptic_events(const oracle_net* n, uint64_t* events) {
   return SPK_OK;
 }
 
+int oracle_ring_depth(const oracle_net* n, int32_t* depth) {
+  if (!n || !depth) return SPK_ERR_INVALID;
+  return dispatch(n, [&](auto& net) {
+    *depth = net.B;
+    return SPK_OK;
+  });
+}
+
 int oracle_sorted_synapses(const oracle_net* n, int32_t* pre, int32_t* post, int32_t* delay,
                            int64_t count) {
   if (!n) return SPK_ERR_INVALID;
@@ -1059,6 +1071,64 @@ double oracle_log_max_ulp(void) {
  * code, 0, SYNAPSE) words 0 and 1.  Writes up to `capacity` synapses in that
  * (creation) order with the spk_net_desc id convention and returns how many
  * there are. */
+// Key range [k0, k1) of the generator restatement: counts (out == nullptr)
+// or writes the synapses of those keys in creation order at out offset n0.
+// One Philox block of four connection uniforms serves four consecutive posts.
+struct GenOut {
+  int32_t *pre, *post, *delay, *label;
+  float *weight, *scale;
+  uint8_t* plastic;
+};
+static int64_t gen_keys(const spk_gen_desc* d, const std::vector<int>& order, int k0, int k1, const GenOut* out,
+                        int64_t n0, int64_t capacity) {
+  int64_t n = n0;
+  for (int k = k0; k < k1; ++k) {
+    const bool is_input = k < d->n_inputs;
+    const int idx = is_input ? d->n_inputs - 1 - k : k - d->n_inputs;
+    const int pop = is_input ? SPK_POP_INPUTS : SPK_POP_NEURONS;
+    const uint32_t code = is_input ? (0x80000000u | (uint32_t)idx) : (uint32_t)idx;
+    for (int j : order) {
+      const spk_projection& P = d->projections[j];
+      if (P.pre_population != pop || idx < P.pre_start || idx >= P.pre_start + P.pre_count) continue;
+      uint32_t words[4] = {0, 0, 0, 0};
+      for (int q = P.post_start; q < P.post_start + P.post_count; ++q) {
+        if (q == P.post_start || (q & 3) == 0) {
+          const spk::u32x4 c = spk::draw4(d->connectivity_seed, (uint32_t)q >> 2, code, spk::DOMAIN_CONNECT);
+          words[0] = c.x;
+          words[1] = c.y;
+          words[2] = c.z;
+          words[3] = c.w;
+        }
+        if (!(spk::uniform_open0(words[q & 3]) <= P.probability)) continue;
+        if (out && n < capacity) {
+          const spk::u32x4 r = spk::draw4(d->connectivity_seed, (uint32_t)q, code, spk::DOMAIN_SYNAPSE);
+          const float span = P.weight_hi - P.weight_lo;
+          const float w = P.weight_lo + span * spk::uniform_open0(r.x);
+          const int nd = P.delay_hi - P.delay_lo + 1;
+          int dd = (int)(spk::uniform_open0(r.y) * (float)nd);
+          if (dd > nd - 1) dd = nd - 1;
+          if (out->pre) out->pre[n] = is_input ? -idx - 1 : idx;
+          if (out->post) out->post[n] = q;
+          if (out->weight) out->weight[n] = w;
+          if (out->scale) out->scale[n] = P.scale;
+          if (out->delay) out->delay[n] = P.delay_lo + dd;
+          if (out->label) out->label[n] = P.label;
+          if (out->plastic) out->plastic[n] = P.plastic ? 1 : 0;
+        }
+        ++n;
+      }
+    }
+  }
+  return n - n0;
+}
+
+// The device generator (spk_gen.cuh) restated: every (pre, post) pair of a
+// projection connects when its Philox(connectivity seed, post/4, pre code)
+// uniform is at most the probability; a connected pair's weight and delay
+// come from Philox(post, pre code).  Creation order: ascending presynaptic
+// key (inputs in reverse order first, then neurons), projections by first
+// post, posts ascending.  Keys are split over host threads; each range is
+// counted, then written at its offset, so the order does not depend on them.
 int64_t oracle_generate(const spk_gen_desc* d, int32_t* pre, int32_t* post, float* weight, float* scale,
                         int32_t* delay, int32_t* label, uint8_t* plastic, int64_t capacity) {
   if (!d || d->n_projections < 0 || (d->n_projections > 0 && !d->projections)) return -1;
@@ -1070,39 +1140,29 @@ int64_t oracle_generate(const spk_gen_desc* d, int32_t* pre, int32_t* post, floa
       order[b] = order[b - 1];
       order[b - 1] = t;
     }
-  int64_t n = 0;
   const int n_keys = d->n_inputs + d->n_neurons;
-  for (int k = 0; k < n_keys; ++k) {
-    const bool is_input = k < d->n_inputs;
-    const int idx = is_input ? d->n_inputs - 1 - k : k - d->n_inputs;
-    const int pop = is_input ? SPK_POP_INPUTS : SPK_POP_NEURONS;
-    const uint32_t code = is_input ? (0x80000000u | (uint32_t)idx) : (uint32_t)idx;
-    for (int j : order) {
-      const spk_projection& P = d->projections[j];
-      if (P.pre_population != pop || idx < P.pre_start || idx >= P.pre_start + P.pre_count) continue;
-      for (int q = P.post_start; q < P.post_start + P.post_count; ++q) {
-        const spk::u32x4 c = spk::draw4(d->connectivity_seed, (uint32_t)q >> 2, code, spk::DOMAIN_CONNECT);
-        const uint32_t words[4] = {c.x, c.y, c.z, c.w};
-        if (!(spk::uniform_open0(words[q & 3]) <= P.probability)) continue;
-        if (n < capacity) {
-          const spk::u32x4 r = spk::draw4(d->connectivity_seed, (uint32_t)q, code, spk::DOMAIN_SYNAPSE);
-          const float span = P.weight_hi - P.weight_lo;
-          const float w = P.weight_lo + span * spk::uniform_open0(r.x);
-          const int nd = P.delay_hi - P.delay_lo + 1;
-          int dd = (int)(spk::uniform_open0(r.y) * (float)nd);
-          if (dd > nd - 1) dd = nd - 1;
-          if (pre) pre[n] = is_input ? -idx - 1 : idx;
-          if (post) post[n] = q;
-          if (weight) weight[n] = w;
-          if (scale) scale[n] = P.scale;
-          if (delay) delay[n] = P.delay_lo + dd;
-          if (label) label[n] = P.label;
-          if (plastic) plastic[n] = P.plastic ? 1 : 0;
-        }
-        ++n;
-      }
-    }
-  }
+  const int T = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), 64));
+  const int parts = std::max(1, std::min(n_keys, 4 * T));
+  std::vector<int64_t> cnt(parts + 1, 0);
+  auto key_of = [&](int p) { return (int)((int64_t)n_keys * p / parts); };
+  auto run = [&](auto&& fn) {
+    std::vector<std::thread> pool;
+    std::atomic<int> next{0};
+    for (int t = 0; t < T; ++t)
+      pool.emplace_back([&]() {
+        for (int p = next++; p < parts; p = next++) fn(p);
+      });
+    for (auto& th : pool) th.join();
+  };
+  run([&](int p) { cnt[p + 1] = gen_keys(d, order, key_of(p), key_of(p + 1), nullptr, 0, 0); });
+  for (int p = 0; p < parts; ++p) cnt[p + 1] += cnt[p];
+  const int64_t n = cnt[parts];
+  const GenOut out{pre, post, delay, label, weight, scale, plastic};
+  const bool any = pre || post || delay || label || weight || scale || plastic;
+  if (any && capacity > 0)
+    run([&](int p) {
+      if (cnt[p] < capacity) gen_keys(d, order, key_of(p), key_of(p + 1), &out, cnt[p], capacity);
+    });
   return n;
 }
 

@@ -22,6 +22,7 @@
 #include "../../include/spike_gb300.h"
 #include "spk_bulk.cuh"
 #include "spk_gen.cuh"
+#include "spk_range.cuh"
 #include "spk_internal.h"
 #include "spk_kernel.cuh"
 
@@ -111,6 +112,11 @@ static cudaError_t launch_overlapped(void (*k)(P...), int grid, int block, size_
 
 struct Plan {
   int W, TS, ITS, nctas, n_tiles, KL, n_keys, n_words, K, smem;
+  // The persistent step kernel can run the plan (its shared memory fits and
+  // its CTAs fit one cooperative launch).  A plan of range tiles (an explicit
+  // schedule with tiles of RANGE_MIN_TS posts or more whose tile does not fit
+  // a warp's shared memory) runs in bulk mode only.
+  bool persistent;
 };
 
 static int plan_bytes(int B, int TS, int L, int ITS, int kind, int stdp, int W) {
@@ -122,7 +128,7 @@ static int plan_bytes(int B, int TS, int L, int ITS, int kind, int stdp, int W) 
 // 64-256 posts over up to one CTA per SM.  Explicit schedule fields override.
 static int make_plan(int N, int Nin, int B, int L, int kind, int stdp, const spk_schedule* s,
                      const DeviceInfo& di, Plan* p) {
-  auto finish = [&](int W, int TS, int nctas) {
+  auto finish = [&](int W, int TS, int nctas, bool allow_bulk = false) {
     p->W = W;
     p->TS = TS;
     p->nctas = nctas;
@@ -133,8 +139,9 @@ static int make_plan(int N, int Nin, int B, int L, int kind, int stdp, const spk
     p->n_words = p->n_keys / 32;
     p->smem = plan_bytes(B, TS, L, p->ITS, kind, stdp, W);
     // per-CTA key counts travel in 16-bit fields of the stamp word
-    return p->smem <= di.max_smem && (int64_t)p->n_tiles * TS >= N && nctas <= MAX_CTAS_PER_NET &&
-           W * TS <= 65535 && W * p->ITS <= 65535;
+    p->persistent = p->smem <= di.max_smem && nctas <= MAX_CTAS_PER_NET && W * TS <= 65535 && W * p->ITS <= 65535;
+    const bool covers = (int64_t)p->n_tiles * TS >= N && (int64_t)p->n_keys < (1ll << 30);
+    return covers && (p->persistent || (allow_bulk && TS >= RANGE_MIN_TS));
   };
   const int K = (s && s->steps_per_launch > 0) ? s->steps_per_launch : DEFAULT_STEPS_PER_LAUNCH;
   p->K = K;
@@ -151,7 +158,7 @@ static int make_plan(int N, int Nin, int B, int L, int kind, int stdp, const spk
     if (!TS && C) TS = std::max(32, ((N + W * C - 1) / (W * C) + 31) / 32 * 32);
     if (!TS) TS = 64;
     if (!C) C = (N + W * TS - 1) / (W * TS);
-    if (!finish(W, TS, C)) {
+    if (!finish(W, TS, C, true)) {
       set_error("schedule W=%d tile=%d ctas=%d does not cover %d neurons within %d B of shared memory (needs %d)",
                 W, TS, C, N, di.max_smem, p->smem);
       return SPK_ERR_INVALID;
@@ -221,8 +228,9 @@ struct spk_net {
   int weight_norm = SPK_NORM_OFF;   // SPK_NORM_* (with an STDP rule only)
   std::vector<float> norm_w0_h;     // per plastic record: initial weight
   std::vector<float> norm_sum_h;    // per post: sum of squares
-  // Runs in bulk mode only: a per-synapse-trace rule or the weight normalisation.
-  bool bulk_only() const { return dense() || weight_norm != SPK_NORM_OFF; }
+  // Runs in bulk mode only: a per-synapse-trace rule, the weight normalisation,
+  // or range tiles (a plan the persistent kernel cannot run).
+  bool bulk_only() const { return dense() || weight_norm != SPK_NORM_OFF || !plan.persistent; }
   // The normalisation's place in a bulk timestep: 0 before the rule, 1 after
   // the per-synapse-trace pass, 2 after the event-driven rule's updates (a
   // first propagation pass that only updates weights, and the afferent pass).
@@ -255,6 +263,9 @@ struct spk_batch {
   std::vector<NetDev> hds;       // host copies of the batch's descriptors
   BulkPropBlock* dpblocks = nullptr;  // [pblocks_total] propagation tile groups
   int pblocks_total = 0;
+  BulkRangeBlock* drblocks = nullptr; // [rblocks_total] propagation ranges (networks of range tiles)
+  int rblocks_total = 0;
+  int range_win_words = 0;            // ring-window words of a propagation range
   BulkBlock* dblocks = nullptr;  // [blocks_total] blocks of 32-key words with real keys
   int blocks_total = 0;
   BulkPostItem* items = nullptr; // afferent-pass work list of a timestep
@@ -836,7 +847,7 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
     set_error("cudaFuncSetAttribute failed: %s", cudaGetErrorString(cudaGetLastError()));
     return fail_free(SPK_ERR_CUDA);
   }
-  if (plan.nctas > 1) {
+  if (plan.nctas > 1 && plan.persistent) {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, step_kernel, plan.W * 32, plan.smem) !=
         cudaSuccess) {
@@ -855,7 +866,7 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
     set_error("initial upload failed: %s", cudaGetErrorString(cudaGetLastError()));
     return fail_free(SPK_ERR_CUDA);
   }
-  build_graph(n);
+  if (plan.persistent) build_graph(n);
   return SPK_OK;
 }
 
@@ -1942,9 +1953,14 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
     b->W = nets[0] ? nets[0]->plan.W : 0;
     b->K = (schedule && schedule->steps_per_launch > 0) ? schedule->steps_per_launch
                                                         : (nets[0] ? nets[0]->plan.K : DEFAULT_STEPS_PER_LAUNCH);
+    // A batch holding a network that the persistent kernel cannot run (range
+    // tiles) runs in bulk mode only: it has no waves, and its networks may
+    // differ in warps per CTA.
+    bool all_persistent = true;
+    for (int i = 0; i < n_nets; ++i) all_persistent = all_persistent && nets[i] && nets[i]->plan.persistent;
     for (int i = 0; i < n_nets; ++i) {
       spk_net* n = nets[i];
-      if (!n || n->plan.W != b->W) {
+      if (!n || (all_persistent && n->plan.W != b->W)) {
         set_error("all networks of a batch need the same warps_per_cta (net %d)", i);
         delete b;
         return SPK_ERR_INVALID;
@@ -1989,6 +2005,7 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
     std::vector<CtaMap> map;
     map.reserve(b->total_ctas);
     spk_batch::Wave cur{0, 0, 0, false};
+    if (!all_persistent) order.clear();
     for (int i : order) {
       spk_net* n = nets[i];
       int cap = 0;
@@ -2016,7 +2033,7 @@ int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* s
       cur.smem = std::max(cur.smem, n->plan.smem);
       cur.cooperative |= n->plan.nctas > 1;
     }
-    b->waves.push_back(cur);
+    if (all_persistent) b->waves.push_back(cur);
     std::vector<NetDev>& hds = b->hds;
     hds.resize(n_nets);
     for (int i = 0; i < n_nets; ++i) hds[i] = nets[i]->hd;
@@ -2101,20 +2118,36 @@ static int bulk_launch_block(spk_batch* b) {
       SPK_CUDA(cudaEventRecord(b->join, b->side));
       ++per_step;
     }
-    SPK_CUDA(launch_overlapped(split ? bulk_prop_kernel<1> : bulk_prop_kernel<0>, b->pblocks_total,
-                               BULK_PROP_WARPS * 32, (size_t)prop_smem, b->stream, (const NetDev*)b->dd,
-                               (const BulkPropBlock*)b->dpblocks, s, b->win_words, b->ts_max));
-    ++per_step;
+    if (b->pblocks_total) {
+      SPK_CUDA(launch_overlapped(split ? bulk_prop_kernel<1> : bulk_prop_kernel<0>, b->pblocks_total,
+                                 BULK_PROP_WARPS * 32, (size_t)prop_smem, b->stream, (const NetDev*)b->dd,
+                                 (const BulkPropBlock*)b->dpblocks, s, b->win_words, b->ts_max));
+      ++per_step;
+    }
+    if (b->rblocks_total) {
+      SPK_CUDA(launch_overlapped(split ? bulk_range_kernel<1> : bulk_range_kernel<0>, b->rblocks_total,
+                                 RANGE_THREADS, (size_t)b->range_win_words * 4, b->stream, (const NetDev*)b->dd,
+                                 (const BulkRangeBlock*)b->drblocks, s, b->range_win_words));
+      ++per_step;
+    }
     if (b->any_plastic) SPK_CUDA(cudaStreamWaitEvent(b->stream, b->join, 0));
     if (split) {
       if (b->n_dense_items) {
         bulk_norm_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s, 2);
         ++per_step;
       }
-      SPK_CUDA(launch_overlapped(bulk_prop_kernel<2>, b->pblocks_total, BULK_PROP_WARPS * 32, (size_t)prop_smem,
-                                 b->stream, (const NetDev*)b->dd, (const BulkPropBlock*)b->dpblocks, s,
-                                 b->win_words, b->ts_max));
-      ++per_step;
+      if (b->pblocks_total) {
+        SPK_CUDA(launch_overlapped(bulk_prop_kernel<2>, b->pblocks_total, BULK_PROP_WARPS * 32,
+                                   (size_t)prop_smem, b->stream, (const NetDev*)b->dd,
+                                   (const BulkPropBlock*)b->dpblocks, s, b->win_words, b->ts_max));
+        ++per_step;
+      }
+      if (b->rblocks_total) {
+        SPK_CUDA(launch_overlapped(bulk_range_kernel<2>, b->rblocks_total, RANGE_THREADS,
+                                   (size_t)b->range_win_words * 4, b->stream, (const NetDev*)b->dd,
+                                   (const BulkRangeBlock*)b->drblocks, s, b->range_win_words));
+        ++per_step;
+      }
     }
   }
   bulk_finish_kernel<<<(n + 255) / 256, 256, 0, b->stream>>>(b->dd, n, b->K);
@@ -2204,8 +2237,8 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
   if (mode == SPK_BATCH_WAVES) {
     for (const spk_net* n : b->nets)
       if (n->bulk_only()) {
-        set_error("waves mode: a network with a per-synapse-trace STDP rule or the weight normalisation "
-                  "runs in bulk mode only");
+        set_error("waves mode: a network with a per-synapse-trace STDP rule, the weight normalisation or "
+                  "range tiles runs in bulk mode only");
         return SPK_ERR_UNSUPPORTED;
       }
     b->mode = mode;
@@ -2214,6 +2247,7 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
   return guarded([&]() -> int {
     if (!b->bulk_mem) {
       std::vector<BulkPropBlock> tiles;
+      std::vector<BulkRangeBlock> ranges;
       std::vector<BulkBlock> words;
       size_t list_words = 0;
       // propagation tile groups of the networks with the most keys first: their
@@ -2222,10 +2256,22 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       for (size_t i = 0; i < by_keys.size(); ++i) by_keys[i] = (int)i;
       std::stable_sort(by_keys.begin(), by_keys.end(),
                        [&](int x, int y) { return b->nets[x]->plan.n_keys > b->nets[y]->plan.n_keys; });
-      for (const int i : by_keys)
+      for (const int i : by_keys) {
+        if (b->nets[i]->plan.TS >= RANGE_MIN_TS) continue;
         for (int t = 0; t < b->nets[i]->plan.n_tiles; t += BULK_PROP_WARPS)
           tiles.push_back(BulkPropBlock{i, t, std::min(BULK_PROP_WARPS, b->nets[i]->plan.n_tiles - t), 0,
                                         b->hds[i].ctl, nullptr});
+      }
+      // ranges (one CTA each) of the networks with the most synapses per range first
+      std::vector<int> by_load(b->nets.size());
+      for (size_t i = 0; i < by_load.size(); ++i) by_load[i] = (int)i;
+      auto load_of = [&](int i) { return (double)b->nets[i]->S / b->nets[i]->plan.n_tiles; };
+      std::stable_sort(by_load.begin(), by_load.end(), [&](int x, int y) { return load_of(x) > load_of(y); });
+      for (const int i : by_load) {
+        if (b->nets[i]->plan.TS < RANGE_MIN_TS) continue;
+        for (int t = 0; t < b->nets[i]->plan.n_tiles; ++t)
+          ranges.push_back(BulkRangeBlock{i, t, 0, 0, b->hds[i].ctl, nullptr});
+      }
       for (size_t i = 0; i < b->nets.size(); ++i) {
         const spk_net* n = b->nets[i];
         const int in_end = (n->Nin + 31) / 32, lif0 = n->plan.KL / 32, lif_end = (n->plan.KL + n->N + 31) / 32;
@@ -2289,16 +2335,26 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       b->win_words = 0;
       b->ts_max = 0;
       for (const spk_net* n : b->nets) {
+        if (n->hd.TS >= RANGE_MIN_TS) continue;
         b->ts_max = std::max(b->ts_max, n->hd.TS);
         b->win_words = std::max(b->win_words, (n->hd.B - 3) * n->hd.TS * n->hd.L);
       }
       b->win_words = std::min(b->win_words, BULK_WIN_CAP);
+      // range windows: as many of a range's delay slots as the cap holds
+      b->range_win_words = 0;
+      for (const spk_net* n : b->nets) {
+        if (n->hd.TS < RANGE_MIN_TS) continue;
+        const int slot_words = n->hd.TS * n->hd.L;
+        const int ws = std::min(n->hd.B - 3, RANGE_WIN_CAP / slot_words);
+        b->range_win_words = std::max(b->range_win_words, ws * slot_words);
+      }
+      const size_t r_bytes = align_up(sizeof(BulkRangeBlock) * ranges.size(), 256);
       const size_t t_bytes = align_up(sizeof(BulkPropBlock) * tiles.size(), 256);
       const size_t w_bytes = align_up(sizeof(BulkBlock) * words.size(), 256);
       const size_t l_bytes = align_up(sizeof(uint32_t) * list_words, 256);
       const size_t c_bytes = align_up(sizeof(int) * (b->nets.size() + 1), 256);
       const size_t i_bytes = align_up(sizeof(BulkPostItem) * std::max<size_t>(cap, 1), 256);
-      if (cudaMalloc(&b->bulk_mem, t_bytes + w_bytes + l_bytes + c_bytes + i_bytes) != cudaSuccess) {
+      if (cudaMalloc(&b->bulk_mem, t_bytes + w_bytes + l_bytes + c_bytes + i_bytes + r_bytes) != cudaSuccess) {
         cudaGetLastError();
         b->bulk_mem = nullptr;
         set_error("bulk mode: device allocation failed");
@@ -2312,6 +2368,8 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       int* counts = (int*)((char*)b->bulk_mem + t_bytes + w_bytes + l_bytes);
       b->item_count = counts + b->nets.size();
       b->items = (BulkPostItem*)((char*)b->bulk_mem + t_bytes + w_bytes + l_bytes + c_bytes);
+      b->drblocks = (BulkRangeBlock*)((char*)b->bulk_mem + t_bytes + w_bytes + l_bytes + c_bytes + i_bytes);
+      b->rblocks_total = (int)ranges.size();
       size_t off = 0;
       for (size_t i = 0; i < b->nets.size(); ++i) {
         b->hds[i].step_list = lists + off;
@@ -2319,7 +2377,10 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
         off += (size_t)b->nets[i]->plan.n_keys;
       }
       for (BulkPropBlock& pb : tiles) pb.n_list = counts + pb.net;
+      for (BulkRangeBlock& rb : ranges) rb.n_list = counts + rb.net;
       SPK_CUDA(cudaMemcpy(b->dpblocks, tiles.data(), sizeof(BulkPropBlock) * tiles.size(), cudaMemcpyHostToDevice));
+      SPK_CUDA(cudaMemcpy(b->drblocks, ranges.data(), sizeof(BulkRangeBlock) * ranges.size(),
+                          cudaMemcpyHostToDevice));
       SPK_CUDA(cudaMemcpy(b->dblocks, words.data(), sizeof(BulkBlock) * words.size(), cudaMemcpyHostToDevice));
       // words of padding keys are never written in bulk mode: zero them once
       SPK_CUDA(cudaStreamSynchronize(b->stream));
@@ -2333,6 +2394,10 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, prop_smem));
       SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, prop_smem));
       SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, prop_smem));
+      const int range_smem = b->range_win_words * 4;
+      SPK_CUDA(cudaFuncSetAttribute(bulk_range_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, range_smem));
+      SPK_CUDA(cudaFuncSetAttribute(bulk_range_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, range_smem));
+      SPK_CUDA(cudaFuncSetAttribute(bulk_range_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, range_smem));
     }
     b->mode = mode;
     return SPK_OK;

@@ -12,9 +12,8 @@ def bits(a):
 
 
 def ring_depth(o: OracleNet) -> int:
-    """D_max + 2G + 1 (SpikingSynapses.cu:48) from the oracle's sorted delays."""
-    _, _, delay = o.sorted_synapses()
-    return int(delay.max() if len(delay) else 1) + 3
+    """D_max + 2G + 1 (SpikingSynapses.cu:48) as the oracle sized its ring."""
+    return o.ring_depth()
 
 
 def assert_same(net: Net, o: OracleNet, n: int, n_in: int, n_labels: int, weights: bool = False, tag: str = ""):
