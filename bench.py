@@ -75,7 +75,7 @@ def parse():
                    help="batched: skip the autotuner (8 warps, tiles of up to 64 posts, costs from synapse counts)")
     p.add_argument("--range", type=int, default=0,
                    help="batched: skip the autotuner and propagate over post ranges of this many posts (bulk mode)")
-    p.add_argument("--plain-block", type=int, default=200,
+    p.add_argument("--plain-block", type=int, default=1000,
                    help="batched: timesteps each instance runs alone for the plain comparison")
     p.add_argument("--block", type=int, default=1000, help="timesteps per bench step")
     p.add_argument("--ctas", type=int, default=0)
@@ -213,9 +213,10 @@ def peaks():
 
 
 def traffic_per_launch(workload: str):
-    """The committed ncu summary of the step kernel on this workload
+    """The committed ncu summary of the timed kernel on this workload
     (profiles/step_kernel_<workload>.json): DRAM bytes of a captured launch per
-    algorithmic byte of that launch, applied to this run's launches."""
+    algorithmic byte (or per synaptic event) of that launch, applied to this
+    run's launches."""
     path = os.path.join(ROOT, "profiles", f"step_kernel_{workload}.json")
     try:
         with open(path) as f:
@@ -408,7 +409,7 @@ def main():
             # the generated network is too large to draw on the host: a
             # 1/20-size network of the same construction stands in
             cs = CpuSample([networks_small_plastic_ff(args.rule)])
-            cv, cel = cs.run(args.cpu_sample_steps // 10, parallel=False)
+            cv, cel = cs.run(args.cpu_sample_steps // 10, 1)
             cpu = {"value": cv, "unit": "events/s", "cores": 1, "kind": "port",
                    "sample": f"the same construction at 1/20 size (2,500 inputs, 10,000 neurons), "
                              f"{args.cpu_sample_steps // 10} timesteps from reset, {cel:.1f} s of CPU"}
@@ -448,8 +449,9 @@ def main():
 
 # ---- batched sweep ------------------------------------------------------------------
 
-BATCH_CPU_INSTANCES = 8      # smallest instances of the sweep run by the CPU baselines
-BATCH_CPU_STEPS = 400
+PLAIN_WARMUP = 200           # timesteps each instance runs alone before the plain form is timed
+BATCH_CPU_INSTANCES = 16     # instances of the sweep run by the CPU baselines, spread over its sizes
+BATCH_CPU_STEPS = 100        # timesteps of each from reset
 
 
 def batched_config(gens, n_syn=None):
@@ -464,18 +466,15 @@ def batched_config(gens, n_syn=None):
     return cfg
 
 
-BATCH_CPU_MAX_N = 8000       # instances up to this size are drawn on the host in about a second
-
-
 def cpu_sample_gens(gens, count=BATCH_CPU_INSTANCES):
-    """`count` instances of the sweep spread over its sizes up to
-    BATCH_CPU_MAX_N neurons (their synapse lists are cheap to draw on the host
-    with the oracle's restatement of the generator)."""
+    """`count` instances of the sweep at evenly spaced ranks of its sizes,
+    smallest to largest (the CPU's events/s depends on the instance size, and
+    on STDP, whose reference form updates every plastic synapse every
+    timestep, so the sample spans the whole range)."""
     order = sorted(range(len(gens)), key=lambda k: gens[k].desc.n_neurons)
-    small = [k for k in order if gens[k].desc.n_neurons <= BATCH_CPU_MAX_N] or order[:1]
-    n = min(count, len(small))
-    pick = [small[(i * (len(small) - 1)) // max(n - 1, 1)] for i in range(n)]
-    return [gens[k] for k in pick]
+    n = min(count, len(order))
+    pick = sorted({order[(i * (len(order) - 1)) // max(n - 1, 1)] for i in range(n)})
+    return [gens[k] for k in pick], pick
 
 
 def oracle_instance(gen):
@@ -504,56 +503,73 @@ class CpuSample:
     """The oracle on the CPU sample of the sweep, built once."""
 
     def __init__(self, gens, count=BATCH_CPU_INSTANCES):
-        picked = cpu_sample_gens(gens, count)
-        self.nets = [oracle_instance(g)[0] for g in picked]
+        picked, self.index = cpu_sample_gens(gens, count)
+        self.gens = picked
+        self.nets = [None] * len(picked)
+        import threading
+        th = [threading.Thread(target=self._build, args=(i,)) for i in range(len(picked))]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
         sizes = [g.desc.n_neurons for g in picked]
-        self.label = f"{len(self.nets)} instances of the sweep (N {min(sizes)}-{max(sizes)})"
+        self.label = (f"{len(self.nets)} instances of the sweep at evenly spaced size ranks (N {min(sizes)}-"
+                      f"{max(sizes)}, {sum(1 for g in picked if g.desc.has_stdp)} with STDP)")
 
-    def run(self, steps, parallel):
-        """Events/s of `steps` timesteps of every sample instance, one thread
-        per instance (parallel) or one after another."""
+    def _build(self, i):
+        self.nets[i] = oracle_instance(self.gens[i])[0]
+
+    def run(self, steps, threads):
+        """Events/s of `steps` timesteps of every sample instance, the
+        instances shared out over `threads` host threads (largest first)."""
         import threading
         results = [0] * len(self.nets)
+        todo = sorted(range(len(self.nets)), key=lambda i: -self.gens[i].desc.n_neurons)
+        lock = threading.Lock()
 
-        def work(i):
-            o = self.nets[i]
-            e0 = o.events()
-            o.run_steps(steps, True)
-            results[i] = o.events() - e0
+        def work():
+            while True:
+                with lock:
+                    if not todo:
+                        return
+                    i = todo.pop(0)
+                o = self.nets[i]
+                e0 = o.events()
+                o.run_steps(steps, True)
+                results[i] = o.events() - e0
 
         t0 = time.perf_counter()
-        if parallel:
-            th = [threading.Thread(target=work, args=(i,)) for i in range(len(self.nets))]
-            for t in th:
-                t.start()
-            for t in th:
-                t.join()
-        else:
-            for i in range(len(self.nets)):
-                work(i)
+        th = [threading.Thread(target=work) for _ in range(max(1, threads))]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
         el = time.perf_counter() - t0
         return sum(results) / el, el
 
 
 def run_reference_batched(args, rank, world):
-    """CPU reference arm for the batched sweep: the oracle port, one instance
-    per host thread, on the smallest instances of the sweep."""
+    """CPU reference arm for the batched sweep: the oracle port of the
+    reference's step loop on a sample of the sweep spread over its whole size
+    range (cpu_sample_gens), every instance from reset, shared out over the
+    host's threads."""
     if rank != 0:
         return
     from spike_gb300 import networks
     gens = networks.batched_sweep(args.instances)
-    threads = os.cpu_count() or 1  # one instance per host thread, every thread busy
-    cs = CpuSample(gens, threads)
-    threads = len(cs.nets)
-    per_step = min(args.block, 100)
+    threads = os.cpu_count() or 1
+    cs = CpuSample(gens)
     vals, els = [], []
     for i in range(args.warmup + args.steps):
-        v, el = cs.run(per_step, parallel=True)
+        for o in cs.nets:
+            o.reset_state()
+            o.reset_time()
+        v, el = cs.run(BATCH_CPU_STEPS, threads)
         if i >= args.warmup:
             vals.append(v)
             els.append(el)
     value = sum(vals) / len(vals)
-    sample = f"{cs.label}, {per_step} timesteps each per step, one host thread per instance"
+    sample = f"{cs.label}, {BATCH_CPU_STEPS} timesteps each from reset per step, {threads} host threads"
     line = {"metric": "synaptic_events_per_s", "value": value, "unit": "events/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(els) / len(els),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -655,27 +671,69 @@ def run_batched(args, rank, world, local):
     per_launch_bytes = alg / units
     peak, peak_kind = peaks()
     achieved = per_launch_bytes / per_launch_s / 1e9
-    tr = traffic_per_launch("batched_bulk" if bulk else "batched")
+    tr = None if bulk else traffic_per_launch("batched")
     traffic = None
     if tr and tr.get("traffic_per_alg_byte"):
         traffic = tr["traffic_per_alg_byte"] * per_launch_bytes
     roof_kernel = ("spk::bulk_neurons_kernel + bulk_list_kernel + bulk_prop_kernel + bulk_post_kernel "
                    "(one timestep of all instances)" if bulk else "spk::step_kernel")
+    roof_timestep = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind, "kernel": roof_kernel, "launches": launches,
+                     "unit_timed": "timestep" if bulk else "launch", "alg_bytes_per_launch": per_launch_bytes,
+                     "ms_per_launch": 1000 * per_launch_s, "events_per_timestep": events / timesteps}
+    roofline, kernels = roof_timestep, None
+    if bulk:
+        # each kernel of one block launched alone between CUDA events on its
+        # stream: the kernels' device times, and the propagation kernel's own
+        # roofline (8 B per synaptic event and per plastic weight updated on a
+        # presynaptic event, both done by the propagation kernel)
+        ke0 = sum(n.events() for n in nets)
+        ks0 = [n.stdp_counts() for n in nets]
+        kms = b.time_kernels(args.block)
+        kev = sum(n.events() for n in nets) - ke0
+        kpre = sum(y[0] - x[0] for x, y in zip(ks0, [n.stdp_counts() for n in nets]))
+        tot = sum(kms.values())
+        kernels = {k: {"ms_per_timestep": v / args.block, "share": v / tot if tot else None} for k, v in kms.items()}
+        prop_bytes = (8 * kev + 8 * kpre) / args.block
+        prop_s = kms["propagation"] / 1000.0 / args.block
+        prop_ach = prop_bytes / prop_s / 1e9 if prop_s > 0 else None
+        pt = traffic_per_launch("batched_bulk_prop")
+        prop_traffic = pt["dram_bytes_per_event"] * kev / args.block if pt and pt.get("dram_bytes_per_event") else None
+        roofline = {"bound": "hbm", "achieved": prop_ach, "peak": peak, "unit": "GB/s",
+                    "frac": prop_ach / peak if prop_ach else None, "traffic": prop_traffic,
+                    "traffic_source": pt.get("source") if pt else None, "peak_kind": peak_kind,
+                    "kernel": "spk::bulk_prop_kernel / bulk_range_kernel (propagation and the STDP pre pass of "
+                              "all instances, one launch per timestep)",
+                    "launches": args.block, "unit_timed": "timestep",
+                    "alg_bytes_per_launch": prop_bytes, "ms_per_launch": 1000 * prop_s,
+                    "events_per_timestep": kev / args.block,
+                    "timing": "CUDA events around each launch on the batch stream, one block of timesteps"}
 
-    # plain form: the same instances, each alone on its own stream, one after another
-    plain_ev, plain_ms = 0, 0.0
-    for n in nets:
+    # plain form: the same instances, each alone with the schedule the
+    # library's planner gives it on its own (the persistent kernel), one after
+    # another: PLAIN_WARMUP timesteps, then plain_block timed
+    plain_ev, plain_ms, plain_sched = 0, 0.0, {}
+    for g in gens:
+        n = Net.generate(g, schedule(0, 0, 0, args.plain_block))
+        sc = n.schedule()
+        k = f"{sc['warps_per_cta']}x{sc['tile_posts']}x{sc['ctas']}"
+        plain_sched[k] = plain_sched.get(k, 0) + 1
         s = torch.cuda.ExternalStream(n.stream())
+        n.run_steps(PLAIN_WARMUP, True)
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         pe0 = n.events()
         a0.record(s)
         n.run_steps(args.plain_block, True)
         a1.record(s)
         a1.synchronize()
+        assert n.synchronize() == 0
         plain_ms += a0.elapsed_time(a1)
         plain_ev += n.events() - pe0
+        n.close()
     plain = {"value": plain_ev / (plain_ms / 1000.0), "unit": "events/s",
-             "sample": f"every instance alone for {args.plain_block} timesteps, one after another",
+             "sample": f"every instance alone under its own planner schedule (the persistent kernel), "
+                       f"{PLAIN_WARMUP} timesteps from reset then {args.plain_block} timed, one after another",
+             "schedules": plain_sched,
              "sim_s_per_wall_s": len(nets) * args.plain_block * DT / (plain_ms / 1000.0)}
 
     # end to end through the public API: rates up, batch step, spikes back
@@ -716,10 +774,29 @@ def run_batched(args, rank, world, local):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
+        # the CPU sample, and the same instances over the same timesteps from
+        # reset on the GPU (a batch of them alone), for a like-for-like ratio
         cs = CpuSample(gens)
-        cv, cel = cs.run(BATCH_CPU_STEPS, parallel=False)
-        cpu = {"value": cv, "unit": "events/s", "cores": 1, "kind": "port",
-               "sample": f"{cs.label}, {BATCH_CPU_STEPS} timesteps each from reset, {cel:.1f} s of CPU"}
+        threads = os.cpu_count() or 1
+        cv, cel = cs.run(BATCH_CPU_STEPS, threads)
+        sub = [Net.generate(gens[k], scheds[k]) for k in cs.index]
+        bs = Batch(sub, schedule(0, 0, 0, BATCH_CPU_STEPS))
+        bs.set_mode(mode)
+        sst = torch.cuda.ExternalStream(bs.stream())
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(sst)
+        bs.run_steps(BATCH_CPU_STEPS, True)
+        a1.record(sst)
+        a1.synchronize()
+        gpu_sample = sum(n.events() for n in sub) / (a0.elapsed_time(a1) / 1000.0)
+        bs.close()
+        for n in sub:
+            n.close()
+        cpu = {"value": cv, "unit": "events/s", "cores": threads, "kind": "port",
+               "sample": f"{cs.label}, {BATCH_CPU_STEPS} timesteps each from reset, {cel:.1f} s on {threads} "
+                         f"host threads",
+               "gpu_on_sample": {"value": gpu_sample, "unit": "events/s",
+                                 "what": "the same instances and timesteps as one batch on the GPU (device time)"}}
 
     if rank == 0:
         sch = {}
@@ -742,10 +819,7 @@ def run_batched(args, rank, world, local):
             "stdp_updates": {"pre": pre_u, "post_afferents": post_u},
             "plain": plain, "batched_over_plain": value / plain["value"],
             "status": status,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": roof_kernel, "launches": launches, "unit_timed": "timestep" if bulk else "launch",
-                         "alg_bytes_per_launch": per_launch_bytes, "ms_per_launch": 1000 * per_launch_s},
+            "roofline": roofline, "roofline_timestep": roof_timestep, "kernels": kernels,
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clk.summary(),
             "gpu_launches": launches + args.steps * len(nets),
         }

@@ -379,6 +379,22 @@ int spk_batch_step_block(spk_batch* batch);
 int spk_batch_run_steps_each(spk_batch* batch, const int64_t* n_steps, const int32_t* plasticity_on);
 int spk_batch_synchronize(spk_batch* batch);
 int spk_batch_launch_count(const spk_batch* batch, int64_t* launches);
+/* Per-kernel timing of a batch in bulk mode (no counterpart in the
+ * reference, whose examples time run() as a whole): advances the batch by
+ * n_steps exactly as spk_batch_run_steps does, but launches every kernel on
+ * its own, one after another on the batch stream (no graph, no programmatic
+ * overlap, the afferent pass not beside propagation), between two CUDA
+ * events, and adds each kind's device time in milliseconds to
+ * ms[SPK_KERNEL_KINDS].  A diagnostic: the sum exceeds the graph-launched
+ * time by the overlap it removes. */
+#define SPK_KERNEL_NEURONS 0     /* LIF, Poisson inputs, traces, spike words */
+#define SPK_KERNEL_LIST 1        /* the step's canonical key lists, spike store */
+#define SPK_KERNEL_RULES 2       /* per-synapse-trace rules, weight normalisation */
+#define SPK_KERNEL_POST 3        /* post-spike afferent pass (a second stream) */
+#define SPK_KERNEL_PROPAGATION 4 /* delayed propagation and the STDP pre pass */
+#define SPK_KERNEL_FINISH 5      /* run counters, once per block */
+#define SPK_KERNEL_KINDS 6
+int spk_batch_time_kernels(spk_batch* batch, int64_t n_steps, int32_t plasticity_on, double* ms);
 int spk_batch_stream(const spk_batch* batch, void** stream);
 /* Spikes of every network of the batch in one call: network after network,
  * each exactly as spk_net_read_spikes gives it (canonical order), gathered on

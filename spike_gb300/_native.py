@@ -123,6 +123,9 @@ class ServerStats(C.Structure):
 
 
 SPK_BATCH_WAVES, SPK_BATCH_BULK = 0, 1
+(SPK_KERNEL_NEURONS, SPK_KERNEL_LIST, SPK_KERNEL_RULES, SPK_KERNEL_POST, SPK_KERNEL_PROPAGATION,
+ SPK_KERNEL_FINISH, SPK_KERNEL_KINDS) = range(7)
+KERNEL_NAMES = ("neurons", "list", "rules", "post", "propagation", "finish")
 SPK_JOB_QUEUED, SPK_JOB_RUNNING, SPK_JOB_DONE, SPK_JOB_FAILED, SPK_JOB_CANCELLED = 0, 1, 2, 3, 4
 
 
@@ -212,6 +215,7 @@ _SIGS = {
     "spk_net_begin_run": (i32, [_VP, i64, i32]),
     "spk_batch_synchronize": (i32, [_VP]),
     "spk_batch_launch_count": (i32, [_VP, P(i64)]),
+    "spk_batch_time_kernels": (i32, [_VP, i64, i32, P(C.c_double)]),
     "spk_batch_stream": (i32, [_VP, P(_VP)]),
     "spk_batch_read_spikes": (i32, [_VP, i32, P(i32), P(f32), i64, P(i64), i32]),
     "spk_batch_destroy": (i32, [_VP]),

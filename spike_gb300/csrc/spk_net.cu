@@ -242,6 +242,10 @@ struct spk_net {
   float step_cost = 0.0f;  // measured or estimated time of one step alone (batch packing)
 };
 
+namespace spk {
+struct KernelTimer;
+}
+
 struct spk_batch {
   struct Wave {
     int first;  // first CTA-map entry of the wave
@@ -265,7 +269,11 @@ struct spk_batch {
   int pblocks_total = 0;
   BulkRangeBlock* drblocks = nullptr; // [rblocks_total] propagation ranges (networks of range tiles)
   int rblocks_total = 0;
-  int range_win_words = 0;            // ring-window words of a propagation range
+  RangeSmem range_smem{0, 0};         // ring window and bucket heads of a propagation range
+  // per-kernel timing (spk_batch_time_kernels): blocks go direct, each kernel
+  // between two events, and the intervals are added to timer_ms
+  spk::KernelTimer* timer = nullptr;
+  double* timer_ms = nullptr;
   BulkBlock* dblocks = nullptr;  // [blocks_total] blocks of 32-key words with real keys
   int blocks_total = 0;
   BulkPostItem* items = nullptr; // afferent-pass work list of a timestep
@@ -2083,41 +2091,110 @@ namespace spk {
 // rules], [normalisation after them], the afferent pass beside propagation,
 // and where a network normalises after the event-driven rule, that
 // normalisation and a second propagation pass that delivers.
-static int bulk_launch_block(spk_batch* b) {
+//
+// With `timer`, each kernel is bracketed by CUDA events on the stream it runs
+// on (the per-kernel timing of spk_batch_time_kernels; launches go direct).
+struct KernelTimer {
+  struct Mark {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  std::vector<Mark> marks;
+  size_t used = 0;
+  int begin(int kind, cudaStream_t st) {
+    if (used == marks.size()) {
+      Mark m{kind, nullptr, nullptr};
+      if (cudaEventCreate(&m.a) != cudaSuccess || cudaEventCreate(&m.b) != cudaSuccess) return SPK_ERR_CUDA;
+      marks.push_back(m);
+    }
+    marks[used].kind = kind;
+    return cudaEventRecord(marks[used].a, st) == cudaSuccess ? SPK_OK : SPK_ERR_CUDA;
+  }
+  int end(cudaStream_t st) { return cudaEventRecord(marks[used++].b, st) == cudaSuccess ? SPK_OK : SPK_ERR_CUDA; }
+  // adds the recorded intervals to ms[kind] (after the stream completed)
+  int collect(double* ms) {
+    for (size_t i = 0; i < used; ++i) {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, marks[i].a, marks[i].b) != cudaSuccess) return SPK_ERR_CUDA;
+      ms[marks[i].kind] += t;
+    }
+    used = 0;
+    return SPK_OK;
+  }
+  ~KernelTimer() {
+    for (auto& m : marks) {
+      cudaEventDestroy(m.a);
+      cudaEventDestroy(m.b);
+    }
+  }
+};
+
+static int bulk_launch_block(spk_batch* b, KernelTimer* timer = nullptr) {
   const int n = (int)b->nets.size();
   const int prop_smem = bulk_prop_layout(b->win_words, b->ts_max).total * 4;
+  const size_t range_bytes = range_smem_bytes(b->range_smem);
   DeviceInfo di;
   const int rc0 = device_info(&di);
   if (rc0) return rc0;
   const bool split = (b->norm_slots & 4) != 0;
   const int item_grid = std::min((b->n_dense_items + 7) / 8, di.sms * 8);
   int per_step = 0;
+#define T_BEGIN(kind, st)                         \
+  do {                                            \
+    if (timer) {                                  \
+      const int trc = timer->begin((kind), (st)); \
+      if (trc) return trc;                        \
+    }                                             \
+  } while (0)
+#define T_END(st)                      \
+  do {                                 \
+    if (timer) {                       \
+      const int trc = timer->end((st)); \
+      if (trc) return trc;             \
+    }                                  \
+  } while (0)
   for (int s = 0; s < b->K; ++s) {
     per_step = 0;
+    T_BEGIN(SPK_KERNEL_NEURONS, b->stream);
     SPK_CUDA(launch_overlapped(bulk_neurons_kernel, b->blocks_total, BULK_NEUR_WARPS * 32, 0, b->stream,
                                (const NetDev*)b->dd, (const BulkBlock*)b->dblocks, s, b->item_count));
+    T_END(b->stream);
+    T_BEGIN(SPK_KERNEL_LIST, b->stream);
     SPK_CUDA(launch_overlapped(bulk_list_kernel, n, BULK_LIST_THREADS, 0, b->stream, (const NetDev*)b->dd, s,
                                b->items, b->item_count, b->item_cap));
+    T_END(b->stream);
     per_step += 2;
     if ((b->norm_slots & 1) && b->n_dense_items) {
+      T_BEGIN(SPK_KERNEL_RULES, b->stream);
       bulk_norm_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s, 0);
+      T_END(b->stream);
       ++per_step;
     }
     if (b->any_dense && b->n_dense_items) {
+      T_BEGIN(SPK_KERNEL_RULES, b->stream);
       bulk_dense_stdp_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s);
+      T_END(b->stream);
       ++per_step;
     }
     if ((b->norm_slots & 2) && b->n_dense_items) {
+      T_BEGIN(SPK_KERNEL_RULES, b->stream);
       bulk_norm_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s, 1);
+      T_END(b->stream);
       ++per_step;
     }
+    // the afferent pass runs beside propagation on the second stream; timed
+    // runs put it on the batch stream so that each kernel has the GPU alone
+    cudaStream_t post_stream = timer ? b->stream : b->side;
     if (b->any_plastic) {
       SPK_CUDA(cudaEventRecord(b->fork, b->stream));
-      SPK_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0));
-      bulk_post_kernel<<<di.sms * 8, 256, 0, b->side>>>(b->dd, b->items, b->item_count, b->item_cap);
-      SPK_CUDA(cudaEventRecord(b->join, b->side));
+      SPK_CUDA(cudaStreamWaitEvent(post_stream, b->fork, 0));
+      T_BEGIN(SPK_KERNEL_POST, post_stream);
+      bulk_post_kernel<<<di.sms * 8, 256, 0, post_stream>>>(b->dd, b->items, b->item_count, b->item_cap);
+      T_END(post_stream);
+      SPK_CUDA(cudaEventRecord(b->join, post_stream));
       ++per_step;
     }
+    T_BEGIN(SPK_KERNEL_PROPAGATION, b->stream);
     if (b->pblocks_total) {
       SPK_CUDA(launch_overlapped(split ? bulk_prop_kernel<1> : bulk_prop_kernel<0>, b->pblocks_total,
                                  BULK_PROP_WARPS * 32, (size_t)prop_smem, b->stream, (const NetDev*)b->dd,
@@ -2126,16 +2203,20 @@ static int bulk_launch_block(spk_batch* b) {
     }
     if (b->rblocks_total) {
       SPK_CUDA(launch_overlapped(split ? bulk_range_kernel<1> : bulk_range_kernel<0>, b->rblocks_total,
-                                 RANGE_THREADS, (size_t)b->range_win_words * 4, b->stream, (const NetDev*)b->dd,
-                                 (const BulkRangeBlock*)b->drblocks, s, b->range_win_words));
+                                 RANGE_THREADS, range_bytes, b->stream, (const NetDev*)b->dd,
+                                 (const BulkRangeBlock*)b->drblocks, s, b->range_smem));
       ++per_step;
     }
+    T_END(b->stream);
     if (b->any_plastic) SPK_CUDA(cudaStreamWaitEvent(b->stream, b->join, 0));
     if (split) {
       if (b->n_dense_items) {
+        T_BEGIN(SPK_KERNEL_RULES, b->stream);
         bulk_norm_kernel<<<item_grid, 256, 0, b->stream>>>(b->dd, b->dense_items, b->n_dense_items, s, 2);
+        T_END(b->stream);
         ++per_step;
       }
+      T_BEGIN(SPK_KERNEL_PROPAGATION, b->stream);
       if (b->pblocks_total) {
         SPK_CUDA(launch_overlapped(bulk_prop_kernel<2>, b->pblocks_total, BULK_PROP_WARPS * 32,
                                    (size_t)prop_smem, b->stream, (const NetDev*)b->dd,
@@ -2143,15 +2224,19 @@ static int bulk_launch_block(spk_batch* b) {
         ++per_step;
       }
       if (b->rblocks_total) {
-        SPK_CUDA(launch_overlapped(bulk_range_kernel<2>, b->rblocks_total, RANGE_THREADS,
-                                   (size_t)b->range_win_words * 4, b->stream, (const NetDev*)b->dd,
-                                   (const BulkRangeBlock*)b->drblocks, s, b->range_win_words));
+        SPK_CUDA(launch_overlapped(bulk_range_kernel<2>, b->rblocks_total, RANGE_THREADS, range_bytes, b->stream,
+                                   (const NetDev*)b->dd, (const BulkRangeBlock*)b->drblocks, s, b->range_smem));
         ++per_step;
       }
+      T_END(b->stream);
     }
   }
+  T_BEGIN(SPK_KERNEL_FINISH, b->stream);
   bulk_finish_kernel<<<(n + 255) / 256, 256, 0, b->stream>>>(b->dd, n, b->K);
+  T_END(b->stream);
   SPK_CUDA(cudaGetLastError());
+#undef T_BEGIN
+#undef T_END
   b->step_launches = per_step;
   return SPK_OK;
 }
@@ -2200,7 +2285,17 @@ int spk_batch_run_steps_each(spk_batch* b, const int64_t* n_steps, const int32_t
   const int64_t blocks = (most + b->K - 1) / b->K;
   for (int64_t blk = 0; blk < blocks; ++blk) {
     if (b->mode == SPK_BATCH_BULK) {
-      const int rc = bulk_run_block(b);
+      int rc;
+      if (b->timer) {
+        rc = bulk_launch_block(b, b->timer);
+        b->launches += (int64_t)b->step_launches * b->K + 1;
+        if (rc == SPK_OK && (cudaStreamSynchronize(b->stream) != cudaSuccess ||
+                             (b->side && cudaStreamSynchronize(b->side) != cudaSuccess)))
+          rc = SPK_ERR_CUDA;
+        if (rc == SPK_OK) rc = b->timer->collect(b->timer_ms);
+      } else {
+        rc = bulk_run_block(b);
+      }
       if (rc) return rc;
       continue;
     }
@@ -2340,13 +2435,16 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
         b->win_words = std::max(b->win_words, (n->hd.B - 3) * n->hd.TS * n->hd.L);
       }
       b->win_words = std::min(b->win_words, BULK_WIN_CAP);
-      // range windows: as many of a range's delay slots as the cap holds
-      b->range_win_words = 0;
+      // range windows: as many of a range's delay slots as the cap holds;
+      // bucket heads: one per delay cell of the D_max slots where they fit
+      b->range_smem = RangeSmem{0, 0};
       for (const spk_net* n : b->nets) {
         if (n->hd.TS < RANGE_MIN_TS) continue;
         const int slot_words = n->hd.TS * n->hd.L;
         const int ws = std::min(n->hd.B - 3, RANGE_WIN_CAP / slot_words);
-        b->range_win_words = std::max(b->range_win_words, ws * slot_words);
+        b->range_smem.win_words = std::max(b->range_smem.win_words, ws * slot_words);
+        b->range_smem.head_words =
+            std::max(b->range_smem.head_words, std::min((n->hd.B - 3) * slot_words, RANGE_HEAD_CAP));
       }
       const size_t r_bytes = align_up(sizeof(BulkRangeBlock) * ranges.size(), 256);
       const size_t t_bytes = align_up(sizeof(BulkPropBlock) * tiles.size(), 256);
@@ -2394,7 +2492,7 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, prop_smem));
       SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, prop_smem));
       SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, prop_smem));
-      const int range_smem = b->range_win_words * 4;
+      const int range_smem = (int)range_smem_bytes(b->range_smem);
       SPK_CUDA(cudaFuncSetAttribute(bulk_range_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, range_smem));
       SPK_CUDA(cudaFuncSetAttribute(bulk_range_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, range_smem));
       SPK_CUDA(cudaFuncSetAttribute(bulk_range_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, range_smem));
@@ -2442,6 +2540,26 @@ int spk_batch_run_steps(spk_batch* b, int64_t n_steps, int32_t plasticity_on) {
     std::vector<int64_t> each(b->nets.size(), n_steps);
     std::vector<int32_t> plastic(b->nets.size(), plasticity_on ? 1 : 0);
     return spk_batch_run_steps_each(b, each.data(), plastic.data());
+  });
+}
+
+int spk_batch_time_kernels(spk_batch* b, int64_t n_steps, int32_t plasticity_on, double* ms) {
+  if (!b || !ms || n_steps < 0 || n_steps > 0x7fffffff) return SPK_ERR_INVALID;
+  if (b->mode != SPK_BATCH_BULK) {
+    set_error("per-kernel timing needs a batch in bulk mode");
+    return SPK_ERR_UNSUPPORTED;
+  }
+  if (n_steps == 0) return SPK_OK;
+  return guarded([&]() -> int {
+    KernelTimer timer;
+    b->timer = &timer;
+    b->timer_ms = ms;
+    std::vector<int64_t> each(b->nets.size(), n_steps);
+    std::vector<int32_t> plastic(b->nets.size(), plasticity_on ? 1 : 0);
+    const int rc = spk_batch_run_steps_each(b, each.data(), plastic.data());
+    b->timer = nullptr;
+    b->timer_ms = nullptr;
+    return rc;
   });
 }
 

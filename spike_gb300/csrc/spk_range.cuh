@@ -39,15 +39,34 @@
 
 namespace spk {
 
-constexpr int RANGE_MIN_TS = 512;                      // tiles propagated by bulk_range_kernel
-constexpr int RANGE_WIN_CAP = 16 * 1024;               // ring-window words of a range at most (64 KB)
-constexpr int RANGE_THREADS = 256;
-constexpr int RANGE_U = 4;                             // stream positions per thread and round
+// Tuning constants (measured on the 256-instance sweep), overridable at
+// compile time.
+#ifndef SPK_RANGE_MIN_TS
+#define SPK_RANGE_MIN_TS 512
+#endif
+#ifndef SPK_RANGE_WIN_CAP
+#define SPK_RANGE_WIN_CAP 0
+#endif
+#ifndef SPK_RANGE_THREADS
+#define SPK_RANGE_THREADS 256
+#endif
+#ifndef SPK_RANGE_U
+#define SPK_RANGE_U 4
+#endif
+#ifndef SPK_RANGE_KEYS
+#define SPK_RANGE_KEYS 1024
+#endif
+#ifndef SPK_RANGE_MINB
+#define SPK_RANGE_MINB 3
+#endif
+constexpr int RANGE_MIN_TS = SPK_RANGE_MIN_TS;         // tiles propagated by bulk_range_kernel
+constexpr int RANGE_WIN_CAP = SPK_RANGE_WIN_CAP;       // ring-window words of a range at most
+constexpr int RANGE_HEAD_CAP = 16 * 1024;              // bucket heads of a range at most (64 KB)
+constexpr int RANGE_THREADS = SPK_RANGE_THREADS;
+constexpr int RANGE_U = SPK_RANGE_U;                   // stream positions per thread and round
 constexpr int RANGE_ROUND = RANGE_THREADS * RANGE_U;   // entries per round
-constexpr int RANGE_KEYS = 1024;                       // list keys per chunk
+constexpr int RANGE_KEYS = SPK_RANGE_KEYS;             // list keys per chunk
 constexpr int RANGE_KPT = RANGE_KEYS / RANGE_THREADS;  // keys per thread while staging
-constexpr int RANGE_HASH_BITS = 12;
-constexpr int RANGE_HASH = 1 << RANGE_HASH_BITS;       // bucket heads
 constexpr int RANGE_POS_BITS = 12;                     // position field of a head word
 constexpr unsigned short RANGE_NONE = 0xffff;
 static_assert(RANGE_ROUND <= (1 << RANGE_POS_BITS), "round positions fit the head word");
@@ -62,8 +81,7 @@ struct BulkRangeBlock {
 };
 
 struct RangeShared {
-  uint32_t head[RANGE_HASH];        // bucket heads: epoch << 12 | position
-  uint32_t ecell[RANGE_ROUND];      // ring cell of each position of the round
+  uint32_t ecell[RANGE_ROUND];      // delay cell of each position of the round
   float econ[RANGE_ROUND];          // its contribution
   unsigned short enxt[RANGE_ROUND]; // next position of its bucket's chain
   uint32_t list[RANGE_KEYS];        // list words of the chunk (key | A << 31 | P << 30)
@@ -74,30 +92,48 @@ struct RangeShared {
   float scl[MAX_CLASSES];
 };
 
-__device__ __forceinline__ uint32_t range_hash(uint32_t cell) {
-  return (cell * 0x9E3779B1u) >> (32 - RANGE_HASH_BITS);
+// Dynamic shared memory of a launch in 4-byte words: the ring window of the
+// largest range followed by its bucket heads.
+struct RangeSmem {
+  int win_words, head_words;
+};
+__host__ __device__ inline size_t range_smem_bytes(const RangeSmem& z) {
+  return 4 * ((size_t)z.win_words + z.head_words);
 }
 
-// Where ring cell `c` of the range lives this step: in the shared-memory
-// window (delays 1..ws after the current slot) or in the ring in global memory.
+// A contribution's target within the range: `dc` its delay cell, the index
+// (delay - 1) * TS * L + post * L + label over the delay slots after the
+// current one (also its index in the ring window); where the cell lives this
+// step: the window (delay <= ws) or the ring slice in global memory.
 struct RangeRing {
   float* ring;   // the range's ring slice [B][TS * L]
   float* win;    // window [ws][TS * L] (shared memory)
   int ws, slot, B, slot_words;
-  __device__ __forceinline__ float* at(uint32_t c) const {
-    const int sl = (int)(c / (uint32_t)slot_words);
-    int dl = sl - slot;
-    if (dl <= 0) dl += B;
-    if (dl <= ws) return win + (size_t)(dl - 1) * slot_words + (c - (uint32_t)sl * slot_words);
-    return ring + c;
+  __device__ __forceinline__ float* global_at(uint32_t dc, int dl) const {
+    int sl = slot + dl;
+    if (sl >= B) sl -= B;
+    return ring + (size_t)sl * slot_words + (dc - (uint32_t)(dl - 1) * slot_words);
+  }
+  // ring words in global memory go through L2 only: a later round's load
+  // must see an earlier round's store made by another thread of the CTA
+  __device__ __forceinline__ float load(uint32_t dc) const {
+    const int dl = (int)(dc / (uint32_t)slot_words) + 1;
+    return dl <= ws ? win[dc] : __ldcg(global_at(dc, dl));
+  }
+  __device__ __forceinline__ void store(uint32_t dc, float v) const {
+    const int dl = (int)(dc / (uint32_t)slot_words) + 1;
+    if (dl <= ws)
+      win[dc] = v;
+    else
+      __stcg(global_at(dc, dl), v);
   }
 };
 
-// Applies a bucket chain of two or more positions (head `r`): cell by cell,
-// contributions in ascending position.  `my_cell`/`my_val` are the head's own
-// cell and its preloaded ring word.
-__device__ __noinline__ void range_apply_chain(const RangeShared& sm, const RangeRing& rr, int r, uint32_t my_cell,
-                                               float my_val) {
+// Applies a bucket chain of positions holding more than one delay cell (a
+// hashed head table): cell by cell, contributions in ascending position.
+// `my_cell`/`my_val` are the head's own cell and its preloaded ring word.
+__device__ __noinline__ void range_apply_mixed_chain(const RangeShared& sm, const RangeRing& rr, int r,
+                                                     uint32_t my_cell, float my_val) {
   unsigned long long last = 0ull;
   long long cur = -1;
   float acc = 0.0f;
@@ -111,28 +147,52 @@ __device__ __noinline__ void range_apply_chain(const RangeShared& sm, const Rang
     const uint32_t c = (uint32_t)(best >> RANGE_POS_BITS);
     const int rk = (int)(best & ((1u << RANGE_POS_BITS) - 1));
     if ((long long)c != cur) {
-      if (cur >= 0) *rr.at((uint32_t)cur) = acc;
+      if (cur >= 0) rr.store((uint32_t)cur, acc);
       cur = c;
-      acc = c == my_cell ? my_val : *rr.at(c);
+      acc = c == my_cell ? my_val : rr.load(c);
     }
     acc = acc + sm.econ[rk];
     last = best + 1;
   }
-  if (cur >= 0) *rr.at((uint32_t)cur) = acc;
+  if (cur >= 0) rr.store((uint32_t)cur, acc);
+}
+
+// The sum, in ascending position, of a chain whose positions all hold the
+// head's cell, added to `val` one contribution at a time.
+__device__ __forceinline__ float range_chain_sum(const RangeShared& sm, int r, float val) {
+  const int b = sm.enxt[r];
+  if (sm.enxt[b] == RANGE_NONE) {  // two positions: the common case
+    const int lo = min(r, b), hi = max(r, b);
+    return (val + sm.econ[lo]) + sm.econ[hi];
+  }
+  float acc = val;
+  int last = -1;
+  for (;;) {
+    int best = RANGE_ROUND;
+    for (int it = r; it != RANGE_NONE; it = sm.enxt[it])
+      if (it > last && it < best) best = it;
+    if (best == RANGE_ROUND) break;
+    acc = acc + sm.econ[best];
+    last = best;
+  }
+  return acc;
 }
 
 // kPass as bulk_prop_kernel: 0 the single fused pass; 1 and 2 the two passes
 // of a batch in which a network normalises its weights after the
 // event-driven rule.
 //
-// `win_words` is the dynamic shared memory of the launch (4-byte words): the
-// range's ring window, the delay slots 1..ws after the current one, read when
-// the step's first chunk says the range's entries are dense enough and
-// written back (slots that received a contribution) at the end.
+// Dynamic shared memory (`sz`, in 4-byte words): the range's ring window, the
+// delay slots 1..ws after the current one, read when the step's first chunk
+// says the range's entries are dense enough and written back (slots that
+// received a contribution) at the end; then the bucket heads.  When the
+// range's D_max delay slots fit the heads, a bucket is one delay cell, so
+// every chain holds one cell; otherwise cells are hashed into the heads and a
+// chain may mix cells.
 template <int kPass>
-__global__ void __launch_bounds__(RANGE_THREADS, 3)
+__global__ void __launch_bounds__(RANGE_THREADS, SPK_RANGE_MINB)
     bulk_range_kernel(const NetDev* __restrict__ nets, const BulkRangeBlock* __restrict__ blocks, int s,
-                      int win_words) {
+                      RangeSmem sz) {
   extern __shared__ __align__(16) float rwin[];
   __shared__ __align__(16) NetDev sd;
   __shared__ unsigned s_dirty;
@@ -140,6 +200,7 @@ __global__ void __launch_bounds__(RANGE_THREADS, 3)
   __shared__ RangeShared sm;
   __shared__ int s_nlist;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  uint32_t* head = (uint32_t*)(rwin + sz.win_words);
   const BulkRangeBlock rb = blocks[blockIdx.x];
   {
     const uint32_t* src = (const uint32_t*)(nets + rb.net);
@@ -147,7 +208,6 @@ __global__ void __launch_bounds__(RANGE_THREADS, 3)
     for (int i = tid; i < (int)(sizeof(NetDev) / 4); i += RANGE_THREADS) dst[i] = __ldg(src + i);
     if (tid == 0) sctl = load_ctl(rb.ctl);
   }
-  for (int i = tid; i < RANGE_HASH; i += RANGE_THREADS) sm.head[i] = 0u;
   if (tid == 0) s_dirty = 0u;
   pdl_wait_then_release();
   if (tid == 0) s_nlist = *rb.n_list;
@@ -171,16 +231,22 @@ __global__ void __launch_bounds__(RANGE_THREADS, 3)
   }
   const int TS = d.TS, L = d.L, B = d.B, KL = d.KL, n_tiles = d.n_tiles;
   const int p0 = rb.tile * TS;
-  float* ring = d.ring + (size_t)rb.tile * B * TS * L;
+  const int slot_words = TS * L;  // a multiple of 32
+  float* ring = d.ring + (size_t)rb.tile * B * slot_words;
   const int* rowptr = d.rowptr + rb.tile;
   const uint2* entries = d.entries;
   uint2* csc = d.csc;
   const StdpConst sc = stdp_const(d);
   if (tid < MAX_CLASSES) sm.scl[tid] = d.scale_tab[tid];
+  // bucket heads: one per delay cell when they fit, else a power-of-two hash
+  const int dcells = (B - 3) * slot_words;
+  const bool direct = dcells <= sz.head_words;
+  const int hbits = 31 - __clz(max(sz.head_words, 1));
+  const int hwords = direct ? dcells : (1 << hbits);
+  for (int i = tid; i < hwords; i += RANGE_THREADS) head[i] = 0u;
 
   unsigned long long ev = 0, n_pre = 0;
   uint32_t epoch = 0;
-  const int slot_words = TS * L;  // a multiple of 32
   RangeRing rr{ring, rwin, 0, st.slot, B, slot_words};
   unsigned dirty = 0u;  // window slots this thread wrote
   for (int kb = 0; kb < n_list; kb += RANGE_KEYS) {
@@ -239,7 +305,7 @@ __global__ void __launch_bounds__(RANGE_THREADS, 3)
       // The window pays when the step's entries (estimated from the first
       // chunk) would touch more ring sectors one by one than the window has
       // words to move: about one entry per four window words.
-      const int ws_max = min(B - 3, win_words / slot_words);
+      const int ws_max = min(B - 3, sz.win_words / slot_words);
       const long long est = (long long)total * ((n_list + RANGE_KEYS - 1) / RANGE_KEYS);
       rr.ws = (ws_max > 0 && est * 4 > (long long)ws_max * slot_words) ? ws_max : 0;
       for (int k = 0; k < rr.ws; ++k) {
@@ -261,7 +327,7 @@ __global__ void __launch_bounds__(RANGE_THREADS, 3)
       const int p = base + tid * RANGE_U;
       int j = 0;
       if (p < total) {
-        int lo = 0, hi = RANGE_KEYS - 1;
+        int lo = 0, hi = nk - 1;
         while (lo < hi) {
           const int mid = (lo + hi) >> 1;
           if (sm.koff[mid + 1] <= p) lo = mid + 1;
@@ -280,25 +346,10 @@ __global__ void __launch_bounds__(RANGE_THREADS, 3)
         }
       }
     };
-    int jj[RANGE_U];
-    uint2 en[RANGE_U];
-    locate(0, jj, en);
-    for (int rbase = 0; rbase < total; rbase += RANGE_ROUND) {
-      ++epoch;
-      int jn[RANGE_U];
-      uint2 enn[RANGE_U];
-      if (rbase + RANGE_ROUND < total) {
-        locate(rbase + RANGE_ROUND, jn, enn);  // the next round's entries in flight
-      } else {
-#pragma unroll
-        for (int u = 0; u < RANGE_U; ++u) {
-          jn[u] = -1;
-          enn[u] = make_uint2(0u, 0u);
-        }
-      }
-      // plastic weights (and the post's trace and spike word) of this round
-      float wv[RANGE_U], ptv[RANGE_U];
-      uint32_t pw[RANGE_U];
+    // the plastic weights of a round's entries, and with STDP their posts'
+    // traces and spike words
+    auto gather = [&](const int (&jj)[RANGE_U], const uint2 (&en)[RANGE_U], float (&wv)[RANGE_U],
+                      float (&ptv)[RANGE_U], uint32_t (&pw)[RANGE_U]) {
 #pragma unroll
       for (int u = 0; u < RANGE_U; ++u) {
         wv[u] = ptv[u] = 0.0f;
@@ -310,6 +361,27 @@ __global__ void __launch_bounds__(RANGE_THREADS, 3)
             ptv[u] = d.post_trace[p0 + q];
             pw[u] = d.bitsA[(KL + p0 + q) >> 5];
           }
+        }
+      }
+    };
+    int jj[RANGE_U];
+    uint2 en[RANGE_U];
+    float wv[RANGE_U], ptv[RANGE_U];
+    uint32_t pw[RANGE_U];
+    locate(0, jj, en);
+    gather(jj, en, wv, ptv, pw);
+    for (int rbase = 0; rbase < total; rbase += RANGE_ROUND) {
+      ++epoch;
+      int jn[RANGE_U];
+      uint2 enn[RANGE_U];
+      const bool more = rbase + RANGE_ROUND < total;
+      if (more) {
+        locate(rbase + RANGE_ROUND, jn, enn);  // the next round's entries in flight
+      } else {
+#pragma unroll
+        for (int u = 0; u < RANGE_U; ++u) {
+          jn[u] = -1;
+          enn[u] = make_uint2(0u, 0u);
         }
       }
       uint32_t cell[RANGE_U], tagv[RANGE_U];
@@ -347,18 +419,17 @@ __global__ void __launch_bounds__(RANGE_THREADS, 3)
         }
         if (A) {
           ++ev;
-          int sl = st.slot + dl;
-          if (sl >= B) sl -= B;
-          const uint32_t c = (uint32_t)((sl * TS + q) * L + lb);
+          const uint32_t dc = (uint32_t)((dl - 1) * slot_words + q * L + lb);
           const int r = tid * RANGE_U + u;
           add[u] = true;
-          cell[u] = c;
+          cell[u] = dc;
           con[u] = contrib;
-          val[u] = dl <= rr.ws ? rwin[(size_t)(dl - 1) * slot_words + (q * L + lb)] : __ldcg(ring + c);
+          val[u] = rr.load(dc);
           tagv[u] = (epoch << RANGE_POS_BITS) | (uint32_t)r;
-          sm.ecell[r] = c;
           sm.econ[r] = contrib;
-          const uint32_t prev = atomicExch(&sm.head[range_hash(c)], tagv[u]);
+          if (!direct) sm.ecell[r] = dc;
+          const uint32_t h = direct ? dc : ((dc * 0x9E3779B1u) >> (32 - hbits));
+          const uint32_t prev = atomicExch(&head[h], tagv[u]);
           sm.enxt[r] = (prev >> RANGE_POS_BITS) == epoch ? (unsigned short)(prev & ((1u << RANGE_POS_BITS) - 1))
                                                            : RANGE_NONE;
         }
@@ -366,28 +437,33 @@ __global__ void __launch_bounds__(RANGE_THREADS, 3)
       __syncthreads();  // the round's chains are complete
 #pragma unroll
       for (int u = 0; u < RANGE_U; ++u) {
-        if (!add[u] || sm.head[range_hash(cell[u])] != tagv[u]) continue;
+        if (!add[u]) continue;
+        const uint32_t h = direct ? cell[u] : ((cell[u] * 0x9E3779B1u) >> (32 - hbits));
+        if (head[h] != tagv[u]) continue;
         const int r = tid * RANGE_U + u;
+        const int dl = (int)(cell[u] / (uint32_t)slot_words) + 1;
         if (sm.enxt[r] == RANGE_NONE) {
-          const int sl = (int)(cell[u] / (uint32_t)slot_words);
-          int dl = sl - st.slot;
-          if (dl <= 0) dl += B;
-          if (dl <= rr.ws) {
-            rwin[(size_t)(dl - 1) * slot_words + (cell[u] - (uint32_t)sl * slot_words)] = val[u] + con[u];
-            dirty |= 1u << (dl - 1);
-          } else {
-            __stcg(ring + cell[u], val[u] + con[u]);
-          }
+          rr.store(cell[u], val[u] + con[u]);
+        } else if (direct) {
+          rr.store(cell[u], range_chain_sum(sm, r, val[u]));
         } else {
-          range_apply_chain(sm, rr, r, cell[u], val[u]);
+          range_apply_mixed_chain(sm, rr, r, cell[u], val[u]);
           dirty |= rr.ws ? (1u << rr.ws) - 1u : 0u;
         }
+        if (dl <= rr.ws) dirty |= 1u << (dl - 1);
       }
+      // the next round's plastic weights in flight across the barrier
+      float wn[RANGE_U], ptn[RANGE_U];
+      uint32_t pwn[RANGE_U];
+      gather(jn, enn, wn, ptn, pwn);
       __syncthreads();  // the round's ring words are written
 #pragma unroll
       for (int u = 0; u < RANGE_U; ++u) {
         jj[u] = jn[u];
         en[u] = enn[u];
+        wv[u] = wn[u];
+        ptv[u] = ptn[u];
+        pw[u] = pwn[u];
       }
     }
   }

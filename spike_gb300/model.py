@@ -417,6 +417,13 @@ class Batch:
     def synchronize(self) -> int:
         return lib().spk_batch_synchronize(self.h)
 
+    def time_kernels(self, steps: int, plasticity_on: bool = True) -> dict:
+        """Advance `steps` timesteps in bulk mode with every kernel timed on
+        its own (spk_batch_time_kernels): milliseconds per kernel kind."""
+        ms = (C.c_double * N.SPK_KERNEL_KINDS)()
+        check(lib().spk_batch_time_kernels(self.h, steps, 1 if plasticity_on else 0, ms), "spk_batch_time_kernels")
+        return {name: ms[i] for i, name in enumerate(N.KERNEL_NAMES)}
+
     def launches(self) -> int:
         b = C.c_int64()
         check(lib().spk_batch_launch_count(self.h, C.byref(b)), "spk_batch_launch_count")
