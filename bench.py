@@ -904,7 +904,7 @@ def run_served(args, rank, world, local):
                      "running_at_close": int(sum(1 for i in infos if i.state == N.SPK_JOB_RUNNING)),
                      "queued_at_close": int(sum(1 for i in infos if i.state == N.SPK_JOB_QUEUED)),
                      "failed": int(sum(1 for i in infos if i.state == N.SPK_JOB_FAILED)),
-                     "blocks": int(st.blocks), "gpu_busy_s": st.busy_s},
+                     "blocks": int(st.blocks), "batch_rebuilds": int(st.rebuilds), "gpu_busy_s": st.busy_s},
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 

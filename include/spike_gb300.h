@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define SPK_ABI_VERSION 2
+#define SPK_ABI_VERSION 3
 
 /* ---- status codes ------------------------------------------------------ */
 #define SPK_OK 0
@@ -477,6 +477,7 @@ typedef struct spk_server_stats {
   int64_t blocks;       /* batch rounds run */
   double busy_s;        /* wall time with at least one job running */
   double uptime_s;
+  int64_t rebuilds;     /* batches built: at the first block and whenever jobs join */
 } spk_server_stats;
 
 int spk_server_start(const spk_server_opts* opts, spk_server** out);

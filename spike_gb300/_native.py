@@ -12,7 +12,7 @@ import os
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libspike_gb300.so")
 
-SPK_ABI_VERSION = 2
+SPK_ABI_VERSION = 3
 SPK_OK = 0
 SPK_ERR_INVALID = -1
 SPK_ERR_CUDA = -2
@@ -119,7 +119,8 @@ class JobInfo(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [("submitted", i64), ("running", i64), ("queued", i64), ("done", i64), ("failed", i64),
-                ("events", u64), ("blocks", i64), ("busy_s", C.c_double), ("uptime_s", C.c_double)]
+                ("events", u64), ("blocks", i64), ("busy_s", C.c_double), ("uptime_s", C.c_double),
+                ("rebuilds", i64)]
 
 
 SPK_BATCH_WAVES, SPK_BATCH_BULK = 0, 1

@@ -170,8 +170,11 @@ void admit(spk_server* S, std::vector<Job*>& out, size_t running_now) {
   }
 }
 
-// Copy a finished job's results to the host and free its network.
-void finish(spk_server* S, Job* j, int status) {
+// Copy a finished job's results to the host and free its network (with
+// `keep_net`, the network stays allocated: it is still held by the running
+// batch, which frees it at its next rebuild; having no steps left, its
+// kernels return at once meanwhile).
+void finish(spk_server* S, Job* j, int status, bool keep_net = false) {
   uint64_t ev = 0;
   spk_net_synaptic_events(j->net, &ev);
   int64_t n = 0;
@@ -185,9 +188,9 @@ void finish(spk_server* S, Job* j, int status) {
     ids.resize(got);
     times.resize(got);
   }
-  spk_net_destroy(j->net);
+  if (!keep_net) spk_net_destroy(j->net);
   std::lock_guard<std::mutex> lk(S->mu);
-  j->net = nullptr;
+  if (!keep_net) j->net = nullptr;
   j->events_seen = j->events;
   j->events = ev;
   j->spikes = n;
@@ -207,17 +210,49 @@ void finish(spk_server* S, Job* j, int status) {
   S->cv.notify_all();
 }
 
+// The batch is rebuilt only when its set of networks must grow: a finished
+// or cancelled job leaves its network in the batch ("retired": results read,
+// no steps left) until the next rebuild, which jobs joining or queued jobs
+// needing its memory trigger.  A set that only shrinks keeps its batch, and
+// with it the instantiated graph of the step block.
 void loop(spk_server* S) {
   cudaSetDevice(S->device);
-  std::vector<Job*> run, pending;
+  std::vector<Job*> run, pending, retired;
   spk_batch* batch = nullptr;
   bool dirty = true;
   const int K = S->o.steps_per_block;
+  auto free_retired = [&]() {
+    for (Job* j : retired) {
+      spk_net_destroy(j->net);
+      std::lock_guard<std::mutex> lk(S->mu);
+      j->net = nullptr;
+    }
+    retired.clear();
+  };
   while (true) {
     const size_t before = run.size();
+    if (batch && !retired.empty()) {
+      // queued work waiting for memory gets the retired networks' share back
+      bool queued = false;
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        queued = !S->queue.empty();
+      }
+      if (queued) {
+        spk_batch_destroy(batch);
+        batch = nullptr;
+        free_retired();
+        dirty = true;
+      }
+    }
     admit(S, run, 0);
     if (run.size() != before) dirty = true;
     if (run.empty()) {
+      if (batch) {
+        spk_batch_destroy(batch);
+        batch = nullptr;
+      }
+      free_retired();
       std::unique_lock<std::mutex> lk(S->mu);
       if (S->stopping) break;
       S->cv.wait_for(lk, std::chrono::milliseconds(20));
@@ -226,16 +261,20 @@ void loop(spk_server* S) {
     if (dirty) {
       if (batch) spk_batch_destroy(batch);
       batch = nullptr;
+      free_retired();
       std::vector<spk_net*> nets;
       for (Job* j : run) nets.push_back(j->net);
       const spk_schedule bs{0, 0, 0, K};
       int rc = spk_batch_create(nets.data(), (int32_t)nets.size(), &bs, &batch);
       if (rc == SPK_OK && S->o.mode == SPK_BATCH_BULK) rc = spk_batch_set_mode(batch, SPK_BATCH_BULK);
       if (rc != SPK_OK) {
+        if (batch) spk_batch_destroy(batch);
+        batch = nullptr;
         for (Job* j : run) finish(S, j, rc);
         run.clear();
         continue;
       }
+      S->st.rebuilds++;
       dirty = false;
     }
     std::vector<int64_t> steps(run.size());
@@ -264,17 +303,30 @@ void loop(spk_server* S) {
     for (Job* j : run) {
       int js = SPK_OK;
       if (st != SPK_OK) js = spk_net_synchronize(j->net);
-      if (js != SPK_OK || j->steps_done >= j->steps_total || j->cancel) {
+      if (js != SPK_OK) {
+        // a failed block: the batch is rebuilt without this network
         if (batch) {
           spk_batch_destroy(batch);  // a batch never outlives a network it holds
           batch = nullptr;
         }
         finish(S, j, js);
         dirty = true;
+      } else if (j->steps_done >= j->steps_total) {
+        finish(S, j, SPK_OK, batch != nullptr);
+        if (batch) retired.push_back(j);
+      } else if (j->cancel) {
+        // a cancelled job still has steps: the batch must drop it
+        if (batch) {
+          spk_batch_destroy(batch);
+          batch = nullptr;
+        }
+        finish(S, j, SPK_OK);
+        dirty = true;
       } else {
         keep.push_back(j);
       }
     }
+    if (!batch) free_retired();  // the batch that held them is gone
     run.swap(keep);
     if (!pending.empty()) {
       run.insert(run.end(), pending.begin(), pending.end());
@@ -285,6 +337,7 @@ void loop(spk_server* S) {
     if (S->stopping) break;
   }
   if (batch) spk_batch_destroy(batch);
+  free_retired();
   for (Job* j : run) {
     j->cancel = true;
     finish(S, j, SPK_OK);
