@@ -543,6 +543,13 @@ int spk_net_generate_estimate(const spk_gen_desc* desc, const spk_schedule* sche
  *    (uint64 at byte 32; zero it to clear the store), the synaptic events
  *    delivered (uint64 at byte 40) and the device status (int32 at byte 48: 0,
  *    SPK_ERR_TIMEOUT or SPK_ERR_OVERFLOW), valid once the stream has finished.
+ *    A non-zero status stays in run_state across later calls until the caller
+ *    clears it.  After SPK_ERR_OVERFLOW the state is sound (only spikes beyond
+ *    spike_capacity were dropped): zero the status and the spike count to go
+ *    on.  After SPK_ERR_TIMEOUT the CTAs stopped at different timesteps, so
+ *    the state buffers (V, last_spike, syn_trace, ring, input_next, the STDP
+ *    traces and plastic weights) are inconsistent: reload them from a copy
+ *    taken before the call and zero run_state before the next call.
  *
  * The first call on a device resolves the scratch array's device address
  * (cudaGetSymbolAddress) with that device current; make that first call
@@ -550,7 +557,9 @@ int spk_net_generate_estimate(const spk_gen_desc* desc, const spk_schedule* sche
  * clears the parts that must start at zero, so calls whose work overlaps on
  * the GPU (different streams, or different host threads on one device) race
  * and must be serialized by the caller.  Networks whose scratch exceeds
- * SPK_NOALLOC_SCRATCH_BYTES are rejected with SPK_ERR_INVALID.  Plasticity
+ * SPK_NOALLOC_SCRATCH_BYTES, and time constants that are not positive (tau_m,
+ * label taus, STDP taus) or a negative refractory period, are rejected with
+ * SPK_ERR_INVALID before any device work.  Plasticity
  * here is the weight-dependent rule (the persistent kernel's); the
  * per-synapse-trace rules and the weight normalisation need a network from
  * spk_net_create. */

@@ -488,6 +488,35 @@ struct ModelSpec {
   int record_inputs = 0;
 };
 
+// The time constants the step divides by (k = dt / tau_m, the label decays,
+// the STDP trace decays) must be positive and the refractory period finite and
+// non-negative: zero or negative values would give the run inf/NaN constants.
+static int check_time_constants(float dt, const spk_neuron_group* groups, int n_groups, int kind, int L,
+                                const float* label_tau, float refractory, bool has_stdp, const spk_stdp_params& sp) {
+  for (int g = 0; g < n_groups; ++g)
+    if (!(groups[g].tau_m > 0.0f) || !std::isfinite(groups[g].tau_m)) {
+      set_error("group %d: tau_m %g must be positive", g, (double)groups[g].tau_m);
+      return SPK_ERR_INVALID;
+    }
+  if (kind != SPK_SYN_VOLTAGE)
+    for (int l = 0; l < L; ++l)
+      if (!(label_tau[l] > 0.0f) || !std::isfinite(label_tau[l])) {
+        set_error("label %d: tau %g must be positive", l, (double)label_tau[l]);
+        return SPK_ERR_INVALID;
+      }
+  if (!(refractory >= 0.0f) || !std::isfinite(refractory)) {
+    set_error("refractory period %g must be finite and non-negative", (double)refractory);
+    return SPK_ERR_INVALID;
+  }
+  if (has_stdp && (!(sp.tau_plus > 0.0f) || !(sp.tau_minus > 0.0f) || !std::isfinite(sp.tau_plus) ||
+                   !std::isfinite(sp.tau_minus))) {
+    set_error("STDP tau_plus %g and tau_minus %g must be positive", (double)sp.tau_plus, (double)sp.tau_minus);
+    return SPK_ERR_INVALID;
+  }
+  (void)dt;
+  return SPK_OK;
+}
+
 static int validate_spec(const ModelSpec& m) {
   if (m.stdp_rule < SPK_STDP_WEIGHT_DEPENDENT || m.stdp_rule > SPK_STDP_CUSTOM) {
     set_error("unknown STDP rule %d", m.stdp_rule);
@@ -537,7 +566,7 @@ static int validate_spec(const ModelSpec& m) {
     set_error("conductance synapses need label_vhat");
     return SPK_ERR_INVALID;
   }
-  return SPK_OK;
+  return check_time_constants(m.dt, m.groups, m.n_groups, m.kind, m.L, m.label_tau, m.t_ref, m.has_stdp, m.stdp);
 }
 
 // A new handle with the model fields of `m` and a plan for ring depth B.
@@ -2931,6 +2960,11 @@ static int step_noalloc_impl(const spk_device_net* a, int64_t n_steps, int plast
                (a->n_plastic_scales > 0 && !a->plastic_scales))) {
     set_error("between 0 and %d plastic weight scales are supported", MAX_CLASSES - 1);
     return SPK_ERR_INVALID;
+  }
+  {
+    const int rc = check_time_constants(a->dt, a->groups, a->n_groups, kind, L, a->label_tau, a->refractory_period,
+                                        stdp != 0, a->stdp);
+    if (rc) return rc;
   }
   if (!a->rowptr || !a->entries || !a->V || !a->last_spike || !a->ring || !a->run_state ||
       (kind != SPK_SYN_VOLTAGE && !a->syn_trace) || (Nin > 0 && (!a->input_next || !a->rates)) ||

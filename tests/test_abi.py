@@ -68,6 +68,40 @@ def test_noalloc_rejects_networks_beyond_its_scratch():
     assert lib.spk_step_noalloc(None, 1, 0, ctypes.c_float(0.0), None) == _native.SPK_ERR_INVALID
 
 
+def test_time_constants_are_validated_before_any_device_call():
+    """A zero membrane or synaptic time constant, a non-positive STDP tau or a
+    negative refractory period would give inf/NaN decay constants:
+    spk_net_create and spk_step_noalloc refuse them before any device call."""
+    import descs
+    from spike_gb300.model import STDPParams
+    lib = _native.lib()
+    good = dict(count=10, tau_m=0.02)
+    cases = [dict(groups=[dict(count=10, tau_m=0.0)]),
+             dict(groups=[good], kind=_native.SPK_SYN_CURRENT, label_tau=[-0.005]),
+             dict(groups=[good], refractory=-0.001),
+             dict(groups=[good], pre=[0], post=[1], weight=[1e-4], delay=[1], plastic=[1],
+                  stdp=STDPParams(tau_plus=0.0, tau_minus=0.02))]
+    for kw in cases:
+        d = descs.Desc(**kw)
+        h = ctypes.c_void_p()
+        assert lib.spk_net_create(ctypes.byref(d.desc), None, ctypes.byref(h)) == _native.SPK_ERR_INVALID, kw
+        assert b"must be" in lib.spk_last_error(), lib.spk_last_error()
+    g = (_native.NeuronGroup * 1)()
+    g[0].start, g[0].count, g[0].tau_m, g[0].R, g[0].theta = 0, 64, 0.0, 1e8, 0.02
+    dummy = ctypes.create_string_buffer(64)
+    addr = ctypes.addressof(dummy)
+    dn = _native.DeviceNet()
+    dn.n_neurons, dn.n_inputs, dn.n_labels, dn.synapse_kind, dn.max_delay = 64, 0, 1, _native.SPK_SYN_VOLTAGE, 1
+    dn.warps_per_cta, dn.tile_posts, dn.ctas = 2, 32, 1
+    dn.dt, dn.refractory_period = 1e-4, 2e-3
+    dn.n_groups, dn.groups = 1, g
+    for f in ("rowptr", "entries", "V", "last_spike", "ring", "spikes", "run_state"):
+        setattr(dn, f, addr)
+    dn.spike_capacity = 1
+    assert lib.spk_step_noalloc(ctypes.byref(dn), 0, 0, ctypes.c_float(0.0), None) == _native.SPK_ERR_INVALID
+    assert b"tau_m" in lib.spk_last_error()
+
+
 def test_malformed_generated_networks_are_rejected_before_any_device_call():
     from spike_gb300 import GenNetwork, Projection
     lib = _native.lib()

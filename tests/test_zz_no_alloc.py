@@ -201,3 +201,56 @@ def test_noalloc_matches_run_steps_conductance():
     d = m.desc()
     spikes = run_both(d, 8, 32, 2, [(300, False), (300, False)])
     assert spikes > 100
+
+
+def test_noalloc_matches_run_steps_current_synapses_single_cta():
+    """Current synapses with two labels on one CTA (no cooperative launch),
+    recording the inputs' spikes too."""
+    rng = np.random.default_rng(3)
+    n, S = 120, 3000
+    pre = rng.integers(-50, n, S)
+    post = rng.integers(0, n, S)
+    d = descs.Desc(kind=N.SPK_SYN_CURRENT, n_labels=2, label_tau=[0.003, 0.008],
+                   groups=[dict(count=n, tau_m=0.02, R=1e8, v0=-0.07, vreset=-0.07, theta=-0.055)],
+                   refractory=0.002, i_bg=0.0, n_inputs=50, rates=rng.uniform(5, 60, 50),
+                   pre=pre, post=post, weight=rng.uniform(0, 3e-10, S), scale=np.ones(S),
+                   delay=np.maximum(1, rng.integers(0, 9, S)), label=(pre < 0).astype(int), record_inputs=True)
+    spikes = run_both(d.desc, 4, 32, 1, [(400, False), (300, False)])
+    assert spikes > 100
+
+
+def test_noalloc_matches_run_steps_two_plastic_scale_classes():
+    """Plastic synapses in two weight-scale classes (input and recurrent
+    excitatory synapses scaled differently)."""
+    base = descs.random_voltage_net(n=300, n_in=200, plastic=True, stdp=STDP, seed=9)
+    a = base.arrays
+    scale = np.where(a["pre"] < 0, 1.0, 0.5).astype(np.float32)
+    pl = np.ctypeslib.as_array(base.desc.plastic, (base.desc.n_synapses,)).copy()
+    groups = [dict(count=240, tau_m=0.02, R=1e8, v0=0.0, vreset=0.0, theta=0.02, v_init_lo=0.0, v_init_hi=0.018),
+              dict(count=60, tau_m=0.01, R=1e8, v0=0.0, vreset=0.002, theta=0.018)]
+    rates = np.ctypeslib.as_array(base.desc.input_rates, (200,)).copy()
+    d = descs.Desc(kind=N.SPK_SYN_VOLTAGE, groups=groups, refractory=0.002, n_inputs=200, rates=rates,
+                   pre=a["pre"], post=a["post"], weight=a["weight"] / scale, scale=scale, delay=a["delay"],
+                   plastic=pl, stdp=STDP, seed=base.desc.seed, record_inputs=True)
+    cn_scales = run_both(d.desc, 4, 32, 3, [(300, True), (200, True)])
+    assert cn_scales > 200
+
+
+def test_noalloc_spike_store_overflow_sets_status():
+    """A spike store too small for the run: the device status in run_state
+    becomes SPK_ERR_OVERFLOW and stays there for the next call, while the
+    network state goes on exactly as the reference entry point's."""
+    d = descs.random_voltage_net(n=300, n_in=200, plastic=False, seed=11)
+    ref = Net.from_desc(d.desc, schedule(4, 32, 3, 0))
+    cn = CallerNet(d.desc, 4, 32, 3, ref, spike_capacity=50)
+    for i, n_steps in enumerate((300, 200)):
+        ref.run_steps(n_steps, False)
+        assert ref.synchronize() == 0
+        cn.step(n_steps, False)
+        torch.cuda.synchronize()
+        rs = cn.t["run_state"].cpu().numpy()
+        assert int(rs[12]) == N.SPK_ERR_OVERFLOW, f"call {i + 1}: status {int(rs[12])}"
+        assert int(rs[8:10].view(np.uint64)[0]) == 50
+        assert int(rs[10:12].view(np.uint64)[0]) == ref.events()
+        assert_close(cn.t["V"].cpu().numpy(), ref.state(N.SPK_FIELD_V, 300), f"call {i + 1} V")
+    ref.close()
