@@ -419,6 +419,20 @@ def main():
                    "sample": f"{args.cpu_sample_steps} timesteps ({args.cpu_sample_steps * DT:.2f} s simulated) "
                              f"from reset, {cel:.1f} s of CPU"}
 
+    # the reference's own CUDA kernels on the same network and GPU model, once
+    # (tests/golden/make_ref_gpu_stats.py): a second reference line for context
+    ref_gpu = None
+    ref_case = {"vogels_abbott": "va", "brunel": "brunel_cfg2"}.get(args.workload)
+    if ref_case and args.rule == "weight_dependent" and args.norm == "off" and args.scale == 1.0:
+        try:
+            with open(os.path.join(ROOT, "tests", "golden", "ref_gpu_stats.json")) as f:
+                rg = json.load(f)[ref_case]
+            ref_gpu = {"value": rg["events_per_s"], "unit": "events/s", "wall_s": rg["wall_s"],
+                       "sim_s": rg["seconds"], "source": "tests/golden/ref_gpu_stats.json (the reference's CUDA "
+                       "backend built for sm_103a, run once on a GB300 host without a spike monitor)"}
+        except Exception:
+            ref_gpu = None
+
     if rank == 0:
         line = {
             "metric": "synaptic_events_per_s", "value": value, "unit": "events/s", "n_gpus": world,
@@ -439,7 +453,7 @@ def main():
                                     "pass, weight normalisation)" if normalised else "spk::step_kernel"),
                          "launches": launches,
                          "alg_bytes_per_launch": per_launch_bytes, "ms_per_launch": 1000 * per_launch_s},
-            "e2e": e2e, "cpu_baseline": cpu, "clocks": clk.summary(),
+            "e2e": e2e, "cpu_baseline": cpu, "reference_gpu": ref_gpu, "clocks": clk.summary(),
             "gpu_launches": launches + args.steps,
         }
         print(json.dumps(line), flush=True)

@@ -474,7 +474,10 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
 constexpr int BULK_PROP_WARPS = SPK_BULK_PROP_WARPS;
 constexpr int BULK_RPW = BULK_PROP_WARPS + 1;  // rowptr words per key: the tiles' starts and the last end
 constexpr int BULK_LIST_CHUNK = 1024;          // list keys staged at a time (a multiple of BULK_STAGE_KEYS)
-constexpr int BULK_WIN_CAP = 1024;             // ring-window words per warp at most
+#ifndef SPK_BULK_WIN_CAP
+#define SPK_BULK_WIN_CAP 1024
+#endif
+constexpr int BULK_WIN_CAP = SPK_BULK_WIN_CAP;  // ring-window words per warp at most
 static_assert(BULK_LIST_CHUNK % BULK_STAGE_KEYS == 0, "rounds never straddle a list chunk");
 static_assert(BULK_STAGE_KEYS % 32 == 0, "a round is whole lanes' worth of keys");
 
