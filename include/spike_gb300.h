@@ -21,9 +21,14 @@
  *  - spk_last_error() returns a per-thread message for the last failure.
  *
  * Timestep grouping: the reference advances G = min delay steps per launch
- * (Spike/Models/SpikingModel.cpp:98).  This library implements G = 1, which is
- * the value for every network whose minimum delay is one step; networks whose
- * minimum delay is larger are rejected with SPK_ERR_UNSUPPORTED.
+ * (Spike/Models/SpikingModel.cpp:98).  A network whose minimum delay is G > 1
+ * steps takes the reference's grouped times (group time start + s*G*dt,
+ * substep time that + g*dt) and runs whole groups only: spk_net_run rounds
+ * the step count down to whole groups as SpikingModel::run does, the
+ * step-count entry points refuse other counts with SPK_ERR_INVALID.  Grouped
+ * timesteps change the plasticity rules' arithmetic, which this library does
+ * not restate: a network with a rule and G > 1 is rejected with
+ * SPK_ERR_UNSUPPORTED.
  */
 #ifndef SPIKE_GB300_H
 #define SPIKE_GB300_H
@@ -35,7 +40,7 @@
 extern "C" {
 #endif
 
-#define SPK_ABI_VERSION 3
+#define SPK_ABI_VERSION 4
 
 /* ---- status codes ------------------------------------------------------ */
 #define SPK_OK 0
@@ -213,11 +218,13 @@ int spk_net_select_stimulus(spk_net* net, int32_t stimulus);
  * makes it truly asynchronous).  Input state is not reset. */
 int spk_net_write_rates(spk_net* net, int32_t stimulus, const float* rates, int64_t n);
 /* SpikingModel::run(seconds, plasticity_on) (Spike/Models/SpikingModel.cpp:214-236):
- * ceilf(seconds/dt) steps, t_s = start + s*dt in float, then time = start + seconds.
+ * ceilf(seconds/dt) steps rounded down to whole groups of G, t_s = start +
+ * (s - s%G)*dt + (s%G)*dt in float, then time = start + seconds.
  * Asynchronous: returns after enqueueing; device errors surface at the next
  * synchronizing call. */
 int spk_net_run(spk_net* net, float seconds, int32_t plasticity_on);
-/* As spk_net_run for an explicit step count (time advances by n_steps*dt). */
+/* As spk_net_run for an explicit step count (time advances by n_steps*dt);
+ * n_steps must be whole groups of the timestep grouping. */
 int spk_net_run_steps(spk_net* net, int64_t n_steps, int32_t plasticity_on);
 /* Start a run of n_steps steps (time advances by n_steps*dt, as in
  * spk_net_run_steps) without launching it; spk_batch_step_block then advances
@@ -227,6 +234,9 @@ int spk_net_begin_run(spk_net* net, int64_t n_steps, int32_t plasticity_on);
  * (SPK_ERR_TIMEOUT / SPK_ERR_OVERFLOW) or SPK_OK. */
 int spk_net_synchronize(spk_net* net);
 int spk_net_current_time(const spk_net* net, float* seconds);
+/* SpikingModel::timestep_grouping (Spike/Models/SpikingModel.cpp:98): the
+ * network's minimum delay in steps (1 without synapses). */
+int spk_net_timestep_grouping(const spk_net* net, int32_t* G);
 /* Spikes recorded since the last clear (SpikingActivityMonitor store,
  * Spike/ActivityMonitor/SpikingActivityMonitor.cpp:79-120).  Ordered by
  * step, then by presynaptic key (the canonical order).  times are the float
@@ -533,7 +543,8 @@ int spk_net_generate_estimate(const spk_gen_desc* desc, const spk_schedule* sche
  *    creation order, as (presynaptic key, float bits of the weight), needed
  *    only with plasticity;
  *  - state: V, last_spike [N]; syn_trace [N*L] (conductance/current);
- *    ring [T][max_delay+3][tile_posts*L]; input_next [Nin]; rates [Nin];
+ *    ring [T][max_delay+2G+1][tile_posts*L] (G = timestep_grouping, at
+ *    least 1); input_next [Nin]; rates [Nin];
  *    post_trace [N] and pre_trace [n_keys] with plasticity;
  *  - spikes [2*spike_capacity] uint32 pairs (key, float time bits), in
  *    step order; spike_capacity 0 records nothing;
@@ -597,6 +608,10 @@ typedef struct spk_device_net {
   uint32_t* spikes;
   int64_t spike_capacity;
   void* run_state;
+  /* timestep grouping G (Spike/Models/SpikingModel.cpp:98: the minimum delay
+   * in steps); 0 or 1 = none.  G > 1 needs has_stdp = 0 and n_steps a
+   * multiple of G (the reference's run() advances whole groups). */
+  int32_t timestep_grouping;
 } spk_device_net;
 
 /* Advance the network n_steps timesteps from start_time (seconds) on `stream`

@@ -37,6 +37,7 @@ def oracle_lib() -> C.CDLL:
             "oracle_read_weights": [vp, C.POINTER(C.c_float), C.c_int64],
             "oracle_synaptic_events": [vp, C.POINTER(C.c_uint64)],
             "oracle_ring_depth": [vp, C.POINTER(C.c_int32)],
+            "oracle_timestep_grouping": [vp, C.POINTER(C.c_int32)],
             "oracle_sorted_synapses": [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                        C.c_int64],
         }
@@ -140,6 +141,11 @@ class OracleNet:
         b = C.c_int32()
         _ok(oracle_lib().oracle_ring_depth(self.h, C.byref(b)), "oracle_ring_depth")
         return b.value
+
+    def timestep_grouping(self) -> int:
+        g = C.c_int32()
+        _ok(oracle_lib().oracle_timestep_grouping(self.h, C.byref(g)), "oracle_timestep_grouping")
+        return g.value
 
     def sorted_synapses(self):
         S = self.n_synapses

@@ -14,11 +14,18 @@
 # archives, then the device-link object and the CUDA runtime.
 #
 # Usage: oracle/build_ref_gpu.sh REFERENCE_ROOT [ARCH]   (ARCH default sm_103a)
+#
+# REF_STRICT_FP=1 compiles every float expression as written: no fused
+# multiply-add on the device (-fmad=false) or the host (-ffp-contract=off),
+# the convention of the oracle and of this library.  The outputs then go to
+# oracle/_ref/gpu_strict/ instead.
 set -euo pipefail
 REF="${1:?usage: build_ref_gpu.sh REFERENCE_ROOT [ARCH]}"
 ARCH="${2:-sm_103a}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref/gpu"
+STRICT="${REF_STRICT_FP:-0}"
+[ "$STRICT" = 1 ] && OUT="$HERE/_ref/gpu_strict"
 if [ ! -d "$REF/Spike/Backend/CUDA" ]; then
   echo "build_ref_gpu: no reference CUDA backend under $REF" >&2
   exit 1
@@ -30,6 +37,10 @@ mkdir -p "$OUT/obj"
 DEF='-DSPIKE_DEFAULT_BACKEND="CUDA"'
 CXXFLAGS=(-std=c++11 -O2 -w -fPIC -I"$REF" -I"$CUDA_HOME/include" -DNDEBUG "$DEF")
 NVFLAGS=(-std=c++11 -O2 -w -gencode "arch=compute_${ARCH#sm_},code=$ARCH" -I"$REF" -Xcompiler -fPIC "$DEF")
+if [ "$STRICT" = 1 ]; then
+  CXXFLAGS+=(-ffp-contract=off)
+  NVFLAGS+=(-fmad=false -Xcompiler -ffp-contract=off)
+fi
 
 front=(); dummy=(); cuda=()
 while IFS= read -r f; do front+=("$f"); done < <(

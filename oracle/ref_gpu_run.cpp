@@ -8,8 +8,9 @@
 // cuRAND XORWOW, so it is not bit-reproducible) and times the reference's
 // kernels on the same GPU.
 //
-// Usage: ref_gpu_run <case> <seconds> <monitor 0|1> <out_dir>
-//   case     va | brunel_cfg2 | brunel_cfg2_plastic (ref_cases.inc)
+// Usage: ref_gpu_run <case> <seconds[,seconds...]> <monitor 0|1> <out_dir>
+//   seconds  one run() per comma-separated value, in turn
+//   case     va | va_g2 | va_g3 | brunel_cfg2 | brunel_cfg2_plastic (ref_cases.inc)
 //   monitor  1: record neuron and input spikes (SpikingActivityMonitor) and
 //            write them, with the final weights of the plastic synapse group,
 //            to out_dir; 0: no monitor
@@ -38,7 +39,15 @@ int main(int argc, char** argv) {
     return 2;
   }
   const std::string name = argv[1], dir = argv[4];
-  const float seconds = (float)atof(argv[2]);
+  std::vector<float> runs;
+  for (const char* p = argv[2]; *p;) {
+    char* end = nullptr;
+    runs.push_back(strtof(p, &end));
+    if (end == p) return 2;
+    p = (*end == ',') ? end + 1 : end;
+  }
+  float seconds = 0.0f;
+  for (float s : runs) seconds += s;
   const bool monitor = atoi(argv[3]) != 0;
   RefCase r = build_case(name);
   if (!r.m) return 2;
@@ -68,10 +77,13 @@ int main(int argc, char** argv) {
   r.m->finalise_model();
   cudaDeviceSynchronize();
   const auto t0 = std::chrono::steady_clock::now();
-  r.m->run(seconds);
+  for (float s : runs) r.m->run(s);
   cudaDeviceSynchronize();
   const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  const long long steps = (long long)std::ceil(seconds / r.m->timestep);
+  // SpikingModel::run: ceil(seconds/dt) timesteps, whole groups of timestep_grouping
+  long long steps = 0;
+  for (float s : runs)
+    steps += (long long)std::ceil(s / r.m->timestep) / r.m->timestep_grouping * r.m->timestep_grouping;
   long long spikes_n = -1, spikes_i = -1, events = -1;
   if (monitor) {
     mon_n->save_spikes_as_binary(dir, name + "_neurons_");
@@ -88,10 +100,10 @@ int main(int argc, char** argv) {
     // the plastic case's E->E synapses are its fourth synapse group (ref_cases.inc)
     if (r.rule) r.syn->save_weights_as_binary(dir, name + "_final_", 3);
   }
-  printf("{\"case\": \"%s\", \"synapses\": %lld, \"neurons\": %d, \"inputs\": %d, \"seconds\": %g, \"timesteps\": %lld, "
+  printf("{\"case\": \"%s\", \"synapses\": %lld, \"neurons\": %d, \"inputs\": %d, \"grouping\": %d, \"seconds\": %g, \"timesteps\": %lld, "
          "\"monitor\": %d, \"wall_s\": %.6f, \"neuron_spikes\": %lld, \"input_spikes\": %lld, \"events\": %lld, "
          "\"cuda_status\": \"%s\"}\n",
-         name.c_str(), S, N, Nin, (double)seconds, steps, monitor ? 1 : 0, wall, spikes_n, spikes_i, events,
+         name.c_str(), S, N, Nin, r.m->timestep_grouping, (double)seconds, steps, monitor ? 1 : 0, wall, spikes_n, spikes_i, events,
          cudaGetErrorString(cudaGetLastError()));
   return 0;
 }

@@ -49,6 +49,7 @@ struct Net {
   R dt = 0;
   int kind = 0;
   int N = 0, Nin = 0, L = 1, B = 0, Dmax = 0;
+  int G = 1;  // timestep grouping: the minimum delay (Spike/Models/SpikingModel.cpp:98)
   std::vector<R> k, kR, v0, vreset, theta;  // per neuron, as the reference backend
   std::vector<float> vinit_lo, vinit_hi;    // per neuron (extension)
   R t_ref = 0, i_bg = 0;
@@ -209,7 +210,10 @@ int Net<R>::init(const spk_net_desc* d) {
     if (dl > Dmax) Dmax = dl;
     if (dl < Dmin) Dmin = dl;
   }
-  if (S > 0 && Dmin != 1) return SPK_ERR_UNSUPPORTED;  // timestep grouping G = 1 only
+  // timestep_grouping = the minimum delay (Spike/Models/SpikingModel.cpp:98);
+  // 1 without synapses.  The plasticity rules are restated for G = 1 only.
+  G = S > 0 ? Dmin : 1;
+  if (G > 1 && d->has_stdp) return SPK_ERR_UNSUPPORTED;
   for (int kk = 0; kk < K; ++kk) cnt[kk + 1] += cnt[kk];
   eff_start.assign(cnt.begin(), cnt.end() - 1);
   eff_count.assign(K, 0);
@@ -235,10 +239,13 @@ int Net<R>::init(const spk_net_desc* d) {
     revsort[s] = pos;
     if (d->plastic && d->plastic[s]) splastic[pos] = 1;
   }
-  // Ring depth D_max + 2G + 1 (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:48);
-  // a network without synapses keeps a ring of delay-1 depth.
+  // Ring depth D_max + 2G + 1 (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:48).
+  // Deliveries land at most D_max slots ahead, but a run of a grouped network
+  // that is not whole groups skips timestep indices (the next run starts at
+  // start + seconds), and a skipped slot's contents are read B steps later.
+  // A network without synapses keeps a ring of delay-1 depth.
   if (S == 0) Dmax = 1;
-  B = Dmax + 2 * 1 + 1;
+  B = Dmax + 2 * G + 1;
 
   has_stdp = d->has_stdp != 0;
   stdp = d->stdp;
@@ -454,14 +461,13 @@ void Net<R>::set_threads(int t) {
 
 // lif_update_membrane_potentials with the injection kernels inlined
 // (Spike/Backend/CUDA/Neurons/LIFSpikingNeurons.cu:105-193,
-// Spike/Backend/CUDA/InlineDeviceFunctions.hpp:22-111), G = 1 so g = 0.
+// Spike/Backend/CUDA/InlineDeviceFunctions.hpp:22-111) for one substep:
+// tg = current_time + g*timestep, T = its timestep index (with g added).
 template <typename R>
-void Net<R>::lif_range(int a, int b, R t, int T) {
-  const int g = 0;
-  const R tg = t + (R)g * dt;
+void Net<R>::lif_range(int a, int b, R tg, int T) {
   const R half_dt = (R)0.5f * dt;
   const size_t row = (size_t)N * L;
-  const size_t bufferloc = (size_t)((T + g) % B) * row;
+  const size_t bufferloc = (size_t)(T % B) * row;
   for (int idx = a; idx < b; ++idx) {
     R Vi = V[idx];
     R input = 0;
@@ -511,12 +517,11 @@ void Net<R>::lif_range(int a, int b, R t, int T) {
 }
 
 // poisson_update_membrane_potentials_kernel
-// (Spike/Backend/CUDA/Neurons/PoissonInputSpikingNeurons.cu:96-129), G = 1,
+// (Spike/Backend/CUDA/Neurons/PoissonInputSpikingNeurons.cu:96-129) for one
+// substep (tg, T as in lif_range),
 // with the uniform drawn from Philox(seed, input, step).
 template <typename R>
-void Net<R>::poisson_range(int a, int b, R t, int T) {
-  const int g = 0;
-  const R tg = t + (R)g * dt;
+void Net<R>::poisson_range(int a, int b, R tg, int T) {
   const float* rt = rates.data() + (size_t)Nin * stim;
   for (int idx = a; idx < b; ++idx) {
     if ((in_next[idx] <= tg) || !in_active[idx]) {
@@ -541,7 +546,7 @@ void Net<R>::poisson_range(int a, int b, R t, int T) {
 // so the (post_g > pre_g) / (pre_g > post_g) corrections never apply.
 template <typename R>
 void Net<R>::stdp_range(int64_t a, int64_t b, R t) {
-  const int G = 1;
+  // G = 1 here: init refuses a rule with a larger grouping
   for (int64_t indx = a; indx < b; ++indx) {
     const int64_t idx = plastic_idx[indx];
     R pre_tr = stdp_pre[indx];
@@ -713,12 +718,20 @@ void Net<R>::propagate_thread(int th, int T) {
 template <typename R>
 void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
   auto step_time = [&](int64_t s, R& t, int& T) {
+    // Timestep s is substep g = s % G of group s / G.  The group's
     // current_time_in_seconds = starttime + s*timestep_grouping*timestep
-    // (Spike/Models/SpikingModel.cpp:226) and timestep_index =
-    // (int)roundf(t/dt) (Spike/Backend/CUDA/Neurons/LIFSpikingNeurons.cu:84).
-    float tf = start + (float)(s * 1) * dt_f;
-    T = round_to_int(tf / dt_f);
-    t = (sizeof(R) == 4) ? (R)tf : (R)start + (R)(s * 1) * dt;
+    // (Spike/Models/SpikingModel.cpp:226), the substep's timestep index
+    // (int)roundf(t/dt) + g (Spike/Backend/CUDA/Neurons/LIFSpikingNeurons.cu:84,115)
+    // and its time t + g*timestep (:172,177; the spike monitor's time,
+    // Spike/Backend/CUDA/ActivityMonitor/SpikingActivityMonitor.cu:93).  With
+    // G = 1 that is start + s*dt.  Advancing a group substep by substep, each
+    // substep's spikes delivered at its end, is the reference's group: a
+    // delay of at least G steps lands every delivery past the group, so no
+    // substep reads what another substep of its group delivers.
+    const int64_t grp = s / G, g = s - grp * G;
+    const float tf = start + (float)(grp * G) * dt_f;
+    T = round_to_int(tf / dt_f) + (int)g;
+    t = (sizeof(R) == 4) ? (R)(tf + (float)g * dt_f) : ((R)start + (R)(grp * G) * dt) + (R)g * dt;
   };
   auto finish_step = [&](R t, int T) {
     active.clear();
@@ -896,10 +909,11 @@ int oracle_select_stimulus(oracle_net* n, int stimulus) {
 int oracle_run(oracle_net* n, float seconds, int plasticity_on) {
   if (!n || !(seconds >= 0.0f)) return SPK_ERR_INVALID;
   return dispatch(n, [&](auto& net) {
-    // number_of_timesteps = ceil(seconds / timestep); G = 1
+    // number_of_timesteps = ceil(seconds / timestep), number_of_steps =
+    // number_of_timesteps / timestep_grouping in integers: whole groups
     // (Spike/Models/SpikingModel.cpp:221-222).
     const float q = seconds / net.dt_f;
-    const int64_t steps = (int64_t)std::ceil(q);
+    const int64_t steps = ((int64_t)std::ceil(q) / net.G) * net.G;
     const float start = net.current_time;
     net.run_steps(steps, start, plasticity_on != 0);
     net.current_time = start + seconds;
@@ -910,6 +924,7 @@ int oracle_run(oracle_net* n, float seconds, int plasticity_on) {
 int oracle_run_steps(oracle_net* n, int64_t n_steps, int plasticity_on) {
   if (!n || n_steps < 0) return SPK_ERR_INVALID;
   return dispatch(n, [&](auto& net) {
+    if (n_steps % net.G != 0) return SPK_ERR_INVALID;  // whole groups only
     const float start = net.current_time;
     net.run_steps(n_steps, start, plasticity_on != 0);
     net.current_time = start + (float)n_steps * net.dt_f;
@@ -1020,6 +1035,14 @@ int oracle_ring_depth(const oracle_net* n, int32_t* depth) {
   if (!n || !depth) return SPK_ERR_INVALID;
   return dispatch(n, [&](auto& net) {
     *depth = net.B;
+    return SPK_OK;
+  });
+}
+
+int oracle_timestep_grouping(const oracle_net* n, int32_t* G) {
+  if (!n || !G) return SPK_ERR_INVALID;
+  return dispatch(n, [&](auto& net) {
+    *G = net.G;
     return SPK_OK;
   });
 }

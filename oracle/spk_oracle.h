@@ -51,6 +51,8 @@ int oracle_read_weights(const oracle_net* net, float* weights, int64_t n);
 int oracle_synaptic_events(const oracle_net* net, uint64_t* events);
 /* Ring depth B = D_max + 2G + 1 (SpikingSynapses.cu:48) of the network. */
 int oracle_ring_depth(const oracle_net* net, int32_t* depth);
+/* Timestep grouping G = the minimum delay (SpikingModel.cpp:98); 1 without synapses. */
+int oracle_timestep_grouping(const oracle_net* net, int32_t* G);
 /* Sorted-order connectivity as the reference backend sees it after
  * prepare_backend_early (for fixture checks): pre/post/delay in sorted order. */
 int oracle_sorted_synapses(const oracle_net* net, int32_t* pre, int32_t* post, int32_t* delay,

@@ -12,7 +12,7 @@ import os
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libspike_gb300.so")
 
-SPK_ABI_VERSION = 3
+SPK_ABI_VERSION = 4
 SPK_OK = 0
 SPK_ERR_INVALID = -1
 SPK_ERR_CUDA = -2
@@ -167,6 +167,7 @@ class DeviceNet(C.Structure):
         ("V", C.c_void_p), ("last_spike", C.c_void_p), ("syn_trace", C.c_void_p), ("ring", C.c_void_p),
         ("input_next", C.c_void_p), ("rates", C.c_void_p), ("post_trace", C.c_void_p),
         ("pre_trace", C.c_void_p), ("spikes", C.c_void_p), ("spike_capacity", i64), ("run_state", C.c_void_p),
+        ("timestep_grouping", i32),
     ]
 
 
@@ -189,6 +190,7 @@ _SIGS = {
     "spk_net_run_steps": (i32, [_VP, i64, i32]),
     "spk_net_synchronize": (i32, [_VP]),
     "spk_net_current_time": (i32, [_VP, P(f32)]),
+    "spk_net_timestep_grouping": (i32, [_VP, P(i32)]),
     "spk_net_spike_count": (i32, [_VP, i32, P(i64)]),
     "spk_net_read_spikes": (i32, [_VP, i32, P(i32), P(f32), i64, P(i64)]),
     "spk_net_clear_spikes": (i32, [_VP]),

@@ -775,13 +775,16 @@ void SpikingModel::finalise_model() {
   spk_net_desc d;
   int rc = build_desc(&d);
   if (rc) fail(rc, "model cannot be flattened into a network descriptor");
-  timestep_grouping = 1;
   const spk_schedule* sp = (schedule.warps_per_cta || schedule.tile_posts || schedule.ctas ||
                             schedule.steps_per_launch)
                                ? &schedule
                                : nullptr;
   rc = spk_net_create(&d, sp, &net_);
   if (rc) fail(rc, spk_last_error());
+  // timestep_grouping = the minimum delay (Spike/Models/SpikingModel.cpp:98)
+  int32_t G = 1;
+  spk_net_timestep_grouping(net_, &G);
+  timestep_grouping = G;
   model_complete = true;
 }
 

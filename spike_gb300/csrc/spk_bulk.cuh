@@ -80,12 +80,8 @@ __device__ __forceinline__ BulkStep bulk_step(const NetDev& d, const RunCtl& c, 
   const int sr = c.step + s;
   b.live = sr < c.steps_total;
   const float dt = d.dt;
-  // current_time_in_seconds = starttime + s*timestep_grouping*timestep
-  // (Spike/Models/SpikingModel.cpp:226), timestep_index = roundf(t/dt).
-  b.t = c.start_time + (float)(sr * 1) * dt;
-  b.T = (int)roundf(b.t / dt);
+  group_time(c.start_time, sr, d.G, dt, b.t, b.T, b.tg);
   b.slot = b.T % d.B;
-  b.tg = b.t + 0.0f * dt;
   // the event-driven (weight-dependent) rule's passes, or the per-synapse-trace rules' pass
   b.stdp_run = d.has_stdp && c.plastic && d.stdp_rule == SPK_STDP_WEIGHT_DEPENDENT;
   b.dense_run = d.has_stdp && c.plastic && d.stdp_rule != SPK_STDP_WEIGHT_DEPENDENT;
@@ -397,7 +393,7 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
       d.step_list[pos++] = key | (fa << 31) | (fp << 30);
       if (fa && rec) {
         if (sp < (unsigned long long)d.spike_cap)
-          d.spikes[sp] = make_uint2(key, __float_as_uint(st.t));
+          d.spikes[sp] = make_uint2(key, __float_as_uint(st.tg));
         else
           atomicCAS(&d.ctl->status, 0, SPK_ERR_OVERFLOW);
         ++sp;
@@ -681,7 +677,7 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
       // A window pays when the step's entries (estimated from the first
       // round) would touch more sectors one by one than the window holds;
       // its reads overlap the first round's entry staging.
-      const int ws_max = min(min(B - 3, 32), win_words / slot_words);
+      const int ws_max = min(min(B - 2 * d.G - 1, 32), win_words / slot_words);  // D_max slots at most
       const long long est = (long long)total_e * ((n_list + BULK_STAGE_KEYS - 1) / BULK_STAGE_KEYS);
       ws = (ws_max > 0 && est * 8 > (long long)ws_max * slot_words) ? ws_max : 0;
       for (int k = 0; k < ws; ++k) {

@@ -1,6 +1,7 @@
 // spk_internal.h - host/device shared definitions of the step engine.
 #pragma once
 
+#include <math.h>
 #include <stdint.h>
 #include <vector_types.h>
 
@@ -25,6 +26,21 @@ constexpr int APPLY_TAGS = 256;    // cell-hash slots of the ordered apply
 // holds its weight (post-major, so a spiking post's afferents are contiguous).
 SPK_HD uint32_t pack_entry(uint32_t post_local, uint32_t delay, uint32_t label, uint32_t cls) {
   return post_local | (delay << 16) | (label << 24) | (cls << 28);
+}
+
+// The times of timestep r of a run started at `start` seconds, with timestep
+// grouping G: the group's current_time_in_seconds = starttime +
+// s*timestep_grouping*timestep for group s = r / G
+// (Spike/Models/SpikingModel.cpp:226), the timestep index roundf(t/dt) + g of
+// substep g = r % G (Spike/Backend/CUDA/Neurons/LIFSpikingNeurons.cu:115,
+// Spike/Backend/CUDA/Synapses/ConductanceSpikingSynapses.cu:113) and the
+// substep's time t + g*timestep (LIFSpikingNeurons.cu:172,177; the spike
+// monitor's time, Spike/Backend/CUDA/ActivityMonitor/SpikingActivityMonitor.cu:93).
+SPK_HD void group_time(float start, int r, int G, float dt, float& t, int& T, float& tg) {
+  const int s = r / G, g = r - s * G;
+  t = start + (float)(s * G) * dt;
+  T = (int)roundf(t / dt) + g;
+  tg = t + (float)g * dt;
 }
 
 struct GroupConst {
@@ -55,6 +71,9 @@ struct NetDev {
   int N, Nin, KL, n_keys, n_words, L, B, kind;
   int n_tiles, TS, ITS, W, nctas, n_groups;
   float dt, half_dt, t_ref, i_bg;
+  // Timestep grouping G: the minimum delay in steps (Spike/Models/SpikingModel.cpp:98).
+  // Timestep r of a run is substep r % G of group r / G.
+  int G;
   GroupConst groups[MAX_GROUPS];
   float decay[MAX_LABELS + 1], vhat[MAX_LABELS + 1];
   float scale_tab[MAX_CLASSES];

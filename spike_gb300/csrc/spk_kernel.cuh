@@ -266,10 +266,9 @@ __global__ void __launch_bounds__(512, 1)
 
   for (int s = 0; s < steps_here && ok_run; ++s) {
     const int sr = ctl0.step + s;
-    // current_time_in_seconds = starttime + s*timestep_grouping*timestep
-    // (Spike/Models/SpikingModel.cpp:226), timestep_index = roundf(t/dt).
-    const float t = ctl0.start_time + (float)(sr * 1) * dt;
-    const int T = (int)roundf(t / dt);
+    float t, tg;
+    int T;
+    group_time(ctl0.start_time, sr, d.G, dt, t, T, tg);
     const long long gs = ctl0.gstep + s;
     const int par = (int)(gs & 1);
     const unsigned stamp = (unsigned)(gs + 1);
@@ -278,7 +277,6 @@ __global__ void __launch_bounds__(512, 1)
     uint32_t* bitsP = d.bitsP + (size_t)par * n_words;
     float* pub = d.pre_pub + (size_t)par * n_keys;
     const int slot = T % B;
-    const float tg = t + 0.0f * dt;  // t + g*timestep with g = 0
     const float half_dt = 0.5f * dt;
 
     // ---- phase A: LIF neurons of the tile ------------------------------------
@@ -502,7 +500,7 @@ __global__ void __launch_bounds__(512, 1)
               if (rec) {
                 const unsigned long long sp = spike_count + (unsigned long long)__popc(m & lanemask_lt());
                 if (sp < (unsigned long long)d.spike_cap)
-                  d.spikes[sp] = make_uint2(key, __float_as_uint(t));
+                  d.spikes[sp] = make_uint2(key, __float_as_uint(tg));
                 else
                   atomicCAS(&d.ctl->status, 0, SPK_ERR_OVERFLOW);
               }

@@ -194,6 +194,7 @@ using namespace spk;
 struct spk_net {
   // model
   int N = 0, Nin = 0, L = 1, B = 0, kind = 0, n_stim = 0, stim = 0;
+  int G = 1;  // timestep grouping: runs advance whole groups of G timesteps
   int64_t S = 0;
   float dt = 0.f;
   bool has_stdp = false, record_inputs = false;
@@ -486,11 +487,24 @@ struct ModelSpec {
   uint64_t seed = 0;
   int64_t spike_capacity = 0;
   int record_inputs = 0;
+  int G = 1;  // timestep grouping: the minimum delay in steps (Spike/Models/SpikingModel.cpp:98)
 };
 
 // The time constants the step divides by (k = dt / tau_m, the label decays,
 // the STDP trace decays) must be positive and the refractory period finite and
 // non-negative: zero or negative values would give the run inf/NaN constants.
+// Grouped timesteps change the plasticity rules' arithmetic (one update per
+// group, with traces decayed over G steps:
+// Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:125-145),
+// which this engine does not restate: a network with a rule needs G = 1.
+static int check_grouping(const ModelSpec& m) {
+  if (m.G > 1 && m.has_stdp) {
+    set_error("minimum delay %d steps (timestep grouping %d) with a plasticity rule is not supported", m.G, m.G);
+    return SPK_ERR_UNSUPPORTED;
+  }
+  return SPK_OK;
+}
+
 static int check_time_constants(float dt, const spk_neuron_group* groups, int n_groups, int kind, int L,
                                 const float* label_tau, float refractory, bool has_stdp, const spk_stdp_params& sp) {
   for (int g = 0; g < n_groups; ++g)
@@ -582,6 +596,7 @@ static int new_net(const ModelSpec& m, int B, int64_t S, const spk_schedule* sch
   n->Nin = m.Nin;
   n->L = m.L;
   n->B = B;
+  n->G = m.G;
   n->kind = m.kind;
   n->S = S;
   n->dt = m.dt;
@@ -739,6 +754,7 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   h.n_groups = m.n_groups;
   h.dt = m.dt;
   h.half_dt = 0.5f * m.dt;
+  h.G = n->G;
   h.t_ref = m.t_ref;
   h.i_bg = m.i_bg;
   for (int g = 0; g < m.n_groups; ++g) {
@@ -962,16 +978,23 @@ static int create_impl(const spk_net_desc* d, const spk_schedule* sched, spk_net
     Dmax = std::max(Dmax, dl);
     Dmin = std::min(Dmin, dl);
   }
-  if (S > 0 && Dmin != 1) {
-    set_error("minimum delay %d steps: timestep grouping > 1 is not supported", Dmin);
-    return SPK_ERR_UNSUPPORTED;
-  }
+  // timestep_grouping = the minimum delay (Spike/Models/SpikingModel.cpp:98).
+  // A network without synapses keeps G = 1: the reference's default minimum
+  // (10^6 steps, Spike/Synapses/SpikingSynapses.hpp:40) would run no step.
+  m.G = S > 0 ? Dmin : 1;
+  rc = check_grouping(m);
+  if (rc) return rc;
   if (Dmax > MAX_DELAY) {
     set_error("delay %d steps exceeds the supported maximum %d", Dmax, MAX_DELAY);
     return SPK_ERR_UNSUPPORTED;
   }
   if (S == 0) Dmax = 1;
-  const int B = Dmax + 2 * 1 + 1;  // SpikingSynapses.cu:48 with G = 1
+  // Ring depth D_max + 2G + 1 (SpikingSynapses.cu:48).  The engine delivers
+  // at most D_max slots ahead, but a run of a grouped network that is not
+  // whole groups skips timestep indices (the next run starts at start +
+  // seconds), and what was delivered to a skipped slot is read B steps later:
+  // the depth decides when.
+  const int B = Dmax + 2 * m.G + 1;
   const int stdp = m.has_stdp;
 
   spk_net* n = nullptr;
@@ -1207,9 +1230,11 @@ static int generate_impl(const spk_gen_desc* d, const spk_schedule* sched, spk_n
     proj.push_back(g);
   }
   std::stable_sort(proj.begin(), proj.end(), [](const GenProj& a, const GenProj& b) { return a.post_lo < b.post_lo; });
-  if (dlo_min != (1 << 30) && dlo_min != 1) {
-    set_error("minimum delay %d steps: timestep grouping > 1 is not supported", dlo_min);
-    return SPK_ERR_UNSUPPORTED;
+  if (dlo_min != (1 << 30) && dlo_min > 1) {
+    // every drawn delay is at least dlo_min, so G > 1 whatever is drawn
+    m.G = dlo_min;
+    rc = check_grouping(m);
+    if (rc) return rc;
   }
 
   DeviceInfo di;
@@ -1221,7 +1246,7 @@ static int generate_impl(const spk_gen_desc* d, const spk_schedule* sched, spk_n
   int dmax_bound = 1;
   for (const auto& g : proj) dmax_bound = std::max(dmax_bound, g.d_lo + g.d_n - 1);
   spk_net* probe = nullptr;
-  rc = new_net(m, dmax_bound + 3, 0, sched, &probe);
+  rc = new_net(m, dmax_bound + 2 * m.G + 1, 0, sched, &probe);
   if (rc) return rc;
   const Plan plan0 = probe->plan;
   delete probe;
@@ -1284,12 +1309,12 @@ static int generate_impl(const spk_gen_desc* d, const spk_schedule* sched, spk_n
     set_error("generated network has %llu synapses; at most 2^31-1 per network are supported", tot[0]);
     return SPK_ERR_UNSUPPORTED;
   }
-  if (tot[0] > 0 && dr[0] != 1) {
-    set_error("minimum drawn delay %d steps: timestep grouping > 1 is not supported", dr[0]);
-    return SPK_ERR_UNSUPPORTED;
-  }
+  // timestep_grouping = the minimum drawn delay (Spike/Models/SpikingModel.cpp:98)
+  m.G = tot[0] > 0 ? dr[0] : 1;
+  rc = check_grouping(m);
+  if (rc) return rc;
   const int Dmax = tot[0] > 0 ? dr[1] : 1;
-  const int B = Dmax + 2 * 1 + 1;  // SpikingSynapses.cu:48 with G = 1
+  const int B = Dmax + 2 * m.G + 1;  // SpikingSynapses.cu:48
   spk_net* n = nullptr;
   rc = new_net(m, B, (int64_t)tot[0], sched, &n);
   if (rc) return rc;
@@ -1673,10 +1698,11 @@ int spk_net_write_rates(spk_net* n, int32_t stimulus, const float* rates, int64_
 
 int spk_net_run(spk_net* n, float seconds, int32_t plasticity_on) {
   if (!n || !(seconds >= 0.0f)) return SPK_ERR_INVALID;
-  // number_of_timesteps = ceil(seconds / timestep) in float
-  // (Spike/Models/SpikingModel.cpp:221-222), end time start + seconds (:235).
+  // number_of_timesteps = ceil(seconds / timestep) in float, number_of_steps
+  // = number_of_timesteps / timestep_grouping in integers (whole groups:
+  // Spike/Models/SpikingModel.cpp:221-222), end time start + seconds (:235).
   const float q = seconds / n->dt;
-  const int64_t steps = (int64_t)std::ceil(q);
+  const int64_t steps = ((int64_t)std::ceil(q) / n->G) * n->G;
   const float start = n->current_time;
   int rc = run_steps_impl(n, steps, plasticity_on, start);
   if (rc) return rc;
@@ -1684,8 +1710,19 @@ int spk_net_run(spk_net* n, float seconds, int32_t plasticity_on) {
   return SPK_OK;
 }
 
+// Runs given in timesteps advance whole groups of the network's timestep grouping.
+static int check_whole_groups(const spk_net* n, int64_t n_steps) {
+  if (n_steps % n->G != 0) {
+    set_error("%lld timesteps are not whole groups of the network's timestep grouping %d (its minimum delay)",
+              (long long)n_steps, n->G);
+    return SPK_ERR_INVALID;
+  }
+  return SPK_OK;
+}
+
 int spk_net_begin_run(spk_net* n, int64_t n_steps, int32_t plasticity_on) {
   if (!n || n_steps < 0 || n_steps > 0x7fffffff) return SPK_ERR_INVALID;
+  if (int rc = check_whole_groups(n, n_steps)) return rc;
   const float start = n->current_time;
   set_ctl_kernel<<<1, 1, 0, n->stream>>>(n->hd.ctl, start, (int)n_steps, (plasticity_on && n->has_stdp) ? 1 : 0,
                                          n->record_inputs ? 1 : 0);
@@ -1696,6 +1733,7 @@ int spk_net_begin_run(spk_net* n, int64_t n_steps, int32_t plasticity_on) {
 
 int spk_net_run_steps(spk_net* n, int64_t n_steps, int32_t plasticity_on) {
   if (!n || n_steps < 0) return SPK_ERR_INVALID;
+  if (int rc = check_whole_groups(n, n_steps)) return rc;
   const float start = n->current_time;
   int rc = run_steps_impl(n, n_steps, plasticity_on, start);
   if (rc) return rc;
@@ -1711,6 +1749,12 @@ int spk_net_synchronize(spk_net* n) {
   if (st == SPK_ERR_TIMEOUT) set_error("a device wait on another CTA timed out");
   if (st == SPK_ERR_OVERFLOW) set_error("the device spike store overflowed; spikes were dropped");
   return st;
+}
+
+int spk_net_timestep_grouping(const spk_net* n, int32_t* G) {
+  if (!n || !G) return SPK_ERR_INVALID;
+  *G = n->G;
+  return SPK_OK;
 }
 
 int spk_net_current_time(const spk_net* n, float* s) {
@@ -2298,6 +2342,7 @@ int spk_batch_run_steps_each(spk_batch* b, const int64_t* n_steps, const int32_t
   int64_t most = 0;
   for (size_t i = 0; i < b->nets.size(); ++i) {
     if (n_steps[i] < 0 || n_steps[i] > 0x7fffffff) return SPK_ERR_INVALID;
+    if (int rc = check_whole_groups(b->nets[i], n_steps[i])) return rc;
     most = std::max(most, n_steps[i]);
   }
   if (most == 0) return SPK_OK;
@@ -2461,7 +2506,7 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       for (const spk_net* n : b->nets) {
         if (n->hd.TS >= RANGE_MIN_TS) continue;
         b->ts_max = std::max(b->ts_max, n->hd.TS);
-        b->win_words = std::max(b->win_words, (n->hd.B - 3) * n->hd.TS * n->hd.L);
+        b->win_words = std::max(b->win_words, (n->hd.B - 2 * n->hd.G - 1) * n->hd.TS * n->hd.L);
       }
       b->win_words = std::min(b->win_words, BULK_WIN_CAP);
       // range windows: as many of a range's delay slots as the cap holds;
@@ -2470,10 +2515,10 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       for (const spk_net* n : b->nets) {
         if (n->hd.TS < RANGE_MIN_TS) continue;
         const int slot_words = n->hd.TS * n->hd.L;
-        const int ws = std::min(n->hd.B - 3, RANGE_WIN_CAP / slot_words);
+        const int ws = std::min(n->hd.B - 2 * n->hd.G - 1, RANGE_WIN_CAP / slot_words);
         b->range_smem.win_words = std::max(b->range_smem.win_words, ws * slot_words);
         b->range_smem.head_words =
-            std::max(b->range_smem.head_words, std::min((n->hd.B - 3) * slot_words, RANGE_HEAD_CAP));
+            std::max(b->range_smem.head_words, std::min((n->hd.B - 2 * n->hd.G - 1) * slot_words, RANGE_HEAD_CAP));
       }
       const size_t r_bytes = align_up(sizeof(BulkRangeBlock) * ranges.size(), 256);
       const size_t t_bytes = align_up(sizeof(BulkPropBlock) * tiles.size(), 256);
@@ -2956,6 +3001,12 @@ static int step_noalloc_impl(const spk_device_net* a, int64_t n_steps, int plast
     set_error("conductance/current synapses need label_tau (and label_vhat for conductance)");
     return SPK_ERR_INVALID;
   }
+  const int G = a->timestep_grouping > 1 ? a->timestep_grouping : 1;
+  if (G > a->max_delay || (G > 1 && stdp) || n_steps % G != 0) {
+    set_error("timestep grouping %d: needs at most the maximum delay %d, no plasticity, and whole groups "
+              "(%lld timesteps)", G, a->max_delay, (long long)n_steps);
+    return SPK_ERR_INVALID;
+  }
   if (stdp && (a->n_plastic_scales < 0 || a->n_plastic_scales >= MAX_CLASSES ||
                (a->n_plastic_scales > 0 && !a->plastic_scales))) {
     set_error("between 0 and %d plastic weight scales are supported", MAX_CLASSES - 1);
@@ -2977,7 +3028,7 @@ static int step_noalloc_impl(const spk_device_net* a, int64_t n_steps, int plast
     set_error("entries, csc, spikes and run_state must be 8-byte aligned");
     return SPK_ERR_INVALID;
   }
-  const int B = a->max_delay + 2 * 1 + 1;  // SpikingSynapses.cu:48 with G = 1
+  const int B = a->max_delay + 2 * G + 1;  // SpikingSynapses.cu:48
   const int n_tiles = W * C;
   if ((int64_t)n_tiles * TS < N) {
     set_error("schedule W=%d tile=%d ctas=%d covers %lld of %d neurons", W, TS, C, (long long)n_tiles * TS, N);
@@ -3051,6 +3102,7 @@ static int step_noalloc_impl(const spk_device_net* a, int64_t n_steps, int plast
   h.n_groups = a->n_groups;
   h.dt = a->dt;
   h.half_dt = 0.5f * a->dt;
+  h.G = G;
   h.t_ref = a->refractory_period;
   h.i_bg = a->background_current;
   for (int g = 0; g < a->n_groups; ++g) {

@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(RANGE_THREADS, SPK_RANGE_MINB)
   const StdpConst sc = stdp_const(d);
   if (tid < MAX_CLASSES) sm.scl[tid] = d.scale_tab[tid];
   // bucket heads: one per delay cell when they fit, else a power-of-two hash
-  const int dcells = (B - 3) * slot_words;
+  const int dcells = (B - 2 * d.G - 1) * slot_words;  // D_max slots
   const bool direct = dcells <= sz.head_words;
   const int hbits = 31 - __clz(max(sz.head_words, 1));
   const int hwords = direct ? dcells : (1 << hbits);
@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(RANGE_THREADS, SPK_RANGE_MINB)
       // The window pays when the step's entries (estimated from the first
       // chunk) would touch more ring sectors one by one than the window has
       // words to move: about one entry per four window words.
-      const int ws_max = min(B - 3, sz.win_words / slot_words);
+      const int ws_max = min(B - 2 * d.G - 1, sz.win_words / slot_words);
       const long long est = (long long)total * ((n_list + RANGE_KEYS - 1) / RANGE_KEYS);
       rr.ws = (ws_max > 0 && est * 4 > (long long)ws_max * slot_words) ? ws_max : 0;
       for (int k = 0; k < rr.ws; ++k) {

@@ -194,6 +194,12 @@ class Net:
         check(lib().spk_net_current_time(self.h, C.byref(t)), "spk_net_current_time")
         return t.value
 
+    def timestep_grouping(self) -> int:
+        """The network's minimum delay in steps: runs advance whole groups of it."""
+        g = C.c_int32()
+        check(lib().spk_net_timestep_grouping(self.h, C.byref(g)), "spk_net_timestep_grouping")
+        return g.value
+
     # ---- readback
     def spikes(self, population: int = N.SPK_POP_NEURONS):
         n = C.c_int64()
@@ -413,6 +419,14 @@ class Batch:
 
     def run_steps(self, steps: int, plasticity_on: bool = True):
         check(lib().spk_batch_run_steps(self.h, steps, 1 if plasticity_on else 0), "spk_batch_run_steps")
+
+    def run_steps_each(self, steps: list[int], plasticity_on: list[bool] | None = None):
+        """Each network its own step count (whole groups of its timestep
+        grouping) and plasticity switch."""
+        n = len(self.nets)
+        st = (C.c_int64 * n)(*steps)
+        pl = (C.c_int32 * n)(*[1 if p else 0 for p in plasticity_on]) if plasticity_on is not None else None
+        check(lib().spk_batch_run_steps_each(self.h, st, pl), "spk_batch_run_steps_each")
 
     def synchronize(self) -> int:
         return lib().spk_batch_synchronize(self.h)

@@ -24,17 +24,20 @@ def _lif(n, v0, vreset, theta, tref, ibg):
                      background_current=ibg)
 
 
-def ref_va(mixed: bool) -> Model:
+def ref_va(mixed: bool, d_lo: int = 1, d_hi: int = 1) -> Model:
+    """oracle/ref_cases.inc build_va: the unmixed net takes delays of d_lo..d_hi steps."""
     m = Model(N.SPK_SYN_CONDUCTANCE, N.SPK_INPUT_NONE, synapse_seed=-1, timestep=float(DT))
     nE, nI = (320, 80) if mixed else (3200, 800)
     args = (-60.0e-3, -60.0e-3, -50.0e-3, 5.0e-3, 2.0e-2)
     ge = m.add_neuron_group(_lif(nE, *args))
     gi = m.add_neuron_group(_lif(nI, *args))
     p = 0.1 if mixed else 0.02
-    es = SynapseParams(connectivity_type=N.SPK_CONN_RANDOM, delay_range=(steps(1), steps(4 if mixed else 1)),
+    es = SynapseParams(connectivity_type=N.SPK_CONN_RANDOM,
+                       delay_range=(steps(1 if mixed else d_lo), steps(4 if mixed else d_hi)),
                        weight_range=(0.2, 0.6) if mixed else (0.4, 0.4), weight_scaling_constant=10.0e-9,
                        random_connectivity_probability=p, reversal_potential_Vhat=0.0, decay_term_tau_g=5.0e-3)
-    is_ = SynapseParams(connectivity_type=N.SPK_CONN_RANDOM, delay_range=(steps(1), steps(6 if mixed else 1)),
+    is_ = SynapseParams(connectivity_type=N.SPK_CONN_RANDOM,
+                        delay_range=(steps(1 if mixed else d_lo), steps(6 if mixed else d_hi)),
                         weight_range=(5.1, 6.1) if mixed else (5.1, 5.1), weight_scaling_constant=10.0e-9,
                         random_connectivity_probability=p, reversal_potential_Vhat=-80.0e-3,
                         decay_term_tau_g=10.0e-3)

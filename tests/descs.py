@@ -91,9 +91,10 @@ class Desc:
 
 def random_voltage_net(n=300, n_in=200, rate=40.0, p=0.08, d_max=12, seed=5, plastic=False, stdp=None,
                        j=8.0e-4, g=4.0, record_inputs=True, stdp_rule=0, weight_norm=0, norm_initial=None,
-                       norm_sum=None):
+                       norm_sum=None, d_min=1):
     """A small random voltage-synapse network with inputs, E/I weights and
-    delays 1..d_max (multapses included), for parity tests."""
+    delays d_min..d_max (multapses included; d_min > 1 groups timesteps), for
+    parity tests."""
     rng = np.random.default_rng(seed)
     n_exc = int(0.8 * n)
     pre, post, w, dl = [], [], [], []
@@ -111,8 +112,8 @@ def random_voltage_net(n=300, n_in=200, rate=40.0, p=0.08, d_max=12, seed=5, pla
             post.append(q)
             w.append(j * 1.5)
     S = len(pre)
-    dl = rng.integers(1, d_max + 1, S)
-    dl[0] = 1
+    dl = rng.integers(d_min, d_max + 1, S)
+    dl[0] = d_min
     plastic_mask = None
     if plastic:
         pre_a = np.asarray(pre)

@@ -6,7 +6,9 @@ cases defined in oracle/ref_dump.cpp and stores what it produced:
 
 * small cases (va_mix, brunel, shapes): every array, as .npz;
 * the full VogelsAbbottNet network (va, 320,261 synapses): counts and SHA-256
-  digests of every array, as .json;
+  digests of every array, as .json; the same for its grouped variants va_g2
+  and va_g3 (delays of 2 and 3-5 steps) with the front end's timestep
+  grouping, as ref_va_grouped.json;
 * the weight and connectivity files the reference's save functions write for
   each case (Spike/Synapses/Synapses.cpp:423-614, SpikingSynapses.cpp:136-189;
   ref_dump's save mode), and the weights read back from the text file and
@@ -99,20 +101,25 @@ def main() -> int:
                   **{k: v for k, v in d.items() if not k.startswith("sorted_")}}
         np.savez_compressed(os.path.join(HERE, f"ref_{case}.npz"), **arrays)
         print(case, int(d["n_synapses"][0]), "synapses")
-    d = run_case(ref_dump, "va")
-    c = creation_order(d)
-    meta = {k: int(d[k][0]) for k in ("n_synapses", "n_neurons", "n_inputs", "min_delay", "max_delay",
-                                      "num_syn_labels", "timestep_grouping")}
-    meta["digests_created"] = {k: digest(v) for k, v in c.items()}
-    meta["digests_sorted"] = {k: digest(d["sorted_" + k]) for k in ("pre", "post", "weight", "delay", "label")}
-    meta["eff_count_digest"] = digest(d["eff_count"])
-    meta["tau_m"] = float(d["tau_m"][0])
-    meta["R"] = float(d["R"][0])
-    meta["vhat"] = [float(x) for x in d["vhat"]]
-    meta["tau_g"] = [float(x) for x in d["tau_g"]]
+    def digests(case):
+        d = run_case(ref_dump, case)
+        c = creation_order(d)
+        meta = {k: int(d[k][0]) for k in ("n_synapses", "n_neurons", "n_inputs", "min_delay", "max_delay",
+                                          "num_syn_labels", "timestep_grouping")}
+        meta["digests_created"] = {k: digest(v) for k, v in c.items()}
+        meta["digests_sorted"] = {k: digest(d["sorted_" + k]) for k in ("pre", "post", "weight", "delay", "label")}
+        meta["eff_count_digest"] = digest(d["eff_count"])
+        meta["tau_m"] = float(d["tau_m"][0])
+        meta["R"] = float(d["R"][0])
+        meta["vhat"] = [float(x) for x in d["vhat"]]
+        meta["tau_g"] = [float(x) for x in d["tau_g"]]
+        print(case, meta["n_synapses"], "synapses, grouping", meta["timestep_grouping"])
+        return meta
+
     with open(os.path.join(HERE, "ref_va.json"), "w") as f:
-        json.dump(meta, f, indent=1, sort_keys=True)
-    print("va", meta["n_synapses"], "synapses")
+        json.dump(digests("va"), f, indent=1, sort_keys=True)
+    with open(os.path.join(HERE, "ref_va_grouped.json"), "w") as f:
+        json.dump({case: digests(case) for case in ("va_g2", "va_g3")}, f, indent=1, sort_keys=True)
     ck = {case: checkpoint_digests(ref_dump, case) for case in ("va", "va_mix", "brunel", "shapes")}
     with open(os.path.join(HERE, "ref_checkpoint.json"), "w") as f:
         json.dump(ck, f, indent=1, sort_keys=True)

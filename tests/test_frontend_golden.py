@@ -81,3 +81,19 @@ def test_vogels_abbott_full_network_digests():
     a = desc_arrays(m.desc())
     for k, h in meta["digests_created"].items():
         assert hashlib.sha256(np.ascontiguousarray(a[k]).tobytes()).hexdigest() == h, k
+
+
+@pytest.mark.parametrize("case,d_lo,d_hi", [("va_g2", 2, 2), ("va_g3", 3, 5)])
+def test_grouped_vogels_abbott_digests(case, d_lo, d_hi):
+    """The network with delays of d_lo..d_hi steps: every array bit-identical,
+    and its minimum delay is the timestep grouping the reference's
+    finalise_model chose (Spike/Models/SpikingModel.cpp:98)."""
+    with open(os.path.join(GOLD, "ref_va_grouped.json")) as f:
+        meta = json.load(f)[case]
+    m = cases.ref_va(False, d_lo, d_hi)
+    assert m.counts() == (meta["n_neurons"], meta["n_inputs"], meta["n_synapses"])
+    a = desc_arrays(m.desc())
+    for k, h in meta["digests_created"].items():
+        assert hashlib.sha256(np.ascontiguousarray(a[k]).tobytes()).hexdigest() == h, k
+    assert int(a["delay"].min()) == meta["min_delay"] == meta["timestep_grouping"] == d_lo
+    assert int(a["delay"].max()) == meta["max_delay"]

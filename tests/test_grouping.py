@@ -1,0 +1,270 @@
+"""Timestep grouping: networks whose minimum delay G is above one step.
+
+The reference advances such a network G timesteps per step of its run loop
+(Spike/Models/SpikingModel.cpp:98, :221-228): the group's time is
+start + s*G*dt in float, substep g's time that + g*dt, and run(seconds)
+simulates whole groups only (the integer division of :222).  Every delay is
+at least G steps, so a group's deliveries all land past it and the engine may
+advance the group substep by substep.
+
+CPU: the oracle against a literal restatement of the reference's grouped loop
+(below), the run-length rule, and the refusals.  GPU: the engine against the
+oracle, bit for bit, on the persistent path under several schedules (blocks
+that cut groups), in batches (bulk and waves mode) and through
+spk_step_noalloc (tests/test_zz_no_alloc.py).
+"""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+import cases
+import descs
+from engine_checks import assert_same, bits
+from oracle import OracleNet
+from spike_gb300 import _native as N
+from spike_gb300 import desc_arrays
+from spike_gb300.model import STDPParams
+
+F = np.float32
+
+
+def _tiny_net(G: int, d_max: int, seed: int = 11):
+    """Forty voltage-synapse LIF neurons driven by a background current over
+    threshold (no inputs, so no random draws during the run), random E/I
+    weights and delays G..d_max."""
+    rng = np.random.default_rng(seed)
+    n, S = 40, 420
+    pre = rng.integers(0, n, S)
+    post = rng.integers(0, n, S)
+    w = np.where(pre < 32, rng.uniform(1e-3, 4e-3, S), -rng.uniform(2e-3, 9e-3, S)).astype(np.float32)
+    delay = rng.integers(G, d_max + 1, S)
+    delay[0] = G
+    groups = [dict(count=32, tau_m=0.005, R=1e8, v0=0.0, vreset=0.0, theta=0.02, v_init_lo=0.0, v_init_hi=0.02),
+              dict(count=8, tau_m=0.004, R=1e8, v0=0.0, vreset=0.005, theta=0.02, v_init_lo=0.0, v_init_hi=0.02)]
+    return descs.Desc(kind=N.SPK_SYN_VOLTAGE, groups=groups, refractory=0.002, i_bg=0.03, n_inputs=0,
+                      pre=pre, post=post, weight=w, scale=np.ones(S), delay=delay, record_inputs=False)
+
+
+class GroupedReference:
+    """SpikingModel::run with timestep grouping G, written as the reference's
+    kernels are structured: per step, lif_update_membrane_potentials loops
+    over the neurons and, inside, over the G substeps
+    (Spike/Backend/CUDA/Neurons/LIFSpikingNeurons.cu:105-193, voltage
+    injection), then activate_synapses delivers the step's spikes to
+    (bufferloc + delay + g) % B (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:168-202),
+    B = D_max + 2G + 1 (:48).  Float32 throughout, no contraction; the ring
+    additions in the canonical order (substep, then presynaptic key, then
+    sorted synapse order)."""
+
+    def __init__(self, d, o: OracleNet):
+        a = desc_arrays(d)
+        pre, post, delay = o.sorted_synapses()
+        # the oracle's sorted order (stable by presynaptic key) with each synapse's weight
+        order = np.argsort(a["pre"], kind="stable")
+        assert np.array_equal(a["pre"][order], pre) and np.array_equal(a["post"][order], post)
+        self.post, self.delay = post, delay
+        self.c = (a["weight"][order].astype(F) * a["scale"][order].astype(F)).astype(F)
+        self.start = np.searchsorted(pre, np.arange(d.n_neurons + 1))
+        self.n, self.G = d.n_neurons, int(delay.min())
+        self.B = int(delay.max()) + 2 * self.G + 1
+        self.dt = F(d.dt)
+        self.ring = np.zeros((self.B, self.n), F)
+        grp = np.ctypeslib.as_array(d.groups, (d.n_groups,))
+        self.k, self.v0, self.vr, self.th = (np.empty(self.n, F) for _ in range(4))
+        for g in grp:
+            sl = slice(g["start"], g["start"] + g["count"])
+            self.k[sl] = F(self.dt / F(g["tau_m"]))
+            self.v0[sl], self.vr[sl], self.th[sl] = F(g["v0"]), F(g["vreset"]), F(g["theta"])
+        self.ibg, self.tref = F(d.background_current), F(d.refractory_period)
+        self.V = o.state(N.SPK_FIELD_V, self.n).copy()  # the initial potentials (Philox-drawn)
+        self.last = np.full(self.n, F(-1000.0), F)
+        self.time = F(0.0)
+        self.ids, self.times = [], []
+
+    def run(self, seconds: float):
+        G, dt, half = self.G, self.dt, F(F(0.5) * self.dt)
+        n_timesteps = int(np.ceil(F(seconds) / dt))
+        start = self.time
+        for s in range(n_timesteps // G):
+            t = F(start + F(s * G) * dt)
+            tidx = int(math.floor(float(F(t / dt)) + 0.5))  # (int)roundf(t/dt), t >= 0
+            fired = [[] for _ in range(G)]
+            for idx in range(self.n):
+                Vi = self.V[idx]
+                for g in range(G):
+                    cell = ((tidx + g) % self.B, idx)
+                    inp = F(F(0.0) + self.ring[cell])
+                    self.ring[cell] = F(0.0)
+                    tg = F(t + F(g) * dt)
+                    if F(F(tg - self.last[idx]) - self.tref) > half:
+                        k = self.k[idx]
+                        Vi = F(F(F(F(k * self.v0[idx]) + F(F(F(1.0) - k) * Vi)) + F(k * self.ibg)) + inp)
+                        if Vi >= self.th[idx]:
+                            self.last[idx] = tg
+                            Vi = self.vr[idx]
+                            fired[g].append(idx)
+                self.V[idx] = Vi
+            for g in range(G):
+                for idx in fired[g]:
+                    self.ids.append(idx)
+                    self.times.append(F(t + F(g) * dt))
+                    for syn in range(self.start[idx], self.start[idx + 1]):
+                        cell = ((tidx + self.delay[syn] + g) % self.B, self.post[syn])
+                        self.ring[cell] = F(self.ring[cell] + self.c[syn])
+        self.time = F(start + F(seconds))
+
+
+@pytest.mark.parametrize("G,d_max", [(2, 2), (3, 7)])
+def test_oracle_follows_the_reference_group_loop(G, d_max):
+    """The oracle (substep by substep) against the reference's grouped loop,
+    bit for bit: spike ids and float times, potentials and the end time, over
+    runs whose step counts are not whole groups (rounded down)."""
+    d = _tiny_net(G, d_max)
+    o = OracleNet(d.desc)
+    assert o.timestep_grouping() == G
+    ref = GroupedReference(d.desc, o)
+    for sec in (0.0137, 0.0071, 0.02):
+        o.run(sec)
+        ref.run(sec)
+        assert o.current_time() == ref.time
+    ids, times = o.spikes()
+    assert len(ids) == len(ref.ids) > 200
+    np.testing.assert_array_equal(ids, np.asarray(ref.ids))
+    np.testing.assert_array_equal(bits(times), bits(np.asarray(ref.times, F)))
+    np.testing.assert_array_equal(bits(o.state(N.SPK_FIELD_V, 40)), bits(ref.V))
+    np.testing.assert_array_equal(bits(o.state(N.SPK_FIELD_LAST_SPIKE, 40)), bits(ref.last))
+
+
+def test_oracle_run_length_is_whole_groups():
+    """run(seconds) simulates floor(ceil(seconds/dt) / G) groups; the time
+    still advances by the seconds asked for, and step counts must be whole
+    groups."""
+    d = _tiny_net(3, 5)
+    o, o9, o12 = OracleNet(d.desc), OracleNet(d.desc), OracleNet(d.desc)
+    o.run(0.0011)  # ceil(11) timesteps = 3 groups = 9 timesteps
+    o9.run_steps(9)
+    o12.run_steps(12)
+    assert o.current_time() == F(0.0011)
+    assert o9.current_time() == F(F(9) * F(1e-4))
+    v, v9, v12 = (x.state(N.SPK_FIELD_V, 40) for x in (o, o9, o12))
+    np.testing.assert_array_equal(bits(v), bits(v9))
+    assert not np.array_equal(bits(v), bits(v12))
+    o.run_steps(6)
+    with pytest.raises(RuntimeError):
+        o.run_steps(4)
+
+
+def test_grouped_spike_times_are_group_time_plus_substep():
+    """Recorded times are (start + (s*G)*dt) + g*dt in float, the spike
+    monitor's current_time + g*timestep, not start + (s*G + g)*dt."""
+    d = descs.random_voltage_net(n=200, n_in=100, d_min=3, d_max=9, rate=80.0)
+    o = OracleNet(d.desc)
+    o.run(0.05)
+    o.run(0.0371)
+    ids, times = o.spikes()
+    dt = F(1e-4)
+    start = F(0.05)
+    late = times > start
+    # in the second run: group s of 3, substep g; the times are exactly those of the formula
+    allowed = {F(F(start + F(s * 3) * dt) + F(g) * dt) for s in range(200) for g in range(3)}
+    assert late.sum() > 50
+    assert set(times[late].tolist()) <= {float(x) for x in allowed}
+
+
+def test_plasticity_with_grouping_is_refused_before_any_device_call():
+    stdp = STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02, lambda_=1.0, alpha=1.0,
+                      w_max=1.0)
+    d = descs.random_voltage_net(n=60, n_in=30, d_min=2, plastic=True, stdp=stdp)
+    h = ctypes.c_void_p()
+    assert N.lib().spk_net_create(ctypes.byref(d.desc), None, ctypes.byref(h)) == N.SPK_ERR_UNSUPPORTED
+    assert b"timestep grouping" in N.lib().spk_last_error()
+    with pytest.raises(RuntimeError):
+        OracleNet(d.desc)
+
+
+def test_noalloc_grouping_checks_before_any_device_call():
+    lib = N.lib()
+    g = (N.NeuronGroup * 1)()
+    g[0].start, g[0].count, g[0].tau_m, g[0].R, g[0].theta = 0, 64, 0.02, 1e8, 0.02
+    dummy = ctypes.create_string_buffer(64)
+    addr = ctypes.addressof(dummy)
+    dn = N.DeviceNet()
+    dn.n_neurons, dn.n_inputs, dn.n_labels, dn.synapse_kind, dn.max_delay = 64, 0, 1, N.SPK_SYN_VOLTAGE, 4
+    dn.warps_per_cta, dn.tile_posts, dn.ctas = 2, 32, 1
+    dn.dt, dn.refractory_period = 1e-4, 2e-3
+    dn.n_groups, dn.groups = 1, g
+    for f in ("rowptr", "entries", "V", "last_spike", "ring", "spikes", "run_state"):
+        setattr(dn, f, addr)
+    dn.spike_capacity = 1
+    dn.timestep_grouping = 3
+    # 0 steps of a grouping of 3 pass the checks (nothing would run); 4 steps are not whole groups
+    assert lib.spk_step_noalloc(ctypes.byref(dn), 4, 0, ctypes.c_float(0.0), None) == N.SPK_ERR_INVALID
+    assert b"timestep grouping" in lib.spk_last_error()
+    dn.timestep_grouping = 5  # above the maximum delay
+    assert lib.spk_step_noalloc(ctypes.byref(dn), 0, 0, ctypes.c_float(0.0), None) == N.SPK_ERR_INVALID
+
+
+# ---- GPU: the engine against the oracle --------------------------------------------------
+
+@pytest.mark.gpu
+def test_grouped_vogels_abbott_engine_equals_oracle():
+    """The Vogels-Abbott network with delays of 3-5 steps (G = 3)."""
+    from spike_gb300 import Net
+    m = cases.ref_va(False, 3, 5)
+    d = m.desc()
+    o = OracleNet(d)
+    net = Net.from_desc(d)
+    assert net.timestep_grouping() == o.timestep_grouping() == 3
+    for sec in (0.05, 0.0333, 0.05):
+        net.run(sec)
+        o.run(sec)
+    net.run_steps(3 * 37)
+    o.run_steps(3 * 37)
+    assert net.synchronize() == 0
+    assert net.current_time() == o.current_time()
+    assert_same(net, o, 4000, 0, 2, tag="va_g3")
+    assert len(o.spikes()[0]) > 1000
+    with pytest.raises(RuntimeError):
+        net.run_steps(4)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("sched", [None, (8, 32, 0, 0), (4, 64, 0, 7), (2, 32, 6, 50)])
+@pytest.mark.parametrize("G", [2, 3])
+def test_grouped_voltage_net_with_inputs_across_schedules(sched, G):
+    """Poisson inputs and recurrent synapses with delays G..12; launches of 7
+    and 50 timesteps cut groups in two."""
+    from spike_gb300 import Net, schedule
+    d = descs.random_voltage_net(n=300, n_in=200, d_min=G, d_max=12, seed=G)
+    o = OracleNet(d.desc)
+    net = Net.from_desc(d.desc, schedule(*sched) if sched else None)
+    for sec in (0.0301, 0.0173, 0.04):
+        net.run(sec)
+        o.run(sec)
+    assert net.synchronize() == 0
+    assert_same(net, o, 300, 200, 1, tag=f"G={G} {net.schedule()}")
+    assert len(o.spikes()[0]) > 200
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [N.SPK_BATCH_BULK, N.SPK_BATCH_WAVES])
+def test_batch_of_grouped_networks_equals_each_alone(mode):
+    """Networks with groupings 1, 2 and 3 in one batch; each run's step count
+    is whole groups of its own network."""
+    from spike_gb300 import Batch, Net, schedule
+    ds = [descs.random_voltage_net(n=n, n_in=ni, seed=s, d_min=g, d_max=10)
+          for n, ni, s, g in ((150, 100, 1, 1), (420, 90, 2, 2), (64, 300, 3, 3), (700, 50, 4, 2))]
+    nets = [Net.from_desc(x.desc, schedule(4, 0, 0, 0)) for x in ds]
+    orcs = [OracleNet(x.desc) for x in ds]
+    b = Batch(nets)
+    b.set_mode(mode)
+    steps = [330, 330, 330, 330]
+    b.run_steps_each(steps)
+    assert b.synchronize() == 0
+    for x, net, o, k in zip(ds, nets, orcs, steps):
+        o.run_steps(k)
+        assert_same(net, o, x.desc.n_neurons, x.desc.n_inputs, 1, tag=f"batch mode {mode}")
+    with pytest.raises(RuntimeError):
+        b.run_steps_each([330, 331, 330, 330])

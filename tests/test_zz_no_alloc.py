@@ -51,7 +51,8 @@ class CallerNet:
         n_keys = KL + n_tiles * TS
         S = len(a["pre"])
         max_delay = int(a["delay"].max()) if S else 1
-        B = max_delay + 3
+        G = int(a["delay"].min()) if S else 1  # timestep grouping: the minimum delay
+        B = max_delay + 2 * G + 1
         self.N, self.Nin, self.L, self.KL, self.B, self.TS, self.n_tiles = Nn, Nin, L, KL, B, TS, n_tiles
 
         # scale classes of plastic synapses, numbered by first appearance
@@ -127,6 +128,7 @@ class CallerNet:
         dn.post_trace, dn.pre_trace = t["post_tr"].data_ptr(), t["pre_tr"].data_ptr()
         dn.spikes, dn.spike_capacity = t["spikes"].data_ptr(), spike_capacity
         dn.run_state = t["run_state"].data_ptr()
+        dn.timestep_grouping = G
         self.dn = dn
         self.dt = np.float32(d.dt)
         self.time = np.float32(0.0)
