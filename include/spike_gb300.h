@@ -231,7 +231,18 @@ int spk_net_run_steps(spk_net* net, int64_t n_steps, int32_t plasticity_on);
  * it a block at a time (the server's continuous batching). */
 int spk_net_begin_run(spk_net* net, int64_t n_steps, int32_t plasticity_on);
 /* Wait for the handle's stream; returns the device status word
- * (SPK_ERR_TIMEOUT / SPK_ERR_OVERFLOW) or SPK_OK. */
+ * (SPK_ERR_TIMEOUT / SPK_ERR_OVERFLOW / SPK_ERR_UNSUPPORTED) or SPK_OK.
+ *
+ * Run boundaries follow the reference's double-buffered active lists
+ * (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:156-202): list (T/G) % 2 is
+ * emptied only by a group step of the other parity, so a run whose first
+ * group index T/G has the parity of the last group step's (the timestep index
+ * repeats at a run start when seconds/dt has a fraction below one half, as
+ * for run(0.1) at dt = 1e-4; a grouped network skips one) delivers the last
+ * group's spikes again to its own first slots before its own.  Were the list
+ * to hold two groups (a one-group run that began so, then another such
+ * start), SPK_ERR_UNSUPPORTED is raised and only the last group is delivered
+ * again. */
 int spk_net_synchronize(spk_net* net);
 int spk_net_current_time(const spk_net* net, float* seconds);
 /* SpikingModel::timestep_grouping (Spike/Models/SpikingModel.cpp:98): the
@@ -553,7 +564,9 @@ int spk_net_generate_estimate(const spk_gen_desc* desc, const spk_schedule* sche
  *    Poisson activity from call to call, and holds the spikes recorded so far
  *    (uint64 at byte 32; zero it to clear the store), the synaptic events
  *    delivered (uint64 at byte 40) and the device status (int32 at byte 48: 0,
- *    SPK_ERR_TIMEOUT or SPK_ERR_OVERFLOW), valid once the stream has finished.
+ *    SPK_ERR_TIMEOUT, SPK_ERR_OVERFLOW or SPK_ERR_UNSUPPORTED, the last for
+ *    an active list of two carried groups, see spk_net_synchronize), valid
+ *    once the stream has finished.
  *    A non-zero status stays in run_state across later calls until the caller
  *    clears it.  After SPK_ERR_OVERFLOW the state is sound (only spikes beyond
  *    spike_capacity were dropped): zero the status and the spike count to go
@@ -612,6 +625,12 @@ typedef struct spk_device_net {
    * in steps); 0 or 1 = none.  G > 1 needs has_stdp = 0 and n_steps a
    * multiple of G (the reference's run() advances whole groups). */
   int32_t timestep_grouping;
+  /* [G * n_keys/32] spike words of each substep of the last group, zeroed by
+   * the caller with run_state: a call whose first group index has the parity
+   * of the last group's delivers that group's spikes again, as the
+   * reference's double-buffered active lists do
+   * (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:179-182). */
+  uint32_t* group_bits;
 } spk_device_net;
 
 /* Advance the network n_steps timesteps from start_time (seconds) on `stream`

@@ -94,6 +94,19 @@ struct Net {
   std::vector<int32_t> rec_ids[2];
   std::vector<float> rec_times[2];
 
+  // The reference's two active-neuron lists (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:156-202)
+  // are double-buffered by the parity of the group index T/G: a group step
+  // appends its spikes to list (T/G) % 2, delivers that whole list, and empties
+  // the other one.  Consecutive group steps whose indices have equal parity (a
+  // run that starts at the group index where the last one ended, or two past
+  // it) therefore deliver the earlier group's spikes again, to the later
+  // group's slots.  Within a run the index advances by one per group, so this
+  // happens only where a run starts; the state below carries it across runs.
+  std::vector<std::vector<int64_t>> group_keys;  // [G]: active keys of each substep of the last group
+  int64_t last_group = -1;        // index T/G of the last group step; -1: none since reset
+  int64_t last_run_groups = 0;    // groups of the run that ended with it
+  bool last_run_repeat = false;   // that run began by delivering its predecessor's group again
+
   // ---- per-step scratch -----------------------------------------------------
   std::vector<uint8_t> spiked;  // per key, this step
   std::vector<int64_t> active;  // keys, ascending
@@ -112,7 +125,8 @@ struct Net {
   void reset_state();
   void reset_inputs();
   void set_threads(int t);
-  void run_steps(int64_t n_steps, float start, bool plastic);
+  int run_steps(int64_t n_steps, float start, bool plastic);
+  void deliver_keys(const std::vector<int64_t>& keys, int T);
   void lif_range(int a, int b, R t, int T);
   void poisson_range(int a, int b, R t, int T);
   void stdp_range(int64_t a, int64_t b, R t);
@@ -387,6 +401,26 @@ void Net<R>::reset_state() {
   std::fill(stdp_pre.begin(), stdp_pre.end(), (R)0);
   std::fill(stdp_post.begin(), stdp_post.end(), (R)0);
   std::fill(hist.begin(), hist.end(), (uint8_t)0);
+  // SpikingSynapses::reset_state empties both active lists (SpikingSynapses.cu:33)
+  group_keys.assign(G, {});
+  last_group = -1;
+  last_run_groups = 0;
+  last_run_repeat = false;
+}
+
+// activate_synapses (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:168-202)
+// for the listed keys' efferent synapses, delivered to (T + delay) % B, one
+// after another in list order and sorted synapse order.
+template <typename R>
+void Net<R>::deliver_keys(const std::vector<int64_t>& keys, int T) {
+  const size_t row = (size_t)N * L;
+  for (int64_t key : keys) {
+    for (int64_t s = eff_start[key]; s < eff_start[key] + eff_count[key]; ++s) {
+      const int targetloc = (T + sdelay[s]) % B;
+      ring[(size_t)targetloc * row + (size_t)spost[s] * L + slabel[s]] += sw[s] * sscale[s];
+    }
+    events += (uint64_t)eff_count[key];
+  }
 }
 
 template <typename R>
@@ -716,7 +750,27 @@ void Net<R>::propagate_thread(int th, int T) {
 }
 
 template <typename R>
-void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
+int Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
+  if (n_steps == 0) return SPK_OK;  // no group step: the lists stay as they are
+  {
+    // The run's first group has index roundf(start/dt) / G.  If the previous
+    // group step's index had the same parity, its list still holds that
+    // group's spikes: they are delivered again to this group's slots, first.
+    const int64_t first = round_to_int(start / dt_f) / G;
+    const bool repeat = last_group >= 0 && ((first ^ last_group) & 1) == 0;
+    if (repeat) {
+      // a run of one group that itself began this way left two groups in the list
+      if (last_run_groups == 1 && last_run_repeat) return SPK_ERR_UNSUPPORTED;
+      const int T0 = round_to_int(start / dt_f);
+      for (int g = 0; g < G; ++g) deliver_keys(group_keys[g], T0 + g);
+    }
+    last_run_repeat = repeat;
+    last_run_groups = n_steps / G;
+    // the run's last group: timestep n_steps - G
+    const int64_t s_last = n_steps - G;
+    const float t_last = start + (float)s_last * dt_f;
+    last_group = round_to_int(t_last / dt_f) / G;
+  }
   auto step_time = [&](int64_t s, R& t, int& T) {
     // Timestep s is substep g = s % G of group s / G.  The group's
     // current_time_in_seconds = starttime + s*timestep_grouping*timestep
@@ -733,11 +787,12 @@ void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
     T = round_to_int(tf / dt_f) + (int)g;
     t = (sizeof(R) == 4) ? (R)(tf + (float)g * dt_f) : ((R)start + (R)(grp * G) * dt) + (R)g * dt;
   };
-  auto finish_step = [&](R t, int T) {
+  auto finish_step = [&](R t, int T, int64_t s) {
     active.clear();
     const int K = nkeys();
     for (int kk = 0; kk < K; ++kk)
       if (spiked[kk]) active.push_back(kk);
+    group_keys[(size_t)(s % G)] = active;
     // this step's spike bits, for the rules that look delays back
     std::copy(spiked.begin(), spiked.end(), hist.begin() + (size_t)(T % H) * K);
     for (int64_t kk : active) events += (uint64_t)eff_count[kk];
@@ -773,11 +828,11 @@ void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
       if (do_stdp) stdp_range(0, (int64_t)plastic_idx.size(), t);
       if (do_dense) dense_stdp_range(0, (int64_t)plastic_idx.size(), T);
       if (norm_after) normalise_weights();
-      finish_step(t, T);
+      finish_step(t, T, s);
       propagate_thread(0, T);
       record(t);
     }
-    return;
+    return SPK_OK;
   }
   std::barrier<> bar(threads);
   R t_cur = 0;
@@ -804,7 +859,7 @@ void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
       }
       // finish_step writes history slot T, which no range reads this step
       // (delays are 1..H-1)
-      if (th == 0) finish_step(t_cur, T_cur);
+      if (th == 0) finish_step(t_cur, T_cur, s);
       bar.arrive_and_wait();
       propagate_thread(th, T_cur);
       if (th == 0) record(t_cur);
@@ -815,6 +870,7 @@ void Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
   for (int th = 1; th < threads; ++th) pool.emplace_back(worker, th);
   worker(0);
   for (auto& x : pool) x.join();
+  return SPK_OK;
 }
 
 struct Handle {
@@ -915,7 +971,8 @@ int oracle_run(oracle_net* n, float seconds, int plasticity_on) {
     const float q = seconds / net.dt_f;
     const int64_t steps = ((int64_t)std::ceil(q) / net.G) * net.G;
     const float start = net.current_time;
-    net.run_steps(steps, start, plasticity_on != 0);
+    const int rc = net.run_steps(steps, start, plasticity_on != 0);
+    if (rc) return rc;
     net.current_time = start + seconds;
     return SPK_OK;
   });
@@ -926,7 +983,8 @@ int oracle_run_steps(oracle_net* n, int64_t n_steps, int plasticity_on) {
   return dispatch(n, [&](auto& net) {
     if (n_steps % net.G != 0) return SPK_ERR_INVALID;  // whole groups only
     const float start = net.current_time;
-    net.run_steps(n_steps, start, plasticity_on != 0);
+    const int rc = net.run_steps(n_steps, start, plasticity_on != 0);
+    if (rc) return rc;
     net.current_time = start + (float)n_steps * net.dt_f;
     return SPK_OK;
   });

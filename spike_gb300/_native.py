@@ -167,7 +167,7 @@ class DeviceNet(C.Structure):
         ("V", C.c_void_p), ("last_spike", C.c_void_p), ("syn_trace", C.c_void_p), ("ring", C.c_void_p),
         ("input_next", C.c_void_p), ("rates", C.c_void_p), ("post_trace", C.c_void_p),
         ("pre_trace", C.c_void_p), ("spikes", C.c_void_p), ("spike_capacity", i64), ("run_state", C.c_void_p),
-        ("timestep_grouping", i32),
+        ("timestep_grouping", i32), ("group_bits", C.c_void_p),
     ]
 
 

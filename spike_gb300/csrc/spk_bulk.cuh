@@ -70,7 +70,7 @@ constexpr int BULK_STAGE_ENTRIES = SPK_BULK_STAGE_ENTRIES;  // entries staged pe
 // Timestep s of the current block of a network's run.
 struct BulkStep {
   float t, tg;
-  int T, slot;
+  int T, slot, g;  // g: substep of the group
   bool live, stdp_run, inputs_active;
   bool dense_run;  // a per-synapse-trace rule updates this step
 };
@@ -82,6 +82,7 @@ __device__ __forceinline__ BulkStep bulk_step(const NetDev& d, const RunCtl& c, 
   const float dt = d.dt;
   group_time(c.start_time, sr, d.G, dt, b.t, b.T, b.tg);
   b.slot = b.T % d.B;
+  b.g = sr % d.G;
   // the event-driven (weight-dependent) rule's passes, or the per-synapse-trace rules' pass
   b.stdp_run = d.has_stdp && c.plastic && d.stdp_rule == SPK_STDP_WEIGHT_DEPENDENT;
   b.dense_run = d.has_stdp && c.plastic && d.stdp_rule != SPK_STDP_WEIGHT_DEPENDENT;
@@ -258,6 +259,7 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
         d.bitsA[bw.word + u] = word;
         d.bitsP[bw.word + u] = st.stdp_run ? word : 0u;
         if (d.hist) d.hist[(size_t)(st.T % d.H) * d.n_words + bw.word + u] = word;
+        d.gbits[(size_t)st.g * d.n_words + bw.word + u] = word;
       }
     }
   } else {
@@ -307,6 +309,7 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
         d.bitsA[bw.word + u] = wa;
         d.bitsP[bw.word + u] = wp;
         if (d.hist) d.hist[(size_t)(st.T % d.H) * d.n_words + bw.word + u] = wa;
+        d.gbits[(size_t)st.g * d.n_words + bw.word + u] = wa;
       }
     }
   }

@@ -63,7 +63,46 @@ struct RunCtl {
   int pad;
   unsigned long long stdp_pre;     // plastic weights updated on a presynaptic event
   unsigned long long stdp_post;    // plastic afferents updated on a postsynaptic spike
+  // The reference's two active-neuron lists
+  // (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:156-202) are double-buffered
+  // by the parity of the group index T/G: a group step appends its spikes to
+  // list (T/G) % 2, delivers that whole list and empties the other one, so
+  // consecutive group steps with indices of equal parity deliver the earlier
+  // group's spikes again.  Within a run the index advances by one per group;
+  // where a run starts, it can repeat or skip one.  State of the lists:
+  int repeat;           // the current run began by delivering the last group's spikes again
+  int last_group_p1;    // 1 + index of the last group step before the current run; 0: none
+  int last_run_groups;  // groups of the run that ended with it
+  int last_run_repeat;  // that run began by delivering a carried group again
 };
+
+// Index T/G of the group of timestep r of a run started at `start`.
+SPK_HD int group_index(float start, int r, int G, float dt) {
+  const int s = r / G;
+  const float t = start + (float)(s * G) * dt;
+  return (int)roundf(t / dt) / G;
+}
+
+// Folds the run recorded in c (if it advanced any step) into the list state.
+SPK_HD void fold_finished_run(RunCtl& c, int G, float dt) {
+  if (c.step <= 0) return;
+  c.last_group_p1 = group_index(c.start_time, c.step - 1, G, dt) + 1;
+  c.last_run_groups = c.step / G;
+  c.last_run_repeat = c.repeat;
+  c.step = 0;
+}
+
+// For a run of `steps` timesteps from `start`, after fold_finished_run: 1 if
+// it begins by delivering the last group's spikes again (its first group
+// index has the last group step's parity), 2 if the list would also hold the
+// group before (a run of one group that began so, followed by another such
+// start), 0 otherwise.
+SPK_HD int carry_decision(const RunCtl& c, int G, float dt, float start, int steps) {
+  if (steps <= 0 || c.last_group_p1 == 0) return 0;
+  const int first = (int)roundf(start / dt) / G;
+  if (((first ^ (c.last_group_p1 - 1)) & 1) != 0) return 0;
+  return (c.last_run_groups == 1 && c.last_run_repeat) ? 2 : 1;
+}
 
 // Everything one CTA needs to run its share of one network.
 struct NetDev {
@@ -120,6 +159,9 @@ struct NetDev {
   int* step_count;            // keys in step_list
   // rate monitor: spikes of each key since the last clear, or null
   int* rate_counts;           // [n_keys]
+  // Spike words of each substep of the last group ([G][n_words]), the list a
+  // run delivers again when it starts at a group index of the same parity.
+  uint32_t* gbits;
   // Rules with two traces per plastic synapse (SPK_STDP_EVANS,
   // SPK_STDP_INHIBITORY, SPK_STDP_CUSTOM; bulk mode only): the records' delays, the traces,
   // and the spike words of the last H timesteps (slot T % H), in which a

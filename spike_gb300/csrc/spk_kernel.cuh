@@ -269,6 +269,7 @@ __global__ void __launch_bounds__(512, 1)
     float t, tg;
     int T;
     group_time(ctl0.start_time, sr, d.G, dt, t, T, tg);
+    const int g_sub = sr % d.G;  // substep of the group
     const long long gs = ctl0.gstep + s;
     const int par = (int)(gs & 1);
     const unsigned stamp = (unsigned)(gs + 1);
@@ -417,6 +418,13 @@ __global__ void __launch_bounds__(512, 1)
           bitsP[wi] = inwp_s[i - nl];
         }
       }
+    }
+    {
+      // this substep's spike words: the list a later run may deliver again
+      uint32_t* gb = d.gbits + (size_t)g_sub * n_words;
+      const int nl = TS >> 5, ni = ITS >> 5;
+      for (int i = lane; i < nl + ni; i += 32)
+        gb[i < nl ? ((KL + p0) >> 5) + i : (kin0 >> 5) + (i - nl)] = i < nl ? spkw_s[i] : inw_s[i - nl];
     }
     __syncthreads();  // every warp's words are in shared memory, its traces written
     if (threadIdx.x == 0) s_nsp = 0;  // read by every thread in the previous step's afferent pass

@@ -52,14 +52,86 @@ constexpr int DEFAULT_STEPS_PER_LAUNCH = 1000;
 constexpr unsigned long long DEFAULT_WAIT_LIMIT_NS = 4000000000ull;  // 4 s
 constexpr int64_t DEFAULT_SPIKE_CAPACITY = 1 << 24;
 
-static __global__ void set_ctl_kernel(RunCtl* ctl, float start, int steps_total, int plastic,
-                                      int record_inputs) {
-  ctl->start_time = start;
-  ctl->step = 0;
-  ctl->steps_total = steps_total;
-  ctl->plastic = plastic;
-  ctl->record_inputs = record_inputs;
+// Starts a run in the run control: the run that ended is folded into the
+// state of the reference's active lists first (see RunCtl), and the new run
+// notes whether it begins by delivering the last group's spikes again
+// (redeliver_kernel, launched just before, does that delivery).
+__device__ void start_run(RunCtl* ctl, int G, float dt, float start, int steps_total, int plastic,
+                          int record_inputs) {
+  RunCtl c = *ctl;
+  fold_finished_run(c, G, dt);
+  const int carry = carry_decision(c, G, dt, start, steps_total);
+  if (steps_total > 0) c.repeat = carry != 0;
+  // a list holding two groups: the reference delivers both, this engine has
+  // kept only the last one
+  if (carry == 2 && c.status == 0) c.status = SPK_ERR_UNSUPPORTED;
+  c.start_time = start;
+  c.step = 0;
+  c.steps_total = steps_total;
+  c.plastic = plastic;
+  c.record_inputs = record_inputs;
+  ctl->start_time = c.start_time;
+  ctl->step = c.step;
+  ctl->steps_total = c.steps_total;
+  ctl->plastic = c.plastic;
+  ctl->record_inputs = c.record_inputs;
+  ctl->status = c.status;
+  ctl->repeat = c.repeat;
+  ctl->last_group_p1 = c.last_group_p1;
+  ctl->last_run_groups = c.last_run_groups;
+  ctl->last_run_repeat = c.last_run_repeat;
 }
+
+static __global__ void set_ctl_kernel(RunCtl* ctl, int G, float dt, float start, int steps_total, int plastic,
+                                      int record_inputs) {
+  start_run(ctl, G, dt, start, steps_total, plastic, record_inputs);
+}
+
+// The reference's active list (T/G) % 2 is emptied only by a group step of
+// the other parity (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:179-182).
+// When a run's first group index has the parity of the last group step's, the
+// list still holds that group's spikes, and activate_synapses delivers them
+// again, to the new group's slots: (T0 + g + delay) % B for the spike of
+// substep g, T0 = roundf(start/dt).  One thread per tile, reading the run
+// control as the run that ended left it (launched before start_run): the
+// substeps in order, their spiking keys ascending, each key's sub-row in order,
+// so every ring cell receives the additions in canonical order, before any of
+// the new run's.
+static __global__ void redeliver_kernel(const NetDev* __restrict__ dp, float start, int steps_total) {
+  const NetDev& d = *dp;
+  RunCtl c = *d.ctl;
+  fold_finished_run(c, d.G, d.dt);
+  if (carry_decision(c, d.G, d.dt, start, steps_total) != 1) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.n_tiles) return;
+  const int T0 = (int)roundf(start / d.dt);
+  const int slot_words = d.TS * d.L, B = d.B, L = d.L, n_tiles = d.n_tiles;
+  float* ring = d.ring + (size_t)t * B * slot_words;
+  unsigned long long ev = 0;
+  for (int g = 0; g < d.G; ++g) {
+    const uint32_t* bits = d.gbits + (size_t)g * d.n_words;
+    for (int w = 0; w < d.n_words; ++w) {
+      uint32_t m = bits[w];
+      while (m) {
+        const int key = w * 32 + __ffs(m) - 1;
+        m &= m - 1;
+        const int e0 = d.rowptr[(size_t)key * n_tiles + t], e1 = d.rowptr[(size_t)key * n_tiles + t + 1];
+        for (int e = e0; e < e1; ++e) {
+          const uint2 en = d.entries[e];
+          const int q = (int)(en.x & 0xffffu), dl = (int)((en.x >> 16) & 0xffu);
+          const int lb = (int)((en.x >> 24) & 0xfu), cl = (int)(en.x >> 28);
+          const float contrib = cl != 0 ? __uint_as_float(d.csc[en.y].y) * d.scale_tab[cl] : __uint_as_float(en.y);
+          const int sl = (T0 + g + dl) % B;
+          float& cell = ring[(size_t)sl * slot_words + q * L + lb];
+          cell = cell + contrib;
+        }
+        ev += (unsigned long long)(e1 - e0);
+      }
+    }
+  }
+  if (ev) atomicAdd(&d.ctl->events, ev);
+}
+
 
 static __global__ void clear_store_kernel(RunCtl* ctl) {
   ctl->spike_count = 0ull;
@@ -344,6 +416,10 @@ static int upload_state_defaults(spk_net* n) {
   // aborted step's exchange words behind: clear them
   SPK_CUDA(cudaMemsetAsync(n->abort_dev, 0, sizeof(int), n->stream));
   SPK_CUDA(cudaMemsetAsync(&h.ctl->status, 0, sizeof(int), n->stream));
+  // SpikingSynapses::reset_state empties both active lists (SpikingSynapses.cu:33)
+  SPK_CUDA(cudaMemsetAsync(&h.ctl->step, 0, sizeof(int), n->stream));
+  SPK_CUDA(cudaMemsetAsync(&h.ctl->repeat, 0, 4 * sizeof(int), n->stream));
+  SPK_CUDA(cudaMemsetAsync(h.gbits, 0, sizeof(uint32_t) * (size_t)n->G * h.n_words, n->stream));
   SPK_CUDA(cudaMemsetAsync(h.cta_stamp, 0, sizeof(unsigned long long) * 2 * (size_t)h.nctas, n->stream));
   SPK_CUDA(cudaMemsetAsync(h.cta_keys, 0, sizeof(unsigned long long) * 2 * (size_t)h.nctas * h.key_cap, n->stream));
   if (n->Nin > 0) {
@@ -354,6 +430,18 @@ static int upload_state_defaults(spk_net* n) {
     SPK_CUDA(cudaMemcpyAsync(&h.ctl->inputs_active, &zero, sizeof(int), cudaMemcpyHostToDevice, n->stream));
     SPK_CUDA(cudaStreamSynchronize(n->stream));
   }
+  return SPK_OK;
+}
+
+// Starts a run of the network on `stream`: the carried list's delivery, then
+// the run control.
+static int begin_run_on(spk_net* n, cudaStream_t stream, float start, int64_t steps, int plastic) {
+  if (steps > 0) {
+    redeliver_kernel<<<(n->hd.n_tiles + 127) / 128, 128, 0, stream>>>(n->dd, start, (int)steps);
+    SPK_CUDA(cudaGetLastError());
+  }
+  set_ctl_kernel<<<1, 1, 0, stream>>>(n->hd.ctl, n->G, n->dt, start, (int)steps, plastic, n->record_inputs ? 1 : 0);
+  SPK_CUDA(cudaGetLastError());
   return SPK_OK;
 }
 
@@ -412,9 +500,10 @@ static int run_steps_impl(spk_net* n, int64_t steps, int plastic, float start) {
     const int32_t pl = plastic ? 1 : 0;
     return spk_batch_run_steps_each(n->self_batch, &each, &pl);
   }
-  set_ctl_kernel<<<1, 1, 0, n->stream>>>(n->hd.ctl, start, (int)steps,
-                                         (plastic && n->has_stdp) ? 1 : 0, n->record_inputs ? 1 : 0);
-  SPK_CUDA(cudaGetLastError());
+  {
+    const int rc = begin_run_on(n, n->stream, start, steps, (plastic && n->has_stdp) ? 1 : 0);
+    if (rc) return rc;
+  }
   const int64_t blocks = (steps + n->plan.K - 1) / n->plan.K;
   for (int64_t b = 0; b < blocks; ++b) {
     if (n->withhold >= 0) {
@@ -622,7 +711,7 @@ static int new_net(const ModelSpec& m, int B, int64_t S, const spk_schedule* sch
 // records' delays, their traces and the spike-word history.
 static std::vector<size_t> arena_part_sizes(const Plan& plan, int N, int Nin, int L, int B, int stdp, int64_t S,
                                             int64_t n_csc, int n_stim, int64_t spike_cap, int dense = 0,
-                                            int norm = 0) {
+                                            int norm = 0, int G = 1) {
   const size_t n_cells = (size_t)plan.n_keys * plan.n_tiles;
   const size_t key_cap = (size_t)plan.W * (plan.TS + plan.ITS);
   return {sizeof(int32_t) * (n_cells + 1),
@@ -652,7 +741,8 @@ static std::vector<size_t> arena_part_sizes(const Plan& plan, int N, int Nin, in
           sizeof(float) * (dense ? 2 * (size_t)n_csc : 0),
           sizeof(uint32_t) * (dense ? (size_t)(B - 2) * plan.n_words : 0),
           sizeof(float) * (norm ? (size_t)n_csc : 0),
-          sizeof(float) * (norm ? (size_t)N : 0)};
+          sizeof(float) * (norm ? (size_t)N : 0),
+          sizeof(uint32_t) * (size_t)G * plan.n_words};
 }
 
 static size_t arena_total(const std::vector<size_t>& sizes) {
@@ -698,15 +788,15 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   const int key_cap = plan.W * (plan.TS + plan.ITS);
   void* p_ctl = nullptr; void* p_abort = nullptr; void* p_dd = nullptr; void* p_map = nullptr;
   void* p_rate = nullptr; void* p_cdelay = nullptr; void* p_dtr = nullptr; void* p_hist = nullptr;
-  void* p_nw0 = nullptr; void* p_nsum = nullptr;
+  void* p_nw0 = nullptr; void* p_nsum = nullptr; void* p_gbits = nullptr;
   const int dense = n->dense() ? 1 : 0;
   const int norm = n->weight_norm != SPK_NORM_OFF ? 1 : 0;
   const std::vector<size_t> sizes =
-      arena_part_sizes(plan, N, Nin, L, B, stdp, S, n_csc, n->n_stim, spike_cap, dense, norm);
+      arena_part_sizes(plan, N, Nin, L, B, stdp, S, n_csc, n->n_stim, spike_cap, dense, norm, n->G);
   void** dsts[] = {&p_rowptr, &p_entries, &p_cscptr, &p_csc,   &p_V,     &p_last,   &p_gtr,  &p_ring,
                    &p_innext, &p_rates,   &p_post,   &p_pre,   &p_pub,   &p_bA,     &p_bP,   &p_ckeys,
                    &p_cstamp, &p_spk,     &p_ctl,    &p_abort, &p_dd,    &p_map,  &p_rate,
-                   &p_cdelay, &p_dtr,     &p_hist,   &p_nw0,   &p_nsum};
+                   &p_cdelay, &p_dtr,     &p_hist,   &p_nw0,   &p_nsum,  &p_gbits};
   std::vector<Part> parts;
   for (size_t i = 0; i < sizes.size(); ++i) parts.push_back(Part{dsts[i], sizes[i]});
   const size_t total = arena_total(sizes);
@@ -794,9 +884,10 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   }
   h.seed = m.seed;
   h.rate_counts = (int*)p_rate;
+  h.gbits = (uint32_t*)p_gbits;
   h.stdp_rule = n->stdp_rule;
   if (dense) {
-    h.H = B - 2;  // D_max + 1
+    h.H = B - 2 * n->G;  // D_max + 1
     h.csc_delay = (const int*)p_cdelay;
     h.dense_tr = (float2*)p_dtr;
     h.hist = (uint32_t*)p_hist;
@@ -1447,10 +1538,11 @@ int spk_net_generate_estimate(const spk_gen_desc* d, const spk_schedule* sched, 
     return SPK_ERR_INVALID;
   return guarded([&]() -> int {
     double mu = 0.0, var = 0.0, mu_p = 0.0, var_p = 0.0;
-    int dmax = 1;
+    int dmax = 1, ghi = 1 << 30;
     for (int j = 0; j < d->n_projections; ++j) {
       const spk_projection& P = d->projections[j];
       const double n = (double)P.pre_count * (double)P.post_count, p = P.probability;
+      if (n * p > 0.0) ghi = std::min(ghi, P.delay_hi);  // the smallest drawn delay is at most this
       mu += n * p;
       var += n * p * (1.0 - p);
       if (P.plastic && d->has_stdp) {
@@ -1465,14 +1557,16 @@ int spk_net_generate_estimate(const spk_gen_desc* d, const spk_schedule* sched, 
     int rc = device_info(&di);
     if (rc) return rc;
     Plan plan;
-    const int B = dmax + 3;
+    // the deepest ring the drawn timestep grouping can need
+    const int G = ghi == (1 << 30) ? 1 : std::max(1, ghi);
+    const int B = dmax + 2 * G + 1;
     rc = make_plan(d->n_neurons, d->n_inputs, B, std::max(1, d->n_labels), d->synapse_kind, d->has_stdp ? 1 : 0,
                    sched, di, &plan);
     if (rc) return rc;
     const int64_t cap = d->spike_capacity == 0 ? DEFAULT_SPIKE_CAPACITY : std::max<int64_t>(0, d->spike_capacity);
     const size_t arena = arena_total(arena_part_sizes(plan, d->n_neurons, d->n_inputs, std::max(1, d->n_labels), B,
                                                       d->has_stdp ? 1 : 0, S, Pl, d->n_inputs ? d->n_stimuli : 0,
-                                                      cap));
+                                                      cap, 0, 0, G));
     // generation temporaries: cell counts, and for plastic synapses the sort
     // keys, values, entry keys (both buffers) and the sort's own storage
     const size_t cells = (size_t)plan.n_keys * plan.n_tiles + 1;
@@ -1518,6 +1612,7 @@ std::vector<SnapPart> snap_parts(spk_net* n) {
     p.push_back({h.dense_tr, sizeof(float2) * (size_t)n->n_csc});
     p.push_back({h.hist, sizeof(uint32_t) * (size_t)h.H * h.n_words});
   }
+  p.push_back({h.gbits, sizeof(uint32_t) * (size_t)n->G * h.n_words});  // the last group's spikes
   return p;
 }
 }  // namespace
@@ -1544,7 +1639,7 @@ int spk_net_snapshot(spk_net* n, void* buf, int64_t bytes) {
     SPK_CUDA(cudaStreamSynchronize(n->stream));
     SnapHeader hd{};
     hd.magic = SNAP_MAGIC;
-    hd.version = 1;
+    hd.version = 2;
     hd.N = n->N;
     hd.Nin = n->Nin;
     hd.L = n->L;
@@ -1582,7 +1677,7 @@ int spk_net_restore(spk_net* n, const void* buf, int64_t bytes) {
   }
   SnapHeader hd;
   std::memcpy(&hd, buf, sizeof(hd));
-  if (hd.magic != SNAP_MAGIC || hd.version != 1 || hd.N != n->N || hd.Nin != n->Nin || hd.L != n->L ||
+  if (hd.magic != SNAP_MAGIC || hd.version != 2 || hd.N != n->N || hd.Nin != n->Nin || hd.L != n->L ||
       hd.B != n->B || hd.n_tiles != n->hd.n_tiles || hd.TS != n->hd.TS || hd.ITS != n->hd.ITS ||
       hd.n_keys != n->hd.n_keys || hd.nctas != n->hd.nctas || hd.has_stdp != (n->has_stdp ? 1 : 0) ||
       hd.S != n->S || hd.n_csc != n->n_csc) {
@@ -1597,6 +1692,7 @@ int spk_net_restore(spk_net* n, const void* buf, int64_t bytes) {
       in += p.bytes;
     }
     RunCtl c = hd.ctl;
+    fold_finished_run(c, n->G, n->dt);  // the snapshot's last run, for the active-list state
     c.step = 0;
     c.steps_total = 0;
     c.spike_count = 0;  // the spike store is not part of a snapshot
@@ -1724,9 +1820,7 @@ int spk_net_begin_run(spk_net* n, int64_t n_steps, int32_t plasticity_on) {
   if (!n || n_steps < 0 || n_steps > 0x7fffffff) return SPK_ERR_INVALID;
   if (int rc = check_whole_groups(n, n_steps)) return rc;
   const float start = n->current_time;
-  set_ctl_kernel<<<1, 1, 0, n->stream>>>(n->hd.ctl, start, (int)n_steps, (plasticity_on && n->has_stdp) ? 1 : 0,
-                                         n->record_inputs ? 1 : 0);
-  SPK_CUDA(cudaGetLastError());
+  if (int rc = begin_run_on(n, n->stream, start, n_steps, (plasticity_on && n->has_stdp) ? 1 : 0)) return rc;
   n->current_time = start + (float)n_steps * n->dt;
   return SPK_OK;
 }
@@ -1748,6 +1842,9 @@ int spk_net_synchronize(spk_net* n) {
   if (rc) return rc;
   if (st == SPK_ERR_TIMEOUT) set_error("a device wait on another CTA timed out");
   if (st == SPK_ERR_OVERFLOW) set_error("the device spike store overflowed; spikes were dropped");
+  if (st == SPK_ERR_UNSUPPORTED)
+    set_error("a run began at the group index parity of a one-group run that itself began so: the reference "
+              "then delivers two earlier groups again, this engine keeps only the last");
   return st;
 }
 
@@ -2351,9 +2448,7 @@ int spk_batch_run_steps_each(spk_batch* b, const int64_t* n_steps, const int32_t
     spk_net* n = b->nets[i];
     SPK_CUDA(cudaStreamSynchronize(n->stream));
     const int plastic = (!plasticity_on || plasticity_on[i]) && n->has_stdp;
-    set_ctl_kernel<<<1, 1, 0, b->stream>>>(n->hd.ctl, n->current_time, (int)n_steps[i], plastic ? 1 : 0,
-                                           n->record_inputs ? 1 : 0);
-    SPK_CUDA(cudaGetLastError());
+    if (int rc = begin_run_on(n, b->stream, n->current_time, n_steps[i], plastic ? 1 : 0)) return rc;
   }
   // networks that finish early leave their launches at once (no steps left)
   const int64_t blocks = (most + b->K - 1) / b->K;
@@ -2926,14 +3021,14 @@ static int noalloc_device(NoallocDevice** out) {
   return SPK_OK;
 }
 
-// Writes the network descriptor and CTA map into the scratch, clears the
-// exchange stamps and keys and the abort flag, and starts the run in the
-// caller's run state.  The stamps and keys must start at zero: a word left by an
-// earlier call of another network (or of this one after its step counter was
-// reset) can carry a stamp this call also produces.
+// Writes the network descriptor and CTA map into the scratch and clears the
+// exchange stamps and keys and the abort flag.  The stamps and keys must
+// start at zero: a word left by an earlier call of another network (or of
+// this one after its step counter was reset) can carry a stamp this call also
+// produces.  The run is then started in the caller's run state
+// (redeliver_kernel, set_ctl_kernel).
 static __global__ void noalloc_setup_kernel(NetDev nd, NetDev* nd_out, CtaMap* map, unsigned long long* xchg,
-                                            size_t xchg_words, float start, int steps_total, int plastic,
-                                            int record_inputs) {
+                                            size_t xchg_words) {
   const size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = i0; i < xchg_words; i += stride) xchg[i] = 0ull;
@@ -2941,12 +3036,6 @@ static __global__ void noalloc_setup_kernel(NetDev nd, NetDev* nd_out, CtaMap* m
   if (i0 == 0) {
     *nd_out = nd;
     *nd.abort_flag = 0;
-    RunCtl* c = nd.ctl;
-    c->start_time = start;
-    c->step = 0;
-    c->steps_total = steps_total;
-    c->plastic = plastic;
-    c->record_inputs = record_inputs;
   }
 }
 
@@ -3064,6 +3153,10 @@ static int step_noalloc_impl(const spk_device_net* a, int64_t n_steps, int plast
     return SPK_ERR_INVALID;
   }
 
+  if (!a->group_bits) {
+    set_error("group_bits missing (the last group's spike words, timestep_grouping * n_keys / 32 words)");
+    return SPK_ERR_INVALID;
+  }
   NoallocDevice* dev = nullptr;
   int rc = noalloc_device(&dev);
   if (rc) return rc;
@@ -3163,13 +3256,18 @@ static int step_noalloc_impl(const spk_device_net* a, int64_t n_steps, int plast
   h.spikes = (uint2*)a->spikes;
   h.spike_cap = a->spike_capacity;
   h.ctl = (RunCtl*)a->run_state;
+  h.gbits = a->group_bits;
   h.abort_flag = (int*)(s + o_abort);
   h.poll_ns = DEFAULT_WAIT_LIMIT_NS;
 
   const int grid = (int)std::min<size_t>((xchg_words + 255) / 256, (size_t)dev->di.sms * 4);
-  noalloc_setup_kernel<<<std::max(grid, 1), 256, 0, stream>>>(
-      h, (NetDev*)(s + o_nd), (CtaMap*)(s + o_map), h.cta_stamp, xchg_words, start, (int)n_steps,
-      (plasticity_on && stdp) ? 1 : 0, a->record_inputs ? 1 : 0);
+  noalloc_setup_kernel<<<std::max(grid, 1), 256, 0, stream>>>(h, (NetDev*)(s + o_nd), (CtaMap*)(s + o_map),
+                                                               h.cta_stamp, xchg_words);
+  SPK_CUDA(cudaGetLastError());
+  redeliver_kernel<<<(h.n_tiles + 127) / 128, 128, 0, stream>>>((const NetDev*)(s + o_nd), start, (int)n_steps);
+  SPK_CUDA(cudaGetLastError());
+  set_ctl_kernel<<<1, 1, 0, stream>>>(h.ctl, G, a->dt, start, (int)n_steps, (plasticity_on && stdp) ? 1 : 0,
+                                      a->record_inputs ? 1 : 0);
   SPK_CUDA(cudaGetLastError());
   const int K = DEFAULT_STEPS_PER_LAUNCH;
   const int64_t blocks = (n_steps + K - 1) / K;

@@ -52,11 +52,13 @@ class GroupedReference:
     kernels are structured: per step, lif_update_membrane_potentials loops
     over the neurons and, inside, over the G substeps
     (Spike/Backend/CUDA/Neurons/LIFSpikingNeurons.cu:105-193, voltage
-    injection), then activate_synapses delivers the step's spikes to
-    (bufferloc + delay + g) % B (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:168-202),
-    B = D_max + 2G + 1 (:48).  Float32 throughout, no contraction; the ring
-    additions in the canonical order (substep, then presynaptic key, then
-    sorted synapse order)."""
+    injection), appending each spike (neuron, substep) to active list
+    (T/G) % 2 (get_active_synapses, Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:151-162);
+    then activate_synapses empties the other list and delivers the whole
+    current one to (bufferloc + delay + g) % B (:168-202), B = D_max + 2G + 1
+    (:48).  Float32 throughout, no contraction; the ring additions in the
+    canonical order (list order: earlier entries first; a step's spikes by
+    substep, then presynaptic key; sorted synapse order)."""
 
     def __init__(self, d, o: OracleNet):
         a = desc_arrays(d)
@@ -82,6 +84,8 @@ class GroupedReference:
         self.last = np.full(self.n, F(-1000.0), F)
         self.time = F(0.0)
         self.ids, self.times = [], []
+        self.lists = [[], []]  # the two active lists: (neuron, substep) entries
+        self.repeats = 0       # group steps that delivered a carried group
 
     def run(self, seconds: float):
         G, dt, half = self.G, self.dt, F(F(0.5) * self.dt)
@@ -91,6 +95,8 @@ class GroupedReference:
             t = F(start + F(s * G) * dt)
             tidx = int(math.floor(float(F(t / dt)) + 0.5))  # (int)roundf(t/dt), t >= 0
             fired = [[] for _ in range(G)]
+            cur = self.lists[(tidx // G) % 2]
+            self.repeats += bool(cur)
             for idx in range(self.n):
                 Vi = self.V[idx]
                 for g in range(G):
@@ -110,25 +116,31 @@ class GroupedReference:
                 for idx in fired[g]:
                     self.ids.append(idx)
                     self.times.append(F(t + F(g) * dt))
-                    for syn in range(self.start[idx], self.start[idx + 1]):
-                        cell = ((tidx + self.delay[syn] + g) % self.B, self.post[syn])
-                        self.ring[cell] = F(self.ring[cell] + self.c[syn])
+                    cur.append((idx, g))
+            self.lists[(tidx // G + 1) % 2] = []
+            for idx, g in cur:
+                for syn in range(self.start[idx], self.start[idx + 1]):
+                    cell = ((tidx + self.delay[syn] + g) % self.B, self.post[syn])
+                    self.ring[cell] = F(self.ring[cell] + self.c[syn])
         self.time = F(start + F(seconds))
 
 
-@pytest.mark.parametrize("G,d_max", [(2, 2), (3, 7)])
+@pytest.mark.parametrize("G,d_max", [(1, 4), (2, 2), (3, 7)])
 def test_oracle_follows_the_reference_group_loop(G, d_max):
     """The oracle (substep by substep) against the reference's grouped loop,
     bit for bit: spike ids and float times, potentials and the end time, over
-    runs whose step counts are not whole groups (rounded down)."""
+    runs whose step counts are not whole groups (rounded down) and whose
+    first group index repeats or skips one, so that the earlier group is
+    delivered again."""
     d = _tiny_net(G, d_max)
     o = OracleNet(d.desc)
     assert o.timestep_grouping() == G
     ref = GroupedReference(d.desc, o)
-    for sec in (0.0137, 0.0071, 0.02):
+    for sec in (0.0137, 0.0071, 0.0173, 0.0101, 0.0337, 0.0173, 0.02):
         o.run(sec)
         ref.run(sec)
         assert o.current_time() == ref.time
+    assert ref.repeats >= 1
     ids, times = o.spikes()
     assert len(ids) == len(ref.ids) > 200
     np.testing.assert_array_equal(ids, np.asarray(ref.ids))
@@ -268,3 +280,60 @@ def test_batch_of_grouped_networks_equals_each_alone(mode):
         assert_same(net, o, x.desc.n_neurons, x.desc.n_inputs, 1, tag=f"batch mode {mode}")
     with pytest.raises(RuntimeError):
         b.run_steps_each([330, 331, 330, 330])
+
+
+# ---- GPU: run boundaries where the reference delivers the last group again --------------
+# (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:179-182: active list (T/G) % 2 is emptied
+# only by a group step of the other parity.)  The run lengths below make the first group
+# index of some runs repeat (0.0173 s is 174 steps at dt 1e-4, the next run starts at
+# index 173) or skip one (grouped networks).
+BOUNDARY_RUNS = (0.0137, 0.0071, 0.0173, 0.0101, 0.0337, 0.0173, 0.02)
+STDP = STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02, lambda_=1.0, alpha=1.0,
+                  w_max=1.0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("sched", [None, (2, 32, 6, 50), (1, 512, 0, 0)])
+@pytest.mark.parametrize("G", [1, 3])
+def test_run_boundaries_deliver_the_carried_group_again(sched, G):
+    """The engine delivers the carried group again exactly as the oracle does:
+    persistent schedules (one and several CTAs, launches of 50 timesteps) and
+    bulk mode over post ranges (one warp per CTA, 512-post tiles)."""
+    from spike_gb300 import Net, schedule
+    d = descs.random_voltage_net(n=600, n_in=200, d_min=G, d_max=12, seed=20 + G)
+    o = OracleNet(d.desc)
+    net = Net.from_desc(d.desc, schedule(*sched) if sched else None)
+    for sec in BOUNDARY_RUNS:
+        net.run(sec)
+        o.run(sec)
+    assert net.synchronize() == 0
+    assert_same(net, o, 600, 200, 1, tag=f"G={G} {net.schedule()}")
+
+
+@pytest.mark.gpu
+def test_plastic_run_boundaries_and_snapshot():
+    """Weight-dependent STDP (the carried group is delivered with the current
+    weights), and a snapshot taken between runs keeps the active-list state:
+    the restored network repeats the next group start as the original does."""
+    from spike_gb300 import Net
+    d = descs.random_voltage_net(n=300, n_in=200, plastic=True, stdp=STDP, seed=31)
+    o = OracleNet(d.desc)
+    a = Net.from_desc(d.desc)
+    for sec in (0.0173, 0.0101, 0.0173):
+        a.run(sec)
+        o.run(sec)
+    assert a.synchronize() == 0
+    snap = a.snapshot()
+    b = Net.from_desc(d.desc)
+    b.run(0.005)  # state that the restore must overwrite
+    b.restore(snap)
+    a.clear_spikes()
+    b.clear_spikes()
+    o.clear_spikes()
+    for sec in (0.0173, 0.0337, 0.0173):
+        a.run(sec)
+        b.run(sec)
+        o.run(sec)
+    assert a.synchronize() == 0 and b.synchronize() == 0
+    assert_same(a, o, 300, 200, 1, weights=True, tag="plastic")
+    assert_same(b, o, 300, 200, 1, weights=True, tag="restored")

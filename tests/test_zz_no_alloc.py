@@ -108,6 +108,7 @@ class CallerNet:
             innext=torch.full((max(Nin, 1),), -1000.0, device=dev), rates=dbuf(rates, np.float32),
             post_tr=torch.zeros(Nn, device=dev), pre_tr=torch.zeros(n_keys, device=dev),
             spikes=torch.zeros(2 * spike_capacity, dtype=torch.int32, device=dev),
+            group_bits=torch.zeros(G * n_keys // 32, dtype=torch.int32, device=dev),
             run_state=torch.zeros(N.SPK_RUN_STATE_BYTES // 4, dtype=torch.int32, device=dev),
         )
         t = self.t
@@ -129,6 +130,8 @@ class CallerNet:
         dn.spikes, dn.spike_capacity = t["spikes"].data_ptr(), spike_capacity
         dn.run_state = t["run_state"].data_ptr()
         dn.timestep_grouping = G
+        dn.group_bits = t["group_bits"].data_ptr()
+        self.G = G
         self.dn = dn
         self.dt = np.float32(d.dt)
         self.time = np.float32(0.0)
@@ -140,6 +143,14 @@ class CallerNet:
                                          C.c_void_p(stream)), "spk_step_noalloc")
         # the time bookkeeping of spk_net_run_steps: start + (float)steps * dt
         self.time = np.float32(self.time + np.float32(np.float32(n_steps) * self.dt))
+
+    def run_seconds(self, seconds: float, plastic: bool):
+        """spk_net_run's steps and time bookkeeping: ceil(seconds/dt) rounded
+        down to whole groups, then start + seconds."""
+        start = self.time
+        steps = int(np.ceil(np.float32(seconds) / self.dt)) // self.G * self.G
+        self.step(steps, plastic)
+        self.time = np.float32(start + np.float32(seconds))
 
     def compare(self, ref: Net, n_synapses: int, tag: str):
         torch.cuda.synchronize()
@@ -255,4 +266,28 @@ def test_noalloc_spike_store_overflow_sets_status():
         assert int(rs[8:10].view(np.uint64)[0]) == 50
         assert int(rs[10:12].view(np.uint64)[0]) == ref.events()
         assert_close(cn.t["V"].cpu().numpy(), ref.state(N.SPK_FIELD_V, 300), f"call {i + 1} V")
+    ref.close()
+
+
+def test_noalloc_matches_run_steps_grouped():
+    """A network whose minimum delay is 3 steps (timestep grouping 3), with
+    Poisson inputs, on three CTAs."""
+    d = descs.random_voltage_net(n=300, n_in=200, d_min=3, d_max=10, seed=7)
+    spikes = run_both(d.desc, 4, 32, 3, [(300, False), (201, False)])
+    assert spikes > 200
+
+
+@pytest.mark.parametrize("d_min", [1, 3])
+def test_noalloc_run_boundaries_deliver_the_carried_group_again(d_min):
+    """Runs of seconds whose first group index repeats (d_min 1: 0.0173 s is
+    174 steps, the next run starts at index 173) or skips one (d_min 3): the
+    carried group is delivered again through group_bits, as spk_net_run does."""
+    d = descs.random_voltage_net(n=300, n_in=200, d_min=d_min, d_max=10, seed=8)
+    ref = Net.from_desc(d.desc, schedule(4, 32, 3, 0))
+    cn = CallerNet(d.desc, 4, 32, 3, ref)
+    for i, sec in enumerate((0.0173, 0.0173, 0.0337, 0.0101, 0.05)):
+        ref.run(sec)
+        assert ref.synchronize() == 0
+        cn.run_seconds(sec, False)
+        cn.compare(ref, d.desc.n_synapses, f"run {i + 1} d_min={d_min}")
     ref.close()
