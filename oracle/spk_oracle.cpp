@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <iterator>
 #include <new>
 #include <thread>
 #include <vector>
@@ -108,8 +109,10 @@ struct Net {
   bool last_run_repeat = false;   // that run began by delivering its predecessor's group again
 
   // ---- per-step scratch -----------------------------------------------------
-  std::vector<uint8_t> spiked;  // per key, this step
-  std::vector<int64_t> active;  // keys, ascending
+  std::vector<uint8_t> spiked;    // per key, this step
+  std::vector<int64_t> active;    // keys delivered this step, ascending
+  std::vector<int64_t> rec_keys;  // keys that spiked this step, ascending
+  std::vector<int64_t> carried;   // a plastic network's carried keys, delivered in its run's first step
 
   // ---- threading: post-range ownership --------------------------------------
   int threads = 1;
@@ -758,11 +761,20 @@ int Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
     // group's spikes: they are delivered again to this group's slots, first.
     const int64_t first = round_to_int(start / dt_f) / G;
     const bool repeat = last_group >= 0 && ((first ^ last_group) & 1) == 0;
+    carried.clear();
     if (repeat) {
       // a run of one group that itself began this way left two groups in the list
       if (last_run_groups == 1 && last_run_repeat) return SPK_ERR_UNSUPPORTED;
-      const int T0 = round_to_int(start / dt_f);
-      for (int g = 0; g < G; ++g) deliver_keys(group_keys[g], T0 + g);
+      if (has_stdp) {
+        // With a plasticity rule (G = 1) the carried keys are delivered in the
+        // first step, after its weight updates (plasticity state_update runs
+        // before activate_synapses, Spike/Models/SpikingModel.cpp:202-207),
+        // merged into the step's list in key order.
+        carried = group_keys[0];
+      } else {
+        const int T0 = round_to_int(start / dt_f);
+        for (int g = 0; g < G; ++g) deliver_keys(group_keys[g], T0 + g);
+      }
     }
     last_run_repeat = repeat;
     last_run_groups = n_steps / G;
@@ -793,6 +805,13 @@ int Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
     for (int kk = 0; kk < K; ++kk)
       if (spiked[kk]) active.push_back(kk);
     group_keys[(size_t)(s % G)] = active;
+    rec_keys = active;
+    if (s == 0 && !carried.empty()) {
+      // the carried keys join the first step's list (a key in both is listed once)
+      std::vector<int64_t> merged;
+      std::set_union(active.begin(), active.end(), carried.begin(), carried.end(), std::back_inserter(merged));
+      active.swap(merged);  // counted with the step's keys below
+    }
     // this step's spike bits, for the rules that look delays back
     std::copy(spiked.begin(), spiked.end(), hist.begin() + (size_t)(T % H) * K);
     for (int64_t kk : active) events += (uint64_t)eff_count[kk];
@@ -801,7 +820,7 @@ int Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
   auto record = [&](R t) {
     // SpikingActivityMonitor: (id, current_time + g*timestep), here in key order.
     const float tf = (float)t;
-    for (int64_t kk : active) {
+    for (int64_t kk : rec_keys) {
       if (kk >= Nin) {
         rec_ids[SPK_POP_NEURONS].push_back((int32_t)(kk - Nin));
         rec_times[SPK_POP_NEURONS].push_back(tf);

@@ -72,6 +72,9 @@ struct BulkStep {
   float t, tg;
   int T, slot, g;  // g: substep of the group
   bool live, stdp_run, inputs_active;
+  // the first step of a plastic network's run that repeats the last group's
+  // index: the carried keys are delivered again in this step's propagation
+  bool rep;
   bool dense_run;  // a per-synapse-trace rule updates this step
 };
 
@@ -87,6 +90,7 @@ __device__ __forceinline__ BulkStep bulk_step(const NetDev& d, const RunCtl& c, 
   b.stdp_run = d.has_stdp && c.plastic && d.stdp_rule == SPK_STDP_WEIGHT_DEPENDENT;
   b.dense_run = d.has_stdp && c.plastic && d.stdp_rule != SPK_STDP_WEIGHT_DEPENDENT;
   b.inputs_active = c.inputs_active != 0 || s > 0;
+  b.rep = d.has_stdp && c.repeat && sr == 0;
   return b;
 }
 
@@ -98,6 +102,7 @@ __device__ __forceinline__ RunCtl load_ctl(const RunCtl* p) {
   c.plastic = p->plastic;
   c.inputs_active = p->inputs_active;
   c.record_inputs = p->record_inputs;
+  c.repeat = p->repeat;
   return c;
 }
 
@@ -238,28 +243,36 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
       if (u >= bw.count) break;
       const int key = (bw.word + u) * 32 + lane;
       const int n = key - KL;
-      bool spk = false;
+      bool spk = false, ev = false;
       if (n < N) {
         float* cell = cellp[u];
         spk = bulk_lif(d, st, n, key, Vv[u], lv[u], cell, inv[u]);
         if (kind == SPK_SYN_VOLTAGE)
           for (int l = 0; l < L; ++l) cell[l] = 0.0f;
         if (st.stdp_run) {
+          // post_spike_g = roundf((last - t)/dt) >= 0
+          // (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:115-121):
+          // this step's spike, or the last step's at a run start that repeats
+          // its timestep index
+          ev = (int)roundf(((spk ? st.tg : lv[u]) - st.t) / d.dt) >= 0;
           float po = pov[u] * d.E_m;
-          po = po + (spk ? d.inc_m : 0.0f);
+          po = po + (ev ? d.inc_m : 0.0f);
           d.post_trace[n] = po;
           float pr = prv[u] * d.E_p;
-          pr = pr + (spk ? d.inc_p : 0.0f);
+          pr = pr + (ev ? d.inc_p : 0.0f);
           d.pre_trace[key] = pr;
           pub[key] = pr;
         }
       }
       const unsigned word = __ballot_sync(FULL, spk);
+      const unsigned evword = __ballot_sync(FULL, ev);
       if (lane == 0) {
-        d.bitsA[bw.word + u] = word;
-        d.bitsP[bw.word + u] = st.stdp_run ? word : 0u;
+        // delivered keys: the spikes, and at a repeating run start the carried keys
+        uint32_t* gb = d.gbits + (size_t)st.g * d.n_words + bw.word + u;
+        d.bitsA[bw.word + u] = word | (st.rep ? *gb : 0u);
+        d.bitsP[bw.word + u] = evword;
         if (d.hist) d.hist[(size_t)(st.T % d.H) * d.n_words + bw.word + u] = word;
-        d.gbits[(size_t)st.g * d.n_words + bw.word + u] = word;
+        *gb = word;
       }
     }
   } else {
@@ -306,10 +319,11 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
       const unsigned wa = __ballot_sync(FULL, spk);
       const unsigned wp = __ballot_sync(FULL, pev);
       if (lane == 0) {
-        d.bitsA[bw.word + u] = wa;
+        uint32_t* gb = d.gbits + (size_t)st.g * d.n_words + bw.word + u;
+        d.bitsA[bw.word + u] = wa | (st.rep ? *gb : 0u);
         d.bitsP[bw.word + u] = wp;
         if (d.hist) d.hist[(size_t)(st.T % d.H) * d.n_words + bw.word + u] = wa;
-        d.gbits[(size_t)st.g * d.n_words + bw.word + u] = wa;
+        *gb = wa;
       }
     }
   }
@@ -353,12 +367,14 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
   const bool recording = d.spike_cap > 0;  // a network created without a spike store records nothing
   const int per = (n_words + BULK_LIST_THREADS - 1) / BULK_LIST_THREADS;
   const int w0 = min(n_words, threadIdx.x * per), w1 = min(n_words, w0 + per);
-  // counts: list keys (low 32 bits) and recorded spikes (high 32 bits)
+  // counts: list keys (low 32 bits) and recorded spikes (high 32 bits); the
+  // step's spikes are its group words (bitsA also holds carried keys)
+  const uint32_t* spw = d.gbits + (size_t)st.g * n_words;
   unsigned long long cnt = 0;
   for (int i = w0; i < w1; ++i) {
     const uint32_t a = d.bitsA[i], p = d.bitsP[i];
     const bool rec = recording && ((i << 5) >= KL || rec_inputs);
-    cnt += (unsigned long long)__popc(a | p) + (rec ? ((unsigned long long)__popc(a) << 32) : 0ull);
+    cnt += (unsigned long long)__popc(a | p) + (rec ? ((unsigned long long)__popc(spw[i]) << 32) : 0ull);
   }
   unsigned long long incl = cnt;
 #pragma unroll
@@ -385,7 +401,7 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
   const unsigned long long sc0 = d.ctl->spike_count;
   unsigned long long sp = sc0 + (excl >> 32);
   for (int i = w0; i < w1; ++i) {
-    const uint32_t a = d.bitsA[i], p = d.bitsP[i];
+    const uint32_t a = d.bitsA[i], p = d.bitsP[i], sw = spw[i];
     const bool rec = recording && ((i << 5) >= KL || rec_inputs);
     uint32_t m = a | p;
     while (m) {
@@ -394,7 +410,7 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
       const uint32_t key = (uint32_t)(i << 5) + (uint32_t)b;
       const uint32_t fa = (a >> b) & 1u, fp = (p >> b) & 1u;
       d.step_list[pos++] = key | (fa << 31) | (fp << 30);
-      if (fa && rec) {
+      if (((sw >> b) & 1u) && rec) {
         if (sp < (unsigned long long)d.spike_cap)
           d.spikes[sp] = make_uint2(key, __float_as_uint(st.tg));
         else
@@ -410,11 +426,12 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
     d.ctl->spike_count = sc > (unsigned long long)d.spike_cap ? (unsigned long long)d.spike_cap : sc;
   }
   if (!st.stdp_run) return;
-  // afferent-pass items: one per spiking post, reserved in the shared item
-  // list with one atomic per network
+  // afferent-pass items: one per post with an STDP event (its spike, or at a
+  // repeating run start the last step's), reserved in the shared item list
+  // with one atomic per network
   const int wl0 = max(w0, KL >> 5);
   int nsp = 0;
-  for (int i = wl0; i < w1; ++i) nsp += __popc(d.bitsA[i]);
+  for (int i = wl0; i < w1; ++i) nsp += __popc(d.bitsP[i]);
   int ic = nsp;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -438,7 +455,7 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
   __syncthreads();
   int ipos = s_item_base + (int)warp_tot[w] + ic - nsp;
   for (int i = wl0; i < w1; ++i) {
-    uint32_t a = d.bitsA[i];
+    uint32_t a = d.bitsP[i];
     while (a) {
       const int b = __ffs(a) - 1;
       a &= a - 1;
@@ -622,7 +639,7 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
       else
         ptr_s[i] = 0.0f;
     }
-    for (int i = lane; i < TS / 32; i += 32) spw_s[i] = d.bitsA[((KL + p0) >> 5) + i];
+    for (int i = lane; i < TS / 32; i += 32) spw_s[i] = d.bitsP[((KL + p0) >> 5) + i];  // post events
   }
   stage_list(0);
   cp_async_wait_all();
@@ -971,7 +988,8 @@ __global__ void __launch_bounds__(256, 4) bulk_dense_stdp_kernel(const NetDev* _
     }
     if (!st.live || !st.dense_run) continue;
     const int key = d.KL + item.post;
-    const bool post_sp = ((d.bitsA[key >> 5] >> (key & 31)) & 1u) != 0;
+    // the post's spike bit of this step (bitsA also holds carried keys)
+    const bool post_sp = ((d.gbits[(size_t)st.g * d.n_words + (key >> 5)] >> (key & 31)) & 1u) != 0;
     const int a0 = item.a0, a1 = item.a1;
     const float dt = d.dt;
     const int H = d.H, n_words = d.n_words;

@@ -195,6 +195,8 @@ __global__ void __launch_bounds__(512, 1)
   float* post_s = (float*)(wreg + wl.post_tr);
   float* pre_s = (float*)(wreg + wl.pre_tr);
   uint32_t* spkw_s = wreg + wl.spkw;
+  uint32_t* evw_s = wreg + wl.evw;
+  uint32_t* fw_s = wreg + wl.fw;
   uint32_t* inw_s = wreg + wl.inw;
   uint32_t* inwp_s = wreg + wl.inwp;
   float* innext_s = (float*)(wreg + wl.in_next);
@@ -270,6 +272,10 @@ __global__ void __launch_bounds__(512, 1)
     int T;
     group_time(ctl0.start_time, sr, d.G, dt, t, T, tg);
     const int g_sub = sr % d.G;  // substep of the group
+    // the first step of a run that repeats the last group's index: a plastic
+    // network delivers that group's spikes again in this step's propagation
+    // (after the step's STDP updates, as activate_synapses follows the rules)
+    const bool rep = d.has_stdp && ctl0.repeat && sr == 0;
     const long long gs = ctl0.gstep + s;
     const int par = (int)(gs & 1);
     const unsigned stamp = (unsigned)(gs + 1);
@@ -286,7 +292,7 @@ __global__ void __launch_bounds__(512, 1)
       for (int base = 0; base < TS; base += 32) {
         const int li = base + lane;
         const int n = p0 + li;
-        bool spk = false;
+        bool spk = false, ev = false;
         if (n < N) {
           GroupConst G = G0;
           if (g_last != g_first) {
@@ -336,17 +342,26 @@ __global__ void __launch_bounds__(512, 1)
           }
           V_s[li] = Vi;
           if (stdp_run) {
+            // post_spike_g = roundf((last - t)/dt) >= 0
+            // (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:115-121):
+            // this step's spike, or the last step's at a run start that
+            // repeats its timestep index
+            ev = (int)roundf((last_s[li] - t) / dt) >= 0;
             float po = post_s[li] * d.E_m;
-            po = po + (spk ? d.inc_m : 0.0f);
+            po = po + (ev ? d.inc_m : 0.0f);
             post_s[li] = po;
             float pr = pre_s[li] * d.E_p;
-            pr = pr + (spk ? d.inc_p : 0.0f);
+            pr = pr + (ev ? d.inc_p : 0.0f);
             pre_s[li] = pr;
             pub[KL + n] = pr;
           }
         }
         const unsigned word = __ballot_sync(FULL, spk);
-        if (lane == 0) spkw_s[base >> 5] = word;
+        const unsigned evword = __ballot_sync(FULL, ev);
+        if (lane == 0) {
+          spkw_s[base >> 5] = word;
+          evw_s[base >> 5] = evword;
+        }
       }
     }
     // ---- phase A: Poisson inputs of the tile ----------------------------------
@@ -392,7 +407,7 @@ __global__ void __launch_bounds__(512, 1)
     {
       const int nl = TS >> 5, ni = ITS >> 5;
       for (int i = 0; i < nl + ni; ++i) {
-        const uint32_t m = i < nl ? spkw_s[i] : (inw_s[i - nl] | (stdp_run ? inwp_s[i - nl] : 0u));
+        const uint32_t m = i < nl ? (spkw_s[i] | evw_s[i]) : (inw_s[i - nl] | (stdp_run ? inwp_s[i - nl] : 0u));
         if (!((m >> lane) & 1u)) continue;
         const int li = i < nl ? 32 * i + lane : TS + 32 * (i - nl) + lane;
         const int key = i < nl ? KL + p0 + li : kin0 + (li - TS);
@@ -404,50 +419,63 @@ __global__ void __launch_bounds__(512, 1)
 
     // ---- publish: the CTA's active keys, then one stamp word per CTA ---------
     __syncwarp();
+    {
+      // This substep's spike words, kept for a later run that repeats the
+      // group's index; at such a repeat (rep) the last group's words are the
+      // carried keys delivered again in this step.
+      uint32_t* gb = d.gbits + (size_t)g_sub * n_words;
+      const int nl = TS >> 5, ni = ITS >> 5;
+      for (int i = lane; i < nl + ni; i += 32) {
+        const int wi = i < nl ? ((KL + p0) >> 5) + i : (kin0 >> 5) + (i - nl);
+        fw_s[i] = rep ? gb[wi] : 0u;
+        gb[wi] = i < nl ? spkw_s[i] : inw_s[i - nl];
+      }
+    }
+    __syncwarp();
     if (stdp_run) {
-      // bitmaps for the post-spike pass, which looks up arbitrary pre keys
+      // bitmaps for the post-spike pass, which looks up arbitrary pre keys:
+      // delivered keys (A) and STDP events (P)
       const int nl = TS >> 5, ni = ITS >> 5;
       for (int i = lane; i < nl + ni; i += 32) {
         if (i < nl) {
           const int wi = ((KL + p0) >> 5) + i;
-          bitsA[wi] = spkw_s[i];
-          bitsP[wi] = spkw_s[i];
+          bitsA[wi] = spkw_s[i] | fw_s[i];
+          bitsP[wi] = evw_s[i];
         } else {
           const int wi = (kin0 >> 5) + (i - nl);
-          bitsA[wi] = inw_s[i - nl];
+          bitsA[wi] = inw_s[i - nl] | fw_s[i];
           bitsP[wi] = inwp_s[i - nl];
         }
       }
     }
-    {
-      // this substep's spike words: the list a later run may deliver again
-      uint32_t* gb = d.gbits + (size_t)g_sub * n_words;
-      const int nl = TS >> 5, ni = ITS >> 5;
-      for (int i = lane; i < nl + ni; i += 32)
-        gb[i < nl ? ((KL + p0) >> 5) + i : (kin0 >> 5) + (i - nl)] = i < nl ? spkw_s[i] : inw_s[i - nl];
-    }
     __syncthreads();  // every warp's words are in shared memory, its traces written
     if (threadIdx.x == 0) s_nsp = 0;  // read by every thread in the previous step's afferent pass
     // The CTA's ballot words in key order: inputs of warps 0..W-1, then neurons
-    // of warps 0..W-1 (x-th word: bits a = spikes, p = pre events, first key).
+    // of warps 0..W-1 (x-th word: bits a = delivered keys, p = STDP pre
+    // events, sp = spikes of the step, first key).  a is sp but at the first
+    // step of a plastic network's run that repeats the last group's index,
+    // where the carried keys are delivered again.
     const int nw_in = W * (ITS >> 5), nw_all = W * ((ITS >> 5) + (TS >> 5));
-    auto cta_word = [&](const int x, uint32_t& a, uint32_t& p, uint32_t& wkey) {
+    auto cta_word = [&](const int x, uint32_t& a, uint32_t& p, uint32_t& sp, uint32_t& wkey) {
       const int ni = ITS >> 5, nl = TS >> 5;
       a = 0u;
       p = 0u;
+      sp = 0u;
       wkey = 0u;
       if (x < nw_in) {
         const int wx = x / ni, k = x - (x / ni) * ni;
         const uint32_t* r = sm + SHARED_WORDS + wx * wl.total;
-        a = r[wl.inw + k];
+        sp = r[wl.inw + k];
+        a = sp | r[wl.fw + nl + k];
         p = stdp_run ? r[wl.inwp + k] : 0u;
         wkey = (uint32_t)((cm.rank * W + wx) * ITS + k * 32);
       } else if (x < nw_all) {
         const int y = x - nw_in;
         const int wx = y / nl, k = y - (y / nl) * nl;
         const uint32_t* r = sm + SHARED_WORDS + wx * wl.total;
-        a = r[wl.spkw + k];
-        p = stdp_run ? a : 0u;
+        sp = r[wl.spkw + k];
+        a = sp | r[wl.fw + k];
+        p = r[wl.evw + k];
         wkey = (uint32_t)(KL + (cm.rank * W + wx) * TS + k * 32);
       }
     };
@@ -456,8 +484,8 @@ __global__ void __launch_bounds__(512, 1)
       int pos = 0, n_in = 0;
       for (int x0 = 0; x0 < nw_all; x0 += 32) {
         const int x = x0 + lane;
-        uint32_t a, p, wkey;
-        cta_word(x, a, p, wkey);
+        uint32_t a, p, sp, wkey;
+        cta_word(x, a, p, sp, wkey);
         uint32_t m = a | p;
         const int c = __popc(m);
         int incl = c;
@@ -470,7 +498,8 @@ __global__ void __launch_bounds__(512, 1)
         while (m) {
           const int b = __ffs(m) - 1;
           m &= m - 1;
-          st_relaxed_u64(keys_out + o++, stamp_hi | (wkey + b) | (((a >> b) & 1u) << 31) | (((p >> b) & 1u) << 30));
+          st_relaxed_u64(keys_out + o++, stamp_hi | (wkey + b) | (((a >> b) & 1u) << 31) | (((p >> b) & 1u) << 30) |
+                                             (((sp >> b) & 1u) << 29));
         }
         n_in += __reduce_add_sync(FULL, x < nw_in ? c : 0);
         pos += __shfl_sync(FULL, incl, 31);
@@ -501,8 +530,8 @@ __global__ void __launch_bounds__(512, 1)
               uint32_t key = 0u;
               if (j < n_round) {
                 const uint32_t lv = list[j];
-                key = lv & 0x3fffffffu;
-                rec = (lv >> 31) && ((int)key >= KL || ctl0.record_inputs);
+                key = lv & 0x1fffffffu;
+                rec = ((lv >> 29) & 1u) && ((int)key >= KL || ctl0.record_inputs);
               }
               const unsigned m = __ballot_sync(FULL, rec);
               if (rec) {
@@ -522,7 +551,7 @@ __global__ void __launch_bounds__(512, 1)
           // (cp.async: every load of the round in flight at once)
           for (int i = lane; i < nk; i += 32) {
             const uint32_t lv = list[kb + i];
-            const int* rp = d.rowptr + (size_t)(lv & 0x3fffffffu) * n_tiles + t_idx;
+            const int* rp = d.rowptr + (size_t)(lv & 0x1fffffffu) * n_tiles + t_idx;
             cp_async4(kst + i, rp);
             cp_async4(koff + i, rp + 1);
             kfl[i] = lv;
@@ -534,7 +563,7 @@ __global__ void __launch_bounds__(512, 1)
 #pragma unroll
             for (int u = 0; u < KPL; ++u) {
               const int i = u * 32 + lane;
-              prs[u] = i < nk ? __ldcg(pub + (list[kb + i] & 0x3fffffffu)) : 0.0f;
+              prs[u] = i < nk ? __ldcg(pub + (list[kb + i] & 0x1fffffffu)) : 0.0f;
             }
 #pragma unroll
             for (int u = 0; u < KPL; ++u) {
@@ -618,7 +647,7 @@ __global__ void __launch_bounds__(512, 1)
                 if (c != 0) {
                   float v = stage_w[f];
                   if (stdp_run) {
-                    const bool post_ev = ((spkw_s[q >> 5] >> (q & 31)) & 1u) != 0;
+                    const bool post_ev = ((evw_s[q >> 5] >> (q & 31)) & 1u) != 0;
                     if (P || post_ev) {
                       v = stdp_update(d, v, P, post_ev, post_s[q], kpre[j]);
                       d.csc[en.y].y = __float_as_uint(v);
@@ -666,8 +695,8 @@ __global__ void __launch_bounds__(512, 1)
       // warps' ballot words in shared memory, with no global exchange.
       int list_n = 0;
       for (int x0 = 0; x0 < nw_all; x0 += 32) {
-        uint32_t a, p, wkey;
-        cta_word(x0 + lane, a, p, wkey);
+        uint32_t a, p, sp, wkey;
+        cta_word(x0 + lane, a, p, sp, wkey);
         uint32_t m = a | p;
         const int c = __popc(m);
         int incl = c;
@@ -693,7 +722,7 @@ __global__ void __launch_bounds__(512, 1)
         while (m) {
           const int b = __ffs(m) - 1;
           m &= m - 1;
-          list[o++] = (wkey + b) | (((a >> b) & 1u) << 31) | (((p >> b) & 1u) << 30);
+          list[o++] = (wkey + b) | (((a >> b) & 1u) << 31) | (((p >> b) & 1u) << 30) | (((sp >> b) & 1u) << 29);
         }
         list_n += tot;
       }
@@ -881,7 +910,7 @@ __global__ void __launch_bounds__(512, 1)
       };
       __syncthreads();
       for (int wi = 0; wi < TS / 32; ++wi) {
-        const uint32_t word = spkw_s[wi];
+        const uint32_t word = evw_s[wi];  // postsynaptic STDP events
         if (!word) continue;
         const int c = __popc(word);
         int base = 0;

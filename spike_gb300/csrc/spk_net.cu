@@ -99,6 +99,9 @@ static __global__ void set_ctl_kernel(RunCtl* ctl, int G, float dt, float start,
 // the new run's.
 static __global__ void redeliver_kernel(const NetDev* __restrict__ dp, float start, int steps_total) {
   const NetDev& d = *dp;
+  // a network with a plasticity rule delivers them in its first step instead,
+  // after that step's weight updates (the step kernels' `rep`)
+  if (d.has_stdp) return;
   RunCtl c = *d.ctl;
   fold_finished_run(c, d.G, d.dt);
   if (carry_decision(c, d.G, d.dt, start, steps_total) != 1) return;
@@ -212,7 +215,8 @@ static int make_plan(int N, int Nin, int B, int L, int kind, int stdp, const spk
     p->smem = plan_bytes(B, TS, L, p->ITS, kind, stdp, W);
     // per-CTA key counts travel in 16-bit fields of the stamp word
     p->persistent = p->smem <= di.max_smem && nctas <= MAX_CTAS_PER_NET && W * TS <= 65535 && W * p->ITS <= 65535;
-    const bool covers = (int64_t)p->n_tiles * TS >= N && (int64_t)p->n_keys < (1ll << 30);
+    // keys travel in 29 bits (list words carry three flags)
+    const bool covers = (int64_t)p->n_tiles * TS >= N && (int64_t)p->n_keys < (1ll << 29);
     return covers && (p->persistent || (allow_bulk && TS >= RANGE_MIN_TS));
   };
   const int K = (s && s->steps_per_launch > 0) ? s->steps_per_launch : DEFAULT_STEPS_PER_LAUNCH;

@@ -293,7 +293,7 @@ STDP = STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02, 
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("sched", [None, (2, 32, 6, 50), (1, 512, 0, 0)])
+@pytest.mark.parametrize("sched", [None, (2, 32, 10, 50), (1, 512, 0, 0)])
 @pytest.mark.parametrize("G", [1, 3])
 def test_run_boundaries_deliver_the_carried_group_again(sched, G):
     """The engine delivers the carried group again exactly as the oracle does:
