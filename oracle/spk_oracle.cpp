@@ -98,11 +98,13 @@ struct Net {
   // The reference's two active-neuron lists (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:156-202)
   // are double-buffered by the parity of the group index T/G: a group step
   // appends its spikes to list (T/G) % 2, delivers that whole list, and empties
-  // the other one.  Consecutive group steps whose indices have equal parity (a
-  // run that starts at the group index where the last one ended, or two past
-  // it) therefore deliver the earlier group's spikes again, to the later
-  // group's slots.  Within a run the index advances by one per group, so this
-  // happens only where a run starts; the state below carries it across runs.
+  // the other one.  Consecutive group steps whose indices have equal parity
+  // therefore deliver the earlier group's spikes again, to the later group's
+  // slots: substep g's carried keys with substep g's own, after its STDP
+  // updates, merged in key order (a key both carried and spiking once).  The
+  // index comes from the float time, so this happens where a run starts at
+  // the index where the last one ended (or two past it) and, where t/dt
+  // falls near a half, within a run.  The state below carries it across runs.
   std::vector<std::vector<int64_t>> group_keys;  // [G]: active keys of each substep of the last group
   int64_t last_group = -1;        // index T/G of the last group step; -1: none since reset
   int64_t last_run_groups = 0;    // groups of the run that ended with it
@@ -112,7 +114,8 @@ struct Net {
   std::vector<uint8_t> spiked;    // per key, this step
   std::vector<int64_t> active;    // keys delivered this step, ascending
   std::vector<int64_t> rec_keys;  // keys that spiked this step, ascending
-  std::vector<int64_t> carried;   // a plastic network's carried keys, delivered in its run's first step
+  bool first_repeat = false;      // the run's first group repeats the last group step's parity
+  int status = SPK_OK;            // SPK_ERR_UNSUPPORTED: a carried list of two groups
 
   // ---- threading: post-range ownership --------------------------------------
   int threads = 1;
@@ -129,7 +132,6 @@ struct Net {
   void reset_inputs();
   void set_threads(int t);
   int run_steps(int64_t n_steps, float start, bool plastic);
-  void deliver_keys(const std::vector<int64_t>& keys, int T);
   void lif_range(int a, int b, R t, int T);
   void poisson_range(int a, int b, R t, int T);
   void stdp_range(int64_t a, int64_t b, R t);
@@ -406,25 +408,12 @@ void Net<R>::reset_state() {
   std::fill(hist.begin(), hist.end(), (uint8_t)0);
   // SpikingSynapses::reset_state empties both active lists (SpikingSynapses.cu:33)
   group_keys.assign(G, {});
+  status = SPK_OK;
   last_group = -1;
   last_run_groups = 0;
   last_run_repeat = false;
 }
 
-// activate_synapses (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:168-202)
-// for the listed keys' efferent synapses, delivered to (T + delay) % B, one
-// after another in list order and sorted synapse order.
-template <typename R>
-void Net<R>::deliver_keys(const std::vector<int64_t>& keys, int T) {
-  const size_t row = (size_t)N * L;
-  for (int64_t key : keys) {
-    for (int64_t s = eff_start[key]; s < eff_start[key] + eff_count[key]; ++s) {
-      const int targetloc = (T + sdelay[s]) % B;
-      ring[(size_t)targetloc * row + (size_t)spost[s] * L + slabel[s]] += sw[s] * sscale[s];
-    }
-    events += (uint64_t)eff_count[key];
-  }
-}
 
 template <typename R>
 void Net<R>::set_threads(int t) {
@@ -761,21 +750,9 @@ int Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
     // group's spikes: they are delivered again to this group's slots, first.
     const int64_t first = round_to_int(start / dt_f) / G;
     const bool repeat = last_group >= 0 && ((first ^ last_group) & 1) == 0;
-    carried.clear();
-    if (repeat) {
-      // a run of one group that itself began this way left two groups in the list
-      if (last_run_groups == 1 && last_run_repeat) return SPK_ERR_UNSUPPORTED;
-      if (has_stdp) {
-        // With a plasticity rule (G = 1) the carried keys are delivered in the
-        // first step, after its weight updates (plasticity state_update runs
-        // before activate_synapses, Spike/Models/SpikingModel.cpp:202-207),
-        // merged into the step's list in key order.
-        carried = group_keys[0];
-      } else {
-        const int T0 = round_to_int(start / dt_f);
-        for (int g = 0; g < G; ++g) deliver_keys(group_keys[g], T0 + g);
-      }
-    }
+    // a run of one group that itself began this way left two groups in the list
+    if (repeat && last_run_groups == 1 && last_run_repeat) status = SPK_ERR_UNSUPPORTED;
+    first_repeat = repeat;
     last_run_repeat = repeat;
     last_run_groups = n_steps / G;
     // the run's last group: timestep n_steps - G
@@ -799,18 +776,32 @@ int Net<R>::run_steps(int64_t n_steps, float start, bool plastic) {
     T = round_to_int(tf / dt_f) + (int)g;
     t = (sizeof(R) == 4) ? (R)(tf + (float)g * dt_f) : ((R)start + (R)(grp * G) * dt) + (R)g * dt;
   };
+  // whether the group of step s has the parity of the group step before it
+  auto group_repeats = [&](int64_t s) {
+    if (s < G) return first_repeat;
+    const int64_t g0 = s - s % G;
+    const int k = round_to_int((start + (float)(g0)*dt_f) / dt_f) / G;
+    const int kp = round_to_int((start + (float)(g0 - G) * dt_f) / dt_f) / G;
+    return ((k ^ kp) & 1) == 0;
+  };
   auto finish_step = [&](R t, int T, int64_t s) {
     active.clear();
     const int K = nkeys();
     for (int kk = 0; kk < K; ++kk)
       if (spiked[kk]) active.push_back(kk);
-    group_keys[(size_t)(s % G)] = active;
     rec_keys = active;
-    if (s == 0 && !carried.empty()) {
-      // the carried keys join the first step's list (a key in both is listed once)
+    std::vector<int64_t>& carried = group_keys[(size_t)(s % G)];
+    const bool rep = group_repeats(s);
+    // a carried list of two earlier groups is beyond the engine this checks
+    if (rep && s % G == 0 && s >= G && group_repeats(s - G)) status = SPK_ERR_UNSUPPORTED;
+    if (rep && !carried.empty()) {
+      // the carried keys join the substep's list (a key in both is listed once)
       std::vector<int64_t> merged;
       std::set_union(active.begin(), active.end(), carried.begin(), carried.end(), std::back_inserter(merged));
+      carried = rec_keys;
       active.swap(merged);  // counted with the step's keys below
+    } else {
+      carried = rec_keys;
     }
     // this step's spike bits, for the rules that look delays back
     std::copy(spiked.begin(), spiked.end(), hist.begin() + (size_t)(T % H) * K);
@@ -993,7 +984,7 @@ int oracle_run(oracle_net* n, float seconds, int plasticity_on) {
     const int rc = net.run_steps(steps, start, plasticity_on != 0);
     if (rc) return rc;
     net.current_time = start + seconds;
-    return SPK_OK;
+    return net.status;
   });
 }
 
@@ -1005,7 +996,7 @@ int oracle_run_steps(oracle_net* n, int64_t n_steps, int plasticity_on) {
     const int rc = net.run_steps(n_steps, start, plasticity_on != 0);
     if (rc) return rc;
     net.current_time = start + (float)n_steps * net.dt_f;
-    return SPK_OK;
+    return net.status;
   });
 }
 

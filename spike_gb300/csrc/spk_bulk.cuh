@@ -70,10 +70,10 @@ constexpr int BULK_STAGE_ENTRIES = SPK_BULK_STAGE_ENTRIES;  // entries staged pe
 // Timestep s of the current block of a network's run.
 struct BulkStep {
   float t, tg;
-  int T, slot, g;  // g: substep of the group
+  int T, slot, g, sr;  // g: substep of the group; sr: timestep of the run
   bool live, stdp_run, inputs_active;
-  // the first step of a plastic network's run that repeats the last group's
-  // index: the carried keys are delivered again in this step's propagation
+  // the group has the parity of the group step before it: its substeps
+  // deliver that group's spikes again (group_repeats)
   bool rep;
   bool dense_run;  // a per-synapse-trace rule updates this step
 };
@@ -90,7 +90,8 @@ __device__ __forceinline__ BulkStep bulk_step(const NetDev& d, const RunCtl& c, 
   b.stdp_run = d.has_stdp && c.plastic && d.stdp_rule == SPK_STDP_WEIGHT_DEPENDENT;
   b.dense_run = d.has_stdp && c.plastic && d.stdp_rule != SPK_STDP_WEIGHT_DEPENDENT;
   b.inputs_active = c.inputs_active != 0 || s > 0;
-  b.rep = d.has_stdp && c.repeat && sr == 0;
+  b.sr = sr;
+  b.rep = group_repeats(c, sr, d.G, dt);
   return b;
 }
 
@@ -364,6 +365,9 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int n_words = d.n_words, KL = d.KL;
   const bool rec_inputs = c.record_inputs != 0;
+  // a carried list of two earlier groups is beyond this engine
+  if (threadIdx.x == 0 && st.rep && st.g == 0 && st.sr >= d.G && group_repeats(c, st.sr - d.G, d.G, d.dt))
+    atomicCAS(&d.ctl->status, 0, SPK_ERR_UNSUPPORTED);
   const bool recording = d.spike_cap > 0;  // a network created without a spike store records nothing
   const int per = (n_words + BULK_LIST_THREADS - 1) / BULK_LIST_THREADS;
   const int w0 = min(n_words, threadIdx.x * per), w1 = min(n_words, w0 + per);

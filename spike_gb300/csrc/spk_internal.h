@@ -68,9 +68,10 @@ struct RunCtl {
   // by the parity of the group index T/G: a group step appends its spikes to
   // list (T/G) % 2, delivers that whole list and empties the other one, so
   // consecutive group steps with indices of equal parity deliver the earlier
-  // group's spikes again.  Within a run the index advances by one per group;
-  // where a run starts, it can repeat or skip one.  State of the lists:
-  int repeat;           // the current run began by delivering the last group's spikes again
+  // group's spikes again.  The index comes from the float time (roundf(t/dt)),
+  // so it can repeat or skip one where a run starts and, when t/dt falls near
+  // a half, within a run.  State of the lists across runs:
+  int repeat;           // the current run's first group repeats the last group step's parity
   int last_group_p1;    // 1 + index of the last group step before the current run; 0: none
   int last_run_groups;  // groups of the run that ended with it
   int last_run_repeat;  // that run began by delivering a carried group again
@@ -102,6 +103,15 @@ SPK_HD int carry_decision(const RunCtl& c, int G, float dt, float start, int ste
   const int first = (int)roundf(start / dt) / G;
   if (((first ^ (c.last_group_p1 - 1)) & 1) != 0) return 0;
   return (c.last_run_groups == 1 && c.last_run_repeat) ? 2 : 1;
+}
+
+// Whether the group of timestep sr of the run in c has the parity of the
+// group step before it, so that its substeps deliver the earlier group's
+// spikes again: the run's first group as decided where the run started, the
+// others from the time of the two groups.
+SPK_HD bool group_repeats(const RunCtl& c, int sr, int G, float dt) {
+  if (sr < G) return c.repeat != 0;
+  return ((group_index(c.start_time, sr, G, dt) ^ group_index(c.start_time, sr - G, G, dt)) & 1) == 0;
 }
 
 // Everything one CTA needs to run its share of one network.

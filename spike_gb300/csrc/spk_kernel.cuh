@@ -272,10 +272,14 @@ __global__ void __launch_bounds__(512, 1)
     int T;
     group_time(ctl0.start_time, sr, d.G, dt, t, T, tg);
     const int g_sub = sr % d.G;  // substep of the group
-    // the first step of a run that repeats the last group's index: a plastic
-    // network delivers that group's spikes again in this step's propagation
-    // (after the step's STDP updates, as activate_synapses follows the rules)
-    const bool rep = d.has_stdp && ctl0.repeat && sr == 0;
+    // A group with the parity of the group step before it delivers that
+    // group's spikes again (carried keys), in each substep's propagation after
+    // its STDP updates, as activate_synapses follows the rules.  A carried
+    // list of two earlier groups is beyond this engine: status.
+    const bool rep = group_repeats(ctl0, sr, d.G, dt);
+    if (rep && sr >= d.G && g_sub == 0 && group_repeats(ctl0, sr - d.G, d.G, dt) && threadIdx.x == 0 &&
+        cm.rank == 0)
+      atomicCAS(&d.ctl->status, 0, SPK_ERR_UNSUPPORTED);
     const long long gs = ctl0.gstep + s;
     const int par = (int)(gs & 1);
     const unsigned stamp = (unsigned)(gs + 1);
@@ -456,17 +460,19 @@ __global__ void __launch_bounds__(512, 1)
     // step of a plastic network's run that repeats the last group's index,
     // where the carried keys are delivered again.
     const int nw_in = W * (ITS >> 5), nw_all = W * ((ITS >> 5) + (TS >> 5));
+    // A key both carried and spiking is listed (and delivered) once.
     auto cta_word = [&](const int x, uint32_t& a, uint32_t& p, uint32_t& sp, uint32_t& wkey) {
       const int ni = ITS >> 5, nl = TS >> 5;
       a = 0u;
       p = 0u;
       sp = 0u;
       wkey = 0u;
+      uint32_t f = 0u;
       if (x < nw_in) {
         const int wx = x / ni, k = x - (x / ni) * ni;
         const uint32_t* r = sm + SHARED_WORDS + wx * wl.total;
         sp = r[wl.inw + k];
-        a = sp | r[wl.fw + nl + k];
+        f = r[wl.fw + nl + k];
         p = stdp_run ? r[wl.inwp + k] : 0u;
         wkey = (uint32_t)((cm.rank * W + wx) * ITS + k * 32);
       } else if (x < nw_all) {
@@ -474,10 +480,11 @@ __global__ void __launch_bounds__(512, 1)
         const int wx = y / nl, k = y - (y / nl) * nl;
         const uint32_t* r = sm + SHARED_WORDS + wx * wl.total;
         sp = r[wl.spkw + k];
-        a = sp | r[wl.fw + k];
+        f = r[wl.fw + k];
         p = r[wl.evw + k];
         wkey = (uint32_t)(KL + (cm.rank * W + wx) * TS + k * 32);
       }
+      a = sp | f;
     };
     if (w == 0 && d.nctas > 1) {
       unsigned long long* keys_out = d.cta_keys + ((size_t)par * d.nctas + cm.rank) * d.key_cap;

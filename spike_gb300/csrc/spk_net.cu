@@ -54,8 +54,8 @@ constexpr int64_t DEFAULT_SPIKE_CAPACITY = 1 << 24;
 
 // Starts a run in the run control: the run that ended is folded into the
 // state of the reference's active lists first (see RunCtl), and the new run
-// notes whether it begins by delivering the last group's spikes again
-// (redeliver_kernel, launched just before, does that delivery).
+// notes whether its first group delivers the last group's spikes again (the
+// step kernels do, group_repeats).
 __device__ void start_run(RunCtl* ctl, int G, float dt, float start, int steps_total, int plastic,
                           int record_inputs) {
   RunCtl c = *ctl;
@@ -86,55 +86,6 @@ static __global__ void set_ctl_kernel(RunCtl* ctl, int G, float dt, float start,
                                       int record_inputs) {
   start_run(ctl, G, dt, start, steps_total, plastic, record_inputs);
 }
-
-// The reference's active list (T/G) % 2 is emptied only by a group step of
-// the other parity (Spike/Backend/CUDA/Synapses/SpikingSynapses.cu:179-182).
-// When a run's first group index has the parity of the last group step's, the
-// list still holds that group's spikes, and activate_synapses delivers them
-// again, to the new group's slots: (T0 + g + delay) % B for the spike of
-// substep g, T0 = roundf(start/dt).  One thread per tile, reading the run
-// control as the run that ended left it (launched before start_run): the
-// substeps in order, their spiking keys ascending, each key's sub-row in order,
-// so every ring cell receives the additions in canonical order, before any of
-// the new run's.
-static __global__ void redeliver_kernel(const NetDev* __restrict__ dp, float start, int steps_total) {
-  const NetDev& d = *dp;
-  // a network with a plasticity rule delivers them in its first step instead,
-  // after that step's weight updates (the step kernels' `rep`)
-  if (d.has_stdp) return;
-  RunCtl c = *d.ctl;
-  fold_finished_run(c, d.G, d.dt);
-  if (carry_decision(c, d.G, d.dt, start, steps_total) != 1) return;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= d.n_tiles) return;
-  const int T0 = (int)roundf(start / d.dt);
-  const int slot_words = d.TS * d.L, B = d.B, L = d.L, n_tiles = d.n_tiles;
-  float* ring = d.ring + (size_t)t * B * slot_words;
-  unsigned long long ev = 0;
-  for (int g = 0; g < d.G; ++g) {
-    const uint32_t* bits = d.gbits + (size_t)g * d.n_words;
-    for (int w = 0; w < d.n_words; ++w) {
-      uint32_t m = bits[w];
-      while (m) {
-        const int key = w * 32 + __ffs(m) - 1;
-        m &= m - 1;
-        const int e0 = d.rowptr[(size_t)key * n_tiles + t], e1 = d.rowptr[(size_t)key * n_tiles + t + 1];
-        for (int e = e0; e < e1; ++e) {
-          const uint2 en = d.entries[e];
-          const int q = (int)(en.x & 0xffffu), dl = (int)((en.x >> 16) & 0xffu);
-          const int lb = (int)((en.x >> 24) & 0xfu), cl = (int)(en.x >> 28);
-          const float contrib = cl != 0 ? __uint_as_float(d.csc[en.y].y) * d.scale_tab[cl] : __uint_as_float(en.y);
-          const int sl = (T0 + g + dl) % B;
-          float& cell = ring[(size_t)sl * slot_words + q * L + lb];
-          cell = cell + contrib;
-        }
-        ev += (unsigned long long)(e1 - e0);
-      }
-    }
-  }
-  if (ev) atomicAdd(&d.ctl->events, ev);
-}
-
 
 static __global__ void clear_store_kernel(RunCtl* ctl) {
   ctl->spike_count = 0ull;
@@ -437,13 +388,8 @@ static int upload_state_defaults(spk_net* n) {
   return SPK_OK;
 }
 
-// Starts a run of the network on `stream`: the carried list's delivery, then
-// the run control.
+// Starts a run of the network on `stream` (start_run in its run control).
 static int begin_run_on(spk_net* n, cudaStream_t stream, float start, int64_t steps, int plastic) {
-  if (steps > 0) {
-    redeliver_kernel<<<(n->hd.n_tiles + 127) / 128, 128, 0, stream>>>(n->dd, start, (int)steps);
-    SPK_CUDA(cudaGetLastError());
-  }
   set_ctl_kernel<<<1, 1, 0, stream>>>(n->hd.ctl, n->G, n->dt, start, (int)steps, plastic, n->record_inputs ? 1 : 0);
   SPK_CUDA(cudaGetLastError());
   return SPK_OK;
@@ -3030,7 +2976,7 @@ static int noalloc_device(NoallocDevice** out) {
 // start at zero: a word left by an earlier call of another network (or of
 // this one after its step counter was reset) can carry a stamp this call also
 // produces.  The run is then started in the caller's run state
-// (redeliver_kernel, set_ctl_kernel).
+// (set_ctl_kernel).
 static __global__ void noalloc_setup_kernel(NetDev nd, NetDev* nd_out, CtaMap* map, unsigned long long* xchg,
                                             size_t xchg_words) {
   const size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -3267,8 +3213,6 @@ static int step_noalloc_impl(const spk_device_net* a, int64_t n_steps, int plast
   const int grid = (int)std::min<size_t>((xchg_words + 255) / 256, (size_t)dev->di.sms * 4);
   noalloc_setup_kernel<<<std::max(grid, 1), 256, 0, stream>>>(h, (NetDev*)(s + o_nd), (CtaMap*)(s + o_map),
                                                                h.cta_stamp, xchg_words);
-  SPK_CUDA(cudaGetLastError());
-  redeliver_kernel<<<(h.n_tiles + 127) / 128, 128, 0, stream>>>((const NetDev*)(s + o_nd), start, (int)n_steps);
   SPK_CUDA(cudaGetLastError());
   set_ctl_kernel<<<1, 1, 0, stream>>>(h.ctl, G, a->dt, start, (int)n_steps, (plasticity_on && stdp) ? 1 : 0,
                                       a->record_inputs ? 1 : 0);

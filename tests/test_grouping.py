@@ -57,8 +57,9 @@ class GroupedReference:
     then activate_synapses empties the other list and delivers the whole
     current one to (bufferloc + delay + g) % B (:168-202), B = D_max + 2G + 1
     (:48).  Float32 throughout, no contraction; the ring additions in the
-    canonical order (list order: earlier entries first; a step's spikes by
-    substep, then presynaptic key; sorted synapse order)."""
+    canonical order of the engine and the oracle (by substep, then
+    presynaptic key, carried entries merged with the group's own, a key in
+    both once; sorted synapse order)."""
 
     def __init__(self, d, o: OracleNet):
         a = desc_arrays(d)
@@ -118,10 +119,11 @@ class GroupedReference:
                     self.times.append(F(t + F(g) * dt))
                     cur.append((idx, g))
             self.lists[(tidx // G + 1) % 2] = []
-            for idx, g in cur:
-                for syn in range(self.start[idx], self.start[idx + 1]):
-                    cell = ((tidx + self.delay[syn] + g) % self.B, self.post[syn])
-                    self.ring[cell] = F(self.ring[cell] + self.c[syn])
+            for g in range(G):  # canonical order: by substep, then key; an entry listed twice once
+                for idx in sorted({i for i, gg in cur if gg == g}):
+                    for syn in range(self.start[idx], self.start[idx + 1]):
+                        cell = ((tidx + self.delay[syn] + g) % self.B, self.post[syn])
+                        self.ring[cell] = F(self.ring[cell] + self.c[syn])
         self.time = F(start + F(seconds))
 
 
@@ -337,3 +339,154 @@ def test_plastic_run_boundaries_and_snapshot():
     assert a.synchronize() == 0 and b.synchronize() == 0
     assert_same(a, o, 300, 200, 1, weights=True, tag="plastic")
     assert_same(b, o, 300, 200, 1, weights=True, tag="restored")
+
+
+def _expf():
+    libm = ctypes.CDLL("libm.so.6")
+    f = libm.expf
+    f.argtypes, f.restype = [ctypes.c_float], ctypes.c_float
+    return lambda x: F(f(float(x)))
+
+
+class PlasticReference:
+    """SpikingModel::run of a voltage-synapse network with weight-dependent
+    STDP on its excitatory synapses, G = 1, written as the reference's step is:
+    lif_update_membrane_potentials (spikes appended to active list T % 2), then
+    ltp_and_ltd for every plastic synapse with its own traces and expf terms
+    (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:85-161),
+    then activate_synapses (the other list emptied, the current one delivered
+    with the weights just updated).  A run that starts at the timestep index
+    where the last one ended finds the last step's spikes still in its list,
+    and their last-spike times give them STDP events again.  The list is
+    delivered in key order (carried keys merged with the step's), the
+    canonical order of the engine and the oracle."""
+
+    def __init__(self, d, o: OracleNet, sp):
+        self.base = GroupedReference(d, o)
+        a = desc_arrays(d)
+        order = np.argsort(a["pre"], kind="stable")
+        self.pl = a["plastic"][order].astype(bool)
+        self.w = a["weight"][order].astype(F)
+        self.scale = a["scale"][order].astype(F)
+        self.pre_tr = np.zeros(len(order), F)
+        self.post_tr = np.zeros(len(order), F)
+        self.pre = np.sort(a["pre"], kind="stable")
+        self.sp = sp
+        self.expf = _expf()
+        self.order = order
+
+    def stdp(self, t):
+        b, sp, expf, dt = self.base, self.sp, self.expf, self.base.dt
+        am, ap, tm, tp = F(sp.a_minus), F(sp.a_plus), F(sp.tau_minus), F(sp.tau_plus)
+        lam, alpha, wmax = F(sp.lambda_), F(sp.alpha), F(sp.w_max)
+        for s in np.flatnonzero(self.pl):
+            pre_g = int(math.floor(float(F(F(b.last[self.pre[s]] - t) / dt)) + 0.5))
+            post_g = int(math.floor(float(F(F(b.last[b.post[s]] - t) / dt)) + 0.5))
+            if pre_g >= 1:
+                pre_g *= -1
+            pot, prt = self.post_tr[s], self.pre_tr[s]
+            pot = F(pot * expf(F(-F(F(1) * dt)) / tm))
+            prt = F(prt * expf(F(-F(F(1) * dt)) / tp))
+            pot = F(pot + (F(am * expf(F(-F(F(1 - post_g) * dt)) / tm)) if post_g >= 0 else F(0)))
+            prt = F(prt + (F(ap * expf(F(-F(F(1 - pre_g) * dt)) / tp)) if pre_g >= 0 else F(0)))
+            old = self.w[s]
+            syn = F(0)
+            if pre_g >= 0:
+                tpt = pot
+                if post_g > pre_g:
+                    tpt = F(tpt + F(-am * expf(F(-F(F(1 - post_g) * dt)) / tm)))
+                tpt = F(tpt * F(F(1) / expf(F(F(F(-(1 - pre_g)) * dt) / tm))))
+                syn = F(syn - F(F(F(lam * alpha) * old) * tpt))
+            if post_g >= 0:
+                tpr = prt
+                if pre_g > post_g:
+                    tpr = F(tpr + F(-ap * expf(F(-F(F(1 - pre_g) * dt)) / tp)))
+                tpr = F(tpr * F(F(1) / expf(F(F(F(-(1 - post_g)) * dt) / tp))))
+                syn = F(syn + F(F(lam * F(wmax - old)) * tpr))
+            nw = F(old + syn)
+            self.w[s] = F(0) if nw < 0 else nw
+            self.post_tr[s], self.pre_tr[s] = pot, prt
+
+    def run(self, seconds: float):
+        b = self.base
+        dt, half = b.dt, F(F(0.5) * b.dt)
+        start = b.time
+        for s in range(int(np.ceil(F(seconds) / dt))):
+            t = F(start + F(s) * dt)
+            T = int(math.floor(float(F(t / dt)) + 0.5))
+            cur = b.lists[T % 2]
+            b.repeats += bool(cur)
+            for idx in range(b.n):
+                cell = (T % b.B, idx)
+                inp = F(F(0.0) + b.ring[cell])
+                b.ring[cell] = F(0.0)
+                if F(F(t - b.last[idx]) - b.tref) > half:
+                    k = b.k[idx]
+                    Vi = F(F(F(F(k * b.v0[idx]) + F(F(F(1.0) - k) * b.V[idx])) + F(k * b.ibg)) + inp)
+                    if Vi >= b.th[idx]:
+                        b.last[idx] = t
+                        Vi = b.vr[idx]
+                        cur.append(idx)
+                        b.ids.append(idx)
+                        b.times.append(t)
+                    b.V[idx] = Vi
+            self.stdp(t)
+            b.lists[(T + 1) % 2] = []
+            for idx in sorted(set(cur)):
+                for syn in range(b.start[idx], b.start[idx + 1]):
+                    cell = ((T + b.delay[syn]) % b.B, b.post[syn])
+                    b.ring[cell] = F(b.ring[cell] + F(self.w[syn] * self.scale[syn]))
+        b.time = F(start + F(seconds))
+
+    def weights(self):
+        out = np.empty(len(self.order), F)
+        out[self.order] = self.w
+        return out
+
+
+def test_oracle_stdp_at_repeating_run_starts_follows_the_reference():
+    """Weight-dependent STDP across run starts that repeat the timestep index
+    (0.00233 s is 24 steps at dt 1e-4, and start + 0.00233 often rounds to the
+    last step's index): the oracle against the reference's step written out
+    above, bit for bit (spikes, potentials, every weight)."""
+    d0 = _tiny_net(1, 4, seed=13)
+    a = desc_arrays(d0.desc)
+    sp = STDPParams(a_plus=0.05, a_minus=0.0525, tau_plus=0.02, tau_minus=0.02, lambda_=1.0, alpha=1.0, w_max=0.01)
+    groups = [dict(count=32, tau_m=0.005, R=1e8, v0=0.0, vreset=0.0, theta=0.02, v_init_lo=0.0, v_init_hi=0.02),
+              dict(count=8, tau_m=0.004, R=1e8, v0=0.0, vreset=0.005, theta=0.02, v_init_lo=0.0, v_init_hi=0.02)]
+    d = descs.Desc(kind=N.SPK_SYN_VOLTAGE, groups=groups, refractory=0.002, i_bg=0.03, n_inputs=0,
+                   pre=a["pre"], post=a["post"], weight=a["weight"], scale=np.ones(len(a["pre"])),
+                   delay=a["delay"], plastic=(a["pre"] < 32).astype(int), stdp=sp, record_inputs=False)
+    o = OracleNet(d.desc)
+    ref = PlasticReference(d.desc, o, sp)
+    for sec in [0.0173] + [0.00233] * 24:  # 24 steps each, many starting at the last index
+        o.run(sec)
+        ref.run(sec)
+        assert o.current_time() == ref.base.time
+    assert ref.base.repeats >= 3
+    ids, times = o.spikes()
+    np.testing.assert_array_equal(ids, np.asarray(ref.base.ids))
+    np.testing.assert_array_equal(bits(times), bits(np.asarray(ref.base.times, F)))
+    np.testing.assert_array_equal(bits(o.state(N.SPK_FIELD_V, 40)), bits(ref.base.V))
+    w = ref.weights()
+    assert not np.array_equal(w, a["weight"].astype(F))
+    np.testing.assert_array_equal(bits(o.weights()), bits(w))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("sched", [None, (1, 512, 0, 0)])
+@pytest.mark.parametrize("plastic", [False, True])
+def test_index_repeats_within_runs(sched, plastic):
+    """Runs of 0.00233 s (24 steps) whose start drifts to a half timestep:
+    the index from roundf(t/dt) then repeats and skips within a run, and each
+    repeat delivers the step before's spikes again (the engine's step kernels
+    against the oracle), with and without STDP, persistent and in bulk mode."""
+    from spike_gb300 import Net, schedule
+    d = descs.random_voltage_net(n=600, n_in=200, d_max=12, seed=41, plastic=plastic, stdp=STDP if plastic else None)
+    o = OracleNet(d.desc)
+    net = Net.from_desc(d.desc, schedule(*sched) if sched else None)
+    for sec in [0.0173] + [0.00233] * 24:
+        net.run(sec)
+        o.run(sec)
+    assert net.synchronize() == 0
+    assert_same(net, o, 600, 200, 1, weights=plastic, tag=f"plastic={plastic} {net.schedule()}")
