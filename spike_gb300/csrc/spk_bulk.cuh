@@ -73,7 +73,7 @@ struct BulkStep {
   int T, slot, g, sr;  // g: substep of the group; sr: timestep of the run
   bool live, stdp_run, inputs_active;
   // the group has the parity of the group step before it: its substeps
-  // deliver that group's spikes again (group_repeats)
+  // deliver that group's spikes again (bulk_rep; set by the kernels that use it)
   bool rep;
   bool dense_run;  // a per-synapse-trace rule updates this step
 };
@@ -85,14 +85,19 @@ __device__ __forceinline__ BulkStep bulk_step(const NetDev& d, const RunCtl& c, 
   const float dt = d.dt;
   group_time(c.start_time, sr, d.G, dt, b.t, b.T, b.tg);
   b.slot = b.T % d.B;
-  b.g = sr % d.G;
+  b.g = d.G == 1 ? 0 : sr % d.G;
   // the event-driven (weight-dependent) rule's passes, or the per-synapse-trace rules' pass
   b.stdp_run = d.has_stdp && c.plastic && d.stdp_rule == SPK_STDP_WEIGHT_DEPENDENT;
   b.dense_run = d.has_stdp && c.plastic && d.stdp_rule != SPK_STDP_WEIGHT_DEPENDENT;
   b.inputs_active = c.inputs_active != 0 || s > 0;
   b.sr = sr;
-  b.rep = group_repeats(c, sr, d.G, dt);
+  b.rep = false;
   return b;
+}
+
+// group_repeats for the step (one float division): the neuron and list kernels
+__device__ __forceinline__ bool bulk_rep(const NetDev& d, const RunCtl& c, const BulkStep& st) {
+  return group_repeats(c, st.sr, d.G == 1 ? st.T : (st.T - st.g) / d.G, d.G, d.dt);
 }
 
 __device__ __forceinline__ RunCtl load_ctl(const RunCtl* p) {
@@ -186,6 +191,7 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
                                                                          int s, int* item_count) {
   __shared__ __align__(16) NetDev sd;
   __shared__ RunCtl sctl;
+  __shared__ BulkStep sst;
   static_assert(sizeof(NetDev) % 4 == 0, "descriptor copied as words");
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const BulkBlock bb = blocks[blockIdx.x];
@@ -193,13 +199,19 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
     const uint32_t* src = (const uint32_t*)(nets + bb.net);
     uint32_t* dst = (uint32_t*)&sd;
     for (int i = threadIdx.x; i < (int)(sizeof(NetDev) / 4); i += blockDim.x) dst[i] = __ldg(src + i);
-    if (threadIdx.x == 0) sctl = load_ctl(bb.ctl);
+    if (threadIdx.x == 0) {
+      // the step's times once per CTA (two float divisions), from the global descriptor
+      sctl = load_ctl(bb.ctl);
+      BulkStep b = bulk_step(nets[bb.net], sctl, s);
+      if (b.live) b.rep = bulk_rep(nets[bb.net], sctl, b);
+      sst = b;
+    }
   }
   pdl_wait_then_release();
   if (blockIdx.x == 0 && threadIdx.x == 0) *item_count = 0;  // the afferent-pass list of this step
   __syncthreads();
   const NetDev& d = sd;
-  const BulkStep st = bulk_step(d, sctl, s);
+  const BulkStep st = sst;
   if (!st.live) return;
   const int w0 = w * BULK_WPW;
   if (w0 >= bb.count) return;
@@ -255,7 +267,9 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
           // (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:115-121):
           // this step's spike, or the last step's at a run start that repeats
           // its timestep index
-          ev = (int)roundf(((spk ? st.tg : lv[u]) - st.t) / d.dt) >= 0;
+          // (a spike older than a step cannot round to 0: no division then)
+          const float lag = (spk ? st.tg : lv[u]) - st.t;
+          ev = spk || (lag >= -d.dt && (int)roundf(lag / d.dt) >= 0);
           float po = pov[u] * d.E_m;
           po = po + (ev ? d.inc_m : 0.0f);
           d.post_trace[n] = po;
@@ -266,7 +280,7 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
         }
       }
       const unsigned word = __ballot_sync(FULL, spk);
-      const unsigned evword = __ballot_sync(FULL, ev);
+      const unsigned evword = st.stdp_run ? __ballot_sync(FULL, ev) : 0u;
       if (lane == 0) {
         // delivered keys: the spikes, and at a repeating run start the carried keys
         uint32_t* gb = d.gbits + (size_t)st.g * d.n_words + bw.word + u;
@@ -356,7 +370,8 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
   __shared__ int s_item_base;
   const NetDev& d = nets[blockIdx.x];
   const RunCtl c = load_ctl(d.ctl);
-  const BulkStep st = bulk_step(d, c, s);
+  BulkStep st = bulk_step(d, c, s);
+  st.rep = bulk_rep(d, c, st);
   pdl_wait_then_release();
   if (!st.live) {
     if (threadIdx.x == 0) *d.step_count = 0;
@@ -366,7 +381,8 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
   const int n_words = d.n_words, KL = d.KL;
   const bool rec_inputs = c.record_inputs != 0;
   // a carried list of two earlier groups is beyond this engine
-  if (threadIdx.x == 0 && st.rep && st.g == 0 && st.sr >= d.G && group_repeats(c, st.sr - d.G, d.G, d.dt))
+  if (threadIdx.x == 0 && st.rep && st.g == 0 && st.sr >= d.G &&
+      group_repeats(c, st.sr - d.G, group_index(c.start_time, st.sr - d.G, d.G, d.dt), d.G, d.dt))
     atomicCAS(&d.ctl->status, 0, SPK_ERR_UNSUPPORTED);
   const bool recording = d.spike_cap > 0;  // a network created without a spike store records nothing
   const int per = (n_words + BULK_LIST_THREADS - 1) / BULK_LIST_THREADS;
@@ -553,6 +569,7 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
   extern __shared__ __align__(16) uint32_t bsm[];
   __shared__ __align__(16) NetDev sd;
   __shared__ RunCtl sctl;
+  __shared__ BulkStep sst;
   __shared__ int s_nlist;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nthr = BULK_PROP_WARPS * 32;
   const BulkPropBlock pb = blocks[blockIdx.x];
@@ -560,13 +577,16 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
     const uint32_t* src = (const uint32_t*)(nets + pb.net);
     uint32_t* dst = (uint32_t*)&sd;
     for (int i = threadIdx.x; i < (int)(sizeof(NetDev) / 4); i += nthr) dst[i] = __ldg(src + i);
-    if (threadIdx.x == 0) sctl = load_ctl(pb.ctl);
+    if (threadIdx.x == 0) {
+      sctl = load_ctl(pb.ctl);
+      sst = bulk_step(nets[pb.net], sctl, s);  // once per CTA
+    }
   }
   pdl_wait_then_release();
   if (threadIdx.x == 0) s_nlist = *pb.n_list;
   __syncthreads();
   const NetDev& d = sd;
-  BulkStep st = bulk_step(d, sctl, s);
+  BulkStep st = sst;
   const int n_list = s_nlist;
   if (!st.live || n_list == 0) return;  // the whole CTA
   // A network that normalises its weights after the event-driven rule's

@@ -37,7 +37,7 @@ SPK_HD uint32_t pack_entry(uint32_t post_local, uint32_t delay, uint32_t label, 
 // substep's time t + g*timestep (LIFSpikingNeurons.cu:172,177; the spike
 // monitor's time, Spike/Backend/CUDA/ActivityMonitor/SpikingActivityMonitor.cu:93).
 SPK_HD void group_time(float start, int r, int G, float dt, float& t, int& T, float& tg) {
-  const int s = r / G, g = r - s * G;
+  const int s = G == 1 ? r : r / G, g = r - s * G;
   t = start + (float)(s * G) * dt;
   T = (int)roundf(t / dt) + g;
   tg = t + (float)g * dt;
@@ -105,13 +105,13 @@ SPK_HD int carry_decision(const RunCtl& c, int G, float dt, float start, int ste
   return (c.last_run_groups == 1 && c.last_run_repeat) ? 2 : 1;
 }
 
-// Whether the group of timestep sr of the run in c has the parity of the
-// group step before it, so that its substeps deliver the earlier group's
-// spikes again: the run's first group as decided where the run started, the
-// others from the time of the two groups.
-SPK_HD bool group_repeats(const RunCtl& c, int sr, int G, float dt) {
+// Whether the group of timestep sr of the run in c (its index k) has the
+// parity of the group step before it, so that its substeps deliver the
+// earlier group's spikes again: the run's first group as decided where the
+// run started, the others from the time of the group before.
+SPK_HD bool group_repeats(const RunCtl& c, int sr, int k, int G, float dt) {
   if (sr < G) return c.repeat != 0;
-  return ((group_index(c.start_time, sr, G, dt) ^ group_index(c.start_time, sr - G, G, dt)) & 1) == 0;
+  return ((k ^ group_index(c.start_time, sr - G, G, dt)) & 1) == 0;
 }
 
 // Everything one CTA needs to run its share of one network.

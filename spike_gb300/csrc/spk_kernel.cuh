@@ -266,19 +266,29 @@ __global__ void __launch_bounds__(512, 1)
   bool ok_run = true;
   __syncwarp();
 
+  // index of the group before the one of the launch's first timestep, and of
+  // the last timestep's group
+  int k_prev = ctl0.step >= d.G ? group_index(ctl0.start_time, ctl0.step - d.G, d.G, dt) : 0;
+  int k_last = 0;
+  bool fw_dirty = true;  // the carried words in shared memory are not known to be zero
   for (int s = 0; s < steps_here && ok_run; ++s) {
     const int sr = ctl0.step + s;
     float t, tg;
     int T;
     group_time(ctl0.start_time, sr, d.G, dt, t, T, tg);
-    const int g_sub = sr % d.G;  // substep of the group
-    // A group with the parity of the group step before it delivers that
-    // group's spikes again (carried keys), in each substep's propagation after
-    // its STDP updates, as activate_synapses follows the rules.  A carried
-    // list of two earlier groups is beyond this engine: status.
-    const bool rep = group_repeats(ctl0, sr, d.G, dt);
-    if (rep && sr >= d.G && g_sub == 0 && group_repeats(ctl0, sr - d.G, d.G, dt) && threadIdx.x == 0 &&
-        cm.rank == 0)
+    const int G = d.G;
+    const int g_sub = G == 1 ? 0 : sr % G;  // substep of the group
+    // A group with the parity of the group step before it (index k_prev,
+    // carried from step to step) delivers that group's spikes again (carried
+    // keys), in each substep's propagation after its STDP updates, as
+    // activate_synapses follows the rules.  A carried list of two earlier
+    // groups is beyond this engine: status.
+    const int k = G == 1 ? T : (T - g_sub) / G;
+    if (g_sub == 0 && s > 0) k_prev = k_last;
+    const bool rep = sr < G ? ctl0.repeat != 0 : ((k ^ k_prev) & 1) == 0;
+    k_last = k;
+    if (rep && sr >= G && g_sub == 0 && threadIdx.x == 0 && cm.rank == 0 &&
+        group_repeats(ctl0, sr - G, k_prev, G, dt))
       atomicCAS(&d.ctl->status, 0, SPK_ERR_UNSUPPORTED);
     const long long gs = ctl0.gstep + s;
     const int par = (int)(gs & 1);
@@ -350,7 +360,9 @@ __global__ void __launch_bounds__(512, 1)
             // (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:115-121):
             // this step's spike, or the last step's at a run start that
             // repeats its timestep index
-            ev = (int)roundf((last_s[li] - t) / dt) >= 0;
+            // (a spike older than a step cannot round to 0: no division then)
+            const float lag = last_s[li] - t;
+            ev = spk || (lag >= -dt && (int)roundf(lag / dt) >= 0);
             float po = post_s[li] * d.E_m;
             po = po + (ev ? d.inc_m : 0.0f);
             post_s[li] = po;
@@ -361,7 +373,7 @@ __global__ void __launch_bounds__(512, 1)
           }
         }
         const unsigned word = __ballot_sync(FULL, spk);
-        const unsigned evword = __ballot_sync(FULL, ev);
+        const unsigned evword = stdp_run ? __ballot_sync(FULL, ev) : 0u;
         if (lane == 0) {
           spkw_s[base >> 5] = word;
           evw_s[base >> 5] = evword;
@@ -431,9 +443,10 @@ __global__ void __launch_bounds__(512, 1)
       const int nl = TS >> 5, ni = ITS >> 5;
       for (int i = lane; i < nl + ni; i += 32) {
         const int wi = i < nl ? ((KL + p0) >> 5) + i : (kin0 >> 5) + (i - nl);
-        fw_s[i] = rep ? gb[wi] : 0u;
+        if (rep || fw_dirty) fw_s[i] = rep ? gb[wi] : 0u;
         gb[wi] = i < nl ? spkw_s[i] : inw_s[i - nl];
       }
+      fw_dirty = rep;
     }
     __syncwarp();
     if (stdp_run) {
