@@ -156,14 +156,14 @@ def plastic_ff_generated(n_in: int = 50000, n_neurons: int = 200000, ff: int = 9
 
 
 def sweep_instance(n: int, p: float, g: float, plastic: bool, seed: int, d_max: int = 10,
-                   rate: float = 20.0, rule: int = N.SPK_STDP_WEIGHT_DEPENDENT) -> GenNetwork:
+                   rate: float = 20.0, rule: int = N.SPK_STDP_WEIGHT_DEPENDENT, d_min: int = 1) -> GenNetwork:
     """One instance of the batched sweep: a Brunel-style voltage-jump LIF
     network of n neurons (80 % excitatory), Bernoulli(p) recurrent
     connectivity, J = 0.1 V / C_E with C_E = 0.8 n p (J C_E as in
-    Examples/Brunel10K.cpp), inhibitory weight -g J, delays U{1..d_max}, and
-    an external drive of n / 5 Poisson inputs at `rate` Hz connected with
-    probability 4p (C_E inputs per neuron, nu_ext = 2 nu_thr).  With
-    plasticity the input synapses are plastic, weights U(0, 1] at scale 2J,
+    Examples/Brunel10K.cpp), inhibitory weight -g J, delays U{d_min..d_max}
+    (d_min > 1 groups timesteps), and an external drive of n / 5 Poisson
+    inputs at `rate` Hz connected with probability 4p (C_E inputs per neuron,
+    nu_ext = 2 nu_thr).  With plasticity the input synapses are plastic, weights U(0, 1] at scale 2J,
     under the weight-dependent rule or (`rule`) the Evans rule."""
     n_e = int(round(0.8 * n))
     n_i = n - n_e
@@ -177,9 +177,9 @@ def sweep_instance(n: int, p: float, g: float, plastic: bool, seed: int, d_max: 
         stdp = EVANS_STDP
     projs = [Projection(N.SPK_POP_INPUTS, 0, n_in, 0, n, p_in,
                         weight=(0.0, 1.0) if plastic else (1.0, 1.0), scale=2.0 * J if plastic else J,
-                        delay=(1, d_max), plastic=plastic),
-             Projection(N.SPK_POP_NEURONS, 0, n_e, 0, n, p, weight=(1.0, 1.0), scale=J, delay=(1, d_max)),
-             Projection(N.SPK_POP_NEURONS, n_e, n_i, 0, n, p, weight=(-g, -g), scale=J, delay=(1, d_max))]
+                        delay=(d_min, d_max), plastic=plastic),
+             Projection(N.SPK_POP_NEURONS, 0, n_e, 0, n, p, weight=(1.0, 1.0), scale=J, delay=(d_min, d_max)),
+             Projection(N.SPK_POP_NEURONS, n_e, n_i, 0, n, p, weight=(-g, -g), scale=J, delay=(d_min, d_max))]
     return GenNetwork(groups=[dict(count=n_e, **BRUNEL_LIF), dict(count=n_i, **BRUNEL_LIF)], projections=projs,
                       refractory=2.0e-3, n_inputs=n_in, rates=np.full(n_in, rate, np.float32), stdp=stdp,
                       seed=seed, connectivity_seed=seed ^ 0x5eed,

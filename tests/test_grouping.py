@@ -490,3 +490,23 @@ def test_index_repeats_within_runs(sched, plastic):
         o.run(sec)
     assert net.synchronize() == 0
     assert_same(net, o, 600, 200, 1, weights=plastic, tag=f"plastic={plastic} {net.schedule()}")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rule,norm", [(N.SPK_STDP_EVANS, 0), (N.SPK_STDP_INHIBITORY, 0), (N.SPK_STDP_CUSTOM, 0),
+                                       (N.SPK_STDP_WEIGHT_DEPENDENT, N.SPK_NORM_AFTER_RULE)])
+def test_bulk_only_rules_at_repeating_boundaries(rule, norm):
+    """The per-synapse-trace rules and the weight normalisation (bulk mode)
+    across run starts and within-run index repeats: carried keys delivered
+    after the rules' updates, the rules' spike lookups unchanged."""
+    from spike_gb300 import Net
+    from test_stdp_rules import CUSTOM, EVANS, VOGELS
+    sp = {N.SPK_STDP_EVANS: EVANS, N.SPK_STDP_INHIBITORY: VOGELS, N.SPK_STDP_CUSTOM: CUSTOM}.get(rule, STDP)
+    d = descs.random_voltage_net(n=300, n_in=200, plastic=True, stdp=sp, stdp_rule=rule, weight_norm=norm, seed=43)
+    o = OracleNet(d.desc)
+    net = Net.from_desc(d.desc)
+    for sec in [0.0173] + [0.00233] * 12:
+        net.run(sec)
+        o.run(sec)
+    assert net.synchronize() == 0
+    assert_same(net, o, 300, 200, 1, weights=True, tag=f"rule {rule} norm {norm}")

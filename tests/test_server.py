@@ -112,3 +112,28 @@ def test_cancel_and_stop_with_work_queued():
     info0 = srv.wait(ids[0], 120.0)
     assert info0.state == N.SPK_JOB_CANCELLED and info0.steps_done < 50000
     srv.stop()  # cancels the rest and frees every network
+
+
+def test_served_grouped_jobs():
+    """Jobs whose minimum delay is 2 steps (timestep grouping 2) run with
+    grouped times, equal to the same network run alone; a job whose step
+    count is not whole groups fails with SPK_ERR_INVALID and the others go on."""
+    srv = Server(steps_per_block=250, reserve_bytes=1 << 30, mode=N.SPK_BATCH_BULK)
+    work = [(sweep_instance(1200 + 300 * i, 0.03, 5.0, False, seed=900 + i, d_min=2, d_max=8), 600) for i in range(3)]
+    ids = [srv.submit(gen, steps, False) for gen, steps in work]
+    bad = srv.submit(sweep_instance(800, 0.03, 5.0, False, seed=950, d_min=2, d_max=8), 301, False)
+    infos = [srv.wait(j, 300.0) for j in ids]
+    assert all(inf.state == N.SPK_JOB_DONE for inf in infos), [inf.state for inf in infos]
+    binfo = srv.wait(bad, 300.0)
+    assert binfo.state == N.SPK_JOB_FAILED and binfo.error == N.SPK_ERR_INVALID
+    for (gen, steps), j in zip(work, ids):
+        ref = Net.generate(gen)
+        assert ref.timestep_grouping() == 2
+        ref.run_steps(steps, False)
+        assert ref.synchronize() == 0
+        ri, rt = ref.spikes()
+        si, stt = srv.spikes(j)
+        np.testing.assert_array_equal(si, ri)
+        np.testing.assert_array_equal(bits(stt), bits(rt))
+        ref.close()
+    srv.stop()
