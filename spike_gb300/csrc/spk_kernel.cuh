@@ -268,15 +268,20 @@ __global__ void __launch_bounds__(512, 1)
 
   // index of the group before the one of the launch's first timestep, and of
   // the last timestep's group
-  int k_prev = ctl0.step >= d.G ? group_index(ctl0.start_time, ctl0.step - d.G, d.G, dt) : 0;
+  const int G = d.G;
+  int k_prev = ctl0.step >= G ? group_index(ctl0.start_time, ctl0.step - G, G, dt) : 0;
   int k_last = 0;
   bool fw_dirty = true;  // the carried words in shared memory are not known to be zero
+  // this lane's word of the warp's group spike words (neurons, then inputs), if any
+  const int gw_n = (TS + ITS) >> 5;
+  uint32_t* const gw = lane < gw_n ? d.gbits + (lane < (TS >> 5) ? ((KL + p0) >> 5) + lane
+                                                                 : (kin0 >> 5) + (lane - (TS >> 5)))
+                                   : nullptr;
   for (int s = 0; s < steps_here && ok_run; ++s) {
     const int sr = ctl0.step + s;
     float t, tg;
     int T;
     group_time(ctl0.start_time, sr, d.G, dt, t, T, tg);
-    const int G = d.G;
     const int g_sub = G == 1 ? 0 : sr % G;  // substep of the group
     // A group with the parity of the group step before it (index k_prev,
     // carried from step to step) delivers that group's spikes again (carried
@@ -376,7 +381,7 @@ __global__ void __launch_bounds__(512, 1)
         const unsigned evword = stdp_run ? __ballot_sync(FULL, ev) : 0u;
         if (lane == 0) {
           spkw_s[base >> 5] = word;
-          evw_s[base >> 5] = evword;
+          if (stdp_run) evw_s[base >> 5] = evword;
         }
       }
     }
@@ -423,7 +428,8 @@ __global__ void __launch_bounds__(512, 1)
     {
       const int nl = TS >> 5, ni = ITS >> 5;
       for (int i = 0; i < nl + ni; ++i) {
-        const uint32_t m = i < nl ? (spkw_s[i] | evw_s[i]) : (inw_s[i - nl] | (stdp_run ? inwp_s[i - nl] : 0u));
+        const uint32_t m = i < nl ? (spkw_s[i] | (stdp_run ? evw_s[i] : 0u))
+                                  : (inw_s[i - nl] | (stdp_run ? inwp_s[i - nl] : 0u));
         if (!((m >> lane) & 1u)) continue;
         const int li = i < nl ? 32 * i + lane : TS + 32 * (i - nl) + lane;
         const int key = i < nl ? KL + p0 + li : kin0 + (li - TS);
@@ -439,16 +445,23 @@ __global__ void __launch_bounds__(512, 1)
       // This substep's spike words, kept for a later run that repeats the
       // group's index; at such a repeat (rep) the last group's words are the
       // carried keys delivered again in this step.
-      uint32_t* gb = d.gbits + (size_t)g_sub * n_words;
       const int nl = TS >> 5, ni = ITS >> 5;
-      for (int i = lane; i < nl + ni; i += 32) {
-        const int wi = i < nl ? ((KL + p0) >> 5) + i : (kin0 >> 5) + (i - nl);
-        if (rep || fw_dirty) fw_s[i] = rep ? gb[wi] : 0u;
-        gb[wi] = i < nl ? spkw_s[i] : inw_s[i - nl];
+      if (gw_n <= 32) {
+        // one word per lane (the common case): pointer set up once per launch;
+        // the new words are stored after the CTA's stamp (below), so that the
+        // stamp does not queue behind them
+        if (gw && (rep || fw_dirty)) fw_s[lane] = rep ? gw[(size_t)g_sub * n_words] : 0u;
+      } else {
+        uint32_t* gb = d.gbits + (size_t)g_sub * n_words;
+        for (int i = lane; i < nl + ni; i += 32) {
+          const int wi = i < nl ? ((KL + p0) >> 5) + i : (kin0 >> 5) + (i - nl);
+          if (rep || fw_dirty) fw_s[i] = rep ? gb[wi] : 0u;
+          gb[wi] = i < nl ? spkw_s[i] : inw_s[i - nl];
+        }
       }
       fw_dirty = rep;
     }
-    __syncwarp();
+    // (each lane reads back only the carried words it wrote)
     if (stdp_run) {
       // bitmaps for the post-spike pass, which looks up arbitrary pre keys:
       // delivered keys (A) and STDP events (P)
@@ -494,7 +507,7 @@ __global__ void __launch_bounds__(512, 1)
         const uint32_t* r = sm + SHARED_WORDS + wx * wl.total;
         sp = r[wl.spkw + k];
         f = r[wl.fw + k];
-        p = r[wl.evw + k];
+        p = stdp_run ? r[wl.evw + k] : 0u;
         wkey = (uint32_t)(KL + (cm.rank * W + wx) * TS + k * 32);
       }
       a = sp | f;
@@ -532,6 +545,11 @@ __global__ void __launch_bounds__(512, 1)
       if (lane == 0)
         st_relaxed_u64(d.cta_stamp + (size_t)par * d.nctas + cm.rank,
                        stamp_hi | ((unsigned long long)n_in << 16) | (unsigned long long)(pos - n_in));
+    }
+    // this substep's spike words for a later repeating group (one word per lane)
+    if (gw_n <= 32 && gw) {
+      const int nl = TS >> 5;
+      gw[(size_t)g_sub * n_words] = lane < nl ? spkw_s[lane] : inw_s[lane - nl];
     }
 
     // ---- phase B: warp 0 gathers the step's active keys from every CTA ------
