@@ -48,6 +48,25 @@ def ref_va(mixed: bool, d_lo: int = 1, d_hi: int = 1) -> Model:
     return m
 
 
+def ref_det(current: bool) -> Model:
+    """oracle/ref_cases.inc build_det: the deterministic voltage (vdet) or
+    current (cdet) synapse network."""
+    kind = N.SPK_SYN_CURRENT if current else N.SPK_SYN_VOLTAGE
+    m = Model(kind, N.SPK_INPUT_NONE, synapse_seed=11, timestep=float(DT))
+    args = (0.0, 0.0, 20.0e-3, 2.0e-3, 25.0e-3)
+    ge = m.add_neuron_group(_lif(800, *args))
+    gi = m.add_neuron_group(_lif(200, *args))
+    J = 2.0 ** (-29 if current else -8)
+    for pre, post in ((ge, ge), (ge, gi), (gi, ge), (gi, gi)):
+        exc = pre == ge
+        w = 1.0 if exc else -4.0
+        sp = SynapseParams(connectivity_type=N.SPK_CONN_RANDOM, weight_range=(w, w), weight_scaling_constant=J,
+                           delay_range=(steps(1), steps(30)), random_connectivity_probability=0.05,
+                           decay_term_tau=(5.0e-3 if exc else 10.0e-3) if current else 0.001)
+        m.add_synapse_group(pre, post, sp)
+    return m
+
+
 def ref_brunel() -> Model:
     m = Model(N.SPK_SYN_VOLTAGE, N.SPK_INPUT_POISSON, synapse_seed=42, timestep=float(DT))
     rule = m.add_stdp_rule(STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02,

@@ -8,7 +8,8 @@ cases defined in oracle/ref_dump.cpp and stores what it produced:
 * the full VogelsAbbottNet network (va, 320,261 synapses): counts and SHA-256
   digests of every array, as .json; the same for its grouped variants va_g2
   and va_g3 (delays of 2 and 3-5 steps) with the front end's timestep
-  grouping, as ref_va_grouped.json;
+  grouping, as ref_va_grouped.json, and of the deterministic voltage and
+  current synapse networks vdet and cdet, as ref_det.json;
 * the weight and connectivity files the reference's save functions write for
   each case (Spike/Synapses/Synapses.cpp:423-614, SpikingSynapses.cpp:136-189;
   ref_dump's save mode), and the weights read back from the text file and
@@ -111,8 +112,9 @@ def main() -> int:
         meta["eff_count_digest"] = digest(d["eff_count"])
         meta["tau_m"] = float(d["tau_m"][0])
         meta["R"] = float(d["R"][0])
-        meta["vhat"] = [float(x) for x in d["vhat"]]
-        meta["tau_g"] = [float(x) for x in d["tau_g"]]
+        for k in ("vhat", "tau_g"):  # conductance synapses only
+            if k in d:
+                meta[k] = [float(x) for x in d[k]]
         print(case, meta["n_synapses"], "synapses, grouping", meta["timestep_grouping"])
         return meta
 
@@ -120,6 +122,8 @@ def main() -> int:
         json.dump(digests("va"), f, indent=1, sort_keys=True)
     with open(os.path.join(HERE, "ref_va_grouped.json"), "w") as f:
         json.dump({case: digests(case) for case in ("va_g2", "va_g3")}, f, indent=1, sort_keys=True)
+    with open(os.path.join(HERE, "ref_det.json"), "w") as f:
+        json.dump({case: digests(case) for case in ("vdet", "cdet")}, f, indent=1, sort_keys=True)
     ck = {case: checkpoint_digests(ref_dump, case) for case in ("va", "va_mix", "brunel", "shapes")}
     with open(os.path.join(HERE, "ref_checkpoint.json"), "w") as f:
         json.dump(ck, f, indent=1, sort_keys=True)

@@ -10,8 +10,12 @@ written (no fused multiply-add, oracle/build_ref_gpu.sh with REF_STRICT_FP=1),
 its spike train is a bit pattern that the oracle and the engine must
 reproduce exactly.
 
+The same holds for networks whose weights are integer multiples of a power
+of two (partial sums are exact in any order): vdet, voltage synapses with E
+weight J and I weight -4 J.
+
 Cases (oracle/ref_cases.inc): va (delay 1 step), va_g2 (2 steps: timestep
-grouping 2), va_g3 (3-5 steps: grouping 3); each run(0.5) from the model's
+grouping 2), va_g3 (3-5 steps: grouping 3), vdet; each run(0.5) from the model's
 initial state, then run(0.0337) (not whole groups: the next run starts at
 start + seconds) and run(0.2).  Per case the neuron spikes, sorted by (time,
 id) (the reference's monitor stores a step's spikes in atomic order), go to
@@ -33,7 +37,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-CASES = ("va", "va_g2", "va_g3")
+# cdet (current synapses) is not run: the reference's current-synapse backend
+# never sets its device decay-constant pointer (CurrentSpikingSynapses.cu:27-29)
+# and its injection kernel faults on it
+CASES = ("va", "va_g2", "va_g3", "vdet")
 RUNS = (0.5, 0.0337, 0.2)
 
 

@@ -97,3 +97,18 @@ def test_grouped_vogels_abbott_digests(case, d_lo, d_hi):
         assert hashlib.sha256(np.ascontiguousarray(a[k]).tobytes()).hexdigest() == h, k
     assert int(a["delay"].min()) == meta["min_delay"] == meta["timestep_grouping"] == d_lo
     assert int(a["delay"].max()) == meta["max_delay"]
+
+
+@pytest.mark.parametrize("case,current", [("vdet", False), ("cdet", True)])
+def test_deterministic_network_digests(case, current):
+    """The deterministic voltage and current synapse networks of the
+    bit-exact comparison with the reference's kernels: every array
+    bit-identical, and the labels the reference front end made."""
+    with open(os.path.join(GOLD, "ref_det.json")) as f:
+        meta = json.load(f)[case]
+    m = cases.ref_det(current)
+    assert m.counts() == (meta["n_neurons"], meta["n_inputs"], meta["n_synapses"])
+    a = desc_arrays(m.desc())
+    for k, h in meta["digests_created"].items():
+        assert hashlib.sha256(np.ascontiguousarray(a[k]).tobytes()).hexdigest() == h, k
+    assert int(a["label"].max()) + 1 == meta["num_syn_labels"]
