@@ -568,8 +568,10 @@ void Net<R>::poisson_range(int a, int b, R tg, int T) {
 }
 
 // ltp_and_ltd (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:85-161),
-// G = 1: pre_g, post_g are 0 for a spike at this step and negative otherwise,
-// so the (post_g > pre_g) / (pre_g > post_g) corrections never apply.
+// G = 1: pre_g, post_g are 0 for a spike at this step (or of the step before,
+// when a run starts at the timestep index where the last one ended) and
+// negative otherwise, so the (post_g > pre_g) / (pre_g > post_g) corrections
+// never apply.
 template <typename R>
 void Net<R>::stdp_range(int64_t a, int64_t b, R t) {
   // G = 1 here: init refuses a rule with a larger grouping
