@@ -1,0 +1,128 @@
+"""Seeded random networks and run sequences: the engine against the oracle,
+bit for bit (GPU).
+
+Each case draws from its seed:
+- the synapse kind: voltage, current or conductance, with 1-3 labels;
+- 60-900 LIF neurons in one to three groups, 0-300 Poisson inputs;
+- delays d_min..d_max, d_min in {1, 2, 3} (the timestep grouping), d_max up to 20;
+- with d_min = 1, weight-dependent STDP on the excitatory and input synapses half the time;
+- a schedule: the planner's, or 2-8 warps of 32-128 posts over as many CTAs as cover the
+  network with launches of 7-1000 timesteps, or (bulk mode) one warp per 512-post range;
+- four to seven actions: run(seconds) with seconds/dt fractions below and above one half
+  (where the next run starts, the timestep index then repeats or skips one, and the
+  reference's active lists deliver the last group again), run_steps of whole groups,
+  plasticity switched off for some runs, reset_time or reset_state between some.
+"""
+import numpy as np
+import pytest
+
+import descs
+from engine_checks import assert_same
+from oracle import OracleNet
+from spike_gb300 import Net, schedule
+from spike_gb300 import _native as N
+from spike_gb300.model import STDPParams
+
+pytestmark = pytest.mark.gpu
+
+STDP = STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02, lambda_=1.0, alpha=1.0, w_max=1.0)
+
+
+def random_case(seed: int):
+    rng = np.random.default_rng(seed)
+    kind = [N.SPK_SYN_VOLTAGE, N.SPK_SYN_CURRENT, N.SPK_SYN_CONDUCTANCE][seed % 3]
+    n = int(rng.integers(60, 900))
+    n_in = int(rng.choice([0, int(rng.integers(20, 300))]))
+    d_min = int(rng.choice([1, 1, 2, 3]))
+    d_max = int(rng.integers(d_min, 21))
+    plastic = d_min == 1 and kind == N.SPK_SYN_VOLTAGE and bool(rng.integers(0, 2))
+    L = 1 if kind == N.SPK_SYN_VOLTAGE else int(rng.integers(1, 4))
+    n_groups = int(rng.integers(1, 4))
+    cuts = np.sort(rng.choice(np.arange(1, n), n_groups - 1, replace=False)) if n_groups > 1 else np.array([], int)
+    counts = np.diff(np.concatenate([[0], cuts, [n]])).astype(int)
+    n_exc = int(0.8 * n)
+    if kind == N.SPK_SYN_CONDUCTANCE:
+        lif = dict(v0=-0.06, vreset=-0.06, theta=-0.05)
+        i_bg = float(rng.uniform(0.011, 0.016))  # over threshold: every network fires
+    else:
+        lif = dict(v0=0.0, vreset=0.0, theta=0.02)
+        i_bg = float(rng.uniform(0.021, 0.03))
+    groups = [dict(count=int(c), tau_m=float(rng.uniform(0.01, 0.03)), R=1e8, v_init_lo=lif["v0"],
+                   v_init_hi=lif["theta"], **lif) for c in counts]
+    # connectivity: Bernoulli p, multapses allowed, inputs at p_in
+    p = float(rng.uniform(0.02, 0.1))
+    pre, post = [], []
+    for q in range(n):
+        k_rec, k_in = rng.binomial(n, p), rng.binomial(n_in, 2 * p) if n_in else 0
+        pre += list(rng.integers(0, n, k_rec)) + list(-rng.integers(0, n_in, k_in) - 1 if k_in else [])
+        post += [q] * (k_rec + k_in)
+    pre, post = np.asarray(pre, np.int64), np.asarray(post, np.int64)
+    S = len(pre)
+    exc = (pre < 0) | (pre < n_exc)
+    if kind == N.SPK_SYN_VOLTAGE:
+        w = np.where(exc, rng.uniform(2e-4, 1.5e-3, S), -rng.uniform(1e-3, 5e-3, S))
+    elif kind == N.SPK_SYN_CURRENT:
+        w = np.where(exc, rng.uniform(1e-10, 6e-10, S), -rng.uniform(4e-10, 2e-9, S))
+    else:
+        w = np.where(exc, rng.uniform(1e-9, 6e-9, S), rng.uniform(1e-8, 5e-8, S))
+    label = np.where(exc, 0, L - 1) if L > 1 else np.zeros(S, int)
+    label = np.where((pre < 0) & (L == 3), 1, label)
+    delay = rng.integers(d_min, d_max + 1, S)
+    if S:
+        delay[0] = d_min
+    tau = list(rng.uniform(0.003, 0.012, L))
+    vhat = [0.0 if l != L - 1 or L == 1 else -0.08 for l in range(L)]
+    d = descs.Desc(kind=kind, groups=groups, refractory=float(rng.uniform(0.001, 0.003)), i_bg=i_bg,
+                   n_inputs=n_in, rates=rng.uniform(10, 60, n_in) if n_in else None, n_labels=L, label_tau=tau,
+                   label_vhat=vhat, pre=pre, post=post, weight=w, delay=delay, label=label,
+                   plastic=exc.astype(int) if plastic else None, stdp=STDP if plastic else None, seed=seed,
+                   record_inputs=bool(rng.integers(0, 2)))
+    # schedule
+    choice = int(rng.integers(0, 3))
+    if choice == 0:
+        sched = None
+    elif choice == 1:
+        W = int(rng.choice([2, 4, 8]))
+        TS = int(rng.choice([32, 64, 128]))
+        C = -(-n // (W * TS))
+        sched = schedule(W, TS, C, int(rng.choice([7, 50, 1000])))
+    else:
+        sched = schedule(1, 512, 0, 0)  # post ranges, bulk mode
+    # actions
+    actions = []
+    for _ in range(int(rng.integers(4, 8))):
+        a = int(rng.integers(0, 10))
+        if a < 6:
+            steps = int(rng.integers(20, 300))
+            frac = float(rng.choice([0.2, 0.35, 0.65, 0.8]))
+            actions.append(("run", float(np.float32((steps + frac) * 1e-4)), bool(rng.integers(0, 4))))
+        elif a < 8:
+            actions.append(("steps", d_min * int(rng.integers(10, 150)), bool(rng.integers(0, 4))))
+        elif a == 8:
+            actions.append(("reset_time",))
+        else:
+            actions.append(("reset_state",))
+    return d, sched, actions, n, n_in, L, plastic
+
+
+@pytest.mark.parametrize("seed", range(18))
+def test_random_network_and_runs(seed):
+    d, sched, actions, n, n_in, L, plastic = random_case(seed)
+    o = OracleNet(d.desc)
+    net = Net.from_desc(d.desc, sched)
+    for act in actions:
+        if act[0] == "run":
+            net.run(act[1], act[2])
+            o.run(act[1], act[2])
+        elif act[0] == "steps":
+            net.run_steps(act[1], act[2])
+            o.run_steps(act[1], act[2])
+        elif act[0] == "reset_time":
+            net.reset_time()
+            o.reset_time()
+        else:
+            net.reset_state()
+            o.reset_state()
+    assert net.synchronize() == 0
+    assert net.current_time() == o.current_time()
+    assert_same(net, o, n, n_in, L, weights=plastic, tag=f"seed {seed} {net.schedule()} {actions}")
