@@ -256,36 +256,40 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
       if (u >= bw.count) break;
       const int key = (bw.word + u) * 32 + lane;
       const int n = key - KL;
-      bool spk = false, ev = false;
+      bool spk = false, ev = false, pe = false;
       if (n < N) {
         float* cell = cellp[u];
         spk = bulk_lif(d, st, n, key, Vv[u], lv[u], cell, inv[u]);
         if (kind == SPK_SYN_VOLTAGE)
           for (int l = 0; l < L; ++l) cell[l] = 0.0f;
         if (st.stdp_run) {
-          // post_spike_g = roundf((last - t)/dt) >= 0
-          // (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:115-121):
-          // this step's spike, or the last step's at a run start that repeats
-          // its timestep index
-          // (a spike older than a step cannot round to 0: no division then)
-          const float lag = (spk ? st.tg : lv[u]) - st.t;
-          ev = spk || (lag >= -d.dt && (int)roundf(lag / d.dt) >= 0);
+          // g = roundf((last - t)/dt)
+          // (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:113-117):
+          // an event as the postsynaptic neuron for g >= 0, as the
+          // presynaptic one for g == 0 (g >= G is negated), as in the
+          // persistent kernel.  A spike older than a step cannot round to 0.
+          const float lag = lv[u] - st.t;
+          const int gq = (spk || lag < -d.dt) ? (spk ? 0 : -1) : (int)roundf(lag / d.dt);
+          ev = gq >= 0;
+          pe = gq == 0;
           float po = pov[u] * d.E_m;
           po = po + (ev ? d.inc_m : 0.0f);
           d.post_trace[n] = po;
           float pr = prv[u] * d.E_p;
-          pr = pr + (ev ? d.inc_p : 0.0f);
+          pr = pr + (pe ? d.inc_p : 0.0f);
           d.pre_trace[key] = pr;
           pub[key] = pr;
         }
       }
       const unsigned word = __ballot_sync(FULL, spk);
       const unsigned evword = st.stdp_run ? __ballot_sync(FULL, ev) : 0u;
+      const unsigned peword = st.stdp_run ? __ballot_sync(FULL, pe) : 0u;
       if (lane == 0) {
         // delivered keys: the spikes, and at a repeating run start the carried keys
         uint32_t* gb = d.gbits + (size_t)st.g * d.n_words + bw.word + u;
         d.bitsA[bw.word + u] = word | (st.rep ? *gb : 0u);
-        d.bitsP[bw.word + u] = evword;
+        d.bitsP[bw.word + u] = peword;
+        d.bitsE[bw.word + u] = evword;
         if (d.hist) d.hist[(size_t)(st.T % d.H) * d.n_words + bw.word + u] = word;
         *gb = word;
       }
@@ -451,7 +455,7 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
   // with one atomic per network
   const int wl0 = max(w0, KL >> 5);
   int nsp = 0;
-  for (int i = wl0; i < w1; ++i) nsp += __popc(d.bitsP[i]);
+  for (int i = wl0; i < w1; ++i) nsp += __popc(d.bitsE[i]);
   int ic = nsp;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -475,7 +479,7 @@ __global__ void __launch_bounds__(BULK_LIST_THREADS) bulk_list_kernel(const NetD
   __syncthreads();
   int ipos = s_item_base + (int)warp_tot[w] + ic - nsp;
   for (int i = wl0; i < w1; ++i) {
-    uint32_t a = d.bitsP[i];
+    uint32_t a = d.bitsE[i];
     while (a) {
       const int b = __ffs(a) - 1;
       a &= a - 1;
@@ -663,7 +667,7 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
       else
         ptr_s[i] = 0.0f;
     }
-    for (int i = lane; i < TS / 32; i += 32) spw_s[i] = d.bitsP[((KL + p0) >> 5) + i];  // post events
+    for (int i = lane; i < TS / 32; i += 32) spw_s[i] = d.bitsE[((KL + p0) >> 5) + i];  // post events
   }
   stage_list(0);
   cp_async_wait_all();

@@ -159,6 +159,10 @@ struct NetDev {
   // post-spike STDP pass to look up arbitrary presynaptic keys.
   uint32_t* bitsA;  // [2][n_words]
   uint32_t* bitsP;  // [2][n_words]
+  // bulk mode: postsynaptic STDP events of the step ([n_words]); a neuron's
+  // presynaptic events (bitsP) differ from these only when its last spike is
+  // later than the clock (after reset_time)
+  uint32_t* bitsE;
   uint2* spikes;    // spike store (key, float time bits)
   long long spike_cap;
   RunCtl* ctl;
@@ -196,8 +200,8 @@ struct CtaMap {
 
 // Per-warp shared-memory words for a schedule (4-byte words).
 struct WarpLayout {
-  int stage, stw, sidx, kst, koff, kfl, kpre, tag, rowb, rowe, ring, V, last, gtr, post_tr, pre_tr, spkw, evw, fw, inw,
-      inwp, in_next, in_rate, in_pre, total;
+  int stage, stw, sidx, kst, koff, kfl, kpre, tag, rowb, rowe, ring, V, last, gtr, post_tr, pre_tr, spkw, evw, pvw, fw,
+      inw, inwp, in_next, in_rate, in_pre, total;
 };
 SPK_HD WarpLayout warp_layout(int B, int TS, int L, int ITS, int kind, int has_stdp) {
   WarpLayout w;
@@ -219,7 +223,8 @@ SPK_HD WarpLayout warp_layout(int B, int TS, int L, int ITS, int kind, int has_s
   w.post_tr = o; o += has_stdp ? TS : 0;
   w.pre_tr = o; o += has_stdp ? TS : 0;
   w.spkw = o; o += TS / 32;   // spike words of the tile's neurons (this step)
-  w.evw = o; o += TS / 32;    // STDP event words of the tile's neurons
+  w.evw = o; o += TS / 32;    // postsynaptic STDP event words of the tile's neurons
+  w.pvw = o; o += TS / 32;    // presynaptic STDP event words of the tile's neurons
   w.fw = o; o += (TS + ITS) / 32;  // carried keys delivered again (neurons, then inputs)
   w.inw = o; o += ITS / 32;   // spike words of the tile's inputs
   w.inwp = o; o += ITS / 32;  // STDP pre-event words of the tile's inputs

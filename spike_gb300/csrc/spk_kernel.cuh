@@ -196,6 +196,7 @@ __global__ void __launch_bounds__(512, 1)
   float* pre_s = (float*)(wreg + wl.pre_tr);
   uint32_t* spkw_s = wreg + wl.spkw;
   uint32_t* evw_s = wreg + wl.evw;
+  uint32_t* pvw_s = wreg + wl.pvw;
   uint32_t* fw_s = wreg + wl.fw;
   uint32_t* inw_s = wreg + wl.inw;
   uint32_t* inwp_s = wreg + wl.inwp;
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(512, 1)
       for (int base = 0; base < TS; base += 32) {
         const int li = base + lane;
         const int n = p0 + li;
-        bool spk = false, ev = false;
+        bool spk = false, ev = false, pe = false;
         if (n < N) {
           GroupConst G = G0;
           if (g_last != g_first) {
@@ -361,27 +362,36 @@ __global__ void __launch_bounds__(512, 1)
           }
           V_s[li] = Vi;
           if (stdp_run) {
-            // post_spike_g = roundf((last - t)/dt) >= 0
-            // (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:115-121):
+            // g = roundf((last - t)/dt)
+            // (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:113-117):
+            // an event as the postsynaptic neuron for g >= 0, as the
+            // presynaptic one for 0 <= g < G (g >= G is negated).  That is
             // this step's spike, or the last step's at a run start that
-            // repeats its timestep index
-            // (a spike older than a step cannot round to 0: no division then)
+            // repeats its timestep index, or (post only) a spike later than
+            // the clock after reset_time.  A spike older than a step cannot
+            // round to 0: no division then.
             const float lag = last_s[li] - t;
-            ev = spk || (lag >= -dt && (int)roundf(lag / dt) >= 0);
+            const int gq = (spk || lag < -dt) ? (spk ? 0 : -1) : (int)roundf(lag / dt);
+            ev = gq >= 0;
+            pe = gq == 0;
             float po = post_s[li] * d.E_m;
             po = po + (ev ? d.inc_m : 0.0f);
             post_s[li] = po;
             float pr = pre_s[li] * d.E_p;
-            pr = pr + (ev ? d.inc_p : 0.0f);
+            pr = pr + (pe ? d.inc_p : 0.0f);
             pre_s[li] = pr;
             pub[KL + n] = pr;
           }
         }
         const unsigned word = __ballot_sync(FULL, spk);
         const unsigned evword = stdp_run ? __ballot_sync(FULL, ev) : 0u;
+        const unsigned peword = stdp_run ? __ballot_sync(FULL, pe) : 0u;
         if (lane == 0) {
           spkw_s[base >> 5] = word;
-          if (stdp_run) evw_s[base >> 5] = evword;
+          if (stdp_run) {
+            evw_s[base >> 5] = evword;
+            pvw_s[base >> 5] = peword;
+          }
         }
       }
     }
@@ -428,7 +438,7 @@ __global__ void __launch_bounds__(512, 1)
     {
       const int nl = TS >> 5, ni = ITS >> 5;
       for (int i = 0; i < nl + ni; ++i) {
-        const uint32_t m = i < nl ? (spkw_s[i] | (stdp_run ? evw_s[i] : 0u))
+        const uint32_t m = i < nl ? (spkw_s[i] | (stdp_run ? pvw_s[i] : 0u))
                                   : (inw_s[i - nl] | (stdp_run ? inwp_s[i - nl] : 0u));
         if (!((m >> lane) & 1u)) continue;
         const int li = i < nl ? 32 * i + lane : TS + 32 * (i - nl) + lane;
@@ -470,7 +480,7 @@ __global__ void __launch_bounds__(512, 1)
         if (i < nl) {
           const int wi = ((KL + p0) >> 5) + i;
           bitsA[wi] = spkw_s[i] | fw_s[i];
-          bitsP[wi] = evw_s[i];
+          bitsP[wi] = pvw_s[i];
         } else {
           const int wi = (kin0 >> 5) + (i - nl);
           bitsA[wi] = inw_s[i - nl] | fw_s[i];
@@ -507,7 +517,7 @@ __global__ void __launch_bounds__(512, 1)
         const uint32_t* r = sm + SHARED_WORDS + wx * wl.total;
         sp = r[wl.spkw + k];
         f = r[wl.fw + k];
-        p = stdp_run ? r[wl.evw + k] : 0u;
+        p = stdp_run ? r[wl.pvw + k] : 0u;
         wkey = (uint32_t)(KL + (cm.rank * W + wx) * TS + k * 32);
       }
       a = sp | f;

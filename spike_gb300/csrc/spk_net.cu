@@ -692,7 +692,8 @@ static std::vector<size_t> arena_part_sizes(const Plan& plan, int N, int Nin, in
           sizeof(uint32_t) * (dense ? (size_t)(B - 2) * plan.n_words : 0),
           sizeof(float) * (norm ? (size_t)n_csc : 0),
           sizeof(float) * (norm ? (size_t)N : 0),
-          sizeof(uint32_t) * (size_t)G * plan.n_words};
+          sizeof(uint32_t) * (size_t)G * plan.n_words,
+          sizeof(uint32_t) * (size_t)plan.n_words};
 }
 
 static size_t arena_total(const std::vector<size_t>& sizes) {
@@ -738,7 +739,7 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   const int key_cap = plan.W * (plan.TS + plan.ITS);
   void* p_ctl = nullptr; void* p_abort = nullptr; void* p_dd = nullptr; void* p_map = nullptr;
   void* p_rate = nullptr; void* p_cdelay = nullptr; void* p_dtr = nullptr; void* p_hist = nullptr;
-  void* p_nw0 = nullptr; void* p_nsum = nullptr; void* p_gbits = nullptr;
+  void* p_nw0 = nullptr; void* p_nsum = nullptr; void* p_gbits = nullptr; void* p_bE = nullptr;
   const int dense = n->dense() ? 1 : 0;
   const int norm = n->weight_norm != SPK_NORM_OFF ? 1 : 0;
   const std::vector<size_t> sizes =
@@ -746,7 +747,7 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   void** dsts[] = {&p_rowptr, &p_entries, &p_cscptr, &p_csc,   &p_V,     &p_last,   &p_gtr,  &p_ring,
                    &p_innext, &p_rates,   &p_post,   &p_pre,   &p_pub,   &p_bA,     &p_bP,   &p_ckeys,
                    &p_cstamp, &p_spk,     &p_ctl,    &p_abort, &p_dd,    &p_map,  &p_rate,
-                   &p_cdelay, &p_dtr,     &p_hist,   &p_nw0,   &p_nsum,  &p_gbits};
+                   &p_cdelay, &p_dtr,     &p_hist,   &p_nw0,   &p_nsum,  &p_gbits, &p_bE};
   std::vector<Part> parts;
   for (size_t i = 0; i < sizes.size(); ++i) parts.push_back(Part{dsts[i], sizes[i]});
   const size_t total = arena_total(sizes);
@@ -835,6 +836,7 @@ static int setup_device(spk_net* n, const ModelSpec& m, int64_t n_csc, const int
   h.seed = m.seed;
   h.rate_counts = (int*)p_rate;
   h.gbits = (uint32_t*)p_gbits;
+  h.bitsE = (uint32_t*)p_bE;
   h.stdp_rule = n->stdp_rule;
   if (dense) {
     h.H = B - 2 * n->G;  // D_max + 1
@@ -2605,6 +2607,7 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
         SPK_CUDA(cudaStreamSynchronize(n->stream));
         SPK_CUDA(cudaMemset(n->hd.bitsA, 0, sizeof(uint32_t) * 2 * (size_t)n->hd.n_words));
         SPK_CUDA(cudaMemset(n->hd.bitsP, 0, sizeof(uint32_t) * 2 * (size_t)n->hd.n_words));
+        SPK_CUDA(cudaMemset(n->hd.bitsE, 0, sizeof(uint32_t) * (size_t)n->hd.n_words));
       }
       SPK_CUDA(cudaMemcpy(b->dd, b->hds.data(), sizeof(NetDev) * b->hds.size(), cudaMemcpyHostToDevice));
       const int prop_smem = bulk_prop_layout(b->win_words, b->ts_max).total * 4;

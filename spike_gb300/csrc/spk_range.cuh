@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(RANGE_THREADS, SPK_RANGE_MINB)
           if (st.stdp_run) {
             const int q = (int)(en[u].x & 0xffffu);
             ptv[u] = d.post_trace[p0 + q];
-            pw[u] = d.bitsP[(KL + p0 + q) >> 5];  // post events
+            pw[u] = d.bitsE[(KL + p0 + q) >> 5];  // post events
           }
         }
       }

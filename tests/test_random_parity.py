@@ -105,7 +105,7 @@ def random_case(seed: int):
     return d, sched, actions, n, n_in, L, plastic
 
 
-@pytest.mark.parametrize("seed", range(18))
+@pytest.mark.parametrize("seed", range(48))
 def test_random_network_and_runs(seed):
     d, sched, actions, n, n_in, L, plastic = random_case(seed)
     o = OracleNet(d.desc)
