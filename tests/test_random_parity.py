@@ -5,7 +5,7 @@ Each case draws from its seed:
 - the synapse kind: voltage, current or conductance, with 1-3 labels;
 - 60-900 LIF neurons in one to three groups, 0-300 Poisson inputs;
 - delays d_min..d_max, d_min in {1, 2, 3} (the timestep grouping), d_max up to 20;
-- with d_min = 1, weight-dependent STDP on the excitatory and input synapses half the time;
+- with d_min = 1, weight-dependent STDP on the excitatory and input synapses (60 %);
 - a schedule: the planner's, or 2-8 warps of 32-128 posts over as many CTAs as cover the
   network with launches of 7-1000 timesteps, or (bulk mode) one warp per 512-post range;
 - four to seven actions: run(seconds) with seconds/dt fractions below and above one half
@@ -35,7 +35,7 @@ def random_case(seed: int):
     n_in = int(rng.choice([0, int(rng.integers(20, 300))]))
     d_min = int(rng.choice([1, 1, 2, 3]))
     d_max = int(rng.integers(d_min, 21))
-    plastic = d_min == 1 and kind == N.SPK_SYN_VOLTAGE and bool(rng.integers(0, 2))
+    plastic = d_min == 1 and rng.random() < 0.6
     L = 1 if kind == N.SPK_SYN_VOLTAGE else int(rng.integers(1, 4))
     n_groups = int(rng.integers(1, 4))
     cuts = np.sort(rng.choice(np.arange(1, n), n_groups - 1, replace=False)) if n_groups > 1 else np.array([], int)
