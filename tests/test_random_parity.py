@@ -126,3 +126,27 @@ def test_random_network_and_runs(seed):
     assert net.synchronize() == 0
     assert net.current_time() == o.current_time()
     assert_same(net, o, n, n_in, L, weights=plastic, tag=f"seed {seed} {net.schedule()} {actions}")
+
+
+@pytest.mark.parametrize("mode", [N.SPK_BATCH_BULK, N.SPK_BATCH_WAVES])
+@pytest.mark.parametrize("seed", range(100, 108))
+def test_random_batches(seed, mode):
+    """Batches of two to five random networks (planner schedules at four warps
+    per CTA, so that waves mode can take them), each run its own whole-group
+    step counts and plasticity switch twice, every network against its oracle."""
+    from spike_gb300 import Batch
+    rng = np.random.default_rng(seed)
+    cases = [random_case(seed * 10 + i) for i in range(int(rng.integers(2, 6)))]
+    nets = [Net.from_desc(c[0].desc, schedule(4, 0, 0, 0)) for c in cases]
+    orcs = [OracleNet(c[0].desc) for c in cases]
+    b = Batch(nets)
+    b.set_mode(mode)
+    for _ in range(2):
+        steps = [int(o.timestep_grouping()) * int(rng.integers(20, 200)) for o in orcs]
+        plastic = [bool(rng.integers(0, 4)) for _ in orcs]
+        b.run_steps_each(steps, plastic)
+        for o, k, pl in zip(orcs, steps, plastic):
+            o.run_steps(k, pl)
+    assert b.synchronize() == 0
+    for (d, _, _, n, n_in, L, pl), net, o in zip(cases, nets, orcs):
+        assert_same(net, o, n, n_in, L, weights=pl, tag=f"batch seed {seed} mode {mode}")
