@@ -8,10 +8,14 @@ Each case draws from its seed:
 - with d_min = 1, weight-dependent STDP on the excitatory and input synapses (60 %);
 - a schedule: the planner's, or 2-8 warps of 32-128 posts over as many CTAs as cover the
   network with launches of 7-1000 timesteps, or (bulk mode) one warp per 512-post range;
+- the rule: weight-dependent STDP, sometimes with the weight normalisation, or the Evans,
+  inhibitory or custom rule (bulk mode);
+- two stimuli when there are inputs;
 - four to seven actions: run(seconds) with seconds/dt fractions below and above one half
   (where the next run starts, the timestep index then repeats or skips one, and the
   reference's active lists deliver the last group again), run_steps of whole groups,
-  plasticity switched off for some runs, reset_time or reset_state between some.
+  plasticity switched off for some runs, reset_time or reset_state, a stimulus switch, a
+  snapshot restored into a fresh network that carries on.
 """
 import numpy as np
 import pytest
@@ -36,6 +40,13 @@ def random_case(seed: int):
     d_min = int(rng.choice([1, 1, 2, 3]))
     d_max = int(rng.integers(d_min, 21))
     plastic = d_min == 1 and rng.random() < 0.6
+    rule, norm = N.SPK_STDP_WEIGHT_DEPENDENT, N.SPK_NORM_OFF
+    if plastic:
+        r = rng.random()
+        if r < 0.3:
+            rule = [N.SPK_STDP_EVANS, N.SPK_STDP_INHIBITORY, N.SPK_STDP_CUSTOM][int(rng.integers(0, 3))]
+        elif r < 0.45:
+            norm = [N.SPK_NORM_AFTER_RULE, N.SPK_NORM_BEFORE_RULE][int(rng.integers(0, 2))]
     L = 1 if kind == N.SPK_SYN_VOLTAGE else int(rng.integers(1, 4))
     n_groups = int(rng.integers(1, 4))
     cuts = np.sort(rng.choice(np.arange(1, n), n_groups - 1, replace=False)) if n_groups > 1 else np.array([], int)
@@ -72,11 +83,13 @@ def random_case(seed: int):
         delay[0] = d_min
     tau = list(rng.uniform(0.003, 0.012, L))
     vhat = [0.0 if l != L - 1 or L == 1 else -0.08 for l in range(L)]
+    from test_stdp_rules import CUSTOM, EVANS, VOGELS
+    sp = {N.SPK_STDP_EVANS: EVANS, N.SPK_STDP_INHIBITORY: VOGELS, N.SPK_STDP_CUSTOM: CUSTOM}.get(rule, STDP)
     d = descs.Desc(kind=kind, groups=groups, refractory=float(rng.uniform(0.001, 0.003)), i_bg=i_bg,
-                   n_inputs=n_in, rates=rng.uniform(10, 60, n_in) if n_in else None, n_labels=L, label_tau=tau,
+                   n_inputs=n_in, rates=rng.uniform(10, 60, 2 * n_in) if n_in else None, n_labels=L, label_tau=tau,
                    label_vhat=vhat, pre=pre, post=post, weight=w, delay=delay, label=label,
-                   plastic=exc.astype(int) if plastic else None, stdp=STDP if plastic else None, seed=seed,
-                   record_inputs=bool(rng.integers(0, 2)))
+                   plastic=exc.astype(int) if plastic else None, stdp=sp if plastic else None, seed=seed,
+                   record_inputs=bool(rng.integers(0, 2)), stdp_rule=rule, weight_norm=norm)
     # schedule
     choice = int(rng.integers(0, 3))
     if choice == 0:
@@ -91,7 +104,13 @@ def random_case(seed: int):
     # actions
     actions = []
     for _ in range(int(rng.integers(4, 8))):
-        a = int(rng.integers(0, 10))
+        a = int(rng.integers(0, 12))
+        if a == 10 and n_in:
+            actions.append(("stimulus", int(rng.integers(0, 2))))
+            continue
+        if a >= 10:
+            actions.append(("snapshot",))
+            continue
         if a < 6:
             steps = int(rng.integers(20, 300))
             frac = float(rng.choice([0.2, 0.35, 0.65, 0.8]))
@@ -111,7 +130,20 @@ def test_random_network_and_runs(seed):
     o = OracleNet(d.desc)
     net = Net.from_desc(d.desc, sched)
     for act in actions:
-        if act[0] == "run":
+        if act[0] == "stimulus":
+            net.select_stimulus(act[1])
+            o.select_stimulus(act[1])
+        elif act[0] == "snapshot":
+            # the spike store is not part of a snapshot: both stores start afresh
+            assert net.synchronize() == 0
+            net.clear_spikes()
+            o.clear_spikes()
+            snap = net.snapshot()
+            fresh = Net.from_desc(d.desc, sched)
+            fresh.restore(snap)
+            net.close()
+            net = fresh
+        elif act[0] == "run":
             net.run(act[1], act[2])
             o.run(act[1], act[2])
         elif act[0] == "steps":
@@ -140,6 +172,13 @@ def test_random_batches(seed, mode):
     nets = [Net.from_desc(c[0].desc, schedule(4, 0, 0, 0)) for c in cases]
     orcs = [OracleNet(c[0].desc) for c in cases]
     b = Batch(nets)
+    bulk_only = any(c[0].desc.stdp_rule != N.SPK_STDP_WEIGHT_DEPENDENT or c[0].desc.weight_norm != N.SPK_NORM_OFF
+                    for c in cases)
+    if mode == N.SPK_BATCH_WAVES and bulk_only:
+        # the per-synapse-trace rules and the normalisation run in bulk mode only: refused
+        with pytest.raises(N.SpikeError):
+            b.set_mode(mode)
+        mode = N.SPK_BATCH_BULK
     b.set_mode(mode)
     for _ in range(2):
         steps = [int(o.timestep_grouping()) * int(rng.integers(20, 200)) for o in orcs]
