@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
       const unsigned evword = st.stdp_run ? __ballot_sync(FULL, ev) : 0u;
       const unsigned peword = st.stdp_run ? __ballot_sync(FULL, pe) : 0u;
       if (lane == 0) {
-        // delivered keys: the spikes, and at a repeating run start the carried keys
+        // delivered keys: the spikes, and in a repeating group the carried keys
         uint32_t* gb = d.gbits + (size_t)st.g * d.n_words + bw.word + u;
         d.bitsA[bw.word + u] = word | (st.rep ? *gb : 0u);
         d.bitsP[bw.word + u] = peword;

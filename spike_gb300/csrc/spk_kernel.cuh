@@ -366,9 +366,9 @@ __global__ void __launch_bounds__(512, 1)
             // (Spike/Backend/CUDA/Plasticity/WeightDependentSTDPPlasticity.cu:113-117):
             // an event as the postsynaptic neuron for g >= 0, as the
             // presynaptic one for 0 <= g < G (g >= G is negated).  That is
-            // this step's spike, or the last step's at a run start that
-            // repeats its timestep index, or (post only) a spike later than
-            // the clock after reset_time.  A spike older than a step cannot
+            // this step's spike, or the last step's where the timestep index
+            // repeats, or (post only) a spike later than the clock after
+            // reset_time.  A spike older than a step cannot
             // round to 0: no division then.
             const float lag = last_s[li] - t;
             const int gq = (spk || lag < -dt) ? (spk ? 0 : -1) : (int)roundf(lag / dt);
@@ -452,9 +452,9 @@ __global__ void __launch_bounds__(512, 1)
     // ---- publish: the CTA's active keys, then one stamp word per CTA ---------
     __syncwarp();
     {
-      // This substep's spike words, kept for a later run that repeats the
-      // group's index; at such a repeat (rep) the last group's words are the
-      // carried keys delivered again in this step.
+      // This substep's spike words are kept for a later group of the same
+      // index parity; in such a repeating group (rep) the last group's words
+      // are the carried keys delivered again in this substep.
       const int nl = TS >> 5, ni = ITS >> 5;
       if (gw_n <= 32) {
         // one word per lane (the common case): pointer set up once per launch;
@@ -492,9 +492,9 @@ __global__ void __launch_bounds__(512, 1)
     if (threadIdx.x == 0) s_nsp = 0;  // read by every thread in the previous step's afferent pass
     // The CTA's ballot words in key order: inputs of warps 0..W-1, then neurons
     // of warps 0..W-1 (x-th word: bits a = delivered keys, p = STDP pre
-    // events, sp = spikes of the step, first key).  a is sp but at the first
-    // step of a plastic network's run that repeats the last group's index,
-    // where the carried keys are delivered again.
+    // events, sp = spikes of the step, first key).  a is sp but in a group
+    // that repeats the last group step's index parity, where the carried keys
+    // are delivered again.
     const int nw_in = W * (ITS >> 5), nw_all = W * ((ITS >> 5) + (TS >> 5));
     // A key both carried and spiking is listed (and delivered) once.
     auto cta_word = [&](const int x, uint32_t& a, uint32_t& p, uint32_t& sp, uint32_t& wkey) {
