@@ -239,10 +239,11 @@ int spk_net_begin_run(spk_net* net, int64_t n_steps, int32_t plasticity_on);
  * group index T/G has the parity of the last group step's (the timestep index
  * repeats at a run start when seconds/dt has a fraction below one half, as
  * for run(0.1) at dt = 1e-4; a grouped network skips one) delivers the last
- * group's spikes again to its own first slots before its own.  Were the list
- * to hold two groups (a one-group run that began so, then another such
- * start), SPK_ERR_UNSUPPORTED is raised and only the last group is delivered
- * again. */
+ * group's spikes again in its substeps, merged with their own (a key in both
+ * once).  The same happens within a run where t/dt falls within rounding of
+ * a half.  Were the list to hold two or more earlier groups (two such
+ * repeats in a row), SPK_ERR_UNSUPPORTED is raised and only the last group is
+ * delivered again. */
 int spk_net_synchronize(spk_net* net);
 int spk_net_current_time(const spk_net* net, float* seconds);
 /* SpikingModel::timestep_grouping (Spike/Models/SpikingModel.cpp:98): the

@@ -32,10 +32,10 @@ pytestmark = pytest.mark.gpu
 STDP = STDPParams(a_plus=0.005, a_minus=0.00525, tau_plus=0.02, tau_minus=0.02, lambda_=1.0, alpha=1.0, w_max=1.0)
 
 
-def random_case(seed: int):
+def random_case(seed: int, n_range=(60, 900)):
     rng = np.random.default_rng(seed)
     kind = [N.SPK_SYN_VOLTAGE, N.SPK_SYN_CURRENT, N.SPK_SYN_CONDUCTANCE][seed % 3]
-    n = int(rng.integers(60, 900))
+    n = int(rng.integers(*n_range))
     n_in = int(rng.choice([0, int(rng.integers(20, 300))]))
     d_min = int(rng.choice([1, 1, 2, 3]))
     d_max = int(rng.integers(d_min, 21))
@@ -60,8 +60,9 @@ def random_case(seed: int):
         i_bg = float(rng.uniform(0.021, 0.03))
     groups = [dict(count=int(c), tau_m=float(rng.uniform(0.01, 0.03)), R=1e8, v_init_lo=lif["v0"],
                    v_init_hi=lif["theta"], **lif) for c in counts]
-    # connectivity: Bernoulli p, multapses allowed, inputs at p_in
-    p = float(rng.uniform(0.02, 0.1))
+    # connectivity: Bernoulli p (about 40-90 afferents for the large cases), multapses
+    # allowed, inputs at p_in
+    p = float(rng.uniform(0.02, 0.1)) if n < 1000 else float(rng.uniform(40, 90)) / n
     pre, post = [], []
     for q in range(n):
         k_rec, k_in = rng.binomial(n, p), rng.binomial(n_in, 2 * p) if n_in else 0
@@ -124,16 +125,33 @@ def random_case(seed: int):
     return d, sched, actions, n, n_in, L, plastic
 
 
-@pytest.mark.parametrize("seed", range(48))
-def test_random_network_and_runs(seed):
-    d, sched, actions, n, n_in, L, plastic = random_case(seed)
+@pytest.mark.parametrize("seed,n_range", [(s, (60, 900)) for s in range(48)] +
+                         [(s, (3000, 12000)) for s in range(200, 206)])
+def test_random_network_and_runs(seed, n_range):
+    d, sched, actions, n, n_in, L, plastic = random_case(seed, n_range)
     o = OracleNet(d.desc)
     net = Net.from_desc(d.desc, sched)
+    # Where t/dt stays within rounding of a half, the timestep index can repeat
+    # and skip in turn within a run, and the reference's active list then holds
+    # more than one earlier group: the engine and the oracle deliver the last
+    # one and report SPK_ERR_UNSUPPORTED (sticky until reset_state).
+    unsupported = False
+
+    def oracle(call, *args):
+        nonlocal unsupported
+        try:
+            call(*args)
+        except RuntimeError as e:
+            assert f"status {N.SPK_ERR_UNSUPPORTED}" in str(e), e
+            unsupported = True
+
     for act in actions:
         if act[0] == "stimulus":
             net.select_stimulus(act[1])
             o.select_stimulus(act[1])
         elif act[0] == "snapshot":
+            if unsupported:
+                continue  # a restore clears the device status; the oracle's stays
             # the spike store is not part of a snapshot: both stores start afresh
             assert net.synchronize() == 0
             net.clear_spikes()
@@ -145,17 +163,19 @@ def test_random_network_and_runs(seed):
             net = fresh
         elif act[0] == "run":
             net.run(act[1], act[2])
-            o.run(act[1], act[2])
+            oracle(o.run, act[1], act[2])
         elif act[0] == "steps":
             net.run_steps(act[1], act[2])
-            o.run_steps(act[1], act[2])
+            oracle(o.run_steps, act[1], act[2])
         elif act[0] == "reset_time":
             net.reset_time()
             o.reset_time()
         else:
+            assert net.synchronize() == (N.SPK_ERR_UNSUPPORTED if unsupported else 0)
             net.reset_state()
             o.reset_state()
-    assert net.synchronize() == 0
+            unsupported = False
+    assert net.synchronize() == (N.SPK_ERR_UNSUPPORTED if unsupported else 0)
     assert net.current_time() == o.current_time()
     assert_same(net, o, n, n_in, L, weights=plastic, tag=f"seed {seed} {net.schedule()} {actions}")
 
