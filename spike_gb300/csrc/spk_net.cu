@@ -2384,6 +2384,27 @@ static int bulk_run_block(spk_batch* b) {
   return SPK_OK;
 }
 
+// The batch holds its own copies of the networks' descriptors.  Two fields of a
+// network's descriptor change after it joins a batch: the rates of the selected
+// stimulus (select_stimulus, restore) and the wait limit.  Bring the copies up to
+// date before a launch, on the batch stream, behind the launches already queued.
+static int refresh_descs(spk_batch* b) {
+  bool changed = false;
+  for (size_t i = 0; i < b->nets.size(); ++i) {
+    const NetDev& src = b->nets[i]->hd;
+    NetDev& dst = b->hds[i];
+    if (dst.rates != src.rates || dst.poll_ns != src.poll_ns) {
+      dst.rates = src.rates;
+      dst.poll_ns = src.poll_ns;
+      changed = true;
+    }
+  }
+  if (changed)
+    SPK_CUDA(cudaMemcpyAsync(b->dd, b->hds.data(), sizeof(NetDev) * b->hds.size(), cudaMemcpyHostToDevice,
+                             b->stream));
+  return SPK_OK;
+}
+
 }  // namespace spk
 
 int spk_batch_run_steps_each(spk_batch* b, const int64_t* n_steps, const int32_t* plasticity_on) {
@@ -2402,6 +2423,7 @@ int spk_batch_run_steps_each(spk_batch* b, const int64_t* n_steps, const int32_t
     const int plastic = (!plasticity_on || plasticity_on[i]) && n->has_stdp;
     if (int rc = begin_run_on(n, b->stream, n->current_time, n_steps[i], plastic ? 1 : 0)) return rc;
   }
+  if (int rc = refresh_descs(b)) return rc;
   // networks that finish early leave their launches at once (no steps left)
   const int64_t blocks = (most + b->K - 1) / b->K;
   for (int64_t blk = 0; blk < blocks; ++blk) {
@@ -2628,6 +2650,7 @@ int spk_batch_step_block(spk_batch* b) {
   if (!b) return SPK_ERR_INVALID;
   // order the batch stream after each network's pending work (its run set-up)
   for (spk_net* n : b->nets) SPK_CUDA(cudaStreamSynchronize(n->stream));
+  if (int rc = refresh_descs(b)) return rc;
   if (b->mode == SPK_BATCH_BULK) {
     const int rc = bulk_run_block(b);
     if (rc) return rc;
