@@ -152,12 +152,14 @@ class CallerNet:
         self.step(steps, plastic)
         self.time = np.float32(start + np.float32(seconds))
 
-    def compare(self, ref: Net, n_synapses: int, tag: str):
+    def compare(self, ref: Net, n_synapses: int, tag: str, status: int = 0):
+        """Everything the two entry points hold, and their device status
+        (0, or SPK_ERR_UNSUPPORTED after an active list of two carried groups)."""
         torch.cuda.synchronize()
-        assert ref.synchronize() == 0
+        assert ref.synchronize() == status
         rs = self.t["run_state"].cpu().numpy()
         count, events = int(rs[8:10].view(np.uint64)[0]), int(rs[10:12].view(np.uint64)[0])
-        assert int(rs[12]) == 0, f"{tag}: device status {int(rs[12])}"
+        assert int(rs[12]) == status, f"{tag}: device status {int(rs[12])}"
         assert events == ref.events(), tag
         store = self.t["spikes"][:2 * count].cpu().numpy().reshape(-1, 2)
         keys, tbits = store[:, 0].astype(np.int64), store[:, 1].copy().view(np.float32)
@@ -290,4 +292,42 @@ def test_noalloc_run_boundaries_deliver_the_carried_group_again(d_min):
         assert ref.synchronize() == 0
         cn.run_seconds(sec, False)
         cn.compare(ref, d.desc.n_synapses, f"run {i + 1} d_min={d_min}")
+    ref.close()
+
+
+@pytest.mark.parametrize("seed", range(40, 52))
+def test_noalloc_random_networks(seed):
+    """Seeded networks of the random parity test whose plasticity the
+    persistent kernel runs (the weight-dependent rule, or none), under the
+    planner's schedule, through that test's random run sequences: run(seconds)
+    with fractions that repeat or skip the timestep index, whole-group
+    run_steps, plasticity switched off, reset_time.  reset_state, stimulus
+    switches and snapshots have no allocation-free form and are skipped."""
+    from test_random_parity import random_case
+    for s in range(seed * 100, seed * 100 + 100):  # even seeds: a plastic network
+        d, _, actions, n, n_in, L, plastic = random_case(s)
+        if d.desc.stdp_rule == N.SPK_STDP_WEIGHT_DEPENDENT and d.desc.weight_norm == N.SPK_NORM_OFF and \
+                plastic == (seed % 2 == 0):
+            break
+    probe = Net.from_desc(d.desc, None)
+    sc = probe.schedule()
+    probe.close()
+    W, TS, ctas = sc["warps_per_cta"], sc["tile_posts"], sc["ctas"]
+    ref = Net.from_desc(d.desc, schedule(W, TS, ctas, 0))
+    cn = CallerNet(d.desc, W, TS, ctas, ref)
+    for i, act in enumerate(actions):
+        if act[0] == "run":
+            ref.run(act[1], act[2])
+            assert ref.synchronize() in (0, N.SPK_ERR_UNSUPPORTED)
+            cn.run_seconds(act[1], act[2])
+        elif act[0] == "steps":
+            ref.run_steps(act[1], act[2])
+            assert ref.synchronize() in (0, N.SPK_ERR_UNSUPPORTED)
+            cn.step(act[1], act[2])
+        elif act[0] == "reset_time":
+            ref.reset_time()
+            cn.time = np.float32(0.0)
+        else:
+            continue
+        cn.compare(ref, d.desc.n_synapses, f"seed {s} {sc} action {i} of {actions}", ref.synchronize())
     ref.close()
