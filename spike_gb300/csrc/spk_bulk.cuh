@@ -120,7 +120,10 @@ __device__ __forceinline__ RunCtl load_ctl(const RunCtl* p) {
 // dependent global loads are its state loads, all issued before any update.
 // Words of padding keys are never written: they stay zero from set-up.
 #ifndef SPK_BULK_NEUR_MINB
-#define SPK_BULK_NEUR_MINB 6
+#define SPK_BULK_NEUR_MINB 4
+#endif
+#ifndef SPK_BULK_NEUR_CTAS_PER_SM
+#define SPK_BULK_NEUR_CTAS_PER_SM 8
 #endif
 constexpr int BULK_WPW = SPK_BULK_WPW;
 #ifndef SPK_BULK_NEUR_WARPS
@@ -186,33 +189,10 @@ __device__ __forceinline__ bool bulk_lif(const NetDev& d, const BulkStep& st, in
   return spk;
 }
 
-__global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk_neurons_kernel(const NetDev* __restrict__ nets,
-                                                                         const BulkBlock* __restrict__ blocks,
-                                                                         int s, int* item_count) {
-  __shared__ __align__(16) NetDev sd;
-  __shared__ RunCtl sctl;
-  __shared__ BulkStep sst;
-  static_assert(sizeof(NetDev) % 4 == 0, "descriptor copied as words");
+// One block's words of one network, with the network's descriptor and the
+// step's times in shared memory (no barrier inside: warps return early).
+__device__ __forceinline__ void bulk_neurons_block(const NetDev& d, const BulkStep st, const BulkBlock& bb) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const BulkBlock bb = blocks[blockIdx.x];
-  {
-    const uint32_t* src = (const uint32_t*)(nets + bb.net);
-    uint32_t* dst = (uint32_t*)&sd;
-    for (int i = threadIdx.x; i < (int)(sizeof(NetDev) / 4); i += blockDim.x) dst[i] = __ldg(src + i);
-    if (threadIdx.x == 0) {
-      // the step's times once per CTA (two float divisions), from the global descriptor
-      sctl = load_ctl(bb.ctl);
-      BulkStep b = bulk_step(nets[bb.net], sctl, s);
-      if (b.live) b.rep = bulk_rep(nets[bb.net], sctl, b);
-      sst = b;
-    }
-  }
-  pdl_wait_then_release();
-  if (blockIdx.x == 0 && threadIdx.x == 0) *item_count = 0;  // the afferent-pass list of this step
-  __syncthreads();
-  const NetDev& d = sd;
-  const BulkStep st = sst;
-  if (!st.live) return;
   const int w0 = w * BULK_WPW;
   if (w0 >= bb.count) return;
   struct {
@@ -346,6 +326,54 @@ __global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB) bulk
       }
     }
   }
+}
+
+// The network's descriptor and the step's times (two float divisions, thread 0)
+// into shared memory.
+__device__ __forceinline__ void bulk_load_net(NetDev& sd, BulkStep& sst, const NetDev* __restrict__ nets,
+                                              const BulkBlock& bb, int s) {
+  const uint32_t* src = (const uint32_t*)(nets + bb.net);
+  uint32_t* dst = (uint32_t*)&sd;
+  for (int i = threadIdx.x; i < (int)(sizeof(NetDev) / 4); i += blockDim.x) dst[i] = __ldg(src + i);
+  if (threadIdx.x == 0) {
+    const RunCtl c = load_ctl(bb.ctl);
+    BulkStep b = bulk_step(nets[bb.net], c, s);
+    if (b.live) b.rep = bulk_rep(nets[bb.net], c, b);
+    sst = b;
+  }
+}
+
+// CTA c takes the blocks [c*n/grid, (c+1)*n/grid) in turn.  Blocks are listed
+// network by network, so consecutive blocks mostly share a network, whose
+// descriptor and step the CTA loads once; with grid = n every CTA takes one
+// block.
+__global__ void __launch_bounds__(BULK_NEUR_WARPS * 32, SPK_BULK_NEUR_MINB)
+    bulk_neurons_kernel(const NetDev* __restrict__ nets, const BulkBlock* __restrict__ blocks, int n_blocks, int s,
+                        int* item_count) {
+  __shared__ __align__(16) NetDev sd;
+  __shared__ BulkStep sst;
+  static_assert(sizeof(NetDev) % 4 == 0, "descriptor copied as words");
+  const int b0 = (int)((long long)blockIdx.x * n_blocks / gridDim.x);
+  const int b1 = (int)((long long)(blockIdx.x + 1) * n_blocks / gridDim.x);
+  int cur = -1;
+  for (int bi = b0; bi < b1; ++bi) {
+    const BulkBlock bb = blocks[bi];
+    if (bb.net != cur) {
+      if (cur >= 0) {
+        __syncthreads();  // every warp is done with the previous network's descriptor
+      }
+      bulk_load_net(sd, sst, nets, bb, s);
+      if (cur < 0) {
+        // the first descriptor (static data) is read before the wait
+        pdl_wait_then_release();
+        if (blockIdx.x == 0 && threadIdx.x == 0) *item_count = 0;  // the afferent-pass list of this step
+      }
+      __syncthreads();
+      cur = bb.net;
+    }
+    if (sst.live) bulk_neurons_block(sd, sst, bb);
+  }
+  if (cur < 0) pdl_wait_then_release();
 }
 
 // ---- timestep part 2: the step's active keys and the spike store ----------------------

@@ -118,6 +118,23 @@ static int device_info(DeviceInfo* di) {
   return SPK_OK;
 }
 
+// The maximum dynamic shared memory of a kernel function holds in the whole
+// process, not for one batch: every batch sets the device's limit (less the
+// kernel's static shared memory), so that none lowers another's.  *limit gets
+// the smallest limit of the kernels set so far.
+template <typename K>
+static int allow_all_dynamic_smem(K kernel, int* limit) {
+  int dev = 0, optin = 0;
+  SPK_CUDA(cudaGetDevice(&dev));
+  SPK_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  SPK_CUDA(cudaFuncGetAttributes(&fa, kernel));
+  const int dyn = optin - (int)fa.sharedSizeBytes;
+  SPK_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn));
+  *limit = *limit ? std::min(*limit, dyn) : dyn;
+  return SPK_OK;
+}
+
 // A launch that may begin while the stream's previous kernel drains (the
 // kernel waits for it with griddepcontrol.wait before touching its outputs).
 template <typename... P, typename... A>
@@ -2260,6 +2277,8 @@ static int bulk_launch_block(spk_batch* b, KernelTimer* timer = nullptr) {
   if (rc0) return rc0;
   const bool split = (b->norm_slots & 4) != 0;
   const int item_grid = std::min((b->n_dense_items + 7) / 8, di.sms * 8);
+  // the neurons kernel: one resident wave of CTAs, each taking a run of blocks
+  const int neur_grid = std::min(b->blocks_total, di.sms * SPK_BULK_NEUR_CTAS_PER_SM);
   int per_step = 0;
 #define T_BEGIN(kind, st)                         \
   do {                                            \
@@ -2278,8 +2297,9 @@ static int bulk_launch_block(spk_batch* b, KernelTimer* timer = nullptr) {
   for (int s = 0; s < b->K; ++s) {
     per_step = 0;
     T_BEGIN(SPK_KERNEL_NEURONS, b->stream);
-    SPK_CUDA(launch_overlapped(bulk_neurons_kernel, b->blocks_total, BULK_NEUR_WARPS * 32, 0, b->stream,
-                               (const NetDev*)b->dd, (const BulkBlock*)b->dblocks, s, b->item_count));
+    SPK_CUDA(launch_overlapped(bulk_neurons_kernel, neur_grid, BULK_NEUR_WARPS * 32, 0, b->stream,
+                               (const NetDev*)b->dd, (const BulkBlock*)b->dblocks, b->blocks_total, s,
+                               b->item_count));
     T_END(b->stream);
     T_BEGIN(SPK_KERNEL_LIST, b->stream);
     SPK_CUDA(launch_overlapped(bulk_list_kernel, n, BULK_LIST_THREADS, 0, b->stream, (const NetDev*)b->dd, s,
@@ -2633,13 +2653,19 @@ int spk_batch_set_mode(spk_batch* b, int32_t mode) {
       }
       SPK_CUDA(cudaMemcpy(b->dd, b->hds.data(), sizeof(NetDev) * b->hds.size(), cudaMemcpyHostToDevice));
       const int prop_smem = bulk_prop_layout(b->win_words, b->ts_max).total * 4;
-      SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, prop_smem));
-      SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, prop_smem));
-      SPK_CUDA(cudaFuncSetAttribute(bulk_prop_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, prop_smem));
       const int range_smem = (int)range_smem_bytes(b->range_smem);
-      SPK_CUDA(cudaFuncSetAttribute(bulk_range_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, range_smem));
-      SPK_CUDA(cudaFuncSetAttribute(bulk_range_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, range_smem));
-      SPK_CUDA(cudaFuncSetAttribute(bulk_range_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, range_smem));
+      int prop_max = 0, range_max = 0;
+      if (int rc = allow_all_dynamic_smem(bulk_prop_kernel<0>, &prop_max)) return rc;
+      if (int rc = allow_all_dynamic_smem(bulk_prop_kernel<1>, &prop_max)) return rc;
+      if (int rc = allow_all_dynamic_smem(bulk_prop_kernel<2>, &prop_max)) return rc;
+      if (int rc = allow_all_dynamic_smem(bulk_range_kernel<0>, &range_max)) return rc;
+      if (int rc = allow_all_dynamic_smem(bulk_range_kernel<1>, &range_max)) return rc;
+      if (int rc = allow_all_dynamic_smem(bulk_range_kernel<2>, &range_max)) return rc;
+      if ((b->pblocks_total && prop_smem > prop_max) || (b->rblocks_total && range_smem > range_max)) {
+        set_error("bulk mode: propagation needs %d / %d B of shared memory per CTA, the device allows %d / %d",
+                  prop_smem, range_smem, prop_max, range_max);
+        return SPK_ERR_INVALID;
+      }
     }
     b->mode = mode;
     return SPK_OK;

@@ -190,3 +190,27 @@ def test_bulk_mode_key_lists_longer_than_one_staged_chunk():
     assert gens[0].desc.n_inputs * 2000.0 * 1e-4 > 1024
     assert sum(len(x.spikes()[0]) for x in batched) > 1000
     b.close()
+
+
+def test_batches_keep_their_shared_memory_limits():
+    """A kernel function's shared-memory limit holds in the whole process.  A
+    batch set up after another, whose propagation needs less shared memory
+    (delay 1 against delays 1-20), must not lower the first batch's limit:
+    both batches run, each equal to its oracle."""
+    import descs
+    from engine_checks import assert_same
+    from oracle import OracleNet
+    from spike_gb300 import schedule
+    deep = descs.random_voltage_net(n=300, n_in=100, d_max=20, seed=21)
+    shallow = descs.random_voltage_net(n=200, n_in=50, d_max=1, seed=22)
+    a_net, b_net = Net.from_desc(deep.desc, schedule(8, 64, 0, 0)), Net.from_desc(shallow.desc, schedule(8, 64, 0, 0))
+    a, b = Batch([a_net]), Batch([b_net])
+    a.set_mode(N.SPK_BATCH_BULK)
+    b.set_mode(N.SPK_BATCH_BULK)
+    a.run_steps(200, True)
+    b.run_steps(200, True)
+    assert a.synchronize() == 0 and b.synchronize() == 0
+    for d, net, n, n_in in ((deep, a_net, 300, 100), (shallow, b_net, 200, 50)):
+        o = OracleNet(d.desc)
+        o.run_steps(200, True)
+        assert_same(net, o, n, n_in, 1, weights=False, tag=f"d_max {d.desc.n_synapses}")

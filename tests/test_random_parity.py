@@ -228,3 +228,76 @@ def test_random_batches(seed, mode):
     assert b.synchronize() == 0
     for (d, _, _, n, n_in, L, pl), net, o in zip(cases, nets, orcs):
         assert_same(net, o, n, n_in, L, weights=pl, tag=f"batch seed {seed} mode {mode}")
+
+
+@pytest.mark.parametrize("mode", [N.SPK_BATCH_BULK, N.SPK_BATCH_WAVES])
+@pytest.mark.parametrize("seed", list(range(110, 118)) + [4041])  # 4041: a second batch with less shared memory
+def test_random_batch_sequences(seed, mode):
+    """Batch runs interleaved with calls on single networks of the batch: a
+    network run alone (run(seconds) with fractions that repeat or skip the
+    timestep index, or whole-group run_steps), reset_time, reset_state, a
+    stimulus switch, a snapshot restored into the same network.  Every
+    network against its oracle at the end."""
+    from spike_gb300 import Batch
+    rng = np.random.default_rng(seed)
+    cases = [random_case(seed * 10 + i) for i in range(int(rng.integers(2, 5)))]
+    nets = [Net.from_desc(c[0].desc, schedule(4, 0, 0, 0)) for c in cases]
+    orcs = [OracleNet(c[0].desc) for c in cases]
+    b = Batch(nets)
+    if mode == N.SPK_BATCH_WAVES and any(c[0].desc.stdp_rule != N.SPK_STDP_WEIGHT_DEPENDENT or
+                                         c[0].desc.weight_norm != N.SPK_NORM_OFF for c in cases):
+        mode = N.SPK_BATCH_BULK  # the per-synapse-trace rules and the normalisation run in bulk mode only
+    b.set_mode(mode)
+    unsupported = [False] * len(nets)
+
+    def oracle(i, call, *args):
+        try:
+            call(*args)
+        except RuntimeError as e:
+            assert f"status {N.SPK_ERR_UNSUPPORTED}" in str(e), e
+            unsupported[i] = True
+
+    actions = []
+    for _ in range(int(rng.integers(5, 10))):
+        a, i = int(rng.integers(0, 8)), int(rng.integers(0, len(nets)))
+        net, o, n_in = nets[i], orcs[i], cases[i][4]
+        if a <= 2:
+            steps = [int(x.timestep_grouping()) * int(rng.integers(10, 120)) for x in orcs]
+            plastic = [bool(rng.integers(0, 4)) for _ in orcs]
+            actions.append(("batch", steps, plastic))
+            b.run_steps_each(steps, plastic)
+            for j, (x, k, pl) in enumerate(zip(orcs, steps, plastic)):
+                oracle(j, x.run_steps, k, pl)
+        elif a == 3:
+            sec = float(np.float32((int(rng.integers(20, 200)) + float(rng.choice([0.2, 0.35, 0.65, 0.8]))) * 1e-4))
+            pl = bool(rng.integers(0, 4))
+            actions.append(("run", i, sec, pl))
+            net.run(sec, pl)
+            oracle(i, o.run, sec, pl)
+        elif a == 4:
+            actions.append(("reset_time", i))
+            net.reset_time()
+            o.reset_time()
+        elif a == 5:
+            actions.append(("reset_state", i))
+            assert net.synchronize() == (N.SPK_ERR_UNSUPPORTED if unsupported[i] else 0)
+            net.reset_state()
+            o.reset_state()
+            unsupported[i] = False
+        elif a == 6 and n_in:
+            stim = int(rng.integers(0, 2))
+            actions.append(("stimulus", i, stim))
+            net.select_stimulus(stim)
+            o.select_stimulus(stim)
+        elif a == 7 and not unsupported[i]:
+            # the spike store is not part of a snapshot: both stores start afresh
+            actions.append(("restore", i))
+            assert net.synchronize() == 0
+            net.clear_spikes()
+            o.clear_spikes()
+            net.restore(net.snapshot())
+    assert b.synchronize() in (0, N.SPK_ERR_UNSUPPORTED)
+    for i, ((d, _, _, n, n_in, L, pl), net, o) in enumerate(zip(cases, nets, orcs)):
+        assert net.synchronize() == (N.SPK_ERR_UNSUPPORTED if unsupported[i] else 0)
+        assert net.current_time() == o.current_time()
+        assert_same(net, o, n, n_in, L, weights=pl, tag=f"batch seed {seed} mode {mode} net {i} {actions}")
