@@ -137,3 +137,41 @@ def test_served_grouped_jobs():
         np.testing.assert_array_equal(bits(stt), bits(rt))
         ref.close()
     srv.stop()
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_served_random_jobs(seed):
+    """Seeded random job streams: sizes 300-4,000, timestep grouping 1 or 2,
+    the event-driven or the Evans rule or none, random step counts in whole
+    groups, arrivals spread over the first blocks, either server mode and
+    block length.  Every job equals the same network run alone."""
+    rng = np.random.default_rng(500 + seed)
+    mode = [N.SPK_BATCH_WAVES, N.SPK_BATCH_BULK][seed % 2]
+    srv = Server(steps_per_block=int(rng.choice([100, 250, 400])), reserve_bytes=1 << 30, mode=mode)
+    work, ids = [], []
+    for i in range(int(rng.integers(5, 10))):
+        d_min = int(rng.choice([1, 1, 2]))
+        plastic = d_min == 1 and rng.random() < 0.5
+        rule = N.SPK_STDP_EVANS if plastic and rng.random() < 0.3 else N.SPK_STDP_WEIGHT_DEPENDENT
+        gen = sweep_instance(int(np.exp(rng.uniform(np.log(300), np.log(4000)))), float(rng.uniform(0.02, 0.06)),
+                             float(rng.uniform(3, 7)), plastic, seed=1000 * seed + i, d_min=d_min,
+                             d_max=int(rng.integers(d_min, 11)), rule=rule)
+        steps = d_min * int(rng.integers(50, 600))
+        on = bool(rng.integers(0, 4))
+        work.append((gen, steps, on))
+        ids.append(srv.submit(gen, steps, on))
+        time.sleep(float(rng.uniform(0.0, 0.03)))
+    infos = [srv.wait(j, 300.0) for j in ids]
+    assert all(inf.state == N.SPK_JOB_DONE for inf in infos), [(inf.state, inf.error) for inf in infos]
+    for (gen, steps, on), j, inf in zip(work, ids, infos):
+        ref = Net.generate(gen)
+        ref.run_steps(steps, on)
+        assert ref.synchronize() == 0
+        ri, rt = ref.spikes()
+        si, stt = srv.spikes(j)
+        assert inf.steps_done == steps
+        np.testing.assert_array_equal(si, ri)
+        np.testing.assert_array_equal(bits(stt), bits(rt))
+        assert inf.events == ref.events()
+        ref.close()
+    srv.stop()
