@@ -376,6 +376,9 @@ class GenNetwork:
         d.connectivity_seed = connectivity_seed
         d.spike_capacity = spike_capacity
         d.record_inputs = 1 if record_inputs else 0
+        # the descriptor keeps its owner (and the arrays it points into) alive, so
+        # that a descriptor taken from a temporary stays valid
+        d._owner = self
         self.desc = d
 
     def expected_synapses(self) -> float:
@@ -582,6 +585,7 @@ class Model:
     def desc(self) -> N.NetDesc:
         d = N.NetDesc()
         check(lib().spk_model_desc(self.h, C.byref(d)), "spk_model_desc")
+        d._owner = self  # the descriptor points into the model's arrays
         return d
 
     def finalise(self, sched: N.Schedule | None = None) -> Net:

@@ -86,6 +86,9 @@ class Desc:
                 a = np.ascontiguousarray(arr, np.float32)
                 self.keep.append(a)
                 setattr(d, name, a.ctypes.data_as(C.POINTER(C.c_float)))
+        # the descriptor keeps its owner (and the arrays it points into) alive, so
+        # that a descriptor taken from a temporary stays valid
+        d._owner = self
         self.desc = d
 
 

@@ -155,3 +155,86 @@ def test_generated_large_network_statistics():
     np.testing.assert_array_equal(ia, ib)
     np.testing.assert_array_equal(ta.view(np.uint32), tb.view(np.uint32))
     assert a.events() == b.events()
+
+
+def desc_from_gen(gen: GenNetwork, arrays: dict) -> descs.Desc:
+    """The generated network as an explicit descriptor: the generator's
+    constants with the oracle's synapses."""
+    dd = gen.desc
+    groups = [dict(count=g.count, tau_m=g.tau_m, R=g.R, v0=g.v0, vreset=g.vreset, theta=g.theta,
+                   v_init_lo=g.v_init_lo, v_init_hi=g.v_init_hi) for g in (dd.groups[i] for i in range(dd.n_groups))]
+    rates = np.ctypeslib.as_array(dd.input_rates, (dd.n_inputs,)).copy() if dd.n_inputs else None
+    return descs.Desc(kind=dd.synapse_kind, groups=groups, refractory=dd.refractory_period,
+                      i_bg=dd.background_current, n_inputs=dd.n_inputs, rates=rates, pre=arrays["pre"],
+                      post=arrays["post"], weight=arrays["weight"], scale=arrays["scale"], delay=arrays["delay"],
+                      label=arrays["label"], plastic=arrays["plastic"] if dd.has_stdp else None,
+                      stdp=dd.stdp if dd.has_stdp else None, seed=dd.seed, record_inputs=bool(dd.record_inputs),
+                      stdp_rule=dd.stdp_rule)
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_generated_networks(seed):
+    """Seeded random generator inputs: 40-1,500 neurons in one or two groups,
+    0-400 inputs, projections from the inputs and each group onto two post
+    ranges (some left out) with p from 0.001 to 1, delay ranges per projection
+    (the smallest low delay sets the timestep grouping), plastic input
+    synapses under the event-driven or the Evans rule, planner, tile or
+    post-range schedules.  The synapses equal the oracle's restatement of the
+    generator, and runs equal the oracle on those synapses."""
+    from spike_gb300.networks import EVANS_STDP
+    rng = np.random.default_rng(7000 + seed)
+    n = int(rng.integers(40, 1500))
+    n_in = int(rng.choice([0, int(rng.integers(1, 400))]))
+    n_exc = int(rng.integers(max(1, n // 2), n + 1))
+    lif = dict(tau_m=float(rng.uniform(0.01, 0.03)), R=1e8, v0=0.0, vreset=0.0, theta=0.02, v_init_lo=0.0,
+               v_init_hi=0.019)
+    groups = [dict(count=n_exc, **lif)] + ([dict(count=n - n_exc, **lif)] if n > n_exc else [])
+    d_min = int(rng.choice([1, 1, 2, 3]))
+    d_max = d_min + int(rng.integers(0, 12))
+    plastic = d_min == 1 and n_in > 0 and rng.random() < 0.6
+    rule = N.SPK_STDP_EVANS if plastic and rng.random() < 0.5 else N.SPK_STDP_WEIGHT_DEPENDENT
+    cut = int(rng.integers(1, n)) if n > 1 else 1
+    projs = []
+    sources = [(N.SPK_POP_INPUTS, 0, n_in, (0.0, 1.0), 4e-4), (N.SPK_POP_NEURONS, 0, n_exc, (0.0, 1.0), 5e-4),
+               (N.SPK_POP_NEURONS, n_exc, n - n_exc, (-1.0, -0.2), 2e-3)]
+    for pop, start, count, w, scale in sources:
+        if count == 0:
+            continue
+        for ps, pc in ((0, cut), (cut, n - cut)):
+            if pc == 0 or rng.random() < 0.2:
+                continue
+            p = float(rng.choice([rng.uniform(0.001, 0.02), rng.uniform(0.02, 0.2), 1.0]))
+            # the first projection's low delay is d_min (plasticity needs grouping 1)
+            lo = int(rng.integers(d_min, d_max + 1)) if projs else d_min
+            projs.append(Projection(pop, start, count, ps, pc, p, weight=w, scale=scale,
+                                    delay=(lo, int(rng.integers(lo, d_max + 1))),
+                                    plastic=plastic and pop == N.SPK_POP_INPUTS))
+    if not projs:
+        projs.append(Projection(N.SPK_POP_NEURONS, 0, n_exc, 0, n, 0.05, weight=(0.0, 1.0), scale=5e-4,
+                                delay=(d_min, d_max)))
+    rates = rng.uniform(5, 60, n_in).astype(np.float32) if n_in else None
+    stdp = (EVANS_STDP if rule == N.SPK_STDP_EVANS else STDP) if plastic else None
+    gen = GenNetwork(groups=groups, projections=projs, n_inputs=n_in, rates=rates, stdp=stdp,
+                     i_bg=float(rng.uniform(0.019, 0.03)), seed=seed + 1, connectivity_seed=seed + 2,
+                     record_inputs=bool(rng.integers(0, 2)), stdp_rule=rule)
+    sched = [None, schedule(4, 32, 0, 0), schedule(8, 64, 0, 0), schedule(1, 512, 0, 0)][int(rng.integers(0, 4))]
+    arrays = generate_synapses(gen.desc)
+    S = len(arrays["pre"])
+    g = Net.generate(gen, sched)
+    assert g.synapse_count() == S
+    np.testing.assert_array_equal(g.weights(S).view(np.uint32), delivered(arrays, plastic).view(np.uint32))
+    ref = desc_from_gen(gen, arrays)  # owns the arrays its descriptor points into
+    o = OracleNet(ref.desc)
+    G = o.timestep_grouping()
+    assert g.timestep_grouping() == G
+    for on, k in ((True, 150), (False, 60), (True, 120)):
+        g.run_steps(G * k, on)
+        o.run_steps(G * k, on)
+    assert g.synchronize() == 0
+    assert_same(g, o, n, n_in, 1, tag=f"seed {seed} n {n} n_in {n_in} G {G} {sched}")
+    # a generated network reads back the value each synapse delivers: the
+    # plastic weights as the oracle holds them, w * scale for static synapses
+    pl = arrays["plastic"].astype(bool) & plastic
+    w = g.weights(S)
+    np.testing.assert_array_equal(w[pl].view(np.uint32), o.weights()[pl].view(np.uint32))
+    np.testing.assert_array_equal(w[~pl].view(np.uint32), delivered(arrays, plastic)[~pl].view(np.uint32))
