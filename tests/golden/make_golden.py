@@ -13,7 +13,9 @@ cases defined in oracle/ref_dump.cpp and stores what it produced:
 * the weight and connectivity files the reference's save functions write for
   each case (Spike/Synapses/Synapses.cpp:423-614, SpikingSynapses.cpp:136-189;
   ref_dump's save mode), and the weights read back from the text file and
-  written again: size and SHA-256 of every file, as ref_checkpoint.json.
+  written again: size and SHA-256 of every file, as ref_checkpoint.json; for
+  the seeded random networks rand1..rand30 of oracle/ref_cases.inc, the file
+  names and one SHA-256 over all files, as ref_checkpoint_random.json.
 
 Usage (in a checkout where the reference sources are present):
     python tests/golden/make_golden.py
@@ -128,7 +130,35 @@ def main() -> int:
     with open(os.path.join(HERE, "ref_checkpoint.json"), "w") as f:
         json.dump(ck, f, indent=1, sort_keys=True)
     print("checkpoint files", {k: len(v) for k, v in ck.items()})
+    # seeded random networks (oracle/ref_cases.inc, case rand<seed>): the file
+    # names and one SHA-256 over every file's name and bytes
+    rnd = {}
+    for seed in RANDOM_SEEDS:
+        files = checkpoint_digests(ref_dump, f"rand{seed}")
+        rnd[str(seed)] = {"files": sorted(files), "sha256": combined_digest(ref_dump, f"rand{seed}")}
+    with open(os.path.join(HERE, "ref_checkpoint_random.json"), "w") as f:
+        json.dump(rnd, f, indent=1, sort_keys=True)
+    print("random checkpoint cases", len(rnd))
     return 0
+
+
+RANDOM_SEEDS = range(1, 31)
+
+
+def files_digest(dirname: str) -> str:
+    """SHA-256 over every file of a directory, by name: name, size, bytes."""
+    h = hashlib.sha256()
+    for name in sorted(os.listdir(dirname)):
+        with open(os.path.join(dirname, name), "rb") as f:
+            data = f.read()
+        h.update(name.encode() + b"\0" + str(len(data)).encode() + b"\0" + data)
+    return h.hexdigest()
+
+
+def combined_digest(ref_dump: str, case: str) -> str:
+    with tempfile.TemporaryDirectory() as td:
+        subprocess.run([ref_dump, "save", case, td], check=True, capture_output=True)
+        return files_digest(td)
 
 
 if __name__ == "__main__":

@@ -61,3 +61,54 @@ def test_saved_files_match_the_reference(program, tmp_path, case):
         assert (n, digest) == (g["bytes"], g["sha256"]), f"{case}: {name} differs from the reference's file"
     # the binary weights read back and written again are the same bytes
     assert rebin[2] == ours["w_SynapticWeights.bin"][2]
+
+
+RANDOM_GOLD = os.path.join(ROOT, "tests", "golden", "ref_checkpoint_random.json")
+REF_DUMP = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
+
+
+def _files_digest(dirname):
+    """SHA-256 over every file of a directory, by name: name, size, bytes
+    (the digest tests/golden/make_golden.py records)."""
+    h = hashlib.sha256()
+    for name in sorted(os.listdir(dirname)):
+        with open(os.path.join(dirname, name), "rb") as f:
+            data = f.read()
+        h.update(name.encode() + b"\0" + str(len(data)).encode() + b"\0" + data)
+    return h.hexdigest()
+
+
+with open(RANDOM_GOLD) as _f:
+    _RANDOM = json.load(_f)
+
+
+@pytest.mark.parametrize("seed", sorted(_RANDOM, key=int))
+def test_random_models_save_the_reference_files(program, tmp_path, seed):
+    """Seeded random networks (oracle/ref_cases.inc, case rand<seed>: every
+    connectivity type, shapes, weight ranges, scales, fractional delay ranges
+    and pairwise weights and delays, over voltage, current and conductance
+    synapses) saved through this library's front end: every file equals the
+    one the reference front end wrote for the same source."""
+    subprocess.run([program, f"rand{seed}", str(tmp_path)], check=True, capture_output=True, text=True, timeout=300)
+    os.remove(os.path.join(tmp_path, "rebin_SynapticWeights.bin"))
+    assert sorted(os.listdir(tmp_path)) == _RANDOM[seed]["files"]
+    assert _files_digest(tmp_path) == _RANDOM[seed]["sha256"], f"rand{seed}: files differ from the reference's"
+
+
+@pytest.mark.parametrize("seed", range(100, 140))
+def test_random_models_against_the_reference_front_end(program, tmp_path, seed):
+    """More seeds, against the reference front end itself where its build
+    (oracle/build_ref.sh) exists: both front ends save the same network and
+    every file must be the same bytes."""
+    from spike_gb300 import _build
+    ref_dump = _build.build_reference_frontend() if os.path.exists(REF_DUMP) else None
+    if not ref_dump:
+        pytest.skip("the reference front end is not built here")
+    ours, theirs = tmp_path / "ours", tmp_path / "ref"
+    ours.mkdir()
+    theirs.mkdir()
+    subprocess.run([ref_dump, "save", f"rand{seed}", str(theirs)], check=True, capture_output=True, timeout=300)
+    subprocess.run([program, f"rand{seed}", str(ours)], check=True, capture_output=True, timeout=300)
+    for name in sorted(os.listdir(theirs)):
+        with open(theirs / name, "rb") as a, open(ours / name, "rb") as b:
+            assert a.read() == b.read(), f"rand{seed}: {name} differs from the reference's file"
