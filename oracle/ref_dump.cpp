@@ -73,6 +73,8 @@ void dump_model(SpikingModel* m, SpikingSynapses* syn, SpikingNeurons* neurons,
     put_f("vhat", cond->reversal_potentials_Vhat.data(), cond->reversal_potentials_Vhat.size());
     put_f("tau_g", cond->decay_terms_tau_g.data(), cond->decay_terms_tau_g.size());
   }
+  auto* cur = dynamic_cast<CurrentSpikingSynapses*>(syn);
+  if (cur) put_f("tau_syn", cur->decay_terms_tau.data(), cur->decay_terms_tau.size());
   if (rule) put_i("plastic_sorted", rule->plastic_synapses.data(), rule->plastic_synapses.size());
 }
 

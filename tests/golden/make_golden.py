@@ -15,7 +15,8 @@ cases defined in oracle/ref_dump.cpp and stores what it produced:
   ref_dump's save mode), and the weights read back from the text file and
   written again: size and SHA-256 of every file, as ref_checkpoint.json; for
   the seeded random networks rand1..rand30 of oracle/ref_cases.inc, the file
-  names and one SHA-256 over all files, as ref_checkpoint_random.json.
+  names, one SHA-256 over all files and one over the synapse arrays in
+  creation order with the label constants, as ref_checkpoint_random.json.
 
 Usage (in a checkout where the reference sources are present):
     python tests/golden/make_golden.py
@@ -135,7 +136,9 @@ def main() -> int:
     rnd = {}
     for seed in RANDOM_SEEDS:
         files = checkpoint_digests(ref_dump, f"rand{seed}")
-        rnd[str(seed)] = {"files": sorted(files), "sha256": combined_digest(ref_dump, f"rand{seed}")}
+        d = run_case(ref_dump, f"rand{seed}")
+        rnd[str(seed)] = {"files": sorted(files), "sha256": combined_digest(ref_dump, f"rand{seed}"),
+                          "arrays_sha256": arrays_digest(creation_order(d), d)}
     with open(os.path.join(HERE, "ref_checkpoint_random.json"), "w") as f:
         json.dump(rnd, f, indent=1, sort_keys=True)
     print("random checkpoint cases", len(rnd))
@@ -152,6 +155,20 @@ def files_digest(dirname: str) -> str:
         with open(os.path.join(dirname, name), "rb") as f:
             data = f.read()
         h.update(name.encode() + b"\0" + str(len(data)).encode() + b"\0" + data)
+    return h.hexdigest()
+
+
+def arrays_digest(created: dict, d: dict) -> str:
+    """SHA-256 over a network's synapse arrays in creation order (pre, post,
+    weight, scale, delay, label), its label count and delay bounds, and the
+    labels' constants (reversal potentials and conductance or current decay
+    times) when the synapses have them."""
+    h = hashlib.sha256()
+    for k in ("pre", "post", "weight", "scale", "delay", "label"):
+        h.update(k.encode() + np.ascontiguousarray(created[k]).tobytes())
+    for k in ("num_syn_labels", "min_delay", "max_delay", "vhat", "tau_g", "tau_syn"):
+        if k in d:
+            h.update(k.encode() + np.ascontiguousarray(d[k]).tobytes())
     return h.hexdigest()
 
 

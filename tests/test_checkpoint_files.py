@@ -17,6 +17,7 @@ import json
 import os
 import shutil
 import subprocess
+import sys
 
 import pytest
 
@@ -63,6 +64,9 @@ def test_saved_files_match_the_reference(program, tmp_path, case):
     assert rebin[2] == ours["w_SynapticWeights.bin"][2]
 
 
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+import make_golden  # noqa: E402  (the fixtures' record reader and digests)
+
 RANDOM_GOLD = os.path.join(ROOT, "tests", "golden", "ref_checkpoint_random.json")
 REF_DUMP = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
 
@@ -93,6 +97,12 @@ def test_random_models_save_the_reference_files(program, tmp_path, seed):
     os.remove(os.path.join(tmp_path, "rebin_SynapticWeights.bin"))
     assert sorted(os.listdir(tmp_path)) == _RANDOM[seed]["files"]
     assert _files_digest(tmp_path) == _RANDOM[seed]["sha256"], f"rand{seed}: files differ from the reference's"
+    # the synapse arrays in creation order (labels and scales included) and the label constants
+    out = str(tmp_path / "arrays.bin")
+    subprocess.run([program, "dump", f"rand{seed}", out], check=True, capture_output=True, timeout=300)
+    d = make_golden.read_dump(out)
+    created = {k: d["created_" + k] for k in ("pre", "post", "weight", "scale", "delay", "label")}
+    assert make_golden.arrays_digest(created, d) == _RANDOM[seed]["arrays_sha256"], f"rand{seed}: arrays differ"
 
 
 @pytest.mark.parametrize("seed", range(100, 140))
@@ -112,3 +122,12 @@ def test_random_models_against_the_reference_front_end(program, tmp_path, seed):
     for name in sorted(os.listdir(theirs)):
         with open(theirs / name, "rb") as a, open(ours / name, "rb") as b:
             assert a.read() == b.read(), f"rand{seed}: {name} differs from the reference's file"
+    subprocess.run([ref_dump, f"rand{seed}", str(tmp_path / "ref.bin")], check=True, capture_output=True, timeout=300)
+    subprocess.run([program, "dump", f"rand{seed}", str(tmp_path / "ours.bin")], check=True, capture_output=True,
+                   timeout=300)
+    r, o = make_golden.read_dump(str(tmp_path / "ref.bin")), make_golden.read_dump(str(tmp_path / "ours.bin"))
+    c = make_golden.creation_order(r)
+    for k in ("pre", "post", "weight", "scale", "delay", "label"):
+        assert c[k].tobytes() == o["created_" + k].tobytes(), f"rand{seed}: {k}"
+    for k in ("num_syn_labels", "min_delay", "max_delay", "vhat", "tau_g", "tau_syn"):
+        assert (k in r) == (k in o) and (k not in r or r[k].tobytes() == o[k].tobytes()), f"rand{seed}: {k}"
