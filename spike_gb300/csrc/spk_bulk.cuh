@@ -855,8 +855,10 @@ __global__ void __launch_bounds__(BULK_PROP_WARPS * 32, SPK_BULK_PROP_MINB)
         const unsigned peers = __match_any_sync(FULL, key);
         const bool leader = add && (__ffs(peers) - 1) == lane;
         float acc = 0.0f;
-        if (leader) acc = inwin ? win_s[cell] : ring[cell];
-        unsigned rest = leader ? peers : 0u;
+        // the leader is its group's lowest lane: its own contribution comes
+        // first, then its peers' in lane order
+        if (leader) acc = (inwin ? win_s[cell] : ring[cell]) + contrib;
+        unsigned rest = leader ? peers & (peers - 1u) : 0u;
         while (__any_sync(FULL, rest != 0u)) {
           const int src = rest ? __ffs(rest) - 1 : lane;
           const float cv = __shfl_sync(FULL, contrib, src);
