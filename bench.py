@@ -14,8 +14,10 @@ Other workloads: brunel (Examples/Brunel10K.cpp at 10,000 + 2,500 LIF with
 10,000 Poisson inputs, in-degree 0.1, delays U{1..20}, 28.1 M synapses),
 vogels_abbott (Examples/VogelsAbbottNet.cpp, 4,000 conductance LIF),
 plastic_ff (50,000 log-normal Poisson inputs onto 200,000 LIF, 1,000
-afferents each, STDP).  Data are synthetic, built by the reference's
-construction rules or drawn on the GPU.
+afferents each, STDP; --construction exact builds the fixed in-degree of 900
+input + 100 recurrent afferents with the host front end, generated draws a
+binomial in-degree of the same mean on the GPU).  Data are synthetic, built
+by the reference's construction rules or drawn on the GPU.
 
 A bench "step" is one block of --block timesteps (default 1000 = 0.1 s of
 simulated time); the default step count covers the workload's simulated time
@@ -65,6 +67,11 @@ def parse():
     p.add_argument("--scale", type=float, default=1.0, help="plastic_ff: network size factor (profiling cases)")
     p.add_argument("--rule", default="weight_dependent", choices=["weight_dependent", "evans"],
                    help="plastic_ff: STDP rule of the input synapses")
+    p.add_argument("--construction", default=None, choices=["exact", "generated"],
+                   help="plastic_ff: exact = fixed in-degree (900 input + 100 recurrent afferents per neuron, "
+                        "the host front end's connect_with_sparsity); generated = Bernoulli pairs drawn on the GPU "
+                        "(binomial in-degree of the same mean; the Evans rule needs it).  Default: exact for the "
+                        "weight-dependent rule, generated for the Evans rule")
     p.add_argument("--norm", default="off", choices=["off", "after", "before"],
                    help="brunel: weight-dependent STDP on the E->E synapses with the weight normalisation "
                         "added after or before it")
@@ -86,6 +93,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     a = p.parse_args()
+    if a.construction is None:
+        a.construction = "exact" if a.rule == "weight_dependent" else "generated"
     if a.steps is None:
         sim_s = {"batched": 1.0, "brunel": 2.0, "vogels_abbott": 1.0, "plastic_ff": 5.0, "served": 0.1}[a.workload]
         a.steps = max(1, int(round(sim_s / (a.block * DT))))
@@ -98,7 +107,8 @@ RULES = {"weight_dependent": 0, "evans": 1}
 NORMS = {"off": 0, "after": 1, "before": 2}
 
 
-def build_model(workload: str, scale: float = 1.0, rule: str = "weight_dependent", norm: str = "off"):
+def build_model(workload: str, scale: float = 1.0, rule: str = "weight_dependent", norm: str = "off",
+                construction: str = "generated"):
     from spike_gb300 import networks
     if workload == "brunel":
         m = networks.brunel(norm=NORMS[norm])
@@ -114,12 +124,20 @@ def build_model(workload: str, scale: float = 1.0, rule: str = "weight_dependent
         L = 2
     else:
         n_in, n_neu = int(round(50000 * scale)), int(round(200000 * scale))
-        m = networks.plastic_ff_generated(n_in=n_in, n_neurons=n_neu, rule=RULES[rule])
         tag = "stdp" if rule == "weight_dependent" else f"{rule}_stdp"
         cfg = {"workload": f"plastic_ff_{n_neu}_lif_{n_in}_lognormal_poisson_{tag}", "neurons": n_neu,
-               "inputs": n_in, "in_degree": "binomial, mean 900 input + 100 recurrent", "delays_steps": [1, 10],
-               "dt_ms": 0.1, "sim_s_per_config": 5.0, "plasticity": True, "stdp_rule": rule,
-               "connectivity": "drawn on the GPU"}
+               "inputs": n_in, "delays_steps": [1, 10], "dt_ms": 0.1, "sim_s_per_config": 5.0,
+               "plasticity": True, "stdp_rule": rule}
+        if construction == "exact":
+            if rule != "weight_dependent":
+                raise SystemExit("plastic_ff: --construction exact builds the weight-dependent rule only")
+            m = networks.plastic_ff(n_in=n_in, n_neurons=n_neu)
+            cfg.update({"in_degree": "fixed per neuron, multapses allowed: int(sparseness x n_pre) in float as the "
+                                     "reference computes it, 900 input + 99 recurrent at full size",
+                        "connectivity": "host front end, connect_with_sparsity (Examples/UtilityFunctions.hpp:51-82)"})
+        else:
+            m = networks.plastic_ff_generated(n_in=n_in, n_neurons=n_neu, rule=RULES[rule])
+            cfg.update({"in_degree": "binomial, mean 900 input + 100 recurrent", "connectivity": "drawn on the GPU"})
         L = 1
     return m, cfg, L
 
@@ -230,6 +248,12 @@ def networks_small_plastic_ff(rule: str = "weight_dependent"):
     return networks.plastic_ff_generated(n_in=2500, n_neurons=10000, ff=900, rec=100, rule=RULES[rule])
 
 
+def networks_small_plastic_ff_exact():
+    """The exact (fixed in-degree) construction at 1/20 size, for the CPU samples."""
+    from spike_gb300 import networks
+    return networks.plastic_ff(n_in=2500, n_neurons=10000, ff=900, rec=100)
+
+
 # Per plastic synapse and timestep, the weight normalisation reads the record
 # (8 B) and the initial weight (4 B) and writes the weight back (8 B record).
 NORM_BYTES = 20
@@ -253,14 +277,20 @@ def run_reference(args, rank, world):
     """CPU reference arm: the oracle port with all host threads."""
     if rank != 0:
         return
-    m, cfg, L = build_model(args.workload, args.scale, args.rule, args.norm)
+    m, cfg, L = build_model(args.workload, args.scale, args.rule, args.norm, args.construction)
     threads = os.cpu_count() or 1
     from oracle import OracleNet
     from spike_gb300 import GenNetwork
+    small = None
     if isinstance(m, GenNetwork):
         # too large to draw on the host: the same construction at 1/20 size
         dd = oracle_instance(networks_small_plastic_ff(args.rule))[1]
         desc = dd.desc
+        cfg = {**cfg, "cpu_sample_network": "same construction at 1/20 size (2,500 inputs, 10,000 neurons)"}
+    elif args.workload == "plastic_ff":
+        # 2e8 synapses: the same construction at 1/20 size keeps the sample bounded
+        small = networks_small_plastic_ff_exact()
+        desc = small.desc()
         cfg = {**cfg, "cpu_sample_network": "same construction at 1/20 size (2,500 inputs, 10,000 neurons)"}
     else:
         desc = m.desc()
@@ -312,7 +342,7 @@ def main():
     from spike_gb300 import schedule
 
     from spike_gb300 import GenNetwork, Net
-    m, cfg, L = build_model(args.workload, args.scale, args.rule, args.norm)
+    m, cfg, L = build_model(args.workload, args.scale, args.rule, args.norm, args.construction)
     sched = schedule(args.warps, args.tile, args.ctas, args.launch_steps or args.block)
     if isinstance(m, GenNetwork):
         net = Net.generate(m, sched)
@@ -384,7 +414,8 @@ def main():
         rates = torch.full((max(n_inputs, 1),), 20.0, dtype=torch.float32).pin_memory()
         if n_inputs and args.workload == "plastic_ff":
             import numpy as np
-            rates.copy_(torch.from_numpy(np.ctypeslib.as_array(m.desc.input_rates, (n_inputs,)).copy()))
+            src = m.desc if isinstance(m, GenNetwork) else desc  # the stimulus the network was built with
+            rates.copy_(torch.from_numpy(np.ctypeslib.as_array(src.input_rates, (n_inputs,)).copy()))
         h2d = 4 * n_inputs
         d2h = 0
         net.clear_spikes()
@@ -410,6 +441,13 @@ def main():
             # 1/20-size network of the same construction stands in
             cs = CpuSample([networks_small_plastic_ff(args.rule)])
             cv, cel = cs.run(args.cpu_sample_steps // 10, 1)
+            cpu = {"value": cv, "unit": "events/s", "cores": 1, "kind": "port",
+                   "sample": f"the same construction at 1/20 size (2,500 inputs, 10,000 neurons), "
+                             f"{args.cpu_sample_steps // 10} timesteps from reset, {cel:.1f} s of CPU"}
+        elif args.workload == "plastic_ff":
+            # 2e8 synapses on one core: the exact construction at 1/20 size stands in
+            small = networks_small_plastic_ff_exact()
+            cv, cel = cpu_baseline(small.desc(), args.cpu_sample_steps // 10, 1)
             cpu = {"value": cv, "unit": "events/s", "cores": 1, "kind": "port",
                    "sample": f"the same construction at 1/20 size (2,500 inputs, 10,000 neurons), "
                              f"{args.cpu_sample_steps // 10} timesteps from reset, {cel:.1f} s of CPU"}
