@@ -108,7 +108,9 @@ NORMS = {"off": 0, "after": 1, "before": 2}
 
 
 def build_model(workload: str, scale: float = 1.0, rule: str = "weight_dependent", norm: str = "off",
-                construction: str = "generated"):
+                construction: str = "generated", describe_only: bool = False):
+    """The workload's network and its description.  With describe_only the
+    exact configuration-3 network (2e8 synapses on the host) is not built."""
     from spike_gb300 import networks
     if workload == "brunel":
         m = networks.brunel(norm=NORMS[norm])
@@ -131,7 +133,7 @@ def build_model(workload: str, scale: float = 1.0, rule: str = "weight_dependent
         if construction == "exact":
             if rule != "weight_dependent":
                 raise SystemExit("plastic_ff: --construction exact builds the weight-dependent rule only")
-            m = networks.plastic_ff(n_in=n_in, n_neurons=n_neu)
+            m = None if describe_only else networks.plastic_ff(n_in=n_in, n_neurons=n_neu)
             cfg.update({"in_degree": "fixed per neuron, multapses allowed: int(sparseness x n_pre) in float as the "
                                      "reference computes it, 900 input + 99 recurrent at full size",
                         "connectivity": "host front end, connect_with_sparsity (Examples/UtilityFunctions.hpp:51-82)"})
@@ -277,7 +279,8 @@ def run_reference(args, rank, world):
     """CPU reference arm: the oracle port with all host threads."""
     if rank != 0:
         return
-    m, cfg, L = build_model(args.workload, args.scale, args.rule, args.norm, args.construction)
+    m, cfg, L = build_model(args.workload, args.scale, args.rule, args.norm, args.construction,
+                            describe_only=True)
     threads = os.cpu_count() or 1
     from oracle import OracleNet
     from spike_gb300 import GenNetwork
