@@ -373,6 +373,10 @@ int spk_net_synapse_count(const spk_net* net, int64_t* n);
 int spk_net_plastic_synapse_count(const spk_net* net, int64_t* n);
 
 /* ---- batch: many independent networks in one persistent launch ---------- */
+/* The networks stay usable on their own between batch runs: a network may be
+ * run alone, reset, snapshotted or restored, switch stimulus or change its
+ * wait limit, and the next batch run starts from that state (the batch brings
+ * its copies of the networks' descriptors up to date before it launches). */
 int spk_batch_create(spk_net* const* nets, int32_t n_nets, const spk_schedule* schedule,
                      spk_batch** out);
 int spk_batch_run_steps(spk_batch* batch, int64_t n_steps, int32_t plasticity_on);
