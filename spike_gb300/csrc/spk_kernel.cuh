@@ -782,6 +782,12 @@ __global__ void __launch_bounds__(512, 1)
       round_barrier(nthreads);
       process_round(list_n);
     } else if (w == 0) {
+      // Without plasticity only the key words are read from the other CTAs,
+      // each carrying its step (a stale word is polled again).  They are read
+      // through L1, whose lines of this buffer may be two steps old: the fence
+      // drops them, here, while the other CTAs publish, rather than after the
+      // last stamp arrives.
+      if (!stdp_run) fence_acq_rel_gpu();
       const int C = d.nctas;
       const unsigned long long* stp = d.cta_stamp + (size_t)par * C;
       constexpr int SPL = MAX_CTAS_PER_NET / 32;
@@ -817,7 +823,10 @@ __global__ void __launch_bounds__(512, 1)
       }
       int total = 0;
       if (ok) {
-        fence_acq_rel_gpu();  // keys, traces and bitmaps published before the stamps
+        // With plasticity the traces and bitmaps published before the stamps
+        // are read next: acquire them (the fence also drops stale L1 lines of
+        // the key words, read next through L1).
+        if (stdp_run) fence_acq_rel_gpu();
 #pragma unroll
         for (int u = 0; u < SPL; ++u) {
           const int r = u * 32 + lane;
