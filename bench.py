@@ -488,6 +488,9 @@ def main():
             "status": status,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "traffic_source": (f"profiles/step_kernel_*.json: DRAM bytes per algorithmic byte of "
+                                            f"one ncu capture ({tr.get('capture', '')}), times this run's "
+                                            f"algorithmic bytes" if tr else None),
                          "kernel": ("bulk kernels of one timestep (neurons, list, per-synapse-trace rule, "
                                     "propagation)" if trace_rule else
                                     "bulk kernels of one timestep (neurons, list, propagation passes, afferent "
